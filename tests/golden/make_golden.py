@@ -1,0 +1,179 @@
+"""Generate the golden fixtures of the nonlocal-density path from the reference.
+
+Each case is one of the reference's own example decks (Examples/*/dft_input.dat),
+optionally edited line by line.  For every case the reference's own C code
+(built into oracle/_ref by oracle/refbuild) is run in a child process:
+
+* set-up (stencils, bulk thermodynamics, mesh, external field, hard-wall lists),
+* its built-in Newton solver to convergence,
+* fill_resid_and_matrix_control at the converged state and at a seeded
+  perturbation of it, recording the residual and the assembled Jacobian.
+
+The fixture keeps the problem description (the reference's stencil tables,
+constants, V_ext, zero-density flags, hard-wall masks), the two states, their
+residuals, and Jacobian products J v, J^T w and the Schur-complement product
+S v2 (S = A22 - A21 A11^-1 A12, block split of src/dft_linsolver_setup.c:182-241)
+for seeded random vectors.  Run from the repository root:
+
+    python tests/golden/make_golden.py [case ...]
+
+The reference tree must be present (it is read in place, never copied).
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import scipy.sparse as sp
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import tref  # noqa: E402
+
+# reference physics ids (src/dft_globals_const.h)
+DENSITY, HSRHOBAR, MF_EQ = 0, 1, 8
+
+
+def deck(example, edits=None, surfaces=None):
+    lines = tref.read_deck(os.path.join(tref.example_dir(example), "dft_input.dat"))
+    if edits:
+        lines = tref.edit_deck(lines, edits)
+    return lines, surfaces or tref.example_dir(example)
+
+
+def write_surfaces(path, text):
+    os.makedirs(path, exist_ok=True)
+    with open(os.path.join(path, "dft_surfaces.dat"), "w") as f:
+        f.write(text)
+    return path
+
+
+SCHUR_LINSOLVE = "1 0 50"       # L_Schur Solver Az_kspace
+MF_UNKNOWNS = "0 50 0 0 0"      # NL_Solver Max_NL_iter Physics_scaling ATTInA22Block Analyt_WJDC_Jac
+
+
+def cases():
+    tmp = os.path.join(ROOT, "_work", "golden_surfaces")
+    c = {}
+    # 1-D FMT1 hard sphere against a hard wall (the reference's HS5 example as is)
+    c["hs1d_wall"] = deck("HS5_FMT1_1D")
+    # 1-D FMT1, hard wall on the left, reflecting boundary on the right (HS3 as is)
+    c["hs1d_reflect"] = deck("HS3_FMT1_1D")
+    # 1-D FMT1 + WCA attraction near a LJ 9-3 wall, mean field as its own unknown
+    c["lj1d_mf"] = deck("LJ1_FMT1_WCA_1D", {
+        "ATTInA22Block": MF_UNKNOWNS, "L_Schur": SCHUR_LINSOLVE})
+    # 1-D binary White-Bear (FMT3) mixture with sizes 1 and 0.6 and WCA attraction
+    c["mix1d_fmt3"] = deck("MIX2_FMT1_WCA_1D", {
+        "Type_func (": "2 0", "Ncomp Mix_type": "2 1", "HS_diam[i]": "1. 0.6",
+        "Sigma_ff[i][j]": "1. 0.8 0.8 0.6", "Eps_ff[i][j]": "1. 0.9 0.9 0.8",
+        "Cut_ff[i][j]": "2.5 2.5 2.5 2.5", "Rho_b_0[icomp]": "0.25 0.35",
+        "Esize_x(idim)": "0.05", "ATTInA22Block": MF_UNKNOWNS, "L_Schur": SCHUR_LINSOLVE})
+    # 3-D FMT1 + WCA, LJ 9-3 planar wall at x=0, bulk at the far x end, periodic y and z
+    surf3d = write_surfaces(os.path.join(tmp, "fmt1_wca_3d"), " 0 0 -1.5 0.0 0.0  0.0\n")
+    c["fmt1_wca_3d"] = deck("GEOM3_PLANE_ROUGH_3D", {
+        "Size_x(idim)": "3.0 5.5 5.5", "Esize_x(idim)": "0.25 0.25 0.25",
+        "Type_bc(x0": "-1 0", "Type_bc(x1": "1 1", "Type_bc(x2": "1 1",
+        "Nwall_types Nwall Nlink": "1 1 1 0 0", "Xtest_reflect_TF": "0 0 0",
+        "Lrough_surf": "0", "Lapply_offest": "0 0 0", "Cut_ff[i][j]": "2.5", "Rho_b_0[icomp]": "0.6",
+        "ATTInA22Block": "0 20 0 0 0", "L_Schur": "1 0 100"}, surfaces=surf3d)
+    return c
+
+
+def block_lists(ints, nunk):
+    """ind / dep / density unknown lists as linsolver_setup_HSTYPE makes them."""
+    ndim, nrb, lhard, nlists = int(ints[0]), int(ints[9]), int(ints[13]), int(ints[14])
+    first_rho, first_rb = int(ints[22]), int(ints[23])
+    ncomp = int(ints[8])
+    one = (lhard and nlists == 2) or (not lhard and nlists == 1)
+    ind, dep, dens = [], [], []
+    nrb_tot = nrb + 2 * ndim
+    for u in range(nunk):
+        if first_rho <= u < first_rho + ncomp:
+            dens.append(u)
+        elif first_rb <= u < first_rb + nrb_tot:
+            k = u - first_rb
+            if one and ((1 < k < nrb) or k >= nrb + ndim):
+                dep.append(u)
+            else:
+                ind.append(u)
+        else:
+            ind.append(u)
+    return ind, dep, dens
+
+
+def probe(n, k):
+    """Deterministic probe vector k of length n (no RNG, so any machine rebuilds it)."""
+    i = np.arange(n, dtype=np.float64)
+    return np.sin(1.3 + 0.7071 * k + 0.61803 * (k + 1) * i)
+
+
+def make_case(name, lines, surfaces, states=("x_newton", ("x_newton", 7, 0.02))):
+    r = tref.extract(lines, surfaces, newton=True, fill_states=list(states))
+    ints = r["info_ints"]
+    nunk, nbox = int(ints[7]), int(ints[5])
+    assert int(ints[6]) == nbox and np.array_equal(r["l2b"], np.arange(nbox)) and np.array_equal(r["b2g"], np.arange(nbox)), \
+        "single-process box must equal the global mesh"
+    out = {"info_ints": ints, "info_doubles": r["info_doubles"], "vext": r["vext"],
+           "zero_density": r["zero_density"].astype(np.int8), "newton_iters": np.int32(r["newton_iters"])}
+    if "boundary_nodes" in r:
+        out["boundary_nodes"] = r["boundary_nodes"]
+        out["fluid_masks"] = r["fluid_masks"].astype(np.int16)
+    for (isten, idx), (off, w, hw) in r["stencils"].items():
+        out[f"sten_{isten}_{idx}_off"] = off.astype(np.int16)
+        out[f"sten_{isten}_{idx}_w"] = w
+        if hw is not None:
+            out[f"sten_{isten}_{idx}_hw"] = hw
+    ind, dep, dens = block_lists(ints, nunk)
+    out["blk_ind"], out["blk_dep"], out["blk_dens"] = (np.array(v, np.int32) for v in (ind, dep, dens))
+    N = nunk * nbox
+    out["x_newton"] = r["x_newton"]
+    out["states"] = np.array([0 if isinstance(st, str) else 1 for st in states], np.int8)
+    for k, f in enumerate(r["fills"]):
+        ng = f["nglobal"]
+        assert ng == nbox
+        J = sp.csr_matrix((f["vals"], (f["rows"], f["cols"])), shape=(N, N))
+        out[f"x{k}"] = f["x"]
+        out[f"resid_sum{k}"] = np.float64(f["resid_sum"])
+        out[f"R{k}"] = -f["rhs"]  # rhs = -residual
+        v = probe(N, 0)
+        out[f"Jv{k}"] = (J @ v).reshape(nunk, nbox)
+        w = probe(N, 1)
+        out[f"JTw{k}"] = (J.T @ w).reshape(nunk, nbox)
+        # Schur product on the density block, block operators built from J
+        idx1 = np.concatenate([np.arange(u * nbox, (u + 1) * nbox) for u in ind + dep])
+        idx2 = np.concatenate([np.arange(u * nbox, (u + 1) * nbox) for u in dens])
+        depmask = np.concatenate([np.full(nbox, u in dep) for u in ind + dep])
+        A11 = J[idx1][:, idx1].tocsr()
+        B = A11.multiply(sp.csr_matrix(depmask[:, None].astype(float))).tocsr()
+        B.setdiag(0.0)
+        B.eliminate_zeros()
+        A12, A21, A22 = J[idx1][:, idx2], J[idx2][:, idx1], J[idx2][:, idx2]
+        v2 = probe(len(idx2), 2)
+        u1 = A12 @ v2
+        y1 = np.where(depmask, -u1 - B @ u1, -u1)
+        Sv = A22 @ v2 - A21 @ y1
+        out[f"schur_Sv{k}"] = Sv.reshape(len(dens), nbox)
+        out[f"nnz{k}"] = np.int64(J.nnz)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    return out
+
+
+def main(argv):
+    if not os.path.exists(tref.REF_LIB):
+        tref.build_ref()
+    allc = cases()
+    names = argv or list(allc)
+    for n in names:
+        lines, surf = allc[n]
+        # the 3-D case keeps only the perturbed state to stay small
+        states = (("x_newton", 7, 0.02),) if n.endswith("3d") else ("x_newton", ("x_newton", 7, 0.02))
+        o = make_case(n, lines, surf, states)
+        k = len(states) - 1
+        print(f"{n}: nodes={o['info_ints'][5]} unknowns={o['info_ints'][7]} newton_iters={o['newton_iters']} "
+              f"|R|={np.abs(o[f'R{k}']).max():.3e} nnz={o[f'nnz{k}']}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
