@@ -1,0 +1,80 @@
+/* CPU restatement of the reference's nonlocal-density path (test infrastructure).
+ *
+ * This is the oracle the GPU path is checked against.  It restates, in plain
+ * serial C with the reference's own loop order, the residual and Jacobian of
+ * Tramonto's hard-sphere FMT + WCA mean-field fill:
+ *   - calc_FMT_derivatives / FMT1_1stderiv / FMT3_1stderiv
+ *       (src/dft_fill_FMT.c:349-385, src/dft_physics_FMT1.c:59-77, src/dft_physics_FMT3.c:61-96)
+ *   - load_rho_bar_s / load_rho_bar_v / resid_and_Jac_sten_fill_sum_Ncomp
+ *       (src/dft_fill_FMT.c:195-347, src/dft_fill_CLSmf.c:38-171)
+ *   - load_nonlocal_hs_rosen_rb with d2phi_drb2_{delta,theta}_rb_FMT{1,3}
+ *       (src/dft_fill_FMT.c:41-189, src/dft_physics_FMT1.c:79-168, src/dft_physics_FMT3.c:101-265)
+ *   - load_euler_lagrange (src/dft_fill_EL.c:38-196, 351-444) and load_mean_field (src/dft_fill_mf.c:38-63)
+ *   - offset_to_node_box (src/dft_mesh_lib.c:203-297), HW_boundary_weight (src/dft_utils.c:41-62)
+ *   - the hard-sphere Schur operator S = A22 - A21 A11^-1 A12 (src/dft_Schur_Epetra_Operator.cpp:86-119,
+ *     src/dft_HardSphereA11_Epetra_Operator.cpp:130-197)
+ * It is pinned against golden vectors produced by the reference itself
+ * (tests/golden).  Only tests, the smoke check and the CPU baseline of
+ * bench.py use it; the product never links it.
+ *
+ * Conventions: one process, the box equals the mesh; fields are SoA
+ * [unknown][node] with node = ix + nx*(iy + ny*iz); unknown order as
+ * setup_nunk_per_node (src/dft_defs_unknowns.c:37-176): densities,
+ * weighted densities in solution-vector order (n3, n2, n1, n0, V2[d], V1[d]),
+ * then mean-field unknowns. */
+#ifndef TRAMONTO_ORACLE_H
+#define TRAMONTO_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAXC 4
+
+enum { ORC_DELTA = 0, ORC_THETA = 1, ORC_UATT = 2 };
+enum { ORC_BC_IN_WALL = -1, ORC_BC_IN_BULK = 0, ORC_BC_PERIODIC = 1, ORC_BC_REFLECT = 2 };
+enum { ORC_FMT1 = 0, ORC_FMT3 = 2 };
+
+typedef struct {
+  int ndim, nx[3];
+  double esize[3];
+  int bc[3][2];
+  int ncomp;
+  int functional;      /* ORC_FMT1 or ORC_FMT3 */
+  int attraction;      /* WCA mean field on/off */
+  int att_in_a22;      /* 0: mean field is its own unknown (MF_EQ rows); 1: summed into the EL rows */
+  int single_size;     /* n1, n0, V1 are dependent unknowns (one particle size) */
+  int hard_surf;       /* Lhard_surf: hard-wall boundary weights */
+  int nlists_hw;
+  int first_rho, first_rb, first_mf, nunk;
+  double rho_b[ORC_MAXC], betamu_hs_ex[ORC_MAXC], betamu_att[ORC_MAXC];
+  double inv_rad[ORC_MAXC], inv_4pir[ORC_MAXC], inv_4pirsq[ORC_MAXC], fac_overlap[ORC_MAXC];
+  double dphi_bulk[4];        /* Dphi_Drhobar_b: bulk dPhi/dn0..dn3 */
+  double vext_max;
+  const double *vext;         /* [ncomp][N] */
+  const signed char *zero_density; /* [ncomp][N] */
+  const int *boundary_nodes;  /* [nlists][N], -1 when not a hard-wall boundary node */
+  const short *fluid_masks;   /* [nlists][2^ndim][N], see tests/golden/make_golden.py */
+  int sten_len[3][ORC_MAXC * ORC_MAXC];
+  const short *sten_off[3][ORC_MAXC * ORC_MAXC];   /* [L][ndim] */
+  const double *sten_w[3][ORC_MAXC * ORC_MAXC];    /* [L] */
+  const double *sten_hw[3][ORC_MAXC * ORC_MAXC];   /* [L][2^ndim] or NULL */
+} orc_problem;
+
+long orc_nnodes(const orc_problem *p);
+/* dPhi/dn at every node, [4+2*ndim][N] in reference order S0,S1,S2,S3,V1[d],V2[d] */
+int orc_dphi(const orc_problem *p, const double *x, double *dphi);
+/* full residual R(x) for every unknown and node (the reference's rhs is -R) */
+int orc_resid(const orc_problem *p, const double *x, double *R);
+/* Jacobian products with the reference's Jacobian entries at state x */
+int orc_jv(const orc_problem *p, const double *x, const double *v, double *Jv);
+int orc_jtv(const orc_problem *p, const double *x, const double *w, double *JTw);
+/* Schur product S v2 on the density block ([ncomp][N] in and out) */
+int orc_schur(const orc_problem *p, const double *x, const double *v2, double *Sv2);
+/* Residual of the first `nrows` nodes only (bounded CPU samples); R is [nunk][N], other rows untouched */
+int orc_resid_rows(const orc_problem *p, const double *x, double *R, long node_begin, long node_end);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

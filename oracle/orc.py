@@ -1,0 +1,144 @@
+"""ctypes binding of the C restatement oracle (oracle.c); test infrastructure.
+
+``build()`` compiles oracle.c with the host C compiler into oracle/_build.
+``Oracle(problem)`` takes any object with the problem attributes used by the
+product (see tramonto_gb300.problem.Problem: geometry, constants, fields and
+stencil tables) and exposes the oracle's residual, Jacobian products and
+Schur product on numpy arrays shaped [unknown][node].
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+MAXC = 4
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.c")
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-o", tmp, src, "-lm"], check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+class _Problem(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int), ("nx", C.c_int * 3), ("esize", C.c_double * 3), ("bc", (C.c_int * 2) * 3),
+        ("ncomp", C.c_int), ("functional", C.c_int), ("attraction", C.c_int), ("att_in_a22", C.c_int),
+        ("single_size", C.c_int), ("hard_surf", C.c_int), ("nlists_hw", C.c_int),
+        ("first_rho", C.c_int), ("first_rb", C.c_int), ("first_mf", C.c_int), ("nunk", C.c_int),
+        ("rho_b", C.c_double * MAXC), ("betamu_hs_ex", C.c_double * MAXC), ("betamu_att", C.c_double * MAXC),
+        ("inv_rad", C.c_double * MAXC), ("inv_4pir", C.c_double * MAXC), ("inv_4pirsq", C.c_double * MAXC),
+        ("fac_overlap", C.c_double * MAXC), ("dphi_bulk", C.c_double * 4), ("vext_max", C.c_double),
+        ("vext", C.POINTER(C.c_double)), ("zero_density", C.POINTER(C.c_int8)),
+        ("boundary_nodes", C.POINTER(C.c_int)), ("fluid_masks", C.POINTER(C.c_int16)),
+        ("sten_len", (C.c_int * (MAXC * MAXC)) * 3),
+        ("sten_off", (C.POINTER(C.c_int16) * (MAXC * MAXC)) * 3),
+        ("sten_w", (C.POINTER(C.c_double) * (MAXC * MAXC)) * 3),
+        ("sten_hw", (C.POINTER(C.c_double) * (MAXC * MAXC)) * 3),
+    ]
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    def __init__(self, prob):
+        self.lib = C.CDLL(build())
+        for fn in ("orc_resid", "orc_jv", "orc_jtv", "orc_schur", "orc_dphi", "orc_resid_rows"):
+            getattr(self.lib, fn).restype = C.c_int
+        self.prob = prob
+        self._keep = []
+        s = _Problem()
+        s.ndim = prob.ndim
+        for d in range(3):
+            s.nx[d] = int(prob.nx[d]) if d < prob.ndim else 1
+            s.esize[d] = float(prob.esize[d]) if d < prob.ndim else 0.0
+            for k in range(2):
+                s.bc[d][k] = int(prob.bc[d][k]) if d < prob.ndim else 0
+        for name in ("ncomp", "functional", "attraction", "att_in_a22", "single_size", "hard_surf", "nlists_hw",
+                     "first_rho", "first_rb", "first_mf", "nunk"):
+            setattr(s, name, int(getattr(prob, name)))
+        for name in ("rho_b", "betamu_hs_ex", "betamu_att", "inv_rad", "inv_4pir", "inv_4pirsq", "fac_overlap"):
+            arr = getattr(s, name)
+            vals = np.asarray(getattr(prob, name), np.float64)
+            for i in range(min(len(vals), MAXC)):
+                arr[i] = vals[i]
+        for i in range(4):
+            s.dphi_bulk[i] = float(prob.dphi_bulk[i])
+        s.vext_max = float(prob.vext_max)
+        self.N = int(np.prod([prob.nx[d] for d in range(prob.ndim)]))
+        vext = np.ascontiguousarray(prob.vext, np.float64)
+        zd = np.ascontiguousarray(prob.zero_density, np.int8)
+        self._keep += [vext, zd]
+        s.vext = _dp(vext)
+        s.zero_density = zd.ctypes.data_as(C.POINTER(C.c_int8))
+        if prob.hard_surf:
+            bn = np.ascontiguousarray(prob.boundary_nodes, np.int32)
+            fm = np.ascontiguousarray(prob.fluid_masks, np.int16)
+            self._keep += [bn, fm]
+            s.boundary_nodes = bn.ctypes.data_as(C.POINTER(C.c_int))
+            s.fluid_masks = fm.ctypes.data_as(C.POINTER(C.c_int16))
+        for (stype, idx), (off, w, hw) in prob.stencils.items():
+            off = np.ascontiguousarray(off, np.int16)
+            w = np.ascontiguousarray(w, np.float64)
+            self._keep += [off, w]
+            s.sten_len[stype][idx] = len(w)
+            s.sten_off[stype][idx] = off.ctypes.data_as(C.POINTER(C.c_int16))
+            s.sten_w[stype][idx] = _dp(w)
+            if hw is not None:
+                hw = np.ascontiguousarray(hw, np.float64)
+                self._keep.append(hw)
+                s.sten_hw[stype][idx] = _dp(hw)
+        self.s = s
+
+    def _vec(self, x, rows=None):
+        x = np.ascontiguousarray(x, np.float64)
+        return x
+
+    def resid(self, x):
+        x = self._vec(x)
+        R = np.zeros((self.prob.nunk, self.N))
+        assert self.lib.orc_resid(C.byref(self.s), _dp(x), _dp(R)) == 0
+        return R
+
+    def resid_rows(self, x, begin, end):
+        x = self._vec(x)
+        R = np.zeros((self.prob.nunk, self.N))
+        assert self.lib.orc_resid_rows(C.byref(self.s), _dp(x), _dp(R), C.c_long(begin), C.c_long(end)) == 0
+        return R
+
+    def jv(self, x, v):
+        x, v = self._vec(x), self._vec(v)
+        out = np.zeros((self.prob.nunk, self.N))
+        assert self.lib.orc_jv(C.byref(self.s), _dp(x), _dp(v), _dp(out)) == 0
+        return out
+
+    def jtv(self, x, w):
+        x, w = self._vec(x), self._vec(w)
+        out = np.zeros((self.prob.nunk, self.N))
+        assert self.lib.orc_jtv(C.byref(self.s), _dp(x), _dp(w), _dp(out)) == 0
+        return out
+
+    def schur(self, x, v2):
+        x, v2 = self._vec(x), self._vec(v2)
+        out = np.zeros((self.prob.ncomp, self.N))
+        assert self.lib.orc_schur(C.byref(self.s), _dp(x), _dp(v2), _dp(out)) == 0
+        return out
+
+    def dphi(self, x):
+        x = self._vec(x)
+        out = np.zeros((4 + 2 * self.prob.ndim, self.N))
+        assert self.lib.orc_dphi(C.byref(self.s), _dp(x), _dp(out)) == 0
+        return out

@@ -1,0 +1,32 @@
+"""Shared helpers for the golden-fixture tests (test infrastructure)."""
+import os
+
+import numpy as np
+
+from tramonto_gb300.problem import from_golden
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+CASES = ["hs1d_wall", "hs1d_reflect", "lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d"]
+
+# The reference fills in IEEE FP64 with its own summation order; any other
+# order differs by rounding.  Residual entries are compared with an absolute
+# tolerance scaled by the size of the terms they sum (O(1..10) for log rho,
+# the chemical potential and the stencil sums), products by their max norm.
+RESID_ATOL = 1e-12
+PROD_RTOL = 1e-12
+
+
+def load(case):
+    z = np.load(os.path.join(GOLDEN, f"{case}.npz"))
+    return z, from_golden(z)
+
+
+def probe(n, k):
+    """Same deterministic probe vectors as tests/golden/make_golden.py."""
+    i = np.arange(n, dtype=np.float64)
+    return np.sin(1.3 + 0.7071 * k + 0.61803 * (k + 1) * i)
+
+
+def rel_err(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
