@@ -1,0 +1,317 @@
+"""Benchmark of the nonlocal-density Newton path on one GB300.
+
+Workload (BASELINE configuration 2): 3-D FMT1 + WCA Lennard-Jones fluid
+(eps=1, r_c=2.5 sigma, kT*=1.2), sigma=1, 128^3 nodes at dx=0.1 sigma,
+rho_b=0.6, periodic in y and z, a rough 12-3 LJ wall (eps_w=1, 16x16 patches
+of U(-0.5,0.5) sigma heights, seeded) on the low-x side, bulk on the high-x side.
+
+A step is one Newton iteration: the FP64 residual fill, the Schur-complement
+GMRES solve (Schur products in FP32: the mixed-precision form; in FP64 for the
+plain form) and the damped update.  W warm-up iterations start from the
+initial state; K timed iterations follow.  The inputs (12 unknowns x 128^3
+doubles = 201 MB, plus the 200+ MB of padded fields) exceed the 129 MB L2, so
+no explicit flush is done between steps.
+
+`--impl reference` times the reference's CPU algorithm (the C oracle under
+oracle/, a restatement of the reference's fill) on the host cores on a bounded
+sample of the same workload and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton iterations/s, 128^3 FMT1+WCA fill + Schur-GMRES solve (mixed FP32 products, FP64 residual)"
+UNIT = "Newton iter/s"
+WORKLOAD = "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall, periodic y,z"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--lin-tol", type=float, default=1e-6)
+    ap.add_argument("--lin-maxit", type=int, default=200)
+    ap.add_argument("--cpu-sample-planes", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def conv_flops_per_apply(p):
+    """Logical flops of the stencil sums of one Schur product (2 per multiply-add)."""
+    nd = p.ndim
+    fwd = tr = att = 0
+    for c in range(p.ncomp):
+        Lt = len(p.stencils[(1, c)][1])
+        Ld = len(p.stencils[(0, c)][1])
+        nout = (1 + nd) if p.single_size else (3 + 2 * nd)
+        fwd += Lt + nout * Ld
+        tr += Lt + (1 + nd) * Ld
+    if p.attraction:
+        for k in range(p.ncomp * p.ncomp):
+            att += len(p.stencils[(2, k)][1])
+    return 2.0 * p.nnodes * (fwd + tr + att), 2.0 * p.nnodes * att
+
+
+def cpu_baseline(p, x, k_gmres, planes, threads=1):
+    """Time the C oracle's residual fill on `planes` x-planes of the workload and
+    extrapolate to one Newton iteration = (1 + k) fills (k = GMRES iterations)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import orc
+    o = orc.Oracle(p)
+    nxy = p.nx[0] * p.nx[1]
+    # sample: the first `planes` z-planes (full x-y extent, wall and bulk included)
+    t0 = time.perf_counter()
+    if threads <= 1:
+        o.resid_rows(x, 0, planes * nxy)
+        dt = time.perf_counter() - t0
+        nodes = planes * nxy
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+        # ctypes releases the GIL: one row range per thread
+        per = max(1, planes // threads)
+        ranges = [(i * per * nxy, (i + 1) * per * nxy) for i in range(threads)]
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda r: o.resid_rows(x, r[0], r[1]), ranges))
+        dt = time.perf_counter() - t0
+        nodes = per * threads * nxy
+    t_fill = dt * p.nnodes / nodes
+    t_iter = (1 + k_gmres) * t_fill
+    return {"value": 1.0 / t_iter, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle residual fill of {nodes} of {p.nnodes} nodes ({dt:.1f} s); Newton iteration "
+                      f"extrapolated as (1 + {k_gmres:.0f} GMRES iterations) x full fill",
+            "t_fill_s": t_fill}
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU algorithm on the host cores."""
+    from tramonto_gb300 import setup
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    p, meta = setup.config2(n=args.n)
+    # initial state on the host: densities rho_b exp(-V), weighted densities from the oracle's sums
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import orc
+    o = orc.Oracle(p)
+    x = np.zeros((p.nunk, p.nnodes))
+    rho = p.rho_b[0] * np.exp(-np.minimum(p.vext[0], 50.0))
+    rho[p.zero_density[0] != 0] = 0.0
+    x[0] = rho
+    threads = os.cpu_count() or 1
+    k_gmres = 20.0   # GMRES iterations per Newton step of the GPU run (order of magnitude)
+    steps = []
+    for _ in range(max(1, args.steps)):
+        cb = cpu_baseline(p, x, k_gmres, planes=max(threads, args.cpu_sample_planes), threads=threads)
+        steps.append(cb["value"])
+    v = float(np.median(steps))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "inputs_exceed_l2": True},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from tramonto_gb300 import native, setup
+    t_setup = time.perf_counter()
+    p, meta = setup.config2(n=args.n)
+    s = native.Solver(p, device=local, precision=native.FP32)
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream.cuda_stream)
+    x0 = setup.initial_state(s, p)
+    t_setup = time.perf_counter() - t_setup
+    n = p.nunk * p.nnodes
+    dx = torch.from_numpy(x0).to("cuda").contiguous()
+    # warm-up (mixed)
+    it_total = 0
+    for _ in range(args.warmup):
+        s.newton_device(dx, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    s.reset_stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gm = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            s.newton_device(dx, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    st = s.stats()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    applies_per_step = st["schur_applies"] / args.steps
+    value = world * 1e3 / ms
+    # per-kernel-family timing: one fill and one Schur product, FP64 and FP32
+    R = torch.empty_like(dx)
+    v2 = torch.randn(p.ncomp * p.nnodes, dtype=torch.float64, device="cuda")
+    y2 = torch.empty_like(v2)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    t_fill = timed(lambda: s.fill_device(dx, R, 0))
+    s.set_precision(native.FP32)
+    t_apply32 = timed(lambda: s.schur_device(v2, y2), reps=5)
+    s.set_precision(native.FP64)
+    t_apply64 = timed(lambda: s.schur_device(v2, y2), reps=2)
+    # plain FP64 Newton iterations from the same state
+    fp64_ms = None
+    if args.fp64_steps > 0:
+        dx64 = torch.from_numpy(x0).to("cuda").contiguous()
+        for _ in range(min(1, args.warmup)):
+            s.newton_device(dx64, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(args.fp64_steps):
+            s.newton_device(dx64, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = a.elapsed_time(b) / args.fp64_steps
+        del dx64
+    s.set_precision(native.FP32)
+    # end to end through the C ABI with host buffers (copies inside the timed region)
+    xh = dx.cpu().numpy().copy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        xh, _, _ = s.newton(xh, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+    flops_apply, flops_att = conv_flops_per_apply(p)
+    hbm, bf16, peak_src = peaks()
+    # dominant kernel: the FP64 residual fill's stencil sums (the WCA sum dominates)
+    flops_fill = flops_apply  # same stencil work as one product
+    ach_tf = flops_fill / (t_fill * 1e-3) / 1e12
+    if rank == 0:
+        cb = None
+        if not args.no_cpu_baseline:
+            k = max(1.0, applies_per_step)
+            cb = cpu_baseline(p, dx.cpu().numpy(), k, planes=args.cpu_sample_planes, threads=1)
+            cb.pop("t_fill_s", None)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 residual, f32 Schur products", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
+                       "rho_b": 0.6, "kT": 1.2, "rcut": 2.5, "lin_tol": args.lin_tol,
+                       "inputs_exceed_l2": True, "l2_flush": "none (working set > L2)"},
+            "gpu_launches": int(st["kernel_launches"]),
+            "clocks": clk.summary(),
+            "e2e": {"value": 1e3 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
+            "roofline": {"bound": "tensor", "kernel": "FP64 residual fill (stencil sums, WCA dominant)",
+                         "achieved": ach_tf, "peak": bf16, "unit": "TFLOP/s", "frac": ach_tf / bf16,
+                         "peak_source": f"{peak_src} bf16 dense", "traffic": None,
+                         "note": "stencil sums run on the FP64/FP32 SIMT pipes; tensor roof shown for reference"},
+            "cpu_baseline": cb,
+            "breakdown_ms": {"fill_fp64": t_fill, "schur_apply_fp32": t_apply32, "schur_apply_fp64": t_apply64,
+                             "schur_applies_per_step": applies_per_step},
+            "plain_fp64": {"ms_per_step": fp64_ms, "speedup_mixed_vs_fp64": (fp64_ms / ms) if fp64_ms else None},
+            "setup_s": t_setup,
+        }
+        print(json.dumps(out))
+    s.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

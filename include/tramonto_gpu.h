@@ -1,0 +1,169 @@
+/* tramonto_gpu.h — C ABI of the GB300 nonlocal-density path.
+ *
+ * One handle holds one hard-sphere (FMT) + WCA mean-field problem resident on
+ * one GPU.  The entry points replace, one level above the per-scalar
+ * dft_linprobmgr_* inserts, the reference calls on the Newton path:
+ *
+ *   tgpu_fill              fill_resid_and_matrix_control   src/dft_fill_control.c:39-63
+ *                          (FMT1stDeriv_switch src/dft_switch_FMT.c:68, fill_resid_and_matrix
+ *                           src/dft_fill_main.c:38-153 with load_euler_lagrange, load_rho_bar_s/v,
+ *                           load_mean_field)
+ *   tgpu_jv / tgpu_jtv     the assembled Jacobian of that fill applied matrix-free
+ *                          (dft_linprobmgr_applymatrix src/dft_basic_lin_prob_mgr_wrapper.h:86;
+ *                           the transpose has no reference counterpart: SetUseTranspose returns -1,
+ *                           src/dft_HardSphereA11_Epetra_Operator.hpp:68)
+ *   tgpu_schur_apply       dft_Schur_Epetra_Operator::Apply src/dft_Schur_Epetra_Operator.cpp:86-119
+ *   tgpu_schur_rhs         dft_Schur_Epetra_Operator::ComputeRHS :121-133
+ *   tgpu_schur_x1          dft_Schur_Epetra_Operator::ComputeX1 :135-147
+ *   tgpu_solve             dft_linprobmgr_setupsolver + dft_linprobmgr_solve
+ *                          (dft_HardSphereLinProbMgr::setupSolver/solve src/dft_HardSphereLinProbMgr.cpp:345-428)
+ *   tgpu_newton            newton_solver + update_solution src/dft_newton.c:131-381
+ *
+ * Conventions
+ *   - Fields are SoA [unknown][node], node = ix + nx*(iy + ny*iz): the layout
+ *     of the reference's x[iunk][inode_box] for one process (src/rf_allo.c:171).
+ *   - Unknown order as setup_nunk_per_node (src/dft_defs_unknowns.c:37-176):
+ *     ncomp densities, 4+2*ndim weighted densities (n3, n2, n1, n0, V2[d], V1[d]),
+ *     then ncomp mean-field unknowns when attractions are on.
+ *   - Residuals R are returned with the reference's sign of "resid"; the
+ *     reference's rhs vector is -R.
+ *   - Functions without the _device suffix take HOST pointers and copy; the
+ *     _device variants take device pointers on the handle's stream.
+ *   - Every function returns a tgpu_status; no C++ exception crosses the ABI.
+ *   - One handle is used from one host thread at a time.
+ */
+#ifndef TRAMONTO_GPU_H
+#define TRAMONTO_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tgpu_ctx *tgpu_handle;
+
+typedef enum {
+  TGPU_OK = 0,
+  TGPU_ERR_ARG = -1,          /* bad argument or size */
+  TGPU_ERR_CUDA = -2,         /* a CUDA call failed; tgpu_last_error() has the text */
+  TGPU_ERR_STATE = -3,        /* call out of order (e.g. apply before fill) */
+  TGPU_ERR_UNSUPPORTED = -4,  /* option outside the implemented path */
+  TGPU_ERR_NOCONV = -5,       /* iteration cap reached (GMRES or Newton) */
+  TGPU_ERR_NONFINITE = -6,    /* NaN/Inf in inputs or iterates */
+  TGPU_ERR_DOMAIN = -7        /* n3 >= 1 or density <= 0 where a log/1/(1-n3) is taken */
+} tgpu_status;
+
+/* boundary codes (reference Type_bc values, src/dft_globals_const.h) */
+enum { TGPU_BC_IN_WALL = -1, TGPU_BC_IN_BULK = 0, TGPU_BC_PERIODIC = 1, TGPU_BC_REFLECT = 2 };
+/* functionals (reference Type_func values) */
+enum { TGPU_FMT1 = 0, TGPU_FMT3 = 2 };
+/* stencil types (reference Stencil ids, src/dft_globals_const.h:152-161) */
+enum { TGPU_STEN_DELTA = 0, TGPU_STEN_THETA = 1, TGPU_STEN_UATT = 2 };
+/* arithmetic of the stencil convolutions */
+enum { TGPU_FP64 = 0, TGPU_FP32 = 1, TGPU_BF16X3 = 2 };
+
+#define TGPU_MAXC 4
+
+typedef struct {
+  int ndim;
+  int nx[3];                 /* nodes per dimension (unused dims: 1) */
+  double esize[3];           /* Esize_x */
+  int bc[3][2];              /* Type_bc[idim][left/right] */
+  int ncomp;
+  int functional;            /* TGPU_FMT1 | TGPU_FMT3 */
+  int attraction;            /* 1: WCA mean field (Type_attr != NONE) */
+  int att_in_a22;            /* ATTInA22Block; only 0 (mean field as its own unknown) is implemented */
+  int single_size;           /* n1, n0, V1 are local copies (src/dft_fill_FMT.c:215, :303) */
+  int hard_surf;             /* Lhard_surf: hard-wall boundary weights */
+  int nlists_hw;             /* Nlists_HW */
+  double rho_b[TGPU_MAXC];
+  double betamu_hs_ex[TGPU_MAXC];
+  double betamu_att[TGPU_MAXC];
+  double inv_rad[TGPU_MAXC];
+  double inv_4pir[TGPU_MAXC];
+  double inv_4pirsq[TGPU_MAXC];
+  double fac_overlap[TGPU_MAXC];
+  double dphi_bulk[4];       /* Dphi_Drhobar_b[0..3]: bulk dPhi/dn0..dn3 */
+  double vext_max;           /* VEXT_MAX: nodes with V_ext == vext_max are zero-density rows */
+} tgpu_geometry;
+
+/* lifecycle: create -> set_stencil/set_vext/set_zero_density/set_hard_wall -> finalize */
+int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out);
+int tgpu_destroy(tgpu_handle h);
+const char *tgpu_last_error(void);
+/* Stencil table (Stencil[type][0][index], src/dft_globals_const.h:635-646):
+ * offsets[length][ndim], weights[length], hw[length][2^ndim] or NULL. */
+int tgpu_set_stencil(tgpu_handle h, int type, int index, int length, const short *offsets,
+                     const double *weights, const double *hw);
+int tgpu_set_vext(tgpu_handle h, const double *vext);                 /* [ncomp][N] */
+int tgpu_set_zero_density(tgpu_handle h, const signed char *flags);   /* [ncomp][N] */
+/* Hard-wall data: boundary_nodes[nlists][N] (Nodes_2_boundary_wall, -1 = none) and
+ * fluid_masks[nlists][2^ndim][N]: bit l set when the element that has the node
+ * as local corner l (for that reflection pattern) is fluid (src/dft_utils.c:41-62). */
+int tgpu_set_hard_wall(tgpu_handle h, const int *boundary_nodes, const short *fluid_masks);
+int tgpu_finalize(tgpu_handle h);
+/* Arithmetic of the Jacobian / Schur products (TGPU_FP64 or TGPU_FP32); the
+ * residual fill always sums in FP64. */
+int tgpu_set_precision(tgpu_handle h, int precision);
+int tgpu_set_stream(tgpu_handle h, void *cuda_stream);
+int tgpu_sizes(tgpu_handle h, long *nnodes, int *nunk, int *ncomp);
+
+/* Residual of every unknown at state x ([nunk][N]).  mode 0 also keeps the
+ * Jacobian state (the weighted densities and 1/rho of x) for the products below;
+ * mode 1 is residual only (resid_only_flag CALC_RESID_ONLY). */
+int tgpu_fill(tgpu_handle h, const double *x, double *resid, int mode);
+int tgpu_fill_device(tgpu_handle h, const double *d_x, double *d_resid, int mode);
+/* J v and J^T w with the Jacobian of the last mode-0 fill ([nunk][N] each) */
+int tgpu_jv(tgpu_handle h, const double *v, double *out);
+int tgpu_jv_device(tgpu_handle h, const double *d_v, double *d_out);
+int tgpu_jtv(tgpu_handle h, const double *w, double *out);
+int tgpu_jtv_device(tgpu_handle h, const double *d_w, double *d_out);
+/* Schur complement on the density block ([ncomp][N] in and out) */
+int tgpu_schur_apply(tgpu_handle h, const double *v2, double *y2);
+int tgpu_schur_apply_device(tgpu_handle h, const double *d_v2, double *d_y2);
+/* b2S = b2 - A21 A11^-1 b1 from a full right-hand side b ([nunk][N]) */
+int tgpu_schur_rhs_device(tgpu_handle h, const double *d_b, double *d_b2s);
+/* x1 = A11^-1 (b1 - A12 x2); writes the block-1 unknowns of d_x ([nunk][N]) and copies x2 in */
+int tgpu_schur_x1_device(tgpu_handle h, const double *d_b, const double *d_x2, double *d_x);
+/* Newton step: solve J dx = b (b = -R) by GMRES on the Schur complement with
+ * A22 as left preconditioner; stops on ||M^-1 r|| / ||M^-1 r0|| < tol. */
+int tgpu_solve(tgpu_handle h, const double *b, double *dx, double tol, int max_iter, int *iters, double *relres);
+int tgpu_solve_device(tgpu_handle h, const double *d_b, double *d_dx, double tol, int max_iter, int *iters,
+                      double *relres);
+/* Damped Newton of src/dft_newton.c:131-381 on host-resident x ([nunk][N], updated in place).
+ * Stops when the weighted update norm ||frac*dx/(rel_tol*x+abs_tol)|| <= 1. */
+int tgpu_newton(tgpu_handle h, double *x, double rel_tol, double abs_tol, double update_floor, int max_iter,
+                double lin_tol, int lin_max_iter, int *iters, double *final_resid_norm);
+int tgpu_newton_device(tgpu_handle h, double *d_x, double rel_tol, double abs_tol, double update_floor,
+                       int max_iter, double lin_tol, int lin_max_iter, int *iters, double *final_resid_norm);
+
+/* ---- set-up helpers (host only, no GPU) ------------------------------------
+ * Stencil tables built as calc_stencils (src/dft_stencil.c:40-287) builds
+ * Stencil[type][0][index] for the delta shell (DELTA_FN_R), the theta ball
+ * (THETA_FN_R) and the WCA attraction (THETA_PAIRPOT_RCUT, Type_attr 0 with the
+ * cut-and-shifted LJ 12-6 tail, src/dft_stencil_theta_uattr.c:35-158).
+ * Call with offsets == NULL to get the length; then with arrays of that
+ * capacity.  hw (may be NULL) receives the per-corner weights [L][2^ndim].
+ * Returns the length or a negative tgpu_status. */
+int tgpu_make_stencil(int type, int ndim, const double *esize, double hs_diam, double sigma, double eps_over_kT,
+                      double rcut, double rmin, int capacity, short *offsets, double *weights, double *hw,
+                      double *volume);
+/* r of the minimum of the cut-and-shifted LJ 12-6 potential, located by the
+ * search of pairPot_find_rmin (src/dft_pairPot.c:98-152) */
+double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0);
+/* the WCA attraction u_att(r) in kT (uLJ12_6_ATT_CS, src/dft_pairPot_LJ12_6.c:128-168) */
+double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double rmin);
+
+/* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */
+typedef struct {
+  double fill_ms, schur_ms, conv_ms, gmres_ms;
+  long schur_applies, conv_launches, kernel_launches;
+} tgpu_stats;
+int tgpu_get_stats(tgpu_handle h, tgpu_stats *out);
+int tgpu_reset_stats(tgpu_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,69 @@
+"""GPU path against the reference's golden vectors and the C oracle (FP64).
+
+Tolerances: residual entries absolute 1e-12 (they sum O(1..10) terms), Jacobian
+and Schur products 1e-12 relative to their max norm.  Every call goes through
+the C ABI (tramonto_gb300.native -> libtramonto_gpu.so)."""
+import numpy as np
+import pytest
+
+import orc
+from goldens import CASES, PROD_RTOL, RESID_ATOL, load, probe, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    from tramonto_gb300.native import Solver
+    z, p = load(request.param)
+    s = Solver(p)
+    yield request.param, z, p, s
+    s.close()
+
+
+def test_fill_matches_reference(case):
+    name, z, p, s = case
+    for k in range(len(z["states"])):
+        R = s.fill(z[f"x{k}"])
+        err = np.abs(R - z[f"R{k}"]).max()
+        assert err <= RESID_ATOL, (name, k, err)
+
+
+def test_jacobian_product_matches_reference(case):
+    name, z, p, s = case
+    N = p.nunk * p.nnodes
+    for k in range(len(z["states"])):
+        x = z[f"x{k}"]
+        s.fill(x)
+        Jv = s.jv(probe(N, 0).reshape(x.shape))
+        assert rel_err(Jv, z[f"Jv{k}"]) <= PROD_RTOL, (name, k, rel_err(Jv, z[f"Jv{k}"]))
+
+
+def test_schur_product_matches_reference(case):
+    name, z, p, s = case
+    for k in range(len(z["states"])):
+        s.fill(z[f"x{k}"])
+        S = s.schur(probe(p.ncomp * p.nnodes, 2).reshape(p.ncomp, p.nnodes))
+        assert rel_err(S, z[f"schur_Sv{k}"]) <= PROD_RTOL, (name, k, rel_err(S, z[f"schur_Sv{k}"]))
+
+
+def test_fill_matches_oracle_on_random_state(case):
+    name, z, p, s = case
+    rng = np.random.default_rng(3)
+    k = len(z["states"]) - 1
+    x = z[f"x{k}"] * (1.0 + 0.01 * rng.uniform(-1, 1, z[f"x{k}"].shape))
+    o = orc.Oracle(p)
+    assert np.abs(s.fill(x) - o.resid(x)).max() <= RESID_ATOL
+    v2 = rng.standard_normal((p.ncomp, p.nnodes))
+    assert rel_err(s.schur(v2), o.schur(x, v2)) <= PROD_RTOL
+
+
+def test_newton_converges_to_reference_solution(case):
+    name, z, p, s = case
+    k = len(z["states"]) - 1
+    x, iters, rn = s.newton(z[f"x{k}"], rel_tol=1e-3, abs_tol=1e-8, update_floor=0.1, max_iter=50, lin_tol=1e-10)
+    ref = z["x_newton"]
+    rho = slice(p.first_rho, p.first_rho + p.ncomp)
+    err = np.abs(x[rho] - ref[rho]).max() / np.abs(ref[rho]).max()
+    assert err < 1e-7, (name, iters, err)
+    assert np.abs(s.fill(x)).max() < 1e-7

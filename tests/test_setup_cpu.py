@@ -1,0 +1,49 @@
+"""Host set-up against the reference: generated stencil tables and bulk constants."""
+import numpy as np
+import pytest
+
+from goldens import load
+from tramonto_gb300 import setup
+
+CASES = ["hs1d_wall", "hs1d_reflect", "lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_stencils_match_reference(case):
+    z, p = load(case)
+    d = z["info_doubles"]
+    nc = p.ncomp
+    sig, eps, cut = (d[a:a + 36].reshape(6, 6) for a in (147, 111, 183))
+    for (t, idx), (off, w, hw) in p.stencils.items():
+        if t < 2:
+            o2, w2, h2 = setup.make_stencil(t, p.ndim, p.esize, hs_diam=p.hs_diam[idx], with_hw=hw is not None)
+        else:
+            i, j = idx % nc, idx // nc
+            rmin = setup.lj_rmin(sig[i, j], eps[i, j], cut[i, j], p.esize[0])
+            o2, w2, h2 = setup.make_stencil(t, p.ndim, p.esize, sigma=sig[i, j], eps=eps[i, j], rcut=cut[i, j],
+                                            rmin=rmin)
+        assert np.array_equal(o2, off), (case, t, idx)
+        assert np.abs(w2 - w).max() <= 1e-14 * np.abs(w).max(), (case, t, idx)
+        if hw is not None:
+            assert np.abs(h2 - hw).max() <= 1e-14 * np.abs(hw).max(), (case, t, idx)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_bulk_constants_match_reference(case):
+    z, p = load(case)
+    d = z["info_doubles"]
+    nc = p.ncomp
+    uat = {k[1]: v for k, v in p.stencils.items() if k[0] == 2}
+    b = setup.bulk_constants(p.functional, d[7:7 + nc], d[13:13 + nc], p.attraction, uat, nc)
+    assert np.allclose(b["rhobar_b"], d[55:59], rtol=1e-14, atol=0)
+    assert np.allclose(b["dphi_bulk"], d[65:69], rtol=1e-14, atol=1e-15)
+    assert np.allclose(b["betamu_hs_ex"], d[19:19 + nc], rtol=1e-13)
+    if p.attraction:
+        assert np.allclose(b["betamu_att"], d[25:25 + nc], rtol=1e-13)
+
+
+def test_config_generators_are_seeded():
+    v1, m1 = setup.rough_wall_vext((16, 16, 16), (0.1, 0.1, 0.1), seed=5)
+    v2, m2 = setup.rough_wall_vext((16, 16, 16), (0.1, 0.1, 0.1), seed=5)
+    assert np.array_equal(v1, v2) and m1 == m2
+    assert v1.max() == 10.0 and v1.min() < 0.0

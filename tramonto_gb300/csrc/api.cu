@@ -1,0 +1,1061 @@
+// Host side of the C ABI declared in include/tramonto_gpu.h: problem set-up,
+// the fill, Jacobian and Schur products, the Schur-complement GMRES and the
+// damped Newton loop.  All device work is issued on the handle's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tgpu_internal.h"
+
+using tgpu::DevStencil;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void ck(cudaError_t e, const char *what)
+{
+  if (e != cudaSuccess) throw Error(TGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class F>
+int guard(F &&f)
+{
+  try {
+    return f();
+  } catch (const Error &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return TGPU_ERR_ARG;
+  }
+}
+
+template <class T>
+T *dalloc(size_t n)
+{
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  ck(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
+  return static_cast<T *>(p);
+}
+
+template <class T>
+void dfree(T *&p)
+{
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+template <class T>
+T *upload(const std::vector<T> &h, cudaStream_t s)
+{
+  T *d = dalloc<T>(h.size());
+  if (!h.empty()) ck(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+  return d;
+}
+
+// One-dimensional source map of the padded box: q -> node index (with the
+// reflect bit) or a sentinel, following offset_to_node_box (src/dft_mesh_lib.c:203-297).
+std::vector<int> build_map(int n, int h, int bcl, int bcr)
+{
+  std::vector<int> m(n + 2 * h);
+  for (int q = 0; q < n + 2 * h; q++) {
+    int s = q - h;
+    int v;
+    if (s < 0) {
+      switch (bcl) {
+        case TGPU_BC_IN_BULK: v = tgpu::kSentBulk; break;
+        case TGPU_BC_IN_WALL: v = tgpu::kSentWall; break;
+        case TGPU_BC_REFLECT:
+          s = -s;
+          if (s >= n) v = bcr == TGPU_BC_IN_BULK ? tgpu::kSentBulk : (bcr == TGPU_BC_IN_WALL ? tgpu::kSentWall : tgpu::kSentBad);
+          else v = s | tgpu::kReflBit;
+          break;
+        case TGPU_BC_PERIODIC: s += n; v = s >= 0 ? s : tgpu::kSentBad; break;
+        default: v = tgpu::kSentBad;
+      }
+    } else if (s >= n) {
+      switch (bcr) {
+        case TGPU_BC_IN_BULK: v = tgpu::kSentBulk; break;
+        case TGPU_BC_IN_WALL: v = tgpu::kSentWall; break;
+        case TGPU_BC_REFLECT:
+          s = 2 * (n - 1) - s;
+          if (s < 0) v = bcl == TGPU_BC_IN_BULK ? tgpu::kSentBulk : (bcl == TGPU_BC_IN_WALL ? tgpu::kSentWall : tgpu::kSentBad);
+          else v = s | tgpu::kReflBit;
+          break;
+        case TGPU_BC_PERIODIC: s -= n; v = s < n ? s : tgpu::kSentBad; break;
+        default: v = tgpu::kSentBad;
+      }
+    } else {
+      v = s;
+    }
+    m[q] = v;
+  }
+  return m;
+}
+
+// padding parameter sets (device arrays): bulk constant, reflection sign mask, zero-density component
+struct PadParams {
+  double *bulk = nullptr;
+  int *sign = nullptr, *zc = nullptr;
+  int nch = 0;
+};
+
+}  // namespace
+
+struct tgpu_pads {
+  PadParams rho_res, rho_jac, tr_res, tr_jac;
+};
+
+namespace {
+
+struct Ctx : tgpu_ctx {
+  tgpu_pads pads;
+  double *d_ymf = nullptr;
+  double *d_b2s = nullptr;
+  long n2 = 0;
+};
+
+// The geometry lives in one __constant__ block per device; the handle that
+// last uploaded it owns it, and any other handle re-uploads before its work.
+const tgpu_ctx *g_geom_owner = nullptr;
+
+Ctx *C(tgpu_handle h)
+{
+  if (!h) throw Error(TGPU_ERR_ARG, "null handle");
+  Ctx *c = static_cast<Ctx *>(h);
+  if (c->finalized && g_geom_owner != c) {
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    tgpu::upload_geom(c->dg, c->stream);
+    g_geom_owner = c;
+  }
+  return c;
+}
+
+void need_final(Ctx *c)
+{
+  if (!c->finalized) throw Error(TGPU_ERR_STATE, "tgpu_finalize has not been called");
+}
+
+PadParams make_pad(const std::vector<double> &bulk, const std::vector<int> &sign, const std::vector<int> &zc,
+                   cudaStream_t s)
+{
+  PadParams p;
+  p.nch = (int)bulk.size();
+  p.bulk = upload(bulk, s);
+  p.sign = upload(sign, s);
+  p.zc = upload(zc, s);
+  return p;
+}
+
+void free_pad(PadParams &p)
+{
+  dfree(p.bulk);
+  dfree(p.sign);
+  dfree(p.zc);
+}
+
+long nnodes(const tgpu_geometry &g)
+{
+  long n = 1;
+  for (int d = 0; d < g.ndim; d++) n *= g.nx[d];
+  return n;
+}
+
+// ---- stencil passes --------------------------------------------------------
+
+// Pad `nch` channels of `src` with parameter set `pp`.  Residual passes are
+// always FP64; Jacobian/Schur passes use the handle's product precision.
+void pad(Ctx *c, const double *src, const PadParams &pp, bool fp64)
+{
+  if (fp64 || c->precision == TGPU_FP64)
+    tgpu::launch_pad<double>(src, c->d_pad, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
+  else
+    tgpu::launch_pad<float>(src, c->d_pad32, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
+  c->stats.kernel_launches++;
+}
+
+void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool fp64)
+{
+  const long NP = c->dg.NP;
+  if (fp64 || c->precision == TGPU_FP64)
+    tgpu::launch_conv<double>(c->d_pad + (long)ch0 * NP, NP, nin, st.d_loff, tr ? st.d_coef_tr : st.d_coef_fwd, st.L,
+                              outs, nout, true, c->dg.N, c->stream);
+  else
+    tgpu::launch_conv<float>(c->d_pad32 + (long)ch0 * NP, NP, nin, st.d_loff, tr ? st.d_coef_tr32 : st.d_coef_fwd32,
+                             st.L, outs, nout, true, c->dg.N, c->stream);
+  c->stats.conv_launches++;
+  c->stats.kernel_launches++;
+}
+
+// Weighted-density (and mean-field) sums of a density-shaped field
+// (`field` points at the first density row, rows N apart) into d_conv.
+void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool fp64)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * (size_t)(g.nrb + g.ncomp) * N, c->stream), "memset");
+  pad(c, field, pp, fp64);
+  const int nd = g.ndim;
+  for (int jc = 0; jc < g.ncomp; jc++) {
+    double *o_th[1] = {c->d_conv};
+    conv(c, jc, 1, c->sten[TGPU_STEN_THETA][jc], false, o_th, 1, fp64);
+    std::vector<double *> o_de;
+    o_de.push_back(c->d_conv + 1 * N);
+    if (!g.single_size) {
+      o_de.push_back(c->d_conv + 2 * N);
+      o_de.push_back(c->d_conv + 3 * N);
+    }
+    for (int d = 0; d < nd; d++) o_de.push_back(c->d_conv + (long)(4 + d) * N);
+    if (!g.single_size)
+      for (int d = 0; d < nd; d++) o_de.push_back(c->d_conv + (long)(4 + nd + d) * N);
+    conv(c, jc, 1, c->sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), fp64);
+    if (g.attraction)
+      for (int ic = 0; ic < g.ncomp; ic++) {
+        double *o_mf[1] = {c->d_conv + (long)(g.nrb + ic) * N};
+        conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o_mf, 1, fp64);
+      }
+  }
+  if (g.hard_surf && !c->hw_targets.empty()) {
+    tgpu::launch_hw_correct(field, N, 0, c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(), nullptr,
+                            c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero, c->d_bnodes, c->d_fmask,
+                            c->d_conv, c->stream);
+    c->stats.kernel_launches++;
+  }
+}
+
+// Euler-Lagrange stencil sums over the channels in d_chan into d_tr.
+void transpose_pass(Ctx *c, const PadParams &pp, bool fp64)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  const int nd = g.ndim;
+  ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+  pad(c, c->d_chan, pp, fp64);
+  for (int ic = 0; ic < g.ncomp; ic++) {
+    double *o[1] = {c->d_tr + (long)ic * N};
+    conv(c, ic * (nd + 2), 1 + nd, c->sten[TGPU_STEN_DELTA][ic], true, o, 1, fp64);
+    conv(c, ic * (nd + 2) + nd + 1, 1, c->sten[TGPU_STEN_THETA][ic], true, o, 1, fp64);
+  }
+}
+
+void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
+{
+  need_final(c);
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  if (d_x != c->d_x && mode == 0)
+    ck(cudaMemcpyAsync(c->d_x, d_x, sizeof(double) * (size_t)g.nunk * N, cudaMemcpyDeviceToDevice, c->stream), "copy x");
+  const double *x = mode == 0 ? c->d_x : d_x;
+  forward_pass(c, x + (long)g.first_rho * N, c->pads.rho_res, true);
+  tgpu::launch_fmt_local(x, c->d_chan, c->stream);
+  transpose_pass(c, c->pads.tr_res, true);
+  tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream);
+  c->stats.kernel_launches += 2;
+  if (mode == 0) c->have_state = true;
+}
+
+void need_state(Ctx *c)
+{
+  need_final(c);
+  if (!c->have_state) throw Error(TGPU_ERR_STATE, "no Jacobian state: call tgpu_fill with mode 0 first");
+}
+
+void schur_device(Ctx *c, const double *d_v2, double *d_y2)
+{
+  need_state(c);
+  forward_pass(c, d_v2, c->pads.rho_jac, false);
+  tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, c->stream);
+  transpose_pass(c, c->pads.tr_jac, false);
+  tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, d_v2, c->d_tr, c->d_ymf, d_y2, c->stream);
+  c->stats.kernel_launches += 2;
+  c->stats.schur_applies++;
+}
+
+void jv_device(Ctx *c, const double *d_v, double *d_out)
+{
+  need_state(c);
+  const long N = c->dg.N;
+  forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, false);
+  tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, c->stream);
+  transpose_pass(c, c->pads.tr_jac, false);
+  tgpu::launch_jv_combine(c->d_x, c->d_vext, c->d_zero, d_v, c->d_conv, c->d_tr, d_out, c->stream);
+  c->stats.kernel_launches += 2;
+}
+
+}  // namespace
+
+// ---- kernels used only by the Schur rhs / back-substitution ------------------
+namespace tgpu {
+void launch_rhs_local(const double *x, const double *b, double *chan, double *ymf, cudaStream_t s);
+void launch_rhs_combine(const double *vext, const signed char *zero, const double *b, const double *tr,
+                        const double *ymf, double *b2s, cudaStream_t s);
+void launch_x1(const double *b, const double *conv, const double *x2, double *dx, cudaStream_t s);
+}  // namespace tgpu
+
+namespace {
+
+void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
+{
+  need_state(c);
+  tgpu::launch_rhs_local(c->d_x, d_b, c->d_chan, c->d_ymf, c->stream);
+  transpose_pass(c, c->pads.tr_jac, false);
+  tgpu::launch_rhs_combine(c->d_vext, c->d_zero, d_b, c->d_tr, c->d_ymf, d_b2s, c->stream);
+  c->stats.kernel_launches += 2;
+}
+
+void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx)
+{
+  need_state(c);
+  forward_pass(c, d_x2, c->pads.rho_jac, false);
+  tgpu::launch_x1(d_b, c->d_conv, d_x2, d_dx, c->stream);
+  c->stats.kernel_launches++;
+}
+
+// ---- GMRES on the Schur complement (src/dft_HardSphereLinProbMgr.cpp:345-428) --
+
+void ensure_krylov(Ctx *c, int kdim)
+{
+  if (kdim <= c->kdim) return;
+  dfree(c->d_V);
+  c->d_V = dalloc<double>((size_t)(kdim + 1) * c->n2);
+  c->kdim = kdim;
+}
+
+void red_to_host(Ctx *c, int n)
+{
+  ck(cudaMemcpyAsync(c->h_red, c->d_red, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream), "d2h");
+  ck(cudaStreamSynchronize(c->stream), "sync");
+}
+
+int gmres(Ctx *c, const double *d_rhs, double *d_x2, double tol, int maxit, int *iters, double *relres)
+{
+  const long n = c->n2;
+  const int nb = tgpu::reduce_blocks(n);
+  const int kdim = std::max(1, std::min(maxit, 500));
+  ensure_krylov(c, kdim);
+  double *V = c->d_V;
+  ck(cudaMemsetAsync(d_x2, 0, sizeof(double) * n, c->stream), "memset");
+  // r0 = M^-1 b
+  tgpu::launch_precond(c->d_x, c->d_vext, c->d_zero, d_rhs, c->d_gt, c->stream);
+  tgpu::launch_norm2(c->d_gt, n, c->d_partial, nb, c->d_red, c->stream);
+  red_to_host(c, 1);
+  const double r0 = std::sqrt(c->h_red[0]);
+  *iters = 0;
+  *relres = 0.0;
+  if (!(r0 > 0.0)) {
+    if (!std::isfinite(r0)) throw Error(TGPU_ERR_NONFINITE, "non-finite right-hand side in the Schur solve");
+    return TGPU_OK;
+  }
+  int it = 0;
+  double rel = 1.0;
+  std::vector<double> H((size_t)(kdim + 1) * kdim), cs(kdim), sn(kdim), gv(kdim + 1), y(kdim);
+  bool first = true;
+  while (it < maxit) {
+    double beta;
+    if (first) {
+      beta = r0;
+      tgpu::launch_scale(V, c->d_gt, 1.0 / beta, n, c->stream);
+      first = false;
+    } else {
+      // r = M^-1 (b - S x)
+      schur_device(c, d_x2, c->d_gw);
+      tgpu::launch_axpby(c->d_gw, 1.0, d_rhs, -1.0, n, c->stream);
+      tgpu::launch_precond(c->d_x, c->d_vext, c->d_zero, c->d_gw, c->d_gt, c->stream);
+      tgpu::launch_norm2(c->d_gt, n, c->d_partial, nb, c->d_red, c->stream);
+      red_to_host(c, 1);
+      beta = std::sqrt(c->h_red[0]);
+      rel = beta / r0;
+      if (rel < tol) break;
+      tgpu::launch_scale(V, c->d_gt, 1.0 / beta, n, c->stream);
+    }
+    const int m = std::min(kdim, maxit - it);
+    std::fill(H.begin(), H.end(), 0.0);
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+    int k = 0;
+    for (; k < m; k++) {
+      schur_device(c, V + (long)k * n, c->d_gw);
+      tgpu::launch_precond(c->d_x, c->d_vext, c->d_zero, c->d_gw, c->d_gt, c->stream);
+      // classical Gram-Schmidt, two passes; h and the norm stay on the device
+      // until one copy per iteration
+      double *d_h1 = c->d_red, *d_h2 = c->d_red + (kdim + 1), *d_nrm = c->d_red + 2 * (kdim + 1);
+      tgpu::launch_multidot(V, n, k + 1, c->d_gt, n, c->d_partial, nb, d_h1, c->stream);
+      tgpu::launch_multiaxpy(c->d_gt, V, n, k + 1, d_h1, n, c->stream);
+      tgpu::launch_multidot(V, n, k + 1, c->d_gt, n, c->d_partial, nb, d_h2, c->stream);
+      tgpu::launch_multiaxpy(c->d_gt, V, n, k + 1, d_h2, n, c->stream);
+      tgpu::launch_norm2(c->d_gt, n, c->d_partial, nb, d_nrm, c->stream);
+      c->stats.kernel_launches += 9;
+      red_to_host(c, 2 * (kdim + 1) + 1);
+      const double hn = std::sqrt(c->h_red[2 * (kdim + 1)]);
+      if (!std::isfinite(hn)) throw Error(TGPU_ERR_NONFINITE, "non-finite Krylov vector in the Schur solve");
+      for (int j = 0; j <= k; j++) H[(size_t)j * kdim + k] = c->h_red[j] + c->h_red[kdim + 1 + j];
+      H[(size_t)(k + 1) * kdim + k] = hn;
+      if (hn > 0.0) tgpu::launch_scale(V + (long)(k + 1) * n, c->d_gt, 1.0 / hn, n, c->stream);
+      for (int j = 0; j < k; j++) {
+        const double a = H[(size_t)j * kdim + k], b = H[(size_t)(j + 1) * kdim + k];
+        H[(size_t)j * kdim + k] = cs[j] * a + sn[j] * b;
+        H[(size_t)(j + 1) * kdim + k] = -sn[j] * a + cs[j] * b;
+      }
+      const double a = H[(size_t)k * kdim + k], b = H[(size_t)(k + 1) * kdim + k];
+      const double den = std::sqrt(a * a + b * b);
+      cs[k] = den == 0.0 ? 1.0 : a / den;
+      sn[k] = den == 0.0 ? 0.0 : b / den;
+      H[(size_t)k * kdim + k] = den;
+      H[(size_t)(k + 1) * kdim + k] = 0.0;
+      gv[k + 1] = -sn[k] * gv[k];
+      gv[k] = cs[k] * gv[k];
+      it++;
+      rel = std::fabs(gv[k + 1]) / r0;
+      if (rel < tol || hn == 0.0) {
+        k++;
+        break;
+      }
+    }
+    for (int i = k - 1; i >= 0; i--) {
+      double s = gv[i];
+      for (int j = i + 1; j < k; j++) s -= H[(size_t)i * kdim + j] * y[j];
+      y[i] = s / H[(size_t)i * kdim + i];
+    }
+    // x -= sum_j (-y_j) V_j
+    for (int j = 0; j < k; j++) c->h_red[j] = -y[j];
+    ck(cudaMemcpyAsync(c->d_red, c->h_red, sizeof(double) * k, cudaMemcpyHostToDevice, c->stream), "h2d");
+    tgpu::launch_multiaxpy(d_x2, V, n, k, c->d_red, n, c->stream);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    if (rel < tol) break;
+  }
+  *iters = it;
+  *relres = rel;
+  return rel < tol ? TGPU_OK : TGPU_ERR_NOCONV;
+}
+
+int solve_device(Ctx *c, const double *d_b, double *d_dx, double tol, int maxit, int *iters, double *relres)
+{
+  need_state(c);
+  schur_rhs_device(c, d_b, c->d_b2s);
+  const int st = gmres(c, c->d_b2s, c->d_gx, tol, maxit, iters, relres);
+  schur_x1_device(c, d_b, c->d_gx, d_dx);
+  return st;
+}
+
+int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double update_floor, int max_iter,
+                  double lin_tol, int lin_max_iter, int *iters, double *final_resid)
+{
+  need_final(c);
+  const tgpu::DevGeom &g = c->dg;
+  const long n = (long)g.nunk * g.N;
+  const int nb = tgpu::reduce_blocks(n);
+  double *d_R = c->d_work, *d_dx = c->d_work2;
+  int it = 0;
+  bool converged = false;
+  double rnorm = 0.0;
+  int st = TGPU_OK;
+  while (it < max_iter && !converged) {
+    it++;
+    fill_device(c, d_x, d_R, 0);
+    tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    rnorm = std::sqrt(c->h_red[0]);
+    if (!std::isfinite(rnorm)) throw Error(TGPU_ERR_NONFINITE, "non-finite residual in Newton");
+    // b = -R (the reference's rhs)
+    tgpu::launch_scale(d_R, d_R, -1.0, n, c->stream);
+    int li = 0;
+    double lr = 0.0;
+    st = solve_device(c, d_R, d_dx, lin_tol, lin_max_iter, &li, &lr);
+    // update_solution (src/dft_newton.c:266-381): positivity fraction, clamps, weighted norm
+    tgpu::launch_newton_frac(d_x, d_dx, update_floor, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    const double frac = c->h_red[0];
+    tgpu::launch_newton_update(d_x, d_dx, frac, rel_tol, abs_tol, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    const double upd = std::sqrt(c->h_red[0]);
+    if (!std::isfinite(upd)) throw Error(TGPU_ERR_NONFINITE, "non-finite Newton update");
+    converged = upd <= 1.0;
+    c->stats.kernel_launches += 6;
+  }
+  *iters = it;
+  if (final_resid) *final_resid = rnorm;
+  (void)st;
+  return converged ? TGPU_OK : TGPU_ERR_NOCONV;
+}
+
+// Host-pointer wrappers: copy in, run on the device, copy out, synchronise.
+void h2d(Ctx *c, double *d, const double *h, size_t n)
+{
+  ck(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
+}
+void d2h(Ctx *c, double *h, const double *d, size_t n)
+{
+  ck(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "d2h");
+  ck(cudaStreamSynchronize(c->stream), "sync");
+}
+
+void build_device_tables(Ctx *c)
+{
+  tgpu_geometry &g = c->g;
+  tgpu::DevGeom &dg = c->dg;
+  const int nd = g.ndim;
+  // halo = largest stencil reach per dimension
+  int h[3] = {0, 0, 0};
+  for (int t = 0; t < 3; t++)
+    for (auto &st : c->sten[t])
+      for (int k = 0; k < st.L; k++)
+        for (int d = 0; d < nd; d++) h[d] = std::max(h[d], std::abs((int)st.off[(size_t)k * nd + d]));
+  long NP = 1;
+  for (int d = 0; d < 3; d++) {
+    dg.nx[d] = d < nd ? g.nx[d] : 1;
+    dg.h[d] = d < nd ? h[d] : 0;
+    dg.P[d] = dg.nx[d] + 2 * dg.h[d];
+    dg.esize[d] = d < nd ? g.esize[d] : 0.0;
+  }
+  dg.pstride[0] = 1;
+  dg.pstride[1] = dg.P[0];
+  dg.pstride[2] = (long)dg.P[0] * dg.P[1];
+  NP = (long)dg.P[0] * dg.P[1] * dg.P[2];
+  dg.NP = NP;
+  for (int d = 0; d < 3; d++) {
+    std::vector<int> m = d < nd ? build_map(dg.nx[d], dg.h[d], g.bc[d][0], g.bc[d][1]) : std::vector<int>{0};
+    c->d_map[d] = upload(m, c->stream);
+    dg.map[d] = c->d_map[d];
+  }
+  // stencil tables
+  for (int t = 0; t < 3; t++)
+    for (int idx = 0; idx < (int)c->sten[t].size(); idx++) {
+      DevStencil &st = c->sten[t][idx];
+      if (st.L == 0) continue;
+      std::vector<int> loff(st.L);
+      std::vector<short> off3((size_t)st.L * 3, 0);
+      for (int k = 0; k < st.L; k++) {
+        long o = 0;
+        for (int d = 0; d < nd; d++) {
+          o += (long)st.off[(size_t)k * nd + d] * dg.pstride[d];
+          off3[(size_t)k * 3 + d] = st.off[(size_t)k * nd + d];
+        }
+        loff[k] = (int)o;
+      }
+      st.d_loff = upload(loff, c->stream);
+      st.d_off = upload(off3, c->stream);
+      st.d_w = upload(st.w, c->stream);
+      if (!st.hw.empty()) st.d_hw = upload(st.hw, c->stream);
+      std::vector<double> fwd, tr;
+      if (t == TGPU_STEN_THETA) {
+        const int jc = idx;
+        st.nout_fwd = 1;
+        for (int k = 0; k < st.L; k++) fwd.push_back(g.fac_overlap[jc] * st.w[k]);
+        st.nin_tr = 1;
+        tr = st.w;
+      } else if (t == TGPU_STEN_DELTA) {
+        const int jc = idx;
+        const double f = g.fac_overlap[jc];
+        st.nout_fwd = g.single_size ? 1 + nd : 3 + 2 * nd;  // n2 [n1 n0] V2[d] [V1[d]]
+        for (int k = 0; k < st.L; k++) {
+          const double w = st.w[k];
+          fwd.push_back(f * w);
+          if (!g.single_size) {
+            fwd.push_back(f * g.inv_4pir[jc] * w);
+            fwd.push_back(f * g.inv_4pirsq[jc] * w);
+          }
+          for (int d = 0; d < nd; d++) fwd.push_back(f * ((double)st.off[(size_t)k * nd + d] * g.esize[d] * g.inv_rad[jc]) * w);
+          if (!g.single_size)
+            for (int d = 0; d < nd; d++)
+              fwd.push_back(f * g.inv_4pir[jc] * ((double)st.off[(size_t)k * nd + d] * g.esize[d] * g.inv_rad[jc]) * w);
+        }
+        st.nin_tr = 1 + nd;
+        for (int k = 0; k < st.L; k++) {
+          tr.push_back(st.w[k]);
+          for (int d = 0; d < nd; d++) tr.push_back(-st.w[k] * (double)st.off[(size_t)k * nd + d] * g.esize[d] * g.inv_rad[idx]);
+        }
+      } else {
+        st.nout_fwd = 1;
+        fwd = st.w;
+      }
+      st.d_coef_fwd = upload(fwd, c->stream);
+      std::vector<float> f32(fwd.begin(), fwd.end());
+      st.d_coef_fwd32 = upload(f32, c->stream);
+      if (!tr.empty()) {
+        st.d_coef_tr = upload(tr, c->stream);
+        std::vector<float> t32(tr.begin(), tr.end());
+        st.d_coef_tr32 = upload(t32, c->stream);
+      }
+    }
+  const long N = dg.N;
+  // fields
+  if (c->h_vext.empty()) c->h_vext.assign((size_t)g.ncomp * N, 0.0);
+  if (c->h_zero.empty()) c->h_zero.assign((size_t)g.ncomp * N, 0);
+  c->d_vext = upload(c->h_vext, c->stream);
+  c->d_zero = upload(c->h_zero, c->stream);
+  if (g.hard_surf) {
+    c->d_bnodes = upload(c->h_bnodes, c->stream);
+    c->d_fmask = upload(c->h_fmask, c->stream);
+    // target nodes: within the largest stencil reach of a boundary node (box dilation)
+    std::vector<char> mark(N, 0);
+    for (int l = 0; l < g.nlists_hw; l++)
+      for (long i = 0; i < N; i++)
+        if (c->h_bnodes[(size_t)l * N + i] != -1) mark[i] = 1;
+    for (int d = 0; d < nd; d++) {
+      std::vector<char> nm(N, 0);
+      const long stride = d == 0 ? 1 : (d == 1 ? dg.nx[0] : (long)dg.nx[0] * dg.nx[1]);
+      for (long i = 0; i < N; i++) {
+        if (!mark[i]) continue;
+        const int coord = (int)((i / stride) % dg.nx[d]);
+        for (int s = -dg.h[d]; s <= dg.h[d]; s++) {
+          int q = coord + s;
+          if (q < 0 || q >= dg.nx[d]) {
+            if (g.bc[d][0] == TGPU_BC_PERIODIC) q = (q % dg.nx[d] + dg.nx[d]) % dg.nx[d];
+            else if (q < 0 && g.bc[d][0] == TGPU_BC_REFLECT) q = std::min(-q, dg.nx[d] - 1);
+            else if (q >= dg.nx[d] && g.bc[d][1] == TGPU_BC_REFLECT) q = std::max(2 * (dg.nx[d] - 1) - q, 0);
+            else continue;
+          }
+          nm[i + (long)(q - coord) * stride] = 1;
+        }
+      }
+      mark.swap(nm);
+    }
+    for (long i = 0; i < N; i++)
+      if (mark[i]) c->hw_targets.push_back((int)i);
+    c->d_hw_targets = upload(c->hw_targets, c->stream);
+  }
+  // padding parameter sets
+  {
+    std::vector<double> b_res, b_jac;
+    std::vector<int> sg, zc;
+    for (int jc = 0; jc < g.ncomp; jc++) {
+      b_res.push_back(g.rho_b[jc]);
+      b_jac.push_back(0.0);
+      sg.push_back(0);
+      zc.push_back(jc);
+    }
+    c->pads.rho_res = make_pad(b_res, sg, zc, c->stream);
+    c->pads.rho_jac = make_pad(b_jac, sg, zc, c->stream);
+  }
+  {
+    std::vector<double> b_res, b_jac;
+    std::vector<int> sg, zc;
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      const double f = g.fac_overlap[ic];
+      const double *b = g.dphi_bulk;
+      b_res.push_back(f * (b[0] * g.inv_4pirsq[ic] + b[1] * g.inv_4pir[ic] + b[2]));
+      b_jac.push_back(0.0);
+      sg.push_back(0);
+      zc.push_back(-1);
+      for (int d = 0; d < nd; d++) {
+        b_res.push_back(0.0);
+        b_jac.push_back(0.0);
+        sg.push_back(1 << d);
+        zc.push_back(-1);
+      }
+      b_res.push_back(f * b[3]);
+      b_jac.push_back(0.0);
+      sg.push_back(0);
+      zc.push_back(-1);
+    }
+    c->pads.tr_res = make_pad(b_res, sg, zc, c->stream);
+    c->pads.tr_jac = make_pad(b_jac, sg, zc, c->stream);
+  }
+  // work buffers
+  c->nch_max = std::max(g.ncomp, g.ncomp * (nd + 2));
+  const size_t U = (size_t)dg.nunk;
+  c->d_x = dalloc<double>(U * N);
+  c->d_work = dalloc<double>(U * N);
+  c->d_work2 = dalloc<double>(U * N);
+  c->d_pad = dalloc<double>((size_t)c->nch_max * NP);
+  c->d_pad32 = dalloc<float>((size_t)c->nch_max * NP);
+  c->d_chan = dalloc<double>((size_t)c->nch_max * N);
+  c->d_conv = dalloc<double>((size_t)(dg.nrb + dg.ncomp) * N);
+  c->d_tr = dalloc<double>((size_t)dg.ncomp * N);
+  c->d_ymf = dalloc<double>((size_t)dg.ncomp * N);
+  c->n2 = (long)dg.ncomp * N;
+  c->d_b2s = dalloc<double>(c->n2);
+  c->d_gw = dalloc<double>(c->n2);
+  c->d_gt = dalloc<double>(c->n2);
+  c->d_gx = dalloc<double>(c->n2);
+  c->d_gb = dalloc<double>(c->n2);
+  c->d_partial = dalloc<double>((size_t)1024 * 1024);
+  c->d_red = dalloc<double>(4096);
+  ck(cudaMallocHost(&c->h_red, 4096 * sizeof(double)), "cudaMallocHost");
+  tgpu::upload_geom(dg, c->stream);
+  g_geom_owner = c;
+  ck(cudaStreamSynchronize(c->stream), "sync");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *tgpu_last_error(void) { return g_last_error.c_str(); }
+
+int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
+{
+  return guard([&] {
+    if (!geom || !out) throw Error(TGPU_ERR_ARG, "null argument");
+    const tgpu_geometry &g = *geom;
+    if (g.ndim < 1 || g.ndim > 3) throw Error(TGPU_ERR_ARG, "ndim must be 1, 2 or 3");
+    if (g.ncomp < 1 || g.ncomp > TGPU_MAXC) throw Error(TGPU_ERR_ARG, "ncomp out of range");
+    for (int d = 0; d < g.ndim; d++) {
+      if (g.nx[d] < 1) throw Error(TGPU_ERR_ARG, "nx must be positive");
+      for (int k = 0; k < 2; k++)
+        if (g.bc[d][k] < TGPU_BC_IN_WALL || g.bc[d][k] > TGPU_BC_REFLECT)
+          throw Error(TGPU_ERR_UNSUPPORTED, "boundary condition outside IN_WALL/IN_BULK/PERIODIC/REFLECT");
+      if ((g.bc[d][0] == TGPU_BC_PERIODIC) != (g.bc[d][1] == TGPU_BC_PERIODIC))
+        throw Error(TGPU_ERR_ARG, "periodic boundaries must be periodic on both sides");
+    }
+    if (g.functional != TGPU_FMT1 && g.functional != TGPU_FMT3)
+      throw Error(TGPU_ERR_UNSUPPORTED, "only the FMT1 (Rosenfeld) and FMT3 (White-Bear) functionals are implemented");
+    if (g.attraction && g.att_in_a22)
+      throw Error(TGPU_ERR_UNSUPPORTED, "mean field summed into the density rows (ATTInA22Block) is not implemented");
+    if (g.hard_surf && g.attraction)
+      throw Error(TGPU_ERR_UNSUPPORTED, "hard-wall boundary weights with mean-field stencils are not implemented");
+    if (g.hard_surf && g.ncomp > 2) throw Error(TGPU_ERR_UNSUPPORTED, "hard walls with more than two components");
+    const long N = nnodes(g);
+    if (N > (1L << 31) / 4) throw Error(TGPU_ERR_ARG, "mesh too large for 32-bit stencil offsets");
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    Ctx *c = new Ctx;
+    c->g = g;
+    c->device = device;
+    tgpu::DevGeom &dg = c->dg;
+    std::memset(&dg, 0, sizeof(dg));
+    dg.ndim = g.ndim;
+    dg.N = N;
+    dg.ncomp = g.ncomp;
+    dg.nrb = 4 + 2 * g.ndim;
+    dg.first_rho = 0;
+    dg.first_rb = g.ncomp;
+    dg.first_mf = g.attraction ? g.ncomp + dg.nrb : -1;
+    dg.nunk = g.ncomp + dg.nrb + (g.attraction ? g.ncomp : 0);
+    dg.functional = g.functional;
+    dg.attraction = g.attraction;
+    dg.single_size = g.single_size;
+    dg.hard_surf = g.hard_surf;
+    dg.nlists = g.nlists_hw;
+    for (int i = 0; i < TGPU_MAXC; i++) {
+      dg.rho_b[i] = g.rho_b[i];
+      dg.betamu_hs_ex[i] = g.betamu_hs_ex[i];
+      dg.betamu_att[i] = g.betamu_att[i];
+      dg.inv_rad[i] = g.inv_rad[i];
+      dg.inv_4pir[i] = g.inv_4pir[i];
+      dg.inv_4pirsq[i] = g.inv_4pirsq[i];
+      dg.fac[i] = g.fac_overlap[i];
+    }
+    for (int i = 0; i < 4; i++) dg.dphi_bulk[i] = g.dphi_bulk[i];
+    dg.vext_max = g.vext_max;
+    for (int t = 0; t < 3; t++) c->sten[t].resize((size_t)g.ncomp * g.ncomp);
+    ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    c->own_stream = true;
+    *out = c;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_destroy(tgpu_handle h)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (int t = 0; t < 3; t++)
+      for (auto &st : c->sten[t]) {
+        dfree(st.d_loff); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
+        dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32);
+      }
+    for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
+    dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);
+    dfree(c->d_x); dfree(c->d_work); dfree(c->d_work2); dfree(c->d_pad); dfree(c->d_pad32); dfree(c->d_chan);
+    dfree(c->d_conv); dfree(c->d_tr); dfree(c->d_ymf); dfree(c->d_b2s); dfree(c->d_V); dfree(c->d_partial);
+    dfree(c->d_red); dfree(c->d_gw); dfree(c->d_gt); dfree(c->d_gx); dfree(c->d_gb);
+    if (c->h_red) cudaFreeHost(c->h_red);
+    free_pad(c->pads.rho_res); free_pad(c->pads.rho_jac); free_pad(c->pads.tr_res); free_pad(c->pads.tr_jac);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (g_geom_owner == c) g_geom_owner = nullptr;
+    delete c;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_stencil(tgpu_handle h, int type, int index, int length, const short *offsets, const double *weights,
+                     const double *hw)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) throw Error(TGPU_ERR_STATE, "stencils are fixed after tgpu_finalize");
+    if (type < 0 || type > 2) throw Error(TGPU_ERR_ARG, "stencil type");
+    const int nidx = type == TGPU_STEN_UATT ? c->g.ncomp * c->g.ncomp : c->g.ncomp;
+    if (index < 0 || index >= nidx) throw Error(TGPU_ERR_ARG, "stencil index");
+    if (length < 0 || (length > 0 && (!offsets || !weights))) throw Error(TGPU_ERR_ARG, "stencil arrays");
+    DevStencil &st = c->sten[type][index];
+    const int nd = c->g.ndim;
+    st.L = length;
+    st.off.assign(offsets, offsets + (size_t)length * nd);
+    st.w.assign(weights, weights + length);
+    if (hw) st.hw.assign(hw, hw + (size_t)length * (1 << nd));
+    else st.hw.clear();
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_vext(tgpu_handle h, const double *vext)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (!vext) throw Error(TGPU_ERR_ARG, "null vext");
+    const size_t n = (size_t)c->g.ncomp * c->dg.N;
+    for (size_t i = 0; i < n; i++)
+      if (std::isnan(vext[i])) throw Error(TGPU_ERR_NONFINITE, "NaN in the external field");
+    c->h_vext.assign(vext, vext + n);
+    if (c->finalized) ck(cudaMemcpyAsync(c->d_vext, vext, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_zero_density(tgpu_handle h, const signed char *flags)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) throw Error(TGPU_ERR_STATE, "zero-density flags are fixed after tgpu_finalize");
+    if (!flags) throw Error(TGPU_ERR_ARG, "null flags");
+    c->h_zero.assign(flags, flags + (size_t)c->g.ncomp * c->dg.N);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_hard_wall(tgpu_handle h, const int *bnodes, const short *fmask)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) throw Error(TGPU_ERR_STATE, "hard-wall data is fixed after tgpu_finalize");
+    if (!c->g.hard_surf) throw Error(TGPU_ERR_ARG, "geometry has no hard surfaces");
+    if (!bnodes || !fmask) throw Error(TGPU_ERR_ARG, "null hard-wall arrays");
+    const size_t N = c->dg.N;
+    const size_t L = c->g.nlists_hw;
+    c->h_bnodes.assign(bnodes, bnodes + L * N);
+    c->h_fmask.assign(fmask, fmask + L * ((size_t)1 << c->g.ndim) * N);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_finalize(tgpu_handle h)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) return TGPU_OK;
+    const tgpu_geometry &g = c->g;
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      if (c->sten[TGPU_STEN_DELTA][ic].L == 0 || c->sten[TGPU_STEN_THETA][ic].L == 0)
+        throw Error(TGPU_ERR_STATE, "missing delta or theta stencil");
+      if (g.hard_surf && (c->sten[TGPU_STEN_DELTA][ic].hw.empty() || c->sten[TGPU_STEN_THETA][ic].hw.empty()))
+        throw Error(TGPU_ERR_STATE, "hard surfaces need the stencils' corner weights");
+    }
+    if (g.attraction)
+      for (int k = 0; k < g.ncomp * g.ncomp; k++)
+        if (c->sten[TGPU_STEN_UATT][k].L == 0) throw Error(TGPU_ERR_STATE, "missing attraction stencil");
+    if (g.hard_surf && c->h_bnodes.empty()) throw Error(TGPU_ERR_STATE, "hard surfaces need tgpu_set_hard_wall");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    build_device_tables(c);
+    c->finalized = true;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_precision(tgpu_handle h, int precision)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (precision != TGPU_FP64 && precision != TGPU_FP32) throw Error(TGPU_ERR_UNSUPPORTED, "precision");
+    c->precision = precision;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_stream(tgpu_handle h, void *stream)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->own_stream = false;
+    c->stream = static_cast<cudaStream_t>(stream);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_sizes(tgpu_handle h, long *nn, int *nunk, int *ncomp)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (nn) *nn = c->dg.N;
+    if (nunk) *nunk = c->dg.nunk;
+    if (ncomp) *ncomp = c->dg.ncomp;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_fill_device(tgpu_handle h, const double *d_x, double *d_R, int mode)
+{
+  return guard([&] {
+    if (mode != 0 && mode != 1) throw Error(TGPU_ERR_ARG, "mode must be 0 or 1");
+    fill_device(C(h), d_x, d_R, mode);
+    ck(cudaGetLastError(), "fill launch");
+    return TGPU_OK;
+  });
+}
+
+int tgpu_fill(tgpu_handle h, const double *x, double *R, int mode)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    if (mode != 0 && mode != 1) throw Error(TGPU_ERR_ARG, "mode must be 0 or 1");
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_work, x, n);
+    fill_device(c, c->d_work, c->d_work2, mode);
+    d2h(c, R, c->d_work2, n);
+    ck(cudaGetLastError(), "fill launch");
+    return TGPU_OK;
+  });
+}
+
+int tgpu_jv_device(tgpu_handle h, const double *d_v, double *d_out)
+{
+  return guard([&] { jv_device(C(h), d_v, d_out); ck(cudaGetLastError(), "jv"); return TGPU_OK; });
+}
+
+int tgpu_jv(tgpu_handle h, const double *v, double *out)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_work, v, n);
+    jv_device(c, c->d_work, c->d_work2);
+    d2h(c, out, c->d_work2, n);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_schur_apply_device(tgpu_handle h, const double *d_v2, double *d_y2)
+{
+  return guard([&] { schur_device(C(h), d_v2, d_y2); ck(cudaGetLastError(), "schur"); return TGPU_OK; });
+}
+
+int tgpu_schur_apply(tgpu_handle h, const double *v2, double *y2)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    h2d(c, c->d_work, v2, c->n2);
+    schur_device(c, c->d_work, c->d_work2);
+    d2h(c, y2, c->d_work2, c->n2);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_schur_rhs_device(tgpu_handle h, const double *d_b, double *d_b2s)
+{
+  return guard([&] { schur_rhs_device(C(h), d_b, d_b2s); return TGPU_OK; });
+}
+
+int tgpu_schur_x1_device(tgpu_handle h, const double *d_b, const double *d_x2, double *d_x)
+{
+  return guard([&] { schur_x1_device(C(h), d_b, d_x2, d_x); return TGPU_OK; });
+}
+
+int tgpu_solve_device(tgpu_handle h, const double *d_b, double *d_dx, double tol, int maxit, int *iters,
+                      double *relres)
+{
+  return guard([&] {
+    int it = 0;
+    double rr = 0.0;
+    const int st = solve_device(C(h), d_b, d_dx, tol, maxit, &it, &rr);
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return st;
+  });
+}
+
+int tgpu_solve(tgpu_handle h, const double *b, double *dx, double tol, int maxit, int *iters, double *relres)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_work, b, n);
+    int it = 0;
+    double rr = 0.0;
+    const int st = solve_device(c, c->d_work, c->d_work2, tol, maxit, &it, &rr);
+    d2h(c, dx, c->d_work2, n);
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return st;
+  });
+}
+
+int tgpu_newton_device(tgpu_handle h, double *d_x, double rel_tol, double abs_tol, double update_floor, int max_iter,
+                       double lin_tol, int lin_max_iter, int *iters, double *final_resid)
+{
+  return guard([&] {
+    int it = 0;
+    const int st = newton_device(C(h), d_x, rel_tol, abs_tol, update_floor, max_iter, lin_tol, lin_max_iter, &it,
+                                 final_resid);
+    if (iters) *iters = it;
+    return st;
+  });
+}
+
+int tgpu_newton(tgpu_handle h, double *x, double rel_tol, double abs_tol, double update_floor, int max_iter,
+                double lin_tol, int lin_max_iter, int *iters, double *final_resid)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    double *d_xs = dalloc<double>(n);
+    int st = TGPU_OK;
+    try {
+      h2d(c, d_xs, x, n);
+      int it = 0;
+      st = newton_device(c, d_xs, rel_tol, abs_tol, update_floor, max_iter, lin_tol, lin_max_iter, &it, final_resid);
+      if (iters) *iters = it;
+      d2h(c, x, d_xs, n);
+    } catch (...) {
+      dfree(d_xs);
+      throw;
+    }
+    dfree(d_xs);
+    return st;
+  });
+}
+
+int tgpu_get_stats(tgpu_handle h, tgpu_stats *out)
+{
+  return guard([&] { *out = C(h)->stats; return TGPU_OK; });
+}
+
+int tgpu_reset_stats(tgpu_handle h)
+{
+  return guard([&] { std::memset(&C(h)->stats, 0, sizeof(tgpu_stats)); return TGPU_OK; });
+}
+
+int tgpu_jtv_device(tgpu_handle, const double *, double *)
+{
+  g_last_error = "J^T w is not implemented yet";
+  return TGPU_ERR_UNSUPPORTED;
+}
+
+int tgpu_jtv(tgpu_handle, const double *, double *)
+{
+  g_last_error = "J^T w is not implemented yet";
+  return TGPU_ERR_UNSUPPORTED;
+}
+
+}  // extern "C"

@@ -1,0 +1,937 @@
+// Device kernels of the nonlocal-density path (FP64 and FP32 stencil sums,
+// local FMT physics, residual assembly, Schur-operator local steps, Krylov
+// and Newton vector kernels).
+//
+// Reference correspondence (file:line in the reference tree):
+//   k_fmt_local      calc_FMT_derivatives + FMT1/FMT3_1stderiv  src/dft_fill_FMT.c:349-385,
+//                    src/dft_physics_FMT1.c:59-77, src/dft_physics_FMT3.c:61-96
+//   k_pad            offset_to_node_box boundary rules          src/dft_mesh_lib.c:203-297
+//                    constant_boundary                          src/dft_utils.c:90-150
+//   k_conv           the stencil loops of resid_and_Jac_sten_fill_sum_Ncomp
+//                    (src/dft_fill_CLSmf.c:129-169) and load_nonlocal_hs_rosen_rb
+//                    (src/dft_fill_FMT.c:77-133)
+//   k_hw_correct     HW_boundary_weight                         src/dft_utils.c:41-62
+//   k_assemble       load_euler_lagrange / load_rho_bar_s/v / load_mean_field
+//                    src/dft_fill_EL.c:38-196, src/dft_fill_FMT.c:195-347, src/dft_fill_mf.c:38-63
+//   k_schur_local    A11^-1 (src/dft_HardSphereA11_Epetra_Operator.cpp:176-192) and the
+//                    local Hessian that the reference spreads over d2phi_drb2_* per stencil
+//                    point (src/dft_physics_FMT1.c:79-168, src/dft_physics_FMT3.c:101-265)
+//   k_newton_*       update_solution                            src/dft_newton.c:266-381
+#include <cstdio>
+#include <cstdlib>
+
+#include "tgpu_internal.h"
+
+namespace tgpu {
+
+__constant__ DevGeom c_g;
+
+void upload_geom(const DevGeom &g, cudaStream_t s)
+{
+  cudaMemcpyToSymbolAsync(c_g, &g, sizeof(DevGeom), 0, cudaMemcpyHostToDevice, s);
+}
+
+constexpr double kPi = 3.141592653589793238462643383279502884197;
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void node_ijk(long i, int *ijk)
+{
+  ijk[0] = (int)(i % c_g.nx[0]);
+  long r = i / c_g.nx[0];
+  ijk[1] = (int)(r % c_g.nx[1]);
+  ijk[2] = (int)(r / c_g.nx[1]);
+}
+
+__device__ __forceinline__ long pad_center(long i)
+{
+  int ijk[3];
+  node_ijk(i, ijk);
+  return (long)(ijk[0] + c_g.h[0]) + c_g.pstride[1] * (ijk[1] + c_g.h[1]) + c_g.pstride[2] * (ijk[2] + c_g.h[2]);
+}
+
+// ---------------------------------------------------------------------------
+// Padding: resolve each padded position to a source node or a sentinel with
+// the reference's dimension order (the first out-of-range dimension decides).
+template <typename T>
+__global__ void k_pad(const double *__restrict__ src, T *__restrict__ dst, int nch, const double *__restrict__ bulk,
+                      const int *__restrict__ signmask, const int *__restrict__ zcomp,
+                      const signed char *__restrict__ zero)
+{
+  const long NP = c_g.NP;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < NP; p += (long)gridDim.x * blockDim.x) {
+    const int q0 = (int)(p % c_g.P[0]);
+    const long r = p / c_g.P[0];
+    const int q1 = (int)(r % c_g.P[1]);
+    const int q2 = (int)(r / c_g.P[1]);
+    const int q[3] = {q0, q1, q2};
+    int sent = 0, refl = 0;
+    int idx[3] = {0, 0, 0};
+    for (int d = 0; d < c_g.ndim; d++) {
+      const int m = c_g.map[d][q[d]];
+      if (m < 0) { sent = m; break; }
+      if (m & kReflBit) refl |= 1 << d;
+      idx[d] = m & ~kReflBit;
+    }
+    const long node = idx[0] + (long)c_g.nx[0] * (idx[1] + (long)c_g.nx[1] * idx[2]);
+    for (int ch = 0; ch < nch; ch++) {
+      double v;
+      if (sent == kSentBulk) v = bulk[ch];
+      else if (sent == kSentWall) v = 0.0;
+      else if (sent != 0) v = __longlong_as_double(0x7ff8000000000000ULL);
+      else {
+        v = src[(long)ch * c_g.N + node];
+        const int zc = zcomp[ch];
+        if (zc >= 0 && zero[(long)zc * c_g.N + node]) v = 0.0;
+        if (__popc(refl & signmask[ch]) & 1) v = -v;
+      }
+      dst[(long)ch * NP + p] = (T)v;
+    }
+  }
+}
+
+template <typename T>
+void launch_pad(const double *src, T *dst, int nch, const double *bulk, const int *signmask, const int *zcomp,
+                const signed char *zero, bool, cudaStream_t s)
+{
+  // bulk/signmask/zcomp live in device memory (small arrays set up by the caller)
+  k_pad<T><<<1184, kThreads, 0, s>>>(src, dst, nch, bulk, signmask, zcomp, zero);
+}
+template void launch_pad<double>(const double *, double *, int, const double *, const int *, const int *,
+                                 const signed char *, bool, cudaStream_t);
+template void launch_pad<float>(const double *, float *, int, const double *, const int *, const int *,
+                                const signed char *, bool, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Stencil sums.  One thread per output node; the stencil's linear offsets and
+// coefficient rows stream through shared memory in chunks that every thread
+// of the block reads in the same order (broadcast), the inputs are gathered
+// from the padded box (neighbouring threads read neighbouring addresses).
+struct OutPtrs {
+  double *p[kMaxRb];
+};
+
+constexpr int kChunk = 256;
+
+template <typename T, typename Acc, int NIN, int NOUT>
+__global__ void __launch_bounds__(kThreads) k_conv(const T *__restrict__ in, long cstride,
+                                                    const int *__restrict__ loff, const T *__restrict__ coef, int L,
+                                                    OutPtrs out, int accumulate)
+{
+  __shared__ int s_off[kChunk];
+  __shared__ T s_coef[kChunk * NIN * NOUT];
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool active = i < c_g.N;
+  const long ip = active ? pad_center(i) : 0;
+  Acc acc[NOUT];
+#pragma unroll
+  for (int o = 0; o < NOUT; o++) acc[o] = 0;
+  for (int k0 = 0; k0 < L; k0 += kChunk) {
+    const int n = min(kChunk, L - k0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s_off[t] = loff[k0 + t];
+    for (int t = threadIdx.x; t < n * NIN * NOUT; t += blockDim.x) s_coef[t] = coef[(long)k0 * NIN * NOUT + t];
+    __syncthreads();
+    if (active) {
+      for (int k = 0; k < n; k++) {
+        const long j = ip + s_off[k];
+        T v[NIN];
+#pragma unroll
+        for (int c = 0; c < NIN; c++) v[c] = __ldg(in + c * cstride + j);
+#pragma unroll
+        for (int o = 0; o < NOUT; o++)
+#pragma unroll
+          for (int c = 0; c < NIN; c++) acc[o] = fma((Acc)s_coef[(k * NOUT + o) * NIN + c], (Acc)v[c], acc[o]);
+      }
+    }
+  }
+  if (active) {
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) {
+      double *dst = out.p[o];
+      if (accumulate) dst[i] += (double)acc[o];
+      else dst[i] = (double)acc[o];
+    }
+  }
+}
+
+template <typename T, typename Acc, int NIN, int NOUT>
+static void conv_dispatch(const T *in, long cstride, const int *loff, const T *coef, int L, const OutPtrs &out,
+                          bool acc, cudaStream_t s, long N)
+{
+  const int grid = (int)((N + kThreads - 1) / kThreads);
+  k_conv<T, Acc, NIN, NOUT><<<grid, kThreads, 0, s>>>(in, cstride, loff, coef, L, out, acc ? 1 : 0);
+}
+
+// Coefficient rows: `coef` is the table for the shape (nin, nout) this call uses.
+template <>
+void launch_conv<double>(const double *in, long cstride, int nin, const int *loff, const double *coef, int L,
+                         double *const *out, int nout, bool acc, long N, cudaStream_t s)
+{
+  OutPtrs o{};
+  for (int k = 0; k < nout; k++) o.p[k] = out[k];
+#define TGPU_CONV(NI, NO) \
+  if (nin == NI && nout == NO) { conv_dispatch<double, double, NI, NO>(in, cstride, loff, coef, L, o, acc, s, N); return; }
+  TGPU_CONV(1, 1) TGPU_CONV(1, 2) TGPU_CONV(1, 3) TGPU_CONV(1, 4) TGPU_CONV(1, 5) TGPU_CONV(1, 6) TGPU_CONV(1, 7)
+  TGPU_CONV(1, 8) TGPU_CONV(1, 9) TGPU_CONV(2, 1) TGPU_CONV(3, 1) TGPU_CONV(4, 1)
+#undef TGPU_CONV
+  fprintf(stderr, "tgpu: no FP64 convolution for nin=%d nout=%d\n", nin, nout);
+  abort();
+}
+
+template <>
+void launch_conv<float>(const float *in, long cstride, int nin, const int *loff, const float *coef, int L,
+                        double *const *out, int nout, bool acc, long N, cudaStream_t s)
+{
+  OutPtrs o{};
+  for (int k = 0; k < nout; k++) o.p[k] = out[k];
+#define TGPU_CONV(NI, NO) \
+  if (nin == NI && nout == NO) { conv_dispatch<float, float, NI, NO>(in, cstride, loff, coef, L, o, acc, s, N); return; }
+  TGPU_CONV(1, 1) TGPU_CONV(1, 2) TGPU_CONV(1, 3) TGPU_CONV(1, 4) TGPU_CONV(1, 5) TGPU_CONV(1, 6) TGPU_CONV(1, 7)
+  TGPU_CONV(1, 8) TGPU_CONV(1, 9) TGPU_CONV(2, 1) TGPU_CONV(3, 1) TGPU_CONV(4, 1)
+#undef TGPU_CONV
+  fprintf(stderr, "tgpu: no FP32 convolution for nin=%d nout=%d\n", nin, nout);
+  abort();
+}
+
+// ---------------------------------------------------------------------------
+// FMT physics at one node.  n is in the reference's n ordering
+// (n0, n1, n2, n3, V1[d], V2[d]); sv is the solution-vector ordering
+// (n3, n2, n1, n0, V2[d], V1[d]) (solutionVec_to_nOrdering, src/dft_utils.c:205-221).
+__device__ __forceinline__ void load_n(const double *__restrict__ x, long i, double *n)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  const double *rb = x + (long)c_g.first_rb * N;
+  n[0] = rb[3 * N + i];
+  n[1] = rb[2 * N + i];
+  n[2] = rb[1 * N + i];
+  n[3] = rb[i];
+  for (int d = 0; d < nd; d++) {
+    n[4 + d] = rb[(4 + nd + d) * N + i];
+    n[4 + nd + d] = rb[(4 + d) * N + i];
+  }
+}
+
+// dPhi/dn (FMT1: Rosenfeld, FMT3: White-Bear), with the reference's n3 guard for FMT3.
+__device__ void fmt_dphi(const double *n, double *dphi)
+{
+  const int nd = c_g.ndim;
+  double dot22 = 0.0, dot12 = 0.0;
+  for (int d = 0; d < nd; d++) {
+    dot22 += n[4 + nd + d] * n[4 + nd + d];
+    dot12 += n[4 + d] * n[4 + nd + d];
+  }
+  const double one_m = 1.0 - n[3];
+  const double a = 1.0 / one_m, a2 = a * a, a3 = a2 * a;
+  dphi[0] = log(a);
+  dphi[1] = n[2] * a;
+  if (c_g.functional == TGPU_FMT3) {
+    const double t = n[3];
+    if (t > 1.e-10) {
+      const double lg = log(one_m);
+      const double F = t + one_m * one_m * lg;            // n3 + (1-n3)^2 ln(1-n3)
+      const double F1 = t - 2.0 * one_m * lg;             // dF/dn3
+      const double f = F * a2 / (36.0 * kPi * t * t);     // Phi_3 = (n2^3 - 3 n2 V2.V2) f(n3)
+      const double G1 = 2.0 * (-a2 / (t * t * t) + a3 / (t * t));
+      const double f1 = (F1 * a2 / (t * t) + F * G1) / (36.0 * kPi);
+      const double g = n[2] * n[2] * n[2] - 3.0 * n[2] * dot22;
+      dphi[2] = n[1] * a + 3.0 * (n[2] * n[2] - dot22) * f;
+      dphi[3] = n[0] * a + (n[1] * n[2] - dot12) * a2 + g * f1;
+      for (int d = 0; d < nd; d++) {
+        dphi[4 + d] = -n[4 + nd + d] * a;
+        dphi[4 + nd + d] = -n[4 + d] * a - 6.0 * n[2] * n[4 + nd + d] * f;
+      }
+    } else {
+      dphi[2] = 0.0;
+      dphi[3] = 0.0;
+      for (int d = 0; d < nd; d++) {
+        dphi[4 + d] = -n[4 + nd + d] * a;
+        dphi[4 + nd + d] = 0.0;
+      }
+    }
+  } else {
+    dphi[2] = n[1] * a + (n[2] * n[2] - dot22) * a2 / (8.0 * kPi);
+    dphi[3] = n[0] * a + (n[1] * n[2] - dot12) * a2 + (n[2] * n[2] * n[2] - 3. * n[2] * dot22) * a3 / (12.0 * kPi);
+    for (int d = 0; d < nd; d++) {
+      dphi[4 + d] = -n[4 + nd + d] * a;
+      dphi[4 + nd + d] = -n[4 + d] * a - n[2] * n[4 + nd + d] * a2 / (4.0 * kPi);
+    }
+  }
+}
+
+// z = H(n) y with H the Hessian of Phi in n ordering.  Derived from the free
+// energy density; it reproduces the reference's per-stencil-point second
+// derivatives (d2phi_drb2_delta_rb / _theta_rb) as c(offset)^T H and H row n3.
+__device__ void fmt_hess_apply(const double *n, const double *y, double *z)
+{
+  const int nd = c_g.ndim;
+  double Q = 0.0, Pd = 0.0;
+  for (int d = 0; d < nd; d++) {
+    Q += n[4 + nd + d] * n[4 + nd + d];
+    Pd += n[4 + d] * n[4 + nd + d];
+  }
+  const double one_m = 1.0 - n[3];
+  const double a = 1.0 / one_m, a2 = a * a, a3 = a2 * a, a4 = a3 * a;
+  double h22, h23, h2v2, h33, h3v2n2, v2v2;  // entries that differ between functionals
+  if (c_g.functional == TGPU_FMT3) {
+    const double t = n[3];
+    if (!(t > 1.e-10)) {
+      for (int k = 0; k < 4 + 2 * nd; k++) z[k] = 0.0;
+      return;
+    }
+    const double lg = log(one_m);
+    const double F = t + one_m * one_m * lg, F1 = t - 2.0 * one_m * lg, F2 = 3.0 + 2.0 * lg;
+    const double t2 = t * t, t3 = t2 * t, t4 = t3 * t;
+    const double G = a2 / t2, G1 = 2.0 * (-a2 / t3 + a3 / t2), G2 = 6.0 * a2 / t4 - 8.0 * a3 / t3 + 6.0 * a4 / t2;
+    const double f = F * G / (36.0 * kPi);
+    const double f1 = (F1 * G + F * G1) / (36.0 * kPi);
+    const double f2 = (F2 * G + 2.0 * F1 * G1 + F * G2) / (36.0 * kPi);
+    const double g = n[2] * n[2] * n[2] - 3.0 * n[2] * Q;
+    h22 = 6.0 * n[2] * f;
+    h23 = n[1] * a2 + 3.0 * (n[2] * n[2] - Q) * f1;
+    h2v2 = -6.0 * f;                 // times V2d
+    h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + g * f2;
+    h3v2n2 = -6.0 * n[2] * f1;       // times V2d, plus -V1d a2
+    v2v2 = -6.0 * n[2] * f;
+  } else {
+    const double i4p = 1.0 / (4.0 * kPi);
+    h22 = n[2] * a2 * i4p;
+    h23 = n[1] * a2 + (n[2] * n[2] - Q) * a3 * i4p;
+    h2v2 = -a2 * i4p;
+    h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + (n[2] * n[2] * n[2] - 3.0 * n[2] * Q) * a4 * i4p;
+    h3v2n2 = -n[2] * a3 / (2.0 * kPi);
+    v2v2 = -n[2] * a2 * i4p;
+  }
+  const double h03 = a, h12 = a, h13 = n[2] * a2;
+  double s2 = 0.0, s3 = 0.0;
+  for (int d = 0; d < nd; d++) {
+    const double V1 = n[4 + d], V2 = n[4 + nd + d];
+    const double yV1 = y[4 + d], yV2 = y[4 + nd + d];
+    s2 += h2v2 * V2 * yV2;
+    s3 += -V2 * a2 * yV1 + (-V1 * a2 + h3v2n2 * V2) * yV2;
+    z[4 + d] = -V2 * a2 * y[3] - a * yV2;
+    z[4 + nd + d] = h2v2 * V2 * y[2] + (-V1 * a2 + h3v2n2 * V2) * y[3] - a * yV1 + v2v2 * yV2;
+  }
+  z[0] = h03 * y[3];
+  z[1] = h12 * y[2] + h13 * y[3];
+  z[2] = h12 * y[1] + h22 * y[2] + h23 * y[3] + s2;
+  z[3] = h03 * y[0] + h13 * y[1] + h23 * y[2] + h33 * y[3] + s3;
+}
+
+// Transpose-convolution channels from a weighted-density-shaped vector q (n ordering):
+// per component A = fac (q0/4piR^2 + q1/4piR + q2), B_d = fac (q_V1d/4piR + q_V2d), C = fac q3.
+__device__ __forceinline__ void write_tr_channels(const double *q, double *chan, long i)
+{
+  const int nd = c_g.ndim;
+  const long N = c_g.N;
+  for (int ic = 0; ic < c_g.ncomp; ic++) {
+    const double f = c_g.fac[ic];
+    const long base = (long)ic * (nd + 2);
+    chan[base * N + i] = f * (q[0] * c_g.inv_4pirsq[ic] + q[1] * c_g.inv_4pir[ic] + q[2]);
+    for (int d = 0; d < nd; d++) chan[(base + 1 + d) * N + i] = f * (q[4 + d] * c_g.inv_4pir[ic] + q[4 + nd + d]);
+    chan[(base + nd + 1) * N + i] = f * q[3];
+  }
+}
+
+__global__ void k_fmt_local(const double *__restrict__ x, double *__restrict__ chan)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < c_g.N; i += (long)gridDim.x * blockDim.x) {
+    double n[kMaxRb], dphi[kMaxRb];
+    load_n(x, i, n);
+    fmt_dphi(n, dphi);
+    write_tr_channels(dphi, chan, i);
+  }
+}
+
+void launch_fmt_local(const double *x, double *chan, cudaStream_t s)
+{
+  k_fmt_local<<<1184, kThreads, 0, s>>>(x, chan);
+}
+
+__device__ __forceinline__ bool zero_row(const double *vext, const signed char *zero, int ic, long i)
+{
+  const long k = (long)ic * c_g.N + i;
+  return zero[k] || vext[k] == c_g.vext_max;
+}
+
+// dependent weighted densities (one particle size): n1 = n2/4piR, n0 = n2/4piR^2, V1 = V2/4piR
+__device__ __forceinline__ bool dep_rb(int k, int *src, double *c)
+{
+  const int nd = c_g.ndim;
+  if (!c_g.single_size) return false;
+  if (k == 2) { *src = 1; *c = c_g.inv_4pir[0]; return true; }
+  if (k == 3) { *src = 1; *c = c_g.inv_4pirsq[0]; return true; }
+  if (k >= 4 + nd) { *src = 4 + (k - 4 - nd); *c = c_g.inv_4pir[0]; return true; }
+  return false;
+}
+
+__global__ void k_assemble(const double *__restrict__ x, const double *__restrict__ vext,
+                           const signed char *__restrict__ zero, const double *__restrict__ conv,
+                           const double *__restrict__ tr, double *__restrict__ R)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const int iu = c_g.first_rho + ic;
+      const double xi = x[(long)iu * N + i];
+      double r;
+      if (zero_row(vext, zero, ic, i)) {
+        r = xi;
+      } else {
+        double mu = -log(c_g.rho_b[ic]) - c_g.betamu_hs_ex[ic];
+        if (c_g.attraction) mu -= c_g.betamu_att[ic];
+        r = log(xi) + mu + vext[(long)ic * N + i] + tr[(long)ic * N + i];
+        if (c_g.attraction) r += x[(long)(c_g.first_mf + ic) * N + i];
+      }
+      R[(long)iu * N + i] = r;
+    }
+    for (int k = 0; k < c_g.nrb; k++) {
+      const int iu = c_g.first_rb + k;
+      int src;
+      double c;
+      double r = -x[(long)iu * N + i];
+      if (dep_rb(k, &src, &c)) r += x[(long)(c_g.first_rb + src) * N + i] * c;
+      else r += conv[(long)k * N + i];
+      R[(long)iu * N + i] = r;
+    }
+    if (c_g.attraction)
+      for (int ic = 0; ic < c_g.ncomp; ic++) {
+        const int iu = c_g.first_mf + ic;
+        R[(long)iu * N + i] = -x[(long)iu * N + i] + conv[(long)(c_g.nrb + ic) * N + i];
+      }
+  }
+}
+
+void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
+                     const double *tr, double *R, cudaStream_t s)
+{
+  k_assemble<<<1184, kThreads, 0, s>>>(x, vext, zero, conv, tr, R);
+}
+
+// Schur local step: y1 = A11^-1 u (u = A12 v in conv), then the EL-side
+// channels of H y1 for the transpose sums; y_MF = -u_MF kept for A21.
+__global__ void k_schur_local(const double *__restrict__ x, const double *__restrict__ conv,
+                              double *__restrict__ chan, double *__restrict__ ymf)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double ysv[kMaxRb], y[kMaxRb], n[kMaxRb], z[kMaxRb];
+    for (int k = 0; k < c_g.nrb; k++) {
+      int src;
+      double c;
+      if (dep_rb(k, &src, &c)) ysv[k] = -c * conv[(long)src * N + i];   // -u_dep - B u_ind, u_dep = 0
+      else ysv[k] = -conv[(long)k * N + i];
+    }
+    y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
+    for (int d = 0; d < nd; d++) { y[4 + d] = ysv[4 + nd + d]; y[4 + nd + d] = ysv[4 + d]; }
+    load_n(x, i, n);
+    fmt_hess_apply(n, y, z);
+    write_tr_channels(z, chan, i);
+    if (c_g.attraction)
+      for (int ic = 0; ic < c_g.ncomp; ic++) ymf[(long)ic * N + i] = -conv[(long)(c_g.nrb + ic) * N + i];
+  }
+}
+
+void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, cudaStream_t s)
+{
+  k_schur_local<<<1184, kThreads, 0, s>>>(x, conv, chan, ymf);
+}
+
+// J v local step: channels of H v_rb for the EL rows.
+__global__ void k_jv_local(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ chan)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double y[kMaxRb], n[kMaxRb], z[kMaxRb];
+    load_n(v, i, y);
+    (void)nd;
+    load_n(x, i, n);
+    fmt_hess_apply(n, y, z);
+    write_tr_channels(z, chan, i);
+  }
+}
+
+void launch_jv_local(const double *x, const double *v, double *chan, cudaStream_t s)
+{
+  k_jv_local<<<1184, kThreads, 0, s>>>(x, v, chan);
+}
+
+__global__ void k_schur_combine(const double *__restrict__ x, const double *__restrict__ vext,
+                                const signed char *__restrict__ zero, const double *__restrict__ v2,
+                                const double *__restrict__ tr, const double *__restrict__ ymf, double *__restrict__ y2)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long k = (long)ic * N + i;
+      if (zero_row(vext, zero, ic, i)) {
+        y2[k] = v2[k];
+      } else {
+        double a21y = tr[k];
+        if (c_g.attraction) a21y += ymf[k];
+        y2[k] = v2[k] / x[(long)(c_g.first_rho + ic) * N + i] - a21y;
+      }
+    }
+}
+
+void launch_schur_combine(const double *x, const double *vext, const signed char *zero, const double *v2,
+                          const double *tr, const double *ymf, double *y2, cudaStream_t s)
+{
+  k_schur_combine<<<1184, kThreads, 0, s>>>(x, vext, zero, v2, tr, ymf, y2);
+}
+
+__global__ void k_jv_combine(const double *__restrict__ x, const double *__restrict__ vext,
+                             const signed char *__restrict__ zero, const double *__restrict__ v,
+                             const double *__restrict__ conv, const double *__restrict__ tr, double *__restrict__ out)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const int iu = c_g.first_rho + ic;
+      const long k = (long)iu * N + i;
+      if (zero_row(vext, zero, ic, i)) {
+        out[k] = v[k];
+      } else {
+        double r = v[k] / x[k] + tr[(long)ic * N + i];
+        if (c_g.attraction) r += v[(long)(c_g.first_mf + ic) * N + i];
+        out[k] = r;
+      }
+    }
+    for (int kk = 0; kk < c_g.nrb; kk++) {
+      const int iu = c_g.first_rb + kk;
+      int src;
+      double c;
+      double r = -v[(long)iu * N + i];
+      if (dep_rb(kk, &src, &c)) r += v[(long)(c_g.first_rb + src) * N + i] * c;
+      else r += conv[(long)kk * N + i];
+      out[(long)iu * N + i] = r;
+    }
+    if (c_g.attraction)
+      for (int ic = 0; ic < c_g.ncomp; ic++) {
+        const int iu = c_g.first_mf + ic;
+        out[(long)iu * N + i] = -v[(long)iu * N + i] + conv[(long)(c_g.nrb + ic) * N + i];
+      }
+  }
+}
+
+void launch_jv_combine(const double *x, const double *vext, const signed char *zero, const double *v,
+                       const double *conv, const double *tr, double *out, cudaStream_t s)
+{
+  k_jv_combine<<<1184, kThreads, 0, s>>>(x, vext, zero, v, conv, tr, out);
+}
+
+// Schur right-hand side: y1 = A11^-1 b1 from the block-1 part of a full
+// vector b, then the channels of H y1 (ComputeRHS, src/dft_Schur_Epetra_Operator.cpp:121-133).
+__global__ void k_rhs_local(const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ chan,
+                            double *__restrict__ ymf)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double ysv[kMaxRb], y[kMaxRb], n[kMaxRb], z[kMaxRb];
+    const double *brb = b + (long)c_g.first_rb * N;
+    for (int k = 0; k < c_g.nrb; k++) {
+      int src;
+      double c;
+      if (dep_rb(k, &src, &c)) ysv[k] = -brb[(long)k * N + i] - c * brb[(long)src * N + i];
+      else ysv[k] = -brb[(long)k * N + i];
+    }
+    y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
+    for (int d = 0; d < nd; d++) { y[4 + d] = ysv[4 + nd + d]; y[4 + nd + d] = ysv[4 + d]; }
+    load_n(x, i, n);
+    fmt_hess_apply(n, y, z);
+    write_tr_channels(z, chan, i);
+    if (c_g.attraction)
+      for (int ic = 0; ic < c_g.ncomp; ic++) ymf[(long)ic * N + i] = -b[(long)(c_g.first_mf + ic) * N + i];
+  }
+}
+
+void launch_rhs_local(const double *x, const double *b, double *chan, double *ymf, cudaStream_t s)
+{
+  k_rhs_local<<<1184, kThreads, 0, s>>>(x, b, chan, ymf);
+}
+
+__global__ void k_rhs_combine(const double *__restrict__ vext, const signed char *__restrict__ zero,
+                              const double *__restrict__ b, const double *__restrict__ tr,
+                              const double *__restrict__ ymf, double *__restrict__ b2s)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long k = (long)ic * N + i;
+      const double bi = b[(long)(c_g.first_rho + ic) * N + i];
+      if (zero_row(vext, zero, ic, i)) {
+        b2s[k] = bi;
+      } else {
+        double a21y = tr[k];
+        if (c_g.attraction) a21y += ymf[k];
+        b2s[k] = bi - a21y;
+      }
+    }
+}
+
+void launch_rhs_combine(const double *vext, const signed char *zero, const double *b, const double *tr,
+                        const double *ymf, double *b2s, cudaStream_t s)
+{
+  k_rhs_combine<<<1184, kThreads, 0, s>>>(vext, zero, b, tr, ymf, b2s);
+}
+
+// Back substitution x1 = A11^-1 (b1 - A12 x2) (ComputeX1, src/dft_Schur_Epetra_Operator.cpp:135-147);
+// writes the full Newton step dx = [x1; x2].
+__global__ void k_x1(const double *__restrict__ b, const double *__restrict__ conv, const double *__restrict__ x2,
+                     double *__restrict__ dx)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double y[kMaxRb];
+    const double *brb = b + (long)c_g.first_rb * N;
+    for (int k = 0; k < c_g.nrb; k++) {
+      int src;
+      double c;
+      y[k] = dep_rb(k, &src, &c) ? brb[(long)k * N + i] : brb[(long)k * N + i] - conv[(long)k * N + i];
+    }
+    for (int k = 0; k < c_g.nrb; k++) {
+      int src;
+      double c;
+      double v = dep_rb(k, &src, &c) ? (-y[k] - c * y[src]) : -y[k];
+      dx[(long)(c_g.first_rb + k) * N + i] = v;
+    }
+    for (int ic = 0; ic < c_g.ncomp; ic++) dx[(long)(c_g.first_rho + ic) * N + i] = x2[(long)ic * N + i];
+    if (c_g.attraction)
+      for (int ic = 0; ic < c_g.ncomp; ic++) {
+        const long k = (long)(c_g.first_mf + ic) * N + i;
+        dx[k] = -(b[k] - conv[(long)(c_g.nrb + ic) * N + i]);
+      }
+  }
+}
+
+void launch_x1(const double *b, const double *conv, const double *x2, double *dx, cudaStream_t s)
+{
+  k_x1<<<1184, kThreads, 0, s>>>(b, conv, x2, dx);
+}
+
+// ---------------------------------------------------------------------------
+// Hard-wall boundary weights: for target nodes whose stencils reach a
+// boundary node, replace w by the fluid-element part of the point's corner
+// weights (HW_boundary_weight) for the weighted-density and mean-field sums.
+__device__ long map_offset(const int *ijk, const short *off, int *refl)
+{
+  int idx[3] = {0, 0, 0};
+  *refl = 0;
+  for (int d = 0; d < c_g.ndim; d++) {
+    const int q = ijk[d] + c_g.h[d] + off[d];
+    const int m = c_g.map[d][q];
+    if (m < 0) return m;
+    if (m & kReflBit) *refl |= 1 << d;
+    idx[d] = m & ~kReflBit;
+  }
+  return idx[0] + (long)c_g.nx[0] * (idx[1] + (long)c_g.nx[1] * idx[2]);
+}
+
+struct HwStencil {
+  int L;
+  const short *off;
+  const double *w, *hw;
+};
+
+__device__ void hw_apply(const HwStencil &st, int kind, int jc, int jlist, const int *ijk, const double *field,
+                         long fcs, int ffirst, const signed char *zero, const int *bnodes, const short *fmask,
+                         double *acc)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  const int nel = 1 << nd;
+  for (int s = 0; s < st.L; s++) {
+    int refl;
+    const short *o = st.off + (long)s * 3;
+    const long jn = map_offset(ijk, o, &refl);
+    if (jn < 0) continue;
+    if (bnodes[(long)jlist * N + jn] == -1) continue;
+    if (zero[(long)jc * N + jn]) continue;
+    const int mask = fmask[((long)jlist * nel + refl) * N + jn];
+    double w = 0.0;
+    for (int l = 0; l < nel; l++)
+      if (mask & (1 << l)) w += st.hw[(long)s * nel + l];
+    const double dw = w - st.w[s];
+    const double rho = field[(long)(ffirst + jc) * fcs + jn];
+    const double f = c_g.fac[jc];
+    if (kind == 0) {          // theta -> n3
+      acc[0] += f * dw * rho;
+    } else if (kind == 1) {   // delta -> n2, n1, n0, V2, V1
+      acc[1] += f * dw * rho;
+      if (!c_g.single_size) {
+        acc[2] += f * c_g.inv_4pir[jc] * dw * rho;
+        acc[3] += f * c_g.inv_4pirsq[jc] * dw * rho;
+      }
+      for (int d = 0; d < nd; d++) {
+        const double v = (double)o[d] * c_g.esize[d] * c_g.inv_rad[jc];
+        acc[4 + d] += f * v * dw * rho;
+        if (!c_g.single_size) acc[4 + nd + d] += f * c_g.inv_4pir[jc] * v * dw * rho;
+      }
+    }
+  }
+}
+
+__global__ void k_hw_correct(const double *__restrict__ field, long fcs, int ffirst, HwStencil th0, HwStencil th1,
+                             HwStencil de0, HwStencil de1, const int *__restrict__ targets, int ntargets,
+                             const signed char *__restrict__ zero, const int *__restrict__ bnodes,
+                             const short *__restrict__ fmask, double *__restrict__ conv)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntargets) return;
+  const long i = targets[t];
+  int ijk[3];
+  node_ijk(i, ijk);
+  double acc[kMaxRb];
+  for (int k = 0; k < kMaxRb; k++) acc[k] = 0.0;
+  for (int jc = 0; jc < c_g.ncomp && jc < 2; jc++) {
+    const int jlist = (c_g.nlists <= 2) ? 0 : jc;
+    hw_apply(jc == 0 ? th0 : th1, 0, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
+    hw_apply(jc == 0 ? de0 : de1, 1, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
+  }
+  for (int k = 0; k < c_g.nrb; k++) conv[(long)k * c_g.N + i] += acc[k];
+}
+
+void launch_hw_correct(const double *field, long fcs, int ffirst, const DevStencil *theta, const DevStencil *delta,
+                       const DevStencil *uatt, const int *targets, int ntargets, const signed char *zero,
+                       const int *bnodes, const short *fmask, double *conv, cudaStream_t s)
+{
+  (void)uatt;  // mean-field stencils with hard walls: see the host-side guard
+  if (ntargets <= 0) return;
+  HwStencil th[2] = {}, de[2] = {};
+  for (int c = 0; c < 2; c++) {
+    if (theta[c].L) th[c] = {theta[c].L, theta[c].d_off, theta[c].d_w, theta[c].d_hw};
+    if (delta[c].L) de[c] = {delta[c].L, delta[c].d_off, delta[c].d_w, delta[c].d_hw};
+  }
+  k_hw_correct<<<(ntargets + 127) / 128, 128, 0, s>>>(field, fcs, ffirst, th[0], th[1], de[0], de[1], targets,
+                                                       ntargets, zero, bnodes, fmask, conv);
+}
+
+// ---------------------------------------------------------------------------
+// Krylov and Newton vector kernels.  Reductions are two-level and ordered
+// (per-block partials, then one block in fixed order): results do not depend
+// on scheduling, so runs repeat bit for bit.
+int reduce_blocks(long n)
+{
+  long b = (n + kThreads * 4 - 1) / (kThreads * 4);
+  if (b > 1024) b = 1024;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  v = 0.0;
+  if (wid == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
+__device__ __forceinline__ double block_min(double v, double *sh)
+{
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  v = 1.0e300;
+  if (wid == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 1.0e300;
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  }
+  __syncthreads();
+  return v;
+}
+
+// partial[j*nb + b] = sum over block b's chunk of V[j] . w
+__global__ void k_multidot(const double *__restrict__ V, long ldv, int nvec, const double *__restrict__ w, long n,
+                           double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  const long chunk = (n + gridDim.x - 1) / gridDim.x;
+  const long b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  for (int j = 0; j < nvec; j++) {
+    double s = 0.0;
+    for (long i = b0 + threadIdx.x; i < b1; i += blockDim.x) s = fma(V[(long)j * ldv + i], w[i], s);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) partial[(long)j * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+__global__ void k_reduce_rows(const double *__restrict__ partial, int nb, int nrow, double *__restrict__ out)
+{
+  __shared__ double sh[32];
+  for (int j = 0; j < nrow; j++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[(long)j * nb + b];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[j] = s;
+  }
+}
+
+void launch_multidot(const double *V, long ldv, int nvec, const double *w, long n, double *partial, int nblocks,
+                     double *result, cudaStream_t s)
+{
+  k_multidot<<<nblocks, kThreads, 0, s>>>(V, ldv, nvec, w, n, partial);
+  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, nvec, result);
+}
+
+__global__ void k_multiaxpy(double *__restrict__ w, const double *__restrict__ V, long ldv, int nvec,
+                            const double *__restrict__ coef, long n)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double s = w[i];
+    for (int j = 0; j < nvec; j++) s -= coef[j] * V[(long)j * ldv + i];
+    w[i] = s;
+  }
+}
+
+void launch_multiaxpy(double *w, const double *V, long ldv, int nvec, const double *coef, long n, cudaStream_t s)
+{
+  k_multiaxpy<<<1184, kThreads, 0, s>>>(w, V, ldv, nvec, coef, n);
+}
+
+__global__ void k_scale(double *__restrict__ y, const double *__restrict__ x, double a, long n)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] = a * x[i];
+}
+
+void launch_scale(double *y, const double *x, double a, long n, cudaStream_t s)
+{
+  k_scale<<<1184, kThreads, 0, s>>>(y, x, a, n);
+}
+
+__global__ void k_axpby(double *__restrict__ y, double a, const double *__restrict__ x, double b, long n)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+void launch_axpby(double *y, double a, const double *x, double b, long n, cudaStream_t s)
+{
+  k_axpby<<<1184, kThreads, 0, s>>>(y, a, x, b, n);
+}
+
+// A22^-1: A22 is diagonal, 1/rho on Euler-Lagrange rows and 1 on zero-density rows.
+__global__ void k_precond(const double *__restrict__ x, const double *__restrict__ vext,
+                          const signed char *__restrict__ zero, const double *__restrict__ in, double *__restrict__ out)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long k = (long)ic * N + i;
+      out[k] = zero_row(vext, zero, ic, i) ? in[k] : in[k] * x[(long)(c_g.first_rho + ic) * N + i];
+    }
+}
+
+void launch_precond(const double *x, const double *vext, const signed char *zero, const double *in, double *out,
+                    cudaStream_t s)
+{
+  k_precond<<<1184, kThreads, 0, s>>>(x, vext, zero, in, out);
+}
+
+__global__ void k_newton_frac(const double *__restrict__ x, const double *__restrict__ dx, double floor_frac,
+                              double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  const long N = c_g.N;
+  double m = 1.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long k = (long)(c_g.first_rho + ic) * N + i;
+      if (x[k] + dx[k] < 0.0) {
+        double f = fmin(1.0, x[k] / (-dx[k]));
+        f = fmax(f, floor_frac);
+        m = fmin(m, f);
+      }
+    }
+  m = block_min(m, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = m;
+}
+
+__global__ void k_min_final(const double *__restrict__ partial, int nb, double *__restrict__ out)
+{
+  __shared__ double sh[32];
+  double m = 1.0e300;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) m = fmin(m, partial[b]);
+  m = block_min(m, sh);
+  if (threadIdx.x == 0) out[0] = m;
+}
+
+void launch_newton_frac(const double *x, const double *dx, double floor_frac, double *partial, int nblocks,
+                        double *result, cudaStream_t s)
+{
+  k_newton_frac<<<nblocks, kThreads, 0, s>>>(x, dx, floor_frac, partial);
+  k_min_final<<<1, kThreads, 0, s>>>(partial, nblocks, result);
+}
+
+__global__ void k_newton_update(double *__restrict__ x, const double *__restrict__ dx, double frac, double rel,
+                                double abs_tol, double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  const long N = c_g.N;
+  double s = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int iu = 0; iu < c_g.nunk; iu++) {
+      const long k = (long)iu * N + i;
+      const double xo = x[k], d = dx[k];
+      const double t = (frac * d) / (rel * xo + abs_tol);
+      s = fma(t, t, s);
+      const bool is_rho = iu >= c_g.first_rho && iu < c_g.first_rho + c_g.ncomp;
+      if (is_rho && xo + frac * d < 1.e-99) x[k] = 0.1 * xo;
+      else if (iu == c_g.first_rb && xo + frac * d > 1.0) x[k] = xo + 0.5 * (1.0 - xo);
+      else x[k] = xo + frac * d;
+    }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+void launch_newton_update(double *x, const double *dx, double frac, double rel, double abs_tol, double *partial,
+                          int nblocks, double *result, cudaStream_t s)
+{
+  k_newton_update<<<nblocks, kThreads, 0, s>>>(x, dx, frac, rel, abs_tol, partial);
+  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
+}
+
+__global__ void k_norm2(const double *__restrict__ x, long n, double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    s = fma(x[i], x[i], s);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+void launch_norm2(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s)
+{
+  k_norm2<<<nblocks, kThreads, 0, s>>>(x, n, partial);
+  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
+}
+
+// counts non-finite entries (result = count as double)
+__global__ void k_count_nonfinite(const double *__restrict__ x, long n, double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    if (!isfinite(x[i])) s += 1.0;
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+void launch_check_finite(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s)
+{
+  k_count_nonfinite<<<nblocks, kThreads, 0, s>>>(x, n, partial);
+  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
+}
+
+}  // namespace tgpu

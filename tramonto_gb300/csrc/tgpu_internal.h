@@ -1,0 +1,151 @@
+// Internal declarations of the GB300 nonlocal-density path.
+//
+// Data layout in HBM (all SoA, node = ix + nx*(iy + ny*iz)):
+//   - state x, residual R, Krylov vectors: double [unknown][node]
+//   - padded channels: the convolution inputs are copied once per pass into a
+//     box padded by the largest stencil reach h[d] in every dimension; the
+//     copy resolves the reference's boundary rules (src/dft_mesh_lib.c:203-297:
+//     bulk and in-wall sentinels, periodic wrap, mirror with vector-sign flip)
+//     so the stencil sums that follow are branch-free loads at
+//     (padded centre + precomputed linear offset).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tramonto_gpu.h"
+
+namespace tgpu {
+
+constexpr int kMaxC = TGPU_MAXC;
+constexpr int kMaxRb = 10;            // 4 + 2*3 weighted densities
+constexpr int kSentBulk = -1, kSentWall = -2, kSentBad = -9;
+constexpr int kReflBit = 1 << 30;     // flag bit in a per-dimension map entry
+
+// Geometry constants visible to every kernel (one problem per launch).
+struct DevGeom {
+  int ndim, nx[3], h[3], P[3];
+  long N, NP, pstride[3];
+  int ncomp, nrb, nunk, first_rho, first_rb, first_mf;
+  int functional, attraction, single_size, hard_surf, nlists;
+  double esize[3];
+  double rho_b[kMaxC], betamu_hs_ex[kMaxC], betamu_att[kMaxC];
+  double inv_rad[kMaxC], inv_4pir[kMaxC], inv_4pirsq[kMaxC], fac[kMaxC];
+  double dphi_bulk[4], vext_max;
+  const int *map[3];                   // per-dimension padded -> source maps
+};
+
+// One stencil table on the device: linear offsets in the padded box and the
+// per-point coefficient rows for each output channel.
+struct DevStencil {
+  int L = 0;
+  std::vector<short> off;               // host copy [L][ndim]
+  std::vector<double> w, hw;            // host copy
+  int *d_loff = nullptr;                // [L] linear offsets in the padded box
+  // forward use (weighted densities / mean field of the density field)
+  int nout_fwd = 0;
+  double *d_coef_fwd = nullptr;         // [L][nout_fwd] FP64
+  float *d_coef_fwd32 = nullptr;        // FP32 copy
+  // transpose use (Euler-Lagrange sums over dPhi/dn or H v channels)
+  int nin_tr = 0;
+  double *d_coef_tr = nullptr;          // [L][nin_tr]
+  float *d_coef_tr32 = nullptr;
+  short *d_off = nullptr;               // [L][3] raw offsets (boundary corrections)
+  double *d_w = nullptr, *d_hw = nullptr;
+};
+
+}  // namespace tgpu
+
+struct tgpu_ctx {
+  tgpu_geometry g{};
+  tgpu::DevGeom dg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int precision = TGPU_FP64;
+  bool finalized = false;
+  bool have_state = false;
+
+  // host tables
+  std::vector<tgpu::DevStencil> sten[3];   // [type][index]
+  std::vector<double> h_vext;
+  std::vector<signed char> h_zero;
+  std::vector<int> h_bnodes;
+  std::vector<short> h_fmask;
+  std::vector<int> hw_targets;             // nodes whose stencils touch a hard-wall boundary node
+
+  // device buffers
+  int *d_map[3] = {nullptr, nullptr, nullptr};
+  double *d_vext = nullptr;
+  signed char *d_zero = nullptr;
+  int *d_bnodes = nullptr;
+  short *d_fmask = nullptr;
+  int *d_hw_targets = nullptr;
+  double *d_x = nullptr;        // state of the last mode-0 fill [nunk][N]
+  double *d_work = nullptr;     // [nunk][N] scratch for host-pointer entry points
+  double *d_work2 = nullptr;    // [nunk][N]
+  double *d_pad = nullptr;      // padded FP64 channels [nch_max][NP]
+  float *d_pad32 = nullptr;     // padded FP32 channels [nch_max][NP]
+  double *d_chan = nullptr;     // unpadded channels [nch_max][N]
+  double *d_conv = nullptr;     // convolution outputs [nrb + 2*ncomp][N]
+  double *d_tr = nullptr;       // transpose-conv output per component [ncomp][N]
+  int nch_max = 0;
+  // Krylov workspace
+  double *d_V = nullptr;        // [kdim+1][n2]
+  double *d_partial = nullptr;  // reduction partials
+  double *d_red = nullptr;      // reduction results
+  double *h_red = nullptr;      // pinned host copy
+  int kdim = 0;
+  double *d_gw = nullptr, *d_gt = nullptr, *d_gx = nullptr, *d_gb = nullptr;  // [n2] each
+
+  tgpu_stats stats{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace tgpu {
+
+// ---- kernels (kernels.cu) ---------------------------------------------------
+void upload_geom(const DevGeom &g, cudaStream_t s);
+// Pad nch channels src[ch][N] -> dst[ch][NP]; bulk[ch] replaces the bulk
+// sentinel, signmask[ch] selects the dimensions whose reflection flips the
+// sign, zcomp[ch] >= 0 masks nodes flagged zero-density for that component.
+template <typename T>
+void launch_pad(const double *src, T *dst, int nch, const double *bulk, const int *signmask, const int *zcomp,
+                const signed char *zero, bool periodic_only, cudaStream_t s);
+// out[o][i] (+)= sum_k sum_c coef[k][o][c] * in[c][pad(i) + loff[k]]
+template <typename T>
+void launch_conv(const T *in, long in_cstride, int nin, const int *loff, const T *coef, int L, double *const *out,
+                 int nout, bool accumulate, long N, cudaStream_t s);
+void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
+void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
+                     const double *tr, double *R, cudaStream_t s);
+void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, cudaStream_t s);
+void launch_jv_local(const double *x, const double *v, double *chan, cudaStream_t s);
+void launch_schur_combine(const double *x, const double *vext, const signed char *zero, const double *v2,
+                          const double *tr, const double *ymf, double *y2, cudaStream_t s);
+void launch_jv_combine(const double *x, const double *vext, const signed char *zero, const double *v,
+                       const double *conv, const double *tr, double *out, cudaStream_t s);
+void launch_hw_correct(const double *field, long field_cstride, int field_first, const DevStencil *theta,
+                       const DevStencil *delta, const DevStencil *uatt, const int *targets, int ntargets,
+                       const signed char *zero, const int *bnodes, const short *fmask, double *conv,
+                       cudaStream_t s);
+// Krylov helpers
+void launch_multidot(const double *V, long ldv, int nvec, const double *w, long n, double *partial, int nblocks,
+                     double *result, cudaStream_t s);
+void launch_multiaxpy(double *w, const double *V, long ldv, int nvec, const double *coef, long n, cudaStream_t s);
+void launch_scale(double *y, const double *x, double a, long n, cudaStream_t s);
+void launch_axpby(double *y, double a, const double *x, double b, long n, cudaStream_t s);
+void launch_precond(const double *x, const double *vext, const signed char *zero, const double *in, double *out,
+                    cudaStream_t s);
+void launch_newton_frac(const double *x, const double *dx, double floor_frac, double *partial, int nblocks,
+                        double *result, cudaStream_t s);
+void launch_newton_update(double *x, const double *dx, double frac, double rel, double abs, double *partial,
+                          int nblocks, double *result, cudaStream_t s);
+void launch_norm2(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s);
+void launch_check_finite(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s);
+
+int reduce_blocks(long n);
+
+}  // namespace tgpu

@@ -1,0 +1,269 @@
+"""ctypes binding of libtramonto_gpu.so and the host-side solver object.
+
+:class:`Solver` mirrors, for one problem, the operations the reference's
+Newton driver performs through its linear-problem manager:
+
+=====================  ==========================================================
+``fill(x, mode)``      fill_resid_and_matrix_control (src/dft_fill_control.c:39)
+``jv(v)``              dft_linprobmgr_applymatrix (src/dft_BasicLinProbMgr.cpp)
+``schur(v2)``          dft_Schur_Epetra_Operator::Apply (src/dft_Schur_Epetra_Operator.cpp:86)
+``solve(b)``           dft_linprobmgr_setupsolver + dft_linprobmgr_solve
+                       (src/dft_HardSphereLinProbMgr.cpp:345-428)
+``newton(x)``          newton_solver (src/dft_newton.c:131-198)
+=====================  ==========================================================
+
+Arrays are numpy ``[unknown][node]`` float64 (host) or torch CUDA tensors
+(``*_device`` methods).  Every call goes through the C ABI of
+include/tramonto_gpu.h; there is no CPU fallback: if the library or a GPU is
+missing the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from .problem import Problem
+
+TGPU_OK = 0
+FP64, FP32, BF16X3 = 0, 1, 2
+STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
+          -5: "no convergence", -6: "non-finite values", -7: "domain error"}
+
+
+class TgpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Geometry(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int), ("nx", C.c_int * 3), ("esize", C.c_double * 3), ("bc", (C.c_int * 2) * 3),
+        ("ncomp", C.c_int), ("functional", C.c_int), ("attraction", C.c_int), ("att_in_a22", C.c_int),
+        ("single_size", C.c_int), ("hard_surf", C.c_int), ("nlists_hw", C.c_int),
+        ("rho_b", C.c_double * 4), ("betamu_hs_ex", C.c_double * 4), ("betamu_att", C.c_double * 4),
+        ("inv_rad", C.c_double * 4), ("inv_4pir", C.c_double * 4), ("inv_4pirsq", C.c_double * 4),
+        ("fac_overlap", C.c_double * 4), ("dphi_bulk", C.c_double * 4), ("vext_max", C.c_double),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [("fill_ms", C.c_double), ("schur_ms", C.c_double), ("conv_ms", C.c_double), ("gmres_ms", C.c_double),
+                ("schur_applies", C.c_long), ("conv_launches", C.c_long), ("kernel_launches", C.c_long)]
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the CUDA library; raises when it is missing (no silent fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run tramonto_gb300.build.build() (nvcc, sm_103a) first")
+        _build.build()
+    lib = C.CDLL(path)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    lib.tgpu_last_error.restype = C.c_char_p
+    sigs = {
+        "tgpu_create": [C.POINTER(Geometry), C.c_int, C.POINTER(vp)],
+        "tgpu_destroy": [vp],
+        "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
+        "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
+        "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
+        "tgpu_sizes": [vp, C.POINTER(C.c_long), ip, ip],
+        "tgpu_fill": [vp, vp, vp, C.c_int], "tgpu_fill_device": [vp, vp, vp, C.c_int],
+        "tgpu_jv": [vp, vp, vp], "tgpu_jv_device": [vp, vp, vp],
+        "tgpu_jtv": [vp, vp, vp], "tgpu_jtv_device": [vp, vp, vp],
+        "tgpu_schur_apply": [vp, vp, vp], "tgpu_schur_apply_device": [vp, vp, vp],
+        "tgpu_schur_rhs_device": [vp, vp, vp], "tgpu_schur_x1_device": [vp, vp, vp, vp],
+        "tgpu_solve": [vp, vp, vp, C.c_double, C.c_int, ip, dp],
+        "tgpu_solve_device": [vp, vp, vp, C.c_double, C.c_int, ip, dp],
+        "tgpu_newton": [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, ip, dp],
+        "tgpu_newton_device": [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, ip, dp],
+        "tgpu_get_stats": [vp, C.POINTER(Stats)], "tgpu_reset_stats": [vp],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    _LIB = lib
+    return lib
+
+
+def _check(st, lib, ok=(TGPU_OK,)):
+    if st not in ok:
+        raise TgpuError(st, lib.tgpu_last_error().decode())
+    return st
+
+
+def geometry(p: Problem) -> Geometry:
+    g = Geometry()
+    g.ndim = p.ndim
+    for d in range(3):
+        g.nx[d] = int(p.nx[d]) if d < p.ndim else 1
+        g.esize[d] = float(p.esize[d]) if d < p.ndim else 0.0
+        for k in range(2):
+            g.bc[d][k] = int(p.bc[d][k]) if d < p.ndim else 0
+    g.ncomp, g.functional, g.attraction = p.ncomp, p.functional, p.attraction
+    g.att_in_a22, g.single_size, g.hard_surf, g.nlists_hw = p.att_in_a22, p.single_size, p.hard_surf, p.nlists_hw
+    for name in ("rho_b", "betamu_hs_ex", "betamu_att", "inv_rad", "inv_4pir", "inv_4pirsq", "fac_overlap"):
+        arr = getattr(g, name)
+        for i, v in enumerate(np.asarray(getattr(p, name), np.float64)[:4]):
+            arr[i] = float(v)
+    for i in range(4):
+        g.dphi_bulk[i] = float(p.dphi_bulk[i])
+    g.vext_max = float(p.vext_max)
+    return g
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Solver:
+    """One problem resident on one GPU (see module doc)."""
+
+    def __init__(self, p: Problem, device: int = 0, precision: int = FP64):
+        self.lib = lib = load()
+        self.p = p
+        self.h = C.c_void_p()
+        _check(lib.tgpu_create(C.byref(geometry(p)), device, C.byref(self.h)), lib)
+        try:
+            for (t, idx), (off, w, hw) in sorted(p.stencils.items()):
+                off = np.ascontiguousarray(off, np.int16)
+                w = np.ascontiguousarray(w, np.float64)
+                hwp = None
+                if hw is not None and p.hard_surf:
+                    hw = np.ascontiguousarray(hw, np.float64)
+                    hwp = _ptr(hw)
+                _check(lib.tgpu_set_stencil(self.h, t, idx, len(w), _ptr(off), _ptr(w), hwp), lib)
+            vext = np.ascontiguousarray(p.vext, np.float64)
+            _check(lib.tgpu_set_vext(self.h, _ptr(vext)), lib)
+            zd = np.ascontiguousarray(p.zero_density, np.int8)
+            _check(lib.tgpu_set_zero_density(self.h, _ptr(zd)), lib)
+            if p.hard_surf:
+                bn = np.ascontiguousarray(p.boundary_nodes, np.int32)
+                fm = np.ascontiguousarray(p.fluid_masks, np.int16)
+                _check(lib.tgpu_set_hard_wall(self.h, _ptr(bn), _ptr(fm)), lib)
+            _check(lib.tgpu_finalize(self.h), lib)
+            self.set_precision(precision)
+        except Exception:
+            self.close()
+            raise
+        self.N = p.nnodes
+        self.shape = (p.nunk, self.N)
+
+    # ---- lifecycle
+    def close(self):
+        if self.h:
+            self.lib.tgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_precision(self, precision: int):
+        _check(self.lib.tgpu_set_precision(self.h, int(precision)), self.lib)
+
+    def set_stream(self, stream_handle: int):
+        _check(self.lib.tgpu_set_stream(self.h, C.c_void_p(stream_handle)), self.lib)
+
+    # ---- host-array entry points
+    def _host(self, a, shape):
+        a = np.ascontiguousarray(a, np.float64)
+        if a.size != int(np.prod(shape)):
+            raise ValueError(f"expected {shape}, got {a.shape}")
+        return a
+
+    def fill(self, x, mode: int = 0):
+        x = self._host(x, self.shape)
+        R = np.empty(self.shape)
+        _check(self.lib.tgpu_fill(self.h, _ptr(x), _ptr(R), mode), self.lib)
+        return R
+
+    def jv(self, v):
+        v = self._host(v, self.shape)
+        out = np.empty(self.shape)
+        _check(self.lib.tgpu_jv(self.h, _ptr(v), _ptr(out)), self.lib)
+        return out
+
+    def jtv(self, w):
+        w = self._host(w, self.shape)
+        out = np.empty(self.shape)
+        _check(self.lib.tgpu_jtv(self.h, _ptr(w), _ptr(out)), self.lib)
+        return out
+
+    def schur(self, v2):
+        shape2 = (self.p.ncomp, self.N)
+        v2 = self._host(v2, shape2)
+        out = np.empty(shape2)
+        _check(self.lib.tgpu_schur_apply(self.h, _ptr(v2), _ptr(out)), self.lib)
+        return out
+
+    def solve(self, b, tol=1e-10, max_iter=500):
+        b = self._host(b, self.shape)
+        dx = np.empty(self.shape)
+        it, rr = C.c_int(0), C.c_double(0.0)
+        st = self.lib.tgpu_solve(self.h, _ptr(b), _ptr(dx), tol, max_iter, C.byref(it), C.byref(rr))
+        _check(st, self.lib, ok=(0, -5))
+        return dx, it.value, rr.value
+
+    def newton(self, x0, rel_tol=1e-3, abs_tol=1e-8, update_floor=0.1, max_iter=50, lin_tol=1e-10, lin_max_iter=500,
+               allow_noconv=False):
+        x = np.array(x0, np.float64, copy=True, order="C")
+        it, rn = C.c_int(0), C.c_double(0.0)
+        st = self.lib.tgpu_newton(self.h, _ptr(x), rel_tol, abs_tol, update_floor, max_iter, lin_tol, lin_max_iter,
+                                  C.byref(it), C.byref(rn))
+        _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
+        return x, it.value, rn.value
+
+    # ---- device entry points (torch CUDA tensors, float64, contiguous)
+    @staticmethod
+    def _dptr(t):
+        assert t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float64"
+        return C.c_void_p(t.data_ptr())
+
+    def fill_device(self, x, R, mode: int = 0):
+        _check(self.lib.tgpu_fill_device(self.h, self._dptr(x), self._dptr(R), mode), self.lib)
+
+    def jv_device(self, v, out):
+        _check(self.lib.tgpu_jv_device(self.h, self._dptr(v), self._dptr(out)), self.lib)
+
+    def schur_device(self, v2, y2):
+        _check(self.lib.tgpu_schur_apply_device(self.h, self._dptr(v2), self._dptr(y2)), self.lib)
+
+    def solve_device(self, b, dx, tol=1e-10, max_iter=500):
+        it, rr = C.c_int(0), C.c_double(0.0)
+        st = self.lib.tgpu_solve_device(self.h, self._dptr(b), self._dptr(dx), tol, max_iter, C.byref(it), C.byref(rr))
+        _check(st, self.lib, ok=(0, -5))
+        return it.value, rr.value
+
+    def newton_device(self, x, rel_tol=1e-3, abs_tol=1e-8, update_floor=0.1, max_iter=50, lin_tol=1e-10,
+                      lin_max_iter=500, allow_noconv=False):
+        it, rn = C.c_int(0), C.c_double(0.0)
+        st = self.lib.tgpu_newton_device(self.h, self._dptr(x), rel_tol, abs_tol, update_floor, max_iter, lin_tol,
+                                         lin_max_iter, C.byref(it), C.byref(rn))
+        _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
+        return it.value, rn.value
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(self.lib.tgpu_get_stats(self.h, C.byref(s)), self.lib)
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def reset_stats(self):
+        _check(self.lib.tgpu_reset_stats(self.h), self.lib)

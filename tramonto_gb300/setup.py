@@ -1,0 +1,233 @@
+"""Host set-up of a problem: stencil tables, bulk constants, synthetic inputs.
+
+Restates the set-up the reference does once per run before its Newton loop:
+
+* stencils (calc_stencils, src/dft_stencil.c:40-287) through the library's
+  ``tgpu_make_stencil`` (tramonto_gb300/csrc/stencils.cpp);
+* bulk FMT constants: rhobar_icomp / dphi_drb_bulk / chempot_FMT_hs
+  (src/dft_thermo_hs.c:58-70, 138-153, 292-334) and the 1/R factors
+  calc_InvR_params (:58-70);
+* the mean-field constants calc_Avdw_att / chempot_att
+  (src/dft_thermo_att.c:44-63, 86-99) with int_stencil_bulk
+  (src/dft_energy_CLSintsten.c:43-69).
+
+The synthetic geometries of the benchmark workloads (rough Lennard-Jones
+12-3 wall, cylindrical pore with a Gaussian random field) are generated here
+from seeds; the reference has no 12-3 wall, so its prefactor is fixed below.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import native
+from .problem import BC_IN_BULK, BC_IN_WALL, BC_PERIODIC, DELTA, FMT1, FMT3, THETA, UATT, Problem
+
+PI = math.pi
+
+
+def _lib():
+    lib = native.load()
+    lib.tgpu_make_stencil.restype = C.c_int
+    lib.tgpu_make_stencil.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.tgpu_lj_rmin.restype = C.c_double
+    lib.tgpu_lj_rmin.argtypes = [C.c_double] * 4
+    return lib
+
+
+def make_stencil(stype, ndim, esize, hs_diam=0.0, sigma=1.0, eps=1.0, rcut=0.0, rmin=0.0, with_hw=False):
+    lib = _lib()
+    es = (C.c_double * 3)(*(list(esize) + [0.0] * (3 - len(esize))))
+    L = lib.tgpu_make_stencil(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, 0, None, None, None, None)
+    if L < 0:
+        raise RuntimeError(f"tgpu_make_stencil failed ({L})")
+    off = np.zeros((L, ndim), np.int16)
+    w = np.zeros(L)
+    hw = np.zeros((L, 1 << ndim)) if with_hw else None
+    L2 = lib.tgpu_make_stencil(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, L, off.ctypes.data, w.ctypes.data,
+                               hw.ctypes.data if with_hw else None, None)
+    assert L2 == L
+    return off, w, hw
+
+
+def lj_rmin(sigma, eps, rcut, esize0):
+    return _lib().tgpu_lj_rmin(sigma, eps, rcut, esize0)
+
+
+def fmt_dphi_bulk(functional, n):
+    """dPhi/dn0..dn3 at a bulk state (vector terms vanish), FMT1 or FMT3."""
+    n0, n1, n2, n3 = n
+    a = 1.0 / (1.0 - n3)
+    d0 = math.log(a)
+    d1 = n2 * a
+    if functional == FMT3:
+        if n3 > 1e-10:
+            lg = math.log(1.0 - n3)
+            F = n3 + (1 - n3) ** 2 * lg
+            F1 = n3 - 2 * (1 - n3) * lg
+            G1 = 2.0 * (-a * a / n3 ** 3 + a ** 3 / n3 ** 2)
+            f = F * a * a / (36 * PI * n3 * n3)
+            f1 = (F1 * a * a / (n3 * n3) + F * G1) / (36 * PI)
+            d2 = n1 * a + 3 * n2 * n2 * f
+            d3 = n0 * a + n1 * n2 * a * a + n2 ** 3 * f1
+        else:
+            d2 = d3 = 0.0
+    else:
+        d2 = n1 * a + n2 * n2 * a * a / (8 * PI)
+        d3 = n0 * a + n1 * n2 * a * a + n2 ** 3 * a ** 3 / (12 * PI)
+    return np.array([d0, d1, d2, d3])
+
+
+def bulk_constants(functional, hs_diam, rho_b, attraction=False, uatt_stencils=None, ncomp=None):
+    """Bulk weighted densities, dPhi/dn, excess chemical potentials (reference set-up)."""
+    hs_diam = np.asarray(hs_diam, float)
+    rho_b = np.asarray(rho_b, float)
+    nc = len(rho_b) if ncomp is None else ncomp
+    inv_rad = 2.0 / hs_diam
+    inv_4pir = inv_rad / (4 * PI)
+    inv_4pirsq = inv_4pir * inv_rad
+    rhobar = np.zeros(4)   # solution-vector order n3, n2, n1, n0
+    for i in range(nc):
+        vol = PI * hs_diam[i] ** 3 / 6.0
+        area = PI * hs_diam[i] ** 2
+        rhobar += np.array([vol * rho_b[i], area * rho_b[i], area * rho_b[i] * inv_4pir[i],
+                            area * rho_b[i] * inv_4pirsq[i]])
+    n = (rhobar[3], rhobar[2], rhobar[1], rhobar[0])
+    dphi = fmt_dphi_bulk(functional, n)
+    betamu_hs = np.zeros(nc)
+    for i in range(nc):
+        r = hs_diam[i] / 2.0
+        sums = np.array([1.0, r, 4 * PI * r * r, 4 * PI / 3 * r ** 3])
+        betamu_hs[i] = float(np.dot(dphi, sums))
+    betamu_att = np.zeros(nc)
+    avdw = np.zeros((nc, nc))
+    if attraction:
+        for i in range(nc):
+            for j in range(nc):
+                avdw[i, j] = float(np.sum(uatt_stencils[i + nc * j][1]))
+        betamu_att = avdw @ rho_b
+    return dict(inv_rad=inv_rad, inv_4pir=inv_4pir, inv_4pirsq=inv_4pirsq, rhobar_b=rhobar, dphi_bulk=dphi,
+                betamu_hs_ex=betamu_hs, betamu_att=betamu_att, avdw=avdw)
+
+
+def build_problem(ndim, nx, esize, bc, hs_diam, rho_b, functional=FMT1, attraction=False, sigma=None, eps=None,
+                  rcut=None, vext=None, zero_density=None, vext_max=10.0):
+    """Assemble a Problem with generated stencils and bulk constants."""
+    nc = len(rho_b)
+    st = {}
+    for i in range(nc):
+        st[(DELTA, i)] = make_stencil(DELTA, ndim, esize, hs_diam=hs_diam[i])
+        st[(THETA, i)] = make_stencil(THETA, ndim, esize, hs_diam=hs_diam[i])
+    uat = {}
+    if attraction:
+        for i in range(nc):
+            for j in range(nc):
+                rmin = lj_rmin(sigma[i][j], eps[i][j], rcut[i][j], esize[0])
+                uat[i + nc * j] = make_stencil(UATT, ndim, esize, sigma=sigma[i][j], eps=eps[i][j], rcut=rcut[i][j],
+                                               rmin=rmin)
+                st[(UATT, i + nc * j)] = uat[i + nc * j]
+    b = bulk_constants(functional, hs_diam, rho_b, attraction, uat, nc)
+    N = int(np.prod(nx[:ndim]))
+    if vext is None:
+        vext = np.zeros((nc, N))
+    if zero_density is None:
+        zero_density = (vext >= vext_max).astype(np.int8)
+    return Problem(ndim=ndim, nx=tuple(nx), esize=tuple(esize), bc=tuple(bc), ncomp=nc, functional=functional,
+                   attraction=int(attraction), att_in_a22=0, single_size=int(nc == 1), hard_surf=0, nlists_hw=1,
+                   rho_b=np.asarray(rho_b, float), hs_diam=np.asarray(hs_diam, float), betamu_hs_ex=b["betamu_hs_ex"],
+                   betamu_att=b["betamu_att"], inv_rad=b["inv_rad"], inv_4pir=b["inv_4pir"],
+                   inv_4pirsq=b["inv_4pirsq"], fac_overlap=np.ones(nc), dphi_bulk=b["dphi_bulk"],
+                   vext_max=vext_max, vext=np.ascontiguousarray(vext, float),
+                   zero_density=np.ascontiguousarray(zero_density, np.int8), stencils=st)
+
+
+# ---- synthetic workloads ----------------------------------------------------
+
+# 12-3 Lennard-Jones wall V(d) = eps_w * C * ((sigma/d)^12 - (sigma/d)^3), C chosen so that min V = -eps_w
+LJ123_PREF = 1.0 / (0.75 * 4.0 ** (-1.0 / 3.0))
+
+
+def rough_wall_vext(nx, esize, eps_w=1.0, kT=1.2, sigma_w=1.0, wall_x=1.0, patches=16, amplitude=0.5, seed=1234,
+                    vext_max=10.0):
+    """V_ext/kT of a rough 12-3 LJ wall normal to x.
+
+    The surface sits at x = wall_x + h(y, z); h is i.i.d. uniform in
+    [-amplitude, amplitude] sigma on a patches x patches grid over the periodic
+    y-z plane (numpy PCG64 seeded with `seed`).  Nodes with d <= 0 or
+    V >= vext_max are clipped to vext_max (zero-density rows).
+    """
+    rng = np.random.default_rng(seed)
+    hpatch = rng.uniform(-amplitude, amplitude, size=(patches, patches))
+    ny, nz = nx[1], nx[2]
+    iy = (np.arange(ny) * patches) // ny
+    iz = (np.arange(nz) * patches) // nz
+    h = hpatch[iy][:, iz]                                  # [ny][nz]
+    x = np.arange(nx[0]) * esize[0]
+    d = x[None, None, :] - (wall_x + h.T[:, :, None])      # [nz][ny][nx]
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        s = np.where(d > 0, sigma_w / np.maximum(d, 1e-300), np.inf)
+        v = (eps_w / kT) * LJ123_PREF * (s ** 12 - s ** 3)
+    v = np.where((d <= 0) | (v >= vext_max) | ~np.isfinite(v), vext_max, v)
+    return v.reshape(1, -1), dict(patches=patches, amplitude=amplitude, seed=seed, wall_x=wall_x, eps_w=eps_w,
+                                  prefactor=LJ123_PREF, form="eps_w*C*((s/d)^12-(s/d)^3)/kT")
+
+
+def config2(n=128, esize=0.1, seed=1234):
+    """3-D FMT1 + WCA (eps=1, r_c=2.5, kT*=1.2) fluid at rho_b=0.6 next to a rough 12-3 LJ wall.
+
+    Periodic in y and z; the wall side of x is IN_WALL, the far side IN_BULK."""
+    nx = (n, n, n)
+    es = (esize, esize, esize)
+    kT = 1.2
+    vext, meta = rough_wall_vext(nx, es, kT=kT, seed=seed)
+    p = build_problem(3, nx, es, ((BC_IN_WALL, BC_IN_BULK), (BC_PERIODIC, BC_PERIODIC), (BC_PERIODIC, BC_PERIODIC)),
+                      hs_diam=[1.0], rho_b=[0.6], functional=FMT1, attraction=True, sigma=[[1.0]], eps=[[1.0 / kT]],
+                      rcut=[[2.5]], vext=vext)
+    meta.update(grid=list(nx), dx=esize, rho_b=0.6, kT=kT, rcut=2.5, functional="FMT1", attraction="WCA LJ12-6")
+    return p, meta
+
+
+def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0):
+    """3-D binary White-Bear (FMT3) hard spheres (sigma 1 and 0.5, rho_b 0.3 and 0.6) in a
+    cylindrical pore of radius 5 along z; V_ext += 0.5 kT * Gaussian random field (corr. length 1)."""
+    es = (esize,) * 3
+    N = int(np.prod(nx))
+    rng = np.random.default_rng(seed)
+    white = rng.standard_normal(nx[::-1])
+    # Gaussian filter with correlation length 1 sigma in Fourier space (periodic)
+    k = [np.fft.fftfreq(m, d=esize) * 2 * PI for m in nx[::-1]]
+    kk = k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2 + k[2][None, None, :] ** 2
+    g = np.real(np.fft.ifftn(np.fft.fftn(white) * np.exp(-0.5 * kk * 1.0 ** 2)))
+    g /= g.std()
+    x = (np.arange(nx[0]) - (nx[0] - 1) / 2) * esize
+    y = (np.arange(nx[1]) - (nx[1] - 1) / 2) * esize
+    r = np.sqrt(x[None, None, :] ** 2 + y[None, :, None] ** 2) * np.ones((nx[2], 1, 1))
+    outside = r >= pore_radius
+    v1 = np.where(outside, 10.0, 0.5 * g).reshape(-1)
+    vext = np.stack([v1, v1])
+    zd = np.stack([outside.reshape(-1), outside.reshape(-1)]).astype(np.int8)
+    p = build_problem(3, nx, es, ((BC_IN_WALL, BC_IN_WALL), (BC_IN_WALL, BC_IN_WALL), (BC_PERIODIC, BC_PERIODIC)),
+                      hs_diam=[1.0, 0.5], rho_b=[0.3, 0.6], functional=FMT3, vext=vext, zero_density=zd)
+    return p, dict(grid=list(nx), dx=esize, seed=seed, pore_radius=pore_radius, rho_b=[0.3, 0.6],
+                   functional="FMT3", field="0.5 kT Gaussian random field, correlation length 1")
+
+
+def initial_state(solver, p: Problem):
+    """Density rho_b*exp(-V) (0 in walls); weighted densities and mean field from their own sums."""
+    N = p.nnodes
+    x = np.zeros((p.nunk, N))
+    for c in range(p.ncomp):
+        v = p.vext[c]
+        rho = p.rho_b[c] * np.exp(-np.minimum(v, 50.0))
+        rho[p.zero_density[c] != 0] = 0.0
+        rho[v >= p.vext_max] = 0.0
+        x[p.first_rho + c] = np.maximum(rho, 0.0)
+    # R = -x + sums on the weighted-density and mean-field rows: two passes set
+    # the independent unknowns to their sums, then the dependent local copies
+    for _ in range(2):
+        R = solver.fill(x, mode=1)
+        x[p.first_rb:] += R[p.first_rb:]
+    return x
