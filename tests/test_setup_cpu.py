@@ -43,7 +43,7 @@ def test_bulk_constants_match_reference(case):
 
 
 def test_config_generators_are_seeded():
-    v1, m1 = setup.rough_wall_vext((16, 16, 16), (0.1, 0.1, 0.1), seed=5)
-    v2, m2 = setup.rough_wall_vext((16, 16, 16), (0.1, 0.1, 0.1), seed=5)
+    v1, m1 = setup.rough_wall_vext((48, 16, 16), (0.1, 0.1, 0.1), seed=5)
+    v2, m2 = setup.rough_wall_vext((48, 16, 16), (0.1, 0.1, 0.1), seed=5)
     assert np.array_equal(v1, v2) and m1 == m2
     assert v1.max() == 10.0 and v1.min() < 0.0
