@@ -1,0 +1,45 @@
+"""Mixed-precision form: FP32 stencil sums in the Schur products, FP64 residual.
+
+The FP32 Schur product must agree with the FP64 one to FP32-level accuracy, and
+a Newton solve whose Schur-GMRES uses FP32 products must converge to the FP64
+solution (residual 1e-8, density error <= 1e-6 relative) because the residual
+stays FP64."""
+import numpy as np
+import pytest
+
+from goldens import load, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FP32_PRODUCT_RTOL = 2e-5
+
+
+def test_fp32_schur_product_close_to_fp64():
+    from tramonto_gb300 import native
+    z, p = load("fmt1_wca_3d")
+    s = native.Solver(p)
+    x = z["x0"]
+    s.fill(x)
+    rng = np.random.default_rng(11)
+    v2 = rng.standard_normal((p.ncomp, p.nnodes))
+    y64 = s.schur(v2)
+    s.set_precision(native.FP32)
+    y32 = s.schur(v2)
+    s.close()
+    assert rel_err(y32, y64) <= FP32_PRODUCT_RTOL
+
+
+def test_mixed_newton_matches_fp64_solution():
+    from tramonto_gb300 import native, setup
+    p, meta = setup.config2(n=40)
+    s = native.Solver(p, precision=native.FP64)
+    x0 = setup.initial_state(s, p)
+    x64, it64, r64 = s.newton(x0, max_iter=40, lin_tol=1e-8, lin_max_iter=300)
+    s.set_precision(native.FP32)
+    x32, it32, r32 = s.newton(x0, max_iter=40, lin_tol=1e-6, lin_max_iter=300)
+    R = s.fill(x32, mode=1)
+    s.close()
+    rho64, rho32 = x64[0], x32[0]
+    err = np.abs(rho32 - rho64).max() / np.abs(rho64).max()
+    assert np.abs(R).max() < 1e-8, np.abs(R).max()
+    assert err <= 1e-6, (err, it64, it32)

@@ -2,6 +2,7 @@
 // the fill, Jacobian and Schur products, the Schur-complement GMRES and the
 // damped Newton loop.  All device work is issued on the handle's stream.
 #include <algorithm>
+#include <map>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -189,7 +190,18 @@ void pad(Ctx *c, const double *src, const PadParams &pp, bool fp64)
 void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool fp64)
 {
   const long NP = c->dg.NP;
-  if (fp64 || c->precision == TGPU_FP64)
+  const bool f32 = !(fp64 || c->precision == TGPU_FP64);
+  if (f32 && nin == 1 && nout == 1) {
+    const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
+    if (ln.nlines > 0) {
+      tgpu::launch_conv_lines(c->d_pad32 + (long)ch0 * NP, ln.d_lines, ln.d_chunks, ln.nchunks, ln.d_w, outs[0],
+                              c->dg.nx[0], (long)c->dg.nx[1] * c->dg.nx[2], c->stream);
+      c->stats.conv_launches++;
+      c->stats.kernel_launches++;
+      return;
+    }
+  }
+  if (!f32)
     tgpu::launch_conv<double>(c->d_pad + (long)ch0 * NP, NP, nin, st.d_loff, tr ? st.d_coef_tr : st.d_coef_fwd, st.L,
                               outs, nout, true, c->dg.N, c->stream);
   else
@@ -501,6 +513,48 @@ void d2h(Ctx *c, double *h, const double *d, size_t n)
   ck(cudaStreamSynchronize(c->stream), "sync");
 }
 
+// Regroup a 3-D stencil into x-lines of constant (oy, oz) for the FP32 line kernel.
+DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &coef, const tgpu::DevGeom &dg,
+                              cudaStream_t s)
+{
+  const int TX = tgpu::kLineTX;
+  std::map<std::pair<int, int>, std::vector<std::pair<int, double>>> groups;
+  for (int k = 0; k < st.L; k++) {
+    const short *o = &st.off[(size_t)k * 3];
+    groups[{o[2], o[1]}].push_back({o[0], coef[k]});
+  }
+  std::vector<int4> lines, chunks;
+  std::vector<float> w;
+  int chunk_first = 0, chunk_w0 = 0;
+  for (auto &gkv : groups) {
+    int xmin = 1 << 30, xmax = -(1 << 30);
+    for (auto &e : gkv.second) { xmin = std::min(xmin, e.first); xmax = std::max(xmax, e.first); }
+    const int len = xmax - xmin + 1;
+    const int nb = (len + TX - 1) / TX;
+    if (nb * TX > tgpu::kLineWChunkMax) throw Error(TGPU_ERR_UNSUPPORTED, "stencil line longer than the chunk");
+    const int nl_in_chunk = (int)lines.size() - chunk_first;
+    if (nl_in_chunk == tgpu::kLineChunkMax || (int)w.size() + nb * TX - chunk_w0 > tgpu::kLineWChunkMax) {
+      chunks.push_back({chunk_first, nl_in_chunk, chunk_w0, (int)w.size() - chunk_w0});
+      chunk_first = (int)lines.size();
+      chunk_w0 = (int)w.size();
+    }
+    const long loff = xmin + (long)gkv.first.second * dg.pstride[1] + (long)gkv.first.first * dg.pstride[2];
+    lines.push_back({(int)loff, nb, (int)w.size(), 0});
+    const size_t base = w.size();
+    w.resize(base + (size_t)nb * TX, 0.0f);
+    for (auto &e : gkv.second) w[base + (e.first - xmin)] = (float)e.second;
+  }
+  if ((int)lines.size() > chunk_first)
+    chunks.push_back({chunk_first, (int)lines.size() - chunk_first, chunk_w0, (int)w.size() - chunk_w0});
+  DevStencil::Lines L;
+  L.nlines = (int)lines.size();
+  L.nchunks = (int)chunks.size();
+  L.d_lines = upload(lines, s);
+  L.d_chunks = upload(chunks, s);
+  L.d_w = upload(w, s);
+  return L;
+}
+
 void build_device_tables(Ctx *c)
 {
   tgpu_geometry &g = c->g;
@@ -588,6 +642,10 @@ void build_device_tables(Ctx *c)
         std::vector<float> t32(tr.begin(), tr.end());
         st.d_coef_tr32 = upload(t32, c->stream);
       }
+      if (nd == 3 && (t == TGPU_STEN_THETA || t == TGPU_STEN_UATT)) {
+        st.lines_fwd = build_lines(st, fwd, dg, c->stream);
+        if (t == TGPU_STEN_THETA) st.lines_tr = build_lines(st, tr, dg, c->stream);
+      }
     }
   const long N = dg.N;
   // fields
@@ -670,7 +728,9 @@ void build_device_tables(Ctx *c)
   c->d_work = dalloc<double>(U * N);
   c->d_work2 = dalloc<double>(U * N);
   c->d_pad = dalloc<double>((size_t)c->nch_max * NP);
-  c->d_pad32 = dalloc<float>((size_t)c->nch_max * NP);
+  // FP32 padded channels with slack: the line kernel reads up to 2*kLineTX past a row end
+  c->d_pad32 = dalloc<float>((size_t)c->nch_max * NP + 64);
+  ck(cudaMemsetAsync(c->d_pad32, 0, sizeof(float) * ((size_t)c->nch_max * NP + 64), c->stream), "memset");
   c->d_chan = dalloc<double>((size_t)c->nch_max * N);
   c->d_conv = dalloc<double>((size_t)(dg.nrb + dg.ncomp) * N);
   c->d_tr = dalloc<double>((size_t)dg.ncomp * N);
@@ -767,6 +827,7 @@ int tgpu_destroy(tgpu_handle h)
       for (auto &st : c->sten[t]) {
         dfree(st.d_loff); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
         dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32);
+        for (auto *L : {&st.lines_fwd, &st.lines_tr}) { dfree(L->d_lines); dfree(L->d_chunks); dfree(L->d_w); }
       }
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);

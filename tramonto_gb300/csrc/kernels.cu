@@ -194,6 +194,92 @@ void launch_conv<float>(const float *in, long cstride, int nin, const int *loff,
 }
 
 // ---------------------------------------------------------------------------
+// FP32 stencil sums over x-lines.  The stencil is regrouped into lines of
+// constant (oy, oz) with a contiguous run of ox (zero weights fill gaps and pad
+// each run to a multiple of TX).  A thread owns TX consecutive outputs along
+// x and slides a 2*TX register window over each line, so every input value
+// loaded serves TX multiply-adds.  Line partial sums are combined with a
+// compensated (Kahan) sum so the FP32 result keeps ~1e-7 relative accuracy
+// over the ~10^5-point attraction stencil.
+constexpr int kTX = 8;
+constexpr int kLineChunk = 256;
+constexpr int kWChunk = 8192;
+
+// lines[l] = {linear offset of the run start from the output, blocks of kTX, weight offset, 0}
+// chunks[c] = {first line, line count, first weight, weight count}; a chunk fits in shared memory.
+__global__ void __launch_bounds__(128) k_conv_lines(const float *__restrict__ in, const int4 *__restrict__ lines,
+                                                   const int4 *__restrict__ chunks, int nchunks,
+                                                   const float *__restrict__ lw, double *__restrict__ out, int nxb)
+{
+  __shared__ int4 s_line[kLineChunk];
+  __shared__ float s_w[kWChunk];
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long nthr = (long)nxb * c_g.nx[1] * c_g.nx[2];
+  const bool active = t < nthr;
+  const int xb = (int)(t % nxb);
+  const long r = t / nxb;
+  const int y = (int)(r % c_g.nx[1]);
+  const int z = (int)(r / c_g.nx[1]);
+  const int x0 = xb * kTX;
+  const long ip0 = (long)(x0 + c_g.h[0]) + c_g.pstride[1] * (y + c_g.h[1]) + c_g.pstride[2] * (z + c_g.h[2]);
+  float sum[kTX], comp[kTX];
+#pragma unroll
+  for (int o = 0; o < kTX; o++) { sum[o] = 0.f; comp[o] = 0.f; }
+  for (int ci = 0; ci < nchunks; ci++) {
+    const int4 ch = chunks[ci];
+    __syncthreads();
+    for (int k = threadIdx.x; k < ch.y; k += blockDim.x) s_line[k] = lines[ch.x + k];
+    for (int k = threadIdx.x; k < ch.w; k += blockDim.x) s_w[k] = lw[ch.z + k];
+    __syncthreads();
+    if (!active) continue;
+    for (int li = 0; li < ch.y; li++) {
+      const int4 ln = s_line[li];
+      const float *src = in + ip0 + ln.x;
+      const float *w = s_w + (ln.z - ch.z);
+      float acc[kTX];
+#pragma unroll
+      for (int o = 0; o < kTX; o++) acc[o] = 0.f;
+      float win[2 * kTX];
+#pragma unroll
+      for (int q = 0; q < kTX; q++) win[q] = __ldg(src + q);
+      for (int kb = 0; kb < ln.y; kb++) {
+#pragma unroll
+        for (int q = 0; q < kTX; q++) win[kTX + q] = __ldg(src + (kb + 1) * kTX + q);
+#pragma unroll
+        for (int kk = 0; kk < kTX; kk++) {
+          const float wk = w[kb * kTX + kk];
+#pragma unroll
+          for (int o = 0; o < kTX; o++) acc[o] = fmaf(wk, win[o + kk], acc[o]);
+        }
+#pragma unroll
+        for (int q = 0; q < kTX; q++) win[q] = win[kTX + q];
+      }
+#pragma unroll
+      for (int o = 0; o < kTX; o++) {   // compensated accumulation of the line sums
+        const float yv = acc[o] - comp[o];
+        const float tv = sum[o] + yv;
+        comp[o] = (tv - sum[o]) - yv;
+        sum[o] = tv;
+      }
+    }
+  }
+  if (active) {
+    const long i0 = x0 + (long)c_g.nx[0] * (y + (long)c_g.nx[1] * z);
+#pragma unroll
+    for (int o = 0; o < kTX; o++)
+      if (x0 + o < c_g.nx[0]) out[i0 + o] += (double)sum[o];
+  }
+}
+
+void launch_conv_lines(const float *in, const int4 *lines, const int4 *chunks, int nchunks, const float *lw,
+                       double *out, int nx0, long ny_nz, cudaStream_t s)
+{
+  const int nxb = (nx0 + kTX - 1) / kTX;
+  const long nthr = (long)nxb * ny_nz;
+  k_conv_lines<<<(unsigned)((nthr + 127) / 128), 128, 0, s>>>(in, lines, chunks, nchunks, lw, out, nxb);
+}
+
+// ---------------------------------------------------------------------------
 // FMT physics at one node.  n is in the reference's n ordering
 // (n0, n1, n2, n3, V1[d], V2[d]); sv is the solution-vector ordering
 // (n3, n2, n1, n0, V2[d], V1[d]) (solutionVec_to_nOrdering, src/dft_utils.c:205-221).

@@ -54,6 +54,12 @@ struct DevStencil {
   float *d_coef_tr32 = nullptr;
   short *d_off = nullptr;               // [L][3] raw offsets (boundary corrections)
   double *d_w = nullptr, *d_hw = nullptr;
+  // x-line form for the FP32 single-channel sums (3-D): forward and transpose coefficients
+  struct Lines {
+    int4 *d_lines = nullptr, *d_chunks = nullptr;
+    float *d_w = nullptr;
+    int nlines = 0, nchunks = 0;
+  } lines_fwd, lines_tr;
 };
 
 }  // namespace tgpu
@@ -118,6 +124,9 @@ void launch_pad(const double *src, T *dst, int nch, const double *bulk, const in
 template <typename T>
 void launch_conv(const T *in, long in_cstride, int nin, const int *loff, const T *coef, int L, double *const *out,
                  int nout, bool accumulate, long N, cudaStream_t s);
+void launch_conv_lines(const float *in, const int4 *lines, const int4 *chunks, int nchunks, const float *lw,
+                       double *out, int nx0, long ny_nz, cudaStream_t s);
+constexpr int kLineTX = 8, kLineChunkMax = 256, kLineWChunkMax = 8192;
 void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
                      const double *tr, double *R, cudaStream_t s);
