@@ -201,6 +201,7 @@ def main():
     t_setup = time.perf_counter()
     p, meta = setup.config2(n=args.n)
     s = native.Solver(p, device=local, precision=native.FP32)
+    s.set_fill_arithmetic(native.FILL_REFINED)
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
     x0 = setup.initial_state(s, p)
@@ -248,12 +249,16 @@ def main():
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
+    s.set_fill_arithmetic(native.FILL_FP64)
     t_fill = timed(lambda: s.fill_device(dx, R, 0))
+    s.set_fill_arithmetic(native.FILL_FP32)
+    t_fill32 = timed(lambda: s.fill_device(dx, R, 0))
     s.set_precision(native.FP32)
     t_apply32 = timed(lambda: s.schur_device(v2, y2), reps=5)
     s.set_precision(native.FP64)
     t_apply64 = timed(lambda: s.schur_device(v2, y2), reps=2)
     # plain FP64 Newton iterations from the same state
+    s.set_fill_arithmetic(native.FILL_FP64)
     fp64_ms = None
     if args.fp64_steps > 0:
         dx64 = torch.from_numpy(x0).to("cuda").contiguous()
@@ -269,6 +274,7 @@ def main():
         fp64_ms = a.elapsed_time(b) / args.fp64_steps
         del dx64
     s.set_precision(native.FP32)
+    s.set_fill_arithmetic(native.FILL_REFINED)
     # end to end through the C ABI with host buffers (copies inside the timed region)
     xh = dx.cpu().numpy().copy()
     torch.cuda.synchronize()
@@ -302,8 +308,9 @@ def main():
                          "peak_source": f"{peak_src} bf16 dense", "traffic": None,
                          "note": "stencil sums run on the FP64/FP32 SIMT pipes; tensor roof shown for reference"},
             "cpu_baseline": cb,
-            "breakdown_ms": {"fill_fp64": t_fill, "schur_apply_fp32": t_apply32, "schur_apply_fp64": t_apply64,
-                             "schur_applies_per_step": applies_per_step},
+            "breakdown_ms": {"fill_fp64": t_fill, "fill_fp32": t_fill32, "schur_apply_fp32": t_apply32,
+                             "schur_apply_fp64": t_apply64, "schur_applies_per_step": applies_per_step,
+                             "fp64_refreshes_in_timed_steps": int(st["fp64_refreshes"])},
             "plain_fp64": {"ms_per_step": fp64_ms, "speedup_mixed_vs_fp64": (fp64_ms / ms) if fp64_ms else None},
             "setup_s": t_setup,
         }

@@ -106,6 +106,15 @@ int tgpu_finalize(tgpu_handle h);
 /* Arithmetic of the Jacobian / Schur products (TGPU_FP64 or TGPU_FP32); the
  * residual fill always sums in FP64. */
 int tgpu_set_precision(tgpu_handle h, int precision);
+/* Arithmetic of the residual fill:
+ *   TGPU_FILL_FP64     every stencil sum in FP64 (default; the reference's arithmetic)
+ *   TGPU_FILL_FP32     FP32 stencil sums (an inexact residual)
+ *   TGPU_FILL_REFINED  FP64 sums of a reference state plus FP32 sums of the change since then;
+ *                      the reference is refreshed in FP64 when the change exceeds tau times the
+ *                      field (max norms).  tgpu_newton uses FP32 sums while ||R|| > switch_norm.
+ * tau / switch_norm <= 0 keep the current values (defaults 1e-3 and 1e-3). */
+enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2 };
+int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm);
 int tgpu_set_stream(tgpu_handle h, void *cuda_stream);
 int tgpu_sizes(tgpu_handle h, long *nnodes, int *nunk, int *ncomp);
 
@@ -158,7 +167,7 @@ double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */
 typedef struct {
   double fill_ms, schur_ms, conv_ms, gmres_ms;
-  long schur_applies, conv_launches, kernel_launches;
+  long schur_applies, conv_launches, kernel_launches, fp64_refreshes;
 } tgpu_stats;
 int tgpu_get_stats(tgpu_handle h, tgpu_stats *out);
 int tgpu_reset_stats(tgpu_handle h);

@@ -29,14 +29,40 @@ def test_fp32_schur_product_close_to_fp64():
     assert rel_err(y32, y64) <= FP32_PRODUCT_RTOL
 
 
-def test_mixed_newton_matches_fp64_solution():
+def test_refined_fill_matches_fp64_fill():
+    """FP64 sums of a reference state + FP32 sums of a small change = the FP64 residual."""
+    from tramonto_gb300 import native
+    z, p = load("fmt1_wca_3d")
+    s = native.Solver(p)
+    x0 = z["x0"]
+    rng = np.random.default_rng(5)
+    x1 = x0 * (1.0 + 1e-4 * rng.uniform(-1, 1, x0.shape))
+    R64 = s.fill(x1)
+    s.set_fill_arithmetic(native.FILL_REFINED, tau=1e-3)
+    s.fill(x0)                         # sets the FP64 reference
+    s.reset_stats()
+    Rref = s.fill(x1)                  # change 1e-4 < tau: FP32 sums of the change only
+    st = s.stats()
+    s.set_fill_arithmetic(native.FILL_FP32)
+    R32 = s.fill(x1)
+    s.close()
+    assert st["fp64_refreshes"] == 0
+    assert np.abs(Rref - R64).max() <= 1e-10, np.abs(Rref - R64).max()
+    assert np.abs(R32 - R64).max() > np.abs(Rref - R64).max()
+
+
+@pytest.mark.parametrize("fill", ["fp64", "refined"])
+def test_mixed_newton_matches_fp64_solution(fill):
     from tramonto_gb300 import native, setup
     p, meta = setup.config2(n=40)
     s = native.Solver(p, precision=native.FP64)
     x0 = setup.initial_state(s, p)
     x64, it64, r64 = s.newton(x0, max_iter=40, lin_tol=1e-8, lin_max_iter=300)
     s.set_precision(native.FP32)
+    if fill == "refined":
+        s.set_fill_arithmetic(native.FILL_REFINED)
     x32, it32, r32 = s.newton(x0, max_iter=40, lin_tol=1e-6, lin_max_iter=300)
+    s.set_fill_arithmetic(native.FILL_FP64)
     R = s.fill(x32, mode=1)
     s.close()
     rho64, rho32 = x64[0], x32[0]

@@ -126,6 +126,12 @@ struct Ctx : tgpu_ctx {
   double *d_ymf = nullptr;
   double *d_b2s = nullptr;
   long n2 = 0;
+  // residual arithmetic and the reference state of the refined fill
+  int fill_mode = TGPU_FILL_FP64;
+  double refine_tau = 1e-3, refine_switch = 1e-3;
+  bool have_ref = false;
+  double *d_rho_ref = nullptr, *d_conv_ref = nullptr, *d_chan_ref = nullptr, *d_tr_ref = nullptr;
+  double *d_drho = nullptr, *d_dchan = nullptr;
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -176,26 +182,27 @@ long nnodes(const tgpu_geometry &g)
 
 // ---- stencil passes --------------------------------------------------------
 
-// Pad `nch` channels of `src` with parameter set `pp`.  Residual passes are
-// always FP64; Jacobian/Schur passes use the handle's product precision.
-void pad(Ctx *c, const double *src, const PadParams &pp, bool fp64)
+// Pad `nch` channels of `src` with parameter set `pp`, into the FP32 or the FP64 padded box.
+void pad(Ctx *c, const double *src, const PadParams &pp, bool f32)
 {
-  if (fp64 || c->precision == TGPU_FP64)
+  if (!f32)
     tgpu::launch_pad<double>(src, c->d_pad, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
   else
     tgpu::launch_pad<float>(src, c->d_pad32, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
   c->stats.kernel_launches++;
 }
 
-void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool fp64)
+void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool f32)
 {
   const long NP = c->dg.NP;
-  const bool f32 = !(fp64 || c->precision == TGPU_FP64);
   if (f32 && nin == 1 && nout == 1) {
     const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
-    if (ln.nlines > 0) {
-      tgpu::launch_conv_lines(c->d_pad32 + (long)ch0 * NP, ln.d_lines, ln.d_chunks, ln.nchunks, ln.d_w, outs[0],
-                              c->dg.nx[0], (long)c->dg.nx[1] * c->dg.nx[2], c->stream);
+    if (ln.nplanes > 0) {
+      // the slab loads stay inside this channel and its successors (the buffer has one spare row)
+      const long total = (long)c->nch_max * NP + 64 - (long)ch0 * NP;
+      tgpu::launch_conv_slab(c->d_pad32 + (long)ch0 * NP, total, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w,
+                             outs[0], ln.pitch, ln.ncols, ln.max_rows, ln.max_lines, ln.max_w, c->dg.nx[0],
+                             c->dg.nx[1], c->dg.nx[2], c->stream);
       c->stats.conv_launches++;
       c->stats.kernel_launches++;
       return;
@@ -213,16 +220,16 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
 
 // Weighted-density (and mean-field) sums of a density-shaped field
 // (`field` points at the first density row, rows N apart) into d_conv.
-void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool fp64)
+void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bool zero_first = true)
 {
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
-  ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * (size_t)(g.nrb + g.ncomp) * N, c->stream), "memset");
-  pad(c, field, pp, fp64);
+  if (zero_first) ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * (size_t)(g.nrb + g.ncomp) * N, c->stream), "memset");
+  pad(c, field, pp, f32);
   const int nd = g.ndim;
   for (int jc = 0; jc < g.ncomp; jc++) {
     double *o_th[1] = {c->d_conv};
-    conv(c, jc, 1, c->sten[TGPU_STEN_THETA][jc], false, o_th, 1, fp64);
+    conv(c, jc, 1, c->sten[TGPU_STEN_THETA][jc], false, o_th, 1, f32);
     std::vector<double *> o_de;
     o_de.push_back(c->d_conv + 1 * N);
     if (!g.single_size) {
@@ -232,11 +239,11 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool fp64)
     for (int d = 0; d < nd; d++) o_de.push_back(c->d_conv + (long)(4 + d) * N);
     if (!g.single_size)
       for (int d = 0; d < nd; d++) o_de.push_back(c->d_conv + (long)(4 + nd + d) * N);
-    conv(c, jc, 1, c->sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), fp64);
+    conv(c, jc, 1, c->sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), f32);
     if (g.attraction)
       for (int ic = 0; ic < g.ncomp; ic++) {
         double *o_mf[1] = {c->d_conv + (long)(g.nrb + ic) * N};
-        conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o_mf, 1, fp64);
+        conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o_mf, 1, f32);
       }
   }
   if (g.hard_surf && !c->hw_targets.empty()) {
@@ -248,21 +255,45 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool fp64)
 }
 
 // Euler-Lagrange stencil sums over the channels in d_chan into d_tr.
-void transpose_pass(Ctx *c, const PadParams &pp, bool fp64)
+void transpose_pass(Ctx *c, const PadParams &pp, bool f32, const double *chan = nullptr, bool zero_first = true)
 {
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
   const int nd = g.ndim;
-  ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
-  pad(c, c->d_chan, pp, fp64);
+  if (zero_first) ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+  pad(c, chan ? chan : c->d_chan, pp, f32);
   for (int ic = 0; ic < g.ncomp; ic++) {
     double *o[1] = {c->d_tr + (long)ic * N};
-    conv(c, ic * (nd + 2), 1 + nd, c->sten[TGPU_STEN_DELTA][ic], true, o, 1, fp64);
-    conv(c, ic * (nd + 2) + nd + 1, 1, c->sten[TGPU_STEN_THETA][ic], true, o, 1, fp64);
+    conv(c, ic * (nd + 2), 1 + nd, c->sten[TGPU_STEN_DELTA][ic], true, o, 1, f32);
+    conv(c, ic * (nd + 2) + nd + 1, 1, c->sten[TGPU_STEN_THETA][ic], true, o, 1, f32);
   }
 }
 
-void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
+void red_to_host(Ctx *c, int n);
+
+void ensure_refs(Ctx *c)
+{
+  if (c->d_rho_ref) return;
+  const tgpu::DevGeom &g = c->dg;
+  const size_t N = g.N;
+  c->d_rho_ref = dalloc<double>(g.ncomp * N);
+  c->d_conv_ref = dalloc<double>((g.nrb + g.ncomp) * N);
+  c->d_chan_ref = dalloc<double>((size_t)c->nch_max * N);
+  c->d_tr_ref = dalloc<double>(g.ncomp * N);
+  c->d_drho = dalloc<double>(g.ncomp * N);
+  c->d_dchan = dalloc<double>((size_t)c->nch_max * N);
+}
+
+void copy_d(Ctx *c, double *dst, const double *src, size_t n)
+{
+  ck(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream), "d2d");
+}
+
+// Residual fill.  arith: TGPU_FILL_FP64 sums everything in FP64; TGPU_FILL_FP32
+// sums in FP32 (inexact residual for early Newton steps); TGPU_FILL_REFINED
+// keeps FP64 sums of a reference state and adds FP32 sums of the change since
+// then, refreshing the reference in FP64 when the change exceeds tau of the field.
+void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
 {
   need_final(c);
   const tgpu::DevGeom &g = c->dg;
@@ -270,12 +301,51 @@ void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
   if (d_x != c->d_x && mode == 0)
     ck(cudaMemcpyAsync(c->d_x, d_x, sizeof(double) * (size_t)g.nunk * N, cudaMemcpyDeviceToDevice, c->stream), "copy x");
   const double *x = mode == 0 ? c->d_x : d_x;
-  forward_pass(c, x + (long)g.first_rho * N, c->pads.rho_res, true);
-  tgpu::launch_fmt_local(x, c->d_chan, c->stream);
-  transpose_pass(c, c->pads.tr_res, true);
+  const double *rho = x + (long)g.first_rho * N;
+  const size_t nrho = (size_t)g.ncomp * N, nconv = (size_t)(g.nrb + g.ncomp) * N;
+  const size_t nchan = (size_t)g.ncomp * (g.ndim + 2) * N, ntr = (size_t)g.ncomp * N;
+  if (arith == TGPU_FILL_REFINED) {
+    ensure_refs(c);
+    tgpu::launch_fmt_local(x, c->d_chan, c->stream);
+    bool refresh = !c->have_ref;
+    if (!refresh) {
+      const int nb = tgpu::reduce_blocks((long)nchan);
+      tgpu::launch_delta_maxabs(rho, c->d_rho_ref, (long)nrho, c->d_drho, c->d_partial, nb, c->d_red, c->stream);
+      tgpu::launch_delta_maxabs(c->d_chan, c->d_chan_ref, (long)nchan, c->d_dchan, c->d_partial + 2048, nb,
+                                c->d_red + 2, c->stream);
+      red_to_host(c, 4);
+      const double *m = c->h_red;
+      refresh = !(m[0] <= c->refine_tau * m[1]) || !(m[2] <= c->refine_tau * m[3]);
+    }
+    if (refresh) {
+      forward_pass(c, rho, c->pads.rho_res, false);
+      transpose_pass(c, c->pads.tr_res, false);
+      copy_d(c, c->d_rho_ref, rho, nrho);
+      copy_d(c, c->d_conv_ref, c->d_conv, nconv);
+      copy_d(c, c->d_chan_ref, c->d_chan, nchan);
+      copy_d(c, c->d_tr_ref, c->d_tr, ntr);
+      c->have_ref = true;
+      c->stats.fp64_refreshes++;
+    } else {
+      copy_d(c, c->d_conv, c->d_conv_ref, nconv);
+      forward_pass(c, c->d_drho, c->pads.rho_jac, true, false);
+      copy_d(c, c->d_tr, c->d_tr_ref, ntr);
+      transpose_pass(c, c->pads.tr_jac, true, c->d_dchan, false);
+    }
+  } else {
+    const bool f32 = arith == TGPU_FILL_FP32;
+    forward_pass(c, rho, c->pads.rho_res, f32);
+    tgpu::launch_fmt_local(x, c->d_chan, c->stream);
+    transpose_pass(c, c->pads.tr_res, f32);
+  }
   tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream);
   c->stats.kernel_launches += 2;
   if (mode == 0) c->have_state = true;
+}
+
+void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
+{
+  fill_arith(c, d_x, d_R, mode, c->fill_mode);
 }
 
 void need_state(Ctx *c)
@@ -287,9 +357,10 @@ void need_state(Ctx *c)
 void schur_device(Ctx *c, const double *d_v2, double *d_y2)
 {
   need_state(c);
-  forward_pass(c, d_v2, c->pads.rho_jac, false);
+  const bool f32 = c->precision == TGPU_FP32;
+  forward_pass(c, d_v2, c->pads.rho_jac, f32);
   tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, c->stream);
-  transpose_pass(c, c->pads.tr_jac, false);
+  transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, d_v2, c->d_tr, c->d_ymf, d_y2, c->stream);
   c->stats.kernel_launches += 2;
   c->stats.schur_applies++;
@@ -299,9 +370,10 @@ void jv_device(Ctx *c, const double *d_v, double *d_out)
 {
   need_state(c);
   const long N = c->dg.N;
-  forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, false);
+  const bool f32 = c->precision == TGPU_FP32;
+  forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, f32);
   tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, c->stream);
-  transpose_pass(c, c->pads.tr_jac, false);
+  transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_jv_combine(c->d_x, c->d_vext, c->d_zero, d_v, c->d_conv, c->d_tr, d_out, c->stream);
   c->stats.kernel_launches += 2;
 }
@@ -322,7 +394,7 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
 {
   need_state(c);
   tgpu::launch_rhs_local(c->d_x, d_b, c->d_chan, c->d_ymf, c->stream);
-  transpose_pass(c, c->pads.tr_jac, false);
+  transpose_pass(c, c->pads.tr_jac, c->precision == TGPU_FP32);
   tgpu::launch_rhs_combine(c->d_vext, c->d_zero, d_b, c->d_tr, c->d_ymf, d_b2s, c->stream);
   c->stats.kernel_launches += 2;
 }
@@ -330,7 +402,7 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
 void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx)
 {
   need_state(c);
-  forward_pass(c, d_x2, c->pads.rho_jac, false);
+  forward_pass(c, d_x2, c->pads.rho_jac, c->precision == TGPU_FP32);
   tgpu::launch_x1(d_b, c->d_conv, d_x2, d_dx, c->stream);
   c->stats.kernel_launches++;
 }
@@ -473,12 +545,18 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
   bool converged = false;
   double rnorm = 0.0;
   int st = TGPU_OK;
+  // With the refined residual, iterations far from the solution use FP32 sums;
+  // once ||R|| falls below refine_switch the residual is FP64-accurate.
+  double rprev = 1e300;
   while (it < max_iter && !converged) {
     it++;
-    fill_device(c, d_x, d_R, 0);
+    int arith = c->fill_mode;
+    if (arith == TGPU_FILL_REFINED && rprev > c->refine_switch) arith = TGPU_FILL_FP32;
+    fill_arith(c, d_x, d_R, 0, arith);
     tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
     red_to_host(c, 1);
     rnorm = std::sqrt(c->h_red[0]);
+    rprev = rnorm;
     if (!std::isfinite(rnorm)) throw Error(TGPU_ERR_NONFINITE, "non-finite residual in Newton");
     // b = -R (the reference's rhs)
     tgpu::launch_scale(d_R, d_R, -1.0, n, c->stream);
@@ -497,7 +575,14 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
     c->stats.kernel_launches += 6;
   }
   *iters = it;
-  if (final_resid) *final_resid = rnorm;
+  if (final_resid) {
+    // residual of the returned state, with the accurate arithmetic of the handle
+    fill_arith(c, d_x, d_R, 1, c->fill_mode == TGPU_FILL_FP32 ? TGPU_FILL_FP32 : c->fill_mode);
+    tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    rnorm = std::sqrt(c->h_red[0]);
+    *final_resid = rnorm;
+  }
   (void)st;
   return converged ? TGPU_OK : TGPU_ERR_NOCONV;
 }
@@ -513,44 +598,50 @@ void d2h(Ctx *c, double *h, const double *d, size_t n)
   ck(cudaStreamSynchronize(c->stream), "sync");
 }
 
-// Regroup a 3-D stencil into x-lines of constant (oy, oz) for the FP32 line kernel.
+// Regroup a 3-D stencil by z offset into x-lines of constant oy for the FP32
+// slab kernel: per plane {first line, count, first weight, weight count} and
+// {oz, oy_lo, oy_hi, 0}; per line {oy - oy_lo, ox_min + h0, blocks of 8, weight offset}.
 DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &coef, const tgpu::DevGeom &dg,
                               cudaStream_t s)
 {
-  const int TX = tgpu::kLineTX;
-  std::map<std::pair<int, int>, std::vector<std::pair<int, double>>> groups;
+  std::map<int, std::map<int, std::vector<std::pair<int, double>>>> planes;
   for (int k = 0; k < st.L; k++) {
     const short *o = &st.off[(size_t)k * 3];
-    groups[{o[2], o[1]}].push_back({o[0], coef[k]});
+    planes[o[2]][o[1]].push_back({o[0], coef[k]});
   }
-  std::vector<int4> lines, chunks;
+  std::vector<int4> pd, lines;
   std::vector<float> w;
-  int chunk_first = 0, chunk_w0 = 0;
-  for (auto &gkv : groups) {
-    int xmin = 1 << 30, xmax = -(1 << 30);
-    for (auto &e : gkv.second) { xmin = std::min(xmin, e.first); xmax = std::max(xmax, e.first); }
-    const int len = xmax - xmin + 1;
-    const int nb = (len + TX - 1) / TX;
-    if (nb * TX > tgpu::kLineWChunkMax) throw Error(TGPU_ERR_UNSUPPORTED, "stencil line longer than the chunk");
-    const int nl_in_chunk = (int)lines.size() - chunk_first;
-    if (nl_in_chunk == tgpu::kLineChunkMax || (int)w.size() + nb * TX - chunk_w0 > tgpu::kLineWChunkMax) {
-      chunks.push_back({chunk_first, nl_in_chunk, chunk_w0, (int)w.size() - chunk_w0});
-      chunk_first = (int)lines.size();
-      chunk_w0 = (int)w.size();
-    }
-    const long loff = xmin + (long)gkv.first.second * dg.pstride[1] + (long)gkv.first.first * dg.pstride[2];
-    lines.push_back({(int)loff, nb, (int)w.size(), 0});
-    const size_t base = w.size();
-    w.resize(base + (size_t)nb * TX, 0.0f);
-    for (auto &e : gkv.second) w[base + (e.first - xmin)] = (float)e.second;
-  }
-  if ((int)lines.size() > chunk_first)
-    chunks.push_back({chunk_first, (int)lines.size() - chunk_first, chunk_w0, (int)w.size() - chunk_w0});
   DevStencil::Lines L;
-  L.nlines = (int)lines.size();
-  L.nchunks = (int)chunks.size();
+  for (auto &pkv : planes) {
+    const int oz = pkv.first;
+    const int oy_lo = pkv.second.begin()->first, oy_hi = pkv.second.rbegin()->first;
+    const int first_line = (int)lines.size(), first_w = (int)w.size();
+    for (auto &ykv : pkv.second) {
+      int xmin = 1 << 30, xmax = -(1 << 30);
+      for (auto &e : ykv.second) { xmin = std::min(xmin, e.first); xmax = std::max(xmax, e.first); }
+      const int nb = (xmax - xmin + 1 + 7) / 8;
+      lines.push_back({ykv.first - oy_lo, xmin + dg.h[0], nb, (int)w.size()});
+      const size_t base = w.size();
+      w.resize(base + (size_t)nb * 8, 0.0f);
+      for (auto &e : ykv.second) w[base + (e.first - xmin)] = (float)e.second;
+    }
+    const int nl = (int)lines.size() - first_line, nw = (int)w.size() - first_w;
+    pd.push_back({first_line, nl, first_w, nw});
+    pd.push_back({oz, oy_lo, oy_hi, 0});
+    L.max_rows = std::max(L.max_rows, tgpu::kSlabTileY + oy_hi - oy_lo);
+    L.max_lines = std::max(L.max_lines, nl);
+    L.max_w = std::max(L.max_w, nw);
+  }
+  // columns: 128 outputs + 2 h0 halo + 16 for the window overrun of the last block of 8
+  L.ncols = tgpu::kSlabTileX + 2 * dg.h[0] + 16;
+  int pitch = L.ncols + (L.ncols >> 3) + 1;
+  while (pitch % 32 != 16) pitch++;
+  L.pitch = pitch;
+  const size_t smem = sizeof(float) * ((size_t)L.max_rows * pitch + L.max_w) + sizeof(int4) * L.max_lines;
+  if (smem > 200 * 1024) throw Error(TGPU_ERR_UNSUPPORTED, "stencil plane too large for the shared-memory slab");
+  L.nplanes = (int)planes.size();
+  L.d_planes = upload(pd, s);
   L.d_lines = upload(lines, s);
-  L.d_chunks = upload(chunks, s);
   L.d_w = upload(w, s);
   return L;
 }
@@ -827,13 +918,15 @@ int tgpu_destroy(tgpu_handle h)
       for (auto &st : c->sten[t]) {
         dfree(st.d_loff); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
         dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32);
-        for (auto *L : {&st.lines_fwd, &st.lines_tr}) { dfree(L->d_lines); dfree(L->d_chunks); dfree(L->d_w); }
+        for (auto *L : {&st.lines_fwd, &st.lines_tr}) { dfree(L->d_planes); dfree(L->d_lines); dfree(L->d_w); }
       }
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);
     dfree(c->d_x); dfree(c->d_work); dfree(c->d_work2); dfree(c->d_pad); dfree(c->d_pad32); dfree(c->d_chan);
     dfree(c->d_conv); dfree(c->d_tr); dfree(c->d_ymf); dfree(c->d_b2s); dfree(c->d_V); dfree(c->d_partial);
     dfree(c->d_red); dfree(c->d_gw); dfree(c->d_gt); dfree(c->d_gx); dfree(c->d_gb);
+    dfree(c->d_rho_ref); dfree(c->d_conv_ref); dfree(c->d_chan_ref); dfree(c->d_tr_ref);
+    dfree(c->d_drho); dfree(c->d_dchan);
     if (c->h_red) cudaFreeHost(c->h_red);
     free_pad(c->pads.rho_res); free_pad(c->pads.rho_jac); free_pad(c->pads.tr_res); free_pad(c->pads.tr_jac);
     if (c->own_stream) cudaStreamDestroy(c->stream);
@@ -934,6 +1027,20 @@ int tgpu_set_precision(tgpu_handle h, int precision)
     Ctx *c = C(h);
     if (precision != TGPU_FP64 && precision != TGPU_FP32) throw Error(TGPU_ERR_UNSUPPORTED, "precision");
     c->precision = precision;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (arith != TGPU_FILL_FP64 && arith != TGPU_FILL_FP32 && arith != TGPU_FILL_REFINED)
+      throw Error(TGPU_ERR_ARG, "fill arithmetic");
+    if (tau > 0) c->refine_tau = tau;
+    if (switch_norm > 0) c->refine_switch = switch_norm;
+    c->fill_mode = arith;
+    c->have_ref = false;
     return TGPU_OK;
   });
 }

@@ -201,61 +201,84 @@ void launch_conv<float>(const float *in, long cstride, int nin, const int *loff,
 // loaded serves TX multiply-adds.  Line partial sums are combined with a
 // compensated (Kahan) sum so the FP32 result keeps ~1e-7 relative accuracy
 // over the ~10^5-point attraction stencil.
-constexpr int kTX = 8;
-constexpr int kLineChunk = 256;
-constexpr int kWChunk = 8192;
+// ---------------------------------------------------------------------------
+// FP32 single-channel stencil sums in 3-D through shared-memory slabs.
+//
+// A block owns a 128 (x) by 16 (y) tile of outputs in one z plane; a thread
+// owns 8 consecutive x outputs of one row.  The stencil is grouped by its z
+// offset oz, and within a plane into x-lines of constant oy (contiguous ox
+// runs, zero-padded to a multiple of 8).  For each oz the block copies the
+// input slab it needs (rows y0+oy_lo .. y0+15+oy_hi, columns x0-h .. x0+127+h+16
+// of plane z+oz of the padded box) into shared memory once, then every thread
+// slides a 16-value register window along each line, so one shared-memory
+// load feeds 8 multiply-adds.  Shared rows insert one padding word after
+// every 8 and use a pitch of 16 mod 32 words, which makes the window loads of
+// a warp (16 threads 8 words apart, two rows) hit 32 distinct banks.
+// Line sums are combined with a compensated (Kahan) sum.
+constexpr int kSlabTX = 128, kSlabTY = 16, kSlabThreads = 256;
 
-// lines[l] = {linear offset of the run start from the output, blocks of kTX, weight offset, 0}
-// chunks[c] = {first line, line count, first weight, weight count}; a chunk fits in shared memory.
-__global__ void __launch_bounds__(128) k_conv_lines(const float *__restrict__ in, const int4 *__restrict__ lines,
-                                                   const int4 *__restrict__ chunks, int nchunks,
-                                                   const float *__restrict__ lw, double *__restrict__ out, int nxb)
+__device__ __forceinline__ int slab_phys(int c) { return c + (c >> 3); }
+
+__global__ void __launch_bounds__(kSlabThreads) k_conv_slab(const float *__restrict__ in, long in_total,
+                                                          const int4 *__restrict__ planes, int nplanes,
+                                                          const int4 *__restrict__ lines,
+                                                          const float *__restrict__ lw, double *__restrict__ out,
+                                                          int pitch, int ncols, int max_rows, int max_lines,
+                                                          int max_w)
 {
-  __shared__ int4 s_line[kLineChunk];
-  __shared__ float s_w[kWChunk];
-  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const long nthr = (long)nxb * c_g.nx[1] * c_g.nx[2];
-  const bool active = t < nthr;
-  const int xb = (int)(t % nxb);
-  const long r = t / nxb;
-  const int y = (int)(r % c_g.nx[1]);
-  const int z = (int)(r / c_g.nx[1]);
-  const int x0 = xb * kTX;
-  const long ip0 = (long)(x0 + c_g.h[0]) + c_g.pstride[1] * (y + c_g.h[1]) + c_g.pstride[2] * (z + c_g.h[2]);
-  float sum[kTX], comp[kTX];
+  extern __shared__ float smem[];
+  float *s_slab = smem;                                        // [max_rows][pitch]
+  float *s_w = s_slab + (size_t)max_rows * pitch;              // [max_w]
+  int4 *s_line = reinterpret_cast<int4 *>(s_w + max_w);       // [max_lines]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int x0 = blockIdx.x * kSlabTX, y0 = blockIdx.y * kSlabTY, z = blockIdx.z;
+  const int hx = c_g.h[0];
+  float sum[8], comp[8];
 #pragma unroll
-  for (int o = 0; o < kTX; o++) { sum[o] = 0.f; comp[o] = 0.f; }
-  for (int ci = 0; ci < nchunks; ci++) {
-    const int4 ch = chunks[ci];
+  for (int o = 0; o < 8; o++) { sum[o] = 0.f; comp[o] = 0.f; }
+  for (int pi = 0; pi < nplanes; pi++) {
+    const int4 pd = planes[2 * pi];        // {first line, line count, first weight, weight count}
+    const int4 pg = planes[2 * pi + 1];    // {oz, oy_lo, oy_hi, 0}
+    const int nrows = kSlabTY + pg.z - pg.y;
     __syncthreads();
-    for (int k = threadIdx.x; k < ch.y; k += blockDim.x) s_line[k] = lines[ch.x + k];
-    for (int k = threadIdx.x; k < ch.w; k += blockDim.x) s_w[k] = lw[ch.z + k];
+    for (int k = threadIdx.x; k < pd.y; k += kSlabThreads) s_line[k] = lines[pd.x + k];
+    for (int k = threadIdx.x; k < pd.w; k += kSlabThreads) s_w[k] = lw[pd.z + k];
+    // padded-box coordinates of the slab origin: x0 - hx + hx = x0, row y0 + oy_lo + h1, plane z + oz + h2
+    const long gz = (long)(z + pg.x + c_g.h[2]) * c_g.pstride[2];
+    for (int e = threadIdx.x; e < nrows * ncols; e += kSlabThreads) {
+      const int r = e / ncols, cidx = e - r * ncols;
+      const int gy = y0 + pg.y + r + c_g.h[1];
+      const long gi = gz + (long)gy * c_g.pstride[1] + x0 + cidx;
+      float v = 0.f;
+      if (gy < c_g.P[1] && gi < in_total) v = __ldg(in + gi);
+      s_slab[r * pitch + slab_phys(cidx)] = v;
+    }
     __syncthreads();
-    if (!active) continue;
-    for (int li = 0; li < ch.y; li++) {
-      const int4 ln = s_line[li];
-      const float *src = in + ip0 + ln.x;
-      const float *w = s_w + (ln.z - ch.z);
-      float acc[kTX];
+    for (int li = 0; li < pd.y; li++) {
+      const int4 ln = s_line[li];          // {row offset oy - oy_lo, first column ox_min + hx, blocks of 8, weight offset}
+      const float *row = s_slab + (ty + ln.x) * pitch;
+      const float *w = s_w + (ln.w - pd.z);
+      const int c0 = 8 * tx + ln.y;
+      float acc[8];
 #pragma unroll
-      for (int o = 0; o < kTX; o++) acc[o] = 0.f;
-      float win[2 * kTX];
+      for (int o = 0; o < 8; o++) acc[o] = 0.f;
+      float win[16];
 #pragma unroll
-      for (int q = 0; q < kTX; q++) win[q] = __ldg(src + q);
-      for (int kb = 0; kb < ln.y; kb++) {
+      for (int q = 0; q < 8; q++) win[q] = row[slab_phys(c0 + q)];
+      for (int kb = 0; kb < ln.z; kb++) {
 #pragma unroll
-        for (int q = 0; q < kTX; q++) win[kTX + q] = __ldg(src + (kb + 1) * kTX + q);
+        for (int q = 0; q < 8; q++) win[8 + q] = row[slab_phys(c0 + 8 * (kb + 1) + q)];
 #pragma unroll
-        for (int kk = 0; kk < kTX; kk++) {
-          const float wk = w[kb * kTX + kk];
+        for (int kk = 0; kk < 8; kk++) {
+          const float wk = w[8 * kb + kk];
 #pragma unroll
-          for (int o = 0; o < kTX; o++) acc[o] = fmaf(wk, win[o + kk], acc[o]);
+          for (int o = 0; o < 8; o++) acc[o] = fmaf(wk, win[o + kk], acc[o]);
         }
 #pragma unroll
-        for (int q = 0; q < kTX; q++) win[q] = win[kTX + q];
+        for (int q = 0; q < 8; q++) win[q] = win[8 + q];
       }
 #pragma unroll
-      for (int o = 0; o < kTX; o++) {   // compensated accumulation of the line sums
+      for (int o = 0; o < 8; o++) {
         const float yv = acc[o] - comp[o];
         const float tv = sum[o] + yv;
         comp[o] = (tv - sum[o]) - yv;
@@ -263,20 +286,31 @@ __global__ void __launch_bounds__(128) k_conv_lines(const float *__restrict__ in
       }
     }
   }
-  if (active) {
-    const long i0 = x0 + (long)c_g.nx[0] * (y + (long)c_g.nx[1] * z);
+  (void)hx;
+  const int y = y0 + ty;
+  if (y < c_g.nx[1]) {
+    const long i0 = (long)c_g.nx[0] * (y + (long)c_g.nx[1] * z);
 #pragma unroll
-    for (int o = 0; o < kTX; o++)
-      if (x0 + o < c_g.nx[0]) out[i0 + o] += (double)sum[o];
+    for (int o = 0; o < 8; o++) {
+      const int x = x0 + 8 * tx + o;
+      if (x < c_g.nx[0]) out[i0 + x] += (double)sum[o];
+    }
   }
 }
 
-void launch_conv_lines(const float *in, const int4 *lines, const int4 *chunks, int nchunks, const float *lw,
-                       double *out, int nx0, long ny_nz, cudaStream_t s)
+void launch_conv_slab(const float *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
+                      const float *lw, double *out, int pitch, int ncols, int max_rows, int max_lines, int max_w,
+                      int nx, int ny, int nz, cudaStream_t s)
 {
-  const int nxb = (nx0 + kTX - 1) / kTX;
-  const long nthr = (long)nxb * ny_nz;
-  k_conv_lines<<<(unsigned)((nthr + 127) / 128), 128, 0, s>>>(in, lines, chunks, nchunks, lw, out, nxb);
+  const size_t smem = sizeof(float) * ((size_t)max_rows * pitch + max_w) + sizeof(int4) * max_lines;
+  static size_t configured = 0;
+  if (smem > configured) {
+    cudaFuncSetAttribute(k_conv_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 grid((nx + kSlabTX - 1) / kSlabTX, (ny + kSlabTY - 1) / kSlabTY, nz);
+  k_conv_slab<<<grid, kSlabThreads, smem, s>>>(in, in_total, planes, nplanes, lines, lw, out, pitch, ncols, max_rows,
+                                                max_lines, max_w);
 }
 
 // ---------------------------------------------------------------------------
@@ -1001,6 +1035,49 @@ void launch_norm2(const double *x, long n, double *partial, int nblocks, double 
 {
   k_norm2<<<nblocks, kThreads, 0, s>>>(x, n, partial);
   k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
+}
+
+// out = a - ref; result[0] = max |a - ref|, result[1] = max |a|
+__global__ void k_delta_maxabs(const double *__restrict__ a, const double *__restrict__ ref, long n,
+                               double *__restrict__ out, double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  double m0 = 0.0, m1 = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double d = a[i] - ref[i];
+    out[i] = d;
+    m0 = fmax(m0, fabs(d));
+    m1 = fmax(m1, fabs(a[i]));
+  }
+  m0 = -block_min(-m0, sh);
+  m1 = -block_min(-m1, sh);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = m0;
+    partial[gridDim.x + blockIdx.x] = m1;
+  }
+}
+
+__global__ void k_max_final2(const double *__restrict__ partial, int nb, double *__restrict__ out)
+{
+  __shared__ double sh[32];
+  double m0 = 0.0, m1 = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    m0 = fmax(m0, partial[b]);
+    m1 = fmax(m1, partial[nb + b]);
+  }
+  m0 = -block_min(-m0, sh);
+  m1 = -block_min(-m1, sh);
+  if (threadIdx.x == 0) {
+    out[0] = m0;
+    out[1] = m1;
+  }
+}
+
+void launch_delta_maxabs(const double *a, const double *ref, long n, double *out, double *partial, int nblocks,
+                         double *result, cudaStream_t s)
+{
+  k_delta_maxabs<<<nblocks, kThreads, 0, s>>>(a, ref, n, out, partial);
+  k_max_final2<<<1, kThreads, 0, s>>>(partial, nblocks, result);
 }
 
 // counts non-finite entries (result = count as double)

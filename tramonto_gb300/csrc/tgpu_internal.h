@@ -54,11 +54,11 @@ struct DevStencil {
   float *d_coef_tr32 = nullptr;
   short *d_off = nullptr;               // [L][3] raw offsets (boundary corrections)
   double *d_w = nullptr, *d_hw = nullptr;
-  // x-line form for the FP32 single-channel sums (3-D): forward and transpose coefficients
+  // z-plane / x-line form for the FP32 single-channel sums (3-D): forward and transpose coefficients
   struct Lines {
-    int4 *d_lines = nullptr, *d_chunks = nullptr;
+    int4 *d_planes = nullptr, *d_lines = nullptr;
     float *d_w = nullptr;
-    int nlines = 0, nchunks = 0;
+    int nplanes = 0, max_rows = 0, max_lines = 0, max_w = 0, ncols = 0, pitch = 0;
   } lines_fwd, lines_tr;
 };
 
@@ -124,9 +124,10 @@ void launch_pad(const double *src, T *dst, int nch, const double *bulk, const in
 template <typename T>
 void launch_conv(const T *in, long in_cstride, int nin, const int *loff, const T *coef, int L, double *const *out,
                  int nout, bool accumulate, long N, cudaStream_t s);
-void launch_conv_lines(const float *in, const int4 *lines, const int4 *chunks, int nchunks, const float *lw,
-                       double *out, int nx0, long ny_nz, cudaStream_t s);
-constexpr int kLineTX = 8, kLineChunkMax = 256, kLineWChunkMax = 8192;
+void launch_conv_slab(const float *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
+                      const float *lw, double *out, int pitch, int ncols, int max_rows, int max_lines, int max_w,
+                      int nx, int ny, int nz, cudaStream_t s);
+constexpr int kSlabTileX = 128, kSlabTileY = 16;
 void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
                      const double *tr, double *R, cudaStream_t s);
@@ -153,6 +154,8 @@ void launch_newton_frac(const double *x, const double *dx, double floor_frac, do
 void launch_newton_update(double *x, const double *dx, double frac, double rel, double abs, double *partial,
                           int nblocks, double *result, cudaStream_t s);
 void launch_norm2(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s);
+void launch_delta_maxabs(const double *a, const double *ref, long n, double *out, double *partial, int nblocks,
+                         double *result, cudaStream_t s);
 void launch_check_finite(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s);
 
 int reduce_blocks(long n);

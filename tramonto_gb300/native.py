@@ -29,6 +29,7 @@ from .problem import Problem
 
 TGPU_OK = 0
 FP64, FP32, BF16X3 = 0, 1, 2
+FILL_FP64, FILL_FP32, FILL_REFINED = 0, 1, 2
 STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
           -5: "no convergence", -6: "non-finite values", -7: "domain error"}
 
@@ -52,7 +53,8 @@ class Geometry(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("fill_ms", C.c_double), ("schur_ms", C.c_double), ("conv_ms", C.c_double), ("gmres_ms", C.c_double),
-                ("schur_applies", C.c_long), ("conv_launches", C.c_long), ("kernel_launches", C.c_long)]
+                ("schur_applies", C.c_long), ("conv_launches", C.c_long), ("kernel_launches", C.c_long),
+                ("fp64_refreshes", C.c_long)]
 
 
 _LIB = None
@@ -81,6 +83,7 @@ def load(build_if_missing: bool = False):
         "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
+        "tgpu_set_fill_arithmetic": [vp, C.c_int, C.c_double, C.c_double],
         "tgpu_sizes": [vp, C.POINTER(C.c_long), ip, ip],
         "tgpu_fill": [vp, vp, vp, C.c_int], "tgpu_fill_device": [vp, vp, vp, C.c_int],
         "tgpu_jv": [vp, vp, vp], "tgpu_jv_device": [vp, vp, vp],
@@ -178,6 +181,10 @@ class Solver:
 
     def set_precision(self, precision: int):
         _check(self.lib.tgpu_set_precision(self.h, int(precision)), self.lib)
+
+    def set_fill_arithmetic(self, arith: int, tau: float = 0.0, switch_norm: float = 0.0):
+        """Residual arithmetic: FILL_FP64, FILL_FP32 or FILL_REFINED (see include/tramonto_gpu.h)."""
+        _check(self.lib.tgpu_set_fill_arithmetic(self.h, int(arith), float(tau), float(switch_norm)), self.lib)
 
     def set_stream(self, stream_handle: int):
         _check(self.lib.tgpu_set_stream(self.h, C.c_void_p(stream_handle)), self.lib)
