@@ -112,7 +112,7 @@ int tgpu_set_precision(tgpu_handle h, int precision);
  *   TGPU_FILL_REFINED  FP64 sums of a reference state plus FP32 sums of the change since then;
  *                      the reference is refreshed in FP64 when the change exceeds tau times the
  *                      field (max norms).  tgpu_newton uses FP32 sums while ||R|| > switch_norm.
- * tau / switch_norm <= 0 keep the current values (defaults 1e-3 and 1e-3). */
+ * tau / switch_norm <= 0 keep the current values (defaults 1e-2 and 1.0). */
 enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2 };
 int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm);
 int tgpu_set_stream(tgpu_handle h, void *cuda_stream);

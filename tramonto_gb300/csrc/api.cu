@@ -128,7 +128,7 @@ struct Ctx : tgpu_ctx {
   long n2 = 0;
   // residual arithmetic and the reference state of the refined fill
   int fill_mode = TGPU_FILL_FP64;
-  double refine_tau = 1e-3, refine_switch = 1e-3;
+  double refine_tau = 1e-2, refine_switch = 1.0;  // change bound for a carried reference; ||R||_2 below which sums are refined
   bool have_ref = false;
   double *d_rho_ref = nullptr, *d_conv_ref = nullptr, *d_chan_ref = nullptr, *d_tr_ref = nullptr;
   double *d_drho = nullptr, *d_dchan = nullptr;
@@ -331,6 +331,13 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
       forward_pass(c, c->d_drho, c->pads.rho_jac, true, false);
       copy_d(c, c->d_tr, c->d_tr_ref, ntr);
       transpose_pass(c, c->pads.tr_jac, true, c->d_dchan, false);
+      // carry the reference forward: the sums just formed become the reference of the
+      // next fill, so each FP32 sum only covers one Newton update (errors add up as
+      // 1e-7 of the sum of the updates, which shrink quadratically near the solution)
+      copy_d(c, c->d_rho_ref, rho, nrho);
+      copy_d(c, c->d_conv_ref, c->d_conv, nconv);
+      copy_d(c, c->d_chan_ref, c->d_chan, nchan);
+      copy_d(c, c->d_tr_ref, c->d_tr, ntr);
     }
   } else {
     const bool f32 = arith == TGPU_FILL_FP32;
