@@ -5,10 +5,12 @@ Workload (BASELINE configuration 2): 3-D FMT1 + WCA Lennard-Jones fluid
 rho_b=0.6, periodic in y and z, a rough 12-3 LJ wall (eps_w=1, 16x16 patches
 of U(-0.5,0.5) sigma heights, seeded) on the low-x side, bulk on the high-x side.
 
-A step is one Newton iteration: the FP64 residual fill, the Schur-complement
-GMRES solve (Schur products in FP32: the mixed-precision form; in FP64 for the
-plain form) and the damped update.  W warm-up iterations start from the
-initial state; K timed iterations follow.  The inputs (12 unknowns x 128^3
+A step is one Newton solve from the initial state (rho_b exp(-V) with its own
+weighted densities) to ||R||_2 <= 1e-8: residual fills (FP32 stencil sums while
+||R||_2 > 0.1, FP64 after), Schur-complement GMRES with FP32 stencil sums in
+the products (inexact Newton, Eisenstat-Walker tolerances) and the damped
+update.  The value is Newton iterations per second over the K timed solves; the
+plain FP64 path (FP64 residual and products) is timed per iteration beside it.  The inputs (12 unknowns x 128^3
 doubles = 201 MB, plus the 200+ MB of padded fields) exceed the 129 MB L2, so
 no explicit flush is done between steps.
 
@@ -31,7 +33,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "Newton iterations/s, 128^3 FMT1+WCA fill + Schur-GMRES solve (mixed FP32 products, FP64 residual)"
+METRIC = ("Newton iterations/s of a mixed-precision solve to ||R||_2 <= 1e-8, 128^3 FMT1+WCA "
+          "(FP32 stencil sums in the Schur products, FP64 residual)")
 UNIT = "Newton iter/s"
 WORKLOAD = "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall, periodic y,z"
 
@@ -39,13 +42,16 @@ WORKLOAD = "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall,
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--lin-tol", type=float, default=1e-6)
     ap.add_argument("--lin-maxit", type=int, default=200)
+    ap.add_argument("--resid-tol", type=float, default=1e-8)
+    ap.add_argument("--max-newton", type=int, default=40)
+    ap.add_argument("--switch", type=float, default=0.1)
     ap.add_argument("--cpu-sample-planes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -198,43 +204,61 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     from tramonto_gb300 import native, setup
+    from tramonto_gb300.problem import DELTA, THETA, UATT
     t_setup = time.perf_counter()
     p, meta = setup.config2(n=args.n)
     s = native.Solver(p, device=local, precision=native.FP32)
-    s.set_fill_arithmetic(native.FILL_REFINED)
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
     x0 = setup.initial_state(s, p)
     t_setup = time.perf_counter() - t_setup
     n = p.nunk * p.nnodes
-    dx = torch.from_numpy(x0).to("cuda").contiguous()
-    # warm-up (mixed)
-    it_total = 0
+    x0_dev = torch.from_numpy(x0).to("cuda").contiguous()
+    dx = torch.empty_like(x0_dev)
+
+    def mixed_mode():
+        s.set_precision(native.FP32)
+        s.set_fill_arithmetic(native.FILL_MIXED, switch_norm=args.switch)
+
+    def solve():
+        dx.copy_(x0_dev)
+        return s.newton_solve_device(dx, resid_tol=args.resid_tol, max_iter=args.max_newton, lin_tol=args.lin_tol,
+                                     lin_max_iter=args.lin_maxit, allow_noconv=True)
+
+    mixed_mode()
     for _ in range(args.warmup):
-        s.newton_device(dx, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+        solve()
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     s.reset_stats()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    gm = []
+    iters = lin_iters = 0
+    final_r = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(args.steps):
-            s.newton_device(dx, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+            it, rn, li = solve()
+            iters += it
+            lin_iters += li
+            final_r.append(rn)
         e1.record(stream)
         torch.cuda.synchronize()
     st = s.stats()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms_total = e0.elapsed_time(e1)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
+        t = torch.tensor([ms_total], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    applies_per_step = st["schur_applies"] / args.steps
-    value = world * 1e3 / ms
-    # per-kernel-family timing: one fill and one Schur product, FP64 and FP32
+        ms_total = float(t.item())
+    ms_per_solve = ms_total / args.steps
+    ms_per_iter = ms_total / max(1, iters)
+    value = world * max(1, iters) / (ms_total * 1e-3)
+    x_mixed = dx.clone()
+
+    # kernel-family timings at the converged state
     R = torch.empty_like(dx)
+    s.set_fill_arithmetic(native.FILL_FP64)
     v2 = torch.randn(p.ncomp * p.nnodes, dtype=torch.float64, device="cuda")
     y2 = torch.empty_like(v2)
 
@@ -249,21 +273,24 @@ def main():
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    s.set_fill_arithmetic(native.FILL_FP64)
-    t_fill = timed(lambda: s.fill_device(dx, R, 0))
+    t_fill = timed(lambda: s.fill_device(x_mixed, R, 0))
     s.set_fill_arithmetic(native.FILL_FP32)
-    t_fill32 = timed(lambda: s.fill_device(dx, R, 0))
+    t_fill32 = timed(lambda: s.fill_device(x_mixed, R, 0))
     s.set_precision(native.FP32)
     t_apply32 = timed(lambda: s.schur_device(v2, y2), reps=5)
     s.set_precision(native.FP64)
     t_apply64 = timed(lambda: s.schur_device(v2, y2), reps=2)
-    # plain FP64 Newton iterations from the same state
+    # dominant kernel: the FP32 attraction (WCA) stencil sum of the Schur products
+    t_wca32 = s.time_stencil_sum(UATT, 0, native.FP32, reps=5)
+    t_wca64 = s.time_stencil_sum(UATT, 0, native.FP64, reps=1)
+    L_att = len(p.stencils[(UATT, 0)][1])
+    flops_att = 2.0 * p.nnodes * L_att
+    # plain FP64 Newton iterations (FP64 residual and FP64 Schur products) from the initial state
     s.set_fill_arithmetic(native.FILL_FP64)
     fp64_ms = None
     if args.fp64_steps > 0:
-        dx64 = torch.from_numpy(x0).to("cuda").contiguous()
-        for _ in range(min(1, args.warmup)):
-            s.newton_device(dx64, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+        dx64 = x0_dev.clone()
+        s.newton_device(dx64, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         a.record(stream)
@@ -273,45 +300,49 @@ def main():
         torch.cuda.synchronize()
         fp64_ms = a.elapsed_time(b) / args.fp64_steps
         del dx64
-    s.set_precision(native.FP32)
-    s.set_fill_arithmetic(native.FILL_REFINED)
-    # end to end through the C ABI with host buffers (copies inside the timed region)
-    xh = dx.cpu().numpy().copy()
+    # end to end through the C ABI with host buffers: copies of the state in and out inside the timed region
+    mixed_mode()
+    xh = x0.copy()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
-        xh, _, _ = s.newton(xh, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
-    flops_apply, flops_att = conv_flops_per_apply(p)
+    _, it_e2e, rn_e2e, _ = s.newton_solve(xh, resid_tol=args.resid_tol, max_iter=args.max_newton,
+                                          lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+    e2e_s = time.perf_counter() - t0
     hbm, bf16, peak_src = peaks()
-    # dominant kernel: the FP64 residual fill's stencil sums (the WCA sum dominates)
-    flops_fill = flops_apply  # same stencil work as one product
-    ach_tf = flops_fill / (t_fill * 1e-3) / 1e12
+    ach_tf = flops_att / (t_wca32 * 1e-3) / 1e12
     if rank == 0:
         cb = None
         if not args.no_cpu_baseline:
-            k = max(1.0, applies_per_step)
-            cb = cpu_baseline(p, dx.cpu().numpy(), k, planes=args.cpu_sample_planes, threads=1)
+            k = max(1.0, lin_iters / max(1, iters))
+            cb = cpu_baseline(p, x_mixed.cpu().numpy(), k, planes=args.cpu_sample_planes, threads=1)
             cb.pop("t_fill_s", None)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 residual, f32 Schur products", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
-                       "rho_b": 0.6, "kT": 1.2, "rcut": 2.5, "lin_tol": args.lin_tol,
-                       "inputs_exceed_l2": True, "l2_flush": "none (working set > L2)"},
+            "warmup": args.warmup, "ms_per_step": ms_per_solve, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 residual near the solution, f32 stencil sums in the Schur products",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "step": "one Newton solve from the initial state to ||R||_2 <= "
+                       f"{args.resid_tol:g}", "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
+                       "rho_b": 0.6, "kT": 1.2, "rcut": 2.5, "lin_tol_floor": args.lin_tol,
+                       "fp32_until_resid": args.switch, "inputs_exceed_l2": True,
+                       "l2_flush": "none (working set > L2)"},
+            "newton_iters_per_step": iters / args.steps, "ms_per_newton_iter": ms_per_iter,
+            "gmres_iters_per_newton_iter": lin_iters / max(1, iters), "final_resid_norm2": max(final_r),
             "gpu_launches": int(st["kernel_launches"]),
             "clocks": clk.summary(),
-            "e2e": {"value": 1e3 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
-            "roofline": {"bound": "tensor", "kernel": "FP64 residual fill (stencil sums, WCA dominant)",
+            "e2e": {"value": it_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
+                    "final_resid_norm2": rn_e2e},
+            "roofline": {"bound": "tensor", "kernel": "FP32 attraction (WCA) stencil sum, k_conv_slab",
                          "achieved": ach_tf, "peak": bf16, "unit": "TFLOP/s", "frac": ach_tf / bf16,
                          "peak_source": f"{peak_src} bf16 dense", "traffic": None,
-                         "note": "stencil sums run on the FP64/FP32 SIMT pipes; tensor roof shown for reference"},
+                         "algorithmic": f"2 x {L_att} stencil points x {p.nnodes} nodes per launch",
+                         "fp32_simt_nominal_tflops": 80.6, "frac_of_fp32_simt_nominal": ach_tf / 80.6,
+                         "ms_per_launch": t_wca32, "fp64_ms_per_launch": t_wca64},
             "cpu_baseline": cb,
             "breakdown_ms": {"fill_fp64": t_fill, "fill_fp32": t_fill32, "schur_apply_fp32": t_apply32,
-                             "schur_apply_fp64": t_apply64, "schur_applies_per_step": applies_per_step,
-                             "fp64_refreshes_in_timed_steps": int(st["fp64_refreshes"])},
-            "plain_fp64": {"ms_per_step": fp64_ms, "speedup_mixed_vs_fp64": (fp64_ms / ms) if fp64_ms else None},
+                             "schur_apply_fp64": t_apply64, "schur_applies_in_timed_steps": int(st["schur_applies"])},
+            "plain_fp64": {"ms_per_newton_iter": fp64_ms,
+                           "speedup_mixed_vs_fp64_per_iter": (fp64_ms / ms_per_iter) if fp64_ms else None},
             "setup_s": t_setup,
         }
         print(json.dumps(out))

@@ -113,7 +113,9 @@ int tgpu_set_precision(tgpu_handle h, int precision);
  *                      the reference is refreshed in FP64 when the change exceeds tau times the
  *                      field (max norms).  tgpu_newton uses FP32 sums while ||R|| > switch_norm.
  * tau / switch_norm <= 0 keep the current values (defaults 1e-2 and 1.0). */
-enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2 };
+enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2, TGPU_FILL_MIXED = 3 };
+/* TGPU_FILL_MIXED: in tgpu_newton_solve, FP32 sums while ||R||_2 > switch_norm, FP64 below;
+ * everywhere else it is the FP64 fill. */
 int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm);
 int tgpu_set_stream(tgpu_handle h, void *cuda_stream);
 int tgpu_sizes(tgpu_handle h, long *nnodes, int *nunk, int *ncomp);
@@ -147,6 +149,17 @@ int tgpu_newton(tgpu_handle h, double *x, double rel_tol, double abs_tol, double
 int tgpu_newton_device(tgpu_handle h, double *d_x, double rel_tol, double abs_tol, double update_floor,
                        int max_iter, double lin_tol, int lin_max_iter, int *iters, double *final_resid_norm);
 
+/* Newton solve to a residual target: iterate until ||R||_2 <= resid_tol, R in
+ * FP64-accurate arithmetic; inexact-Newton GMRES tolerances (Eisenstat-Walker,
+ * floor lin_tol); damped update as update_solution (src/dft_newton.c:266-381).
+ * Returns TGPU_ERR_NOCONV after max_iter iterations.  lin_iters_total: GMRES
+ * iterations summed over the solve. */
+int tgpu_newton_solve(tgpu_handle h, double *x, double resid_tol, int max_iter, double lin_tol, int lin_max_iter,
+                      double update_floor, int *iters, double *final_resid, int *lin_iters_total);
+int tgpu_newton_solve_device(tgpu_handle h, double *d_x, double resid_tol, int max_iter, double lin_tol,
+                             int lin_max_iter, double update_floor, int *iters, double *final_resid,
+                             int *lin_iters_total);
+
 /* ---- set-up helpers (host only, no GPU) ------------------------------------
  * Stencil tables built as calc_stencils (src/dft_stencil.c:40-287) builds
  * Stencil[type][0][index] for the delta shell (DELTA_FN_R), the theta ball
@@ -163,6 +176,11 @@ int tgpu_make_stencil(int type, int ndim, const double *esize, double hs_diam, d
 double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0);
 /* the WCA attraction u_att(r) in kT (uLJ12_6_ATT_CS, src/dft_pairPot_LJ12_6.c:128-168) */
 double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double rmin);
+
+/* Benchmark hook: device time (CUDA events on the handle's stream) of one
+ * forward stencil sum with stencil (type, index) over the density of the last
+ * fill, in TGPU_FP64 or TGPU_FP32, averaged over reps launches. */
+int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum);
 
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */
 typedef struct {

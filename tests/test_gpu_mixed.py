@@ -69,3 +69,24 @@ def test_mixed_newton_matches_fp64_solution(fill):
     err = np.abs(rho32 - rho64).max() / np.abs(rho64).max()
     assert np.abs(R).max() < 1e-8, np.abs(R).max()
     assert err <= 1e-6, (err, it64, it32)
+
+
+def test_mixed_newton_solve_reaches_fp64_residual_target():
+    """Residual-targeted solve: FP32 residual sums far from the solution, FP64 near it,
+    FP32 Schur products throughout; the result must have an FP64 residual <= 1e-8 and
+    match the plain FP64 solve's density to 1e-6."""
+    from tramonto_gb300 import native, setup
+    p, meta = setup.config2(n=40)
+    s = native.Solver(p, precision=native.FP64)
+    x0 = setup.initial_state(s, p)
+    x64, it64, r64, _ = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-10)
+    s.set_precision(native.FP32)
+    s.set_fill_arithmetic(native.FILL_MIXED, switch_norm=0.1)
+    x32, it32, r32, li = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-6)
+    s.set_fill_arithmetic(native.FILL_FP64)
+    R = s.fill(x32, mode=1)
+    s.close()
+    assert r64 <= 1e-8 and r32 <= 1e-8
+    assert np.sqrt((R ** 2).sum()) <= 1e-8
+    err = np.abs(x32[0] - x64[0]).max() / np.abs(x64[0]).max()
+    assert err <= 1e-6, (err, it64, it32)

@@ -132,6 +132,7 @@ struct Ctx : tgpu_ctx {
   bool have_ref = false;
   double *d_rho_ref = nullptr, *d_conv_ref = nullptr, *d_chan_ref = nullptr, *d_tr_ref = nullptr;
   double *d_drho = nullptr, *d_dchan = nullptr;
+  double *d_newton_x = nullptr;   // device copy of the state for the host-pointer Newton solve
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -352,7 +353,8 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
 
 void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
 {
-  fill_arith(c, d_x, d_R, mode, c->fill_mode);
+  // outside the Newton solve the mixed policy means the accurate (FP64) residual
+  fill_arith(c, d_x, d_R, mode, c->fill_mode == TGPU_FILL_MIXED ? TGPU_FILL_FP64 : c->fill_mode);
 }
 
 void need_state(Ctx *c)
@@ -591,6 +593,71 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
     *final_resid = rnorm;
   }
   (void)st;
+  return converged ? TGPU_OK : TGPU_ERR_NOCONV;
+}
+
+// Residual-targeted Newton: iterate until ||R||_2 <= resid_tol with R taken in
+// FP64-accurate arithmetic.  The inexact-Newton linear tolerance follows
+// Eisenstat and Walker's second choice, eta_k = 0.9 (||R_k|| / ||R_k-1||)^2,
+// kept in [lin_tol, 0.1] and not below 0.9 eta_k-1^2 when that exceeds 0.1.
+// Under TGPU_FILL_MIXED (and TGPU_FILL_REFINED) the residual is summed in FP32
+// while ||R||_2 > refine_switch; below it the final iterations use FP64
+// (respectively refined) sums, so the returned residual is FP64-accurate.
+int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, double lin_tol, int lin_max_iter,
+                        double update_floor, int *iters, double *final_resid, int *lin_iters_total)
+{
+  need_final(c);
+  const tgpu::DevGeom &g = c->dg;
+  const long n = (long)g.nunk * g.N;
+  const int nb = tgpu::reduce_blocks(n);
+  double *d_R = c->d_work, *d_dx = c->d_work2;
+  int it = 0, lin_total = 0;
+  double rprev = 1e300, eta = 0.1, rnorm = 1e300;
+  bool converged = false;
+  for (;;) {
+    int arith = c->fill_mode;
+    const bool inexact = (arith == TGPU_FILL_MIXED || arith == TGPU_FILL_REFINED) && rprev > c->refine_switch;
+    if (inexact) arith = TGPU_FILL_FP32;
+    else if (arith == TGPU_FILL_MIXED) arith = TGPU_FILL_FP64;
+    fill_arith(c, d_x, d_R, 0, arith);
+    tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    rnorm = std::sqrt(c->h_red[0]);
+    if (!std::isfinite(rnorm)) throw Error(TGPU_ERR_NONFINITE, "non-finite residual in Newton");
+    if (inexact && rnorm <= c->refine_switch) {
+      rprev = rnorm;   // close enough: redo this residual in the accurate arithmetic
+      continue;
+    }
+    if (!inexact && rnorm <= resid_tol) {
+      converged = true;
+      break;
+    }
+    if (it >= max_iter) break;
+    if (it > 0 && rprev < 1e299) {
+      const double r = rnorm / rprev;
+      double e = 0.9 * r * r;
+      const double safe = 0.9 * eta * eta;
+      if (safe > 0.1) e = std::max(e, safe);
+      eta = std::min(0.1, std::max(e, lin_tol));
+    }
+    it++;
+    rprev = rnorm;
+    tgpu::launch_scale(d_R, d_R, -1.0, n, c->stream);
+    int li = 0;
+    double lr = 0.0;
+    solve_device(c, d_R, d_dx, eta, lin_max_iter, &li, &lr);
+    lin_total += li;
+    tgpu::launch_newton_frac(d_x, d_dx, update_floor, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    const double frac = c->h_red[0];
+    tgpu::launch_newton_update(d_x, d_dx, frac, 1.0, 1.0, c->d_partial, nb, c->d_red, c->stream);
+    red_to_host(c, 1);
+    if (!std::isfinite(c->h_red[0])) throw Error(TGPU_ERR_NONFINITE, "non-finite Newton update");
+    c->stats.kernel_launches += 6;
+  }
+  *iters = it;
+  if (final_resid) *final_resid = rnorm;
+  if (lin_iters_total) *lin_iters_total = lin_total;
   return converged ? TGPU_OK : TGPU_ERR_NOCONV;
 }
 
@@ -834,6 +901,7 @@ void build_device_tables(Ctx *c)
   c->d_tr = dalloc<double>((size_t)dg.ncomp * N);
   c->d_ymf = dalloc<double>((size_t)dg.ncomp * N);
   c->n2 = (long)dg.ncomp * N;
+  c->d_newton_x = dalloc<double>(U * N);
   c->d_b2s = dalloc<double>(c->n2);
   c->d_gw = dalloc<double>(c->n2);
   c->d_gt = dalloc<double>(c->n2);
@@ -933,7 +1001,7 @@ int tgpu_destroy(tgpu_handle h)
     dfree(c->d_conv); dfree(c->d_tr); dfree(c->d_ymf); dfree(c->d_b2s); dfree(c->d_V); dfree(c->d_partial);
     dfree(c->d_red); dfree(c->d_gw); dfree(c->d_gt); dfree(c->d_gx); dfree(c->d_gb);
     dfree(c->d_rho_ref); dfree(c->d_conv_ref); dfree(c->d_chan_ref); dfree(c->d_tr_ref);
-    dfree(c->d_drho); dfree(c->d_dchan);
+    dfree(c->d_drho); dfree(c->d_dchan); dfree(c->d_newton_x);
     if (c->h_red) cudaFreeHost(c->h_red);
     free_pad(c->pads.rho_res); free_pad(c->pads.rho_jac); free_pad(c->pads.tr_res); free_pad(c->pads.tr_jac);
     if (c->own_stream) cudaStreamDestroy(c->stream);
@@ -1042,7 +1110,7 @@ int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch
 {
   return guard([&] {
     Ctx *c = C(h);
-    if (arith != TGPU_FILL_FP64 && arith != TGPU_FILL_FP32 && arith != TGPU_FILL_REFINED)
+    if (arith != TGPU_FILL_FP64 && arith != TGPU_FILL_FP32 && arith != TGPU_FILL_REFINED && arith != TGPU_FILL_MIXED)
       throw Error(TGPU_ERR_ARG, "fill arithmetic");
     if (tau > 0) c->refine_tau = tau;
     if (switch_norm > 0) c->refine_switch = switch_norm;
@@ -1208,6 +1276,73 @@ int tgpu_newton(tgpu_handle h, double *x, double rel_tol, double abs_tol, double
     }
     dfree(d_xs);
     return st;
+  });
+}
+
+int tgpu_newton_solve_device(tgpu_handle h, double *d_x, double resid_tol, int max_iter, double lin_tol,
+                             int lin_max_iter, double update_floor, int *iters, double *final_resid,
+                             int *lin_iters_total)
+{
+  return guard([&] {
+    int it = 0, lt = 0;
+    double fr = 0.0;
+    const int st = newton_solve_device(C(h), d_x, resid_tol, max_iter, lin_tol, lin_max_iter, update_floor, &it, &fr, &lt);
+    if (iters) *iters = it;
+    if (final_resid) *final_resid = fr;
+    if (lin_iters_total) *lin_iters_total = lt;
+    return st;
+  });
+}
+
+int tgpu_newton_solve(tgpu_handle h, double *x, double resid_tol, int max_iter, double lin_tol, int lin_max_iter,
+                      double update_floor, int *iters, double *final_resid, int *lin_iters_total)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_newton_x, x, n);
+    int it = 0, lt = 0;
+    double fr = 0.0;
+    const int st = newton_solve_device(c, c->d_newton_x, resid_tol, max_iter, lin_tol, lin_max_iter, update_floor,
+                                       &it, &fr, &lt);
+    d2h(c, x, c->d_newton_x, n);
+    if (iters) *iters = it;
+    if (final_resid) *final_resid = fr;
+    if (lin_iters_total) *lin_iters_total = lt;
+    return st;
+  });
+}
+
+int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    if (type < 0 || type > 2 || index < 0 || index >= (int)c->sten[type].size() || c->sten[type][index].L == 0)
+      throw Error(TGPU_ERR_ARG, "no such stencil");
+    if (reps < 1) throw Error(TGPU_ERR_ARG, "reps");
+    const bool f32 = precision == TGPU_FP32;
+    const DevStencil &st = c->sten[type][index];
+    const int jc = type == TGPU_STEN_UATT ? index / c->dg.ncomp : index;
+    const long N = c->dg.N;
+    // density of the handle's state (or zeros before any fill) as the field
+    pad(c, c->d_x + (long)c->dg.first_rho * N, c->pads.rho_res, f32);
+    double *out[1] = {c->d_tr};
+    ck(cudaEventCreate(&c->ev0), "event");
+    ck(cudaEventCreate(&c->ev1), "event");
+    conv(c, jc, 1, st, false, out, 1, f32);   // warm-up
+    ck(cudaEventRecord(c->ev0, c->stream), "event");
+    for (int r = 0; r < reps; r++) conv(c, jc, 1, st, false, out, 1, f32);
+    ck(cudaEventRecord(c->ev1, c->stream), "event");
+    ck(cudaEventSynchronize(c->ev1), "event");
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event");
+    cudaEventDestroy(c->ev0);
+    cudaEventDestroy(c->ev1);
+    c->ev0 = c->ev1 = nullptr;
+    *ms_per_sum = ms / reps;
+    return TGPU_OK;
   });
 }
 

@@ -29,7 +29,7 @@ from .problem import Problem
 
 TGPU_OK = 0
 FP64, FP32, BF16X3 = 0, 1, 2
-FILL_FP64, FILL_FP32, FILL_REFINED = 0, 1, 2
+FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED = 0, 1, 2, 3
 STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
           -5: "no convergence", -6: "non-finite values", -7: "domain error"}
 
@@ -94,6 +94,9 @@ def load(build_if_missing: bool = False):
         "tgpu_solve_device": [vp, vp, vp, C.c_double, C.c_int, ip, dp],
         "tgpu_newton": [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, ip, dp],
         "tgpu_newton_device": [vp, vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, ip, dp],
+        "tgpu_newton_solve": [vp, vp, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double, ip, dp, ip],
+        "tgpu_newton_solve_device": [vp, vp, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double, ip, dp, ip],
+        "tgpu_time_stencil_sum": [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp],
         "tgpu_get_stats": [vp, C.POINTER(Stats)], "tgpu_reset_stats": [vp],
     }
     for name, args in sigs.items():
@@ -266,6 +269,30 @@ class Solver:
                                          lin_max_iter, C.byref(it), C.byref(rn))
         _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
         return it.value, rn.value
+
+    def newton_solve(self, x0, resid_tol=1e-8, max_iter=50, lin_tol=1e-8, lin_max_iter=300, update_floor=0.1,
+                     allow_noconv=False):
+        """Newton to ||R||_2 <= resid_tol (host arrays); returns (x, iterations, ||R||_2, GMRES iterations)."""
+        x = np.array(x0, np.float64, copy=True, order="C")
+        it, rn, li = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        st = self.lib.tgpu_newton_solve(self.h, _ptr(x), resid_tol, max_iter, lin_tol, lin_max_iter, update_floor,
+                                        C.byref(it), C.byref(rn), C.byref(li))
+        _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
+        return x, it.value, rn.value, li.value
+
+    def newton_solve_device(self, x, resid_tol=1e-8, max_iter=50, lin_tol=1e-8, lin_max_iter=300,
+                            update_floor=0.1, allow_noconv=False):
+        it, rn, li = C.c_int(0), C.c_double(0.0), C.c_int(0)
+        st = self.lib.tgpu_newton_solve_device(self.h, self._dptr(x), resid_tol, max_iter, lin_tol, lin_max_iter,
+                                               update_floor, C.byref(it), C.byref(rn), C.byref(li))
+        _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
+        return it.value, rn.value, li.value
+
+    def time_stencil_sum(self, stype, index, precision, reps=5) -> float:
+        """Device milliseconds of one forward stencil sum (benchmark hook)."""
+        ms = C.c_double(0.0)
+        _check(self.lib.tgpu_time_stencil_sum(self.h, stype, index, precision, reps, C.byref(ms)), self.lib)
+        return ms.value
 
     def stats(self) -> dict:
         s = Stats()
