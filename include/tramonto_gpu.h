@@ -177,6 +177,34 @@ double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0
 /* the WCA attraction u_att(r) in kT (uLJ12_6_ATT_CS, src/dft_pairPot_LJ12_6.c:128-168) */
 double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double rmin);
 
+/* ---- allocation-free stencil sum -------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory where they need a weighted-density sum: code inside a framework that
+ * owns all device allocations (its buffers come in as pointers and the op may
+ * not call cudaMalloc), or code that must not allocate between two phases of
+ * a larger computation.  Computes, for one density field,
+ *     out[i] = sum_k weights[k] * field(i + offsets[k])
+ * with the reference's boundary rules (src/dft_mesh_lib.c:203-297): bulk
+ * sentinel -> bulk_value, inside a wall -> 0, periodic wrap, mirror for
+ * REFLECT.  d_field and d_out are device arrays of prod(nx) doubles; bc is
+ * [ndim][2] flattened; offsets/weights are host arrays ([length][ndim], [length]).
+ * The padded copy of the field, the boundary maps and the stencil table live in
+ * fixed arrays inside the library (about 18 MB per GPU that loads it, held
+ * until exit): the padded box (nx + 2*reach per dimension, multiplied) may
+ * not exceed TGPU_NOALLOC_MAX_PADDED points, nor the stencil
+ * TGPU_NOALLOC_MAX_STENCIL points, nor any padded extent 4096; larger inputs
+ * return TGPU_ERR_ARG with a message in tgpu_noalloc_last_error().  The first
+ * call on a device looks up the device addresses of those arrays (make that
+ * first call before any stream capture).  Every call shares the arrays and
+ * rewrites what it reads; calls whose work overlaps on the GPU race.  Returns
+ * after the sum is complete on `stream` (NULL: the legacy default stream). */
+#define TGPU_NOALLOC_MAX_PADDED 2097152
+#define TGPU_NOALLOC_MAX_STENCIL 131072
+int tgpu_stencil_sum_noalloc(int ndim, const int *nx, const int *bc, double bulk_value, int length,
+                             const short *offsets, const double *weights, const double *d_field, double *d_out,
+                             void *stream);
+const char *tgpu_noalloc_last_error(void);
+
 /* Benchmark hook: device time (CUDA events on the handle's stream) of one
  * forward stencil sum with stencil (type, index) over the density of the last
  * fill, in TGPU_FP64 or TGPU_FP32, averaged over reps launches. */
