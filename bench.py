@@ -175,7 +175,7 @@ def run_reference(args):
     rho[p.zero_density[0] != 0] = 0.0
     x[0] = rho
     threads = os.cpu_count() or 1
-    k_gmres = 20.0   # GMRES iterations per Newton step of the GPU run (order of magnitude)
+    k_gmres = 7.4    # GMRES iterations per Newton iteration of the GPU solve (bench.py default run)
     steps = []
     for _ in range(max(1, args.steps)):
         cb = cpu_baseline(p, x, k_gmres, planes=max(threads, args.cpu_sample_planes), threads=threads)
