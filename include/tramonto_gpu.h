@@ -130,6 +130,18 @@ int tgpu_jv(tgpu_handle h, const double *v, double *out);
 int tgpu_jv_device(tgpu_handle h, const double *d_v, double *d_out);
 int tgpu_jtv(tgpu_handle h, const double *w, double *out);
 int tgpu_jtv_device(tgpu_handle h, const double *d_w, double *d_out);
+/* Adjoint solve J^T lambda = g ([nunk][N] each) with the Jacobian of the last mode-0 fill: GMRES on the
+ * transposed Schur complement S^T = A22^T - A12^T A11^-T A21^T (A22 as left preconditioner, same stopping
+ * test as tgpu_solve), then lambda1 = A11^-T (g1 - A21^T lambda2).  No reference counterpart (the
+ * reference's operators refuse the transpose, src/dft_HardSphereA11_Epetra_Operator.hpp:68).  With g the
+ * gradient of an objective F(x) at a converged state x*, the sensitivity of F(x*) to a parameter p that
+ * enters the residual is dF/dp = dF/dp|_x - lambda^T dR/dp; for the external field the residual's
+ * Euler-Lagrange rows hold +V_ext, so dF/dV_ext[ic][i] = dF/dV_ext|_x - lambda[ic][i] off zero-density rows.
+ * Reflecting boundaries and hard-wall boundary weights return TGPU_ERR_UNSUPPORTED (also for tgpu_jtv). */
+int tgpu_adjoint_solve(tgpu_handle h, const double *g, double *lambda, double tol, int max_iter, int *iters,
+                       double *relres);
+int tgpu_adjoint_solve_device(tgpu_handle h, const double *d_g, double *d_lambda, double tol, int max_iter,
+                              int *iters, double *relres);
 /* Schur complement on the density block ([ncomp][N] in and out) */
 int tgpu_schur_apply(tgpu_handle h, const double *v2, double *y2);
 int tgpu_schur_apply_device(tgpu_handle h, const double *d_v2, double *d_y2);

@@ -47,3 +47,21 @@ def test_config_generators_are_seeded():
     v2, m2 = setup.rough_wall_vext((48, 16, 16), (0.1, 0.1, 0.1), seed=5)
     assert np.array_equal(v1, v2) and m1 == m2
     assert v1.max() == 10.0 and v1.min() < 0.0
+
+
+def test_lj93_wall_matches_reference_field():
+    """The lj1d_mf deck's field is the cut-and-shifted 9-3 wall with eps_wf*rho_w = 3, sigma_wf = 1,
+    cut 3, surface at x = 0.5; nodes the reference flags zero-density hold VEXT_MAX."""
+    z, p = load("lj1d_mf")
+    d = np.arange(p.nnodes) * p.esize[0] - 0.5
+    v, de, ds = setup.lj93_wall_1d(d, 3.0, 1.0, 3.0, p.vext_max)
+    zero = np.asarray(p.zero_density, bool).reshape(-1)
+    ref = np.asarray(p.vext).reshape(-1)
+    assert np.abs(np.where(zero, p.vext_max, v) - ref).max() <= 1e-8
+    # analytic parameter derivatives against central differences of the formula itself
+    live = ~zero & (d < 3.0)
+    h = 1e-6
+    fd_e = (setup.lj93_wall_1d(d, 3.0 + h, 1.0, 3.0, 1e300)[0] - setup.lj93_wall_1d(d, 3.0 - h, 1.0, 3.0, 1e300)[0]) / (2 * h)
+    fd_s = (setup.lj93_wall_1d(d, 3.0, 1.0 + h, 3.0, 1e300)[0] - setup.lj93_wall_1d(d, 3.0, 1.0 - h, 3.0, 1e300)[0]) / (2 * h)
+    assert np.abs(de[live] - fd_e[live]).max() <= 1e-6 * np.abs(de[live]).max()
+    assert np.abs(ds[live] - fd_s[live]).max() <= 1e-6 * np.abs(ds[live]).max()

@@ -117,6 +117,7 @@ struct PadParams {
 
 struct tgpu_pads {
   PadParams rho_res, rho_jac, tr_res, tr_jac;
+  PadParams zero_ext;   // transposed sums: zero outside the mesh, no masking, no sign flips
 };
 
 namespace {
@@ -133,6 +134,9 @@ struct Ctx : tgpu_ctx {
   double *d_rho_ref = nullptr, *d_conv_ref = nullptr, *d_chan_ref = nullptr, *d_tr_ref = nullptr;
   double *d_drho = nullptr, *d_dchan = nullptr;
   double *d_newton_x = nullptr;   // device copy of the state for the host-pointer Newton solve
+  bool gmres_transpose = false;   // GMRES operator: S (false) or S^T (adjoint solve)
+  // adjoint work buffers (allocated on first use)
+  double *d_adj_chan = nullptr, *d_adj_pad = nullptr, *d_adj_g = nullptr, *d_adj_v = nullptr, *d_adj_t = nullptr;
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -432,6 +436,8 @@ void red_to_host(Ctx *c, int n)
   ck(cudaStreamSynchronize(c->stream), "sync");
 }
 
+void schur_t_device(Ctx *c, const double *d_v2, double *d_y2);
+
 int gmres(Ctx *c, const double *d_rhs, double *d_x2, double tol, int maxit, int *iters, double *relres)
 {
   const long n = c->n2;
@@ -463,7 +469,8 @@ int gmres(Ctx *c, const double *d_rhs, double *d_x2, double tol, int maxit, int 
       first = false;
     } else {
       // r = M^-1 (b - S x)
-      schur_device(c, d_x2, c->d_gw);
+      if (c->gmres_transpose) schur_t_device(c, d_x2, c->d_gw);
+      else schur_device(c, d_x2, c->d_gw);
       tgpu::launch_axpby(c->d_gw, 1.0, d_rhs, -1.0, n, c->stream);
       tgpu::launch_precond(c->d_x, c->d_vext, c->d_zero, c->d_gw, c->d_gt, c->stream);
       tgpu::launch_norm2(c->d_gt, n, c->d_partial, nb, c->d_red, c->stream);
@@ -479,7 +486,8 @@ int gmres(Ctx *c, const double *d_rhs, double *d_x2, double tol, int maxit, int 
     gv[0] = beta;
     int k = 0;
     for (; k < m; k++) {
-      schur_device(c, V + (long)k * n, c->d_gw);
+      if (c->gmres_transpose) schur_t_device(c, V + (long)k * n, c->d_gw);
+      else schur_device(c, V + (long)k * n, c->d_gw);
       tgpu::launch_precond(c->d_x, c->d_vext, c->d_zero, c->d_gw, c->d_gt, c->stream);
       // classical Gram-Schmidt, two passes; h and the norm stay on the device
       // until one copy per iteration
@@ -661,6 +669,141 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
   return converged ? TGPU_OK : TGPU_ERR_NOCONV;
 }
 
+// ---- adjoint: J^T w and J^T lambda = g ------------------------------------
+
+void ensure_adjoint(Ctx *c)
+{
+  if (c->d_adj_chan) return;
+  const tgpu::DevGeom &g = c->dg;
+  const size_t N = g.N;
+  const int nch = g.ncomp * (g.ndim + 3);
+  c->d_adj_chan = dalloc<double>((size_t)nch * N);
+  c->d_adj_pad = dalloc<double>((size_t)nch * g.NP);
+  c->d_adj_g = dalloc<double>((size_t)g.ncomp * (g.ndim + 2) * N);
+  c->d_adj_v = dalloc<double>((size_t)g.nunk * N);
+  c->d_adj_t = dalloc<double>((size_t)g.nunk * N);
+}
+
+// transposed stencil sum (FP64): out[j] (+)= sum_k coef[k] . in(j - offset_k), coefficient rows of shape (nin, nout)
+void adj_conv(Ctx *c, int ch0, int nin, const DevStencil &st, const double *coef, double *const *outs, int nout)
+{
+  tgpu::launch_conv<double>(c->d_adj_pad + (long)ch0 * c->dg.NP, c->dg.NP, nin, st.d_loff_neg, coef, st.L, outs, nout,
+                            true, c->dg.N, c->stream);
+  c->stats.conv_launches++;
+  c->stats.kernel_launches++;
+}
+
+void adj_pad(Ctx *c, int nch)
+{
+  tgpu::launch_pad<double>(c->d_adj_chan, c->d_adj_pad, nch, c->pads.zero_ext.bulk, c->pads.zero_ext.sign,
+                           c->pads.zero_ext.zc, c->d_zero, false, c->stream);
+  c->stats.kernel_launches++;
+}
+
+void jtv_device(Ctx *c, const double *d_w, double *d_out)
+{
+  need_state(c);
+  const tgpu::DevGeom &g = c->dg;
+  for (int d = 0; d < g.ndim; d++)
+    if (c->g.bc[d][0] == TGPU_BC_REFLECT || c->g.bc[d][1] == TGPU_BC_REFLECT)
+      throw Error(TGPU_ERR_UNSUPPORTED, "J^T with reflecting boundaries is not implemented");
+  if (g.hard_surf) throw Error(TGPU_ERR_UNSUPPORTED, "J^T with hard-wall boundary weights is not implemented");
+  ensure_adjoint(c);
+  const long N = g.N;
+  const int nd = g.ndim;
+  const int cpc = nd + 2;   // channels per component: A, B[d], C
+  ck(cudaMemsetAsync(d_out, 0, sizeof(double) * (size_t)g.nunk * N, c->stream), "memset");
+  // (a) density columns <- transposed weighted-density sums of the rb rows and mean-field sums of the MF rows
+  {
+    tgpu::launch_adj_rb_channels(d_w, c->d_adj_chan, c->stream);
+    const int nch = g.ncomp * cpc + (g.attraction ? g.ncomp : 0);
+    adj_pad(c, nch);
+    for (int jc = 0; jc < g.ncomp; jc++) {
+      double *o[1] = {d_out + (long)(g.first_rho + jc) * N};
+      const DevStencil &sd = c->sten[TGPU_STEN_DELTA][jc], &st = c->sten[TGPU_STEN_THETA][jc];
+      adj_conv(c, jc * cpc, 1 + nd, sd, sd.d_coef_adj, o, 1);
+      adj_conv(c, jc * cpc + nd + 1, 1, st, st.d_coef_fwd, o, 1);
+      if (g.attraction)
+        for (int ic = 0; ic < g.ncomp; ic++) {
+          const DevStencil &su = c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc];
+          adj_conv(c, g.ncomp * cpc + ic, 1, su, su.d_coef_fwd, o, 1);
+        }
+    }
+    // density columns exist only off zero-density nodes
+    tgpu::launch_mask_rows(d_out + (long)g.first_rho * N, nullptr, c->d_vext, c->d_zero, 0, g.ncomp, 1, c->stream);
+  }
+  // (b) rb columns <- H(n) g with g gathered from the EL rows of w by the transposed delta/theta sums
+  {
+    tgpu::launch_mask_rows(c->d_adj_chan, d_w, c->d_vext, c->d_zero, g.first_rho, g.ncomp, 0, c->stream);
+    adj_pad(c, g.ncomp);
+    const int gst = nd + 2;   // per component: delta outputs (scalar, vector[d]) then theta
+    ck(cudaMemsetAsync(c->d_adj_g, 0, sizeof(double) * (size_t)g.ncomp * gst * N, c->stream), "memset");
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      double *o[tgpu::kMaxRb];
+      for (int q = 0; q < gst; q++) o[q] = c->d_adj_g + ((long)ic * gst + q) * N;
+      const DevStencil &sd = c->sten[TGPU_STEN_DELTA][ic], &st = c->sten[TGPU_STEN_THETA][ic];
+      adj_conv(c, ic, 1, sd, sd.d_coef_adj, o, 1 + nd);
+      adj_conv(c, ic, 1, st, st.d_coef_fwd, o + nd + 1, 1);
+    }
+    tgpu::launch_jtv_local(c->d_x, c->d_vext, c->d_zero, d_w, c->d_adj_g, gst, 1, d_out, c->stream);
+    c->stats.kernel_launches += 4;
+  }
+}
+
+// J^T lambda = g by GMRES on the transposed Schur complement
+//   S^T = A22^T - A12^T A11^-T A21^T,  right-hand side g2 - A12^T A11^-T g1,
+//   lambda1 = A11^-T (g1 - A21^T lambda2),
+// with every block product taken from J^T on masked full vectors and
+// A11^-T [u_ind; u_dep] = [-u_ind - B^T u_dep; -u_dep].
+// S^T v2: t = J^T [0; v2]; y1 = A11^-T (t_block1); S^T v2 = t_rho - (J^T [y1; 0])_rho
+void schur_t_device(Ctx *c, const double *d_v2, double *d_y2)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  const size_t n = (size_t)g.nunk * N;
+  double *full = c->d_adj_v, *t = c->d_adj_t;
+  ck(cudaMemsetAsync(full, 0, n * sizeof(double), c->stream), "memset");
+  copy_d(c, full + (long)g.first_rho * N, d_v2, (size_t)g.ncomp * N);
+  jtv_device(c, full, t);
+  copy_d(c, d_y2, t + (long)g.first_rho * N, (size_t)g.ncomp * N);   // A22^T v2 - nothing else yet
+  tgpu::launch_a11inv_t(t, full, c->stream);                           // y1 in block-1 rows, density rows 0
+  jtv_device(c, full, t);                                              // t_rho = A12^T y1
+  tgpu::launch_axpby(d_y2, -1.0, t + (long)g.first_rho * N, 1.0, (long)g.ncomp * N, c->stream);
+  c->stats.schur_applies++;
+}
+
+int adjoint_solve_device(Ctx *c, const double *d_g, double *d_lam, double tol, int maxit, int *iters, double *relres)
+{
+  need_state(c);
+  ensure_adjoint(c);
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  const size_t n = (size_t)g.nunk * N;
+  double *full = c->d_adj_v, *t = c->d_adj_t;
+  // rhs2 = g2 - A12^T A11^-T g1
+  tgpu::launch_a11inv_t(d_g, full, c->stream);
+  jtv_device(c, full, t);
+  copy_d(c, c->d_b2s, d_g + (long)g.first_rho * N, (size_t)g.ncomp * N);
+  tgpu::launch_axpby(c->d_b2s, -1.0, t + (long)g.first_rho * N, 1.0, (long)g.ncomp * N, c->stream);
+  c->gmres_transpose = true;
+  int st;
+  try {
+    st = gmres(c, c->d_b2s, c->d_gx, tol, maxit, iters, relres);
+  } catch (...) {
+    c->gmres_transpose = false;
+    throw;
+  }
+  c->gmres_transpose = false;
+  // lambda1 = A11^-T (g1 - A21^T lambda2)
+  ck(cudaMemsetAsync(full, 0, n * sizeof(double), c->stream), "memset");
+  copy_d(c, full + (long)g.first_rho * N, c->d_gx, (size_t)g.ncomp * N);
+  jtv_device(c, full, t);                                   // block-1 rows: A21^T lambda2
+  tgpu::launch_axpby(t, 1.0, d_g, -1.0, (long)n, c->stream);  // t = g - J^T[0; lambda2] (block-1 rows used)
+  tgpu::launch_a11inv_t(t, d_lam, c->stream);
+  copy_d(c, d_lam + (long)g.first_rho * N, c->d_gx, (size_t)g.ncomp * N);
+  return st;
+}
+
 // Host-pointer wrappers: copy in, run on the device, copy out, synchronise.
 void h2d(Ctx *c, double *d, const double *h, size_t n)
 {
@@ -764,6 +907,9 @@ void build_device_tables(Ctx *c)
         loff[k] = (int)o;
       }
       st.d_loff = upload(loff, c->stream);
+      std::vector<int> lneg(loff.size());
+      for (size_t k = 0; k < loff.size(); k++) lneg[k] = -loff[k];
+      st.d_loff_neg = upload(lneg, c->stream);
       st.d_off = upload(off3, c->stream);
       st.d_w = upload(st.w, c->stream);
       if (!st.hw.empty()) st.d_hw = upload(st.hw, c->stream);
@@ -791,6 +937,12 @@ void build_device_tables(Ctx *c)
               fwd.push_back(f * g.inv_4pir[jc] * ((double)st.off[(size_t)k * nd + d] * g.esize[d] * g.inv_rad[jc]) * w);
         }
         st.nin_tr = 1 + nd;
+        std::vector<double> adj;   // [L][1+nd]: fac (w, e_d w), the forward scalar and vector rows
+        for (int k = 0; k < st.L; k++) {
+          adj.push_back(f * st.w[k]);
+          for (int d = 0; d < nd; d++) adj.push_back(f * ((double)st.off[(size_t)k * nd + d] * g.esize[d] * g.inv_rad[jc]) * st.w[k]);
+        }
+        st.d_coef_adj = upload(adj, c->stream);
         for (int k = 0; k < st.L; k++) {
           tr.push_back(st.w[k]);
           for (int d = 0; d < nd; d++) tr.push_back(-st.w[k] * (double)st.off[(size_t)k * nd + d] * g.esize[d] * g.inv_rad[idx]);
@@ -885,6 +1037,10 @@ void build_device_tables(Ctx *c)
     }
     c->pads.tr_res = make_pad(b_res, sg, zc, c->stream);
     c->pads.tr_jac = make_pad(b_jac, sg, zc, c->stream);
+  }
+  {
+    const int nz = TGPU_MAXC * 6;   // adjoint channels: per component A, B[d], C and the mean-field row
+    c->pads.zero_ext = make_pad(std::vector<double>(nz, 0.0), std::vector<int>(nz, 0), std::vector<int>(nz, -1), c->stream);
   }
   // work buffers
   c->nch_max = std::max(g.ncomp, g.ncomp * (nd + 2));
@@ -991,8 +1147,8 @@ int tgpu_destroy(tgpu_handle h)
     cudaStreamSynchronize(c->stream);
     for (int t = 0; t < 3; t++)
       for (auto &st : c->sten[t]) {
-        dfree(st.d_loff); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
-        dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32);
+        dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
+        dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
         for (auto *L : {&st.lines_fwd, &st.lines_tr}) { dfree(L->d_planes); dfree(L->d_lines); dfree(L->d_w); }
       }
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
@@ -1004,6 +1160,8 @@ int tgpu_destroy(tgpu_handle h)
     dfree(c->d_drho); dfree(c->d_dchan); dfree(c->d_newton_x);
     if (c->h_red) cudaFreeHost(c->h_red);
     free_pad(c->pads.rho_res); free_pad(c->pads.rho_jac); free_pad(c->pads.tr_res); free_pad(c->pads.tr_jac);
+    free_pad(c->pads.zero_ext);
+    dfree(c->d_adj_chan); dfree(c->d_adj_pad); dfree(c->d_adj_g); dfree(c->d_adj_v); dfree(c->d_adj_t);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     if (g_geom_owner == c) g_geom_owner = nullptr;
     delete c;
@@ -1356,16 +1514,53 @@ int tgpu_reset_stats(tgpu_handle h)
   return guard([&] { std::memset(&C(h)->stats, 0, sizeof(tgpu_stats)); return TGPU_OK; });
 }
 
-int tgpu_jtv_device(tgpu_handle, const double *, double *)
+int tgpu_jtv_device(tgpu_handle h, const double *d_w, double *d_out)
 {
-  g_last_error = "J^T w is not implemented yet";
-  return TGPU_ERR_UNSUPPORTED;
+  return guard([&] { jtv_device(C(h), d_w, d_out); ck(cudaGetLastError(), "jtv"); return TGPU_OK; });
 }
 
-int tgpu_jtv(tgpu_handle, const double *, double *)
+int tgpu_jtv(tgpu_handle h, const double *w, double *out)
 {
-  g_last_error = "J^T w is not implemented yet";
-  return TGPU_ERR_UNSUPPORTED;
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_work, w, n);
+    jtv_device(c, c->d_work, c->d_work2);
+    d2h(c, out, c->d_work2, n);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_adjoint_solve_device(tgpu_handle h, const double *d_g, double *d_lambda, double tol, int max_iter,
+                              int *iters, double *relres)
+{
+  return guard([&] {
+    int it = 0;
+    double rr = 0.0;
+    const int st = adjoint_solve_device(C(h), d_g, d_lambda, tol, max_iter, &it, &rr);
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return st;
+  });
+}
+
+int tgpu_adjoint_solve(tgpu_handle h, const double *g, double *lambda, double tol, int max_iter, int *iters,
+                       double *relres)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_work, g, n);
+    int it = 0;
+    double rr = 0.0;
+    const int st = adjoint_solve_device(c, c->d_work, c->d_work2, tol, max_iter, &it, &rr);
+    d2h(c, lambda, c->d_work2, n);
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return st;
+  });
 }
 
 }  // extern "C"

@@ -733,6 +733,157 @@ void launch_x1(const double *b, const double *conv, const double *x2, double *dx
 }
 
 // ---------------------------------------------------------------------------
+// Adjoint (J^T w) local step.  The Jacobian rows of the fill are
+//   EL_i(j):  1/rho (diag; 1 on zero rows), + MF_i(j), + sum_o fac w(o) [c(o)^T H(n(j+o))] on rb(j+o)
+//   rb_k(j):  -1 (diag), + B (dependent copies), + fac_k w(o) on rho_jc(j+o)
+//   MF_i(j):  -1 (diag), + w_att(o) on rho_jc(j+o)
+// so for the transpose the rb columns receive H(n(j)) g(j) with g gathered from
+// the EL rows by the transposed delta/theta sums (gel: per component the delta
+// outputs then the theta output, already scaled by fac), plus -w_rb and the B^T couplings; the MF columns receive -w_MF + w_EL;
+// the density columns receive the A22 diagonal times w_EL (the transposed
+// weighted-density and mean-field sums are added by the caller).
+__global__ void k_jtv_local(const double *__restrict__ x, const double *__restrict__ vext,
+                            const signed char *__restrict__ zero, const double *__restrict__ w,
+                            const double *__restrict__ gel, int gstride_ic, int v2_first,
+                            double *__restrict__ out)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double g[kMaxRb], n[kMaxRb], z[kMaxRb];
+    for (int k = 0; k < 4 + 2 * nd; k++) g[k] = 0.0;
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const double *G = gel + (long)ic * gstride_ic * N;
+      const double g0 = G[i];
+      g[2] += g0;
+      g[1] += c_g.inv_4pir[ic] * g0;
+      g[0] += c_g.inv_4pirsq[ic] * g0;
+      g[3] += G[(long)(gstride_ic - 1) * N + i];   // theta sum: last in the component's block
+      for (int d = 0; d < nd; d++) {
+        const double gd = G[(long)(v2_first + d) * N + i];
+        g[4 + nd + d] -= gd;
+        g[4 + d] -= c_g.inv_4pir[ic] * gd;
+      }
+    }
+    load_n(x, i, n);
+    fmt_hess_apply(n, g, z);
+    // rb columns in solution-vector order: -w_rb + B^T w_dep + z
+    double wrb[kMaxRb];
+    for (int k = 0; k < c_g.nrb; k++) wrb[k] = w[(long)(c_g.first_rb + k) * N + i];
+    double o[kMaxRb];
+    o[0] = -wrb[0] + z[3];
+    o[1] = -wrb[1] + z[2];
+    o[2] = -wrb[2] + z[1];
+    o[3] = -wrb[3] + z[0];
+    for (int d = 0; d < nd; d++) {
+      o[4 + d] = -wrb[4 + d] + z[4 + nd + d];
+      o[4 + nd + d] = -wrb[4 + nd + d] + z[4 + d];
+    }
+    if (c_g.single_size) {
+      o[1] += c_g.inv_4pir[0] * wrb[2] + c_g.inv_4pirsq[0] * wrb[3];
+      for (int d = 0; d < nd; d++) o[4 + d] += c_g.inv_4pir[0] * wrb[4 + nd + d];
+    }
+    for (int k = 0; k < c_g.nrb; k++) out[(long)(c_g.first_rb + k) * N + i] = o[k];
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long kr = (long)(c_g.first_rho + ic) * N + i;
+      const bool zr = zero_row(vext, zero, ic, i);
+      const double wel = zr ? 0.0 : w[kr];
+      // density column: transposed sums already in out; add the A22 diagonal
+      out[kr] += zr ? w[kr] : w[kr] / x[kr];
+      if (c_g.attraction) {
+        const long km = (long)(c_g.first_mf + ic) * N + i;
+        out[km] = -w[km] + wel;
+      }
+    }
+  }
+}
+
+void launch_jtv_local(const double *x, const double *vext, const signed char *zero, const double *w,
+                      const double *gel, int gstride_ic, int v2_first, double *out, cudaStream_t s)
+{
+  k_jtv_local<<<1184, kThreads, 0, s>>>(x, vext, zero, w, gel, gstride_ic, v2_first, out);
+}
+
+// Adjoint channels from the rb and MF rows of w, per component jc ([jc][ndim+2][N]):
+// A = w_n2 + w_n1/4piR + w_n0/4piR^2, B_d = w_V2d + w_V1d/4piR, C = w_n3 (the rb rows'
+// dependence on rho_jc, without fac); then the ncomp MF rows.  With one particle
+// size the n1, n0, V1 rows do not depend on the densities and drop out.
+__global__ void k_adj_rb_channels(const double *__restrict__ w, double *__restrict__ chan)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  const int cpc = nd + 2;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    const double *W = w + (long)c_g.first_rb * N + i;
+    const double wn3 = W[0], wn2 = W[N];
+    const double wn1 = c_g.single_size ? 0.0 : W[2 * N], wn0 = c_g.single_size ? 0.0 : W[3 * N];
+    for (int jc = 0; jc < c_g.ncomp; jc++) {
+      double *ch = chan + (long)jc * cpc * N + i;
+      ch[0] = wn2 + c_g.inv_4pir[jc] * wn1 + c_g.inv_4pirsq[jc] * wn0;
+      for (int d = 0; d < nd; d++) {
+        const double wv1 = c_g.single_size ? 0.0 : W[(long)(4 + nd + d) * N];
+        ch[(long)(1 + d) * N] = W[(long)(4 + d) * N] + c_g.inv_4pir[jc] * wv1;
+      }
+      ch[(long)(nd + 1) * N] = wn3;
+    }
+    if (c_g.attraction)
+      for (int ic = 0; ic < c_g.ncomp; ic++)
+        chan[(long)(c_g.ncomp * cpc + ic) * N + i] = w[(long)(c_g.first_mf + ic) * N + i];
+  }
+}
+
+void launch_adj_rb_channels(const double *w, double *chan, cudaStream_t s)
+{
+  k_adj_rb_channels<<<1184, kThreads, 0, s>>>(w, chan);
+}
+
+// y = A11^-T u on the block-1 rows of full vectors (density rows set to zero):
+// y_dep = -u_dep, y_ind = -u_ind - B^T u_dep, y_MF = -u_MF
+__global__ void k_a11inv_t(const double *__restrict__ u, double *__restrict__ y)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double v[kMaxRb];
+    for (int k = 0; k < c_g.nrb; k++) v[k] = -u[(long)(c_g.first_rb + k) * N + i];
+    if (c_g.single_size) {
+      v[1] -= c_g.inv_4pir[0] * u[(long)(c_g.first_rb + 2) * N + i] + c_g.inv_4pirsq[0] * u[(long)(c_g.first_rb + 3) * N + i];
+      for (int d = 0; d < nd; d++) v[4 + d] -= c_g.inv_4pir[0] * u[(long)(c_g.first_rb + 4 + nd + d) * N + i];
+    }
+    for (int k = 0; k < c_g.nrb; k++) y[(long)(c_g.first_rb + k) * N + i] = v[k];
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      y[(long)(c_g.first_rho + ic) * N + i] = 0.0;
+      if (c_g.attraction) y[(long)(c_g.first_mf + ic) * N + i] = -u[(long)(c_g.first_mf + ic) * N + i];
+    }
+  }
+}
+
+void launch_a11inv_t(const double *u, double *y, cudaStream_t s)
+{
+  k_a11inv_t<<<1184, kThreads, 0, s>>>(u, y);
+}
+
+// mode 0: out[r][i] = w[first + r][i] on non-zero EL rows, 0 on zero rows (masking of the EL block of w)
+// mode 1: out[r][i] *= !zero_density[r][i] (density columns exist only off zero-density nodes)
+__global__ void k_mask_rows(double *__restrict__ out, const double *__restrict__ w, const double *__restrict__ vext,
+                            const signed char *__restrict__ zero, int first, int nrows, int mode)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int r = 0; r < nrows; r++) {
+      const long k = (long)r * N + i;
+      if (mode == 0) out[k] = zero_row(vext, zero, r, i) ? 0.0 : w[(long)(first + r) * N + i];
+      else if (zero[k]) out[k] = 0.0;
+    }
+}
+
+void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,
+                      int mode, cudaStream_t s)
+{
+  k_mask_rows<<<1184, kThreads, 0, s>>>(out, w, vext, zero, first, nrows, mode);
+}
+
+// ---------------------------------------------------------------------------
 // Hard-wall boundary weights: for target nodes whose stencils reach a
 // boundary node, replace w by the fluid-element part of the point's corner
 // weights (HW_boundary_weight) for the weighted-density and mean-field sums.

@@ -44,6 +44,7 @@ struct DevStencil {
   std::vector<short> off;               // host copy [L][ndim]
   std::vector<double> w, hw;            // host copy
   int *d_loff = nullptr;                // [L] linear offsets in the padded box
+  int *d_loff_neg = nullptr;            // [L] the same offsets negated (transposed sums)
   // forward use (weighted densities / mean field of the density field)
   int nout_fwd = 0;
   double *d_coef_fwd = nullptr;         // [L][nout_fwd] FP64
@@ -52,6 +53,7 @@ struct DevStencil {
   int nin_tr = 0;
   double *d_coef_tr = nullptr;          // [L][nin_tr]
   float *d_coef_tr32 = nullptr;
+  double *d_coef_adj = nullptr;         // delta only: [L][1+ndim] fac (w, e_d w) for the transposed sums
   short *d_off = nullptr;               // [L][3] raw offsets (boundary corrections)
   double *d_w = nullptr, *d_hw = nullptr;
   // z-plane / x-line form for the FP32 single-channel sums (3-D): forward and transpose coefficients
@@ -154,6 +156,13 @@ void launch_newton_frac(const double *x, const double *dx, double floor_frac, do
 void launch_newton_update(double *x, const double *dx, double frac, double rel, double abs, double *partial,
                           int nblocks, double *result, cudaStream_t s);
 void launch_norm2(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s);
+// J^T w local step: A22, A11^T (with B^T), the MF coupling and H g for the rb columns
+void launch_jtv_local(const double *x, const double *vext, const signed char *zero, const double *w,
+                      const double *gel, int gstride_ic, int v2_first, double *out, cudaStream_t s);
+void launch_adj_rb_channels(const double *w, double *chan, cudaStream_t s);
+void launch_a11inv_t(const double *u, double *y, cudaStream_t s);
+void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,
+                      int mode, cudaStream_t s);
 void launch_delta_maxabs(const double *a, const double *ref, long n, double *out, double *partial, int nblocks,
                          double *result, cudaStream_t s);
 void launch_check_finite(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s);

@@ -88,6 +88,8 @@ def load(build_if_missing: bool = False):
         "tgpu_fill": [vp, vp, vp, C.c_int], "tgpu_fill_device": [vp, vp, vp, C.c_int],
         "tgpu_jv": [vp, vp, vp], "tgpu_jv_device": [vp, vp, vp],
         "tgpu_jtv": [vp, vp, vp], "tgpu_jtv_device": [vp, vp, vp],
+        "tgpu_adjoint_solve": [vp, vp, vp, C.c_double, C.c_int, ip, dp],
+        "tgpu_adjoint_solve_device": [vp, vp, vp, C.c_double, C.c_int, ip, dp],
         "tgpu_schur_apply": [vp, vp, vp], "tgpu_schur_apply_device": [vp, vp, vp],
         "tgpu_schur_rhs_device": [vp, vp, vp], "tgpu_schur_x1_device": [vp, vp, vp, vp],
         "tgpu_solve": [vp, vp, vp, C.c_double, C.c_int, ip, dp],
@@ -182,6 +184,11 @@ class Solver:
         except Exception:
             pass
 
+    def set_vext(self, vext):
+        """Replace V_ext/kT ([ncomp][N]); nodes equal to vext_max stay zero-density rows."""
+        v = self._host(vext, (self.p.ncomp, self.N))
+        _check(self.lib.tgpu_set_vext(self.h, _ptr(v)), self.lib)
+
     def set_precision(self, precision: int):
         _check(self.lib.tgpu_set_precision(self.h, int(precision)), self.lib)
 
@@ -216,6 +223,15 @@ class Solver:
         out = np.empty(self.shape)
         _check(self.lib.tgpu_jtv(self.h, _ptr(w), _ptr(out)), self.lib)
         return out
+
+    def adjoint_solve(self, g, tol=1e-12, max_iter=500):
+        """Solve J^T lambda = g (host arrays [nunk][N]); returns (lambda, GMRES iterations, relative residual)."""
+        g = self._host(g, self.shape)
+        lam = np.empty(self.shape)
+        it, rr = C.c_int(0), C.c_double(0.0)
+        st = self.lib.tgpu_adjoint_solve(self.h, _ptr(g), _ptr(lam), tol, max_iter, C.byref(it), C.byref(rr))
+        _check(st, self.lib, ok=(0, -5))
+        return lam, it.value, rr.value
 
     def schur(self, v2):
         shape2 = (self.p.ncomp, self.N)
@@ -252,6 +268,16 @@ class Solver:
 
     def jv_device(self, v, out):
         _check(self.lib.tgpu_jv_device(self.h, self._dptr(v), self._dptr(out)), self.lib)
+
+    def jtv_device(self, w, out):
+        _check(self.lib.tgpu_jtv_device(self.h, self._dptr(w), self._dptr(out)), self.lib)
+
+    def adjoint_solve_device(self, g, lam, tol=1e-12, max_iter=500):
+        it, rr = C.c_int(0), C.c_double(0.0)
+        st = self.lib.tgpu_adjoint_solve_device(self.h, self._dptr(g), self._dptr(lam), tol, max_iter, C.byref(it),
+                                                C.byref(rr))
+        _check(st, self.lib, ok=(0, -5))
+        return it.value, rr.value
 
     def schur_device(self, v2, y2):
         _check(self.lib.tgpu_schur_apply_device(self.h, self._dptr(v2), self._dptr(y2)), self.lib)

@@ -175,6 +175,32 @@ def rough_wall_vext(nx, esize, eps_w=1.0, kT=1.2, sigma_w=1.0, wall_x=1.0, patch
                                   prefactor=LJ123_PREF, form="eps_w*C*((s/d)^12-(s/d)^3)/kT")
 
 
+def lj93_wall_1d(dist, eps_w, sigma_w, cut_w, vext_max=10.0):
+    """V_ext/kT of a planar cut-and-shifted LJ 9-3 wall and its derivatives in (eps_w, sigma_w).
+
+    Vext_LJ9_3_CS (src/dft_vext_1D.c:42-56): with prefactor eps_w (the reference's
+    Eps_wf*Rho_w, already over kT) and d the distance from the wall surface,
+    V = eps_w (2 pi/3) sigma^3 [(2/15)((sigma/d)^9 - (sigma/cut)^9) - ((sigma/d)^3 - (sigma/cut)^3)]
+    for d <= cut and 0 beyond.  Nodes with d <= 0 or V >= vext_max hold vext_max
+    (zero-density rows, derivatives 0).  Returns (V, dV/deps_w, dV/dsigma_w).
+    """
+    d = np.asarray(dist, np.float64)
+    inside = (d > 0) & (d <= cut_w)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        dd = np.where(inside, d, 1.0)
+        a9 = 1.0 / dd ** 9 - 1.0 / cut_w ** 9
+        a3 = 1.0 / dd ** 3 - 1.0 / cut_w ** 3
+        pref = 2.0 * np.pi / 3.0
+        shape = pref * ((2.0 / 15.0) * sigma_w ** 12 * a9 - sigma_w ** 6 * a3)
+        dshape = pref * ((2.0 / 15.0) * 12.0 * sigma_w ** 11 * a9 - 6.0 * sigma_w ** 5 * a3)
+    v = np.where(inside, eps_w * shape, 0.0)
+    clamp = (d <= 0) | (v >= vext_max)
+    v = np.where(clamp, vext_max, v)
+    dv_de = np.where(inside & ~clamp, shape, 0.0)
+    dv_ds = np.where(inside & ~clamp, eps_w * dshape, 0.0)
+    return v, dv_de, dv_ds
+
+
 def config2(n=128, esize=0.1, seed=1234):
     """3-D FMT1 + WCA (eps=1, r_c=2.5, kT*=1.2) fluid at rho_b=0.6 next to a rough 12-3 LJ wall.
 
