@@ -142,6 +142,35 @@ int tgpu_adjoint_solve(tgpu_handle h, const double *g, double *lambda, double to
                        double *relres);
 int tgpu_adjoint_solve_device(tgpu_handle h, const double *d_g, double *d_lambda, double tol, int max_iter,
                               int *iters, double *relres);
+/* ---- Objectives and their sensitivities ----------------------------------
+ * Integration weights of integrateInSpace (src/dft_out_utils.c:38-62), per component and node ([ncomp][N]):
+ *   w_fluid = Nel_hit2 * Vol_el / Nnodes_per_el_V * F,   w_bulk = Nel_hit * Vol_el / Nnodes_per_el_V * F,
+ * with F = Fac_vol, or Fac_vol / (Fac_area * Area) for per-area results (Lper_area); Nel_hit / Nel_hit2 as
+ * setup_integrals (src/dft_out_utils.c:179-270).  rhobar_b: the bulk weighted densities n3 n2 n1 n0
+ * (Rhobar_b); betamu: the chemical potentials (Betamu). */
+int tgpu_set_integration(tgpu_handle h, const double *w_fluid, const double *w_bulk, const double *rhobar_b,
+                         const double *betamu);
+/* omega_s: the surface excess grand free energy of calc_free_energy (src/dft_energy.c:31-168, ideal gas,
+ * chemical potential, external field, FMT and mean-field terms minus their bulk terms); gamma_ex[ncomp]:
+ * the excess adsorption of calc_adsorption (src/dft_out_ads.c:33-112).  Either pointer may be NULL. */
+int tgpu_objectives(tgpu_handle h, const double *x, double *omega_s, double *gamma_ex);
+int tgpu_objectives_device(tgpu_handle h, const double *d_x, double *omega_s, double *gamma_ex);
+enum { TGPU_OBJ_OMEGA = 0, TGPU_OBJ_GAMMA = 1 };
+/* Partial derivatives of omega_s (kind TGPU_OBJ_OMEGA) or gamma_ex[icomp] (TGPU_OBJ_GAMMA) at state d_x:
+ * d_gx = dF/dx ([nunk][N]), d_gv = dF/dV_ext at fixed x ([ncomp][N]). */
+int tgpu_objective_grad_device(tgpu_handle h, const double *d_x, int kind, int icomp, double *d_gx, double *d_gv);
+/* Total sensitivity of an objective of the converged state x to the external field, dF/dV_ext ([ncomp][N]):
+ * an FP64 mode-0 fill at x, the adjoint solve J^T lambda = dF/dx (tol, max_iter as tgpu_adjoint_solve) and
+ * dF/dV_ext = dF/dV|_x - lambda on the Euler-Lagrange rows.  No reference counterpart. */
+int tgpu_grad_vext_device(tgpu_handle h, const double *d_x, int kind, int icomp, double tol, int max_iter,
+                          double *d_dF_dV, int *iters);
+int tgpu_grad_omega_vext(tgpu_handle h, const double *x, double tol, int max_iter, double *dOmega_dV, int *iters);
+int tgpu_grad_gamma_vext(tgpu_handle h, const double *x, int icomp, double tol, int max_iter, double *dGamma_dV,
+                         int *iters);
+/* Sensitivity to a wall parameter p (e.g. eps_w) that enters only through V_ext: dF/dp = sum dF/dV dV/dp,
+ * with dvext_deps = dV_ext/dp ([ncomp][N]). */
+int tgpu_grad_epsw(tgpu_handle h, const double *x, int kind, int icomp, const double *dvext_deps, double tol,
+                   int max_iter, double *dF_deps, int *iters);
 /* Schur complement on the density block ([ncomp][N] in and out) */
 int tgpu_schur_apply(tgpu_handle h, const double *v2, double *y2);
 int tgpu_schur_apply_device(tgpu_handle h, const double *d_v2, double *d_y2);

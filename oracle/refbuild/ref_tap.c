@@ -279,3 +279,46 @@ void tref_classify_unknowns(int *ind, int *nind, int *dep, int *ndep, int *dens,
     }
   }
 }
+
+/* Integration data of setup_integrals / setup_domain_multipliers (src/dft_out_utils.c:141-270):
+ * hit = Nel_hit, hit2 = Nel_hit2 as [Ncomp][Nnodes_per_proc];
+ * d = {Vol_el, Nnodes_per_el_V, Area, Fac_vol, Fac_area, Lper_area, Betamu[0..Ncomp-1]}. */
+extern int **Nel_hit, **Nel_hit2;
+extern double Area, Fac_vol, Fac_area, Vol_el;
+extern int Lper_area;
+int tref_integration(int *hit, int *hit2, double *d)
+{
+  int c, i;
+  for (c = 0; c < Ncomp; c++)
+    for (i = 0; i < Nnodes_per_proc; i++) {
+      hit[(size_t)c * Nnodes_per_proc + i] = Nel_hit[c][L2B_node[i]];
+      hit2[(size_t)c * Nnodes_per_proc + i] = Nel_hit2[c][L2B_node[i]];
+    }
+  d[0] = Vol_el;
+  d[1] = Nnodes_per_el_V;
+  d[2] = Area;
+  d[3] = Fac_vol;
+  d[4] = Fac_area;
+  d[5] = Lper_area;
+  for (c = 0; c < Ncomp; c++) d[6 + c] = Betamu[c];
+  return 6 + Ncomp;
+}
+
+/* Surface excess free energy (calc_free_energy, src/dft_energy.c:31) and the
+ * adsorption integrals of calc_adsorption (src/dft_out_ads.c:33-112) of the
+ * current state: ads[icomp] over Nel_hit2, ads_b[icomp] over Nel_hit. */
+double calc_free_energy(FILE *fp, double **x);
+double integrateInSpace(double (*fp_integrand)(int, int, double **), int iunk, int **nelhit, double **x,
+                        double *profile);
+double integrand_adsorption(int iunk, int inode_box, double **x);
+double integrand_adsorption_bulk(int iunk, int inode_box, double **x);
+int tref_energy(double *omega_s, double *ads, double *ads_b)
+{
+  int c;
+  *omega_s = calc_free_energy(NULL, g_x);
+  for (c = 0; c < Ncomp; c++) {
+    ads[c] = integrateInSpace(&integrand_adsorption, Phys2Unk_first[DENSITY] + c, Nel_hit2, g_x, NULL);
+    ads_b[c] = integrateInSpace(&integrand_adsorption_bulk, Phys2Unk_first[DENSITY] + c, Nel_hit, g_x, NULL);
+  }
+  return 0;
+}

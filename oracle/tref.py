@@ -202,6 +202,11 @@ def _child_extract(deck_lines, surfaces_from, opts, q):
                     lib.tref_stencil(isten, 0, idx, ip(off), dp(w), dp(hw) if hw is not None else None)
                     sten[(isten, idx)] = (off.reshape(L, ndim), w, None if hw is None else hw.reshape(L, nel_v))
             out["stencils"] = sten
+            hit = np.zeros(ncomp * nown, np.int32)
+            hit2 = np.zeros(ncomp * nown, np.int32)
+            integ = np.zeros(6 + ncomp)
+            lib.tref_integration(ip(hit), ip(hit2), dp(integ))
+            out["nel_hit"], out["nel_hit2"], out["integ"] = hit.reshape(ncomp, nown), hit2.reshape(ncomp, nown), integ
             x0 = np.zeros(nunk * nbox)
             lib.tref_get_x(dp(x0))
             out["x_guess"] = x0.reshape(nunk, nbox).copy()
@@ -232,8 +237,13 @@ def _child_extract(deck_lines, surfaces_from, opts, q):
                 cols = np.zeros(nnz, np.int64)
                 vals = np.zeros(nnz)
                 lib.tref_mgr_matrix(rows.ctypes.data_as(c_ll_p), cols.ctypes.data_as(c_ll_p), dp(vals))
+                lib.tref_set_x(dp(xs))
+                om = ctypes.c_double(0.0)
+                ads, ads_b = np.zeros(ncomp), np.zeros(ncomp)
+                lib.tref_energy(ctypes.byref(om), dp(ads), dp(ads_b))
                 fills.append({"x": xs.reshape(nunk, nbox), "rhs": rhs.reshape(nunk, nown), "rows": rows,
-                              "cols": cols, "vals": vals, "nglobal": ng, "resid_sum": rs.value})
+                              "cols": cols, "vals": vals, "nglobal": ng, "resid_sum": rs.value,
+                              "omega_s": om.value, "ads": ads, "ads_b": ads_b})
             out["fills"] = fills
             q.put(out)
     except Exception as exc:  # pragma: no cover

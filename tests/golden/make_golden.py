@@ -125,6 +125,8 @@ def make_case(name, lines, surfaces, states=("x_newton", ("x_newton", 7, 0.02)))
         out[f"sten_{isten}_{idx}_w"] = w
         if hw is not None:
             out[f"sten_{isten}_{idx}_hw"] = hw
+    out["nel_hit"], out["nel_hit2"] = r["nel_hit"].astype(np.int8), r["nel_hit2"].astype(np.int8)
+    out["integ"] = r["integ"]
     ind, dep, dens = block_lists(ints, nunk)
     out["blk_ind"], out["blk_dep"], out["blk_dens"] = (np.array(v, np.int32) for v in (ind, dep, dens))
     N = nunk * nbox
@@ -156,6 +158,8 @@ def make_case(name, lines, surfaces, states=("x_newton", ("x_newton", 7, 0.02)))
         Sv = A22 @ v2 - A21 @ y1
         out[f"schur_Sv{k}"] = Sv.reshape(len(dens), nbox)
         out[f"nnz{k}"] = np.int64(J.nnz)
+        out[f"omega_s{k}"] = np.float64(f["omega_s"])
+        out[f"ads{k}"], out[f"ads_b{k}"] = f["ads"], f["ads_b"]
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     return out
 

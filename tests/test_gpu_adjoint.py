@@ -3,8 +3,9 @@
 J^T w (tgpu_jtv) against the transpose of the Jacobian the reference assembles
 (fixtures JTw*, products of the reference's own matrix) and against the C
 oracle; J^T lambda = g (tgpu_adjoint_solve); and sensitivities of the grand
-potential and the excess adsorption of the converged LJ fluid at a 9-3 wall
-with respect to the per-node external field and to the wall parameters
+potential (Omega_s, the reference's calc_free_energy) and the excess
+adsorption of the converged LJ fluid at a 9-3 wall with respect to the
+per-node external field and to the wall parameters
 (eps_w, sigma_w), checked against central finite differences with h = 1e-6
 and, through a torch.autograd.Function wrapper, by torch.autograd.gradcheck.
 
@@ -101,20 +102,11 @@ def test_transpose_rejects_reflecting_boundaries():
 WALL = dict(eps_w=3.0, sigma_w=1.0, cut_w=3.0, x_wall=0.5)   # the lj1d_mf field (9-3 cut and shifted)
 
 
-def _phi_fmt1(n, ndim):
-    """Rosenfeld FMT free-energy density on SV-ordered weighted densities (torch)."""
-    import torch
-    n3, n2, n1, n0 = n[0], n[1], n[2], n[3]
-    V2 = n[4:4 + ndim]
-    V1 = n[4 + ndim:4 + 2 * ndim]
-    one = 1.0 - n3
-    v1v2 = (V1 * V2).sum(0)
-    v2v2 = (V2 * V2).sum(0)
-    return -n0 * torch.log(one) + (n1 * n2 - v1v2) / one + (n2 ** 3 - 3.0 * n2 * v2v2) / (24.0 * np.pi * one ** 2)
-
-
 class _Fluid:
-    """lj1d_mf (FMT1 + mean-field LJ, one component) with the 9-3 wall field as a function of its parameters."""
+    """lj1d_mf (FMT1 + mean-field LJ, one component) with the 9-3 wall field as a function of its parameters.
+
+    The objectives are the library's Omega_s and Gamma_ex (the reference's calc_free_energy and
+    calc_adsorption integrals); their V_ext sensitivities come from tgpu_grad_omega_vext / _gamma_vext."""
 
     def __init__(self):
         from tramonto_gb300 import native, setup
@@ -124,8 +116,6 @@ class _Fluid:
         self.zero = np.asarray(p.zero_density, bool).reshape(-1)
         self.s = native.Solver(p)
         self.setup = setup
-        self.dv = float(p.esize[0])
-        self.mu = -(np.log(p.rho_b[0]) + p.betamu_hs_ex[0] + p.betamu_att[0])
         self.x = np.array(self.z[f"x{len(self.z['states']) - 1}"], copy=True)
         self.vext0 = self.field(WALL["eps_w"], WALL["sigma_w"])[0]
         self.x = self.solve(self.vext0)
@@ -145,37 +135,15 @@ class _Fluid:
         return x
 
     def objectives(self, x, vext):
-        """(Omega, Gamma) at (x, V) and their partial gradients in x and V (torch autograd, float64)."""
-        import torch
-        p = self.p
-        with torch.enable_grad():   # also inside a torch.autograd.Function forward
-            xt = torch.tensor(x, dtype=torch.float64, requires_grad=True)
-            vt = torch.tensor(vext, dtype=torch.float64, requires_grad=True)
-            live = torch.tensor(~self.zero)
-            rho = xt[p.first_rho]
-            rl = torch.where(live, rho, torch.ones_like(rho))
-            ideal = torch.where(live, rl * (torch.log(rl) - 1.0) + (vt + self.mu) * rl + 0.5 * rl * xt[p.first_mf],
-                                torch.zeros_like(rl))
-            omega = self.dv * (ideal.sum() + _phi_fmt1(xt[p.first_rb:p.first_rb + p.nrb], p.ndim).sum())
-            gamma = self.dv * torch.where(live, rho - p.rho_b[0], torch.zeros_like(rho)).sum()
-            out = []
-            for f in (omega, gamma):
-                gx, gv = torch.autograd.grad(f, (xt, vt), retain_graph=True, allow_unused=True)
-                gv = np.zeros(vext.shape) if gv is None else gv.numpy()
-                out.append((f.item(), gx.numpy(), gv))
-        return out
+        """(Omega_s, Gamma_ex) at (x, V)."""
+        self.s.set_vext(vext.reshape(1, -1))
+        om, gam = self.s.objectives(x)
+        return om, float(gam[0])
 
     def gradients(self, x, vext):
-        """dOmega/dV and dGamma/dV at the converged state (adjoint)."""
-        p = self.p
+        """dOmega_s/dV and dGamma_ex/dV at the converged state (adjoint)."""
         self.s.set_vext(vext.reshape(1, -1))
-        self.s.fill(x, mode=0)
-        res = []
-        for f, gx, gv in self.objectives(x, vext):
-            lam, it, rr = self.s.adjoint_solve(gx, tol=1e-13, max_iter=1000)
-            dv = gv - np.where(self.zero, 0.0, lam[p.first_rho])
-            res.append((f, dv))
-        return res
+        return [self.s.grad_vext(x, kind=k, tol=1e-13, max_iter=1000).reshape(-1) for k in (0, 1)]
 
 
 @pytest.fixture(scope="module")
@@ -183,18 +151,6 @@ def fluid():
     f = _Fluid()
     yield f
     f.s.close()
-
-
-def test_phi_gradient_matches_oracle(fluid):
-    import torch
-    p = fluid.p
-    o = orc.Oracle(p)
-    n = torch.tensor(fluid.x[p.first_rb:p.first_rb + p.nrb], dtype=torch.float64, requires_grad=True)
-    (g,) = torch.autograd.grad(_phi_fmt1(n, p.ndim).sum(), n)
-    d = o.dphi(fluid.x)                      # S0 S1 S2 S3 V1 V2
-    nd = p.ndim
-    ref = np.concatenate([d[3:4], d[2:3], d[1:2], d[0:1], d[4 + nd:4 + 2 * nd], d[4:4 + nd]])
-    assert rel_err(g.numpy(), ref) <= 1e-12
 
 
 def test_wall_field_restatement_matches_reference_field(fluid):
@@ -215,12 +171,12 @@ def test_vext_gradient_matches_finite_differences(fluid):
     for d in dirs:
         fp = fluid.objectives(fluid.solve(v0 + FD_H * d), v0 + FD_H * d)
         fm = fluid.objectives(fluid.solve(v0 - FD_H * d), v0 - FD_H * d)
-        for j, name in enumerate(("Omega", "Gamma")):
-            fd = (fp[j][0] - fm[j][0]) / (2 * FD_H)
-            adj = float(np.sum(grads[j][1] * d))
+        for j, name in enumerate(("Omega_s", "Gamma_ex")):
+            fd = (fp[j] - fm[j]) / (2 * FD_H)
+            adj = float(np.sum(grads[j] * d))
             # judged against the gradient's size: a central difference with h = 1e-6 resolves
             # F(+h) - F(-h) only to ~1e-14 of F, i.e. ~1e-8 in a derivative
-            ref_scale = max(abs(fd), float(np.abs(grads[j][1]).max() * np.abs(d).max()))
+            ref_scale = max(abs(fd), float(np.abs(grads[j]).max() * np.abs(d).max()))
             assert abs(adj - fd) <= GRAD_RTOL * ref_scale, (name, adj, fd)
     fluid.solve(v0)
 
@@ -229,14 +185,15 @@ def test_wall_parameter_gradcheck(fluid):
     import torch
 
     class GrandPotential(torch.autograd.Function):
-        """Omega and Gamma of the converged fluid as functions of (eps_w, sigma_w); backward by the adjoint."""
+        """Omega_s and Gamma_ex of the converged fluid as functions of (eps_w, sigma_w); backward by the adjoint."""
 
         @staticmethod
         def forward(ctx, theta):
             e, s = float(theta[0]), float(theta[1])
             v, de, ds = fluid.field(e, s)
             x = fluid.solve(v)
-            (om, dom), (ga, dga) = fluid.gradients(x, v)
+            om, ga = fluid.objectives(x, v)
+            dom, dga = fluid.gradients(x, v)
             jac = np.array([[np.sum(dom * de), np.sum(dom * ds)], [np.sum(dga * de), np.sum(dga * ds)]])
             ctx.save_for_backward(torch.tensor(jac, dtype=torch.float64))
             return torch.tensor([om, ga], dtype=torch.float64)

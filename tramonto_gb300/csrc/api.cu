@@ -137,6 +137,11 @@ struct Ctx : tgpu_ctx {
   bool gmres_transpose = false;   // GMRES operator: S (false) or S^T (adjoint solve)
   // adjoint work buffers (allocated on first use)
   double *d_adj_chan = nullptr, *d_adj_pad = nullptr, *d_adj_g = nullptr, *d_adj_v = nullptr, *d_adj_t = nullptr;
+  // objectives (Omega_s, Gamma_ex): integration weights and work buffers
+  bool have_integ = false;
+  tgpu::ObjConst oc{};
+  double *d_wf = nullptr, *d_wb = nullptr;
+  double *d_obj_gx = nullptr, *d_obj_gv = nullptr, *d_obj_lam = nullptr, *d_obj_R = nullptr;
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -804,6 +809,106 @@ int adjoint_solve_device(Ctx *c, const double *d_g, double *d_lam, double tol, i
   return st;
 }
 
+// ---- objectives: Omega_s and Gamma_ex, their gradients, sensitivities to V_ext ----
+
+void need_integ(Ctx *c)
+{
+  need_final(c);
+  if (!c->have_integ) throw Error(TGPU_ERR_STATE, "no integration weights: call tgpu_set_integration first");
+}
+
+// mean-field sums S_ic = sum_jc sum_o u_ic,jc(o) rho_jc(i+o) of the densities of d_x into d_conv rows nrb..
+const double *attraction_sums(Ctx *c, const double *d_x)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  if (!g.attraction) return c->d_conv;   // unused
+  double *S = c->d_conv + (long)g.nrb * N;
+  ck(cudaMemsetAsync(S, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+  pad(c, d_x + (long)g.first_rho * N, c->pads.rho_res, false);
+  for (int jc = 0; jc < g.ncomp; jc++)
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      double *o[1] = {S + (long)ic * N};
+      conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o, 1, false);
+    }
+  return S;
+}
+
+void objectives_device(Ctx *c, const double *d_x, double *omega_s, double *gamma_ex)
+{
+  need_integ(c);
+  const tgpu::DevGeom &g = c->dg;
+  const double *S = attraction_sums(c, d_x);
+  const int nb = tgpu::reduce_blocks(g.N);
+  tgpu::launch_objectives(d_x, c->d_vext, S, c->d_wf, c->d_wb, c->oc, g.ncomp, c->d_partial, nb, c->d_red, c->stream);
+  c->stats.kernel_launches += 2;
+  red_to_host(c, 1 + g.ncomp);
+  if (omega_s) *omega_s = c->h_red[0];
+  if (gamma_ex)
+    for (int ic = 0; ic < g.ncomp; ic++) gamma_ex[ic] = c->h_red[1 + ic];
+}
+
+// dF/dx ([nunk][N]) and the explicit dF/dV_ext ([ncomp][N]) of F = Omega_s (kind 0) or Gamma_ex[icomp] (kind 1)
+void objective_grad_device(Ctx *c, const double *d_x, int kind, int icomp, double *d_gx, double *d_gv)
+{
+  need_integ(c);
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  if (kind != TGPU_OBJ_OMEGA && kind != TGPU_OBJ_GAMMA) throw Error(TGPU_ERR_ARG, "objective kind");
+  if (kind == TGPU_OBJ_GAMMA && (icomp < 0 || icomp >= g.ncomp)) throw Error(TGPU_ERR_ARG, "component index");
+  const bool att = kind == TGPU_OBJ_OMEGA && g.attraction;
+  if (att) {
+    for (int d = 0; d < g.ndim; d++)
+      if (c->g.bc[d][0] == TGPU_BC_REFLECT || c->g.bc[d][1] == TGPU_BC_REFLECT)
+        throw Error(TGPU_ERR_UNSUPPORTED, "free-energy gradient with attraction and reflecting boundaries");
+    ensure_adjoint(c);
+  }
+  const double *S = att ? attraction_sums(c, d_x) : c->d_conv;
+  tgpu::launch_objective_grad(d_x, c->d_vext, S, c->d_wf, c->d_wb, c->oc, kind, icomp, d_gx, d_gv,
+                              att ? c->d_adj_chan : nullptr, c->stream);
+  c->stats.kernel_launches++;
+  if (att) {
+    // the other nodes' mean-field terms: d/drho_jc(j) sum_i wf_ic rho_ic(i) S_ic(i) / 2 =
+    // transposed attraction sums of wf rho / 2 (the kernel stored wf rho on rho > 0 nodes)
+    tgpu::launch_scale(c->d_adj_chan, c->d_adj_chan, 0.5, (long)g.ncomp * N, c->stream);
+    adj_pad(c, g.ncomp);
+    for (int jc = 0; jc < g.ncomp; jc++) {
+      double *o[1] = {d_gx + (long)(g.first_rho + jc) * N};
+      for (int ic = 0; ic < g.ncomp; ic++) {
+        const DevStencil &su = c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc];
+        adj_conv(c, ic, 1, su, su.d_coef_fwd, o, 1);
+      }
+    }
+    // densities at zero-density nodes are not unknowns of the sums (int_stencil skips them)
+    tgpu::launch_mask_rows(d_gx + (long)g.first_rho * N, nullptr, c->d_vext, c->d_zero, 0, g.ncomp, 1, c->stream);
+    c->stats.kernel_launches += 2;
+  }
+}
+
+void ensure_obj(Ctx *c)
+{
+  if (c->d_obj_gx) return;
+  const size_t N = c->dg.N, U = c->dg.nunk;
+  c->d_obj_gx = dalloc<double>(U * N);
+  c->d_obj_lam = dalloc<double>(U * N);
+  c->d_obj_R = dalloc<double>(U * N);
+  c->d_obj_gv = dalloc<double>((size_t)c->dg.ncomp * N);
+}
+
+// dF/dV_ext at the state d_x: Jacobian at d_x (FP64 fill), J^T lambda = dF/dx, dF/dV = dF/dV|_x - lambda_EL
+int grad_vext_device(Ctx *c, const double *d_x, int kind, int icomp, double tol, int maxit, double *d_out, int *iters)
+{
+  need_integ(c);
+  ensure_obj(c);
+  fill_arith(c, d_x, c->d_obj_R, 0, TGPU_FILL_FP64);
+  objective_grad_device(c, c->d_x, kind, icomp, c->d_obj_gx, c->d_obj_gv);
+  double rr = 0.0;
+  const int st = adjoint_solve_device(c, c->d_obj_gx, c->d_obj_lam, tol, maxit, iters, &rr);
+  tgpu::launch_vext_sens(c->d_obj_lam, c->d_obj_gv, c->d_vext, c->d_zero, d_out, c->stream);
+  c->stats.kernel_launches++;
+  return st;
+}
+
 // Host-pointer wrappers: copy in, run on the device, copy out, synchronise.
 void h2d(Ctx *c, double *d, const double *h, size_t n)
 {
@@ -1162,6 +1267,7 @@ int tgpu_destroy(tgpu_handle h)
     free_pad(c->pads.rho_res); free_pad(c->pads.rho_jac); free_pad(c->pads.tr_res); free_pad(c->pads.tr_jac);
     free_pad(c->pads.zero_ext);
     dfree(c->d_adj_chan); dfree(c->d_adj_pad); dfree(c->d_adj_g); dfree(c->d_adj_v); dfree(c->d_adj_t);
+    dfree(c->d_wf); dfree(c->d_wb); dfree(c->d_obj_gx); dfree(c->d_obj_gv); dfree(c->d_obj_lam); dfree(c->d_obj_R);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     if (g_geom_owner == c) g_geom_owner = nullptr;
     delete c;
@@ -1561,6 +1667,126 @@ int tgpu_adjoint_solve(tgpu_handle h, const double *g, double *lambda, double to
     if (relres) *relres = rr;
     return st;
   });
+}
+
+int tgpu_set_integration(tgpu_handle h, const double *w_fluid, const double *w_bulk, const double *rhobar_b,
+                         const double *betamu)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    if (!w_fluid || !w_bulk || !rhobar_b || !betamu) throw Error(TGPU_ERR_ARG, "null argument");
+    const tgpu::DevGeom &g = c->dg;
+    const size_t n = (size_t)g.ncomp * g.N;
+    if (!c->d_wf) {
+      c->d_wf = dalloc<double>(n);
+      c->d_wb = dalloc<double>(n);
+    }
+    ck(cudaMemcpyAsync(c->d_wf, w_fluid, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
+    ck(cudaMemcpyAsync(c->d_wb, w_bulk, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
+    tgpu::ObjConst oc{};
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      const double rb = g.rho_b[ic];
+      oc.betamu[ic] = betamu[ic];
+      oc.bulk[ic] = rb * (std::log(rb) - 1.0) - rb * betamu[ic] + (g.attraction ? 0.5 * rb * g.betamu_att[ic] : 0.0);
+    }
+    // bulk weighted densities (n3 n2 n1 n0 in solution-vector order), vectors zero
+    double nb[tgpu::kMaxRb] = {0.0};
+    nb[0] = rhobar_b[3];
+    nb[1] = rhobar_b[2];
+    nb[2] = rhobar_b[1];
+    nb[3] = rhobar_b[0];
+    oc.phi_b = tgpu::fmt_phi(nb, g.ndim, g.functional);
+    c->oc = oc;
+    c->have_integ = true;
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    return TGPU_OK;
+  });
+}
+
+int tgpu_objectives_device(tgpu_handle h, const double *d_x, double *omega_s, double *gamma_ex)
+{
+  return guard([&] {
+    objectives_device(C(h), d_x, omega_s, gamma_ex);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_objectives(tgpu_handle h, const double *x, double *omega_s, double *gamma_ex)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_integ(c);
+    h2d(c, c->d_work, x, (size_t)c->dg.nunk * c->dg.N);
+    objectives_device(c, c->d_work, omega_s, gamma_ex);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_objective_grad_device(tgpu_handle h, const double *d_x, int kind, int icomp, double *d_gx, double *d_gv)
+{
+  return guard([&] {
+    objective_grad_device(C(h), d_x, kind, icomp, d_gx, d_gv);
+    ck(cudaGetLastError(), "objective gradient");
+    return TGPU_OK;
+  });
+}
+
+int tgpu_grad_vext_device(tgpu_handle h, const double *d_x, int kind, int icomp, double tol, int max_iter,
+                          double *d_dF_dV, int *iters)
+{
+  return guard([&] {
+    int it = 0;
+    const int st = grad_vext_device(C(h), d_x, kind, icomp, tol, max_iter, d_dF_dV, &it);
+    if (iters) *iters = it;
+    return st;
+  });
+}
+
+namespace {
+int grad_vext_host(tgpu_handle h, const double *x, int kind, int icomp, double tol, int max_iter, double *dF_dV,
+                   int *iters)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_integ(c);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    h2d(c, c->d_work, x, n);
+    int it = 0;
+    const int st = grad_vext_device(c, c->d_work, kind, icomp, tol, max_iter, c->d_work2, &it);
+    d2h(c, dF_dV, c->d_work2, (size_t)c->dg.ncomp * c->dg.N);
+    if (iters) *iters = it;
+    return st;
+  });
+}
+}  // namespace
+
+int tgpu_grad_omega_vext(tgpu_handle h, const double *x, double tol, int max_iter, double *dOmega_dV, int *iters)
+{
+  return grad_vext_host(h, x, TGPU_OBJ_OMEGA, 0, tol, max_iter, dOmega_dV, iters);
+}
+
+int tgpu_grad_gamma_vext(tgpu_handle h, const double *x, int icomp, double tol, int max_iter, double *dGamma_dV,
+                         int *iters)
+{
+  return grad_vext_host(h, x, TGPU_OBJ_GAMMA, icomp, tol, max_iter, dGamma_dV, iters);
+}
+
+int tgpu_grad_epsw(tgpu_handle h, const double *x, int kind, int icomp, const double *dvext_deps, double tol,
+                   int max_iter, double *dF_deps, int *iters)
+{
+  if (!dvext_deps || !dF_deps) return guard([&]() -> int { throw Error(TGPU_ERR_ARG, "null argument"); });
+  Ctx *c = nullptr;
+  const int st0 = guard([&] { c = C(h); need_integ(c); return TGPU_OK; });
+  if (st0 != TGPU_OK) return st0;
+  const size_t n = (size_t)c->dg.ncomp * c->dg.N;
+  std::vector<double> s(n);
+  const int st = grad_vext_host(h, x, kind, icomp, tol, max_iter, s.data(), iters);
+  if (st != TGPU_OK && st != TGPU_ERR_NOCONV) return st;
+  double acc = 0.0;
+  for (size_t k = 0; k < n; k++) acc += s[k] * dvext_deps[k];
+  *dF_deps = acc;
+  return st;
 }
 
 }  // extern "C"

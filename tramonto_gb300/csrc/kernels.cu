@@ -1248,4 +1248,135 @@ void launch_check_finite(const double *x, long n, double *partial, int nblocks, 
   k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
 }
 
+// ---------------------------------------------------------------------------
+// Objectives of a state: the surface excess grand free energy Omega_s of
+// calc_free_energy (src/dft_energy.c:31-168: ideal gas, chemical potential,
+// external field, hard-sphere and mean-field terms, each minus its bulk term)
+// and the excess adsorption of calc_adsorption (src/dft_out_ads.c:33-112),
+// both as integrateInSpace sums (src/dft_out_utils.c:38-62) with per-node
+// weights wf (Nel_hit2) and wb (Nel_hit) that already hold Vol_el /
+// Nnodes_per_el_V and the area / reflection factors.  The mean-field term takes
+// the attraction sums S_ic (int_stencil, src/dft_energy_CLSintsten.c:73) of
+// the densities; the hard-sphere term Phi(n) reads the weighted-density
+// unknowns and uses component 0's wb, as integrand_hs_freen does.
+// partial rows: [0] Omega_s, [1 + ic] Gamma_ex[ic].
+__global__ void k_objectives(const double *__restrict__ x, const double *__restrict__ vext,
+                             const double *__restrict__ satt, const double *__restrict__ wf,
+                             const double *__restrict__ wb, ObjConst oc, double *__restrict__ partial)
+{
+  __shared__ double sh[32];
+  const long N = c_g.N;
+  const int nc = c_g.ncomp;
+  double om = 0.0, gam[kMaxC];
+  for (int ic = 0; ic < kMaxC; ic++) gam[ic] = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    for (int ic = 0; ic < nc; ic++) {
+      const long k = (long)ic * N + i;
+      const double rho = x[(long)(c_g.first_rho + ic) * N + i];
+      double e = 0.0;
+      if (rho > kDensityMin) e = rho * (log(rho) - 1.0) - rho * oc.betamu[ic] + rho * vext[k];
+      if (c_g.attraction && rho > 0.0) e += 0.5 * rho * satt[k];
+      om += wf[k] * e - wb[k] * oc.bulk[ic];
+      gam[ic] += wf[k] * rho - wb[k] * c_g.rho_b[ic];
+    }
+    double n[kMaxRb];
+    load_n(x, i, n);
+    om += wb[i] * (fmt_phi(n, c_g.ndim, c_g.functional) - oc.phi_b);
+  }
+  om = block_sum(om, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = om;
+  for (int ic = 0; ic < nc; ic++) {
+    const double v = block_sum(gam[ic], sh);
+    if (threadIdx.x == 0) partial[(long)(1 + ic) * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+void launch_objectives(const double *x, const double *vext, const double *satt, const double *wf, const double *wb,
+                       const ObjConst &oc, int ncomp, double *partial, int nblocks, double *result, cudaStream_t s)
+{
+  k_objectives<<<nblocks, kThreads, 0, s>>>(x, vext, satt, wf, wb, oc, partial);
+  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1 + ncomp, result);
+}
+
+// Partial derivatives of an objective at fixed V_ext.
+//   kind 0 (Omega_s): d/drho_ic = wf (ln rho - betamu + V) + wf S/2 and, from the
+//   other nodes' mean-field terms, T_ic/2 (added by the caller: the transposed
+//   attraction sums of wf rho); d/dn_k = wb0 dPhi/dn_k; d/dV_ic = wf rho.
+//   kind 1 (Gamma_ex[icomp]): d/drho_icomp = wf.
+// gx [nunk][N], gv [ncomp][N]; the MF unknowns do not enter (the mean-field
+// term integrates the attraction sums of the densities, not the unknowns).
+// chan (kind 0, attraction): wf rho on rho > 0 nodes per component [ncomp][N].
+__global__ void k_objective_grad(const double *__restrict__ x, const double *__restrict__ vext,
+                                 const double *__restrict__ satt, const double *__restrict__ wf,
+                                 const double *__restrict__ wb, ObjConst oc, int kind, int icomp,
+                                 double *__restrict__ gx, double *__restrict__ gv, double *__restrict__ chan)
+{
+  const long N = c_g.N;
+  const int nc = c_g.ncomp;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    for (int u = 0; u < c_g.nunk; u++) gx[(long)u * N + i] = 0.0;
+    for (int ic = 0; ic < nc; ic++) {
+      const long k = (long)ic * N + i;
+      const double rho = x[(long)(c_g.first_rho + ic) * N + i];
+      double g = 0.0, v = 0.0;
+      if (kind == 0) {
+        if (rho > kDensityMin) {
+          g = wf[k] * (log(rho) - oc.betamu[ic] + vext[k]);
+          v = wf[k] * rho;
+        }
+        if (c_g.attraction) {
+          if (rho > 0.0) g += 0.5 * wf[k] * satt[k];
+          chan[k] = rho > 0.0 ? wf[k] * rho : 0.0;
+        }
+      } else if (ic == icomp) {
+        g = wf[k];
+      }
+      gx[(long)(c_g.first_rho + ic) * N + i] = g;
+      gv[k] = v;
+    }
+    if (kind == 0) {
+      double n[kMaxRb], d[kMaxRb];
+      load_n(x, i, n);
+      fmt_dphi(n, d);
+      const int nd = c_g.ndim;
+      const double w0 = wb[i];
+      double *G = gx + (long)c_g.first_rb * N + i;
+      G[0] = w0 * d[3];
+      G[N] = w0 * d[2];
+      G[2 * N] = w0 * d[1];
+      G[3 * N] = w0 * d[0];
+      for (int dd = 0; dd < nd; dd++) {
+        G[(long)(4 + dd) * N] = w0 * d[4 + nd + dd];
+        G[(long)(4 + nd + dd) * N] = w0 * d[4 + dd];
+      }
+    }
+  }
+}
+
+void launch_objective_grad(const double *x, const double *vext, const double *satt, const double *wf,
+                           const double *wb, const ObjConst &oc, int kind, int icomp, double *gx, double *gv,
+                           double *chan, cudaStream_t s)
+{
+  k_objective_grad<<<1184, kThreads, 0, s>>>(x, vext, satt, wf, wb, oc, kind, icomp, gx, gv, chan);
+}
+
+// dF/dV_ext = dF/dV|_x - lambda on the Euler-Lagrange rows (which hold +V_ext), 0 on zero-density rows
+__global__ void k_vext_sens(const double *__restrict__ lam, const double *__restrict__ gv,
+                            const double *__restrict__ vext, const signed char *__restrict__ zero,
+                            double *__restrict__ out)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long k = (long)ic * N + i;
+      out[k] = zero_row(vext, zero, ic, i) ? gv[k] : gv[k] - lam[(long)(c_g.first_rho + ic) * N + i];
+    }
+}
+
+void launch_vext_sens(const double *lam, const double *gv, const double *vext, const signed char *zero, double *out,
+                      cudaStream_t s)
+{
+  k_vext_sens<<<1184, kThreads, 0, s>>>(lam, gv, vext, zero, out);
+}
+
 }  // namespace tgpu

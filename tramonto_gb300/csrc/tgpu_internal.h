@@ -12,6 +12,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include <string>
 #include <vector>
 
@@ -36,6 +38,43 @@ struct DevGeom {
   double dphi_bulk[4], vext_max;
   const int *map[3];                   // per-dimension padded -> source maps
 };
+
+constexpr double kDensityMin = 1.e-20;   // integrands vanish at or below this density (DENSITY_MIN)
+
+// Constants of the free-energy objective: per component the chemical potential
+// betamu and the bulk integrand rho_b(ln rho_b - 1) - rho_b betamu [+ rho_b betamu_att / 2],
+// and the hard-sphere energy density of the bulk weighted densities.
+struct ObjConst {
+  double betamu[kMaxC];
+  double bulk[kMaxC];
+  double phi_b;
+};
+
+// FMT free-energy density Phi(n), n in the order n0 n1 n2 n3 V1[d] V2[d]:
+// Rosenfeld (FMT1_energy_density src/dft_physics_FMT1.c:39-57) or White-Bear
+// (FMT3_energy_density src/dft_physics_FMT3.c:39-58).  For n3 <= 1e-10 the
+// White-Bear third term takes its n3 -> 0 limit, the Rosenfeld form (the
+// reference's expression is 0/0 at n3 = 0).
+__host__ __device__ inline double fmt_phi(const double *n, int ndim, int functional)
+{
+  double dot12 = 0.0, dot22 = 0.0;
+  for (int d = 0; d < ndim; d++) {
+    dot12 += n[4 + d] * n[4 + ndim + d];
+    dot22 += n[4 + ndim + d] * n[4 + ndim + d];
+  }
+  const double one = 1.0 - n[3];
+  const double l = log(one);
+  const double p1 = -n[0] * l;
+  const double p2 = (n[1] * n[2] - dot12) / one;
+  const double c3 = n[2] * n[2] * n[2] - 3.0 * n[2] * dot22;
+  const double pi = 3.141592653589793238462643383279502884197;
+  double p3;
+  if (functional == TGPU_FMT3 && n[3] > 1.e-10)
+    p3 = c3 * (n[3] + one * one * l) / (36.0 * pi * n[3] * n[3] * one * one);
+  else
+    p3 = c3 / (24.0 * pi * one * one);
+  return p1 + p2 + p3;
+}
 
 // One stencil table on the device: linear offsets in the padded box and the
 // per-point coefficient rows for each output channel.
@@ -159,6 +198,13 @@ void launch_norm2(const double *x, long n, double *partial, int nblocks, double 
 // J^T w local step: A22, A11^T (with B^T), the MF coupling and H g for the rb columns
 void launch_jtv_local(const double *x, const double *vext, const signed char *zero, const double *w,
                       const double *gel, int gstride_ic, int v2_first, double *out, cudaStream_t s);
+void launch_objectives(const double *x, const double *vext, const double *satt, const double *wf, const double *wb,
+                       const ObjConst &oc, int ncomp, double *partial, int nblocks, double *result, cudaStream_t s);
+void launch_objective_grad(const double *x, const double *vext, const double *satt, const double *wf,
+                           const double *wb, const ObjConst &oc, int kind, int icomp, double *gx, double *gv,
+                           double *chan, cudaStream_t s);
+void launch_vext_sens(const double *lam, const double *gv, const double *vext, const signed char *zero, double *out,
+                      cudaStream_t s);
 void launch_adj_rb_channels(const double *w, double *chan, cudaStream_t s);
 void launch_a11inv_t(const double *u, double *y, cudaStream_t s);
 void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,

@@ -100,6 +100,13 @@ def load(build_if_missing: bool = False):
         "tgpu_newton_solve_device": [vp, vp, C.c_double, C.c_int, C.c_double, C.c_int, C.c_double, ip, dp, ip],
         "tgpu_time_stencil_sum": [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp],
         "tgpu_get_stats": [vp, C.POINTER(Stats)], "tgpu_reset_stats": [vp],
+        "tgpu_set_integration": [vp, vp, vp, vp, vp],
+        "tgpu_objectives": [vp, vp, dp, dp], "tgpu_objectives_device": [vp, vp, dp, dp],
+        "tgpu_objective_grad_device": [vp, vp, C.c_int, C.c_int, vp, vp],
+        "tgpu_grad_vext_device": [vp, vp, C.c_int, C.c_int, C.c_double, C.c_int, vp, ip],
+        "tgpu_grad_omega_vext": [vp, vp, C.c_double, C.c_int, vp, ip],
+        "tgpu_grad_gamma_vext": [vp, vp, C.c_int, C.c_double, C.c_int, vp, ip],
+        "tgpu_grad_epsw": [vp, vp, C.c_int, C.c_int, vp, C.c_double, C.c_int, dp, ip],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -166,6 +173,8 @@ class Solver:
                 _check(lib.tgpu_set_hard_wall(self.h, _ptr(bn), _ptr(fm)), lib)
             _check(lib.tgpu_finalize(self.h), lib)
             self.set_precision(precision)
+            if p.w_fluid is not None:
+                self.set_integration(p.w_fluid, p.w_bulk, p.rhobar_b, p.betamu)
         except Exception:
             self.close()
             raise
@@ -188,6 +197,56 @@ class Solver:
         """Replace V_ext/kT ([ncomp][N]); nodes equal to vext_max stay zero-density rows."""
         v = self._host(vext, (self.p.ncomp, self.N))
         _check(self.lib.tgpu_set_vext(self.h, _ptr(v)), self.lib)
+
+    def set_integration(self, w_fluid, w_bulk, rhobar_b, betamu):
+        """Integration weights ([ncomp][N] each), bulk n3 n2 n1 n0 and betamu of the objectives."""
+        nc = self.p.ncomp
+        wf = np.ascontiguousarray(w_fluid, np.float64).reshape(nc, -1)
+        wb = np.ascontiguousarray(w_bulk, np.float64).reshape(nc, -1)
+        rb = np.ascontiguousarray(rhobar_b, np.float64).reshape(4)
+        bm = np.ascontiguousarray(betamu, np.float64).reshape(nc)
+        _check(self.lib.tgpu_set_integration(self.h, _ptr(wf), _ptr(wb), _ptr(rb), _ptr(bm)), self.lib)
+
+    def objectives(self, x):
+        """(Omega_s, Gamma_ex[ncomp]) of the state x (host array)."""
+        x = self._host(x, self.shape)
+        om = C.c_double(0.0)
+        gam = np.zeros(self.p.ncomp)
+        _check(self.lib.tgpu_objectives(self.h, _ptr(x), C.byref(om), gam.ctypes.data_as(C.POINTER(C.c_double))), self.lib)
+        return om.value, gam
+
+    def objective_grad(self, x, kind=0, icomp=0):
+        """(dF/dx, dF/dV_ext at fixed x) of Omega_s (kind 0) or Gamma_ex[icomp] (kind 1); host arrays."""
+        import torch
+        xt = torch.tensor(self._host(x, self.shape), dtype=torch.float64, device="cuda")
+        gx = torch.empty_like(xt)
+        gv = torch.empty((self.p.ncomp, self.N), dtype=torch.float64, device="cuda")
+        _check(self.lib.tgpu_objective_grad_device(self.h, self._dptr(xt), kind, icomp, self._dptr(gx),
+                                                   self._dptr(gv)), self.lib)
+        torch.cuda.synchronize()
+        return gx.cpu().numpy(), gv.cpu().numpy()
+
+    def grad_vext(self, x, kind=0, icomp=0, tol=1e-12, max_iter=500):
+        """dF/dV_ext ([ncomp][N]) of Omega_s (kind 0) or Gamma_ex[icomp] (kind 1) at the converged state x."""
+        x = self._host(x, self.shape)
+        out = np.empty((self.p.ncomp, self.N))
+        it = C.c_int(0)
+        if kind == 0:
+            st = self.lib.tgpu_grad_omega_vext(self.h, _ptr(x), tol, max_iter, _ptr(out), C.byref(it))
+        else:
+            st = self.lib.tgpu_grad_gamma_vext(self.h, _ptr(x), icomp, tol, max_iter, _ptr(out), C.byref(it))
+        _check(st, self.lib)
+        return out
+
+    def grad_param(self, x, dvext_dp, kind=0, icomp=0, tol=1e-12, max_iter=500):
+        """dF/dp for a wall parameter p entering through V_ext (dvext_dp = dV_ext/dp, [ncomp][N])."""
+        x = self._host(x, self.shape)
+        dv = self._host(dvext_dp, (self.p.ncomp, self.N))
+        val = C.c_double(0.0)
+        it = C.c_int(0)
+        _check(self.lib.tgpu_grad_epsw(self.h, _ptr(x), kind, icomp, _ptr(dv), tol, max_iter, C.byref(val),
+                                       C.byref(it)), self.lib)
+        return val.value
 
     def set_precision(self, precision: int):
         _check(self.lib.tgpu_set_precision(self.h, int(precision)), self.lib)

@@ -53,6 +53,12 @@ class Problem:
     boundary_nodes: np.ndarray = None  # [nlists][N] int32, -1 = not a boundary node
     fluid_masks: np.ndarray = None     # [nlists][2^ndim][N] int16
     stencils: dict = field(default_factory=dict)
+    # integration (objectives Omega_s and Gamma_ex): per-node weights [ncomp][N] of integrateInSpace with
+    # Nel_hit2 (w_fluid) and Nel_hit (w_bulk), the bulk weighted densities n3 n2 n1 n0 and betamu
+    w_fluid: np.ndarray = None
+    w_bulk: np.ndarray = None
+    rhobar_b: np.ndarray = None
+    betamu: np.ndarray = None
 
     # ---- unknown layout (setup_nunk_per_node, src/dft_defs_unknowns.c:37-176)
     @property
@@ -117,4 +123,13 @@ def from_golden(z) -> Problem:
         fluid_masks=np.asarray(z["fluid_masks"], np.int16) if "fluid_masks" in z.files else None,
         stencils=st)
     assert p.nunk == int(ints[7]), (p.nunk, int(ints[7]))
+    if "integ" in z.files:
+        integ = np.asarray(z["integ"])
+        vol_el, nel_v, area, fac_vol, fac_area, per_area = integ[:6]
+        scale = fac_vol / (fac_area * area) if (per_area and area > 0) else fac_vol
+        unit = vol_el / nel_v * scale
+        p.w_fluid = np.asarray(z["nel_hit2"], np.float64) * unit
+        p.w_bulk = np.asarray(z["nel_hit"], np.float64) * unit
+        p.rhobar_b = np.array(d[55:59])
+        p.betamu = np.array(integ[6:6 + ncomp])
     return p
