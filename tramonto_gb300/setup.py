@@ -135,13 +135,31 @@ def build_problem(ndim, nx, esize, bc, hs_diam, rho_b, functional=FMT1, attracti
         vext = np.zeros((nc, N))
     if zero_density is None:
         zero_density = (vext >= vext_max).astype(np.int8)
+    w = integration_weights(ndim, nx, esize, bc)
+    betamu = np.log(np.asarray(rho_b, float)) + b["betamu_hs_ex"] + b["betamu_att"]
     return Problem(ndim=ndim, nx=tuple(nx), esize=tuple(esize), bc=tuple(bc), ncomp=nc, functional=functional,
                    attraction=int(attraction), att_in_a22=0, single_size=int(nc == 1), hard_surf=0, nlists_hw=1,
                    rho_b=np.asarray(rho_b, float), hs_diam=np.asarray(hs_diam, float), betamu_hs_ex=b["betamu_hs_ex"],
                    betamu_att=b["betamu_att"], inv_rad=b["inv_rad"], inv_4pir=b["inv_4pir"],
                    inv_4pirsq=b["inv_4pirsq"], fac_overlap=np.ones(nc), dphi_bulk=b["dphi_bulk"],
                    vext_max=vext_max, vext=np.ascontiguousarray(vext, float),
-                   zero_density=np.ascontiguousarray(zero_density, np.int8), stencils=st)
+                   zero_density=np.ascontiguousarray(zero_density, np.int8), stencils=st,
+                   w_fluid=np.tile(w, (nc, 1)), w_bulk=np.tile(w, (nc, 1)), rhobar_b=b["rhobar_b"], betamu=betamu)
+
+
+def integration_weights(ndim, nx, esize, bc):
+    """Per-node integration weights of a box without wall elements: Vol_el times the fraction of the
+    node's 2^ndim elements that lie in the box (setup_integrals, src/dft_out_utils.c:179-270, with no
+    surfaces), i.e. the trapezoid rule with half weights on non-periodic faces.  [N]"""
+    w = np.ones(1)
+    for d in range(ndim):
+        f = np.ones(nx[d])
+        if bc[d][0] != BC_PERIODIC:
+            f[0] *= 0.5
+        if bc[d][1] != BC_PERIODIC:
+            f[-1] *= 0.5
+        w = np.multiply.outer(f, w)          # slowest index last: [.., d] -> node = x + nx*(y + ny*z)
+    return (w * float(np.prod(esize[:ndim]))).reshape(-1)
 
 
 # ---- synthetic workloads ----------------------------------------------------
@@ -216,38 +234,67 @@ def config2(n=128, esize=0.1, seed=1234):
     return p, meta
 
 
-def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0):
-    """3-D binary White-Bear (FMT3) hard spheres (sigma 1 and 0.5, rho_b 0.3 and 0.6) in a
-    cylindrical pore of radius 5 along z; V_ext += 0.5 kT * Gaussian random field (corr. length 1)."""
-    es = (esize,) * 3
-    N = int(np.prod(nx))
+def gaussian_random_field(nx, esize, corr_len=1.0, seed=4321):
+    """Zero-mean, unit-variance Gaussian random field on the periodic box (numpy PCG64 `seed`): white noise filtered in
+    Fourier space by exp(-k^2 corr_len^2 / 2), so the covariance falls as exp(-r^2 / (4 corr_len^2)). [nz][ny][nx]"""
     rng = np.random.default_rng(seed)
-    white = rng.standard_normal(nx[::-1])
-    # Gaussian filter with correlation length 1 sigma in Fourier space (periodic)
-    k = [np.fft.fftfreq(m, d=esize) * 2 * PI for m in nx[::-1]]
+    white = rng.standard_normal(tuple(nx[::-1]))
+    k = [np.fft.fftfreq(m, d=esize[0]) * 2 * PI for m in nx[::-1]]
     kk = k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2 + k[2][None, None, :] ** 2
-    g = np.real(np.fft.ifftn(np.fft.fftn(white) * np.exp(-0.5 * kk * 1.0 ** 2)))
-    g /= g.std()
-    x = (np.arange(nx[0]) - (nx[0] - 1) / 2) * esize
-    y = (np.arange(nx[1]) - (nx[1] - 1) / 2) * esize
+    g = np.real(np.fft.ifftn(np.fft.fftn(white) * np.exp(-0.5 * kk * corr_len ** 2)))
+    g -= g.mean()
+    return g / g.std()
+
+
+def pore_vext(nx, esize, hs_diam, eps_w, field, pore_radius=5.0, grf_amplitude=0.5, vext_max=10.0):
+    """V_ext/kT of a cylindrical pore along z (axis at the box centre in x, y) and its eps_w derivative.
+
+    Species i sees amplitude * field plus a soft cut-and-shifted 9-3 shell eps_w f_i(d) (the form of
+    Vext_LJ9_3_CS, src/dft_vext_1D.c:42-56) of the distance d = R - r from the pore surface, with
+    sigma_wf = (sigma_i + 1)/2 and cut 2.5 sigma_wf.  Nodes with d <= 0 or V >= vext_max hold vext_max
+    (zero-density rows).  Returns (V [ncomp][N], dV/deps_w [ncomp][N], zero-density flags [ncomp][N])."""
+    x = (np.arange(nx[0]) - (nx[0] - 1) / 2) * esize[0]
+    y = (np.arange(nx[1]) - (nx[1] - 1) / 2) * esize[1]
     r = np.sqrt(x[None, None, :] ** 2 + y[None, :, None] ** 2) * np.ones((nx[2], 1, 1))
-    outside = r >= pore_radius
-    v1 = np.where(outside, 10.0, 0.5 * g).reshape(-1)
-    vext = np.stack([v1, v1])
-    zd = np.stack([outside.reshape(-1), outside.reshape(-1)]).astype(np.int8)
+    d = (pore_radius - r).reshape(-1)
+    g = grf_amplitude * np.asarray(field).reshape(-1)
+    vs, ds, zs = [], [], []
+    for sig in hs_diam:
+        swf = 0.5 * (sig + 1.0)
+        v, de, _ = lj93_wall_1d(d, eps_w, swf, 2.5 * swf, vext_max=np.inf)
+        v = np.where(d > 0, v + g, vext_max)
+        zero = (d <= 0) | (v >= vext_max)
+        vs.append(np.where(zero, vext_max, v))
+        ds.append(np.where(zero, 0.0, de))
+        zs.append(zero)
+    return np.array(vs), np.array(ds), np.array(zs, np.int8)
+
+
+def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0, eps_w=0.5):
+    """3-D binary White-Bear (FMT3) hard spheres (sigma 1 and 0.5, rho_b 0.3 and 0.6) in a cylindrical pore
+    of radius 5 along z with a soft 9-3 shell of strength eps_w; V_ext += 0.5 kT * Gaussian random field
+    (correlation length 1).  Walls outside the box in x and y, periodic in z."""
+    es = (esize,) * 3
+    field = gaussian_random_field(nx, es, 1.0, seed)
+    vext, dv_deps, zd = pore_vext(nx, es, [1.0, 0.5], eps_w, field, pore_radius)
     p = build_problem(3, nx, es, ((BC_IN_WALL, BC_IN_WALL), (BC_IN_WALL, BC_IN_WALL), (BC_PERIODIC, BC_PERIODIC)),
                       hs_diam=[1.0, 0.5], rho_b=[0.3, 0.6], functional=FMT3, vext=vext, zero_density=zd)
-    return p, dict(grid=list(nx), dx=esize, seed=seed, pore_radius=pore_radius, rho_b=[0.3, 0.6],
-                   functional="FMT3", field="0.5 kT Gaussian random field, correlation length 1")
+    return p, dict(grid=list(nx), dx=esize, seed=seed, pore_radius=pore_radius, rho_b=[0.3, 0.6], eps_w=eps_w,
+                   functional="FMT3", field="0.5 kT Gaussian random field, correlation length 1",
+                   shell="eps_w * 9-3 cut-and-shifted, sigma_wf=(sigma_i+1)/2, cut 2.5 sigma_wf",
+                   grf=field, dv_deps=dv_deps)
 
 
-def initial_state(solver, p: Problem):
-    """Density rho_b*exp(-V) (0 in walls); weighted densities and mean field from their own sums."""
+def initial_state(solver, p: Problem, max_enhancement=None):
+    """Density rho_b*exp(-V) (0 in walls; at most max_enhancement*rho_b when given); weighted densities
+    and mean field from their own sums."""
     N = p.nnodes
     x = np.zeros((p.nunk, N))
     for c in range(p.ncomp):
         v = p.vext[c]
         rho = p.rho_b[c] * np.exp(-np.minimum(v, 50.0))
+        if max_enhancement is not None:
+            rho = np.minimum(rho, max_enhancement * p.rho_b[c])
         rho[p.zero_density[c] != 0] = 0.0
         rho[v >= p.vext_max] = 0.0
         x[p.first_rho + c] = np.maximum(rho, 0.0)
