@@ -61,7 +61,7 @@ enum { TGPU_FMT1 = 0, TGPU_FMT3 = 2 };
 /* stencil types (reference Stencil ids, src/dft_globals_const.h:152-161) */
 enum { TGPU_STEN_DELTA = 0, TGPU_STEN_THETA = 1, TGPU_STEN_UATT = 2 };
 /* arithmetic of the stencil convolutions */
-enum { TGPU_FP64 = 0, TGPU_FP32 = 1, TGPU_BF16X3 = 2 };
+enum { TGPU_FP64 = 0, TGPU_FP32 = 1, TGPU_BF16X3 = 2, TGPU_FP16TC = 3 };
 
 #define TGPU_MAXC 4
 
@@ -103,8 +103,10 @@ int tgpu_set_zero_density(tgpu_handle h, const signed char *flags);   /* [ncomp]
  * as local corner l (for that reflection pattern) is fluid (src/dft_utils.c:41-62). */
 int tgpu_set_hard_wall(tgpu_handle h, const int *boundary_nodes, const short *fluid_masks);
 int tgpu_finalize(tgpu_handle h);
-/* Arithmetic of the Jacobian / Schur products (TGPU_FP64 or TGPU_FP32); the
- * residual fill always sums in FP64. */
+/* Arithmetic of the Jacobian / Schur products: TGPU_FP64, TGPU_FP32 (stencil sums in FP32), or
+ * TGPU_FP16TC (as TGPU_FP32, but the 3-D attraction sums on the tensor cores: FP16 inputs scaled by
+ * powers of two, FP32 accumulation; TGPU_ERR_UNSUPPORTED when the problem has none).  The residual
+ * fill's arithmetic is set by tgpu_set_fill_arithmetic. */
 int tgpu_set_precision(tgpu_handle h, int precision);
 /* Arithmetic of the residual fill:
  *   TGPU_FILL_FP64     every stencil sum in FP64 (default; the reference's arithmetic)

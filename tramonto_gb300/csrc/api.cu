@@ -138,6 +138,10 @@ struct Ctx : tgpu_ctx {
   // adjoint work buffers (allocated on first use)
   double *d_adj_chan = nullptr, *d_adj_pad = nullptr, *d_adj_g = nullptr, *d_adj_v = nullptr, *d_adj_t = nullptr;
   // objectives (Omega_s, Gamma_ex): integration weights and work buffers
+  // tensor-core attraction sums: the FP16 slab, whether it exists, whether the current call uses it
+  tgpu::TcSlab tcslab{};
+  bool tc_ready = false, tc_on = false;
+  std::string tc_why;
   bool have_integ = false;
   tgpu::ObjConst oc{};
   double *d_wf = nullptr, *d_wb = nullptr;
@@ -205,6 +209,12 @@ void pad(Ctx *c, const double *src, const PadParams &pp, bool f32)
 void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool f32)
 {
   const long NP = c->dg.NP;
+  if (f32 && c->tc_on && !tr && nin == 1 && nout == 1 && st.tc.nplanes > 0) {
+    tgpu::launch_sten_tc(c->d_pad32 + (long)ch0 * NP, c->dg, c->tcslab, st.tc, outs[0], true, c->stream);
+    c->stats.conv_launches++;
+    c->stats.kernel_launches += 4;
+    return;
+  }
   if (f32 && nin == 1 && nout == 1) {
     const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
     if (ln.nplanes > 0) {
@@ -372,10 +382,19 @@ void need_state(Ctx *c)
   if (!c->have_state) throw Error(TGPU_ERR_STATE, "no Jacobian state: call tgpu_fill with mode 0 first");
 }
 
+// Jacobian / Schur products run their 3-D attraction sums on the tensor cores in TGPU_FP16TC
+struct TcScope {
+  Ctx *c;
+  bool prev;
+  explicit TcScope(Ctx *c_) : c(c_), prev(c_->tc_on) { c->tc_on = c->precision == TGPU_FP16TC && c->tc_ready; }
+  ~TcScope() { c->tc_on = prev; }
+};
+
 void schur_device(Ctx *c, const double *d_v2, double *d_y2)
 {
   need_state(c);
-  const bool f32 = c->precision == TGPU_FP32;
+  TcScope tcs(c);
+  const bool f32 = c->precision != TGPU_FP64;
   forward_pass(c, d_v2, c->pads.rho_jac, f32);
   tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, c->stream);
   transpose_pass(c, c->pads.tr_jac, f32);
@@ -387,8 +406,9 @@ void schur_device(Ctx *c, const double *d_v2, double *d_y2)
 void jv_device(Ctx *c, const double *d_v, double *d_out)
 {
   need_state(c);
+  TcScope tcs(c);
   const long N = c->dg.N;
-  const bool f32 = c->precision == TGPU_FP32;
+  const bool f32 = c->precision != TGPU_FP64;
   forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, f32);
   tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, c->stream);
   transpose_pass(c, c->pads.tr_jac, f32);
@@ -412,7 +432,8 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
 {
   need_state(c);
   tgpu::launch_rhs_local(c->d_x, d_b, c->d_chan, c->d_ymf, c->stream);
-  transpose_pass(c, c->pads.tr_jac, c->precision == TGPU_FP32);
+  TcScope tcs(c);
+  transpose_pass(c, c->pads.tr_jac, c->precision != TGPU_FP64);
   tgpu::launch_rhs_combine(c->d_vext, c->d_zero, d_b, c->d_tr, c->d_ymf, d_b2s, c->stream);
   c->stats.kernel_launches += 2;
 }
@@ -420,7 +441,8 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
 void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx)
 {
   need_state(c);
-  forward_pass(c, d_x2, c->pads.rho_jac, c->precision == TGPU_FP32);
+  TcScope tcs(c);
+  forward_pass(c, d_x2, c->pads.rho_jac, c->precision != TGPU_FP64);
   tgpu::launch_x1(d_b, c->d_conv, d_x2, d_dx, c->stream);
   c->stats.kernel_launches++;
 }
@@ -441,6 +463,7 @@ void red_to_host(Ctx *c, int n)
   ck(cudaStreamSynchronize(c->stream), "sync");
 }
 
+void tc_check(Ctx *c);
 void schur_t_device(Ctx *c, const double *d_v2, double *d_y2);
 
 int gmres(Ctx *c, const double *d_rhs, double *d_x2, double tol, int maxit, int *iters, double *relres)
@@ -671,6 +694,7 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
   *iters = it;
   if (final_resid) *final_resid = rnorm;
   if (lin_iters_total) *lin_iters_total = lin_total;
+  tc_check(c);
   return converged ? TGPU_OK : TGPU_ERR_NOCONV;
 }
 
@@ -909,6 +933,19 @@ int grad_vext_device(Ctx *c, const double *d_x, int kind, int icomp, double tol,
   return st;
 }
 
+// A bounded wait of the tensor-core kernel that ran out leaves a flag on the device.
+void tc_check(Ctx *c)
+{
+  if (!c->tc_ready) return;
+  int err = 0;
+  ck(cudaMemcpyAsync(&err, c->tcslab.d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "d2h");
+  ck(cudaStreamSynchronize(c->stream), "sync");
+  if (err) {
+    ck(cudaMemsetAsync(c->tcslab.d_err, 0, sizeof(int), c->stream), "memset");
+    throw Error(TGPU_ERR_CUDA, "tensor-core stencil sum: a bounded wait ran out (code " + std::to_string(err) + ")");
+  }
+}
+
 // Host-pointer wrappers: copy in, run on the device, copy out, synchronise.
 void h2d(Ctx *c, double *d, const double *h, size_t n)
 {
@@ -918,6 +955,7 @@ void d2h(Ctx *c, double *h, const double *d, size_t n)
 {
   ck(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "d2h");
   ck(cudaStreamSynchronize(c->stream), "sync");
+  tc_check(c);
 }
 
 // Regroup a 3-D stencil by z offset into x-lines of constant oy for the FP32
@@ -1068,6 +1106,7 @@ void build_device_tables(Ctx *c)
         st.lines_fwd = build_lines(st, fwd, dg, c->stream);
         if (t == TGPU_STEN_THETA) st.lines_tr = build_lines(st, tr, dg, c->stream);
       }
+      if (nd == 3 && t == TGPU_STEN_UATT) tgpu::tc_build_tables(st.off, fwd, st.L, dg.h[1], st.tc, c->stream);
     }
   const long N = dg.N;
   // fields
@@ -1255,8 +1294,10 @@ int tgpu_destroy(tgpu_handle h)
         dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
         dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
         for (auto *L : {&st.lines_fwd, &st.lines_tr}) { dfree(L->d_planes); dfree(L->d_lines); dfree(L->d_w); }
+        tgpu::tc_free_tables(st.tc);
       }
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
+    tgpu::tc_free_slab(c->tcslab);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);
     dfree(c->d_x); dfree(c->d_work); dfree(c->d_work2); dfree(c->d_pad); dfree(c->d_pad32); dfree(c->d_chan);
     dfree(c->d_conv); dfree(c->d_tr); dfree(c->d_ymf); dfree(c->d_b2s); dfree(c->d_V); dfree(c->d_partial);
@@ -1355,6 +1396,10 @@ int tgpu_finalize(tgpu_handle h)
     if (g.hard_surf && c->h_bnodes.empty()) throw Error(TGPU_ERR_STATE, "hard surfaces need tgpu_set_hard_wall");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     build_device_tables(c);
+    bool any_tc = false;
+    for (auto &st : c->sten[TGPU_STEN_UATT]) any_tc = any_tc || st.tc.nplanes > 0;
+    if (any_tc) c->tc_ready = tgpu::tc_make_slab(c->tcslab, c->dg, c->tc_why);
+    else c->tc_why = "no 3-D attraction stencil";
     c->finalized = true;
     return TGPU_OK;
   });
@@ -1364,7 +1409,10 @@ int tgpu_set_precision(tgpu_handle h, int precision)
 {
   return guard([&] {
     Ctx *c = C(h);
-    if (precision != TGPU_FP64 && precision != TGPU_FP32) throw Error(TGPU_ERR_UNSUPPORTED, "precision");
+    if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC)
+      throw Error(TGPU_ERR_UNSUPPORTED, "precision");
+    if (precision == TGPU_FP16TC && !c->tc_ready)
+      throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
     c->precision = precision;
     return TGPU_OK;
   });
@@ -1586,7 +1634,11 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     if (type < 0 || type > 2 || index < 0 || index >= (int)c->sten[type].size() || c->sten[type][index].L == 0)
       throw Error(TGPU_ERR_ARG, "no such stencil");
     if (reps < 1) throw Error(TGPU_ERR_ARG, "reps");
-    const bool f32 = precision == TGPU_FP32;
+    const bool f32 = precision == TGPU_FP32 || precision == TGPU_FP16TC;
+    if (precision == TGPU_FP16TC && !c->tc_ready)
+      throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
+    const bool tc_prev = c->tc_on;
+    c->tc_on = precision == TGPU_FP16TC;
     const DevStencil &st = c->sten[type][index];
     const int jc = type == TGPU_STEN_UATT ? index / c->dg.ncomp : index;
     const long N = c->dg.N;
@@ -1605,6 +1657,8 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
     c->ev0 = c->ev1 = nullptr;
+    c->tc_on = tc_prev;
+    tc_check(c);
     *ms_per_sum = ms / reps;
     return TGPU_OK;
   });

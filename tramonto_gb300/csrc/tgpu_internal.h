@@ -10,6 +10,7 @@
 //     (padded centre + precomputed linear offset).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -76,6 +77,26 @@ __host__ __device__ inline double fmt_phi(const double *n, int ndim, int functio
   return p1 + p2 + p3;
 }
 
+// Tensor-core form of a large 3-D single-channel stencil sum (wca_tc.cu): tiles of
+// kTcN x-outputs by kTcM y-rows; the field slab spans kTcN + 2 kTcXHalo x-inputs.
+constexpr int kTcN = 64, kTcM = 128, kTcXHalo = 32, kTcCores = 24, kTcRing = 8;
+
+struct TcTables {                 // per stencil: lines grouped by z offset, Hankel tables
+  int4 *d_planes = nullptr;       // {oz, first line, lines, 0}
+  int4 *d_lines = nullptr;        // {oy, first K-step, last K-step, table}
+  void *d_tables = nullptr;       // FP16 [table][high, low][24][8][8]
+  int nplanes = 0, nlines = 0;
+  double out_mult = 1.0;          // 1 / weight scale
+};
+
+struct TcSlab {                   // per problem: the FP16 copy of a padded channel and its TMA map
+  CUtensorMap tmap;
+  void *d_slab = nullptr;         // FP16 [high, low][Zp][G][Yp][8]
+  float *d_scale = nullptr;       // [0] field scale, [1] max |field| (bits)
+  int *d_err = nullptr;           // nonzero after a bounded wait ran out
+  int G = 0, Yp = 0, Zp = 0, R = 0, hy = 0, hz = 0, nring = 0;
+};
+
 // One stencil table on the device: linear offsets in the padded box and the
 // per-point coefficient rows for each output channel.
 struct DevStencil {
@@ -93,6 +114,7 @@ struct DevStencil {
   double *d_coef_tr = nullptr;          // [L][nin_tr]
   float *d_coef_tr32 = nullptr;
   double *d_coef_adj = nullptr;         // delta only: [L][1+ndim] fac (w, e_d w) for the transposed sums
+  TcTables tc;                          // tensor-core form (3-D attraction stencils)
   short *d_off = nullptr;               // [L][3] raw offsets (boundary corrections)
   double *d_w = nullptr, *d_hw = nullptr;
   // z-plane / x-line form for the FP32 single-channel sums (3-D): forward and transpose coefficients
@@ -205,6 +227,13 @@ void launch_objective_grad(const double *x, const double *vext, const double *sa
                            double *chan, cudaStream_t s);
 void launch_vext_sens(const double *lam, const double *gv, const double *vext, const signed char *zero, double *out,
                       cudaStream_t s);
+bool tc_build_tables(const std::vector<short> &off, const std::vector<double> &w, int L, int hy, TcTables &t,
+                     cudaStream_t s);
+void tc_free_tables(TcTables &t);
+bool tc_make_slab(TcSlab &sl, const DevGeom &g, std::string &why);
+void tc_free_slab(TcSlab &sl);
+void launch_sten_tc(const float *pad_channel, const DevGeom &g, const TcSlab &sl, const TcTables &t, double *out,
+                    bool accumulate, cudaStream_t s);
 void launch_adj_rb_channels(const double *w, double *chan, cudaStream_t s);
 void launch_a11inv_t(const double *u, double *y, cudaStream_t s);
 void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,

@@ -28,7 +28,7 @@ from . import build as _build
 from .problem import Problem
 
 TGPU_OK = 0
-FP64, FP32, BF16X3 = 0, 1, 2
+FP64, FP32, BF16X3, FP16TC = 0, 1, 2, 3
 FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED = 0, 1, 2, 3
 STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
           -5: "no convergence", -6: "non-finite values", -7: "domain error"}
