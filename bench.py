@@ -7,9 +7,10 @@ of U(-0.5,0.5) sigma heights, seeded) on the low-x side, bulk on the high-x side
 
 A step is one Newton solve from the initial state (rho_b exp(-V) with its own
 weighted densities) to ||R||_2 <= 1e-8: residual fills (FP32 stencil sums while
-||R||_2 > 0.1, FP64 after), Schur-complement GMRES with FP32 stencil sums in
-the products (inexact Newton, Eisenstat-Walker tolerances) and the damped
-update.  The value is Newton iterations per second over the K timed solves; the
+||R||_2 > 0.1, FP64 after), Schur-complement GMRES whose products sum the 3-D
+attraction stencil on the tensor cores (tcgen05, split FP16 x3, FP32
+accumulation) and the other stencils in FP32 (inexact Newton,
+Eisenstat-Walker tolerances), and the damped update.  The value is Newton iterations per second over the K timed solves; the
 plain FP64 path (FP64 residual and products) is timed per iteration beside it.  The inputs (12 unknowns x 128^3
 doubles = 201 MB, plus the 200+ MB of padded fields) exceed the 129 MB L2, so
 no explicit flush is done between steps.
@@ -34,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = ("Newton iterations/s of a mixed-precision solve to ||R||_2 <= 1e-8, 128^3 FMT1+WCA "
-          "(FP32 stencil sums in the Schur products, FP64 residual)")
+          "(tensor-core / FP32 stencil sums in the Schur products, FP64 residual)")
 UNIT = "Newton iter/s"
 WORKLOAD = "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall, periodic y,z"
 
@@ -54,6 +55,8 @@ def parse():
     ap.add_argument("--switch", type=float, default=0.1)
     ap.add_argument("--cpu-sample-planes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--products", default="fp16tc", choices=["fp16tc", "fp32"],
+                    help="arithmetic of the Schur products' attraction sums")
     return ap.parse_args()
 
 
@@ -102,6 +105,23 @@ class ClockSampler:
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_sten_tc launch at 128^3 (ncu, profiles/)
+TC_TRAFFIC_BYTES = 47.724e6 + 0.538e6
+
+
+def tc_issued_flops(p):
+    """MMA flops the tensor-core attraction sum issues per launch: per stencil line (oy, oz) and output
+    tile (64 x by 128 y of one z-plane), 3 MMAs of 128x64x16 per 16-input K-step of the line's band."""
+    from tramonto_gb300.problem import UATT
+    off = p.stencils[(UATT, 0)][0]
+    lines = {}
+    for ox, oy, oz in off:
+        lines[(oz, oy)] = max(lines.get((oz, oy), 0), abs(int(ox)))
+    ksteps = sum((32 + 63 + l) // 16 - (32 - l) // 16 + 1 for l in lines.values())
+    tiles = -(-p.nx[0] // 64) * -(-p.nx[1] // 128) * p.nx[2]
+    return float(tiles) * ksteps * 3 * 2 * 128 * 64 * 16
 
 
 def peaks():
@@ -207,6 +227,7 @@ def main():
     from tramonto_gb300.problem import DELTA, THETA, UATT
     t_setup = time.perf_counter()
     p, meta = setup.config2(n=args.n)
+    prod_prec = native.FP16TC if args.products == "fp16tc" else native.FP32
     s = native.Solver(p, device=local, precision=native.FP32)
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
@@ -217,7 +238,7 @@ def main():
     dx = torch.empty_like(x0_dev)
 
     def mixed_mode():
-        s.set_precision(native.FP32)
+        s.set_precision(prod_prec)
         s.set_fill_arithmetic(native.FILL_MIXED, switch_norm=args.switch)
 
     def solve():
@@ -278,13 +299,17 @@ def main():
     t_fill32 = timed(lambda: s.fill_device(x_mixed, R, 0))
     s.set_precision(native.FP32)
     t_apply32 = timed(lambda: s.schur_device(v2, y2), reps=5)
+    s.set_precision(native.FP16TC)
+    t_apply_tc = timed(lambda: s.schur_device(v2, y2), reps=5)
     s.set_precision(native.FP64)
     t_apply64 = timed(lambda: s.schur_device(v2, y2), reps=2)
-    # dominant kernel: the FP32 attraction (WCA) stencil sum of the Schur products
+    # dominant kernel of the Schur products: the attraction (WCA) stencil sum
+    t_wca_tc = s.time_stencil_sum(UATT, 0, native.FP16TC, reps=5)
     t_wca32 = s.time_stencil_sum(UATT, 0, native.FP32, reps=5)
     t_wca64 = s.time_stencil_sum(UATT, 0, native.FP64, reps=1)
     L_att = len(p.stencils[(UATT, 0)][1])
     flops_att = 2.0 * p.nnodes * L_att
+    mma_flops = tc_issued_flops(p)
     # plain FP64 Newton iterations (FP64 residual and FP64 Schur products) from the initial state
     s.set_fill_arithmetic(native.FILL_FP64)
     fp64_ms = None
@@ -309,7 +334,9 @@ def main():
                                           lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
     e2e_s = time.perf_counter() - t0
     hbm, bf16, peak_src = peaks()
-    ach_tf = flops_att / (t_wca32 * 1e-3) / 1e12
+    t_dom = t_wca_tc if args.products == "fp16tc" else t_wca32
+    ach_tf = flops_att / (t_dom * 1e-3) / 1e12
+    issued_tf = mma_flops / (t_wca_tc * 1e-3) / 1e12
     if rank == 0:
         cb = None
         if not args.no_cpu_baseline:
@@ -319,7 +346,10 @@ def main():
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_solve, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 residual near the solution, f32 stencil sums in the Schur products",
+            "vs_baseline": None,
+            "dtype": ("f64 residual near the solution; Schur products: split-f16 x3 tensor-core attraction sums, "
+                      "f32 other stencil sums" if args.products == "fp16tc" else
+                      "f64 residual near the solution, f32 stencil sums in the Schur products"),
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "step": "one Newton solve from the initial state to ||R||_2 <= "
                        f"{args.resid_tol:g}", "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
@@ -332,14 +362,23 @@ def main():
             "clocks": clk.summary(),
             "e2e": {"value": it_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,
                     "final_resid_norm2": rn_e2e},
-            "roofline": {"bound": "tensor", "kernel": "FP32 attraction (WCA) stencil sum, k_conv_slab",
+            "roofline": {"bound": "tensor",
+                         "kernel": ("attraction (WCA) stencil sum, k_sten_tc (tcgen05 split FP16 x3)"
+                                    if args.products == "fp16tc" else
+                                    "attraction (WCA) stencil sum, k_conv_slab (FP32 SIMT)"),
                          "achieved": ach_tf, "peak": bf16, "unit": "TFLOP/s", "frac": ach_tf / bf16,
-                         "peak_source": f"{peak_src} bf16 dense", "traffic": None,
-                         "algorithmic": f"2 x {L_att} stencil points x {p.nnodes} nodes per launch",
-                         "fp32_simt_nominal_tflops": 80.6, "frac_of_fp32_simt_nominal": ach_tf / 80.6,
-                         "ms_per_launch": t_wca32, "fp64_ms_per_launch": t_wca64},
+                         "peak_source": f"{peak_src} bf16 dense",
+                         "traffic": TC_TRAFFIC_BYTES if args.products == "fp16tc" and args.n == 128 else None,
+                         "traffic_source": "profiles/k_sten_tc_wca_128.md (ncu dram bytes, one launch)",
+                         "algorithmic": f"2 x {L_att} stencil points x {p.nnodes} nodes per launch (logical)",
+                         "ms_per_launch": t_dom, "issued_mma_tflops": issued_tf,
+                         "issued_mma_frac": issued_tf / bf16,
+                         "issued_mma": "3 MMAs (hi*hi, hi*lo, lo*hi) of 128x64x16 per K-step of each stencil line",
+                         "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
+                         "fp64_ms_per_launch": t_wca64},
             "cpu_baseline": cb,
             "breakdown_ms": {"fill_fp64": t_fill, "fill_fp32": t_fill32, "schur_apply_fp32": t_apply32,
+                             "schur_apply_fp16tc": t_apply_tc,
                              "schur_apply_fp64": t_apply64, "schur_applies_in_timed_steps": int(st["schur_applies"])},
             "plain_fp64": {"ms_per_newton_iter": fp64_ms,
                            "speedup_mixed_vs_fp64_per_iter": (fp64_ms / ms_per_iter) if fp64_ms else None},

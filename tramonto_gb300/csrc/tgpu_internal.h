@@ -82,11 +82,26 @@ __host__ __device__ inline double fmt_phi(const double *n, int ndim, int functio
 constexpr int kTcN = 64, kTcM = 128, kTcXHalo = 32, kTcCores = 24, kTcRing = 8;
 
 struct TcTables {                 // per stencil: lines grouped by z offset, Hankel tables
-  int4 *d_planes = nullptr;       // {oz, first line, lines, 0}
-  int4 *d_lines = nullptr;        // {oy, first K-step, last K-step, table}
+  int4 *d_planes = nullptr;       // {oz, first record, records, lines}
+  int4 *d_lines = nullptr;        // record headers (host reference copy)
   void *d_tables = nullptr;       // FP16 [table][high, low][24][8][8]
   int nplanes = 0, nlines = 0;
   double out_mult = 1.0;          // 1 / weight scale
+  int split_first[9][9] = {};     // [ns][k]: plane ranges when ns CTAs share an output tile
+  // CTAs per tile: the smallest ns (1..8) that fills the SMs' waves to 95%, else the best fill
+  int split_for(int tiles, int nsm) const
+  {
+    int best = 1;
+    double best_fill = 0.0;
+    for (int ns = 1; ns <= 8 && ns <= nplanes; ns++) {
+      const long ctas = (long)tiles * ns;
+      const long waves = (ctas + nsm - 1) / nsm;
+      const double fill = (double)ctas / (double)(waves * nsm);
+      if (fill >= 0.95) return ns;
+      if (fill > best_fill + 1e-9) { best_fill = fill; best = ns; }
+    }
+    return best;
+  }
 };
 
 struct TcSlab {                   // per problem: the FP16 copy of a padded channel and its TMA map
@@ -94,7 +109,7 @@ struct TcSlab {                   // per problem: the FP16 copy of a padded chan
   void *d_slab = nullptr;         // FP16 [high, low][Zp][G][Yp][8]
   float *d_scale = nullptr;       // [0] field scale, [1] max |field| (bits)
   int *d_err = nullptr;           // nonzero after a bounded wait ran out
-  int G = 0, Yp = 0, Zp = 0, R = 0, hy = 0, hz = 0, nring = 0;
+  int G = 0, Yp = 0, Zp = 0, R = 0, hy = 0, hz = 0, nring = 0, nsm = 1;
 };
 
 // One stencil table on the device: linear offsets in the padded box and the

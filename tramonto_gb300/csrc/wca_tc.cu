@@ -37,6 +37,8 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstring>
+#include <cstdint>
 #include <map>
 #include <vector>
 
@@ -57,9 +59,14 @@ T *upload_vec(const std::vector<T> &h, cudaStream_t s)
   return d;
 }
 constexpr int kTableHalfs = kTcCores * 64;              // one part (high or low) of a line's table
-constexpr uint32_t kTableBytes = 2 * kTableHalfs * 2;    // both parts
+// a record: int4 {oy_a, oy_b, first K-step | last K-step << 8, lines (1 or 2)}, then the high and the low
+// table; the lines oy_a and oy_b of one plane share it when their weights are equal (the stencil's mirror
+// symmetry in y)
+constexpr int kRecHalfs = 8 + 2 * kTableHalfs;
+constexpr uint32_t kTableBytes = 2 * kRecHalfs;
 constexpr long kSpin = 1L << 21;
-constexpr int kAccBufs = 4;   // TMEM accumulators (64 columns each)
+constexpr int kAccBufs = 4;   // chunk accumulator sets in TMEM
+constexpr int kRot = 1;       // accumulators per set (64 columns each), taken in turn by consecutive MMAs
 constexpr int kChunk = 4;     // lines per accumulation chunk
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
@@ -149,10 +156,11 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t *r)
 }
 
 struct TcArgs {
-  const int4 *planes;     // {oz, first line, lines, 0}
-  const int4 *lines;      // {oy, first K-step, last K-step, table}
-  const __half *tables;   // [table][part][24][8][8]
+  const int4 *planes;     // {oz, first record, records, lines}
+  const __half *tables;   // records: int4 header, high and low tables
   int nplanes, nring;
+  int nsplit;             // CTAs per output tile, each over a contiguous range of planes
+  int split_first[9];     // plane ranges [split_first[k], split_first[k + 1])
   int nx, ny, nz, hy, hz, R;
   const float *in_scale;  // device: the field's scale
   double out_mult;        // 1 / weight scale
@@ -174,8 +182,10 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 //
 // Warps 0-3 drain the accumulators (warp w owns TMEM lanes 32w..32w+31, i.e.
 // y rows), warp 4 lane 0 produces the copies, warp 5 lane 0 issues the MMAs.
-// The lines are taken in chunks of kChunk; chunk c accumulates in TMEM buffer
-// c % kAccBufs (64 columns each) from zero, and the drain warps add each
+// The lines are taken in chunks of kChunk; chunk c accumulates in TMEM set
+// c % kAccBufs from zero (kRot accumulators of 64 columns per set, used in
+// turn by consecutive MMAs; one is fastest: rotating over four measured 30%
+// slower, consecutive MMAs into the same accumulator being the cheap case), and the drain warps add each
 // finished chunk into FP32 register sums (ordinary round-to-nearest adds).  Short chunks keep the number of
 // accumulations into one FP32 accumulator small: the tensor core adds the
 // products of an MMA to the accumulator with a rounding that shrinks its
@@ -201,9 +211,12 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
   int *armed = reinterpret_cast<int *>(gb + (tslot + 8 - base));
   int *used = armed + 2 + kRing;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int x0 = blockIdx.x * kTcN, y0 = blockIdx.y * kTcM, z = blockIdx.z;
+  const int x0 = blockIdx.x * kTcN, y0 = blockIdx.y * kTcM;
+  const int z = blockIdx.z / P.nsplit, part = blockIdx.z % P.nsplit;
+  const int p_begin = P.split_first[part], p_end = P.split_first[part + 1];
+  const int np = p_end - p_begin;
   int nlines_total = 0;
-  for (int pi = 0; pi < P.nplanes; pi++) nlines_total += P.planes[pi].z;
+  for (int pi = p_begin; pi < p_end; pi++) nlines_total += P.planes[pi].w;
   const int nchunks = (nlines_total + kChunk - 1) / kChunk;
 
   if (threadIdx.x == 0) {
@@ -226,7 +239,7 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
   if (threadIdx.x < 2 + kRing) armed[threadIdx.x] = used[threadIdx.x] = 0;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tslot),
-                 "r"(kTcN * kAccBufs)
+                 "r"(kTcN * kAccBufs * kRot)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -239,21 +252,20 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
     if (lane == 0) {
       // producer: plane slabs (5-D TMA, both parts) and line tables (bulk copies)
       bool ok = true;
-      int bi = 0;
-      for (int pi = 0; pi < P.nplanes && ok; pi++) {
-        const int4 pl = P.planes[pi];
+      int ri = 0;   // running record index (ring slot)
+      for (int pi = 0; pi < np && ok; pi++) {
+        const int4 pl = P.planes[p_begin + pi];
         const int s = pi & 1;
         if (pi >= 2 && !mbar_wait(pempty + 8 * s, ((pi >> 1) - 1) & 1)) { ok = false; break; }
         mbar_expect_tx(pfull + 8 * s, plane_bytes);
         tma_load_5d(plane[s], &tmap, 0, y0, x0 / 8, z + pl.x + P.hz, 0, pfull + 8 * s);
         armed[s]++;
-        for (int li = 0; li < pl.z; li++, bi++) {
-          const int bs = bi % nring;
-          if (bi >= nring && !mbar_wait(bempty + 8 * bs, ((bi / nring) - 1) & 1)) { ok = false; break; }
+        for (int rj = 0; rj < pl.z; rj++, ri++) {
+          const int bs = ri % nring;
+          if (ri >= nring && !mbar_wait(bempty + 8 * bs, ((ri / nring) - 1) & 1)) { ok = false; break; }
           if (*abort_flag) { ok = false; break; }
-          const int4 ln = P.lines[pl.y + li];
           mbar_expect_tx(bfull + 8 * bs, kTableBytes);
-          bulk_load(ring + bs * kTableBytes, P.tables + (size_t)ln.w * 2 * kTableHalfs, kTableBytes, bfull + 8 * bs);
+          bulk_load(ring + bs * kTableBytes, P.tables + (size_t)(pl.y + rj) * kRecHalfs, kTableBytes, bfull + 8 * bs);
           armed[2 + bs]++;
         }
       }
@@ -269,40 +281,56 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
       const uint32_t idesc = (1u << 4) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
       const uint32_t lbo_a = 16u * (uint32_t)P.R;
       bool ok = true;
-      int bi = 0;   // running line index (ring slot, chunk)
-      for (int pi = 0; pi < P.nplanes && ok; pi++) {
-        const int4 pl = P.planes[pi];
+      int bi = 0;   // running line index (chunks)
+      int ri = 0;   // running record index (ring slot)
+      int rot = 0;                        // next accumulator of the current set
+      uint32_t fresh = (1u << kRot) - 1;  // accumulators not yet written in the current chunk
+      for (int pi = 0; pi < np && ok; pi++) {
+        const int4 pl = P.planes[p_begin + pi];
         const int s = pi & 1;
         if (!mbar_wait(pfull + 8 * s, (pi >> 1) & 1)) { ok = false; break; }
         used[s]++;
-        for (int li = 0; li < pl.z; li++, bi++) {
-          const int chunk = bi / kChunk, cb = chunk % kAccBufs;
-          const bool chunk_start = bi % kChunk == 0;
-          if (chunk_start && chunk >= kAccBufs && !mbar_wait(aempty + 8 * cb, ((chunk / kAccBufs) - 1) & 1)) {
-            ok = false;
-            break;
-          }
-          const int bs = bi % nring;
-          if (!mbar_wait(bfull + 8 * bs, (bi / nring) & 1)) { ok = false; break; }
+        for (int rj = 0; rj < pl.z && ok; rj++, ri++) {
+          const int bs = ri % nring;
+          if (!mbar_wait(bfull + 8 * bs, (ri / nring) & 1)) { ok = false; break; }
           if (*abort_flag) { ok = false; break; }
           used[2 + bs]++;
           tc_fence_after();
-          const int4 ln = P.lines[pl.y + li];
-          const uint32_t arow = plane[s] + 16u * (uint32_t)(ln.x + P.hy);
           const uint32_t btab = ring + bs * kTableBytes;
-          const uint32_t dt = tmem + (uint32_t)(cb * kTcN);
-          uint32_t acc = chunk_start ? 0u : 1u;
-          for (int k = ln.y; k <= ln.z; k++) {
-            const uint32_t ak = arow + 2u * (uint32_t)k * lbo_a, bk = btab + 256u * (uint32_t)k;
-            const uint64_t a_hi = sdesc(ak, lbo_a, 128), a_lo = sdesc(ak + part_bytes, lbo_a, 128);
-            const uint64_t b_hi = sdesc(bk, 128, 128), b_lo = sdesc(bk + kTableBytes / 2, 128, 128);
-            tc_mma(dt, a_lo, b_hi, idesc, acc);   // small terms first
-            tc_mma(dt, a_hi, b_lo, idesc, 1);
-            tc_mma(dt, a_hi, b_hi, idesc, 1);
-            acc = 1;
+          const int4 hd = *reinterpret_cast<const int4 *>(gb + (btab - base));   // the record's header
+          const int k_lo = hd.z & 0xff, k_hi = hd.z >> 8;
+          for (int j = 0; j < hd.w; j++, bi++) {
+            const int chunk = bi / kChunk, cb = chunk % kAccBufs;
+            const bool chunk_start = bi % kChunk == 0;
+            if (chunk_start && chunk >= kAccBufs && !mbar_wait(aempty + 8 * cb, ((chunk / kAccBufs) - 1) & 1)) {
+              ok = false;
+              break;
+            }
+            if (chunk_start) tc_fence_after();
+            if (chunk_start) {
+              rot = 0;
+              fresh = (1u << kRot) - 1;
+            }
+            const int oy = j == 0 ? hd.x : hd.y;
+            const uint32_t arow = plane[s] + 16u * (uint32_t)(oy + P.hy);
+            const uint32_t dset = tmem + (uint32_t)(cb * kRot * kTcN);
+            for (int k = k_lo; k <= k_hi; k++) {
+              const uint32_t ak = arow + 2u * (uint32_t)k * lbo_a, bk = btab + 16u + 256u * (uint32_t)k;
+              const uint64_t a_hi = sdesc(ak, lbo_a, 128), a_lo = sdesc(ak + part_bytes, lbo_a, 128);
+              const uint64_t b_hi = sdesc(bk, 128, 128), b_lo = sdesc(bk + 2u * kTableHalfs, 128, 128);
+              // the set's accumulators in turn (one per set: consecutive MMAs into the same accumulator)
+              const uint64_t ops[3][2] = {{a_lo, b_hi}, {a_hi, b_lo}, {a_hi, b_hi}};
+#pragma unroll
+              for (int q = 0; q < 3; q++) {
+                const uint32_t use = (fresh >> rot) & 1u ? 0u : 1u;
+                tc_mma(dset + (uint32_t)(rot * kTcN), ops[q][0], ops[q][1], idesc, use);
+                fresh &= ~(1u << rot);
+                rot = (rot + 1) % kRot;
+              }
+            }
+            if (bi % kChunk == kChunk - 1 || bi == nlines_total - 1) tc_commit(afull + 8 * cb);
           }
           tc_commit(bempty + 8 * bs);
-          if (bi % kChunk == kChunk - 1 || bi == nlines_total - 1) tc_commit(afull + 8 * cb);
         }
         if (!ok) break;
         tc_commit(pempty + 8 * s);
@@ -332,12 +360,14 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
       if (!got) { ok = false; break; }
       tc_fence_after();
       uint32_t r[16];
+      for (int q = 0; q < kRot; q++) {
 #pragma unroll
-      for (int h = 0; h < kTcN; h += 16) {
-        tc_ld16(tmem + lane_off + (uint32_t)(cb * kTcN + h), r);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int h = 0; h < kTcN; h += 16) {
+          tc_ld16(tmem + lane_off + (uint32_t)((cb * kRot + q) * kTcN + h), r);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int n = 0; n < 16; n++) sum[h + n] += __uint_as_float(r[n]);
+          for (int n = 0; n < 16; n++) sum[h + n] += __uint_as_float(r[n]);
+        }
       }
       tc_fence_before();
       mbar_arrive(aempty + 8 * cb);
@@ -351,7 +381,10 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
         for (int n = 0; n < kTcN; n++) {
           const int x = x0 + kTcN - 1 - n;
           const double v = (double)sum[n] * mult;
-          if (x < P.nx) row[x] = P.accumulate ? row[x] + v : v;
+          if (x < P.nx) {
+            if (P.nsplit > 1) atomicAdd(row + x, v);
+            else row[x] = P.accumulate ? row[x] + v : v;
+          }
         }
       }
     } else if (lane == 0) {
@@ -372,7 +405,7 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcN * kAccBufs)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcN * kAccBufs * kRot)
                  : "memory");
   }
 }
@@ -443,14 +476,30 @@ bool tc_build_tables(const std::vector<short> &off, const std::vector<double> &w
   const double sw = std::ldexp(1.0, -e);
   std::vector<int4> planes, lns;
   std::vector<__half> tab;
+  auto same_profile = [&](const std::map<int, double> &a, const std::map<int, double> &b) {
+    if (a.size() != b.size()) return false;
+    for (auto ia = a.begin(), ib = b.begin(); ia != a.end(); ++ia, ++ib)
+      if (ia->first != ib->first || std::fabs(ia->second - ib->second) > 1e-12 * wmax) return false;
+    return true;
+  };
   for (auto &pz : lines) {
-    const int first = (int)lns.size();
+    const int first = (int)(tab.size() / kRecHalfs);
+    int nl = 0;
     for (auto &py : pz.second) {
+      if (py.first < 0) {
+        auto mirror = pz.second.find(-py.first);
+        if (mirror != pz.second.end() && same_profile(py.second, mirror->second)) continue;   // shares +oy's record
+      }
+      int oy_b = INT32_MIN, nrec = 1;
+      if (py.first > 0) {
+        auto mirror = pz.second.find(-py.first);
+        if (mirror != pz.second.end() && same_profile(py.second, mirror->second)) { oy_b = -py.first; nrec = 2; }
+      }
       int l = 0;
       for (auto &px : py.second) l = std::max(l, std::abs(px.first));
-      const int table = (int)(tab.size() / (2 * kTableHalfs));
-      tab.resize(tab.size() + 2 * kTableHalfs, __float2half_rn(0.0f));
-      __half *T = tab.data() + (size_t)table * 2 * kTableHalfs;
+      const int table = (int)(tab.size() / kRecHalfs);
+      tab.resize(tab.size() + kRecHalfs, __float2half_rn(0.0f));
+      __half *T = tab.data() + (size_t)table * kRecHalfs + 8;
       // core matrix d, row b (n' in group), column a (k in group): w(8d + a + b - (32 + 63)); high then low part
       for (int d = 0; d < kTcCores; d++)
         for (int b = 0; b < 8; b++)
@@ -464,12 +513,26 @@ bool tc_build_tables(const std::vector<short> &off, const std::vector<double> &w
             T[kTableHalfs + d * 64 + b * 8 + a] = __float2half_rn((float)(v - (double)__half2float(hi)));
           }
       const int k_lo = (kTcXHalo - l) / 16, k_hi = (kTcXHalo + kTcN - 1 + l) / 16;
-      lns.push_back(make_int4(py.first, k_lo, k_hi, table));
+      const int4 head = make_int4(py.first, oy_b, k_lo | (k_hi << 8), nrec);
+      std::memcpy(tab.data() + (size_t)table * kRecHalfs, &head, sizeof(head));
+      lns.push_back(head);
+      nl += nrec;
     }
-    planes.push_back(make_int4(pz.first, first, (int)lns.size() - first, 0));
+    planes.push_back(make_int4(pz.first, first, (int)(tab.size() / kRecHalfs) - first, nl));
   }
   t.nplanes = (int)planes.size();
-  t.nlines = (int)lns.size();
+  t.nlines = 0;
+  for (auto &pl : planes) t.nlines += pl.w;
+  // plane ranges for 1..8 CTAs per tile, balanced by line count
+  for (int ns = 1; ns <= 8; ns++) {
+    t.split_first[ns][0] = 0;
+    int k = 1, acc = 0;
+    for (int pi = 0; pi < t.nplanes && k < ns; pi++) {
+      acc += planes[pi].w;
+      if ((long)acc * ns >= (long)k * t.nlines) t.split_first[ns][k++] = pi + 1;
+    }
+    while (k <= ns) t.split_first[ns][k++] = t.nplanes;
+  }
   t.out_mult = 1.0 / sw;
   t.d_planes = upload_vec(planes, s);
   t.d_lines = upload_vec(lns, s);
@@ -496,6 +559,7 @@ bool tc_make_slab(TcSlab &sl, const DevGeom &g, std::string &why)
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&sl.nsm, cudaDevAttrMultiProcessorCount, dev);
   sl.nring = 0;
   for (int r = kTcRing; r >= 2; r--)
     if (tc_smem_bytes(sl.R, r) <= (size_t)optin) { sl.nring = r; break; }
@@ -559,7 +623,6 @@ void launch_sten_tc(const float *pad_channel, const DevGeom &g, const TcSlab &sl
                                 static_cast<__half *>(sl.d_slab));
   TcArgs a;
   a.planes = t.d_planes;
-  a.lines = t.d_lines;
   a.tables = static_cast<const __half *>(t.d_tables);
   a.nplanes = t.nplanes;
   a.nring = sl.nring;
@@ -574,7 +637,11 @@ void launch_sten_tc(const float *pad_channel, const DevGeom &g, const TcSlab &sl
   a.out = out;
   a.accumulate = accumulate ? 1 : 0;
   a.err = sl.d_err;
-  const dim3 grid((g.nx[0] + kTcN - 1) / kTcN, (g.nx[1] + kTcM - 1) / kTcM, g.nx[2]);
+  const int tiles = ((g.nx[0] + kTcN - 1) / kTcN) * ((g.nx[1] + kTcM - 1) / kTcM) * g.nx[2];
+  const int ns = accumulate ? t.split_for(tiles, sl.nsm) : 1;
+  a.nsplit = ns;
+  for (int k = 0; k <= ns; k++) a.split_first[k] = t.split_first[ns][k];
+  const dim3 grid((g.nx[0] + kTcN - 1) / kTcN, (g.nx[1] + kTcM - 1) / kTcM, g.nx[2] * ns);
   k_sten_tc<<<grid, 192, tc_smem_bytes(sl.R, sl.nring), s>>>(sl.tmap, a);
 }
 
