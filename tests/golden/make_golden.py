@@ -59,6 +59,9 @@ def cases():
     c = {}
     # 1-D FMT1 hard sphere against a hard wall (the reference's HS5 example as is)
     c["hs1d_wall"] = deck("HS5_FMT1_1D")
+    # configuration 1: HS5 at L = 20 sigma, dx = 0.01 sigma (2000 elements), rho_b = 0.7, Newton to 1e-10
+    c["hs1d_c1"] = deck("HS5_FMT1_1D", {"Size_x(idim)": "20.0", "Esize_x(idim)": "0.01",
+                                        "Rho_b_0[icomp]": "0.7", "NL_rel_tol NL_abs_tol": "1.0e-6 1.0e-10 0.1"})
     # 1-D FMT1, hard wall on the left, reflecting boundary on the right (HS3 as is)
     c["hs1d_reflect"] = deck("HS3_FMT1_1D")
     # 1-D FMT1 + WCA attraction near a LJ 9-3 wall, mean field as its own unknown
