@@ -18,7 +18,7 @@ def declared_symbols():
         with open(h) as f:
             txt = f.read()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-        for m in re.finditer(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(tgpu_\w+)\s*\(", txt, flags=re.M):
+        for m in re.finditer(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b((?:tgpu|dft)_\w+)\s*\(", txt, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
@@ -32,6 +32,7 @@ def lib():
 def test_header_declares_entry_points():
     names = declared_symbols()
     assert "tgpu_fill" in names and "tgpu_schur_apply" in names and len(names) > 20
+    assert "dft_linprobmgr_insertonematrixvalue" in names and "dft_hardsphere_lin_prob_mgr_create" in names
 
 
 def test_library_exports_every_declared_symbol(lib):
