@@ -37,7 +37,19 @@ sys.path.insert(0, ROOT)
 METRIC = ("Newton iterations/s of a mixed-precision solve to ||R||_2 <= 1e-8, 128^3 FMT1+WCA "
           "(tensor-core / FP32 stencil sums in the Schur products, FP64 residual)")
 UNIT = "Newton iter/s"
-WORKLOAD = "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall, periodic y,z"
+WORKLOADS = {
+    "config2": "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall, periodic y,z",
+    "config4": "config4: 3-D FMT1+WCA, 256^3, dx=0.08, rho_b=0.75, rough 12-3 LJ wall, periodic y,z",
+    "config5": ("config5: 64 slit pores, FMT1+WCA, 32 1-D (dx=0.01, widths U(3,40)) and 32 2-D (n^2, "
+                "n in [100,400], dx=0.05, patterned walls), rho_b U(0.05,0.8) each; seed 2024"),
+}
+
+
+def make_problem(args):
+    from tramonto_gb300 import setup
+    if args.workload == "config4":
+        return setup.config4()
+    return setup.config2(n=args.n)
 
 
 def parse():
@@ -46,7 +58,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--n", type=int, default=128, help="grid of the config2 workload")
+    ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--lin-tol", type=float, default=1e-6)
     ap.add_argument("--lin-maxit", type=int, default=200)
@@ -55,6 +68,8 @@ def parse():
     ap.add_argument("--switch", type=float, default=0.1)
     ap.add_argument("--cpu-sample-planes", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--light", action="store_true",
+                    help="one repetition of each FP64 kernel-family timing (large workloads)")
     ap.add_argument("--products", default="fp16tc", choices=["fp16tc", "fp32"],
                     help="arithmetic of the Schur products' attraction sums")
     return ap.parse_args()
@@ -185,7 +200,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    p, meta = setup.config2(n=args.n)
+    p, meta = make_problem(args)
     # initial state on the host: densities rho_b exp(-V), weighted densities from the oracle's sums
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import orc
@@ -204,16 +219,49 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "inputs_exceed_l2": True},
+           "config": {"workload": WORKLOADS[args.workload], "inputs_exceed_l2": True},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
+
+
+def run_config5(args):
+    """Configuration 5: every slit-pore problem solved at its state point from its initial state, with
+    dN/d(beta mu) by the adjoint, in mixed precision and in plain FP64; wall time of the whole sweep
+    (set-up, solve and derivative of each problem) and Newton iterations per second."""
+    import torch
+    from tramonto_gb300 import isotherm, setup
+    torch.cuda.set_device(0)
+    specs = setup.config5()
+    isotherm.sweep(specs[:1] + specs[32:33], mixed=True)        # warm-up (library load, first contexts)
+    out = {}
+    for name, mixed in (("mixed", True), ("fp64", False)):
+        t0 = time.perf_counter()
+        recs = isotherm.sweep(specs, mixed=mixed)
+        wall = time.perf_counter() - t0
+        iters = sum(r["iters"] for r in recs)
+        out[name] = {"wall_s": wall, "newton_iters": iters, "converged": sum(r["converged"] for r in recs),
+                     "iters_per_s": iters / wall, "wall_s_1d": sum(r["wall_s"] for r in recs if r["ndim"] == 1),
+                     "wall_s_2d": sum(r["wall_s"] for r in recs if r["ndim"] == 2)}
+        if mixed:
+            out["dN_dbetamu_sample"] = [(r["ndim"], r["nodes"], round(r["rho_b"], 4), r.get("dN_dbetamu"))
+                                        for r in recs[::8]]
+    line = {"metric": "Newton iterations/s over the configuration-5 slit-pore sweep (mixed precision)",
+            "value": out["mixed"]["iters_per_s"], "unit": "Newton iter/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": out["mixed"]["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 residual near the solution, f32 stencil sums in the Schur products",
+            "data": "synthetic", "config": {"workload": WORKLOADS["config5"], "step": "the whole sweep"},
+            "sweep": out, "speedup_mixed_vs_fp64_wall": out["fp64"]["wall_s"] / out["mixed"]["wall_s"]}
+    print(json.dumps(line))
 
 
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "config5":
+        run_config5(args)
         return
     import torch
     import torch.distributed as dist
@@ -225,8 +273,8 @@ def main():
     torch.cuda.set_device(local)
     from tramonto_gb300 import native, setup
     from tramonto_gb300.problem import DELTA, THETA, UATT
-    t_setup = time.perf_counter()
-    p, meta = setup.config2(n=args.n)
+    t_setup = t_start = time.perf_counter()
+    p, meta = make_problem(args)
     prod_prec = native.FP16TC if args.products == "fp16tc" else native.FP32
     s = native.Solver(p, device=local, precision=native.FP32)
     stream = torch.cuda.current_stream()
@@ -246,9 +294,16 @@ def main():
         return s.newton_solve_device(dx, resid_tol=args.resid_tol, max_iter=args.max_newton, lin_tol=args.lin_tol,
                                      lin_max_iter=args.lin_maxit, allow_noconv=True)
 
+    def progress(msg):
+        if rank == 0:
+            print(f"[bench {time.perf_counter() - t_start:8.1f} s] {msg}", file=sys.stderr, flush=True)
+
+    progress(f"set-up done ({p.nnodes} nodes, {p.nunk} unknowns per node)")
     mixed_mode()
-    for _ in range(args.warmup):
-        solve()
+    for w in range(args.warmup):
+        it_w, rn_w, li_w = solve()
+        torch.cuda.synchronize()
+        progress(f"warm-up solve {w}: {it_w} Newton iterations, {li_w} GMRES, ||R||_2 = {rn_w:.2e}")
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -264,6 +319,7 @@ def main():
             iters += it
             lin_iters += li
             final_r.append(rn)
+            progress(f"timed solve: {it} Newton iterations, {li} GMRES, ||R||_2 = {rn:.2e}")
         e1.record(stream)
         torch.cuda.synchronize()
     st = s.stats()
@@ -294,7 +350,8 @@ def main():
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
 
-    t_fill = timed(lambda: s.fill_device(x_mixed, R, 0))
+    rep64 = 1 if args.light else 3
+    t_fill = timed(lambda: s.fill_device(x_mixed, R, 0), reps=rep64)
     s.set_fill_arithmetic(native.FILL_FP32)
     t_fill32 = timed(lambda: s.fill_device(x_mixed, R, 0))
     s.set_precision(native.FP32)
@@ -302,7 +359,8 @@ def main():
     s.set_precision(native.FP16TC)
     t_apply_tc = timed(lambda: s.schur_device(v2, y2), reps=5)
     s.set_precision(native.FP64)
-    t_apply64 = timed(lambda: s.schur_device(v2, y2), reps=2)
+    t_apply64 = timed(lambda: s.schur_device(v2, y2), reps=1 if args.light else 2)
+    progress("kernel-family timings done")
     # dominant kernel of the Schur products: the attraction (WCA) stencil sum
     t_wca_tc = s.time_stencil_sum(UATT, 0, native.FP16TC, reps=5)
     t_wca32 = s.time_stencil_sum(UATT, 0, native.FP32, reps=5)
@@ -351,9 +409,9 @@ def main():
                       "f32 other stencil sums" if args.products == "fp16tc" else
                       "f64 residual near the solution, f32 stencil sums in the Schur products"),
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "step": "one Newton solve from the initial state to ||R||_2 <= "
+            "config": {"workload": WORKLOADS[args.workload], "step": "one Newton solve from the initial state to ||R||_2 <= "
                        f"{args.resid_tol:g}", "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
-                       "rho_b": 0.6, "kT": 1.2, "rcut": 2.5, "lin_tol_floor": args.lin_tol,
+                       "rho_b": meta["rho_b"], "kT": 1.2, "rcut": 2.5, "lin_tol_floor": args.lin_tol,
                        "fp32_until_resid": args.switch, "inputs_exceed_l2": True,
                        "l2_flush": "none (working set > L2)"},
             "newton_iters_per_step": iters / args.steps, "ms_per_newton_iter": ms_per_iter,
@@ -368,7 +426,8 @@ def main():
                                     "attraction (WCA) stencil sum, k_conv_slab (FP32 SIMT)"),
                          "achieved": ach_tf, "peak": bf16, "unit": "TFLOP/s", "frac": ach_tf / bf16,
                          "peak_source": f"{peak_src} bf16 dense",
-                         "traffic": TC_TRAFFIC_BYTES if args.products == "fp16tc" and args.n == 128 else None,
+                         "traffic": (TC_TRAFFIC_BYTES if args.products == "fp16tc" and args.workload == "config2"
+                                     and args.n == 128 else None),
                          "traffic_source": "profiles/k_sten_tc_wca_128.md (ncu dram bytes, one launch)",
                          "algorithmic": f"2 x {L_att} stencil points x {p.nnodes} nodes per launch (logical)",
                          "ms_per_launch": t_dom, "issued_mma_tflops": issued_tf,

@@ -103,6 +103,13 @@ int tgpu_set_zero_density(tgpu_handle h, const signed char *flags);   /* [ncomp]
  * as local corner l (for that reflection pattern) is fluid (src/dft_utils.c:41-62). */
 int tgpu_set_hard_wall(tgpu_handle h, const int *boundary_nodes, const short *fluid_masks);
 int tgpu_finalize(tgpu_handle h);
+/* Move the bulk state (chemical potential) of a finalized problem: bulk densities, excess chemical
+ * potentials (hard-sphere and attraction) per component and the bulk dPhi/dn0..dn3.  The Euler-Lagrange
+ * rows then hold betamu = ln rho_b + betamu_hs_ex + betamu_att: the parameter the reference's continuation
+ * in the chemical potential sets (assign_parameter_tramonto, CONT_BETAMU_I, src/dft_switch_continuation.c:
+ * 123,170-180).  Stencils and V_ext stay; the next call must be a fill (the Jacobian state is dropped). */
+int tgpu_set_bulk_state(tgpu_handle h, const double *rho_b, const double *betamu_hs_ex, const double *betamu_att,
+                        const double *dphi_bulk);
 /* Arithmetic of the Jacobian / Schur products: TGPU_FP64, TGPU_FP32 (stencil sums in FP32), or
  * TGPU_FP16TC (as TGPU_FP32, but the 3-D attraction sums on the tensor cores: FP16 inputs scaled by
  * powers of two, FP32 accumulation; TGPU_ERR_UNSUPPORTED when the problem has none).  The residual

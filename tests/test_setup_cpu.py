@@ -65,3 +65,20 @@ def test_lj93_wall_matches_reference_field():
     fd_s = (setup.lj93_wall_1d(d, 3.0, 1.0 + h, 3.0, 1e300)[0] - setup.lj93_wall_1d(d, 3.0, 1.0 - h, 3.0, 1e300)[0]) / (2 * h)
     assert np.abs(de[live] - fd_e[live]).max() <= 1e-6 * np.abs(de[live]).max()
     assert np.abs(ds[live] - fd_s[live]).max() <= 1e-6 * np.abs(ds[live]).max()
+
+
+def test_config5_problems_are_seeded_and_in_range():
+    a, b = setup.config5(), setup.config5()
+    assert a == b and len(a) == 64
+    for s in a[:32]:
+        assert s["ndim"] == 1 and 300 <= s["nx"][0] <= 4001 and 3.0 <= s["width"] <= 40.0
+    for s in a[32:]:
+        assert s["ndim"] == 2 and 100 <= s["nx"][0] <= 400 and s["nx"][0] == s["nx"][1]
+    assert all(0.05 <= s["rho_b"] <= 0.8 for s in a)
+
+
+def test_slit_pore_field_is_mirror_symmetric():
+    v = setup.slit_pore_vext(1, (501, 1, 1), (0.01,))[0]
+    assert np.allclose(v, v[::-1], rtol=1e-10, atol=1e-12) and v[0] == 10.0 and v.min() < -1.0
+    v2 = setup.slit_pore_vext(2, (120, 80, 1), (0.05, 0.05)).reshape(80, 120)
+    assert np.allclose(v2, v2[:, ::-1]) and not np.allclose(v2[0], v2[40])

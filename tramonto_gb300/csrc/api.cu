@@ -169,6 +169,28 @@ void need_final(Ctx *c)
   if (!c->finalized) throw Error(TGPU_ERR_STATE, "tgpu_finalize has not been called");
 }
 
+// Values the padded boxes take at bulk sentinels: the bulk densities (density channels) and the
+// bulk dPhi/dn combinations of the Euler-Lagrange channels (Dphi_Drhobar_b, src/dft_fill_FMT.c:104-127).
+std::vector<double> bulk_values_rho(const tgpu_geometry &g)
+{
+  std::vector<double> v;
+  for (int jc = 0; jc < g.ncomp; jc++) v.push_back(g.rho_b[jc]);
+  return v;
+}
+
+std::vector<double> bulk_values_tr(const tgpu_geometry &g)
+{
+  std::vector<double> v;
+  for (int ic = 0; ic < g.ncomp; ic++) {
+    const double f = g.fac_overlap[ic];
+    const double *b = g.dphi_bulk;
+    v.push_back(f * (b[0] * g.inv_4pirsq[ic] + b[1] * g.inv_4pir[ic] + b[2]));
+    for (int d = 0; d < g.ndim; d++) v.push_back(0.0);
+    v.push_back(f * b[3]);
+  }
+  return v;
+}
+
 PadParams make_pad(const std::vector<double> &bulk, const std::vector<int> &sign, const std::vector<int> &zc,
                    cudaStream_t s)
 {
@@ -1147,10 +1169,9 @@ void build_device_tables(Ctx *c)
   }
   // padding parameter sets
   {
-    std::vector<double> b_res, b_jac;
+    std::vector<double> b_res = bulk_values_rho(g), b_jac;
     std::vector<int> sg, zc;
     for (int jc = 0; jc < g.ncomp; jc++) {
-      b_res.push_back(g.rho_b[jc]);
       b_jac.push_back(0.0);
       sg.push_back(0);
       zc.push_back(jc);
@@ -1159,22 +1180,17 @@ void build_device_tables(Ctx *c)
     c->pads.rho_jac = make_pad(b_jac, sg, zc, c->stream);
   }
   {
-    std::vector<double> b_res, b_jac;
+    std::vector<double> b_res = bulk_values_tr(g), b_jac;
     std::vector<int> sg, zc;
     for (int ic = 0; ic < g.ncomp; ic++) {
-      const double f = g.fac_overlap[ic];
-      const double *b = g.dphi_bulk;
-      b_res.push_back(f * (b[0] * g.inv_4pirsq[ic] + b[1] * g.inv_4pir[ic] + b[2]));
       b_jac.push_back(0.0);
       sg.push_back(0);
       zc.push_back(-1);
       for (int d = 0; d < nd; d++) {
-        b_res.push_back(0.0);
         b_jac.push_back(0.0);
         sg.push_back(1 << d);
         zc.push_back(-1);
       }
-      b_res.push_back(f * b[3]);
       b_jac.push_back(0.0);
       sg.push_back(0);
       zc.push_back(-1);
@@ -1347,6 +1363,36 @@ int tgpu_set_vext(tgpu_handle h, const double *vext)
       if (std::isnan(vext[i])) throw Error(TGPU_ERR_NONFINITE, "NaN in the external field");
     c->h_vext.assign(vext, vext + n);
     if (c->finalized) ck(cudaMemcpyAsync(c->d_vext, vext, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_bulk_state(tgpu_handle h, const double *rho_b, const double *betamu_hs_ex, const double *betamu_att,
+                        const double *dphi_bulk)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    if (!rho_b || !betamu_hs_ex || !betamu_att || !dphi_bulk) throw Error(TGPU_ERR_ARG, "null argument");
+    tgpu_geometry &g = c->g;
+    tgpu::DevGeom &dg = c->dg;
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      if (!(rho_b[ic] > 0.0)) throw Error(TGPU_ERR_ARG, "bulk densities must be positive");
+      g.rho_b[ic] = dg.rho_b[ic] = rho_b[ic];
+      g.betamu_hs_ex[ic] = dg.betamu_hs_ex[ic] = betamu_hs_ex[ic];
+      g.betamu_att[ic] = dg.betamu_att[ic] = betamu_att[ic];
+    }
+    for (int k = 0; k < 4; k++) g.dphi_bulk[k] = dg.dphi_bulk[k] = dphi_bulk[k];
+    const std::vector<double> br = bulk_values_rho(g), bt = bulk_values_tr(g);
+    ck(cudaMemcpyAsync(c->pads.rho_res.bulk, br.data(), br.size() * sizeof(double), cudaMemcpyHostToDevice,
+                       c->stream), "h2d");
+    ck(cudaMemcpyAsync(c->pads.tr_res.bulk, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+       "h2d");
+    tgpu::upload_geom(dg, c->stream);
+    g_geom_owner = c;
+    c->have_state = false;
+    c->have_ref = false;
     ck(cudaStreamSynchronize(c->stream), "sync");
     return TGPU_OK;
   });

@@ -101,6 +101,7 @@ def load(build_if_missing: bool = False):
         "tgpu_time_stencil_sum": [vp, C.c_int, C.c_int, C.c_int, C.c_int, dp],
         "tgpu_get_stats": [vp, C.POINTER(Stats)], "tgpu_reset_stats": [vp],
         "tgpu_set_integration": [vp, vp, vp, vp, vp],
+        "tgpu_set_bulk_state": [vp, vp, vp, vp, vp],
         "tgpu_objectives": [vp, vp, dp, dp], "tgpu_objectives_device": [vp, vp, dp, dp],
         "tgpu_objective_grad_device": [vp, vp, C.c_int, C.c_int, vp, vp],
         "tgpu_grad_vext_device": [vp, vp, C.c_int, C.c_int, C.c_double, C.c_int, vp, ip],
@@ -197,6 +198,24 @@ class Solver:
         """Replace V_ext/kT ([ncomp][N]); nodes equal to vext_max stay zero-density rows."""
         v = self._host(vext, (self.p.ncomp, self.N))
         _check(self.lib.tgpu_set_vext(self.h, _ptr(v)), self.lib)
+
+    def set_bulk(self, rho_b):
+        """Move the bulk state (chemical potential) to the bulk densities rho_b: the bulk constants are
+        recomputed as at set-up (tgpu_set_bulk_state) and the objectives' constants follow."""
+        from . import setup
+        from .problem import UATT
+        p = self.p
+        rho_b = np.asarray(rho_b, np.float64).reshape(p.ncomp)
+        uat = {k[1]: v for k, v in p.stencils.items() if k[0] == UATT} if p.attraction else None
+        b = setup.bulk_constants(p.functional, p.hs_diam, rho_b, bool(p.attraction), uat, p.ncomp)
+        hs, att = np.ascontiguousarray(b["betamu_hs_ex"], np.float64), np.ascontiguousarray(b["betamu_att"], np.float64)
+        dphi = np.ascontiguousarray(b["dphi_bulk"], np.float64)
+        _check(self.lib.tgpu_set_bulk_state(self.h, _ptr(rho_b), _ptr(hs), _ptr(att), _ptr(dphi)), self.lib)
+        p.rho_b, p.betamu_hs_ex, p.betamu_att, p.dphi_bulk = rho_b.copy(), hs, att, dphi
+        if p.w_fluid is not None:
+            p.rhobar_b = b["rhobar_b"]
+            p.betamu = np.log(rho_b) + hs + att
+            self.set_integration(p.w_fluid, p.w_bulk, p.rhobar_b, p.betamu)
 
     def set_integration(self, w_fluid, w_bulk, rhobar_b, betamu):
         """Integration weights ([ncomp][N] each), bulk n3 n2 n1 n0 and betamu of the objectives."""

@@ -219,7 +219,7 @@ def lj93_wall_1d(dist, eps_w, sigma_w, cut_w, vext_max=10.0):
     return v, dv_de, dv_ds
 
 
-def config2(n=128, esize=0.1, seed=1234):
+def config2(n=128, esize=0.1, seed=1234, rho_b=0.6):
     """3-D FMT1 + WCA (eps=1, r_c=2.5, kT*=1.2) fluid at rho_b=0.6 next to a rough 12-3 LJ wall.
 
     Periodic in y and z; the wall side of x is IN_WALL, the far side IN_BULK."""
@@ -228,10 +228,16 @@ def config2(n=128, esize=0.1, seed=1234):
     kT = 1.2
     vext, meta = rough_wall_vext(nx, es, kT=kT, seed=seed)
     p = build_problem(3, nx, es, ((BC_IN_WALL, BC_IN_BULK), (BC_PERIODIC, BC_PERIODIC), (BC_PERIODIC, BC_PERIODIC)),
-                      hs_diam=[1.0], rho_b=[0.6], functional=FMT1, attraction=True, sigma=[[1.0]], eps=[[1.0 / kT]],
-                      rcut=[[2.5]], vext=vext)
-    meta.update(grid=list(nx), dx=esize, rho_b=0.6, kT=kT, rcut=2.5, functional="FMT1", attraction="WCA LJ12-6")
+                      hs_diam=[1.0], rho_b=[rho_b], functional=FMT1, attraction=True, sigma=[[1.0]],
+                      eps=[[1.0 / kT]], rcut=[[2.5]], vext=vext)
+    meta.update(grid=list(nx), dx=esize, rho_b=rho_b, kT=kT, rcut=2.5, functional="FMT1", attraction="WCA LJ12-6")
     return p, meta
+
+
+def config4(n=256, esize=0.08, seed=1234):
+    """The configuration-2 fluid and wall at scale: 256^3 nodes, dx = 0.08 (attraction reach 31 nodes,
+    1.4e5 stencil points), rho_b = 0.75 (bulk n3 = 0.39)."""
+    return config2(n=n, esize=esize, seed=seed, rho_b=0.75)
 
 
 def gaussian_random_field(nx, esize, corr_len=1.0, seed=4321):
@@ -283,6 +289,58 @@ def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0, eps_w=0.5):
                    functional="FMT3", field="0.5 kT Gaussian random field, correlation length 1",
                    shell="eps_w * 9-3 cut-and-shifted, sigma_wf=(sigma_i+1)/2, cut 2.5 sigma_wf",
                    grf=field, dv_deps=dv_deps)
+
+
+def slit_pore_vext(ndim, nx, esize, eps_w=1.0, sigma_w=1.0, cut_w=3.0, pattern=0.5, vext_max=10.0):
+    """V_ext/kT of a slit pore: two planar cut-and-shifted 9-3 walls (the form of Vext_LJ9_3_CS,
+    src/dft_vext_1D.c:42-56) with surfaces at the two x ends of the box; in 2-D the wall strength varies
+    along the periodic y direction as eps_w (1 + pattern cos(2 pi y / L_y)) (a chemically patterned slit).
+    Nodes with V >= vext_max or on a surface hold vext_max.  Returns [1][N] (node = ix + nx*iy)."""
+    L = (nx[0] - 1) * esize[0]
+    x = np.arange(nx[0]) * esize[0]
+    s1 = lj93_wall_1d(x, 1.0, sigma_w, cut_w, vext_max=np.inf)[0]
+    s2 = lj93_wall_1d(L - x, 1.0, sigma_w, cut_w, vext_max=np.inf)[0]
+    shape = s1 + s2
+    surface = (x <= 0) | (x >= L)
+    if ndim == 1:
+        eps = np.array([eps_w])
+    else:
+        y = np.arange(nx[1]) * esize[1]
+        eps = eps_w * (1.0 + pattern * np.cos(2 * PI * y / (nx[1] * esize[1])))
+    v = eps[:, None] * shape[None, :]
+    v = np.where(surface[None, :] | (v >= vext_max), vext_max, v)
+    return v.reshape(1, -1)
+
+
+def slit_pore(spec, rho_b=None):
+    """One configuration-5 problem: FMT1 + WCA (eps = 1, r_c = 2.5, kT* = 1.2) in a slit pore
+    (spec from config5); walls beyond both x ends, periodic y in 2-D."""
+    ndim, nx, dx = spec["ndim"], tuple(spec["nx"]), spec["dx"]
+    es = (dx,) * ndim
+    kT = 1.2
+    bc = [(BC_IN_WALL, BC_IN_WALL)] + [(BC_PERIODIC, BC_PERIODIC)] * (ndim - 1)
+    vext = slit_pore_vext(ndim, nx, es)
+    return build_problem(ndim, nx, es, tuple(bc), hs_diam=[1.0], rho_b=[spec["rho_b"] if rho_b is None else rho_b],
+                         functional=FMT1, attraction=True, sigma=[[1.0]], eps=[[1.0 / kT]], rcut=[[2.5]], vext=vext)
+
+
+def config5(seed=2024, n_problems=64):
+    """Configuration 5: 64 independent slit-pore problems (numpy PCG64 `seed`): the first half 1-D with
+    widths U(3, 40) sigma at dx = 0.01 (300-4000 nodes), the second half 2-D cross-sections of n x n nodes,
+    n uniform in [100, 400], at dx = 0.05; each with its own bulk density U(0.05, 0.8)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(n_problems):
+        if k < n_problems // 2:
+            width = rng.uniform(3.0, 40.0)
+            n = int(round(width / 0.01)) + 1
+            spec = dict(ndim=1, nx=(n, 1, 1), dx=0.01, width=(n - 1) * 0.01)
+        else:
+            n = int(rng.integers(100, 401))
+            spec = dict(ndim=2, nx=(n, n, 1), dx=0.05, width=(n - 1) * 0.05)
+        spec["rho_b"] = float(rng.uniform(0.05, 0.8))
+        specs.append(spec)
+    return specs
 
 
 def initial_state(solver, p: Problem, max_enhancement=None):
