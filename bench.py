@@ -72,6 +72,8 @@ def parse():
                     help="one repetition of each FP64 kernel-family timing (large workloads)")
     ap.add_argument("--products", default="fp16tc", choices=["fp16tc", "fp32"],
                     help="arithmetic of the Schur products' attraction sums")
+    ap.add_argument("--accurate-fill", default="ff", choices=["ff", "fp64"],
+                    help="arithmetic of the fills once ||R||_2 < switch: float-float or FP64 single-channel sums")
     return ap.parse_args()
 
 
@@ -279,15 +281,17 @@ def main():
     s = native.Solver(p, device=local, precision=native.FP32)
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
-    x0 = setup.initial_state(s, p)
+    x0 = setup.initial_state(s, p, max_enhancement=meta.get("initial_cap"))
     t_setup = time.perf_counter() - t_setup
     n = p.nunk * p.nnodes
     x0_dev = torch.from_numpy(x0).to("cuda").contiguous()
     dx = torch.empty_like(x0_dev)
 
+    fill_mode = native.FILL_MIXED_FF if args.accurate_fill == "ff" else native.FILL_MIXED
+
     def mixed_mode():
         s.set_precision(prod_prec)
-        s.set_fill_arithmetic(native.FILL_MIXED, switch_norm=args.switch)
+        s.set_fill_arithmetic(fill_mode, switch_norm=args.switch)
 
     def solve():
         dx.copy_(x0_dev)
@@ -332,6 +336,13 @@ def main():
     ms_per_iter = ms_total / max(1, iters)
     value = world * max(1, iters) / (ms_total * 1e-3)
     x_mixed = dx.clone()
+    # the returned state's residual re-evaluated with FP64 sums
+    s.set_fill_arithmetic(native.FILL_FP64)
+    R_chk = torch.empty_like(dx)
+    s.fill_device(x_mixed, R_chk, 1)
+    resid_fp64 = float(torch.linalg.vector_norm(R_chk).item())
+    del R_chk
+    progress(f"residual of the solution in FP64: {resid_fp64:.2e}")
 
     # kernel-family timings at the converged state
     R = torch.empty_like(dx)
@@ -405,9 +416,10 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_solve, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": ("f64 residual near the solution; Schur products: split-f16 x3 tensor-core attraction sums, "
-                      "f32 other stencil sums" if args.products == "fp16tc" else
-                      "f64 residual near the solution, f32 stencil sums in the Schur products"),
+            "dtype": (("f64-accurate residual near the solution (float-float 3-D sums, rechecked in f64)"
+                       if args.accurate_fill == "ff" else "f64 residual near the solution") +
+                      ("; Schur products: split-f16 x3 tensor-core attraction sums, f32 other stencil sums"
+                       if args.products == "fp16tc" else "; f32 stencil sums in the Schur products")),
             "data": "synthetic",
             "config": {"workload": WORKLOADS[args.workload], "step": "one Newton solve from the initial state to ||R||_2 <= "
                        f"{args.resid_tol:g}", "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
@@ -416,6 +428,7 @@ def main():
                        "l2_flush": "none (working set > L2)"},
             "newton_iters_per_step": iters / args.steps, "ms_per_newton_iter": ms_per_iter,
             "gmres_iters_per_newton_iter": lin_iters / max(1, iters), "final_resid_norm2": max(final_r),
+            "final_resid_norm2_fp64_recheck": resid_fp64, "accurate_fill": args.accurate_fill,
             "gpu_launches": int(st["kernel_launches"]),
             "clocks": clk.summary(),
             "e2e": {"value": it_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8,

@@ -122,7 +122,11 @@ int tgpu_set_precision(tgpu_handle h, int precision);
  *                      the reference is refreshed in FP64 when the change exceeds tau times the
  *                      field (max norms).  tgpu_newton uses FP32 sums while ||R|| > switch_norm.
  * tau / switch_norm <= 0 keep the current values (defaults 1e-2 and 1.0). */
-enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2, TGPU_FILL_MIXED = 3 };
+enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2, TGPU_FILL_MIXED = 3, TGPU_FILL_FF = 4,
+       TGPU_FILL_MIXED_FF = 5 };
+/* TGPU_FILL_FF: as TGPU_FILL_FP64, but the 3-D single-channel stencil sums (attraction, theta) run in
+ * float-float arithmetic (FP32 high/low pairs, error-free products and two-sums: ~48-bit sums, within
+ * ~1e-13 of FP64); TGPU_FILL_MIXED_FF: FP32 sums while ||R||_2 > switch_norm, TGPU_FILL_FF below. */
 /* TGPU_FILL_MIXED: in tgpu_newton_solve, FP32 sums while ||R||_2 > switch_norm, FP64 below;
  * everywhere else it is the FP64 fill. */
 int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm);

@@ -141,6 +141,7 @@ struct Ctx : tgpu_ctx {
   // tensor-core attraction sums: the FP16 slab, whether it exists, whether the current call uses it
   tgpu::TcSlab tcslab{};
   bool tc_ready = false, tc_on = false;
+  bool ff_on = false;   // the current fill's 3-D single-channel sums in float-float arithmetic
   std::string tc_why;
   bool have_integ = false;
   tgpu::ObjConst oc{};
@@ -245,6 +246,18 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
       tgpu::launch_conv_slab(c->d_pad32 + (long)ch0 * NP, total, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w,
                              outs[0], ln.pitch, ln.ncols, ln.max_rows, ln.max_lines, ln.max_w, c->dg.nx[0],
                              c->dg.nx[1], c->dg.nx[2], c->stream);
+      c->stats.conv_launches++;
+      c->stats.kernel_launches++;
+      return;
+    }
+  }
+  if (!f32 && c->ff_on && nin == 1 && nout == 1) {
+    const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
+    if (ln.nplanes > 0 && ln.ff_ok) {
+      const long total = (long)c->nch_max * NP - (long)ch0 * NP;
+      tgpu::launch_conv_slab_ff(c->d_pad + (long)ch0 * NP, total, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w,
+                                ln.d_w_lo, outs[0], ln.pitch, ln.ncols, ln.max_rows, ln.max_lines, ln.max_w,
+                                c->dg.nx[0], c->dg.nx[1], c->dg.nx[2], c->stream);
       c->stats.conv_launches++;
       c->stats.kernel_launches++;
       return;
@@ -383,9 +396,11 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
     }
   } else {
     const bool f32 = arith == TGPU_FILL_FP32;
+    c->ff_on = arith == TGPU_FILL_FF;
     forward_pass(c, rho, c->pads.rho_res, f32);
     tgpu::launch_fmt_local(x, c->d_chan, c->stream);
     transpose_pass(c, c->pads.tr_res, f32);
+    c->ff_on = false;
   }
   tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream);
   c->stats.kernel_launches += 2;
@@ -395,7 +410,9 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
 void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
 {
   // outside the Newton solve the mixed policy means the accurate (FP64) residual
-  fill_arith(c, d_x, d_R, mode, c->fill_mode == TGPU_FILL_MIXED ? TGPU_FILL_FP64 : c->fill_mode);
+  fill_arith(c, d_x, d_R, mode,
+             c->fill_mode == TGPU_FILL_MIXED ? TGPU_FILL_FP64
+             : c->fill_mode == TGPU_FILL_MIXED_FF ? TGPU_FILL_FF : c->fill_mode);
 }
 
 void need_state(Ctx *c)
@@ -674,9 +691,11 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
   bool converged = false;
   for (;;) {
     int arith = c->fill_mode;
-    const bool inexact = (arith == TGPU_FILL_MIXED || arith == TGPU_FILL_REFINED) && rprev > c->refine_switch;
+    const bool inexact = (arith == TGPU_FILL_MIXED || arith == TGPU_FILL_MIXED_FF || arith == TGPU_FILL_REFINED) &&
+                         rprev > c->refine_switch;
     if (inexact) arith = TGPU_FILL_FP32;
     else if (arith == TGPU_FILL_MIXED) arith = TGPU_FILL_FP64;
+    else if (arith == TGPU_FILL_MIXED_FF) arith = TGPU_FILL_FF;
     fill_arith(c, d_x, d_R, 0, arith);
     tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
     red_to_host(c, 1);
@@ -992,7 +1011,7 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
     planes[o[2]][o[1]].push_back({o[0], coef[k]});
   }
   std::vector<int4> pd, lines;
-  std::vector<float> w;
+  std::vector<float> w, w_lo;
   DevStencil::Lines L;
   for (auto &pkv : planes) {
     const int oz = pkv.first;
@@ -1005,7 +1024,12 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
       lines.push_back({ykv.first - oy_lo, xmin + dg.h[0], nb, (int)w.size()});
       const size_t base = w.size();
       w.resize(base + (size_t)nb * 8, 0.0f);
-      for (auto &e : ykv.second) w[base + (e.first - xmin)] = (float)e.second;
+      w_lo.resize(base + (size_t)nb * 8, 0.0f);
+      for (auto &e : ykv.second) {
+        const float hi = (float)e.second;
+        w[base + (e.first - xmin)] = hi;
+        w_lo[base + (e.first - xmin)] = (float)(e.second - (double)hi);
+      }
     }
     const int nl = (int)lines.size() - first_line, nw = (int)w.size() - first_w;
     pd.push_back({first_line, nl, first_w, nw});
@@ -1025,6 +1049,8 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
   L.d_planes = upload(pd, s);
   L.d_lines = upload(lines, s);
   L.d_w = upload(w, s);
+  L.d_w_lo = upload(w_lo, s);
+  L.ff_ok = tgpu::conv_slab_ff_smem(L.pitch, L.max_rows, L.max_lines, L.max_w) <= 220 * 1024;
   return L;
 }
 
@@ -1309,7 +1335,9 @@ int tgpu_destroy(tgpu_handle h)
       for (auto &st : c->sten[t]) {
         dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
         dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
-        for (auto *L : {&st.lines_fwd, &st.lines_tr}) { dfree(L->d_planes); dfree(L->d_lines); dfree(L->d_w); }
+        for (auto *L : {&st.lines_fwd, &st.lines_tr}) {
+          dfree(L->d_planes); dfree(L->d_lines); dfree(L->d_w); dfree(L->d_w_lo);
+        }
         tgpu::tc_free_tables(st.tc);
       }
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
@@ -1468,7 +1496,8 @@ int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch
 {
   return guard([&] {
     Ctx *c = C(h);
-    if (arith != TGPU_FILL_FP64 && arith != TGPU_FILL_FP32 && arith != TGPU_FILL_REFINED && arith != TGPU_FILL_MIXED)
+    if (arith != TGPU_FILL_FP64 && arith != TGPU_FILL_FP32 && arith != TGPU_FILL_REFINED && arith != TGPU_FILL_MIXED &&
+        arith != TGPU_FILL_FF && arith != TGPU_FILL_MIXED_FF)
       throw Error(TGPU_ERR_ARG, "fill arithmetic");
     if (tau > 0) c->refine_tau = tau;
     if (switch_norm > 0) c->refine_switch = switch_norm;

@@ -314,6 +314,145 @@ void launch_conv_slab(const float *in, long in_total, const int4 *planes, int np
 }
 
 // ---------------------------------------------------------------------------
+// FP64-accurate single-channel 3-D stencil sums in float-float arithmetic.
+//
+// The same slab / x-line traversal as k_conv_slab, on an FP64 padded field:
+// every value is split into FP32 high and low parts (f = f_hi + f_lo, exact to
+// ~2^-48 relative) and every weight likewise.  Each term w f is formed as
+// p = fl(w_hi f_hi) plus its exact rounding error e = fma(w_hi, f_hi, -p) and
+// the cross terms w_hi f_lo + w_lo f_hi; p is added to the running sum s by an
+// error-free two-sum and the errors go to a compensation c, so s + c carries
+// about 48 bits (Ogita-Rump-Oishi compensated summation) over one x-line; the
+// line sums go into an FP64 total.  Twelve FP32 operations per term against
+// one FP64 FMA: on GB300, whose FP64 pipe runs at 1/64 of the FP32 rate, that
+// is ~5x fewer issue slots.  Intrinsics (__fmul_rn,
+// __fadd_rn) keep the compiler from fusing the products into the sums.
+__device__ __forceinline__ void ff_term(float wh, float wl, float fh, float fl, float &s, float &c)
+{
+  const float p = __fmul_rn(wh, fh);
+  const float e = __fmaf_rn(wh, fh, -p);
+  const float t = __fadd_rn(s, p);
+  const float bp = __fsub_rn(t, s);
+  const float e2 = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(e, e2));
+  c = __fmaf_rn(wh, fl, c);
+  c = __fmaf_rn(wl, fh, c);
+}
+
+__global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__restrict__ in, long in_total,
+                                                             const int4 *__restrict__ planes, int nplanes,
+                                                             const int4 *__restrict__ lines,
+                                                             const float *__restrict__ lw,
+                                                             const float *__restrict__ lw_lo,
+                                                             double *__restrict__ out, int pitch, int ncols,
+                                                             int max_rows, int max_lines, int max_w)
+{
+  extern __shared__ float smem[];
+  float *s_hi = smem;                                          // [max_rows][pitch]
+  float *s_lo = s_hi + (size_t)max_rows * pitch;               // [max_rows][pitch]
+  float *s_w = s_lo + (size_t)max_rows * pitch;                // [max_w]
+  float *s_wl = s_w + max_w;                                   // [max_w]
+  int4 *s_line = reinterpret_cast<int4 *>(s_wl + max_w);      // [max_lines]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int x0 = blockIdx.x * kSlabTX, y0 = blockIdx.y * kSlabTY, z = blockIdx.z;
+  double total[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) total[o] = 0.0;
+  for (int pi = 0; pi < nplanes; pi++) {
+    const int4 pd = planes[2 * pi];
+    const int4 pg = planes[2 * pi + 1];
+    const int nrows = kSlabTY + pg.z - pg.y;
+    __syncthreads();
+    for (int k = threadIdx.x; k < pd.y; k += kSlabThreads) s_line[k] = lines[pd.x + k];
+    for (int k = threadIdx.x; k < pd.w; k += kSlabThreads) {
+      s_w[k] = lw[pd.z + k];
+      s_wl[k] = lw_lo[pd.z + k];
+    }
+    const long gz = (long)(z + pg.x + c_g.h[2]) * c_g.pstride[2];
+    for (int e = threadIdx.x; e < nrows * ncols; e += kSlabThreads) {
+      const int r = e / ncols, cidx = e - r * ncols;
+      const int gy = y0 + pg.y + r + c_g.h[1];
+      const long gi = gz + (long)gy * c_g.pstride[1] + x0 + cidx;
+      double v = 0.0;
+      if (gy < c_g.P[1] && gi < in_total) v = __ldg(in + gi);
+      const float hi = __double2float_rn(v);
+      s_hi[r * pitch + slab_phys(cidx)] = hi;
+      s_lo[r * pitch + slab_phys(cidx)] = __double2float_rn(v - (double)hi);
+    }
+    __syncthreads();
+    for (int li = 0; li < pd.y; li++) {
+      const int4 ln = s_line[li];
+      const float *rh = s_hi + (ty + ln.x) * pitch;
+      const float *rl = s_lo + (ty + ln.x) * pitch;
+      const float *w = s_w + (ln.w - pd.z);
+      const float *wlo = s_wl + (ln.w - pd.z);
+      const int c0 = 8 * tx + ln.y;
+      // one line (<= a few dozen terms) in float-float, then added to an FP64 total: the compensation
+      // stays short, so its own rounding does not build up over the 1e5 terms of a large stencil
+      float sum[8], comp[8];
+#pragma unroll
+      for (int o = 0; o < 8; o++) { sum[o] = 0.f; comp[o] = 0.f; }
+      float wh_[16], wl_[16];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        wh_[q] = rh[slab_phys(c0 + q)];
+        wl_[q] = rl[slab_phys(c0 + q)];
+      }
+      for (int kb = 0; kb < ln.z; kb++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          wh_[8 + q] = rh[slab_phys(c0 + 8 * (kb + 1) + q)];
+          wl_[8 + q] = rl[slab_phys(c0 + 8 * (kb + 1) + q)];
+        }
+#pragma unroll
+        for (int kk = 0; kk < 8; kk++) {
+          const float a = w[8 * kb + kk], al = wlo[8 * kb + kk];
+#pragma unroll
+          for (int o = 0; o < 8; o++) ff_term(a, al, wh_[o + kk], wl_[o + kk], sum[o], comp[o]);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          wh_[q] = wh_[8 + q];
+          wl_[q] = wl_[8 + q];
+        }
+      }
+#pragma unroll
+      for (int o = 0; o < 8; o++) total[o] += (double)sum[o] + (double)comp[o];
+    }
+  }
+  const int y = y0 + ty;
+  if (y < c_g.nx[1]) {
+    const long i0 = (long)c_g.nx[0] * (y + (long)c_g.nx[1] * z);
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+      const int x = x0 + 8 * tx + o;
+      if (x < c_g.nx[0]) out[i0 + x] += total[o];
+    }
+  }
+}
+
+size_t conv_slab_ff_smem(int pitch, int max_rows, int max_lines, int max_w)
+{
+  return sizeof(float) * (2 * (size_t)max_rows * pitch + 2 * (size_t)max_w) + sizeof(int4) * max_lines;
+}
+
+void launch_conv_slab_ff(const double *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
+                         const float *lw, const float *lw_lo, double *out, int pitch, int ncols, int max_rows,
+                         int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s)
+{
+  const size_t smem = conv_slab_ff_smem(pitch, max_rows, max_lines, max_w);
+  static size_t configured = 0;
+  if (smem > configured) {
+    cudaFuncSetAttribute(k_conv_slab_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 grid((nx + kSlabTX - 1) / kSlabTX, (ny + kSlabTY - 1) / kSlabTY, nz);
+  k_conv_slab_ff<<<grid, kSlabThreads, smem, s>>>(in, in_total, planes, nplanes, lines, lw, lw_lo, out, pitch, ncols,
+                                                   max_rows, max_lines, max_w);
+}
+
+// ---------------------------------------------------------------------------
 // FMT physics at one node.  n is in the reference's n ordering
 // (n0, n1, n2, n3, V1[d], V2[d]); sv is the solution-vector ordering
 // (n3, n2, n1, n0, V2[d], V1[d]) (solutionVec_to_nOrdering, src/dft_utils.c:205-221).

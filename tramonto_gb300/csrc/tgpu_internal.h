@@ -136,7 +136,9 @@ struct DevStencil {
   struct Lines {
     int4 *d_planes = nullptr, *d_lines = nullptr;
     float *d_w = nullptr;
+    float *d_w_lo = nullptr;            // FP32 remainder of each weight (float-float sums)
     int nplanes = 0, max_rows = 0, max_lines = 0, max_w = 0, ncols = 0, pitch = 0;
+    bool ff_ok = false;                 // the float-float slab fits in shared memory
   } lines_fwd, lines_tr;
 };
 
@@ -205,6 +207,10 @@ void launch_conv(const T *in, long in_cstride, int nin, const int *loff, const T
 void launch_conv_slab(const float *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
                       const float *lw, double *out, int pitch, int ncols, int max_rows, int max_lines, int max_w,
                       int nx, int ny, int nz, cudaStream_t s);
+size_t conv_slab_ff_smem(int pitch, int max_rows, int max_lines, int max_w);
+void launch_conv_slab_ff(const double *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
+                         const float *lw, const float *lw_lo, double *out, int pitch, int ncols, int max_rows,
+                         int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s);
 constexpr int kSlabTileX = 128, kSlabTileY = 16;
 void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,

@@ -48,10 +48,14 @@ def set_mode(s, mixed):
 
 
 def solve_state(s, p, x0, mixed=True, resid_tol=1e-8, max_iter=60):
-    """Newton solve from x0; returns (x, iterations, ||R||_2, GMRES iterations, converged)."""
+    """Newton solve from x0; returns (x, iterations, ||R||_2, GMRES iterations, converged).  A solve that
+    runs into non-finite values (a Newton path through n3 >= 1) returns unconverged with x0."""
     set_mode(s, mixed)
-    x, it, rn, li = s.newton_solve(x0, resid_tol=resid_tol, max_iter=max_iter, lin_tol=1e-6 if mixed else 1e-10,
-                                   lin_max_iter=300, allow_noconv=True)
+    try:
+        x, it, rn, li = s.newton_solve(x0, resid_tol=resid_tol, max_iter=max_iter,
+                                       lin_tol=1e-6 if mixed else 1e-10, lin_max_iter=300, allow_noconv=True)
+    except native.TgpuError:
+        return np.array(x0), max_iter, float("inf"), 0, False
     return x, it, rn, li, bool(rn <= resid_tol)
 
 
@@ -78,13 +82,32 @@ def isotherm(spec, rho_ladder, mixed=True, resid_tol=1e-8, with_derivative=True)
         s.close()
 
 
+def ladders_to(rho_b, steps=4):
+    """Bulk-density ladders for reaching rho_b by continuation: from the gas side (0.05) and from the liquid
+    side (0.55) of the mean-field van der Waals loop (kT* = 1.2: gas below ~0.2, liquid above ~0.3), the
+    side rho_b lies on first."""
+    gas = list(np.linspace(0.05, rho_b, steps))
+    liquid = list(np.linspace(0.55, rho_b, steps))
+    return [gas, liquid] if rho_b < 0.25 else [liquid, gas]
+
+
 def sweep(specs, mixed=True, resid_tol=1e-8, with_derivative=True):
-    """Every configuration-5 problem at its own state point, solved from its initial state."""
+    """Every configuration-5 problem at its own state point, solved from its initial state; a state point
+    that does not converge directly is reached by continuation along ladders_to(rho_b)."""
     recs = []
     for spec in specs:
         t0 = time.perf_counter()
         r, _ = isotherm(spec, [spec["rho_b"]], mixed, resid_tol, with_derivative)
-        r[0]["wall_s"] = time.perf_counter() - t0
-        r[0]["ndim"], r[0]["nodes"] = spec["ndim"], int(np.prod(spec["nx"][:spec["ndim"]]))
-        recs.append(r[0])
+        rec = r[0]
+        rec["path"] = "direct"
+        for ladder in ([] if rec["converged"] else ladders_to(spec["rho_b"])):
+            r, _ = isotherm(spec, ladder, mixed, resid_tol, with_derivative)
+            rec = r[-1]
+            rec["path"] = f"continuation from {ladder[0]:.2f}"
+            rec["iters"] = sum(q["iters"] for q in r)
+            if rec["converged"]:
+                break
+        rec["wall_s"] = time.perf_counter() - t0
+        rec["ndim"], rec["nodes"] = spec["ndim"], int(np.prod(spec["nx"][:spec["ndim"]]))
+        recs.append(rec)
     return recs

@@ -29,7 +29,7 @@ from .problem import Problem
 
 TGPU_OK = 0
 FP64, FP32, BF16X3, FP16TC = 0, 1, 2, 3
-FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED = 0, 1, 2, 3
+FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF, FILL_MIXED_FF = 0, 1, 2, 3, 4, 5
 STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
           -5: "no convergence", -6: "non-finite values", -7: "domain error"}
 
@@ -271,7 +271,8 @@ class Solver:
         _check(self.lib.tgpu_set_precision(self.h, int(precision)), self.lib)
 
     def set_fill_arithmetic(self, arith: int, tau: float = 0.0, switch_norm: float = 0.0):
-        """Residual arithmetic: FILL_FP64, FILL_FP32 or FILL_REFINED (see include/tramonto_gpu.h)."""
+        """Residual arithmetic: FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF or FILL_MIXED_FF
+        (see include/tramonto_gpu.h)."""
         _check(self.lib.tgpu_set_fill_arithmetic(self.h, int(arith), float(tau), float(switch_norm)), self.lib)
 
     def set_stream(self, stream_handle: int):

@@ -237,7 +237,9 @@ def config2(n=128, esize=0.1, seed=1234, rho_b=0.6):
 def config4(n=256, esize=0.08, seed=1234):
     """The configuration-2 fluid and wall at scale: 256^3 nodes, dx = 0.08 (attraction reach 31 nodes,
     1.4e5 stencil points), rho_b = 0.75 (bulk n3 = 0.39)."""
-    return config2(n=n, esize=esize, seed=seed, rho_b=0.75)
+    p, meta = config2(n=n, esize=esize, seed=seed, rho_b=0.75)
+    meta["initial_cap"] = 1.0   # initial densities at most rho_b: rho_b exp(-V) in the wall's well overlaps (n3 > 1)
+    return p, meta
 
 
 def gaussian_random_field(nx, esize, corr_len=1.0, seed=4321):
