@@ -363,6 +363,8 @@ def main():
 
     rep64 = 1 if args.light else 3
     t_fill = timed(lambda: s.fill_device(x_mixed, R, 0), reps=rep64)
+    s.set_fill_arithmetic(native.FILL_FF)
+    t_fill_ff = timed(lambda: s.fill_device(x_mixed, R, 0), reps=rep64)
     s.set_fill_arithmetic(native.FILL_FP32)
     t_fill32 = timed(lambda: s.fill_device(x_mixed, R, 0))
     s.set_precision(native.FP32)
@@ -449,7 +451,8 @@ def main():
                          "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
                          "fp64_ms_per_launch": t_wca64},
             "cpu_baseline": cb,
-            "breakdown_ms": {"fill_fp64": t_fill, "fill_fp32": t_fill32, "schur_apply_fp32": t_apply32,
+            "breakdown_ms": {"fill_fp64": t_fill, "fill_float_float": t_fill_ff, "fill_fp32": t_fill32,
+                             "schur_apply_fp32": t_apply32,
                              "schur_apply_fp16tc": t_apply_tc,
                              "schur_apply_fp64": t_apply64, "schur_applies_in_timed_steps": int(st["schur_applies"])},
             "plain_fp64": {"ms_per_newton_iter": fp64_ms,
