@@ -56,8 +56,12 @@ typedef enum {
 
 /* boundary codes (reference Type_bc values, src/dft_globals_const.h) */
 enum { TGPU_BC_IN_WALL = -1, TGPU_BC_IN_BULK = 0, TGPU_BC_PERIODIC = 1, TGPU_BC_REFLECT = 2 };
-/* functionals (reference Type_func values) */
-enum { TGPU_FMT1 = 0, TGPU_FMT3 = 2 };
+/* functionals (reference Type_func values, src/dft_globals_const.h:247-250): Rosenfeld (FMT1),
+ * Rosenfeld with the zero-dimensional-crossover third term (FMT2), White-Bear (FMT3), White-Bear
+ * with the FMT2 vector form (FMT4) */
+enum { TGPU_FMT1 = 0, TGPU_FMT2 = 1, TGPU_FMT3 = 2, TGPU_FMT4 = 3 };
+/* second derivatives of the FMT terms in J, J^T and Schur products (tgpu_set_jacobian_form) */
+enum { TGPU_JAC_REFERENCE = 0, TGPU_JAC_EXACT = 1 };
 /* stencil types (reference Stencil ids, src/dft_globals_const.h:152-161) */
 enum { TGPU_STEN_DELTA = 0, TGPU_STEN_THETA = 1, TGPU_STEN_UATT = 2 };
 /* arithmetic of the stencil convolutions */
@@ -71,7 +75,7 @@ typedef struct {
   double esize[3];           /* Esize_x */
   int bc[3][2];              /* Type_bc[idim][left/right] */
   int ncomp;
-  int functional;            /* TGPU_FMT1 | TGPU_FMT3 */
+  int functional;            /* TGPU_FMT1 .. TGPU_FMT4 */
   int attraction;            /* 1: WCA mean field (Type_attr != NONE) */
   int att_in_a22;            /* ATTInA22Block; only 0 (mean field as its own unknown) is implemented */
   int single_size;           /* n1, n0, V1 are local copies (src/dft_fill_FMT.c:215, :303) */
@@ -130,6 +134,15 @@ enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2, TGPU_FILL_
 /* TGPU_FILL_MIXED: in tgpu_newton_solve, FP32 sums while ||R||_2 > switch_norm, FP64 below;
  * everywhere else it is the FP64 fill. */
 int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm);
+/* Second derivatives of the FMT energy density in J, J^T and Schur products (and so in Newton):
+ *   TGPU_JAC_REFERENCE  the reference's tables, entry for entry (default): d2phi_drb2_{delta,theta}_rb_FMT*
+ *                       (src/dft_physics_FMT{1,2,3,4}.c, via FMT2ndDeriv*_switch, src/dft_switch_FMT.c:122-152)
+ *   TGPU_JAC_EXACT      the Hessian of the energy density
+ * The two agree for FMT1 and FMT3.  For FMT2 in 2-D and 3-D the reference's V2-V2 entry has |gamma|^2 v_d
+ * where the Hessian has gamma_d (gamma . v); for FMT4 its n2-V2 entry has (fac^2 - 4 V2.V2 fac / n2) where
+ * the Hessian has fac (1 + 3 V2.V2 / n2^2), fac = 1 - V2.V2/n2^2 (src/dft_physics_FMT2.c:178-184,
+ * src/dft_physics_FMT4.c:175-182).  The sensitivities (tgpu_grad_*) always use the exact form. */
+int tgpu_set_jacobian_form(tgpu_handle h, int form);
 int tgpu_set_stream(tgpu_handle h, void *cuda_stream);
 int tgpu_sizes(tgpu_handle h, long *nnodes, int *nunk, int *ncomp);
 

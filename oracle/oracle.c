@@ -144,6 +144,61 @@ static void fmt3_d1(int nd, const double *n, double dot12, double dot22, const d
   }
 }
 
+/* FMT2_1stderiv (src/dft_physics_FMT2.c:60-99): the Rosenfeld terms with the
+ * third term (n2 - V2.V2/n2)^3 / (24 pi (1-n3)^2); alpha = n2 - V2.V2/n2,
+ * beta = 1 + V2.V2/n2^2, gamma = V2/n2, and alpha = n2, beta = 1, gamma = 0
+ * where n2 <= 1e-15. */
+static void fmt2_d1(int nd, const double *n, double dot12, double dot22, const double *inv, double *out)
+{
+  out[0] = log(inv[1]);
+  out[1] = n[2] * inv[1];
+  out[2] = n[1] * inv[1];
+  out[3] = n[0] * inv[1] + (n[1] * n[2] - dot12) * inv[2];
+  for (int d = 0; d < nd; d++) {
+    out[4 + d] = -n[4 + nd + d] * inv[1];
+    out[4 + nd + d] = -n[4 + d] * inv[1];
+  }
+  double alpha = n[2], beta = 1.0, gamma[3] = {0.0, 0.0, 0.0};
+  if (n[2] > 1.e-15) {
+    alpha = n[2] - dot22 / n[2];
+    beta = 1.0 + dot22 / (n[2] * n[2]);
+    for (int d = 0; d < nd; d++) gamma[d] = n[4 + nd + d] / n[2];
+  }
+  const double a2 = alpha * alpha, a3 = a2 * alpha;
+  out[2] += a2 * beta * inv[2] / (8.0 * PI);
+  out[3] += a3 * inv[3] / (12.0 * PI);
+  for (int d = 0; d < nd; d++) out[4 + nd + d] -= inv[2] * a2 * gamma[d] / (4.0 * PI);
+}
+
+/* FMT4_1stderiv (src/dft_physics_FMT4.c:61-97): White-Bear n3 dependence with
+ * the (1 - V2.V2/n2^2)^3 vector correction; all n2, n3 and V2 derivatives are
+ * zero where n3 <= 1e-10, as in the reference. */
+static void fmt4_d1(int nd, const double *n, double dot12, double dot22, const double *inv, double *out)
+{
+  out[0] = log(inv[1]);
+  out[1] = n[2] * inv[1];
+  double fac = 0.0, fac2 = 0.0;
+  if (n[3] > 1.e-10) {
+    fac = 1 - dot22 / (n[2] * n[2]);
+    const double fac1 = n[3] - 2. * (1. - n[3]) * log(1. - n[3]);
+    fac2 = (n[3] + (1. - n[3]) * (1. - n[3]) * log(1. - n[3]));
+    const double f3 = fac * fac * fac, n2c = n[2] * n[2] * n[2];
+    out[2] = n[1] * inv[1] + (n[2] * n[2] * f3 + 2 * fac * fac * dot22) * inv[2] * fac2 / (12.0 * PI * n[3] * n[3]);
+    out[3] = n[0] * inv[1] + (n[1] * n[2] - dot12) * inv[2] + fac1 * n2c * f3 * inv[2] / (36.0 * PI * n[3] * n[3]) +
+             fac2 * n2c * f3 * (-inv[2] / (n[3] * n[3] * n[3]) + inv[3] / (n[3] * n[3])) / (18.0 * PI);
+  } else {
+    out[2] = 0.0;
+    out[3] = 0.0;
+  }
+  for (int d = 0; d < nd; d++) {
+    const int iv1 = 4 + d, iv2 = 4 + nd + d;
+    out[iv1] = -n[iv2] * inv[1];
+    out[iv2] = (n[3] > 1.e-10)
+                   ? -n[iv1] * inv[1] - n[2] * n[iv2] * fac2 * inv[2] * fac * fac / (6.0 * PI * n[3] * n[3])
+                   : 0.0;
+  }
+}
+
 /* calc_FMT_derivatives (src/dft_fill_FMT.c:349-385) at one node */
 static void node_dphi(const orc_problem *p, const double *x, long node, double *out)
 {
@@ -160,8 +215,12 @@ static void node_dphi(const orc_problem *p, const double *x, long node, double *
     dot22 += n[4 + nd + d] * n[4 + nd + d];
     dot12 += n[4 + d] * n[4 + nd + d];
   }
-  if (p->functional == ORC_FMT3) fmt3_d1(nd, n, dot12, dot22, inv, out);
-  else fmt1_d1(nd, n, dot12, dot22, inv, out);
+  switch (p->functional) {
+    case ORC_FMT2: fmt2_d1(nd, n, dot12, dot22, inv, out); break;
+    case ORC_FMT3: fmt3_d1(nd, n, dot12, dot22, inv, out); break;
+    case ORC_FMT4: fmt4_d1(nd, n, dot12, dot22, inv, out); break;
+    default: fmt1_d1(nd, n, dot12, dot22, inv, out); break;
+  }
 }
 
 int orc_dphi(const orc_problem *p, const double *x, double *dphi)
@@ -298,6 +357,193 @@ static rbs d2_theta_fmt3(const orc_problem *p, const double *n)
   return t;
 }
 
+/* The n2/V2 structure of the FMT2 third term at one node: alpha, beta, gamma as
+ * in fmt2_d1 (gamma from the signed vector densities), eps = alpha/n2 and
+ * |gamma|^2, with eps = 1, gamma = 0 where n2 <= 1e-15. */
+typedef struct { double alpha, beta, eps, gg, gamma[3]; } fmt2_terms;
+
+static fmt2_terms fmt2_terms_of(int nd, double n2, const double *n2v)
+{
+  fmt2_terms t = {n2, 1.0, 1.0, 0.0, {0.0, 0.0, 0.0}};
+  double q = 0.0;
+  for (int d = 0; d < nd; d++) q += n2v[d] * n2v[d];
+  if (n2 > 1.e-15) {
+    t.alpha = n2 - q / n2;
+    t.beta = 1.0 + q / (n2 * n2);
+    for (int d = 0; d < nd; d++) {
+      t.gamma[d] = n2v[d] / n2;
+      t.gg += t.gamma[d] * t.gamma[d];
+    }
+    t.eps = t.alpha / n2;
+  }
+  return t;
+}
+
+/* d2phi_drb2_delta_rb_FMT2 (src/dft_physics_FMT2.c:104-186).  The V2-V2 entry
+ * keeps the reference's form, -alpha (4 |gamma|^2 - eps) v_d / (4 pi (1-n3)^2):
+ * the Hessian of the FMT2 energy density has 4 gamma_d (gamma . v) there, the
+ * same in one dimension. */
+static rbs d2_delta_fmt2(const orc_problem *p, const double *n, const short *off, const double *sign, int ic)
+{
+  rbs t;
+  const int nd = p->ndim;
+  double n1v[3], n2v[3], v[3];
+  for (int d = 0; d < nd; d++) {
+    n2v[d] = sign[d] * n[4 + nd + d];
+    n1v[d] = sign[d] * n[4 + d];
+  }
+  const fmt2_terms g = fmt2_terms_of(nd, n[2], n2v);
+  const double a = 1.0 / (1.0 - n[3]), a2 = a * a, a3 = a2 * a;
+  const double i4p = 1.0 / (4.0 * PI);
+  for (int d = 0; d < nd; d++) v[d] = off[d] * p->esize[d] * p->inv_rad[ic];
+  t.S2 = a * p->inv_4pir[ic] + i4p * a2 * g.alpha * (g.beta * g.beta - g.eps * g.gg);
+  for (int d = 0; d < nd; d++) t.S2 -= i4p * a2 * g.alpha * (g.eps - 2 * g.beta) * g.gamma[d] * v[d];
+  t.S3 = (p->inv_4pirsq[ic] * a + n[2] * p->inv_4pir[ic] * a2 + n[1] * a2);
+  for (int d = 0; d < nd; d++) t.S3 += a2 * v[d] * (n2v[d] * p->inv_4pir[ic] + n1v[d]);
+  t.S3 += i4p * a3 * g.alpha * g.alpha * g.beta;
+  for (int d = 0; d < nd; d++) t.S3 += 2.0 * i4p * a3 * g.alpha * g.alpha * g.gamma[d] * v[d];
+  t.S0 = 0.0;
+  t.S1 = a;
+  for (int d = 0; d < nd; d++) {
+    t.V1[d] = sign[d] * a * v[d];
+    t.V2[d] = sign[d] * (p->inv_4pir[ic] * a) * v[d];
+  }
+  for (int d = 0; d < nd; d++) {
+    t.V2[d] += sign[d] * i4p * a2 * g.alpha * (g.eps - 2.0 * g.beta) * g.gamma[d];
+    t.V2[d] -= sign[d] * i4p * a2 * g.alpha * (4.0 * g.gg - g.eps) * v[d];
+  }
+  return t;
+}
+
+/* d2phi_drb2_theta_rb_FMT2 (src/dft_physics_FMT2.c:191-250) */
+static rbs d2_theta_fmt2(const orc_problem *p, const double *n)
+{
+  rbs t;
+  const int nd = p->ndim;
+  double dot12 = 0.0;
+  for (int d = 0; d < nd; d++) dot12 += n[4 + d] * n[4 + nd + d];
+  const fmt2_terms g = fmt2_terms_of(nd, n[2], n + 4 + nd);
+  const double a = 1.0 / (1.0 - n[3]), a2 = a * a, a3 = a2 * a, a4 = a3 * a;
+  const double i4p = 1.0 / (4.0 * PI);
+  const double al2 = g.alpha * g.alpha;
+  t.S2 = n[1] * a2 + i4p * a3 * al2 * g.beta;
+  t.S3 = n[0] * a2 + 2.0 * (n[1] * n[2] - dot12) * a3 + i4p * a4 * al2 * g.alpha;
+  t.S0 = a;
+  t.S1 = n[2] * a2;
+  for (int d = 0; d < nd; d++) {
+    t.V1[d] = -n[4 + nd + d] * a2;
+    t.V2[d] = -n[4 + d] * a2 - 2.0 * i4p * a3 * al2 * g.gamma[d];
+  }
+  return t;
+}
+
+/* d2phi_drb2_delta_rb_FMT4 (src/dft_physics_FMT4.c:102-196).  As FMT3, it uses
+ * the vector densities without the reflection sign.  Its V2 entry keeps the
+ * reference's n2-V2 coefficient (fac^2 - 4 |V2|^2 fac / n2); the Hessian of the
+ * FMT4 energy density has fac (1 + 3 |V2|^2 / n2^2) there. */
+static rbs d2_delta_fmt4(const orc_problem *p, const double *n, const short *off, const double *sign, int ic)
+{
+  rbs t;
+  const int nd = p->ndim;
+  double inv[5], v[3];
+  double dot22 = 0.0;
+  for (int d = 0; d < nd; d++) dot22 += n[4 + nd + d] * n[4 + nd + d];
+  inv[0] = (1. - n[3]);
+  inv[1] = 1.0 / (1.0 - n[3]);
+  inv[2] = inv[1] * inv[1];
+  inv[3] = inv[2] * inv[1];
+  inv[4] = inv[3] * inv[1];
+  const double n3sq = n[3] * n[3], n3cb = n3sq * n[3], n2sq = n[2] * n[2], n2cb = n2sq * n[2];
+  memset(&t, 0, sizeof(t));
+  if (n[3] > 1.e-10) {
+    const double fac1 = n[3] - 2 * (1. - n[3]) * log(1. - n[3]);
+    const double fac2 = n[3] + (1. - n[3]) * (1. - n[3]) * log(1. - n[3]);
+    const double fac3 = -(inv[2] / n3cb) + (inv[3] / n3sq);
+    const double fac = 1 - dot22 / (n[2] * n[2]);
+    const double k6 = fac2 * inv[2] / (6. * PI * n3sq);
+    const double k3 = (2. * fac2 * fac3) + (fac1 * inv[2] / n3sq);
+    for (int d = 0; d < nd; d++) v[d] = off[d] * p->esize[d] * p->inv_rad[ic];
+    t.S2 = (inv[1] * p->inv_4pir[ic] +
+            k6 * (n[2] * fac * fac * fac + 3 * dot22 * fac * fac / n[2] + 4 * dot22 * dot22 * fac / n2cb));
+    for (int d = 0; d < nd; d++) t.S2 += v[d] * n[4 + nd + d] * k6 * (fac * fac + 4 * dot22 * fac / n2sq);
+    t.S3 = (p->inv_4pirsq[ic] * inv[1] + p->inv_4pir[ic] * n[2] * inv[2] + n[1] * inv[2] +
+            (n2sq * fac * fac * fac + 2 * dot22 * fac * fac) * k3 / (12. * PI));
+    for (int d = 0; d < nd; d++)
+      t.S3 += v[d] * (n[4 + nd + d] * p->inv_4pir[ic] * inv[2] + n[4 + d] * inv[2] +
+                      n[2] * n[4 + nd + d] * fac * fac * k3 / (6. * PI));
+    t.S0 = 0.0;
+    t.S1 = inv[1];
+    double dot_nw = 0.0;
+    for (int d = 0; d < nd; d++) {
+      t.V1[d] = sign[d] * inv[1] * v[d];
+      dot_nw += n[4 + nd + d] * v[d];
+    }
+    for (int d = 0; d < nd; d++)
+      t.V2[d] = sign[d] * (-(n[4 + nd + d] * k6) * (fac * fac - 4 * dot22 * fac / n[2] + 4 * dot_nw * fac / n[2]) -
+                           (-p->inv_4pir[ic] * inv[1] - n[2] * fac * fac * k6) * v[d]);
+  }
+  return t;
+}
+
+/* d2phi_drb2_theta_rb_FMT4 (src/dft_physics_FMT4.c:201-275) */
+static rbs d2_theta_fmt4(const orc_problem *p, const double *n)
+{
+  rbs t;
+  const int nd = p->ndim;
+  double inv[5];
+  double dot22 = 0.0, dot12 = 0.0;
+  for (int d = 0; d < nd; d++) {
+    dot22 += n[4 + nd + d] * n[4 + nd + d];
+    dot12 += n[4 + d] * n[4 + nd + d];
+  }
+  inv[0] = (1. - n[3]);
+  inv[1] = 1.0 / (1.0 - n[3]);
+  inv[2] = inv[1] * inv[1];
+  inv[3] = inv[2] * inv[1];
+  inv[4] = inv[3] * inv[1];
+  const double n3sq = n[3] * n[3], n3cb = n3sq * n[3], n3_4th = n3cb * n[3];
+  const double n2sq = n[2] * n[2], n2cb = n2sq * n[2];
+  memset(&t, 0, sizeof(t));
+  if (n[3] > 1.e-10) {
+    const double fac1 = n[3] - 2 * (1. - n[3]) * log(1. - n[3]);
+    const double fac2 = n[3] + (1. - n[3]) * (1. - n[3]) * log(1. - n[3]);
+    const double fac3 = -(inv[2] / n3cb) + (inv[3] / n3sq);
+    const double fac = 1 - dot22 / (n[2] * n[2]);
+    const double k3 = (fac1 * inv[2] / n3sq) + (2. * fac2 * fac3);
+    t.S2 = (n[1] * inv[2] + (n2sq * fac * fac * fac + 2 * fac * fac * dot22) * k3 / (12 * PI));
+    t.S3 = (n[0] * inv[2] + 2 * (n[1] * n[2] - dot12) * inv[3] +
+            ((n2cb * fac * fac * fac) / (36. * PI)) *
+                (+(((2. * log(1. - n[3]) + 3) * inv[2]) / n3sq) + (4. * fac1 * fac3) +
+                 (fac2 * (6. * inv[2] / n3_4th + 6. * inv[4] / n3sq - 8. * inv[3] / n3cb))));
+    t.S0 = inv[1];
+    t.S1 = n[2] * inv[2];
+    for (int d = 0; d < nd; d++) t.V1[d] = -n[4 + nd + d] * inv[2];
+    for (int d = 0; d < nd; d++) t.V2[d] = -(n[4 + d] * inv[2] + n[2] * n[4 + nd + d] * fac * fac * k3 / (6. * PI));
+  }
+  return t;
+}
+
+/* FMT2ndDerivDelta_switch / FMT2ndDerivTheta_switch (src/dft_switch_FMT.c:122-152) */
+static rbs d2_delta(const orc_problem *p, const double *n, const short *off, const double *sign, int ic)
+{
+  switch (p->functional) {
+    case ORC_FMT2: return d2_delta_fmt2(p, n, off, sign, ic);
+    case ORC_FMT3: return d2_delta_fmt3(p, n, off, sign, ic);
+    case ORC_FMT4: return d2_delta_fmt4(p, n, off, sign, ic);
+    default: return d2_delta_fmt1(p, n, off, sign, ic);
+  }
+}
+
+static rbs d2_theta(const orc_problem *p, const double *n)
+{
+  switch (p->functional) {
+    case ORC_FMT2: return d2_theta_fmt2(p, n);
+    case ORC_FMT3: return d2_theta_fmt3(p, n);
+    case ORC_FMT4: return d2_theta_fmt4(p, n);
+    default: return d2_theta_fmt1(p, n);
+  }
+}
+
 /* ---------------------------------------------------------------------------
  * One pass over every row of the fill.  For each row the residual is summed in
  * the reference's order, and every Jacobian entry is handed to `entry`. */
@@ -409,9 +655,9 @@ static double rosen_rb(pass_t *ps, int stype, int iu, long inode, const int *ijk
       sv_to_n(p, ps->x, jn, n);
       rbs t;
       if (stype == ORC_DELTA)
-        t = (p->functional == ORC_FMT3) ? d2_delta_fmt3(p, n, o, sign, ic) : d2_delta_fmt1(p, n, o, sign, ic);
+        t = d2_delta(p, n, o, sign, ic);
       else
-        t = (p->functional == ORC_FMT3) ? d2_theta_fmt3(p, n) : d2_theta_fmt1(p, n);
+        t = d2_theta(p, n);
       const int jb = p->first_rb;
       ps->entry(ps->ctx, iu, inode, jb + 0, jn, fo * weight * t.S3);
       ps->entry(ps->ctx, iu, inode, jb + 1, jn, fo * weight * t.S2);

@@ -3,12 +3,14 @@
  * This is the oracle the GPU path is checked against.  It restates, in plain
  * serial C with the reference's own loop order, the residual and Jacobian of
  * Tramonto's hard-sphere FMT + WCA mean-field fill:
- *   - calc_FMT_derivatives / FMT1_1stderiv / FMT3_1stderiv
- *       (src/dft_fill_FMT.c:349-385, src/dft_physics_FMT1.c:59-77, src/dft_physics_FMT3.c:61-96)
+ *   - calc_FMT_derivatives / FMT{1,2,3,4}_1stderiv (src/dft_fill_FMT.c:349-385,
+ *       src/dft_physics_FMT1.c:59-77, src/dft_physics_FMT2.c:60-99, src/dft_physics_FMT3.c:61-96,
+ *       src/dft_physics_FMT4.c:61-97)
  *   - load_rho_bar_s / load_rho_bar_v / resid_and_Jac_sten_fill_sum_Ncomp
  *       (src/dft_fill_FMT.c:195-347, src/dft_fill_CLSmf.c:38-171)
- *   - load_nonlocal_hs_rosen_rb with d2phi_drb2_{delta,theta}_rb_FMT{1,3}
- *       (src/dft_fill_FMT.c:41-189, src/dft_physics_FMT1.c:79-168, src/dft_physics_FMT3.c:101-265)
+ *   - load_nonlocal_hs_rosen_rb with d2phi_drb2_{delta,theta}_rb_FMT{1,2,3,4}
+ *       (src/dft_fill_FMT.c:41-189, src/dft_physics_FMT1.c:79-168, src/dft_physics_FMT2.c:104-250,
+ *       src/dft_physics_FMT3.c:101-265, src/dft_physics_FMT4.c:102-275)
  *   - load_euler_lagrange (src/dft_fill_EL.c:38-196, 351-444) and load_mean_field (src/dft_fill_mf.c:38-63)
  *   - offset_to_node_box (src/dft_mesh_lib.c:203-297), HW_boundary_weight (src/dft_utils.c:41-62)
  *   - the hard-sphere Schur operator S = A22 - A21 A11^-1 A12 (src/dft_Schur_Epetra_Operator.cpp:86-119,
@@ -33,14 +35,14 @@ extern "C" {
 
 enum { ORC_DELTA = 0, ORC_THETA = 1, ORC_UATT = 2 };
 enum { ORC_BC_IN_WALL = -1, ORC_BC_IN_BULK = 0, ORC_BC_PERIODIC = 1, ORC_BC_REFLECT = 2 };
-enum { ORC_FMT1 = 0, ORC_FMT3 = 2 };
+enum { ORC_FMT1 = 0, ORC_FMT2 = 1, ORC_FMT3 = 2, ORC_FMT4 = 3 };
 
 typedef struct {
   int ndim, nx[3];
   double esize[3];
   int bc[3][2];
   int ncomp;
-  int functional;      /* ORC_FMT1 or ORC_FMT3 */
+  int functional;      /* ORC_FMT1 .. ORC_FMT4 (Type_func) */
   int attraction;      /* WCA mean field on/off */
   int att_in_a22;      /* 0: mean field is its own unknown (MF_EQ rows); 1: summed into the EL rows */
   int single_size;     /* n1, n0, V1 are dependent unknowns (one particle size) */

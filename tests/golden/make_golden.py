@@ -81,6 +81,26 @@ def cases():
         "Nwall_types Nwall Nlink": "1 1 1 0 0", "Xtest_reflect_TF": "0 0 0",
         "Lrough_surf": "0", "Lapply_offest": "0 0 0", "Cut_ff[i][j]": "2.5", "Rho_b_0[icomp]": "0.6",
         "ATTInA22Block": "0 20 0 0 0", "L_Schur": "1 0 100"}, surfaces=surf3d)
+    # 1-D HS5 with the zero-dimensional-crossover Rosenfeld functional (FMT2) and the
+    # White-Bear functional with the same vector correction (FMT4)
+    c["hs1d_fmt2"] = deck("HS5_FMT1_1D", {"Type_func (": "1 0"})
+    c["hs1d_fmt4"] = deck("HS5_FMT1_1D", {"Type_func (": "3 0"})
+    # a binary hard-sphere FMT4 mixture (sizes 1 and 0.6) against a hard wall
+    c["mix1d_fmt4"] = deck("MIX2_FMT1_WCA_1D", {
+        "Type_func (": "3 0", "Ncomp Mix_type": "2 1", "HS_diam[i]": "1. 0.6",
+        "Sigma_ff[i][j]": "1. 0.8 0.8 0.6", "Eps_ff[i][j]": "1. 0.9 0.9 0.8",
+        "Cut_ff[i][j]": "2.5 2.5 2.5 2.5", "Rho_b_0[icomp]": "0.25 0.35", "Esize_x(idim)": "0.05",
+        "Type_attr Type_pairPot": "-1 0", "Type of neutral surface-fluid": "1"})
+    # 3-D hard spheres against a rough hard wall (patches of 0.5 sigma, heights up to 0.5 sigma),
+    # periodic y and z: vector weighted densities with all three components nonzero
+    rough3d = {"Size_x(idim)": "3.0 3.0 3.0", "Esize_x(idim)": "0.25 0.25 0.25",
+               "Type_bc(x0": "-1 0", "Type_bc(x1": "1 1", "Type_bc(x2": "1 1",
+               "Nwall_types Nwall Nlink": "1 1 1 0 0", "Xtest_reflect_TF": "0 0 0",
+               "Lrough_surf": "1", "Lapply_offest": "1 0 0", "Type_attr Type_pairPot": "-1 0",
+               "Type of neutral surface-fluid": "1",
+               "Rho_b_0[icomp]": "0.6", "ATTInA22Block": "0 30 0 0 0", "L_Schur": "1 0 100"}
+    for name, func in (("rough3d_fmt2", "1 0"), ("rough3d_fmt4", "3 0")):
+        c[name] = deck("GEOM3_PLANE_ROUGH_3D", dict(rough3d, **{"Type_func (": func}), surfaces=surf3d)
     return c
 
 
@@ -174,8 +194,8 @@ def main(argv):
     names = argv or list(allc)
     for n in names:
         lines, surf = allc[n]
-        # the 3-D case keeps only the perturbed state to stay small
-        states = (("x_newton", 7, 0.02),) if n.endswith("3d") else ("x_newton", ("x_newton", 7, 0.02))
+        # the 3-D cases keep only the perturbed state to stay small
+        states = (("x_newton", 7, 0.02),) if "3d" in n else ("x_newton", ("x_newton", 7, 0.02))
         o = make_case(n, lines, surf, states)
         k = len(states) - 1
         print(f"{n}: nodes={o['info_ints'][5]} unknowns={o['info_ints'][7]} newton_iters={o['newton_iters']} "

@@ -23,7 +23,7 @@ from goldens import PROD_RTOL, load, probe, rel_err
 
 pytestmark = pytest.mark.gpu
 
-ADJ_CASES = ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d"]
+ADJ_CASES = ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "mix1d_fmt4", "rough3d_fmt2", "rough3d_fmt4"]
 GRAD_RTOL = 1e-5
 FD_H = 1e-6
 

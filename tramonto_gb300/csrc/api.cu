@@ -961,8 +961,30 @@ void ensure_obj(Ctx *c)
 }
 
 // dF/dV_ext at the state d_x: Jacobian at d_x (FP64 fill), J^T lambda = dF/dx, dF/dV = dF/dV|_x - lambda_EL
+// The sensitivities need the derivative of the residual itself: the exact FMT second
+// derivatives for the duration of a gradient, whatever tgpu_set_jacobian_form chose.
+struct ExactJacScope {
+  Ctx *c;
+  int saved;
+  explicit ExactJacScope(Ctx *c_) : c(c_), saved(c_->dg.jac_exact)
+  {
+    if (!saved) {
+      c->dg.jac_exact = 1;
+      tgpu::upload_geom(c->dg, c->stream);
+    }
+  }
+  ~ExactJacScope()
+  {
+    if (!saved) {
+      c->dg.jac_exact = 0;
+      tgpu::upload_geom(c->dg, c->stream);
+    }
+  }
+};
+
 int grad_vext_device(Ctx *c, const double *d_x, int kind, int icomp, double tol, int maxit, double *d_out, int *iters)
 {
+  ExactJacScope exact(c);
   need_integ(c);
   ensure_obj(c);
   fill_arith(c, d_x, c->d_obj_R, 0, TGPU_FILL_FP64);
@@ -1278,8 +1300,8 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
       if ((g.bc[d][0] == TGPU_BC_PERIODIC) != (g.bc[d][1] == TGPU_BC_PERIODIC))
         throw Error(TGPU_ERR_ARG, "periodic boundaries must be periodic on both sides");
     }
-    if (g.functional != TGPU_FMT1 && g.functional != TGPU_FMT3)
-      throw Error(TGPU_ERR_UNSUPPORTED, "only the FMT1 (Rosenfeld) and FMT3 (White-Bear) functionals are implemented");
+    if (g.functional < TGPU_FMT1 || g.functional > TGPU_FMT4)
+      throw Error(TGPU_ERR_UNSUPPORTED, "functional outside FMT1..FMT4");
     if (g.attraction && g.att_in_a22)
       throw Error(TGPU_ERR_UNSUPPORTED, "mean field summed into the density rows (ATTInA22Block) is not implemented");
     if (g.hard_surf && g.attraction)
@@ -1488,6 +1510,18 @@ int tgpu_set_precision(tgpu_handle h, int precision)
     if (precision == TGPU_FP16TC && !c->tc_ready)
       throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
     c->precision = precision;
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_jacobian_form(tgpu_handle h, int form)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (form != TGPU_JAC_REFERENCE && form != TGPU_JAC_EXACT) throw Error(TGPU_ERR_ARG, "jacobian form");
+    c->dg.jac_exact = form == TGPU_JAC_EXACT ? 1 : 0;
+    tgpu::upload_geom(c->dg, c->stream);
+    ck(cudaStreamSynchronize(c->stream), "sync");
     return TGPU_OK;
   });
 }

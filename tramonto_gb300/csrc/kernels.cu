@@ -471,110 +471,14 @@ __device__ __forceinline__ void load_n(const double *__restrict__ x, long i, dou
   }
 }
 
-// dPhi/dn (FMT1: Rosenfeld, FMT3: White-Bear), with the reference's n3 guard for FMT3.
-__device__ void fmt_dphi(const double *n, double *dphi)
+__device__ __forceinline__ void fmt_dphi(const double *n, double *dphi)
 {
-  const int nd = c_g.ndim;
-  double dot22 = 0.0, dot12 = 0.0;
-  for (int d = 0; d < nd; d++) {
-    dot22 += n[4 + nd + d] * n[4 + nd + d];
-    dot12 += n[4 + d] * n[4 + nd + d];
-  }
-  const double one_m = 1.0 - n[3];
-  const double a = 1.0 / one_m, a2 = a * a, a3 = a2 * a;
-  dphi[0] = log(a);
-  dphi[1] = n[2] * a;
-  if (c_g.functional == TGPU_FMT3) {
-    const double t = n[3];
-    if (t > 1.e-10) {
-      const double lg = log(one_m);
-      const double F = t + one_m * one_m * lg;            // n3 + (1-n3)^2 ln(1-n3)
-      const double F1 = t - 2.0 * one_m * lg;             // dF/dn3
-      const double f = F * a2 / (36.0 * kPi * t * t);     // Phi_3 = (n2^3 - 3 n2 V2.V2) f(n3)
-      const double G1 = 2.0 * (-a2 / (t * t * t) + a3 / (t * t));
-      const double f1 = (F1 * a2 / (t * t) + F * G1) / (36.0 * kPi);
-      const double g = n[2] * n[2] * n[2] - 3.0 * n[2] * dot22;
-      dphi[2] = n[1] * a + 3.0 * (n[2] * n[2] - dot22) * f;
-      dphi[3] = n[0] * a + (n[1] * n[2] - dot12) * a2 + g * f1;
-      for (int d = 0; d < nd; d++) {
-        dphi[4 + d] = -n[4 + nd + d] * a;
-        dphi[4 + nd + d] = -n[4 + d] * a - 6.0 * n[2] * n[4 + nd + d] * f;
-      }
-    } else {
-      dphi[2] = 0.0;
-      dphi[3] = 0.0;
-      for (int d = 0; d < nd; d++) {
-        dphi[4 + d] = -n[4 + nd + d] * a;
-        dphi[4 + nd + d] = 0.0;
-      }
-    }
-  } else {
-    dphi[2] = n[1] * a + (n[2] * n[2] - dot22) * a2 / (8.0 * kPi);
-    dphi[3] = n[0] * a + (n[1] * n[2] - dot12) * a2 + (n[2] * n[2] * n[2] - 3. * n[2] * dot22) * a3 / (12.0 * kPi);
-    for (int d = 0; d < nd; d++) {
-      dphi[4 + d] = -n[4 + nd + d] * a;
-      dphi[4 + nd + d] = -n[4 + d] * a - n[2] * n[4 + nd + d] * a2 / (4.0 * kPi);
-    }
-  }
+  fmt_dphi_at(n, dphi, c_g.ndim, c_g.functional);
 }
 
-// z = H(n) y with H the Hessian of Phi in n ordering.  Derived from the free
-// energy density; it reproduces the reference's per-stencil-point second
-// derivatives (d2phi_drb2_delta_rb / _theta_rb) as c(offset)^T H and H row n3.
-__device__ void fmt_hess_apply(const double *n, const double *y, double *z)
+__device__ __forceinline__ void fmt_hess_apply(const double *n, const double *y, double *z, bool transpose = false)
 {
-  const int nd = c_g.ndim;
-  double Q = 0.0, Pd = 0.0;
-  for (int d = 0; d < nd; d++) {
-    Q += n[4 + nd + d] * n[4 + nd + d];
-    Pd += n[4 + d] * n[4 + nd + d];
-  }
-  const double one_m = 1.0 - n[3];
-  const double a = 1.0 / one_m, a2 = a * a, a3 = a2 * a, a4 = a3 * a;
-  double h22, h23, h2v2, h33, h3v2n2, v2v2;  // entries that differ between functionals
-  if (c_g.functional == TGPU_FMT3) {
-    const double t = n[3];
-    if (!(t > 1.e-10)) {
-      for (int k = 0; k < 4 + 2 * nd; k++) z[k] = 0.0;
-      return;
-    }
-    const double lg = log(one_m);
-    const double F = t + one_m * one_m * lg, F1 = t - 2.0 * one_m * lg, F2 = 3.0 + 2.0 * lg;
-    const double t2 = t * t, t3 = t2 * t, t4 = t3 * t;
-    const double G = a2 / t2, G1 = 2.0 * (-a2 / t3 + a3 / t2), G2 = 6.0 * a2 / t4 - 8.0 * a3 / t3 + 6.0 * a4 / t2;
-    const double f = F * G / (36.0 * kPi);
-    const double f1 = (F1 * G + F * G1) / (36.0 * kPi);
-    const double f2 = (F2 * G + 2.0 * F1 * G1 + F * G2) / (36.0 * kPi);
-    const double g = n[2] * n[2] * n[2] - 3.0 * n[2] * Q;
-    h22 = 6.0 * n[2] * f;
-    h23 = n[1] * a2 + 3.0 * (n[2] * n[2] - Q) * f1;
-    h2v2 = -6.0 * f;                 // times V2d
-    h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + g * f2;
-    h3v2n2 = -6.0 * n[2] * f1;       // times V2d, plus -V1d a2
-    v2v2 = -6.0 * n[2] * f;
-  } else {
-    const double i4p = 1.0 / (4.0 * kPi);
-    h22 = n[2] * a2 * i4p;
-    h23 = n[1] * a2 + (n[2] * n[2] - Q) * a3 * i4p;
-    h2v2 = -a2 * i4p;
-    h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + (n[2] * n[2] * n[2] - 3.0 * n[2] * Q) * a4 * i4p;
-    h3v2n2 = -n[2] * a3 / (2.0 * kPi);
-    v2v2 = -n[2] * a2 * i4p;
-  }
-  const double h03 = a, h12 = a, h13 = n[2] * a2;
-  double s2 = 0.0, s3 = 0.0;
-  for (int d = 0; d < nd; d++) {
-    const double V1 = n[4 + d], V2 = n[4 + nd + d];
-    const double yV1 = y[4 + d], yV2 = y[4 + nd + d];
-    s2 += h2v2 * V2 * yV2;
-    s3 += -V2 * a2 * yV1 + (-V1 * a2 + h3v2n2 * V2) * yV2;
-    z[4 + d] = -V2 * a2 * y[3] - a * yV2;
-    z[4 + nd + d] = h2v2 * V2 * y[2] + (-V1 * a2 + h3v2n2 * V2) * y[3] - a * yV1 + v2v2 * yV2;
-  }
-  z[0] = h03 * y[3];
-  z[1] = h12 * y[2] + h13 * y[3];
-  z[2] = h12 * y[1] + h22 * y[2] + h23 * y[3] + s2;
-  z[3] = h03 * y[0] + h13 * y[1] + h23 * y[2] + h33 * y[3] + s3;
+  fmt_hess_apply_at(n, y, z, c_g.ndim, c_g.functional, c_g.jac_exact != 0, transpose);
 }
 
 // Transpose-convolution channels from a weighted-density-shaped vector q (n ordering):
@@ -905,7 +809,7 @@ __global__ void k_jtv_local(const double *__restrict__ x, const double *__restri
       }
     }
     load_n(x, i, n);
-    fmt_hess_apply(n, g, z);
+    fmt_hess_apply(n, g, z, true);
     // rb columns in solution-vector order: -w_rb + B^T w_dep + z
     double wrb[kMaxRb];
     for (int k = 0; k < c_g.nrb; k++) wrb[k] = w[(long)(c_g.first_rb + k) * N + i];

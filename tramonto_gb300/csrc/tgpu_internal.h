@@ -33,6 +33,7 @@ struct DevGeom {
   long N, NP, pstride[3];
   int ncomp, nrb, nunk, first_rho, first_rb, first_mf;
   int functional, attraction, single_size, hard_surf, nlists;
+  int jac_exact;                       // 1: Hessian of the energy density; 0: the reference's tables
   double esize[3];
   double rho_b[kMaxC], betamu_hs_ex[kMaxC], betamu_att[kMaxC];
   double inv_rad[kMaxC], inv_4pir[kMaxC], inv_4pirsq[kMaxC], fac[kMaxC];
@@ -51,30 +52,178 @@ struct ObjConst {
   double phi_b;
 };
 
-// FMT free-energy density Phi(n), n in the order n0 n1 n2 n3 V1[d] V2[d]:
-// Rosenfeld (FMT1_energy_density src/dft_physics_FMT1.c:39-57) or White-Bear
-// (FMT3_energy_density src/dft_physics_FMT3.c:39-58).  For n3 <= 1e-10 the
-// White-Bear third term takes its n3 -> 0 limit, the Rosenfeld form (the
-// reference's expression is 0/0 at n3 = 0).
+// The four hard-sphere functionals (Type_func) share Phi_1 = -n0 ln(1-n3) and
+// Phi_2 = (n1 n2 - V1.V2)/(1-n3); the third term is Phi_3 = g(n2, V2) f(n3) with
+//   g = n2^3 - 3 n2 V2.V2                         FMT1, FMT3 (Rosenfeld's vector form)
+//   g = alpha^3, alpha = n2 - V2.V2/n2            FMT2, FMT4 (zero-dimensional crossover)
+//   f = 1 / (24 pi (1-n3)^2)                      FMT1, FMT2
+//   f = (n3 + (1-n3)^2 ln(1-n3)) / (36 pi n3^2 (1-n3)^2)   FMT3, FMT4 (White-Bear)
+// (FMT{1,2,3,4}_energy_density, src/dft_physics_FMT{1,2,3,4}.c).  The White-Bear
+// functionals are cut where n3 <= 1e-10: there the reference sets dPhi/dn2,
+// dPhi/dn3, dPhi/dV2 and all second derivatives to zero.
+inline __host__ __device__ bool fmt_alpha_form(int functional) { return functional == TGPU_FMT2 || functional == TGPU_FMT4; }
+inline __host__ __device__ bool fmt_white_bear(int functional) { return functional == TGPU_FMT3 || functional == TGPU_FMT4; }
+
+// g and its derivatives: gv and g2v multiply V2_d; the V2-V2 block is
+// gvv delta_de + gvv_out V2_d V2_e.
+struct FmtG { double g, g2, gv, g22, g2v, gvv, gvv_out; };
+// f and its first two n3 derivatives
+struct FmtF { double f, f1, f2; };
+
+// g at (n2, Q = V2.V2).  The alpha form takes alpha = n2, gamma = V2/n2 = 0 where
+// n2 <= 1e-15, as FMT2_1stderiv does (src/dft_physics_FMT2.c:80-91).
+inline __host__ __device__ FmtG fmt_g(double n2, double Q, int functional)
+{
+  FmtG r;
+  if (!fmt_alpha_form(functional)) {
+    r.g = n2 * n2 * n2 - 3.0 * n2 * Q;
+    r.g2 = 3.0 * n2 * n2 - 3.0 * Q;
+    r.gv = -6.0 * n2;
+    r.g22 = 6.0 * n2;
+    r.g2v = -6.0;
+    r.gvv = -6.0 * n2;
+    r.gvv_out = 0.0;
+  } else if (n2 > 1.e-15) {
+    const double al = n2 - Q / n2, be = 1.0 + Q / (n2 * n2);
+    r.g = al * al * al;
+    r.g2 = 3.0 * al * al * be;
+    r.gv = -6.0 * al * al / n2;
+    r.g22 = 6.0 * al * be * be - 6.0 * al * al * Q / (n2 * n2 * n2);
+    r.g2v = -12.0 * al * be / n2 + 6.0 * al * al / (n2 * n2);
+    r.gvv = -6.0 * al * al / n2;
+    r.gvv_out = 24.0 * al / (n2 * n2);
+  } else {
+    r.g = n2 * n2 * n2;
+    r.g2 = 3.0 * n2 * n2;
+    r.gv = 0.0;
+    r.g22 = 6.0 * n2;
+    r.g2v = 0.0;
+    r.gvv = -6.0 * n2;
+    r.gvv_out = 0.0;
+  }
+  return r;
+}
+
+// f at n3 (White-Bear: only called where n3 > 1e-10)
+inline __host__ __device__ FmtF fmt_f(double n3, int functional)
+{
+  const double pi = 3.141592653589793238462643383279502884197;
+  const double one = 1.0 - n3, a = 1.0 / one, a2 = a * a, a3 = a2 * a, a4 = a3 * a;
+  FmtF r;
+  if (!fmt_white_bear(functional)) {
+    r.f = a2 / (24.0 * pi);
+    r.f1 = a3 / (12.0 * pi);
+    r.f2 = a4 / (4.0 * pi);
+  } else {
+    const double t = n3, t2 = t * t, t3 = t2 * t, t4 = t3 * t;
+    const double lg = log(one);
+    const double F = t + one * one * lg, F1 = t - 2.0 * one * lg, F2 = 3.0 + 2.0 * lg;
+    const double G = a2 / t2, G1 = 2.0 * (-a2 / t3 + a3 / t2), G2 = 6.0 * a2 / t4 - 8.0 * a3 / t3 + 6.0 * a4 / t2;
+    r.f = F * G / (36.0 * pi);
+    r.f1 = (F1 * G + F * G1) / (36.0 * pi);
+    r.f2 = (F2 * G + 2.0 * F1 * G1 + F * G2) / (36.0 * pi);
+  }
+  return r;
+}
+
+// FMT free-energy density Phi(n), n in the order n0 n1 n2 n3 V1[d] V2[d]; zero
+// unless n3 < 1, n2 > 0 and n3 > 1e-10 (phispt_switch, src/dft_switch_FMT.c:41-65).
 __host__ __device__ inline double fmt_phi(const double *n, int ndim, int functional)
 {
+  if (!(n[3] < 1.0 && n[2] > 0.0 && n[3] > 1.e-10)) return 0.0;
   double dot12 = 0.0, dot22 = 0.0;
   for (int d = 0; d < ndim; d++) {
     dot12 += n[4 + d] * n[4 + ndim + d];
     dot22 += n[4 + ndim + d] * n[4 + ndim + d];
   }
   const double one = 1.0 - n[3];
-  const double l = log(one);
-  const double p1 = -n[0] * l;
-  const double p2 = (n[1] * n[2] - dot12) / one;
-  const double c3 = n[2] * n[2] * n[2] - 3.0 * n[2] * dot22;
-  const double pi = 3.141592653589793238462643383279502884197;
-  double p3;
-  if (functional == TGPU_FMT3 && n[3] > 1.e-10)
-    p3 = c3 * (n[3] + one * one * l) / (36.0 * pi * n[3] * n[3] * one * one);
-  else
-    p3 = c3 / (24.0 * pi * one * one);
-  return p1 + p2 + p3;
+  return -n[0] * log(one) + (n[1] * n[2] - dot12) / one + fmt_g(n[2], dot22, functional).g * fmt_f(n[3], functional).f;
+}
+
+// dPhi/dn for the four functionals (FMT{1,2,3,4}_1stderiv, src/dft_physics_FMT{1,2,3,4}.c),
+// Phi_3 = g f as in tgpu_internal.h, with the White-Bear cut where n3 <= 1e-10.
+__host__ __device__ inline void fmt_dphi_at(const double *n, double *dphi, int nd, int functional)
+{
+  double dot22 = 0.0, dot12 = 0.0;
+  for (int d = 0; d < nd; d++) {
+    dot22 += n[4 + nd + d] * n[4 + nd + d];
+    dot12 += n[4 + d] * n[4 + nd + d];
+  }
+  const double a = 1.0 / (1.0 - n[3]), a2 = a * a;
+  dphi[0] = log(a);
+  dphi[1] = n[2] * a;
+  for (int d = 0; d < nd; d++) dphi[4 + d] = -n[4 + nd + d] * a;
+  if (fmt_white_bear(functional) && !(n[3] > 1.e-10)) {
+    dphi[2] = 0.0;
+    dphi[3] = 0.0;
+    for (int d = 0; d < nd; d++) dphi[4 + nd + d] = 0.0;
+    return;
+  }
+  const FmtG g = fmt_g(n[2], dot22, functional);
+  const FmtF f = fmt_f(n[3], functional);
+  dphi[2] = n[1] * a + g.g2 * f.f;
+  dphi[3] = n[0] * a + (n[1] * n[2] - dot12) * a2 + g.g * f.f1;
+  for (int d = 0; d < nd; d++) dphi[4 + nd + d] = -n[4 + d] * a + g.gv * f.f * n[4 + nd + d];
+}
+
+// z = M y for the per-node matrix M of FMT second derivatives (n ordering); with
+// transpose, z = M^T y.  With exact, M is the Hessian of Phi (symmetric).
+// Otherwise M reproduces the reference's per-stencil-point tables
+// d2phi_drb2_delta_rb / _theta_rb as c(offset)^T M and M row n3: the Hessian
+// except for FMT2's V2-V2 block (gamma_d gamma_e replaced by |gamma|^2 delta_de,
+// src/dft_physics_FMT2.c:182-183) and FMT4's n2-row V2 entries (coefficient
+// -6 (fac^2 - 4 V2.V2 fac / n2) f for the Hessian's -6 fac (1 + 3 V2.V2/n2^2) f,
+// src/dft_physics_FMT4.c:179, fac = 1 - V2.V2/n2^2).
+__host__ __device__ inline void fmt_hess_apply_at(const double *n, const double *y, double *z, int nd, int fn,
+                                                  bool exact, bool transpose)
+{
+  if (fmt_white_bear(fn) && !(n[3] > 1.e-10)) {
+    for (int k = 0; k < 4 + 2 * nd; k++) z[k] = 0.0;
+    return;
+  }
+  double Q = 0.0, Pd = 0.0, Vy = 0.0;
+  for (int d = 0; d < nd; d++) {
+    Q += n[4 + nd + d] * n[4 + nd + d];
+    Pd += n[4 + d] * n[4 + nd + d];
+    Vy += n[4 + nd + d] * y[4 + nd + d];
+  }
+  const double a = 1.0 / (1.0 - n[3]), a2 = a * a, a3 = a2 * a;
+  const FmtG g = fmt_g(n[2], Q, fn);
+  const FmtF f = fmt_f(n[3], fn);
+  double gvv = g.gvv, gvv_out = g.gvv_out;
+  double g2v_row = g.g2v, g2v_col = g.g2v;   // M[n2][V2d] / V2d and M[V2d][n2] / V2d
+  if (!exact && fmt_alpha_form(fn) && n[2] > 1.e-15) {
+    if (fn == TGPU_FMT2) {
+      const double al = n[2] - Q / n[2];
+      gvv = -6.0 * al * al / n[2] + 24.0 * al * Q / (n[2] * n[2]);
+      gvv_out = 0.0;
+    } else {
+      const double fac = 1.0 - Q / (n[2] * n[2]);
+      g2v_row = -6.0 * (fac * fac - 4.0 * Q * fac / n[2]);
+    }
+  }
+  if (transpose) {
+    const double t = g2v_row;
+    g2v_row = g2v_col;
+    g2v_col = t;
+  }
+  const double h22 = g.g22 * f.f, h23 = n[1] * a2 + g.g2 * f.f1;
+  const double h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + g.g * f.f2;
+  const double h13 = n[2] * a2;
+  double s2 = 0.0, s3 = 0.0;
+  for (int d = 0; d < nd; d++) {
+    const double V1 = n[4 + d], V2 = n[4 + nd + d];
+    const double yV1 = y[4 + d], yV2 = y[4 + nd + d];
+    const double h3v2 = -V1 * a2 + g.gv * f.f1 * V2;    // M[n3][V2d] = M[V2d][n3]
+    s2 += g2v_row * f.f * V2 * yV2;
+    s3 += -V2 * a2 * yV1 + h3v2 * yV2;
+    z[4 + d] = -V2 * a2 * y[3] - a * yV2;
+    z[4 + nd + d] = g2v_col * f.f * V2 * y[2] + h3v2 * y[3] - a * yV1 + f.f * (gvv * yV2 + gvv_out * V2 * Vy);
+  }
+  z[0] = a * y[3];
+  z[1] = a * y[2] + h13 * y[3];
+  z[2] = a * y[1] + h22 * y[2] + h23 * y[3] + s2;
+  z[3] = a * y[0] + h13 * y[1] + h23 * y[2] + h33 * y[3] + s3;
 }
 
 // Tensor-core form of a large 3-D single-channel stencil sum (wca_tc.cu): tiles of

@@ -30,6 +30,7 @@ from .problem import Problem
 TGPU_OK = 0
 FP64, FP32, BF16X3, FP16TC = 0, 1, 2, 3
 FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF, FILL_MIXED_FF = 0, 1, 2, 3, 4, 5
+JAC_REFERENCE, JAC_EXACT = 0, 1
 STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
           -5: "no convergence", -6: "non-finite values", -7: "domain error"}
 
@@ -83,6 +84,7 @@ def load(build_if_missing: bool = False):
         "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
+        "tgpu_set_jacobian_form": [vp, C.c_int],
         "tgpu_set_fill_arithmetic": [vp, C.c_int, C.c_double, C.c_double],
         "tgpu_sizes": [vp, C.POINTER(C.c_long), ip, ip],
         "tgpu_fill": [vp, vp, vp, C.c_int], "tgpu_fill_device": [vp, vp, vp, C.c_int],
@@ -269,6 +271,11 @@ class Solver:
 
     def set_precision(self, precision: int):
         _check(self.lib.tgpu_set_precision(self.h, int(precision)), self.lib)
+
+    def set_jacobian_form(self, form: int):
+        """FMT second derivatives in J, J^T and Schur products: JAC_REFERENCE (the reference's tables,
+        default) or JAC_EXACT (the Hessian of the energy density); they differ for FMT2 and FMT4 only."""
+        _check(self.lib.tgpu_set_jacobian_form(self.h, int(form)), self.lib)
 
     def set_fill_arithmetic(self, arith: int, tau: float = 0.0, switch_norm: float = 0.0):
         """Residual arithmetic: FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF or FILL_MIXED_FF

@@ -21,7 +21,7 @@ import numpy as np
 
 # reference codes (src/dft_globals_const.h)
 BC_IN_WALL, BC_IN_BULK, BC_PERIODIC, BC_REFLECT = -1, 0, 1, 2
-FMT1, FMT3 = 0, 2
+FMT1, FMT2, FMT3, FMT4 = 0, 1, 2, 3
 DELTA, THETA, UATT = 0, 1, 2
 
 

@@ -23,7 +23,7 @@ import math
 import numpy as np
 
 from . import native
-from .problem import BC_IN_BULK, BC_IN_WALL, BC_PERIODIC, DELTA, FMT1, FMT3, THETA, UATT, Problem
+from .problem import BC_IN_BULK, BC_IN_WALL, BC_PERIODIC, DELTA, FMT1, FMT3, FMT4, THETA, UATT, Problem
 
 PI = math.pi
 
@@ -58,12 +58,13 @@ def lj_rmin(sigma, eps, rcut, esize0):
 
 
 def fmt_dphi_bulk(functional, n):
-    """dPhi/dn0..dn3 at a bulk state (vector terms vanish), FMT1 or FMT3."""
+    """dPhi/dn0..dn3 at a bulk state (vector terms vanish): FMT2 equals FMT1 there and FMT4 equals
+    FMT3 (FMT1stDerivBulk_switch, src/dft_switch_FMT.c:98-120)."""
     n0, n1, n2, n3 = n
     a = 1.0 / (1.0 - n3)
     d0 = math.log(a)
     d1 = n2 * a
-    if functional == FMT3:
+    if functional in (FMT3, FMT4):
         if n3 > 1e-10:
             lg = math.log(1.0 - n3)
             F = n3 + (1 - n3) ** 2 * lg
