@@ -227,7 +227,7 @@ int tgpu_newton_solve_device(tgpu_handle h, double *d_x, double resid_tol, int m
                              int lin_max_iter, double update_floor, int *iters, double *final_resid,
                              int *lin_iters_total);
 
-/* ---- set-up helpers (host only, no GPU) ------------------------------------
+/* ---- set-up helpers ----------------------------------------------------------
  * Stencil tables built as calc_stencils (src/dft_stencil.c:40-287) builds
  * Stencil[type][0][index] for the delta shell (DELTA_FN_R), the theta ball
  * (THETA_FN_R) and the WCA attraction (THETA_PAIRPOT_RCUT, Type_attr 0 with the
@@ -238,6 +238,44 @@ int tgpu_newton_solve_device(tgpu_handle h, double *d_x, double resid_tol, int m
 int tgpu_make_stencil(int type, int ndim, const double *esize, double hs_diam, double sigma, double eps_over_kT,
                       double rcut, double rmin, int capacity, short *offsets, double *weights, double *hw,
                       double *volume);
+/* The same tables built on the GPU (current device): one thread per element for the quadrature, one per
+ * node for the corner sums, first-touch ordering by a radix sort and the renormalisation sum in table order.
+ * The tables are bit-identical to tgpu_make_stencil's (both builders perform the same IEEE operations in
+ * the same order).  Same arguments and return value; TGPU_ERR_CUDA without a usable device. */
+int tgpu_make_stencil_device(int type, int ndim, const double *esize, double hs_diam, double sigma,
+                             double eps_over_kT, double rcut, double rmin, int capacity, short *offsets,
+                             double *weights, double *hw, double *volume);
+/* External field of planar walls, generated on the GPU (the surfaces and wall-fluid potentials of
+ * setup_external_field_n, src/dft_vext.c:38, for planar walls: Vext_LJ9_3_CS src/dft_vext_1D.c:42-56,
+ * the 12-3 form, rough surfaces as in surface roughness patches, src/dft_surfacesAdjust_roughness.c:38-62).
+ * Each wall faces +x (side 0: surface at x = position + h, d = x - position - h) or -x (side 1: surface at
+ * x = position - h, d = position - h - x), x = ix esize[0]; h is the roughness height of the patch that
+ * holds the node: heights[py][pz] (row-major) over patches[0] x patches[1] equal patches of the periodic
+ * y (and z) extent, h = 0 without heights.  Per wall, with s = sigma/d:
+ *   TGPU_WALL_LJ93_CS: eps (2 pi/3) sigma^3 [(2/15)(s^9 - (sigma/cut)^9) - (s^3 - (sigma/cut)^3)], 0 beyond cut
+ *   TGPU_WALL_LJ123:   eps (s^12 - s^3)
+ * eps is in kT and carries every prefactor; in 2-D and 3-D it is modulated along y as
+ * eps (1 + pattern cos(2 pi y / L_y)), y = iy esize[1], L_y = nx[1] esize[1].  The field is the sum over
+ * the walls; nodes with d <= 0 for some wall or a sum >= vext_max hold vext_max (zero-density rows).
+ * Output [N] (node = ix + nx0 (iy + nx1 iz)).  No reference counterpart as a single call. */
+enum { TGPU_WALL_LJ93_CS = 0, TGPU_WALL_LJ123 = 1 };
+typedef struct {
+  int form, side;
+  double position, eps, sigma, cut, pattern;
+  int patches[2];
+  const double *heights;     /* host array [patches[0]][patches[1]] or NULL */
+} tgpu_wall;
+typedef struct {
+  int ndim, nx[3];
+  double esize[3];
+  int nwalls;                /* 1 or 2 */
+  tgpu_wall wall[2];
+  double vext_max;
+} tgpu_wall_field;
+/* the field into device memory d_out [N] (current device, default stream, synchronised) */
+int tgpu_wall_field_device(const tgpu_wall_field *f, double *d_out);
+/* the same into host memory out [N] */
+int tgpu_wall_field_host(const tgpu_wall_field *f, double *out);
 /* r of the minimum of the cut-and-shifted LJ 12-6 potential, located by the
  * search of pairPot_find_rmin (src/dft_pairPot.c:98-152) */
 double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0);

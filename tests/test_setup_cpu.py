@@ -5,7 +5,7 @@ import pytest
 from goldens import load
 from tramonto_gb300 import setup
 
-CASES = ["hs1d_wall", "hs1d_reflect", "lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "hs1d_c1"]
+CASES = ["hs1d_wall", "hs1d_reflect", "lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "hs1d_c1", "mix1d_fmt4", "rough3d_fmt2"]
 
 
 @pytest.mark.parametrize("case", CASES)

@@ -20,6 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr",
            "-diag-suppress", "550,177"]
+# stencils.cu: the host and device stencil builders must perform the same IEEE operations
+FILE_FLAGS = {"stencils.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:
@@ -41,7 +43,8 @@ def _compile(src: str, extra) -> str:
         return obj
     tmp = obj + f".tmp{os.getpid()}"
     if ext == ".cu":
-        cmd = [nvcc(), *ARCH, *NVFLAGS, *extra, "-I", INCLUDE, "-c", src, "-o", tmp]
+        cmd = [nvcc(), *ARCH, *NVFLAGS, *FILE_FLAGS.get(os.path.basename(src), []), *extra, "-I", INCLUDE, "-c", src,
+               "-o", tmp]
     else:  # host-only C++ (set-up code)
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-I", INCLUDE, "-c", src, "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)

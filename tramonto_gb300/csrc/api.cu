@@ -254,12 +254,15 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
   if (!f32 && c->ff_on && nin == 1 && nout == 1) {
     const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
     if (ln.nplanes > 0 && ln.ff_ok) {
-      const long total = (long)c->nch_max * NP - (long)ch0 * NP;
-      tgpu::launch_conv_slab_ff(c->d_pad + (long)ch0 * NP, total, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w,
-                                ln.d_w_lo, outs[0], ln.pitch, ln.ncols, ln.max_rows, ln.max_lines, ln.max_w,
-                                c->dg.nx[0], c->dg.nx[1], c->dg.nx[2], c->stream);
+      // high and low FP32 parts of the channel in the (idle) FP32 padded buffer, which holds at least two
+      // channels; loads past a part's end read zeros
+      float *hi = c->d_pad32, *lo = c->d_pad32 + NP;
+      tgpu::launch_split_hilo(c->d_pad + (long)ch0 * NP, NP, hi, lo, c->stream);
+      tgpu::launch_conv_slab_ff(hi, lo, NP, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w, ln.d_w_lo, outs[0], ln.pitch,
+                                ln.ncols, ln.max_rows, ln.max_lines, ln.max_w, c->dg.nx[0], c->dg.nx[1], c->dg.nx[2],
+                                c->stream);
       c->stats.conv_launches++;
-      c->stats.kernel_launches++;
+      c->stats.kernel_launches += 2;
       return;
     }
   }

@@ -316,17 +316,24 @@ void launch_conv_slab(const float *in, long in_total, const int4 *planes, int np
 // ---------------------------------------------------------------------------
 // FP64-accurate single-channel 3-D stencil sums in float-float arithmetic.
 //
-// The same slab / x-line traversal as k_conv_slab, on an FP64 padded field:
-// every value is split into FP32 high and low parts (f = f_hi + f_lo, exact to
-// ~2^-48 relative) and every weight likewise.  Each term w f is formed as
+// The same slab / x-line traversal as k_conv_slab, on the padded field split
+// into FP32 high and low parts (f = f_hi + f_lo, exact to ~2^-48 relative, by
+// k_split_hilo) and weights split likewise.  Each term w f is formed as
 // p = fl(w_hi f_hi) plus its exact rounding error e = fma(w_hi, f_hi, -p) and
 // the cross terms w_hi f_lo + w_lo f_hi; p is added to the running sum s by an
 // error-free two-sum and the errors go to a compensation c, so s + c carries
-// about 48 bits (Ogita-Rump-Oishi compensated summation) over one x-line; the
-// line sums go into an FP64 total.  Twelve FP32 operations per term against
-// one FP64 FMA: on GB300, whose FP64 pipe runs at 1/64 of the FP32 rate, that
-// is ~5x fewer issue slots.  Intrinsics (__fmul_rn,
-// __fadd_rn) keep the compiler from fusing the products into the sums.
+// about 48 bits (Ogita-Rump-Oishi compensated summation) over one x-line.  The
+// compensation is reset per line (a few dozen terms: its own rounding stays
+// at ~1e-14 of the line); groups of kFFGroup line sums are added in
+// double-word arithmetic (the accurate double-word addition of Joldes, Muller
+// and Popescu, relative error <= 3 u^2 per addition) and each group goes into
+// an FP64 total.  Twelve FP32 operations per term against one FP64 FMA: on
+// GB300, whose FP64 pipe runs at 1/64 of the FP32 rate, that is ~5x fewer issue
+// slots, and the grouping keeps the FP64 pipe to one addition per kFFGroup
+// lines.  Intrinsics (__fmul_rn, __fadd_rn) keep the compiler from fusing
+// products into sums.
+constexpr int kFFGroup = 8;
+
 __device__ __forceinline__ void ff_term(float wh, float wl, float fh, float fl, float &s, float &c)
 {
   const float p = __fmul_rn(wh, fh);
@@ -340,7 +347,35 @@ __device__ __forceinline__ void ff_term(float wh, float wl, float fh, float fl, 
   c = __fmaf_rn(wl, fh, c);
 }
 
-__global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__restrict__ in, long in_total,
+// (a, b) <- (a, b) + (c, d) in double-word arithmetic (accurate version: two two-sums, two fast two-sums)
+__device__ __forceinline__ void dw_add(float &a, float &b, float c, float d)
+{
+  const float sh = __fadd_rn(a, c);
+  const float z1 = __fsub_rn(sh, a);
+  const float sl = __fadd_rn(__fsub_rn(a, __fsub_rn(sh, z1)), __fsub_rn(c, z1));
+  const float th = __fadd_rn(b, d);
+  const float z2 = __fsub_rn(th, b);
+  const float tl = __fadd_rn(__fsub_rn(b, __fsub_rn(th, z2)), __fsub_rn(d, z2));
+  const float cc = __fadd_rn(sl, th);
+  const float vh = __fadd_rn(sh, cc);
+  const float vl = __fsub_rn(cc, __fsub_rn(vh, sh));
+  const float w = __fadd_rn(tl, vl);
+  a = __fadd_rn(vh, w);
+  b = __fsub_rn(w, __fsub_rn(a, vh));
+}
+
+__global__ void k_split_hilo(const double *__restrict__ in, long n, float *__restrict__ hi, float *__restrict__ lo)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = in[i];
+    const float h = __double2float_rn(v);
+    hi[i] = h;
+    lo[i] = __double2float_rn(v - (double)h);
+  }
+}
+
+__global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const float *__restrict__ in_hi,
+                                                             const float *__restrict__ in_lo, long in_total,
                                                              const int4 *__restrict__ planes, int nplanes,
                                                              const int4 *__restrict__ lines,
                                                              const float *__restrict__ lw,
@@ -357,8 +392,10 @@ __global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__r
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int x0 = blockIdx.x * kSlabTX, y0 = blockIdx.y * kSlabTY, z = blockIdx.z;
   double total[8];
+  float gh[8], gl[8];   // the current group of line sums, double-word
 #pragma unroll
-  for (int o = 0; o < 8; o++) total[o] = 0.0;
+  for (int o = 0; o < 8; o++) { total[o] = 0.0; gh[o] = 0.f; gl[o] = 0.f; }
+  int ng = 0;
   for (int pi = 0; pi < nplanes; pi++) {
     const int4 pd = planes[2 * pi];
     const int4 pg = planes[2 * pi + 1];
@@ -374,11 +411,13 @@ __global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__r
       const int r = e / ncols, cidx = e - r * ncols;
       const int gy = y0 + pg.y + r + c_g.h[1];
       const long gi = gz + (long)gy * c_g.pstride[1] + x0 + cidx;
-      double v = 0.0;
-      if (gy < c_g.P[1] && gi < in_total) v = __ldg(in + gi);
-      const float hi = __double2float_rn(v);
-      s_hi[r * pitch + slab_phys(cidx)] = hi;
-      s_lo[r * pitch + slab_phys(cidx)] = __double2float_rn(v - (double)hi);
+      float vh = 0.f, vl = 0.f;
+      if (gy < c_g.P[1] && gi < in_total) {
+        vh = __ldg(in_hi + gi);
+        vl = __ldg(in_lo + gi);
+      }
+      s_hi[r * pitch + slab_phys(cidx)] = vh;
+      s_lo[r * pitch + slab_phys(cidx)] = vl;
     }
     __syncthreads();
     for (int li = 0; li < pd.y; li++) {
@@ -388,8 +427,6 @@ __global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__r
       const float *w = s_w + (ln.w - pd.z);
       const float *wlo = s_wl + (ln.w - pd.z);
       const int c0 = 8 * tx + ln.y;
-      // one line (<= a few dozen terms) in float-float, then added to an FP64 total: the compensation
-      // stays short, so its own rounding does not build up over the 1e5 terms of a large stencil
       float sum[8], comp[8];
 #pragma unroll
       for (int o = 0; o < 8; o++) { sum[o] = 0.f; comp[o] = 0.f; }
@@ -418,7 +455,16 @@ __global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__r
         }
       }
 #pragma unroll
-      for (int o = 0; o < 8; o++) total[o] += (double)sum[o] + (double)comp[o];
+      for (int o = 0; o < 8; o++) dw_add(gh[o], gl[o], sum[o], comp[o]);
+      if (++ng == kFFGroup) {
+#pragma unroll
+        for (int o = 0; o < 8; o++) {
+          total[o] += (double)gh[o] + (double)gl[o];
+          gh[o] = 0.f;
+          gl[o] = 0.f;
+        }
+        ng = 0;
+      }
     }
   }
   const int y = y0 + ty;
@@ -427,7 +473,7 @@ __global__ void __launch_bounds__(kSlabThreads) k_conv_slab_ff(const double *__r
 #pragma unroll
     for (int o = 0; o < 8; o++) {
       const int x = x0 + 8 * tx + o;
-      if (x < c_g.nx[0]) out[i0 + x] += total[o];
+      if (x < c_g.nx[0]) out[i0 + x] += total[o] + ((double)gh[o] + (double)gl[o]);
     }
   }
 }
@@ -437,9 +483,14 @@ size_t conv_slab_ff_smem(int pitch, int max_rows, int max_lines, int max_w)
   return sizeof(float) * (2 * (size_t)max_rows * pitch + 2 * (size_t)max_w) + sizeof(int4) * max_lines;
 }
 
-void launch_conv_slab_ff(const double *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
-                         const float *lw, const float *lw_lo, double *out, int pitch, int ncols, int max_rows,
-                         int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s)
+void launch_split_hilo(const double *in, long n, float *hi, float *lo, cudaStream_t s)
+{
+  k_split_hilo<<<1184, kThreads, 0, s>>>(in, n, hi, lo);
+}
+
+void launch_conv_slab_ff(const float *in_hi, const float *in_lo, long in_total, const int4 *planes, int nplanes,
+                         const int4 *lines, const float *lw, const float *lw_lo, double *out, int pitch, int ncols,
+                         int max_rows, int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s)
 {
   const size_t smem = conv_slab_ff_smem(pitch, max_rows, max_lines, max_w);
   static size_t configured = 0;
@@ -448,8 +499,8 @@ void launch_conv_slab_ff(const double *in, long in_total, const int4 *planes, in
     configured = smem;
   }
   dim3 grid((nx + kSlabTX - 1) / kSlabTX, (ny + kSlabTY - 1) / kSlabTY, nz);
-  k_conv_slab_ff<<<grid, kSlabThreads, smem, s>>>(in, in_total, planes, nplanes, lines, lw, lw_lo, out, pitch, ncols,
-                                                   max_rows, max_lines, max_w);
+  k_conv_slab_ff<<<grid, kSlabThreads, smem, s>>>(in_hi, in_lo, in_total, planes, nplanes, lines, lw, lw_lo, out,
+                                                   pitch, ncols, max_rows, max_lines, max_w);
 }
 
 // ---------------------------------------------------------------------------

@@ -357,9 +357,10 @@ void launch_conv_slab(const float *in, long in_total, const int4 *planes, int np
                       const float *lw, double *out, int pitch, int ncols, int max_rows, int max_lines, int max_w,
                       int nx, int ny, int nz, cudaStream_t s);
 size_t conv_slab_ff_smem(int pitch, int max_rows, int max_lines, int max_w);
-void launch_conv_slab_ff(const double *in, long in_total, const int4 *planes, int nplanes, const int4 *lines,
-                         const float *lw, const float *lw_lo, double *out, int pitch, int ncols, int max_rows,
-                         int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s);
+void launch_split_hilo(const double *in, long n, float *hi, float *lo, cudaStream_t s);
+void launch_conv_slab_ff(const float *in_hi, const float *in_lo, long in_total, const int4 *planes, int nplanes,
+                         const int4 *lines, const float *lw, const float *lw_lo, double *out, int pitch, int ncols,
+                         int max_rows, int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s);
 constexpr int kSlabTileX = 128, kSlabTileY = 16;
 void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,

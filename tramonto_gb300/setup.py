@@ -3,7 +3,7 @@
 Restates the set-up the reference does once per run before its Newton loop:
 
 * stencils (calc_stencils, src/dft_stencil.c:40-287) through the library's
-  ``tgpu_make_stencil`` (tramonto_gb300/csrc/stencils.cpp);
+  ``tgpu_make_stencil`` / ``tgpu_make_stencil_device`` (tramonto_gb300/csrc/stencils.cu);
 * bulk FMT constants: rhobar_icomp / dphi_drb_bulk / chempot_FMT_hs
   (src/dft_thermo_hs.c:58-70, 138-153, 292-334) and the 1/R factors
   calc_InvR_params (:58-70);
@@ -30,25 +30,46 @@ PI = math.pi
 
 def _lib():
     lib = native.load()
-    lib.tgpu_make_stencil.restype = C.c_int
-    lib.tgpu_make_stencil.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double,
-                                      C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    for fn in (lib.tgpu_make_stencil, lib.tgpu_make_stencil_device):
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.tgpu_wall_field_host.restype = C.c_int
+    lib.tgpu_wall_field_host.argtypes = [C.c_void_p, C.c_void_p]
     lib.tgpu_lj_rmin.restype = C.c_double
     lib.tgpu_lj_rmin.argtypes = [C.c_double] * 4
     return lib
 
 
-def make_stencil(stype, ndim, esize, hs_diam=0.0, sigma=1.0, eps=1.0, rcut=0.0, rmin=0.0, with_hw=False):
+def _gpu_visible():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except ImportError:
+        return False
+
+
+def make_stencil(stype, ndim, esize, hs_diam=0.0, sigma=1.0, eps=1.0, rcut=0.0, rmin=0.0, with_hw=False,
+                 device=None):
+    """Stencil table (offsets [L][ndim], weights [L], per-corner weights [L][2^ndim] or None), built on the
+    GPU (tgpu_make_stencil_device) or on the host (tgpu_make_stencil); the two builders give bit-identical
+    tables.  device=None picks the GPU, when one is visible, for the 3-D tables whose quadrature outweighs
+    the GPU's fixed cost: the attraction stencil and shells/balls wider than 5.5 nodes."""
     lib = _lib()
+    if device is None:
+        reach = (rcut if stype == UATT else 0.5 * hs_diam) / min(esize[:ndim])
+        device = ndim == 3 and (stype == UATT or reach > 5.5) and _gpu_visible()
+    fn = lib.tgpu_make_stencil_device if device else lib.tgpu_make_stencil
     es = (C.c_double * 3)(*(list(esize) + [0.0] * (3 - len(esize))))
-    L = lib.tgpu_make_stencil(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, 0, None, None, None, None)
+    # one call builds the table; the second (with arrays) rebuilds it, so size the arrays generously
+    L = fn(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, 0, None, None, None, None)
     if L < 0:
-        raise RuntimeError(f"tgpu_make_stencil failed ({L})")
+        raise RuntimeError(f"tgpu_make_stencil{'_device' if device else ''} failed ({L})")
     off = np.zeros((L, ndim), np.int16)
     w = np.zeros(L)
     hw = np.zeros((L, 1 << ndim)) if with_hw else None
-    L2 = lib.tgpu_make_stencil(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, L, off.ctypes.data, w.ctypes.data,
-                               hw.ctypes.data if with_hw else None, None)
+    L2 = fn(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, L, off.ctypes.data, w.ctypes.data,
+            hw.ctypes.data if with_hw else None, None)
     assert L2 == L
     return off, w, hw
 
@@ -169,17 +190,68 @@ def integration_weights(ndim, nx, esize, bc):
 LJ123_PREF = 1.0 / (0.75 * 4.0 ** (-1.0 / 3.0))
 
 
+WALL_LJ93_CS, WALL_LJ123 = 0, 1
+
+
+class _Wall(C.Structure):
+    _fields_ = [("form", C.c_int), ("side", C.c_int), ("position", C.c_double), ("eps", C.c_double),
+                ("sigma", C.c_double), ("cut", C.c_double), ("pattern", C.c_double), ("patches", C.c_int * 2),
+                ("heights", C.c_void_p)]
+
+
+class _WallField(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("nx", C.c_int * 3), ("esize", C.c_double * 3), ("nwalls", C.c_int),
+                ("wall", _Wall * 2), ("vext_max", C.c_double)]
+
+
+def wall_field_device(ndim, nx, esize, walls, vext_max):
+    """The field of one or two planar walls computed on the GPU (tgpu_wall_field_host); walls are dicts
+    with form, side, position, eps, sigma, cut, pattern and optional heights [py][pz]."""
+    lib = _lib()
+    f = _WallField()
+    f.ndim = ndim
+    for d in range(3):
+        f.nx[d] = int(nx[d]) if d < ndim else 1
+        f.esize[d] = float(esize[d]) if d < ndim else 0.0
+    f.nwalls = len(walls)
+    f.vext_max = float(vext_max)
+    keep = []
+    for k, w in enumerate(walls):
+        o = f.wall[k]
+        o.form, o.side = int(w["form"]), int(w.get("side", 0))
+        o.position, o.eps, o.sigma = float(w["position"]), float(w["eps"]), float(w["sigma"])
+        o.cut, o.pattern = float(w.get("cut", 0.0)), float(w.get("pattern", 0.0))
+        h = w.get("heights")
+        if h is not None:
+            h = np.ascontiguousarray(h, np.float64)
+            keep.append(h)
+            o.patches[0], o.patches[1] = h.shape
+            o.heights = h.ctypes.data
+    out = np.empty(int(np.prod([nx[d] for d in range(ndim)])))
+    st = lib.tgpu_wall_field_host(C.byref(f), out.ctypes.data_as(C.c_void_p))
+    if st != 0:
+        raise RuntimeError(f"tgpu_wall_field_host failed ({st})")
+    return out
+
+
 def rough_wall_vext(nx, esize, eps_w=1.0, kT=1.2, sigma_w=1.0, wall_x=1.0, patches=16, amplitude=0.5, seed=1234,
-                    vext_max=10.0):
+                    vext_max=10.0, device=None):
     """V_ext/kT of a rough 12-3 LJ wall normal to x.
 
     The surface sits at x = wall_x + h(y, z); h is i.i.d. uniform in
     [-amplitude, amplitude] sigma on a patches x patches grid over the periodic
     y-z plane (numpy PCG64 seeded with `seed`).  Nodes with d <= 0 or
-    V >= vext_max are clipped to vext_max (zero-density rows).
+    V >= vext_max are clipped to vext_max (zero-density rows).  The field is computed on the GPU
+    (tgpu_wall_field_host) when one is visible or device=True, else with numpy.
     """
     rng = np.random.default_rng(seed)
     hpatch = rng.uniform(-amplitude, amplitude, size=(patches, patches))
+    meta = dict(patches=patches, amplitude=amplitude, seed=seed, wall_x=wall_x, eps_w=eps_w,
+                prefactor=LJ123_PREF, form="eps_w*C*((s/d)^12-(s/d)^3)/kT")
+    if _gpu_visible() if device is None else device:
+        wall = dict(form=WALL_LJ123, side=0, position=wall_x, eps=(eps_w / kT) * LJ123_PREF, sigma=sigma_w,
+                    heights=hpatch)
+        return wall_field_device(3, nx, esize, [wall], vext_max).reshape(1, -1), meta
     ny, nz = nx[1], nx[2]
     iy = (np.arange(ny) * patches) // ny
     iz = (np.arange(nz) * patches) // nz
@@ -190,8 +262,7 @@ def rough_wall_vext(nx, esize, eps_w=1.0, kT=1.2, sigma_w=1.0, wall_x=1.0, patch
         s = np.where(d > 0, sigma_w / np.maximum(d, 1e-300), np.inf)
         v = (eps_w / kT) * LJ123_PREF * (s ** 12 - s ** 3)
     v = np.where((d <= 0) | (v >= vext_max) | ~np.isfinite(v), vext_max, v)
-    return v.reshape(1, -1), dict(patches=patches, amplitude=amplitude, seed=seed, wall_x=wall_x, eps_w=eps_w,
-                                  prefactor=LJ123_PREF, form="eps_w*C*((s/d)^12-(s/d)^3)/kT")
+    return v.reshape(1, -1), meta
 
 
 def lj93_wall_1d(dist, eps_w, sigma_w, cut_w, vext_max=10.0):
@@ -294,12 +365,18 @@ def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0, eps_w=0.5):
                    grf=field, dv_deps=dv_deps)
 
 
-def slit_pore_vext(ndim, nx, esize, eps_w=1.0, sigma_w=1.0, cut_w=3.0, pattern=0.5, vext_max=10.0):
+def slit_pore_vext(ndim, nx, esize, eps_w=1.0, sigma_w=1.0, cut_w=3.0, pattern=0.5, vext_max=10.0, device=None):
     """V_ext/kT of a slit pore: two planar cut-and-shifted 9-3 walls (the form of Vext_LJ9_3_CS,
     src/dft_vext_1D.c:42-56) with surfaces at the two x ends of the box; in 2-D the wall strength varies
     along the periodic y direction as eps_w (1 + pattern cos(2 pi y / L_y)) (a chemically patterned slit).
-    Nodes with V >= vext_max or on a surface hold vext_max.  Returns [1][N] (node = ix + nx*iy)."""
+    Nodes with V >= vext_max or on a surface hold vext_max.  Returns [1][N] (node = ix + nx*iy).  Computed on
+    the GPU (tgpu_wall_field_host) when one is visible or device=True, else with numpy."""
     L = (nx[0] - 1) * esize[0]
+    if _gpu_visible() if device is None else device:
+        pat = pattern if ndim >= 2 else 0.0
+        walls = [dict(form=WALL_LJ93_CS, side=side, position=pos, eps=eps_w, sigma=sigma_w, cut=cut_w, pattern=pat)
+                 for side, pos in ((0, 0.0), (1, L))]
+        return wall_field_device(ndim, nx, esize, walls, vext_max).reshape(1, -1)
     x = np.arange(nx[0]) * esize[0]
     s1 = lj93_wall_1d(x, 1.0, sigma_w, cut_w, vext_max=np.inf)[0]
     s2 = lj93_wall_1d(L - x, 1.0, sigma_w, cut_w, vext_max=np.inf)[0]
