@@ -334,17 +334,19 @@ void launch_conv_slab(const float *in, long in_total, const int4 *planes, int np
 // products into sums.
 constexpr int kFFGroup = 8;
 
+// One term: the product's rounding error and cross terms are gathered off the loop-carried chains, so
+// s and c each take one addition per term.
 __device__ __forceinline__ void ff_term(float wh, float wl, float fh, float fl, float &s, float &c)
 {
   const float p = __fmul_rn(wh, fh);
-  const float e = __fmaf_rn(wh, fh, -p);
+  float e = __fmaf_rn(wh, fh, -p);
+  e = __fmaf_rn(wh, fl, e);
+  e = __fmaf_rn(wl, fh, e);
   const float t = __fadd_rn(s, p);
   const float bp = __fsub_rn(t, s);
   const float e2 = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
   s = t;
   c = __fadd_rn(c, __fadd_rn(e, e2));
-  c = __fmaf_rn(wh, fl, c);
-  c = __fmaf_rn(wl, fh, c);
 }
 
 // (a, b) <- (a, b) + (c, d) in double-word arithmetic (accurate version: two two-sums, two fast two-sums)
