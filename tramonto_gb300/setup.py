@@ -308,9 +308,13 @@ def config2(n=128, esize=0.1, seed=1234, rho_b=0.6):
 
 def config4(n=256, esize=0.08, seed=1234):
     """The configuration-2 fluid and wall at scale: 256^3 nodes, dx = 0.08 (attraction reach 31 nodes,
-    1.4e5 stencil points), rho_b = 0.75 (bulk n3 = 0.39)."""
-    p, meta = config2(n=n, esize=esize, seed=seed, rho_b=0.75)
+    1.4e5 stencil points).  The problem is built at rho_b = 0.6 and brought to rho_b = 0.70 by continuation
+    (meta["ladder"]): at this resolution the contact density grows without bound as rho_b approaches ~0.71
+    (max rho 2.0, 3.6, 8.3, 10.3 at rho_b 0.60, 0.65, 0.70, 0.705; n3 up to 0.67), and Newton (mixed or FP64,
+    direct or by continuation in steps of 0.005) finds no solution at 0.71-0.75."""
+    p, meta = config2(n=n, esize=esize, seed=seed, rho_b=0.6)
     meta["initial_cap"] = 1.0   # initial densities at most rho_b: rho_b exp(-V) in the wall's well overlaps (n3 > 1)
+    meta["ladder"] = [0.6, 0.65, 0.7]
     return p, meta
 
 
