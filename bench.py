@@ -444,8 +444,10 @@ def main():
                       ("; Schur products: split-f16 x3 tensor-core attraction sums, f32 other stencil sums"
                        if args.products == "fp16tc" else "; f32 stencil sums in the Schur products")),
             "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload], "step": "one Newton solve from the initial state to ||R||_2 <= "
-                       f"{args.resid_tol:g}", "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
+            "config": {"workload": WORKLOADS[args.workload],
+                       "step": (f"the continuation {ladder}, each rung solved to ||R||_2 <= {args.resid_tol:g}" if ladder
+                                else f"one Newton solve from the initial state to ||R||_2 <= {args.resid_tol:g}"),
+                       "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
                        "rho_b": (ladder or [meta["rho_b"]])[-1], "continuation": ladder, "kT": 1.2, "rcut": 2.5,
                        "lin_tol_floor": args.lin_tol,
                        "fp32_until_resid": args.switch, "inputs_exceed_l2": True,

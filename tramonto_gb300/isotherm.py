@@ -13,6 +13,11 @@ are not zero-density rows:
 An isotherm is a continuation in the chemical potential (the reference's LOCA
 CONT_BETAMU_I steps): the bulk state moves along a ladder of bulk densities and
 every solve starts from the previous state point's solution (tgpu_set_bulk_state).
+Around turning points (capillary condensation and evaporation in a pore, where
+N(beta mu) folds back) natural steps fail; `arclength` follows the branch by
+pseudo-arclength continuation (LOCA's arc-length stepper, NOXLOCA_Solver.cpp:51-134,
+loca_lib.c:72): the Newton system is bordered by the arclength equation and solved
+by the bordering algorithm, two solves with the Jacobian per corrector iteration.
 """
 from __future__ import annotations
 
@@ -111,3 +116,111 @@ def sweep(specs, mixed=True, resid_tol=1e-8, with_derivative=True):
         rec["ndim"], rec["nodes"] = spec["ndim"], int(np.prod(spec["nx"][:spec["ndim"]]))
         recs.append(rec)
     return recs
+
+
+def _live_rows(p):
+    """Euler-Lagrange rows that carry -beta mu (not zero-density rows)."""
+    v = np.asarray(p.vext, np.float64).reshape(p.ncomp, -1)
+    z = np.asarray(p.zero_density).reshape(p.ncomp, -1) != 0
+    return ~z & (v < p.vext_max)
+
+
+def arclength(spec, rho_b0, n_steps, ds=0.02, ds_min=1e-5, ds_max=0.2, direction=1, mixed=False, tol=1e-9,
+              max_corrector=12, x0=None, stop=None, keep_states=False):
+    """Pseudo-arclength continuation in beta mu of one configuration-5 pore problem (one component).
+
+    The branch is parametrised by arclength in (rho, beta mu) with the density part measured as
+    (sum_i w_i drho_i^2 / sum_i w_i)^(1/2) (w: integration weights).  Starting from the converged state at
+    bulk density rho_b0 (or from x0), each step predicts along the tangent, then corrects with Newton on
+        R(x, mu) = 0,   t_x . (x - x_k) + t_mu (mu - mu_k) - ds = 0
+    by the bordering algorithm (J a = -R, J b = -dR/dmu, dmu = -(g + t_x.a)/(t_x.b + t_mu), dx = a + dmu b),
+    with the density-positivity fraction of update_solution applied to the whole step.  The step halves
+    when the corrector fails and grows by 1.5 when it converges in 3 iterations or fewer; the next tangent is
+    the secant of the last step.  Returns one record per point: beta mu, N, ||R||_2, corrector iterations,
+    the tangent's mu component (its sign changes at turning points) and the step length (and the state,
+    with keep_states).  stop(record) ends the continuation early when it returns True."""
+    p = setup.slit_pore(spec, rho_b=rho_b0)
+    if p.ncomp != 1:
+        raise ValueError("one component")
+    s = native.Solver(p)
+    try:
+        set_mode(s, mixed)
+        if x0 is None:
+            x0 = setup.initial_state(s, p, max_enhancement=1.0)
+        x, _, rn, _, ok = solve_state(s, p, x0, mixed, resid_tol=tol)
+        if not ok:
+            raise RuntimeError(f"no converged start at rho_b = {rho_b0} (||R||_2 = {rn:.2e})")
+        r0 = p.first_rho
+        wv = np.asarray(p.w_fluid, np.float64).reshape(-1)
+        W = wv / wv.sum()
+        live = _live_rows(p)[0]
+        R_mu = np.zeros(s.shape)
+        R_mu[r0][live] = -1.0
+        lin_tol = 1e-6 if mixed else 1e-12
+
+        def dot(a, b):
+            return float(np.sum(W * a[r0] * b[r0]))
+
+        def lin(rhs):
+            return s.solve(rhs, tol=lin_tol, max_iter=1000)[0]
+
+        mu = float(p.betamu[0])
+        s.set_chemical_potential([mu])
+        s.fill(x, mode=0)
+        b = lin(-R_mu)
+        nrm = np.sqrt(dot(b, b) + 1.0)
+        tx, tm = direction * b / nrm, direction * 1.0 / nrm
+        recs = [dict(betamu=mu, N=float(adsorption(p, x)[0]), resid=float(rn), iters=0, t_mu=tm, ds=0.0)]
+        if keep_states:
+            recs[0]["x"] = x.copy()
+
+        def corrector(xc, mc, xk, mk):
+            for it in range(max_corrector + 1):
+                s.set_chemical_potential([mc])
+                R = s.fill(xc, mode=0)
+                g = dot(tx, xc - xk) + tm * (mc - mk) - ds
+                rn_c = float(np.linalg.norm(R))
+                if not np.isfinite(rn_c):
+                    return False, xc, mc, it, rn_c
+                if rn_c <= tol and abs(g) <= tol:
+                    return True, xc, mc, it, rn_c
+                if it == max_corrector:
+                    break
+                a = lin(-R)
+                bb = lin(-R_mu)
+                den = dot(tx, bb) + tm
+                if den == 0.0 or not np.isfinite(den):
+                    return False, xc, mc, it, rn_c
+                dm = -(g + dot(tx, a)) / den
+                dxv = a + dm * bb
+                rho, drho = xc[r0], dxv[r0]
+                neg = live & (drho < -0.9 * rho)
+                f = min(1.0, float(np.min(-0.9 * rho[neg] / drho[neg]))) if neg.any() else 1.0
+                xc = xc + f * dxv
+                mc = mc + f * dm
+            return False, xc, mc, max_corrector, rn_c
+
+        for _ in range(n_steps):
+            while True:
+                xp = x + ds * tx
+                xp[r0] = np.where(live, np.maximum(xp[r0], 1e-12), xp[r0])
+                ok, xn, mn, its, rn_c = corrector(xp, mu + ds * tm, x, mu)
+                if ok:
+                    break
+                ds *= 0.5
+                if ds < ds_min:
+                    raise RuntimeError(f"arclength step below {ds_min} at beta mu = {mu:.6f}")
+            sx, sm = xn - x, mn - mu
+            nrm = np.sqrt(dot(sx, sx) + sm * sm)
+            tx, tm = sx / nrm, sm / nrm
+            x, mu = xn, mn
+            recs.append(dict(betamu=mu, N=float(adsorption(p, x)[0]), resid=rn_c, iters=its, t_mu=tm, ds=ds))
+            if keep_states:
+                recs[-1]["x"] = x.copy()
+            if stop is not None and stop(recs[-1]):
+                break
+            if its <= 3:
+                ds = min(1.5 * ds, ds_max)
+        return recs, x
+    finally:
+        s.close()

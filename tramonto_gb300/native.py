@@ -219,6 +219,24 @@ class Solver:
             p.betamu = np.log(rho_b) + hs + att
             self.set_integration(p.w_fluid, p.w_bulk, p.rhobar_b, p.betamu)
 
+    def set_chemical_potential(self, betamu):
+        """Set beta mu_i directly, for problems without bulk boundaries (pores): the Euler-Lagrange rows
+        hold -(ln rho_b + betamu_hs_ex + betamu_att) = -beta mu (src/dft_fill_EL.c:401-410), and rho_b
+        itself is read only at bulk boundaries and by the objectives' bulk terms.  rho_b is kept and
+        betamu_att takes up the change (tgpu_set_bulk_state); Omega_s and Gamma_ex, which compare with
+        the bulk at rho_b, are then not those of the new state, the absolute adsorption is."""
+        from .problem import BC_IN_BULK
+        p = self.p
+        if any(BC_IN_BULK in tuple(p.bc[d]) for d in range(p.ndim)):
+            raise ValueError("beta mu can be set directly only without bulk boundaries")
+        bm = np.asarray(betamu, np.float64).reshape(p.ncomp)
+        rho_b = np.ascontiguousarray(p.rho_b, np.float64)
+        hs = np.ascontiguousarray(p.betamu_hs_ex, np.float64)
+        att = np.ascontiguousarray(bm - np.log(rho_b) - hs, np.float64)
+        dphi = np.ascontiguousarray(p.dphi_bulk, np.float64)
+        _check(self.lib.tgpu_set_bulk_state(self.h, _ptr(rho_b), _ptr(hs), _ptr(att), _ptr(dphi)), self.lib)
+        p.betamu_att = att
+
     def set_integration(self, w_fluid, w_bulk, rhobar_b, betamu):
         """Integration weights ([ncomp][N] each), bulk n3 n2 n1 n0 and betamu of the objectives."""
         nc = self.p.ncomp
