@@ -238,9 +238,22 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
     c->stats.kernel_launches += 4;
     return;
   }
+  if (f32 && (nin > 1 || nout > 1)) {
+    const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
+    if (ln.nplanes > 0 && ln.mc_ok && ln.ncoef == nin * nout) {
+      const long total = (long)c->nch_max * NP + 64 - (long)ch0 * NP;
+      if (tgpu::launch_conv_slab_mc(c->d_pad32 + (long)ch0 * NP, NP, total, nin, ln.d_planes, ln.nplanes,
+                                    ln.d_lines, ln.d_w, ln.wstride, outs, nout, ln.pitch, ln.ncols, ln.max_rows,
+                                    ln.max_lines, ln.max_w, c->dg.nx[0], c->dg.nx[1], c->dg.nx[2], c->stream)) {
+        c->stats.conv_launches++;
+        c->stats.kernel_launches++;
+        return;
+      }
+    }
+  }
   if (f32 && nin == 1 && nout == 1) {
     const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
-    if (ln.nplanes > 0) {
+    if (ln.nplanes > 0 && ln.ncoef == 1) {
       // the slab loads stay inside this channel and its successors (the buffer has one spare row)
       const long total = (long)c->nch_max * NP + 64 - (long)ch0 * NP;
       tgpu::launch_conv_slab(c->d_pad32 + (long)ch0 * NP, total, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w,
@@ -253,7 +266,7 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
   }
   if (!f32 && c->ff_on && nin == 1 && nout == 1) {
     const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
-    if (ln.nplanes > 0 && ln.ff_ok) {
+    if (ln.nplanes > 0 && ln.ncoef == 1 && ln.ff_ok) {
       // high and low FP32 parts of the channel in the (idle) FP32 padded buffer, which holds at least two
       // channels; loads past a part's end read zeros
       float *hi = c->d_pad32, *lo = c->d_pad32 + NP;
@@ -1028,12 +1041,13 @@ void d2h(Ctx *c, double *h, const double *d, size_t n)
 // slab kernel: per plane {first line, count, first weight, weight count} and
 // {oz, oy_lo, oy_hi, 0}; per line {oy - oy_lo, ox_min + h0, blocks of 8, weight offset}.
 DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &coef, const tgpu::DevGeom &dg,
-                              cudaStream_t s)
+                              cudaStream_t s, int ncoef = 1, int nin = 1)
 {
-  std::map<int, std::map<int, std::vector<std::pair<int, double>>>> planes;
+  // per point: its x offset and the index of its coefficient row
+  std::map<int, std::map<int, std::vector<std::pair<int, int>>>> planes;
   for (int k = 0; k < st.L; k++) {
     const short *o = &st.off[(size_t)k * 3];
-    planes[o[2]][o[1]].push_back({o[0], coef[k]});
+    planes[o[2]][o[1]].push_back({o[0], k});
   }
   std::vector<int4> pd, lines;
   std::vector<float> w, w_lo;
@@ -1051,9 +1065,10 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
       w.resize(base + (size_t)nb * 8, 0.0f);
       w_lo.resize(base + (size_t)nb * 8, 0.0f);
       for (auto &e : ykv.second) {
-        const float hi = (float)e.second;
+        const double v = coef[(size_t)e.second * ncoef];
+        const float hi = (float)v;
         w[base + (e.first - xmin)] = hi;
-        w_lo[base + (e.first - xmin)] = (float)(e.second - (double)hi);
+        w_lo[base + (e.first - xmin)] = (float)(v - (double)hi);
       }
     }
     const int nl = (int)lines.size() - first_line, nw = (int)w.size() - first_w;
@@ -1068,14 +1083,34 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
   int pitch = L.ncols + (L.ncols >> 3) + 1;
   while (pitch % 32 != 16) pitch++;
   L.pitch = pitch;
-  const size_t smem = sizeof(float) * ((size_t)L.max_rows * pitch + L.max_w) + sizeof(int4) * L.max_lines;
-  if (smem > 200 * 1024) throw Error(TGPU_ERR_UNSUPPORTED, "stencil plane too large for the shared-memory slab");
   L.nplanes = (int)planes.size();
   L.d_planes = upload(pd, s);
   L.d_lines = upload(lines, s);
-  L.d_w = upload(w, s);
-  L.d_w_lo = upload(w_lo, s);
-  L.ff_ok = tgpu::conv_slab_ff_smem(L.pitch, L.max_rows, L.max_lines, L.max_w) <= 220 * 1024;
+  L.ncoef = ncoef;
+  L.wstride = (int)w.size();
+  if (ncoef == 1) {
+    const size_t smem = sizeof(float) * ((size_t)L.max_rows * pitch + L.max_w) + sizeof(int4) * L.max_lines;
+    if (smem > 200 * 1024) throw Error(TGPU_ERR_UNSUPPORTED, "stencil plane too large for the shared-memory slab");
+    L.d_w = upload(w, s);
+    L.d_w_lo = upload(w_lo, s);
+    L.ff_ok = tgpu::conv_slab_ff_smem(L.pitch, L.max_rows, L.max_lines, L.max_w) <= 220 * 1024;
+  } else {
+    // coefficient c of every point at w + c * wstride, in the line layout of coefficient 0
+    std::vector<float> wall((size_t)ncoef * w.size(), 0.0f);
+    size_t pos = 0;
+    for (auto &pkv : planes)
+      for (auto &ykv : pkv.second) {
+        int xmin = 1 << 30, xmax = -(1 << 30);
+        for (auto &e : ykv.second) { xmin = std::min(xmin, e.first); xmax = std::max(xmax, e.first); }
+        const int nb = (xmax - xmin + 1 + 7) / 8;
+        for (auto &e : ykv.second)
+          for (int cc = 0; cc < ncoef; cc++)
+            wall[(size_t)cc * w.size() + pos + (e.first - xmin)] = (float)coef[(size_t)e.second * ncoef + cc];
+        pos += (size_t)nb * 8;
+      }
+    L.d_w = upload(wall, s);
+    L.mc_ok = tgpu::conv_slab_mc_smem(nin, ncoef, L.pitch, L.max_rows, L.max_lines, L.max_w) <= 200 * 1024;
+  }
   return L;
 }
 
@@ -1178,6 +1213,11 @@ void build_device_tables(Ctx *c)
       if (nd == 3 && (t == TGPU_STEN_THETA || t == TGPU_STEN_UATT)) {
         st.lines_fwd = build_lines(st, fwd, dg, c->stream);
         if (t == TGPU_STEN_THETA) st.lines_tr = build_lines(st, tr, dg, c->stream);
+      }
+      if (nd == 3 && t == TGPU_STEN_DELTA && g.single_size) {
+        // the forward table is [L][1 + nd] (one input), the transpose table [L][1 + nd] (one output)
+        st.lines_fwd = build_lines(st, fwd, dg, c->stream, st.nout_fwd, 1);
+        st.lines_tr = build_lines(st, tr, dg, c->stream, st.nin_tr, st.nin_tr);
       }
       if (nd == 3 && t == TGPU_STEN_UATT) tgpu::tc_build_tables(st.off, fwd, st.L, dg.h[1], st.tc, c->stream);
     }

@@ -314,6 +314,146 @@ void launch_conv_slab(const float *in, long in_total, const int4 *planes, int np
 }
 
 // ---------------------------------------------------------------------------
+// Multi-channel FP32 slab sums (the delta stencil's weighted densities and
+// their transposes in the Schur products).  The traversal of k_conv_slab with
+// NIN input channels staged per plane and NIN*NOUT coefficients per stencil
+// point (stored per coefficient along the lines, wstride apart): output channel
+// o of the thread's 8 x-outputs accumulates sum_c coef[o*NIN + c] * in_c over
+// the stencil in one FP32 chain, as k_conv does point by point.
+template <int NIN, int NOUT>
+__global__ void __launch_bounds__(kSlabThreads) k_conv_slab_mc(const float *__restrict__ in, long cstride,
+                                                             long in_total, const int4 *__restrict__ planes,
+                                                             int nplanes, const int4 *__restrict__ lines,
+                                                             const float *__restrict__ lw, int wstride, OutPtrs out,
+                                                             int pitch, int ncols, int max_rows, int max_lines,
+                                                             int max_w)
+{
+  constexpr int NC = NIN * NOUT;
+  extern __shared__ float smem[];
+  float *s_slab = smem;                                        // [NIN][max_rows][pitch]
+  float *s_w = s_slab + (size_t)NIN * max_rows * pitch;        // [NC][max_w]
+  int4 *s_line = reinterpret_cast<int4 *>(s_w + (size_t)NC * max_w);   // [max_lines]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int x0 = blockIdx.x * kSlabTX, y0 = blockIdx.y * kSlabTY, z = blockIdx.z;
+  float acc[NOUT][8];
+#pragma unroll
+  for (int o = 0; o < NOUT; o++)
+#pragma unroll
+    for (int q = 0; q < 8; q++) acc[o][q] = 0.f;
+  for (int pi = 0; pi < nplanes; pi++) {
+    const int4 pd = planes[2 * pi];
+    const int4 pg = planes[2 * pi + 1];
+    const int nrows = kSlabTY + pg.z - pg.y;
+    __syncthreads();
+    for (int k = threadIdx.x; k < pd.y; k += kSlabThreads) s_line[k] = lines[pd.x + k];
+    for (int k = threadIdx.x; k < NC * pd.w; k += kSlabThreads) {
+      const int cc = k / pd.w, kk = k - cc * pd.w;
+      s_w[cc * max_w + kk] = lw[(long)cc * wstride + pd.z + kk];
+    }
+    const long gz = (long)(z + pg.x + c_g.h[2]) * c_g.pstride[2];
+    for (int e = threadIdx.x; e < nrows * ncols; e += kSlabThreads) {
+      const int r = e / ncols, cidx = e - r * ncols;
+      const int gy = y0 + pg.y + r + c_g.h[1];
+      const long gi = gz + (long)gy * c_g.pstride[1] + x0 + cidx;
+#pragma unroll
+      for (int c = 0; c < NIN; c++) {
+        float v = 0.f;
+        if (gy < c_g.P[1] && gi < in_total - (long)c * cstride) v = __ldg(in + (long)c * cstride + gi);
+        s_slab[((size_t)c * max_rows + r) * pitch + slab_phys(cidx)] = v;
+      }
+    }
+    __syncthreads();
+    for (int li = 0; li < pd.y; li++) {
+      const int4 ln = s_line[li];
+      const int c0 = 8 * tx + ln.y;
+      const float *w = s_w + (ln.w - pd.z);
+      float win[NIN][16];
+#pragma unroll
+      for (int c = 0; c < NIN; c++) {
+        const float *row = s_slab + ((size_t)c * max_rows + ty + ln.x) * pitch;
+#pragma unroll
+        for (int q = 0; q < 8; q++) win[c][q] = row[slab_phys(c0 + q)];
+      }
+      for (int kb = 0; kb < ln.z; kb++) {
+#pragma unroll
+        for (int c = 0; c < NIN; c++) {
+          const float *row = s_slab + ((size_t)c * max_rows + ty + ln.x) * pitch;
+#pragma unroll
+          for (int q = 0; q < 8; q++) win[c][8 + q] = row[slab_phys(c0 + 8 * (kb + 1) + q)];
+        }
+#pragma unroll
+        for (int kk = 0; kk < 8; kk++) {
+          float wk[NC];
+#pragma unroll
+          for (int cc = 0; cc < NC; cc++) wk[cc] = w[cc * max_w + 8 * kb + kk];
+#pragma unroll
+          for (int o = 0; o < NOUT; o++)
+#pragma unroll
+            for (int c = 0; c < NIN; c++)
+#pragma unroll
+              for (int q = 0; q < 8; q++) acc[o][q] = fmaf(wk[o * NIN + c], win[c][q + kk], acc[o][q]);
+        }
+#pragma unroll
+        for (int c = 0; c < NIN; c++)
+#pragma unroll
+          for (int q = 0; q < 8; q++) win[c][q] = win[c][8 + q];
+      }
+    }
+  }
+  const int y = y0 + ty;
+  if (y < c_g.nx[1]) {
+    const long i0 = (long)c_g.nx[0] * (y + (long)c_g.nx[1] * z);
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) {
+      double *dst = out.p[o];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int x = x0 + 8 * tx + q;
+        if (x < c_g.nx[0]) dst[i0 + x] += (double)acc[o][q];
+      }
+    }
+  }
+}
+
+size_t conv_slab_mc_smem(int nin, int ncoef, int pitch, int max_rows, int max_lines, int max_w)
+{
+  return sizeof(float) * ((size_t)nin * max_rows * pitch + (size_t)ncoef * max_w) + sizeof(int4) * max_lines;
+}
+
+template <int NIN, int NOUT>
+static void slab_mc_dispatch(const float *in, long cstride, long in_total, const int4 *planes, int nplanes,
+                             const int4 *lines, const float *lw, int wstride, const OutPtrs &o, int pitch, int ncols,
+                             int max_rows, int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s)
+{
+  const size_t smem = conv_slab_mc_smem(NIN, NIN * NOUT, pitch, max_rows, max_lines, max_w);
+  static size_t configured = 0;
+  if (smem > configured) {
+    cudaFuncSetAttribute(k_conv_slab_mc<NIN, NOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 grid((nx + kSlabTX - 1) / kSlabTX, (ny + kSlabTY - 1) / kSlabTY, nz);
+  k_conv_slab_mc<NIN, NOUT><<<grid, kSlabThreads, smem, s>>>(in, cstride, in_total, planes, nplanes, lines, lw,
+                                                              wstride, o, pitch, ncols, max_rows, max_lines, max_w);
+}
+
+bool launch_conv_slab_mc(const float *in, long cstride, long in_total, int nin, const int4 *planes, int nplanes,
+                         const int4 *lines, const float *lw, int wstride, double *const *out, int nout, int pitch,
+                         int ncols, int max_rows, int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s)
+{
+  OutPtrs o{};
+  for (int k = 0; k < nout; k++) o.p[k] = out[k];
+#define TGPU_SLAB_MC(NI, NO)                                                                                       \
+  if (nin == NI && nout == NO) {                                                                                  \
+    slab_mc_dispatch<NI, NO>(in, cstride, in_total, planes, nplanes, lines, lw, wstride, o, pitch, ncols, max_rows, \
+                             max_lines, max_w, nx, ny, nz, s);                                                   \
+    return true;                                                                                                 \
+  }
+  TGPU_SLAB_MC(1, 4) TGPU_SLAB_MC(4, 1)
+#undef TGPU_SLAB_MC
+  return false;
+}
+
+// ---------------------------------------------------------------------------
 // FP64-accurate single-channel 3-D stencil sums in float-float arithmetic.
 //
 // The same slab / x-line traversal as k_conv_slab, on the padded field split

@@ -287,7 +287,9 @@ struct DevStencil {
     float *d_w = nullptr;
     float *d_w_lo = nullptr;            // FP32 remainder of each weight (float-float sums)
     int nplanes = 0, max_rows = 0, max_lines = 0, max_w = 0, ncols = 0, pitch = 0;
+    int ncoef = 1, wstride = 0;         // coefficients per stencil point, stored wstride apart
     bool ff_ok = false;                 // the float-float slab fits in shared memory
+    bool mc_ok = false;                 // the multi-channel slab fits in shared memory
   } lines_fwd, lines_tr;
 };
 
@@ -357,6 +359,11 @@ void launch_conv_slab(const float *in, long in_total, const int4 *planes, int np
                       const float *lw, double *out, int pitch, int ncols, int max_rows, int max_lines, int max_w,
                       int nx, int ny, int nz, cudaStream_t s);
 size_t conv_slab_ff_smem(int pitch, int max_rows, int max_lines, int max_w);
+size_t conv_slab_mc_smem(int nin, int ncoef, int pitch, int max_rows, int max_lines, int max_w);
+// false when (nin, nout) has no multi-channel slab kernel (1x4 and 4x1 exist: 3-D delta sums, one particle size)
+bool launch_conv_slab_mc(const float *in, long cstride, long in_total, int nin, const int4 *planes, int nplanes,
+                         const int4 *lines, const float *lw, int wstride, double *const *out, int nout, int pitch,
+                         int ncols, int max_rows, int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s);
 void launch_split_hilo(const double *in, long n, float *hi, float *lo, cudaStream_t s);
 void launch_conv_slab_ff(const float *in_hi, const float *in_lo, long in_total, const int4 *planes, int nplanes,
                          const int4 *lines, const float *lw, const float *lw_lo, double *out, int pitch, int ncols,

@@ -61,7 +61,7 @@ def make_stencil(stype, ndim, esize, hs_diam=0.0, sigma=1.0, eps=1.0, rcut=0.0, 
         device = ndim == 3 and (stype == UATT or reach > 5.5) and _gpu_visible()
     fn = lib.tgpu_make_stencil_device if device else lib.tgpu_make_stencil
     es = (C.c_double * 3)(*(list(esize) + [0.0] * (3 - len(esize))))
-    # one call builds the table; the second (with arrays) rebuilds it, so size the arrays generously
+    # the size query builds the table once; the second call builds it again into the arrays
     L = fn(stype, ndim, es, hs_diam, sigma, eps, rcut, rmin, 0, None, None, None, None)
     if L < 0:
         raise RuntimeError(f"tgpu_make_stencil{'_device' if device else ''} failed ({L})")
@@ -397,11 +397,11 @@ def slit_pore_vext(ndim, nx, esize, eps_w=1.0, sigma_w=1.0, cut_w=3.0, pattern=0
 
 
 def slit_pore(spec, rho_b=None):
-    """One configuration-5 problem: FMT1 + WCA (eps = 1, r_c = 2.5, kT* = 1.2) in a slit pore
+    """One configuration-5 problem: FMT1 + WCA (eps = 1, r_c = 2.5, kT* = spec.get("kT", 1.2)) in a slit pore
     (spec from config5); walls beyond both x ends, periodic y in 2-D."""
     ndim, nx, dx = spec["ndim"], tuple(spec["nx"]), spec["dx"]
     es = (dx,) * ndim
-    kT = 1.2
+    kT = float(spec.get("kT", 1.2))
     bc = [(BC_IN_WALL, BC_IN_WALL)] + [(BC_PERIODIC, BC_PERIODIC)] * (ndim - 1)
     vext = slit_pore_vext(ndim, nx, es)
     return build_problem(ndim, nx, es, tuple(bc), hs_diam=[1.0], rho_b=[spec["rho_b"] if rho_b is None else rho_b],
