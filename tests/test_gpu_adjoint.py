@@ -23,7 +23,8 @@ from goldens import PROD_RTOL, load, probe, rel_err
 
 pytestmark = pytest.mark.gpu
 
-ADJ_CASES = ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "mix1d_fmt4", "rough3d_fmt2", "rough3d_fmt4"]
+ADJ_CASES = ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "mix1d_fmt4", "rough3d_fmt2", "rough3d_fmt4",
+             "hs1d_wall", "hs1d_c1", "hs1d_fmt2", "hs1d_fmt4"]   # the last four with hard-wall boundary weights
 GRAD_RTOL = 1e-5
 FD_H = 1e-6
 
@@ -207,3 +208,36 @@ def test_wall_parameter_gradcheck(fluid):
     ok = torch.autograd.gradcheck(GrandPotential.apply, (theta,), eps=FD_H, atol=1e-7, rtol=GRAD_RTOL,
                                   nondet_tol=1e-9)
     assert ok
+
+
+def test_hard_wall_vext_gradient_matches_finite_differences():
+    """Configuration 1 (HS5 at L = 20, hard wall with boundary weights): dOmega_s/dV_ext by the adjoint,
+    whose J^T includes the transpose of the hard-wall weight correction, against central differences of
+    re-converged states."""
+    from tramonto_gb300 import native
+    z, p = load("hs1d_c1")
+    s = native.Solver(p)
+    vext0 = np.array(p.vext, dtype=np.float64).reshape(p.ncomp, p.nnodes)
+
+    def converge(v, x0):
+        s.set_vext(v)
+        x, _, rn, _ = s.newton_solve(x0, resid_tol=1e-12, lin_tol=1e-12, lin_max_iter=1000, max_iter=60,
+                                     allow_noconv=True)
+        assert rn <= 1e-11, rn
+        return x
+
+    x0 = converge(vext0, z["x_newton"])
+    g = s.grad_vext(x0, kind=0, tol=1e-13, max_iter=2000)
+    live = np.nonzero((np.asarray(p.zero_density).reshape(-1) == 0) & (vext0.reshape(-1) < p.vext_max))[0]
+    u = np.zeros(vext0.size)
+    u[live] = np.cos(0.37 * np.arange(live.size)) * np.exp(-0.01 * np.arange(live.size))
+    dirs = [u, np.eye(1, vext0.size, live[3]).reshape(-1), np.eye(1, vext0.size, live[40]).reshape(-1)]
+    for d in dirs:
+        d = d.reshape(vext0.shape)
+        om_p = s.objectives(converge(vext0 + FD_H * d, x0))[0]
+        om_m = s.objectives(converge(vext0 - FD_H * d, x0))[0]
+        fd = (om_p - om_m) / (2 * FD_H)
+        adj = float(np.sum(g * d))
+        scale = max(abs(fd), float(np.abs(g).max() * np.abs(d).max()))
+        assert abs(adj - fd) <= GRAD_RTOL * scale, (adj, fd)
+    s.close()

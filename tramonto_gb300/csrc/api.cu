@@ -793,7 +793,6 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
   for (int d = 0; d < g.ndim; d++)
     if (c->g.bc[d][0] == TGPU_BC_REFLECT || c->g.bc[d][1] == TGPU_BC_REFLECT)
       throw Error(TGPU_ERR_UNSUPPORTED, "J^T with reflecting boundaries is not implemented");
-  if (g.hard_surf) throw Error(TGPU_ERR_UNSUPPORTED, "J^T with hard-wall boundary weights is not implemented");
   ensure_adjoint(c);
   const long N = g.N;
   const int nd = g.ndim;
@@ -814,6 +813,13 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
           const DevStencil &su = c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc];
           adj_conv(c, g.ncomp * cpc + ic, 1, su, su.d_coef_fwd, o, 1);
         }
+    }
+    // hard-wall boundary weights: the transpose of the forward correction
+    if (g.hard_surf && !c->hw_targets.empty()) {
+      tgpu::launch_hw_correct_t(d_w, c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(),
+                                c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero, c->d_bnodes, c->d_fmask,
+                                d_out, c->stream);
+      c->stats.kernel_launches++;
     }
     // density columns exist only off zero-density nodes
     tgpu::launch_mask_rows(d_out + (long)g.first_rho * N, nullptr, c->d_vext, c->d_zero, 0, g.ncomp, 1, c->stream);

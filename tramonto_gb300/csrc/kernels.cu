@@ -1216,6 +1216,77 @@ void launch_hw_correct(const double *field, long fcs, int ffirst, const DevStenc
                                                        ntargets, zero, bnodes, fmask, conv);
 }
 
+// Transpose of the hard-wall correction: the density column of every boundary node j receives, from each
+// target node i whose stencil point lands on j, the weight change times the adjoint rb rows at i (the
+// coefficients of hw_apply).  Several targets reach one j: FP64 atomic additions.
+__device__ void hw_apply_t(const HwStencil &st, int kind, int jc, int jlist, const int *ijk, long i,
+                           const double *__restrict__ w, const signed char *zero, const int *bnodes,
+                           const short *fmask, double *out)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  const int nel = 1 << nd;
+  const double *W = w + (long)c_g.first_rb * N + i;   // adjoint rb rows at i, N apart
+  for (int s = 0; s < st.L; s++) {
+    int refl;
+    const short *o = st.off + (long)s * 3;
+    const long jn = map_offset(ijk, o, &refl);
+    if (jn < 0) continue;
+    if (bnodes[(long)jlist * N + jn] == -1) continue;
+    if (zero[(long)jc * N + jn]) continue;
+    const int mask = fmask[((long)jlist * nel + refl) * N + jn];
+    double wh = 0.0;
+    for (int l = 0; l < nel; l++)
+      if (mask & (1 << l)) wh += st.hw[(long)s * nel + l];
+    const double dw = wh - st.w[s];
+    const double f = c_g.fac[jc];
+    double g;
+    if (kind == 0) {
+      g = W[0];
+    } else {
+      g = W[N];
+      if (!c_g.single_size) g += c_g.inv_4pir[jc] * W[2 * N] + c_g.inv_4pirsq[jc] * W[3 * N];
+      for (int d = 0; d < nd; d++) {
+        const double v = (double)o[d] * c_g.esize[d] * c_g.inv_rad[jc];
+        g += v * W[(long)(4 + d) * N];
+        if (!c_g.single_size) g += c_g.inv_4pir[jc] * v * W[(long)(4 + nd + d) * N];
+      }
+    }
+    atomicAdd(out + (long)(c_g.first_rho + jc) * N + jn, f * dw * g);
+  }
+}
+
+__global__ void k_hw_correct_t(const double *__restrict__ w, HwStencil th0, HwStencil th1, HwStencil de0,
+                               HwStencil de1, const int *__restrict__ targets, int ntargets,
+                               const signed char *__restrict__ zero, const int *__restrict__ bnodes,
+                               const short *__restrict__ fmask, double *__restrict__ out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntargets) return;
+  const long i = targets[t];
+  int ijk[3];
+  node_ijk(i, ijk);
+  for (int jc = 0; jc < c_g.ncomp && jc < 2; jc++) {
+    const int jlist = (c_g.nlists <= 2) ? 0 : jc;
+    hw_apply_t(jc == 0 ? th0 : th1, 0, jc, jlist, ijk, i, w, zero, bnodes, fmask, out);
+    hw_apply_t(jc == 0 ? de0 : de1, 1, jc, jlist, ijk, i, w, zero, bnodes, fmask, out);
+  }
+}
+
+void launch_hw_correct_t(const double *w, const DevStencil *theta, const DevStencil *delta, const int *targets,
+                         int ntargets, const signed char *zero, const int *bnodes, const short *fmask, double *out,
+                         cudaStream_t s)
+{
+  if (ntargets <= 0) return;
+  HwStencil th[2] = {}, de[2] = {};
+  for (int c = 0; c < 2; c++) {
+    if (theta[c].L) th[c] = {theta[c].L, theta[c].d_off, theta[c].d_w, theta[c].d_hw};
+    if (delta[c].L) de[c] = {delta[c].L, delta[c].d_off, delta[c].d_w, delta[c].d_hw};
+  }
+  k_hw_correct_t<<<(ntargets + 127) / 128, 128, 0, s>>>(w, th[0], th[1], de[0], de[1], targets, ntargets, zero,
+                                                         bnodes, fmask, out);
+}
+
 // ---------------------------------------------------------------------------
 // Krylov and Newton vector kernels.  Reductions are two-level and ordered
 // (per-block partials, then one block in fixed order): results do not depend

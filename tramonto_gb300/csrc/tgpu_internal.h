@@ -382,6 +382,9 @@ void launch_hw_correct(const double *field, long field_cstride, int field_first,
                        const DevStencil *delta, const DevStencil *uatt, const int *targets, int ntargets,
                        const signed char *zero, const int *bnodes, const short *fmask, double *conv,
                        cudaStream_t s);
+void launch_hw_correct_t(const double *w, const DevStencil *theta, const DevStencil *delta, const int *targets,
+                         int ntargets, const signed char *zero, const int *bnodes, const short *fmask, double *out,
+                         cudaStream_t s);
 // Krylov helpers
 void launch_multidot(const double *V, long ldv, int nvec, const double *w, long n, double *partial, int nblocks,
                      double *result, cudaStream_t s);
