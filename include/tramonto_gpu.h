@@ -163,7 +163,7 @@ int tgpu_jtv_device(tgpu_handle h, const double *d_w, double *d_out);
  * gradient of an objective F(x) at a converged state x*, the sensitivity of F(x*) to a parameter p that
  * enters the residual is dF/dp = dF/dp|_x - lambda^T dR/dp; for the external field the residual's
  * Euler-Lagrange rows hold +V_ext, so dF/dV_ext[ic][i] = dF/dV_ext|_x - lambda[ic][i] off zero-density rows.
- * Reflecting boundaries return TGPU_ERR_UNSUPPORTED (also for tgpu_jtv). */
+ * Reflecting boundaries and hard-wall boundary weights are transposed exactly. */
 int tgpu_adjoint_solve(tgpu_handle h, const double *g, double *lambda, double tol, int max_iter, int *iters,
                        double *relres);
 int tgpu_adjoint_solve_device(tgpu_handle h, const double *d_g, double *d_lambda, double tol, int max_iter,

@@ -24,7 +24,8 @@ from goldens import PROD_RTOL, load, probe, rel_err
 pytestmark = pytest.mark.gpu
 
 ADJ_CASES = ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "mix1d_fmt4", "rough3d_fmt2", "rough3d_fmt4",
-             "hs1d_wall", "hs1d_c1", "hs1d_fmt2", "hs1d_fmt4"]   # the last four with hard-wall boundary weights
+             "hs1d_wall", "hs1d_c1", "hs1d_fmt2", "hs1d_fmt4", "hs1d_reflect"]
+# hs1d_*: hard-wall boundary weights; hs1d_reflect also a reflecting boundary
 GRAD_RTOL = 1e-5
 FD_H = 1e-6
 
@@ -87,14 +88,33 @@ def test_adjoint_solve(name):
     s.close()
 
 
-def test_transpose_rejects_reflecting_boundaries():
-    from tramonto_gb300 import native
-    z, p = load("hs1d_reflect")
+def _reflecting_3d_problem():
+    """16 x 12 x 12 FMT1 + WCA problem at a rough 12-3 wall, reflecting in y, periodic in z."""
+    from tramonto_gb300 import setup
+    from tramonto_gb300.problem import BC_IN_BULK, BC_IN_WALL, BC_PERIODIC, BC_REFLECT, FMT1
+    nx, es = (16, 12, 12), (0.25, 0.25, 0.25)
+    vext, _ = setup.rough_wall_vext(nx, es, kT=1.2, patches=4, device=False)
+    return setup.build_problem(3, nx, es, ((BC_IN_WALL, BC_IN_BULK), (BC_REFLECT, BC_REFLECT), (BC_PERIODIC, BC_PERIODIC)),
+                               hs_diam=[1.0], rho_b=[0.6], functional=FMT1, attraction=True, sigma=[[1.0]],
+                               eps=[[1.0 / 1.2]], rcut=[[2.5]], vext=vext)
+
+
+def test_jtv_is_the_adjoint_of_jv_with_reflecting_boundaries_in_3d():
+    """Reflections fold mirrored contributions back with the vector components' sign: <u, J v> = <J^T u, v>
+    on a 3-D problem reflecting in y (no reference fixture: J v itself is pinned by the forward parity)."""
+    from tramonto_gb300 import native, setup
+    p = _reflecting_3d_problem()
     s = native.Solver(p)
-    s.fill(z["x0"], mode=0)
-    with pytest.raises(native.TgpuError) as e:
-        s.jtv(np.zeros(s.shape))
-    assert e.value.status == -4
+    x = setup.initial_state(s, p, max_enhancement=1.0)
+    s.fill(x, mode=0)
+    rng = np.random.default_rng(11)
+    for _ in range(3):
+        u = rng.standard_normal(s.shape)
+        v = rng.standard_normal(s.shape)
+        lhs = float(np.sum(u * s.jv(v)))
+        rhs = float(np.sum(s.jtv(u) * v))
+        scale = float(np.abs(u * s.jv(v)).sum())
+        assert abs(lhs - rhs) <= 1e-12 * scale, (lhs, rhs)
     s.close()
 
 

@@ -771,18 +771,35 @@ void ensure_adjoint(Ctx *c)
 }
 
 // transposed stencil sum (FP64): out[j] (+)= sum_k coef[k] . in(j - offset_k), coefficient rows of shape (nin, nout)
-void adj_conv(Ctx *c, int ch0, int nin, const DevStencil &st, const double *coef, double *const *outs, int nout)
+bool has_reflect(const Ctx *c)
+{
+  for (int d = 0; d < c->g.ndim; d++)
+    if (c->g.bc[d][0] == TGPU_BC_REFLECT || c->g.bc[d][1] == TGPU_BC_REFLECT) return true;
+  return false;
+}
+
+// Transposed sums of the padded adjoint channels ch0.. into outs; with reflecting boundaries also the
+// fold of the mirrored positions (vecdim[o] >= 0: output o is the vector component along that dimension).
+void adj_conv(Ctx *c, int ch0, int nin, const DevStencil &st, const double *coef, double *const *outs, int nout,
+              const int *vecdim = nullptr)
 {
   tgpu::launch_conv<double>(c->d_adj_pad + (long)ch0 * c->dg.NP, c->dg.NP, nin, st.d_loff_neg, coef, st.L, outs, nout,
                             true, c->dg.N, c->stream);
   c->stats.conv_launches++;
   c->stats.kernel_launches++;
+  if (has_reflect(c)) {
+    int sm[tgpu::kMaxRb] = {0};
+    for (int o = 0; o < nout; o++) sm[o] = (vecdim && vecdim[o] >= 0) ? 1 << vecdim[o] : 0;
+    tgpu::launch_reflect_fold(c->d_adj_pad + (long)ch0 * c->dg.NP, c->dg.NP, nin, st.d_off, coef, st.L, outs, sm,
+                              nout, c->stream);
+    c->stats.kernel_launches++;
+  }
 }
 
 void adj_pad(Ctx *c, int nch)
 {
   tgpu::launch_pad<double>(c->d_adj_chan, c->d_adj_pad, nch, c->pads.zero_ext.bulk, c->pads.zero_ext.sign,
-                           c->pads.zero_ext.zc, c->d_zero, false, c->stream);
+                           c->pads.zero_ext.zc, c->d_zero, has_reflect(c), c->stream);
   c->stats.kernel_launches++;
 }
 
@@ -790,9 +807,6 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
 {
   need_state(c);
   const tgpu::DevGeom &g = c->dg;
-  for (int d = 0; d < g.ndim; d++)
-    if (c->g.bc[d][0] == TGPU_BC_REFLECT || c->g.bc[d][1] == TGPU_BC_REFLECT)
-      throw Error(TGPU_ERR_UNSUPPORTED, "J^T with reflecting boundaries is not implemented");
   ensure_adjoint(c);
   const long N = g.N;
   const int nd = g.ndim;
@@ -834,7 +848,8 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
       double *o[tgpu::kMaxRb];
       for (int q = 0; q < gst; q++) o[q] = c->d_adj_g + ((long)ic * gst + q) * N;
       const DevStencil &sd = c->sten[TGPU_STEN_DELTA][ic], &st = c->sten[TGPU_STEN_THETA][ic];
-      adj_conv(c, ic, 1, sd, sd.d_coef_adj, o, 1 + nd);
+      const int vd[tgpu::kMaxRb] = {-1, 0, 1, 2};   // outputs: the scalar sum, then one per dimension
+      adj_conv(c, ic, 1, sd, sd.d_coef_adj, o, 1 + nd, vd);
       adj_conv(c, ic, 1, st, st.d_coef_fwd, o + nd + 1, 1);
     }
     tgpu::launch_jtv_local(c->d_x, c->d_vext, c->d_zero, d_w, c->d_adj_g, gst, 1, d_out, c->stream);
@@ -944,12 +959,7 @@ void objective_grad_device(Ctx *c, const double *d_x, int kind, int icomp, doubl
   if (kind != TGPU_OBJ_OMEGA && kind != TGPU_OBJ_GAMMA) throw Error(TGPU_ERR_ARG, "objective kind");
   if (kind == TGPU_OBJ_GAMMA && (icomp < 0 || icomp >= g.ncomp)) throw Error(TGPU_ERR_ARG, "component index");
   const bool att = kind == TGPU_OBJ_OMEGA && g.attraction;
-  if (att) {
-    for (int d = 0; d < g.ndim; d++)
-      if (c->g.bc[d][0] == TGPU_BC_REFLECT || c->g.bc[d][1] == TGPU_BC_REFLECT)
-        throw Error(TGPU_ERR_UNSUPPORTED, "free-energy gradient with attraction and reflecting boundaries");
-    ensure_adjoint(c);
-  }
+  if (att) ensure_adjoint(c);
   const double *S = att ? attraction_sums(c, d_x) : c->d_conv;
   tgpu::launch_objective_grad(d_x, c->d_vext, S, c->d_wf, c->d_wb, c->oc, kind, icomp, d_gx, d_gv,
                               att ? c->d_adj_chan : nullptr, c->stream);

@@ -52,10 +52,12 @@ __device__ __forceinline__ long pad_center(long i)
 // ---------------------------------------------------------------------------
 // Padding: resolve each padded position to a source node or a sentinel with
 // the reference's dimension order (the first out-of-range dimension decides).
+// With no_mirror, mirrored positions read 0: the zero extension of a field that the transposed sums of a
+// problem with reflecting boundaries start from (their mirrored contributions are folded back separately).
 template <typename T>
 __global__ void k_pad(const double *__restrict__ src, T *__restrict__ dst, int nch, const double *__restrict__ bulk,
                       const int *__restrict__ signmask, const int *__restrict__ zcomp,
-                      const signed char *__restrict__ zero)
+                      const signed char *__restrict__ zero, int no_mirror)
 {
   const long NP = c_g.NP;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < NP; p += (long)gridDim.x * blockDim.x) {
@@ -78,6 +80,7 @@ __global__ void k_pad(const double *__restrict__ src, T *__restrict__ dst, int n
       if (sent == kSentBulk) v = bulk[ch];
       else if (sent == kSentWall) v = 0.0;
       else if (sent != 0) v = __longlong_as_double(0x7ff8000000000000ULL);
+      else if (no_mirror && refl) v = 0.0;
       else {
         v = src[(long)ch * c_g.N + node];
         const int zc = zcomp[ch];
@@ -91,10 +94,10 @@ __global__ void k_pad(const double *__restrict__ src, T *__restrict__ dst, int n
 
 template <typename T>
 void launch_pad(const double *src, T *dst, int nch, const double *bulk, const int *signmask, const int *zcomp,
-                const signed char *zero, bool, cudaStream_t s)
+                const signed char *zero, bool no_mirror, cudaStream_t s)
 {
   // bulk/signmask/zcomp live in device memory (small arrays set up by the caller)
-  k_pad<T><<<1184, kThreads, 0, s>>>(src, dst, nch, bulk, signmask, zcomp, zero);
+  k_pad<T><<<1184, kThreads, 0, s>>>(src, dst, nch, bulk, signmask, zcomp, zero, no_mirror ? 1 : 0);
 }
 template void launch_pad<double>(const double *, double *, int, const double *, const int *, const int *,
                                  const signed char *, bool, cudaStream_t);
@@ -1214,6 +1217,69 @@ void launch_hw_correct(const double *field, long fcs, int ffirst, const DevStenc
   }
   k_hw_correct<<<(ntargets + 127) / 128, 128, 0, s>>>(field, fcs, ffirst, th[0], th[1], de[0], de[1], targets,
                                                        ntargets, zero, bnodes, fmask, conv);
+}
+
+// Reflecting boundaries in the transposed sums.  A forward sum reads a mirrored
+// position p (beyond a reflecting boundary) as its interior image m(p), with a
+// sign flip of vector channels; its transpose therefore evaluates the transposed
+// sum T(p) = sum_s coef_s in(p - o_s) also at mirrored positions (the input is
+// the zero extension, k_pad with no_mirror, read at interior nodes only) and adds sign T(p) into out(m(p)).
+// One thread per padded position; mirrored positions of one interior node come
+// from several threads: FP64 atomic additions.
+struct FoldOut {
+  double *p[kMaxRb];
+  int signmask[kMaxRb];   // bit d: the output flips sign under a reflection in dimension d
+};
+
+__global__ void k_reflect_fold(const double *__restrict__ in, long cstride, int nin, const short *__restrict__ off,
+                               const double *__restrict__ coef, int L, int nout, FoldOut out)
+{
+  const long NP = c_g.NP;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < NP; p += (long)gridDim.x * blockDim.x) {
+    const int q[3] = {(int)(p % c_g.P[0]), (int)((p / c_g.P[0]) % c_g.P[1]), (int)(p / ((long)c_g.P[0] * c_g.P[1]))};
+    int refl = 0, idx[3] = {0, 0, 0};
+    bool ok = true;
+    for (int d = 0; d < c_g.ndim; d++) {
+      const int m = c_g.map[d][q[d]];
+      if (m < 0) { ok = false; break; }
+      if (m & kReflBit) refl |= 1 << d;
+      idx[d] = m & ~kReflBit;
+    }
+    if (!ok || !refl) continue;
+    const long node = idx[0] + (long)c_g.nx[0] * (idx[1] + (long)c_g.nx[1] * idx[2]);
+    double t[kMaxRb];
+    for (int o = 0; o < nout; o++) t[o] = 0.0;
+    for (int s = 0; s < L; s++) {
+      // only reads from interior nodes p - o_s exist (a periodic image in the halo is the same read landing
+      // at another padded position, counted there)
+      const short *os = off + (long)s * 3;
+      long qi = 0;
+      bool inb = true;
+      for (int d = 0; d < c_g.ndim; d++) {
+        const int qq = q[d] - os[d];
+        if (qq < c_g.h[d] || qq >= c_g.h[d] + c_g.nx[d]) { inb = false; break; }
+        qi += (long)qq * c_g.pstride[d];
+      }
+      if (!inb) continue;
+      for (int o = 0; o < nout; o++)
+        for (int c = 0; c < nin; c++) t[o] += coef[((long)s * nout + o) * nin + c] * in[(long)c * cstride + qi];
+    }
+    for (int o = 0; o < nout; o++) {
+      const double v = (__popc(refl & out.signmask[o]) & 1) ? -t[o] : t[o];
+      if (v != 0.0) atomicAdd(out.p[o] + node, v);
+    }
+  }
+}
+
+void launch_reflect_fold(const double *in, long cstride, int nin, const short *off, const double *coef, int L,
+                         double *const *outs, const int *signmask, int nout, cudaStream_t s)
+{
+  FoldOut o{};
+  for (int k = 0; k < nout; k++) {
+    o.p[k] = outs[k];
+    o.signmask[k] = signmask[k];
+  }
+  k_reflect_fold<<<1184, kThreads, 0, s>>>(in, cstride, nin, off, coef, L, nout, o);
 }
 
 // Transpose of the hard-wall correction: the density column of every boundary node j receives, from each

@@ -382,6 +382,8 @@ void launch_hw_correct(const double *field, long field_cstride, int field_first,
                        const DevStencil *delta, const DevStencil *uatt, const int *targets, int ntargets,
                        const signed char *zero, const int *bnodes, const short *fmask, double *conv,
                        cudaStream_t s);
+void launch_reflect_fold(const double *in, long cstride, int nin, const short *off, const double *coef, int L,
+                         double *const *outs, const int *signmask, int nout, cudaStream_t s);
 void launch_hw_correct_t(const double *w, const DevStencil *theta, const DevStencil *delta, const int *targets,
                          int ntargets, const signed char *zero, const int *bnodes, const short *fmask, double *out,
                          cudaStream_t s);
