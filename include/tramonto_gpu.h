@@ -276,6 +276,27 @@ typedef struct {
 int tgpu_wall_field_device(const tgpu_wall_field *f, double *d_out);
 /* the same into host memory out [N] */
 int tgpu_wall_field_host(const tgpu_wall_field *f, double *out);
+/* Mean-field attraction stencils for the reference's other pair potentials and cores (THETA_PAIRPOT_RCUT
+ * with Type_pairPot and the core that Type_attr selects, src/dft_defs_stencil.c:85-103):
+ *   pot         TGPU_PAIR_LJ12_6_CS, TGPU_PAIR_YUKAWA_CS, TGPU_PAIR_EXP_CS, TGPU_PAIR_SW (Type_pairPot values)
+ *   core_r      LJ only: TGPU_CORE_SIGMA, TGPU_CORE_UMIN, TGPU_CORE_UCSZERO, TGPU_CORE_SIGTOUMIN (Type_CoreATT_R)
+ *   core_const  TGPU_CORECONST_UCONST (u held at its core value), TGPU_CORECONST_ZERO (Type_CoreATT_CONST)
+ *   rmin, rzero LJ: the potential's minimum (tgpu_lj_rmin) and the zero of its cut-and-shifted form
+ *   kappa       YukawaK_ff: K sigma for Yukawa, the decay length for the exponential
+ * The Yukawa and exponential weights call exp(), whose last bit may differ between the host and the GPU: their
+ * device tables agree with the host's to rounding; the LJ and square-well tables are bit-identical. */
+enum { TGPU_PAIR_LJ12_6_CS = 0, TGPU_PAIR_YUKAWA_CS = 3, TGPU_PAIR_EXP_CS = 4, TGPU_PAIR_SW = 5 };
+enum { TGPU_CORE_SIGMA = 0, TGPU_CORE_UMIN = 1, TGPU_CORE_UCSZERO = 2, TGPU_CORE_SIGTOUMIN = 3 };
+enum { TGPU_CORECONST_UCONST = 0, TGPU_CORECONST_ZERO = 1 };
+typedef struct {
+  int pot, core_r, core_const;
+  double sigma, eps_over_kT, rcut;
+  double rmin, rzero, kappa;
+} tgpu_pairpot;
+int tgpu_make_attraction_stencil(const tgpu_pairpot *pp, int ndim, const double *esize, int device, int capacity,
+                                 short *offsets, double *weights, double *hw, double *volume);
+/* the attractive part u_att(r) in kT of the pair potential pp (pairPot_ATT_CS_switch, src/dft_switch_pairPot.c) */
+double tgpu_pairpot_att(double r, const tgpu_pairpot *pp);
 /* r of the minimum of the cut-and-shifted LJ 12-6 potential, located by the
  * search of pairPot_find_rmin (src/dft_pairPot.c:98-152) */
 double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0);

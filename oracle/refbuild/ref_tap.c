@@ -78,7 +78,7 @@ int tref_setup(const char *dir)
  * Nrho_bar_s Type_func Type_attr ATTInA22Block Lhard_surf Nlists_HW Nwall
  * Type_bc[3][2] Phys2Unk_first[DENSITY,HSRHOBAR,MF_EQ] Nzone Nodes_x_box[3]
  * Max_sten_length[3] Pflag[3] Iguess Type_interface Mesh_coarsening Coarser_jac
- * Nnodes_per_el_V Type_pairPot Lcut_jac */
+ * Nnodes_per_el_V Type_pairPot Lcut_jac Type_CoreATT_R Type_CoreATT_CONST */
 int tref_info_ints(int *o)
 {
   int k = 0, i;
@@ -95,13 +95,15 @@ int tref_info_ints(int *o)
   for (i = 0; i < 3; i++) o[k++] = Pflag[i];
   o[k++] = Iguess; o[k++] = Type_interface; o[k++] = Mesh_coarsening; o[k++] = Coarser_jac;
   o[k++] = Nnodes_per_el_V; o[k++] = Type_pairPot; o[k++] = Lcut_jac;
+  o[k++] = Type_CoreATT_R; o[k++] = Type_CoreATT_CONST;
   return k;
 }
 
 /* doubles: Esize_x[3] Size_x[3] VEXT_MAX then per component (NCOMP_MAX each):
  * HS_diam Rho_b Betamu_hs_ex Betamu_att Inv_rad Inv_4pir Inv_4pirsq
  * Fac_overlap_hs, then Rhobar_b[10] Dphi_Drhobar_b[10], Avdw[NCOMP_MAX^2],
- * Eps_ff Sigma_ff Cut_ff [NCOMP_MAX^2 each], Temp, Jac_threshold */
+ * Eps_ff Sigma_ff Cut_ff [NCOMP_MAX^2 each], Temp, Jac_threshold, then YukawaK_ff Rmin_ff Rzero_ff
+ * [NCOMP_MAX^2 each] */
 int tref_info_doubles(double *o)
 {
   int k = 0, i, j;
@@ -124,6 +126,9 @@ int tref_info_doubles(double *o)
   for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = Cut_ff[i][j];
   o[k++] = Temp;
   o[k++] = Jac_threshold;
+  for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = YukawaK_ff[i][j];
+  for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = Rmin_ff[i][j];
+  for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = Rzero_ff[i][j];
   return k;
 }
 

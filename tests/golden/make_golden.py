@@ -101,6 +101,15 @@ def cases():
                "Rho_b_0[icomp]": "0.6", "ATTInA22Block": "0 30 0 0 0", "L_Schur": "1 0 100"}
     for name, func in (("rough3d_fmt2", "1 0"), ("rough3d_fmt4", "3 0")):
         c[name] = deck("GEOM3_PLANE_ROUGH_3D", dict(rough3d, **{"Type_func (": func}), surfaces=surf3d)
+    # the LJ1 fluid with the other mean-field kernels: LJ 12-6 cores (Type_attr 1: zero inside sigma; 3: zero
+    # inside sigma, u(r_min) from sigma to r_min), Yukawa (K sigma = 1.8), exponential (decay length 0.5) and
+    # square-well (range 1.5 sigma) attractions
+    mf = {"ATTInA22Block": MF_UNKNOWNS, "L_Schur": SCHUR_LINSOLVE}
+    c["lj1d_sigzero"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "1 0"}))
+    c["lj1d_jdc"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "3 0"}))
+    c["yuk1d_mf"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "0 3", "YukawaK_ff[i][j]": "1.8"}))
+    c["exp1d_mf"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "0 4", "YukawaK_ff[i][j]": "0.5"}))
+    c["sw1d_mf"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "0 5", "Cut_ff[i][j]": "1.5"}))
     return c
 
 

@@ -76,3 +76,28 @@ def test_device_builder_matches_reference_tables(case):
         assert np.abs(w2 - w).max() <= 1e-14 * np.abs(w).max(), (case, t, idx)
         if hw is not None:
             assert np.abs(h2 - hw).max() <= 1e-14 * np.abs(hw).max(), (case, t, idx)
+
+
+POTS = [("lj_sigma_zero", dict(pot=0, core_r=0, core_const=1)), ("lj_jdc", dict(pot=0, core_r=3, core_const=0)),
+        ("yukawa", dict(pot=3, core_r=1, core_const=0, kappa=1.8)), ("exp", dict(pot=4, core_r=1, core_const=0, kappa=0.5)),
+        ("square_well", dict(pot=5, core_r=1, core_const=0))]
+
+
+@pytest.mark.parametrize("name,pp", POTS, ids=[n for n, _ in POTS])
+@pytest.mark.parametrize("ndim,h", [(1, 0.05), (3, 0.1)])
+def test_attraction_stencils_of_other_pair_potentials(name, pp, ndim, h):
+    """Host and GPU builders of the other mean-field kernels: bit-identical for the LJ cores and the square
+    well (pure arithmetic), within 1e-14 for Yukawa and exponential (exp() of two libraries)."""
+    from tramonto_gb300 import setup
+    rcut = 1.5 if name == "square_well" else 2.5
+    rmin = setup.lj_rmin(1.0, 1.0 / 1.2, rcut, h)
+    kw = dict(pp, sigma=1.0, eps=1.0 / 1.2, rcut=rcut, rmin=rmin)
+    oh, wh, hh = setup.make_attraction_stencil(ndim, [h] * ndim, with_hw=True, device=False, **kw)
+    od, wd, hd = setup.make_attraction_stencil(ndim, [h] * ndim, with_hw=True, device=True, **kw)
+    assert np.array_equal(oh, od)
+    if pp["pot"] in (3, 4):
+        assert np.abs(wh - wd).max() <= 1e-14 * np.abs(wh).max()
+        assert np.abs(hh - hd).max() <= 1e-14 * np.abs(hh).max()
+    else:
+        assert np.array_equal(wh.view(np.uint64), wd.view(np.uint64))
+        assert np.array_equal(hh.view(np.uint64), hd.view(np.uint64))

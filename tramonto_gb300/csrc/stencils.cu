@@ -11,9 +11,12 @@
 // for hard walls (merge_load_stencil :598-650); the table is finally
 // renormalised to the analytic volume (renormalize_stencil :685-711).
 // Weight functions: delta shell (src/dft_stencil_delta_R.c:34-79), theta ball
-// (src/dft_stencil_theta_R.c:34-75) and the WCA attraction
-// (src/dft_stencil_theta_uattr.c:35-158) with the cut-and-shifted
-// Lennard-Jones tail (src/dft_pairPot_LJ12_6.c:96-230).
+// (src/dft_stencil_theta_R.c:34-75) and the mean-field attraction
+// (src/dft_stencil_theta_uattr.c:35-158) with the attractive parts of the
+// cut-and-shifted pair potentials: Lennard-Jones 12-6 with the cores of
+// Type_CoreATT_R / Type_CoreATT_CONST (src/dft_pairPot_LJ12_6.c:96-230),
+// Yukawa (src/dft_pairPot_Yukawa.c:96-175), exponential
+// (src/dft_pairPot_EXP.c:98-170) and square well (src/dft_pairPot_SW.c:96-145).
 //
 // The per-element quadrature (elem_weights) is one __host__ __device__ routine.
 // The host builder (tgpu_make_stencil) runs it element by element and merges
@@ -23,7 +26,9 @@
 // nodes by first touch (the host's insertion order) and renormalises with a
 // sequential sum in table order.  This file is compiled without contraction of
 // multiply-adds (nvcc -fmad=false, host -ffp-contract=off), so both builders
-// perform the same IEEE operations and their tables are bit-identical.
+// perform the same IEEE operations and their tables are bit-identical (the
+// Yukawa and exponential weights call exp(), whose last bit may differ between
+// the host's and the GPU's libraries: those tables agree to rounding).
 //
 // Gauss-Legendre nodes are computed here (Newton iteration on the Legendre
 // recurrence) rather than taken from tables, so weights agree with the
@@ -103,36 +108,122 @@ struct StenSpec {
   int type, ndim;
   double esize[3];
   double R;                          // stencil radius
-  double sigma, eps, rcut, rmin;     // WCA attraction
+  double sigma, eps, rcut, rmin;     // mean-field attraction
+  int pot, core_r, core_const;       // pair potential, core range and core value (TGPU_PAIR_*, TGPU_CORE_*)
+  double rzero, kappa;               // LJ: zero of the cut-shifted potential; Yukawa K sigma / decay length
   int ext[3];                        // elements per half-axis
   int lo[3], n[3];                   // element box: first index and count per dimension
   int nel;                           // corners per element
 };
 
-// cut-and-shifted attractive tail with the core held at u(r_min) (Type_attr 0: ATTCORE_UMIN, CORECONST_UCONST)
+// r where the LJ core ends (uLJ12_6_ATT_CS's r_min for each Type_CoreATT_R)
+__host__ __device__ inline double lj_core_r(const StenSpec &p)
+{
+  if (p.core_r == TGPU_CORE_SIGMA) return p.sigma;
+  if (p.core_r == TGPU_CORE_UCSZERO) return p.rzero;
+  return p.rmin;   // UMIN, SIGTOUMIN
+}
+
+// The attractive part of the cut-and-shifted pair potential (pairPot_ATT_CS_switch): the LJ form is held at
+// its core value inside the core (or zero there with CORECONST_ZERO; zero inside sigma for SIGTOUMIN).
 __host__ __device__ inline double u_att_cs(double r, const StenSpec &p)
 {
+  if (p.pot == TGPU_PAIR_YUKAWA_CS) {
+    const double a = p.kappa * p.sigma;
+    const double cut = exp(-a * (p.rcut / p.sigma - 1.)) / (p.rcut / p.sigma);
+    if (r < p.sigma) return p.core_const == TGPU_CORECONST_ZERO ? 0.0 : p.eps * (1.0 - cut);
+    if (r <= p.rcut) return p.eps * exp(-a * (r / p.sigma - 1.)) / (r / p.sigma) - p.eps * cut;
+    return 0.0;
+  }
+  if (p.pot == TGPU_PAIR_EXP_CS) {
+    const double cut = exp(-(p.rcut - p.sigma) / p.kappa);
+    if (r < p.sigma) return p.core_const == TGPU_CORECONST_ZERO ? 0.0 : p.eps * (-1.0 + cut);
+    if (r <= p.rcut) return -p.eps * exp(-(r - p.sigma) / p.kappa) + p.eps * cut;
+    return 0.0;
+  }
+  if (p.pot == TGPU_PAIR_SW) {
+    if (r < p.sigma) return 0.0;
+    if (r <= p.rcut) return -p.eps;
+    return 0.0;
+  }
   const double s2 = p.sigma * p.sigma, s6 = s2 * s2 * s2;
   const double rc = 1.0 / p.rcut, rc2 = rc * rc, rc6 = rc2 * rc2 * rc2, rc12 = rc6 * rc6;
+  const double rm = lj_core_r(p);
+  if ((r < rm && p.core_const == TGPU_CORECONST_ZERO) || (r < p.sigma && p.core_r == TGPU_CORE_SIGTOUMIN)) return 0.0;
   if (r > p.rcut) return 0.0;
-  if (r < p.rmin) r = p.rmin;
+  if (r < rm) r = rm;
   const double ri = 1.0 / r, r2 = ri * ri, r6 = r2 * r2 * r2, r12 = r6 * r6;
   return 4.0 * p.eps * s6 * (s6 * (r12 - rc12) - (r6 - rc6));
 }
 
+// The attractive part without the cut and shift (pairPot_ATT_noCS_switch)
 double u_att_nocs(double r, const StenSpec &p)
 {
+  if (p.pot == TGPU_PAIR_YUKAWA_CS) {
+    if (r < p.sigma) return p.core_const == TGPU_CORECONST_ZERO ? 0.0 : p.eps;
+    return p.eps * exp(-p.kappa * p.sigma * (r / p.sigma - 1.)) / (r / p.sigma);
+  }
+  if (p.pot == TGPU_PAIR_EXP_CS) {
+    if (r < p.sigma) return p.core_const == TGPU_CORECONST_ZERO ? 0.0 : -p.eps;
+    return -p.eps * exp(-(r - p.sigma) / p.kappa);
+  }
+  if (p.pot == TGPU_PAIR_SW) return r < p.sigma ? 0.0 : -p.eps;
   const double s2 = p.sigma * p.sigma, s6 = s2 * s2 * s2;
-  if (r < p.rmin) r = p.rmin;
+  const double rm = lj_core_r(p);
+  if ((r < rm && p.core_const == TGPU_CORECONST_ZERO) || (r < p.sigma && p.core_r == TGPU_CORE_SIGTOUMIN)) return 0.0;
+  if (r < rm) r = rm;
   const double ri = 1.0 / r, r2 = ri * ri, r6 = r2 * r2 * r2, r12 = r6 * r6;
   return 4.0 * p.eps * s6 * (s6 * r12 - r6);
 }
 
+// The integral that sets the stencil's magnitude (pairPot_integral_switch)
 double u_integral(double r, const StenSpec &p)
 {
+  if (p.pot == TGPU_PAIR_YUKAWA_CS) {
+    const double a = p.kappa * p.sigma, c = a / p.sigma;
+    return 4 * kPi * p.eps * p.sigma * std::exp(a) * ((std::exp(-c * r) / (c * c)) * (-c * r - 1.0));
+  }
+  if (p.pot == TGPU_PAIR_EXP_CS) {
+    const double al = p.kappa, a3 = al * al * al;
+    return -4.0 * kPi * p.eps * std::exp(-(r - p.sigma) / al) * (-al * r * r + 2 * a3 * (-r / al - 1.));
+  }
+  if (p.pot == TGPU_PAIR_SW) return -(4.0 / 3.0) * kPi * p.eps * std::pow(r, 3);
   const double s2 = p.sigma * p.sigma, s6 = s2 * s2 * s2;
   const double ri = 1.0 / r, r3 = ri * ri * ri, r9 = r3 * r3 * r3;
   return 16 * kPi * p.eps * s6 * (-s6 * r9 / 9.0 + r3 / 3.0);
+}
+
+// The potential's inner core (pairPot_InnerCore_switch): [0, left) and [left, right) with value eps_core
+void inner_core(const StenSpec &p, double *left, double *right, double *eps_core)
+{
+  *left = 0.0;
+  if (p.pot == TGPU_PAIR_LJ12_6_CS) {
+    *right = lj_core_r(p);
+    if (p.core_r == TGPU_CORE_SIGTOUMIN) *left = p.sigma;
+  } else {
+    *right = p.sigma;
+  }
+  *eps_core = (p.pot == TGPU_PAIR_SW || p.core_const == TGPU_CORECONST_ZERO) ? 0.0 : u_att_nocs(*right, p);
+}
+
+// StenTheta_uattr_sten_vol (src/dft_stencil_theta_uattr.c:39-87)
+double uattr_volume(const StenSpec &p)
+{
+  double left, right, epsc;
+  inner_core(p, &left, &right, &epsc);
+  const double rc = p.rcut, rm = right;
+  if (std::fabs(epsc) >= 1.e-8) {
+    if (std::fabs(left) < p.esize[0])
+      return (4.0 / 3.0) * kPi * std::pow(rm, 3.0) * u_att_nocs(rm, p) -
+             (4.0 / 3.0) * kPi * std::pow(rc, 3.0) * u_att_nocs(rc, p) + u_integral(rc, p) - u_integral(rm, p);
+    return (4.0 / 3.0) * kPi * std::pow(rm, 3.0) * u_att_nocs(rm, p) -
+           (4.0 / 3.0) * kPi * std::pow(rc, 3.0) * u_att_nocs(rc, p) -
+           (4.0 / 3.0) * kPi * std::pow(left, 3.0) * u_att_nocs(rm, p) +
+           (4.0 / 3.0) * kPi * std::pow(left, 3.0) * u_att_nocs(rc, p) + u_integral(rc, p) - u_integral(rm, p);
+  }
+  if (p.pot == TGPU_PAIR_SW) return u_integral(rc, p) - u_integral(rm, p);
+  return (u_integral(rc, p) - (4.0 / 3.0) * kPi * std::pow(rc, 3.0) * u_att_nocs(rc, p)) -
+         (u_integral(rm, p) - (4.0 / 3.0) * kPi * std::pow(rm, 3.0) * u_att_nocs(rc, p));
 }
 
 double u_lj_cs(double r, double sigma, double eps, double rc)
@@ -376,8 +467,7 @@ __host__ __device__ inline void elem_ijk(const StenSpec &s, long e, int *ijk)
   ijk[0] = s.lo[0] + (int)(e / s.n[1]);
 }
 
-StenSpec make_spec(int type, int ndim, const double *esize, double hs_diam, double sigma, double eps, double rcut,
-                   double rmin, double *vol)
+StenSpec make_spec(int type, int ndim, const double *esize, double hs_diam, const tgpu_pairpot &pp, double *vol)
 {
   StenSpec s;
   std::memset(&s, 0, sizeof(s));
@@ -391,14 +481,17 @@ StenSpec make_spec(int type, int ndim, const double *esize, double hs_diam, doub
     s.R = hs_diam / 2.0;
     *vol = kPi * std::pow(hs_diam, 3) / 6.0;
   } else {
-    s.R = rcut;
-    s.sigma = sigma;
-    s.eps = eps;
-    s.rcut = rcut;
-    s.rmin = rmin;
-    // StenTheta_uattr_sten_vol (src/dft_stencil_theta_uattr.c:39-88), WCA core held at u(r_min)
-    *vol = (4.0 / 3.0) * kPi * std::pow(rmin, 3.0) * u_att_nocs(rmin, s) -
-           (4.0 / 3.0) * kPi * std::pow(rcut, 3.0) * u_att_nocs(rcut, s) + u_integral(rcut, s) - u_integral(rmin, s);
+    s.R = pp.rcut;
+    s.sigma = pp.sigma;
+    s.eps = pp.eps_over_kT;
+    s.rcut = pp.rcut;
+    s.rmin = pp.rmin;
+    s.rzero = pp.rzero;
+    s.kappa = pp.kappa;
+    s.pot = pp.pot;
+    s.core_r = pp.core_r;
+    s.core_const = pp.core_const;
+    *vol = uattr_volume(s);
   }
   s.nel = 1 << ndim;
   for (int d = 0; d < 3; d++) {
@@ -649,13 +742,22 @@ double find_rmin(double sigma, double eps, double rcut, double h0)
   return rmin;
 }
 
-int make_stencil(bool device, int type, int ndim, const double *esize, double hs_diam, double sigma, double eps,
-                 double rcut, double rmin, int capacity, short *offsets, double *weights, double *hw, double *volume)
+int make_stencil(bool device, int type, int ndim, const double *esize, double hs_diam, const tgpu_pairpot &pp,
+                 int capacity, short *offsets, double *weights, double *hw, double *volume)
 {
   if (ndim < 1 || ndim > 3 || !esize) return TGPU_ERR_ARG;
   if (type != TGPU_STEN_DELTA && type != TGPU_STEN_THETA && type != TGPU_STEN_UATT) return TGPU_ERR_ARG;
+  if (type == TGPU_STEN_UATT) {
+    if (pp.pot != TGPU_PAIR_LJ12_6_CS && pp.pot != TGPU_PAIR_YUKAWA_CS && pp.pot != TGPU_PAIR_EXP_CS &&
+        pp.pot != TGPU_PAIR_SW)
+      return TGPU_ERR_UNSUPPORTED;
+    if (pp.core_r < TGPU_CORE_SIGMA || pp.core_r > TGPU_CORE_SIGTOUMIN || pp.core_const < TGPU_CORECONST_UCONST ||
+        pp.core_const > TGPU_CORECONST_ZERO || !(pp.rcut > 0.0) || !(pp.sigma > 0.0))
+      return TGPU_ERR_ARG;
+    if ((pp.pot == TGPU_PAIR_YUKAWA_CS || pp.pot == TGPU_PAIR_EXP_CS) && !(pp.kappa > 0.0)) return TGPU_ERR_ARG;
+  }
   double vol = 0.0;
-  const StenSpec s = make_spec(type, ndim, esize, hs_diam, sigma, eps, rcut, rmin, &vol);
+  const StenSpec s = make_spec(type, ndim, esize, hs_diam, pp, &vol);
   Table t;
   if (device) {
     const int st = build_device(s, vol, t);
@@ -682,31 +784,56 @@ double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0
   return find_rmin(sigma, eps_over_kT, rcut, esize0);
 }
 
+static tgpu_pairpot lj_umin(double sigma, double eps_over_kT, double rcut, double rmin)
+{
+  tgpu_pairpot pp;
+  std::memset(&pp, 0, sizeof(pp));
+  pp.pot = TGPU_PAIR_LJ12_6_CS;
+  pp.core_r = TGPU_CORE_UMIN;
+  pp.core_const = TGPU_CORECONST_UCONST;
+  pp.sigma = sigma;
+  pp.eps_over_kT = eps_over_kT;
+  pp.rcut = rcut;
+  pp.rmin = rmin;
+  return pp;
+}
+
 double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double rmin)
 {
-  StenSpec p;
-  std::memset(&p, 0, sizeof(p));
-  p.sigma = sigma;
-  p.eps = eps_over_kT;
-  p.rcut = rcut;
-  p.rmin = rmin;
-  return u_att_cs(r, p);
+  double vol = 0.0;
+  const double es[3] = {1.0, 1.0, 1.0};
+  return u_att_cs(r, make_spec(TGPU_STEN_UATT, 1, es, 0.0, lj_umin(sigma, eps_over_kT, rcut, rmin), &vol));
+}
+
+double tgpu_pairpot_att(double r, const tgpu_pairpot *pp)
+{
+  if (!pp) return 0.0;
+  double vol = 0.0;
+  const double es[3] = {1.0, 1.0, 1.0};
+  return u_att_cs(r, make_spec(TGPU_STEN_UATT, 1, es, 0.0, *pp, &vol));
 }
 
 int tgpu_make_stencil(int type, int ndim, const double *esize, double hs_diam, double sigma, double eps_over_kT,
                       double rcut, double rmin, int capacity, short *offsets, double *weights, double *hw,
                       double *volume)
 {
-  return make_stencil(false, type, ndim, esize, hs_diam, sigma, eps_over_kT, rcut, rmin, capacity, offsets, weights,
-                      hw, volume);
+  return make_stencil(false, type, ndim, esize, hs_diam, lj_umin(sigma, eps_over_kT, rcut, rmin), capacity, offsets,
+                      weights, hw, volume);
 }
 
 int tgpu_make_stencil_device(int type, int ndim, const double *esize, double hs_diam, double sigma,
                              double eps_over_kT, double rcut, double rmin, int capacity, short *offsets,
                              double *weights, double *hw, double *volume)
 {
-  return make_stencil(true, type, ndim, esize, hs_diam, sigma, eps_over_kT, rcut, rmin, capacity, offsets, weights,
-                      hw, volume);
+  return make_stencil(true, type, ndim, esize, hs_diam, lj_umin(sigma, eps_over_kT, rcut, rmin), capacity, offsets,
+                      weights, hw, volume);
+}
+
+int tgpu_make_attraction_stencil(const tgpu_pairpot *pp, int ndim, const double *esize, int device, int capacity,
+                                 short *offsets, double *weights, double *hw, double *volume)
+{
+  if (!pp) return TGPU_ERR_ARG;
+  return make_stencil(device != 0, TGPU_STEN_UATT, ndim, esize, 0.0, *pp, capacity, offsets, weights, hw, volume);
 }
 
 }  // extern "C"

@@ -74,6 +74,45 @@ def make_stencil(stype, ndim, esize, hs_diam=0.0, sigma=1.0, eps=1.0, rcut=0.0, 
     return off, w, hw
 
 
+PAIR_LJ12_6_CS, PAIR_YUKAWA_CS, PAIR_EXP_CS, PAIR_SW = 0, 3, 4, 5
+CORE_SIGMA, CORE_UMIN, CORE_UCSZERO, CORE_SIGTOUMIN = 0, 1, 2, 3
+CORECONST_UCONST, CORECONST_ZERO = 0, 1
+# Type_attr (MFPAIR_*) -> (Type_CoreATT_R, Type_CoreATT_CONST), as src/dft_defs_stencil.c:85-103 sets them
+MFPAIR_CORES = {0: (CORE_UMIN, CORECONST_UCONST), 1: (CORE_SIGMA, CORECONST_ZERO), 2: (CORE_SIGMA, CORECONST_UCONST),
+                3: (CORE_SIGTOUMIN, CORECONST_UCONST), 4: (CORE_UCSZERO, CORECONST_ZERO)}
+
+
+class _PairPot(C.Structure):
+    _fields_ = [("pot", C.c_int), ("core_r", C.c_int), ("core_const", C.c_int), ("sigma", C.c_double),
+                ("eps_over_kT", C.c_double), ("rcut", C.c_double), ("rmin", C.c_double), ("rzero", C.c_double),
+                ("kappa", C.c_double)]
+
+
+def make_attraction_stencil(ndim, esize, pot=PAIR_LJ12_6_CS, core_r=CORE_UMIN, core_const=CORECONST_UCONST,
+                            sigma=1.0, eps=1.0, rcut=2.5, rmin=0.0, rzero=0.0, kappa=0.0, with_hw=False, device=None):
+    """Mean-field attraction stencil of any of the reference's attraction pair potentials and cores
+    (tgpu_make_attraction_stencil); device as in make_stencil."""
+    lib = _lib()
+    lib.tgpu_make_attraction_stencil.restype = C.c_int
+    lib.tgpu_make_attraction_stencil.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                                 C.c_void_p, C.c_void_p, C.c_void_p]
+    if device is None:
+        device = ndim == 3 and _gpu_visible()
+    pp = _PairPot(int(pot), int(core_r), int(core_const), float(sigma), float(eps), float(rcut), float(rmin),
+                  float(rzero), float(kappa))
+    es = (C.c_double * 3)(*(list(esize) + [0.0] * (3 - len(esize))))
+    L = lib.tgpu_make_attraction_stencil(C.byref(pp), ndim, es, int(bool(device)), 0, None, None, None, None)
+    if L < 0:
+        raise RuntimeError(f"tgpu_make_attraction_stencil failed ({L})")
+    off = np.zeros((L, ndim), np.int16)
+    w = np.zeros(L)
+    hw = np.zeros((L, 1 << ndim)) if with_hw else None
+    L2 = lib.tgpu_make_attraction_stencil(C.byref(pp), ndim, es, int(bool(device)), L, off.ctypes.data,
+                                          w.ctypes.data, hw.ctypes.data if with_hw else None, None)
+    assert L2 == L
+    return off, w, hw
+
+
 def lj_rmin(sigma, eps, rcut, esize0):
     return _lib().tgpu_lj_rmin(sigma, eps, rcut, esize0)
 
@@ -136,8 +175,10 @@ def bulk_constants(functional, hs_diam, rho_b, attraction=False, uatt_stencils=N
 
 
 def build_problem(ndim, nx, esize, bc, hs_diam, rho_b, functional=FMT1, attraction=False, sigma=None, eps=None,
-                  rcut=None, vext=None, zero_density=None, vext_max=10.0):
-    """Assemble a Problem with generated stencils and bulk constants."""
+                  rcut=None, vext=None, zero_density=None, vext_max=10.0, pair=None):
+    """Assemble a Problem with generated stencils and bulk constants.  pair (optional) selects the attraction's
+    pair potential and core: dict(pot=PAIR_*, core_r=CORE_*, core_const=CORECONST_*, kappa=...); the default is
+    the cut-and-shifted LJ 12-6 with its core held at u(r_min) (Type_attr 0)."""
     nc = len(rho_b)
     st = {}
     for i in range(nc):
@@ -148,8 +189,12 @@ def build_problem(ndim, nx, esize, bc, hs_diam, rho_b, functional=FMT1, attracti
         for i in range(nc):
             for j in range(nc):
                 rmin = lj_rmin(sigma[i][j], eps[i][j], rcut[i][j], esize[0])
-                uat[i + nc * j] = make_stencil(UATT, ndim, esize, sigma=sigma[i][j], eps=eps[i][j], rcut=rcut[i][j],
-                                               rmin=rmin)
+                if pair is None:
+                    uat[i + nc * j] = make_stencil(UATT, ndim, esize, sigma=sigma[i][j], eps=eps[i][j],
+                                                   rcut=rcut[i][j], rmin=rmin)
+                else:
+                    uat[i + nc * j] = make_attraction_stencil(ndim, esize, sigma=sigma[i][j], eps=eps[i][j],
+                                                              rcut=rcut[i][j], rmin=rmin, **pair)
                 st[(UATT, i + nc * j)] = uat[i + nc * j]
     b = bulk_constants(functional, hs_diam, rho_b, attraction, uat, nc)
     N = int(np.prod(nx[:ndim]))
