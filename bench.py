@@ -394,6 +394,7 @@ def main():
     t_wca_tc = s.time_stencil_sum(UATT, 0, native.FP16TC, reps=5)
     t_wca32 = s.time_stencil_sum(UATT, 0, native.FP32, reps=5)
     t_wca64 = s.time_stencil_sum(UATT, 0, native.FP64, reps=1)
+    t_wca_ff = s.time_stencil_sum(UATT, 0, native.FILL_FF, reps=rep64)
     L_att = len(p.stencils[(UATT, 0)][1])
     flops_att = 2.0 * p.nnodes * L_att
     mma_flops = tc_issued_flops(p)
@@ -475,6 +476,17 @@ def main():
                          "issued_mma": "3 MMAs (hi*hi, hi*lo, lo*hi) of 128x64x16 per K-step of each stencil line",
                          "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
                          "fp64_ms_per_launch": t_wca64},
+            # the other large kernel of a solve: the float-float attraction sum of the accurate fills, bound by
+            # the FP32 issue rate (12 FP32 operations per term; nominal 152 SMs x 128 lanes x clock)
+            "fill_kernel": {"kernel": "k_conv_slab_ff (float-float attraction sum of the accurate fills)",
+                            "bound": "fp32 issue", "ms_per_launch": t_wca_ff,
+                            "achieved": 12.0 * flops_att / 2.0 / (t_wca_ff * 1e-3) / 1e12,
+                            "peak": 152 * 128 * (clk.summary().get("sm_max_mhz") or 2070.0) * 1e6 / 1e12,
+                            "unit": "Top/s (FP32 operations)",
+                            "frac": (12.0 * flops_att / 2.0 / (t_wca_ff * 1e-3)) /
+                                    (152 * 128 * (clk.summary().get("sm_max_mhz") or 2070.0) * 1e6),
+                            "peak_source": "nominal FP32 issue rate at the maximum SM clock",
+                            "logical_tflops": flops_att / (t_wca_ff * 1e-3) / 1e12},
             "cpu_baseline": cb,
             "breakdown_ms": {"fill_fp64": t_fill, "fill_float_float": t_fill_ff, "fill_fp32": t_fill32,
                              "schur_apply_fp32": t_apply32,

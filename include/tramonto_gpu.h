@@ -333,7 +333,8 @@ const char *tgpu_noalloc_last_error(void);
 
 /* Benchmark hook: device time (CUDA events on the handle's stream) of one
  * forward stencil sum with stencil (type, index) over the density of the last
- * fill, in TGPU_FP64 or TGPU_FP32, averaged over reps launches. */
+ * fill, in TGPU_FP64, TGPU_FP32, TGPU_FP16TC or TGPU_FILL_FF (the float-float sum
+ * of the accurate fills), averaged over reps launches. */
 int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum);
 
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */

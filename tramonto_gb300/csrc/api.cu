@@ -264,6 +264,28 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
       return;
     }
   }
+  if (!f32 && c->ff_on && (nin > 1 || nout > 1)) {
+    // multi-channel sums as one single-coefficient float-float sum per channel
+    const std::vector<DevStencil::Lines> &tabs = tr ? st.ff_tr : st.ff_fwd;
+    bool ok = (int)tabs.size() == std::max(nin, nout) && (nin == 1 || nout == 1);
+    for (const auto &ln : tabs) ok = ok && ln.nplanes > 0 && ln.ff_ok;
+    if (ok) {
+      float *hi = c->d_pad32, *lo = c->d_pad32 + NP;
+      for (int q = 0; q < (int)tabs.size(); q++) {
+        const DevStencil::Lines &ln = tabs[q];
+        if (q == 0 || nin > 1) {
+          tgpu::launch_split_hilo(c->d_pad + (long)(ch0 + (nin > 1 ? q : 0)) * NP, NP, hi, lo, c->stream);
+          c->stats.kernel_launches++;
+        }
+        tgpu::launch_conv_slab_ff(hi, lo, NP, ln.d_planes, ln.nplanes, ln.d_lines, ln.d_w, ln.d_w_lo,
+                                  outs[nout > 1 ? q : 0], ln.pitch, ln.ncols, ln.max_rows, ln.max_lines, ln.max_w,
+                                  c->dg.nx[0], c->dg.nx[1], c->dg.nx[2], c->stream);
+        c->stats.kernel_launches++;
+      }
+      c->stats.conv_launches++;
+      return;
+    }
+  }
   if (!f32 && c->ff_on && nin == 1 && nout == 1) {
     const DevStencil::Lines &ln = tr ? st.lines_tr : st.lines_fwd;
     if (ln.nplanes > 0 && ln.ncoef == 1 && ln.ff_ok) {
@@ -1234,6 +1256,17 @@ void build_device_tables(Ctx *c)
         // the forward table is [L][1 + nd] (one input), the transpose table [L][1 + nd] (one output)
         st.lines_fwd = build_lines(st, fwd, dg, c->stream, st.nout_fwd, 1);
         st.lines_tr = build_lines(st, tr, dg, c->stream, st.nin_tr, st.nin_tr);
+        // one table per coefficient for the float-float sums
+        for (int q = 0; q < st.nout_fwd; q++) {
+          std::vector<double> col(st.L);
+          for (int k = 0; k < st.L; k++) col[k] = fwd[(size_t)k * st.nout_fwd + q];
+          st.ff_fwd.push_back(build_lines(st, col, dg, c->stream));
+        }
+        for (int q = 0; q < st.nin_tr; q++) {
+          std::vector<double> col(st.L);
+          for (int k = 0; k < st.L; k++) col[k] = tr[(size_t)k * st.nin_tr + q];
+          st.ff_tr.push_back(build_lines(st, col, dg, c->stream));
+        }
       }
       if (nd == 3 && t == TGPU_STEN_UATT) tgpu::tc_build_tables(st.off, fwd, st.L, dg.h[1], st.tc, c->stream);
     }
@@ -1419,6 +1452,10 @@ int tgpu_destroy(tgpu_handle h)
         for (auto *L : {&st.lines_fwd, &st.lines_tr}) {
           dfree(L->d_planes); dfree(L->d_lines); dfree(L->d_w); dfree(L->d_w_lo);
         }
+        for (auto *V : {&st.ff_fwd, &st.ff_tr})
+          for (auto &L : *V) {
+            dfree(L.d_planes); dfree(L.d_lines); dfree(L.d_w); dfree(L.d_w_lo);
+          }
         tgpu::tc_free_tables(st.tc);
       }
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
@@ -1802,11 +1839,14 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     if (type < 0 || type > 2 || index < 0 || index >= (int)c->sten[type].size() || c->sten[type][index].L == 0)
       throw Error(TGPU_ERR_ARG, "no such stencil");
     if (reps < 1) throw Error(TGPU_ERR_ARG, "reps");
+    if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC && precision != TGPU_FILL_FF)
+      throw Error(TGPU_ERR_ARG, "precision");
     const bool f32 = precision == TGPU_FP32 || precision == TGPU_FP16TC;
     if (precision == TGPU_FP16TC && !c->tc_ready)
       throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
-    const bool tc_prev = c->tc_on;
+    const bool tc_prev = c->tc_on, ff_prev = c->ff_on;
     c->tc_on = precision == TGPU_FP16TC;
+    c->ff_on = precision == TGPU_FILL_FF;
     const DevStencil &st = c->sten[type][index];
     const int jc = type == TGPU_STEN_UATT ? index / c->dg.ncomp : index;
     const long N = c->dg.N;
@@ -1826,6 +1866,7 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     cudaEventDestroy(c->ev1);
     c->ev0 = c->ev1 = nullptr;
     c->tc_on = tc_prev;
+    c->ff_on = ff_prev;
     tc_check(c);
     *ms_per_sum = ms / reps;
     return TGPU_OK;

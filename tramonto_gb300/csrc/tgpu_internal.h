@@ -291,6 +291,9 @@ struct DevStencil {
     bool ff_ok = false;                 // the float-float slab fits in shared memory
     bool mc_ok = false;                 // the multi-channel slab fits in shared memory
   } lines_fwd, lines_tr;
+  // float-float single-coefficient tables of a multi-channel stencil (3-D delta, one size): per forward
+  // output channel and per transpose input channel, for the accurate fills
+  std::vector<Lines> ff_fwd, ff_tr;
 };
 
 }  // namespace tgpu
