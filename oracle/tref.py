@@ -166,7 +166,7 @@ def _child_extract(deck_lines, surfaces_from, opts, q):
             ndim = int(ints[0])
             nnodes, nbox, nown, nunk, ncomp = (int(v) for v in ints[4:9])
             nlists = int(ints[14])
-            nel_v = int(ints[-3])
+            nel_v = int(ints[39])   # Nnodes_per_el_V (tref_info_ints order)
             lhard = int(ints[13])
             l2b = np.zeros(nown, np.int32)
             b2g = np.zeros(nbox, np.int32)

@@ -110,6 +110,10 @@ def cases():
     c["yuk1d_mf"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "0 3", "YukawaK_ff[i][j]": "1.8"}))
     c["exp1d_mf"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "0 4", "YukawaK_ff[i][j]": "0.5"}))
     c["sw1d_mf"] = deck("LJ1_FMT1_WCA_1D", dict(mf, **{"Type_attr Type_pairPot": "0 5", "Cut_ff[i][j]": "1.5"}))
+    # HS5's hard wall (boundary weights) with a WCA fluid (eps 1/1.2 kT, cut 2.5) at HS5's rho_b = 0.75: the
+    # mean-field stencil takes the hard-wall weights too
+    c["hslj1d_wall"] = deck("HS5_FMT1_1D", dict(mf, **{"Type_attr Type_pairPot": "0 0", "Eps_ff[i][j]": "0.8333333333333334",
+                                                   "Cut_ff[i][j]": "2.5", "Rho_b_0[icomp]": "0.75"}))
     return c
 
 

@@ -6,7 +6,7 @@ from goldens import load
 from tramonto_gb300 import setup
 
 CASES = ["hs1d_wall", "hs1d_reflect", "lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "hs1d_c1", "mix1d_fmt4", "rough3d_fmt2",
-         "lj1d_sigzero", "lj1d_jdc", "yuk1d_mf", "exp1d_mf", "sw1d_mf"]
+         "lj1d_sigzero", "lj1d_jdc", "yuk1d_mf", "exp1d_mf", "sw1d_mf", "hslj1d_wall"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -27,10 +27,10 @@ def test_stencils_match_reference(case):
                 kappa, rzero = d[221:257].reshape(6, 6)[i, j], d[293:329].reshape(6, 6)[i, j]
                 o2, w2, h2 = setup.make_attraction_stencil(p.ndim, p.esize, pot, core_r, core_c, sigma=sig[i, j],
                                                            eps=eps[i, j], rcut=cut[i, j], rmin=rmin, rzero=rzero,
-                                                           kappa=kappa)
+                                                           kappa=kappa, with_hw=hw is not None)
             else:
                 o2, w2, h2 = setup.make_stencil(t, p.ndim, p.esize, sigma=sig[i, j], eps=eps[i, j], rcut=cut[i, j],
-                                                rmin=rmin)
+                                                rmin=rmin, with_hw=hw is not None)
         assert np.array_equal(o2, off), (case, t, idx)
         assert np.abs(w2 - w).max() <= 1e-14 * np.abs(w).max(), (case, t, idx)
         if hw is not None:

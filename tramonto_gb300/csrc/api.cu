@@ -340,7 +340,8 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bo
       }
   }
   if (g.hard_surf && !c->hw_targets.empty()) {
-    tgpu::launch_hw_correct(field, N, 0, c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(), nullptr,
+    tgpu::launch_hw_correct(field, N, 0, c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(),
+                            g.attraction ? c->sten[TGPU_STEN_UATT].data() : nullptr, g.ncomp, true, g.attraction != 0,
                             c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero, c->d_bnodes, c->d_fmask,
                             c->d_conv, c->stream);
     c->stats.kernel_launches++;
@@ -852,9 +853,11 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
     }
     // hard-wall boundary weights: the transpose of the forward correction
     if (g.hard_surf && !c->hw_targets.empty()) {
-      tgpu::launch_hw_correct_t(d_w, c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(),
-                                c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero, c->d_bnodes, c->d_fmask,
-                                d_out, c->stream);
+      tgpu::launch_hw_correct_t(d_w, g.attraction ? d_w + (long)g.first_mf * N : nullptr,
+                                c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(),
+                                g.attraction ? c->sten[TGPU_STEN_UATT].data() : nullptr, g.ncomp, true,
+                                g.attraction != 0, c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero,
+                                c->d_bnodes, c->d_fmask, d_out, c->stream);
       c->stats.kernel_launches++;
     }
     // density columns exist only off zero-density nodes
@@ -955,6 +958,13 @@ const double *attraction_sums(Ctx *c, const double *d_x)
       double *o[1] = {S + (long)ic * N};
       conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o, 1, false);
     }
+  // hard-wall boundary weights of the mean-field stencils (int_stencil, src/dft_energy_CLSintsten.c:73-129)
+  if (g.hard_surf && !c->hw_targets.empty()) {
+    tgpu::launch_hw_correct(d_x + (long)g.first_rho * N, N, 0, nullptr, nullptr, c->sten[TGPU_STEN_UATT].data(),
+                            g.ncomp, false, true, c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero,
+                            c->d_bnodes, c->d_fmask, c->d_conv, c->stream);
+    c->stats.kernel_launches++;
+  }
   return S;
 }
 
@@ -997,6 +1007,12 @@ void objective_grad_device(Ctx *c, const double *d_x, int kind, int icomp, doubl
         const DevStencil &su = c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc];
         adj_conv(c, ic, 1, su, su.d_coef_fwd, o, 1);
       }
+    }
+    if (g.hard_surf && !c->hw_targets.empty()) {
+      tgpu::launch_hw_correct_t(nullptr, c->d_adj_chan, nullptr, nullptr, c->sten[TGPU_STEN_UATT].data(), g.ncomp,
+                                false, true, c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero, c->d_bnodes,
+                                c->d_fmask, d_gx, c->stream);
+      c->stats.kernel_launches++;
     }
     // densities at zero-density nodes are not unknowns of the sums (int_stencil skips them)
     tgpu::launch_mask_rows(d_gx + (long)g.first_rho * N, nullptr, c->d_vext, c->d_zero, 0, g.ncomp, 1, c->stream);
@@ -1396,8 +1412,6 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
       throw Error(TGPU_ERR_UNSUPPORTED, "functional outside FMT1..FMT4");
     if (g.attraction && g.att_in_a22)
       throw Error(TGPU_ERR_UNSUPPORTED, "mean field summed into the density rows (ATTInA22Block) is not implemented");
-    if (g.hard_surf && g.attraction)
-      throw Error(TGPU_ERR_UNSUPPORTED, "hard-wall boundary weights with mean-field stencils are not implemented");
     if (g.hard_surf && g.ncomp > 2) throw Error(TGPU_ERR_UNSUPPORTED, "hard walls with more than two components");
     const long N = nnodes(g);
     if (N > (1L << 31) / 4) throw Error(TGPU_ERR_ARG, "mesh too large for 32-bit stencil offsets");
@@ -1585,6 +1599,8 @@ int tgpu_finalize(tgpu_handle h)
     if (g.attraction)
       for (int k = 0; k < g.ncomp * g.ncomp; k++)
         if (c->sten[TGPU_STEN_UATT][k].L == 0) throw Error(TGPU_ERR_STATE, "missing attraction stencil");
+        else if (g.hard_surf && c->sten[TGPU_STEN_UATT][k].hw.empty())
+          throw Error(TGPU_ERR_STATE, "hard surfaces need the attraction stencils' corner weights");
     if (g.hard_surf && c->h_bnodes.empty()) throw Error(TGPU_ERR_STATE, "hard surfaces need tgpu_set_hard_wall");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     build_device_tables(c);

@@ -1146,9 +1146,16 @@ struct HwStencil {
   const double *w, *hw;
 };
 
-__device__ void hw_apply(const HwStencil &st, int kind, int jc, int jlist, const int *ijk, const double *field,
-                         long fcs, int ffirst, const signed char *zero, const int *bnodes, const short *fmask,
-                         double *acc)
+// The hard-wall stencils of up to two components: theta and delta per component, the mean-field
+// stencils per (output component, input component) pair
+struct HwSet {
+  HwStencil th[2], de[2], ua[4];
+};
+
+// kind 0: theta -> n3; 1: delta -> n2 [n1 n0] V2 [V1]; 2: mean field -> row orow (no prefactor)
+__device__ void hw_apply(const HwStencil &st, int kind, int orow, int jc, int jlist, const int *ijk,
+                         const double *field, long fcs, int ffirst, const signed char *zero, const int *bnodes,
+                         const short *fmask, double *acc)
 {
   const long N = c_g.N;
   const int nd = c_g.ndim;
@@ -1180,43 +1187,66 @@ __device__ void hw_apply(const HwStencil &st, int kind, int jc, int jlist, const
         acc[4 + d] += f * v * dw * rho;
         if (!c_g.single_size) acc[4 + nd + d] += f * c_g.inv_4pir[jc] * v * dw * rho;
       }
+    } else {                  // mean field
+      acc[orow] += dw * rho;
     }
   }
 }
 
-__global__ void k_hw_correct(const double *__restrict__ field, long fcs, int ffirst, HwStencil th0, HwStencil th1,
-                             HwStencil de0, HwStencil de1, const int *__restrict__ targets, int ntargets,
-                             const signed char *__restrict__ zero, const int *__restrict__ bnodes,
-                             const short *__restrict__ fmask, double *__restrict__ conv)
+// conv rows 0..nrb-1 (do_fmt) and nrb..nrb+ncomp-1 (do_mf) of the target nodes
+__global__ void k_hw_correct(const double *__restrict__ field, long fcs, int ffirst, HwSet hs, int do_fmt, int do_mf,
+                             const int *__restrict__ targets, int ntargets, const signed char *__restrict__ zero,
+                             const int *__restrict__ bnodes, const short *__restrict__ fmask,
+                             double *__restrict__ conv)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntargets) return;
   const long i = targets[t];
   int ijk[3];
   node_ijk(i, ijk);
-  double acc[kMaxRb];
-  for (int k = 0; k < kMaxRb; k++) acc[k] = 0.0;
-  for (int jc = 0; jc < c_g.ncomp && jc < 2; jc++) {
+  const int nc = c_g.ncomp;
+  double acc[kMaxRb + kMaxC];
+  for (int k = 0; k < kMaxRb + kMaxC; k++) acc[k] = 0.0;
+  for (int jc = 0; jc < nc && jc < 2; jc++) {
     const int jlist = (c_g.nlists <= 2) ? 0 : jc;
-    hw_apply(jc == 0 ? th0 : th1, 0, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
-    hw_apply(jc == 0 ? de0 : de1, 1, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
+    if (do_fmt) {
+      hw_apply(hs.th[jc], 0, 0, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
+      hw_apply(hs.de[jc], 1, 0, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
+    }
+    if (do_mf)
+      for (int ic = 0; ic < nc && ic < 2; ic++)
+        hw_apply(hs.ua[ic + 2 * jc], 2, c_g.nrb + ic, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
   }
-  for (int k = 0; k < c_g.nrb; k++) conv[(long)k * c_g.N + i] += acc[k];
+  if (do_fmt)
+    for (int k = 0; k < c_g.nrb; k++) conv[(long)k * c_g.N + i] += acc[k];
+  if (do_mf)
+    for (int ic = 0; ic < nc && ic < 2; ic++) conv[(long)(c_g.nrb + ic) * c_g.N + i] += acc[c_g.nrb + ic];
+}
+
+static HwSet hw_set(const DevStencil *theta, const DevStencil *delta, const DevStencil *uatt, int ncomp)
+{
+  HwSet h{};
+  for (int c = 0; c < 2 && c < ncomp; c++) {
+    if (theta && theta[c].L) h.th[c] = {theta[c].L, theta[c].d_off, theta[c].d_w, theta[c].d_hw};
+    if (delta && delta[c].L) h.de[c] = {delta[c].L, delta[c].d_off, delta[c].d_w, delta[c].d_hw};
+  }
+  if (uatt)
+    for (int jc = 0; jc < 2 && jc < ncomp; jc++)
+      for (int ic = 0; ic < 2 && ic < ncomp; ic++) {
+        const DevStencil &u = uatt[ic + ncomp * jc];
+        if (u.L && u.d_hw) h.ua[ic + 2 * jc] = {u.L, u.d_off, u.d_w, u.d_hw};
+      }
+  return h;
 }
 
 void launch_hw_correct(const double *field, long fcs, int ffirst, const DevStencil *theta, const DevStencil *delta,
-                       const DevStencil *uatt, const int *targets, int ntargets, const signed char *zero,
-                       const int *bnodes, const short *fmask, double *conv, cudaStream_t s)
+                       const DevStencil *uatt, int ncomp, bool do_fmt, bool do_mf, const int *targets, int ntargets,
+                       const signed char *zero, const int *bnodes, const short *fmask, double *conv, cudaStream_t s)
 {
-  (void)uatt;  // mean-field stencils with hard walls: see the host-side guard
   if (ntargets <= 0) return;
-  HwStencil th[2] = {}, de[2] = {};
-  for (int c = 0; c < 2; c++) {
-    if (theta[c].L) th[c] = {theta[c].L, theta[c].d_off, theta[c].d_w, theta[c].d_hw};
-    if (delta[c].L) de[c] = {delta[c].L, delta[c].d_off, delta[c].d_w, delta[c].d_hw};
-  }
-  k_hw_correct<<<(ntargets + 127) / 128, 128, 0, s>>>(field, fcs, ffirst, th[0], th[1], de[0], de[1], targets,
-                                                       ntargets, zero, bnodes, fmask, conv);
+  k_hw_correct<<<(ntargets + 127) / 128, 128, 0, s>>>(field, fcs, ffirst, hw_set(theta, delta, uatt, ncomp),
+                                                       do_fmt ? 1 : 0, do_mf ? 1 : 0, targets, ntargets, zero, bnodes,
+                                                       fmask, conv);
 }
 
 // Reflecting boundaries in the transposed sums.  A forward sum reads a mirrored
@@ -1283,16 +1313,16 @@ void launch_reflect_fold(const double *in, long cstride, int nin, const short *o
 }
 
 // Transpose of the hard-wall correction: the density column of every boundary node j receives, from each
-// target node i whose stencil point lands on j, the weight change times the adjoint rb rows at i (the
-// coefficients of hw_apply).  Several targets reach one j: FP64 atomic additions.
-__device__ void hw_apply_t(const HwStencil &st, int kind, int jc, int jlist, const int *ijk, long i,
-                           const double *__restrict__ w, const signed char *zero, const int *bnodes,
+// target node i whose stencil point lands on j, the weight change times the adjoint rows at i (the
+// coefficients of hw_apply): the rb rows of w for theta and delta, the mean-field rows (mfw, N apart) for the
+// mean-field stencils.  Several targets reach one j: FP64 atomic additions.
+__device__ void hw_apply_t(const HwStencil &st, int kind, int jc, int jlist, const int *ijk,
+                           const double *__restrict__ W, const signed char *zero, const int *bnodes,
                            const short *fmask, double *out)
 {
   const long N = c_g.N;
   const int nd = c_g.ndim;
   const int nel = 1 << nd;
-  const double *W = w + (long)c_g.first_rb * N + i;   // adjoint rb rows at i, N apart
   for (int s = 0; s < st.L; s++) {
     int refl;
     const short *o = st.off + (long)s * 3;
@@ -1305,11 +1335,10 @@ __device__ void hw_apply_t(const HwStencil &st, int kind, int jc, int jlist, con
     for (int l = 0; l < nel; l++)
       if (mask & (1 << l)) wh += st.hw[(long)s * nel + l];
     const double dw = wh - st.w[s];
-    const double f = c_g.fac[jc];
     double g;
     if (kind == 0) {
-      g = W[0];
-    } else {
+      g = c_g.fac[jc] * W[0];
+    } else if (kind == 1) {
       g = W[N];
       if (!c_g.single_size) g += c_g.inv_4pir[jc] * W[2 * N] + c_g.inv_4pirsq[jc] * W[3 * N];
       for (int d = 0; d < nd; d++) {
@@ -1317,40 +1346,46 @@ __device__ void hw_apply_t(const HwStencil &st, int kind, int jc, int jlist, con
         g += v * W[(long)(4 + d) * N];
         if (!c_g.single_size) g += c_g.inv_4pir[jc] * v * W[(long)(4 + nd + d) * N];
       }
+      g *= c_g.fac[jc];
+    } else {
+      g = W[0];
     }
-    atomicAdd(out + (long)(c_g.first_rho + jc) * N + jn, f * dw * g);
+    atomicAdd(out + (long)(c_g.first_rho + jc) * N + jn, dw * g);
   }
 }
 
-__global__ void k_hw_correct_t(const double *__restrict__ w, HwStencil th0, HwStencil th1, HwStencil de0,
-                               HwStencil de1, const int *__restrict__ targets, int ntargets,
+__global__ void k_hw_correct_t(const double *__restrict__ w, const double *__restrict__ mfw, HwSet hs, int do_fmt,
+                               int do_mf, const int *__restrict__ targets, int ntargets,
                                const signed char *__restrict__ zero, const int *__restrict__ bnodes,
                                const short *__restrict__ fmask, double *__restrict__ out)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntargets) return;
   const long i = targets[t];
+  const long N = c_g.N;
   int ijk[3];
   node_ijk(i, ijk);
-  for (int jc = 0; jc < c_g.ncomp && jc < 2; jc++) {
+  const int nc = c_g.ncomp;
+  for (int jc = 0; jc < nc && jc < 2; jc++) {
     const int jlist = (c_g.nlists <= 2) ? 0 : jc;
-    hw_apply_t(jc == 0 ? th0 : th1, 0, jc, jlist, ijk, i, w, zero, bnodes, fmask, out);
-    hw_apply_t(jc == 0 ? de0 : de1, 1, jc, jlist, ijk, i, w, zero, bnodes, fmask, out);
+    if (do_fmt) {
+      const double *W = w + (long)c_g.first_rb * N + i;   // adjoint rb rows at i, N apart
+      hw_apply_t(hs.th[jc], 0, jc, jlist, ijk, W, zero, bnodes, fmask, out);
+      hw_apply_t(hs.de[jc], 1, jc, jlist, ijk, W, zero, bnodes, fmask, out);
+    }
+    if (do_mf)
+      for (int ic = 0; ic < nc && ic < 2; ic++)
+        hw_apply_t(hs.ua[ic + 2 * jc], 2, jc, jlist, ijk, mfw + (long)ic * N + i, zero, bnodes, fmask, out);
   }
 }
 
-void launch_hw_correct_t(const double *w, const DevStencil *theta, const DevStencil *delta, const int *targets,
-                         int ntargets, const signed char *zero, const int *bnodes, const short *fmask, double *out,
-                         cudaStream_t s)
+void launch_hw_correct_t(const double *w, const double *mfw, const DevStencil *theta, const DevStencil *delta,
+                         const DevStencil *uatt, int ncomp, bool do_fmt, bool do_mf, const int *targets, int ntargets,
+                         const signed char *zero, const int *bnodes, const short *fmask, double *out, cudaStream_t s)
 {
   if (ntargets <= 0) return;
-  HwStencil th[2] = {}, de[2] = {};
-  for (int c = 0; c < 2; c++) {
-    if (theta[c].L) th[c] = {theta[c].L, theta[c].d_off, theta[c].d_w, theta[c].d_hw};
-    if (delta[c].L) de[c] = {delta[c].L, delta[c].d_off, delta[c].d_w, delta[c].d_hw};
-  }
-  k_hw_correct_t<<<(ntargets + 127) / 128, 128, 0, s>>>(w, th[0], th[1], de[0], de[1], targets, ntargets, zero,
-                                                         bnodes, fmask, out);
+  k_hw_correct_t<<<(ntargets + 127) / 128, 128, 0, s>>>(w, mfw, hw_set(theta, delta, uatt, ncomp), do_fmt ? 1 : 0,
+                                                         do_mf ? 1 : 0, targets, ntargets, zero, bnodes, fmask, out);
 }
 
 // ---------------------------------------------------------------------------

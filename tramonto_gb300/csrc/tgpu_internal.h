@@ -381,15 +381,14 @@ void launch_schur_combine(const double *x, const double *vext, const signed char
                           const double *tr, const double *ymf, double *y2, cudaStream_t s);
 void launch_jv_combine(const double *x, const double *vext, const signed char *zero, const double *v,
                        const double *conv, const double *tr, double *out, cudaStream_t s);
-void launch_hw_correct(const double *field, long field_cstride, int field_first, const DevStencil *theta,
-                       const DevStencil *delta, const DevStencil *uatt, const int *targets, int ntargets,
-                       const signed char *zero, const int *bnodes, const short *fmask, double *conv,
-                       cudaStream_t s);
+void launch_hw_correct(const double *field, long fcs, int ffirst, const DevStencil *theta, const DevStencil *delta,
+                       const DevStencil *uatt, int ncomp, bool do_fmt, bool do_mf, const int *targets, int ntargets,
+                       const signed char *zero, const int *bnodes, const short *fmask, double *conv, cudaStream_t s);
 void launch_reflect_fold(const double *in, long cstride, int nin, const short *off, const double *coef, int L,
                          double *const *outs, const int *signmask, int nout, cudaStream_t s);
-void launch_hw_correct_t(const double *w, const DevStencil *theta, const DevStencil *delta, const int *targets,
-                         int ntargets, const signed char *zero, const int *bnodes, const short *fmask, double *out,
-                         cudaStream_t s);
+void launch_hw_correct_t(const double *w, const double *mfw, const DevStencil *theta, const DevStencil *delta,
+                         const DevStencil *uatt, int ncomp, bool do_fmt, bool do_mf, const int *targets, int ntargets,
+                         const signed char *zero, const int *bnodes, const short *fmask, double *out, cudaStream_t s);
 // Krylov helpers
 void launch_multidot(const double *V, long ldv, int nvec, const double *w, long n, double *partial, int nblocks,
                      double *result, cudaStream_t s);
