@@ -77,7 +77,8 @@ typedef struct {
   int ncomp;
   int functional;            /* TGPU_FMT1 .. TGPU_FMT4 */
   int attraction;            /* 1: WCA mean field (Type_attr != NONE) */
-  int att_in_a22;            /* ATTInA22Block; only 0 (mean field as its own unknown) is implemented */
+  int att_in_a22;            /* ATTInA22Block: 0 mean field as its own unknown (MF_EQ rows); 1 summed into the
+                                Euler-Lagrange rows: vectors then have ncomp + 4 + 2 ndim rows per node */
   int single_size;           /* n1, n0, V1 are local copies (src/dft_fill_FMT.c:215, :303) */
   int hard_surf;             /* Lhard_surf: hard-wall boundary weights */
   int nlists_hw;             /* Nlists_HW */

@@ -30,7 +30,7 @@ def test_objectives_match_reference(name):
     s.close()
 
 
-@pytest.mark.parametrize("name", ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "hs1d_wall", "hslj1d_wall"])
+@pytest.mark.parametrize("name", ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "hs1d_wall", "hslj1d_wall", "lj1d_a22"])
 def test_objective_partials_match_finite_differences(name):
     from tramonto_gb300 import native
     z, p = load(name)

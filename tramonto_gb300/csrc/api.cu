@@ -134,6 +134,10 @@ struct Ctx : tgpu_ctx {
   double *d_rho_ref = nullptr, *d_conv_ref = nullptr, *d_chan_ref = nullptr, *d_tr_ref = nullptr;
   double *d_drho = nullptr, *d_dchan = nullptr;
   double *d_newton_x = nullptr;   // device copy of the state for the host-pointer Newton solve
+  // ATTInA22Block = 1: the caller's vectors have no mean-field rows (nunk_ext per node); internal scratch
+  bool a22 = false;
+  int nunk_ext = 0;
+  double *d_a22[3] = {nullptr, nullptr, nullptr};
   bool gmres_transpose = false;   // GMRES operator: S (false) or S^T (adjoint solve)
   // adjoint work buffers (allocated on first use)
   double *d_adj_chan = nullptr, *d_adj_pad = nullptr, *d_adj_g = nullptr, *d_adj_v = nullptr, *d_adj_t = nullptr;
@@ -968,6 +972,59 @@ const double *attraction_sums(Ctx *c, const double *d_x)
   return S;
 }
 
+// ATTInA22Block = 1 (the mean field summed into the Euler-Lagrange rows, src/dft_fill_EL.c:143-161,
+// linsolver_setup_HSTYPE's A22 block, src/dft_linsolver_setup.c:234-236): the caller's vectors have no
+// mean-field rows.  Inside, the mean field stays an unknown of its own, so every kernel is shared with
+// ATTInA22Block = 0.  With J = [[J_ee, C], [B, -I]] (C: the mean field in the EL rows, B: its stencil sums)
+// the caller's Jacobian is J_ee + C B, and at the boundary
+//   states and perturbations v  -> [v; B v]        (mean-field rows equal to their attraction sums)
+//   right-hand sides b of J, J^T -> [b; 0]
+//   arguments w of J^T          -> [w; C^T w]      (mean-field rows equal to the EL rows off zero-density rows)
+// and results drop the mean-field rows.  The density block of the Schur complement is the same in both forms.
+void a22_mf_sums(Ctx *c, const double *x, bool jac, double *mf)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  ck(cudaMemsetAsync(mf, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+  pad(c, x + (long)g.first_rho * N, jac ? c->pads.rho_jac : c->pads.rho_res, false);
+  for (int jc = 0; jc < g.ncomp; jc++)
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      double *o[1] = {mf + (long)ic * N};
+      conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o, 1, false);
+    }
+  if (g.hard_surf && !c->hw_targets.empty()) {
+    tgpu::launch_hw_correct(x + (long)g.first_rho * N, N, 0, nullptr, nullptr, c->sten[TGPU_STEN_UATT].data(),
+                            g.ncomp, false, true, c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero,
+                            c->d_bnodes, c->d_fmask, mf - (long)g.nrb * N, c->stream);
+    c->stats.kernel_launches++;
+  }
+}
+
+enum { A22_SUMS = 0, A22_JAC_SUMS = 1, A22_ZERO = 2, A22_EL = 3 };
+
+// the internal-layout copy of a caller vector in scratch slot (the caller's own vector without ATTInA22Block)
+const double *a22_in(Ctx *c, const double *ext, int how, int slot)
+{
+  if (!c->a22) return ext;
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  double *in = c->d_a22[slot];
+  copy_d(c, in, ext, (size_t)c->nunk_ext * N);
+  double *mf = in + (long)g.first_mf * N;
+  if (how == A22_ZERO) ck(cudaMemsetAsync(mf, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+  else if (how == A22_EL)   // C^T w: the EL rows, except zero-density rows (they hold no mean field)
+    tgpu::launch_mask_rows(mf, ext, c->d_vext, c->d_zero, g.first_rho, g.ncomp, 0, c->stream);
+  else a22_mf_sums(c, in, how == A22_JAC_SUMS, mf);
+  return in;
+}
+
+// where an internal-layout result goes (scratch slot, or the caller's vector), and its copy back
+double *a22_out_buf(Ctx *c, double *ext, int slot) { return c->a22 ? c->d_a22[slot] : ext; }
+void a22_out(Ctx *c, const double *in, double *ext)
+{
+  if (c->a22) copy_d(c, ext, in, (size_t)c->nunk_ext * c->dg.N);
+}
+
 void objectives_device(Ctx *c, const double *d_x, double *omega_s, double *gamma_ex)
 {
   need_integ(c);
@@ -1374,6 +1431,8 @@ void build_device_tables(Ctx *c)
   c->d_ymf = dalloc<double>((size_t)dg.ncomp * N);
   c->n2 = (long)dg.ncomp * N;
   c->d_newton_x = dalloc<double>(U * N);
+  if (c->a22)
+    for (auto &b : c->d_a22) b = dalloc<double>(U * N);
   c->d_b2s = dalloc<double>(c->n2);
   c->d_gw = dalloc<double>(c->n2);
   c->d_gt = dalloc<double>(c->n2);
@@ -1410,8 +1469,6 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
     }
     if (g.functional < TGPU_FMT1 || g.functional > TGPU_FMT4)
       throw Error(TGPU_ERR_UNSUPPORTED, "functional outside FMT1..FMT4");
-    if (g.attraction && g.att_in_a22)
-      throw Error(TGPU_ERR_UNSUPPORTED, "mean field summed into the density rows (ATTInA22Block) is not implemented");
     if (g.hard_surf && g.ncomp > 2) throw Error(TGPU_ERR_UNSUPPORTED, "hard walls with more than two components");
     const long N = nnodes(g);
     if (N > (1L << 31) / 4) throw Error(TGPU_ERR_ARG, "mesh too large for 32-bit stencil offsets");
@@ -1429,6 +1486,8 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
     dg.first_rb = g.ncomp;
     dg.first_mf = g.attraction ? g.ncomp + dg.nrb : -1;
     dg.nunk = g.ncomp + dg.nrb + (g.attraction ? g.ncomp : 0);
+    c->a22 = g.attraction && g.att_in_a22;
+    c->nunk_ext = c->a22 ? dg.nunk - g.ncomp : dg.nunk;
     dg.functional = g.functional;
     dg.attraction = g.attraction;
     dg.single_size = g.single_size;
@@ -1480,6 +1539,7 @@ int tgpu_destroy(tgpu_handle h)
     dfree(c->d_red); dfree(c->d_gw); dfree(c->d_gt); dfree(c->d_gx); dfree(c->d_gb);
     dfree(c->d_rho_ref); dfree(c->d_conv_ref); dfree(c->d_chan_ref); dfree(c->d_tr_ref);
     dfree(c->d_drho); dfree(c->d_dchan); dfree(c->d_newton_x);
+    for (auto &b : c->d_a22) dfree(b);
     if (c->h_red) cudaFreeHost(c->h_red);
     free_pad(c->pads.rho_res); free_pad(c->pads.rho_jac); free_pad(c->pads.tr_res); free_pad(c->pads.tr_jac);
     free_pad(c->pads.zero_ext);
@@ -1670,7 +1730,7 @@ int tgpu_sizes(tgpu_handle h, long *nn, int *nunk, int *ncomp)
   return guard([&] {
     Ctx *c = C(h);
     if (nn) *nn = c->dg.N;
-    if (nunk) *nunk = c->dg.nunk;
+    if (nunk) *nunk = c->nunk_ext;
     if (ncomp) *ncomp = c->dg.ncomp;
     return TGPU_OK;
   });
@@ -1680,7 +1740,11 @@ int tgpu_fill_device(tgpu_handle h, const double *d_x, double *d_R, int mode)
 {
   return guard([&] {
     if (mode != 0 && mode != 1) throw Error(TGPU_ERR_ARG, "mode must be 0 or 1");
-    fill_device(C(h), d_x, d_R, mode);
+    Ctx *c = C(h);
+    need_final(c);
+    double *R = a22_out_buf(c, d_R, 1);
+    fill_device(c, a22_in(c, d_x, A22_SUMS, 0), R, mode);
+    a22_out(c, R, d_R);
     ck(cudaGetLastError(), "fill launch");
     return TGPU_OK;
   });
@@ -1692,9 +1756,11 @@ int tgpu_fill(tgpu_handle h, const double *x, double *R, int mode)
     Ctx *c = C(h);
     need_final(c);
     if (mode != 0 && mode != 1) throw Error(TGPU_ERR_ARG, "mode must be 0 or 1");
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->nunk_ext * c->dg.N;
     h2d(c, c->d_work, x, n);
-    fill_device(c, c->d_work, c->d_work2, mode);
+    double *Rd = a22_out_buf(c, c->d_work2, 1);
+    fill_device(c, a22_in(c, c->d_work, A22_SUMS, 0), Rd, mode);
+    a22_out(c, Rd, c->d_work2);
     d2h(c, R, c->d_work2, n);
     ck(cudaGetLastError(), "fill launch");
     return TGPU_OK;
@@ -1703,7 +1769,15 @@ int tgpu_fill(tgpu_handle h, const double *x, double *R, int mode)
 
 int tgpu_jv_device(tgpu_handle h, const double *d_v, double *d_out)
 {
-  return guard([&] { jv_device(C(h), d_v, d_out); ck(cudaGetLastError(), "jv"); return TGPU_OK; });
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    double *o = a22_out_buf(c, d_out, 1);
+    jv_device(c, a22_in(c, d_v, A22_JAC_SUMS, 0), o);
+    a22_out(c, o, d_out);
+    ck(cudaGetLastError(), "jv");
+    return TGPU_OK;
+  });
 }
 
 int tgpu_jv(tgpu_handle h, const double *v, double *out)
@@ -1711,9 +1785,11 @@ int tgpu_jv(tgpu_handle h, const double *v, double *out)
   return guard([&] {
     Ctx *c = C(h);
     need_state(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->nunk_ext * c->dg.N;
     h2d(c, c->d_work, v, n);
-    jv_device(c, c->d_work, c->d_work2);
+    double *o = a22_out_buf(c, c->d_work2, 1);
+    jv_device(c, a22_in(c, c->d_work, A22_JAC_SUMS, 0), o);
+    a22_out(c, o, c->d_work2);
     d2h(c, out, c->d_work2, n);
     return TGPU_OK;
   });
@@ -1738,12 +1814,22 @@ int tgpu_schur_apply(tgpu_handle h, const double *v2, double *y2)
 
 int tgpu_schur_rhs_device(tgpu_handle h, const double *d_b, double *d_b2s)
 {
-  return guard([&] { schur_rhs_device(C(h), d_b, d_b2s); return TGPU_OK; });
+  return guard([&] {
+    Ctx *c = C(h);
+    schur_rhs_device(c, a22_in(c, d_b, A22_ZERO, 0), d_b2s);
+    return TGPU_OK;
+  });
 }
 
 int tgpu_schur_x1_device(tgpu_handle h, const double *d_b, const double *d_x2, double *d_x)
 {
-  return guard([&] { schur_x1_device(C(h), d_b, d_x2, d_x); return TGPU_OK; });
+  return guard([&] {
+    Ctx *c = C(h);
+    double *o = a22_out_buf(c, d_x, 1);
+    schur_x1_device(c, a22_in(c, d_b, A22_ZERO, 0), d_x2, o);
+    a22_out(c, o, d_x);
+    return TGPU_OK;
+  });
 }
 
 int tgpu_solve_device(tgpu_handle h, const double *d_b, double *d_dx, double tol, int maxit, int *iters,
@@ -1752,7 +1838,10 @@ int tgpu_solve_device(tgpu_handle h, const double *d_b, double *d_dx, double tol
   return guard([&] {
     int it = 0;
     double rr = 0.0;
-    const int st = solve_device(C(h), d_b, d_dx, tol, maxit, &it, &rr);
+    Ctx *c = C(h);
+    double *o = a22_out_buf(c, d_dx, 1);
+    const int st = solve_device(c, a22_in(c, d_b, A22_ZERO, 0), o, tol, maxit, &it, &rr);
+    a22_out(c, o, d_dx);
     if (iters) *iters = it;
     if (relres) *relres = rr;
     return st;
@@ -1764,11 +1853,13 @@ int tgpu_solve(tgpu_handle h, const double *b, double *dx, double tol, int maxit
   return guard([&] {
     Ctx *c = C(h);
     need_state(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->nunk_ext * c->dg.N;
     h2d(c, c->d_work, b, n);
     int it = 0;
     double rr = 0.0;
-    const int st = solve_device(c, c->d_work, c->d_work2, tol, maxit, &it, &rr);
+    double *o = a22_out_buf(c, c->d_work2, 1);
+    const int st = solve_device(c, a22_in(c, c->d_work, A22_ZERO, 0), o, tol, maxit, &it, &rr);
+    a22_out(c, o, c->d_work2);
     d2h(c, dx, c->d_work2, n);
     if (iters) *iters = it;
     if (relres) *relres = rr;
@@ -1781,8 +1872,12 @@ int tgpu_newton_device(tgpu_handle h, double *d_x, double rel_tol, double abs_to
 {
   return guard([&] {
     int it = 0;
-    const int st = newton_device(C(h), d_x, rel_tol, abs_tol, update_floor, max_iter, lin_tol, lin_max_iter, &it,
+    Ctx *c = C(h);
+    need_final(c);
+    double *x = c->a22 ? const_cast<double *>(a22_in(c, d_x, A22_SUMS, 2)) : d_x;
+    const int st = newton_device(c, x, rel_tol, abs_tol, update_floor, max_iter, lin_tol, lin_max_iter, &it,
                                  final_resid);
+    a22_out(c, x, d_x);
     if (iters) *iters = it;
     return st;
   });
@@ -1794,15 +1889,16 @@ int tgpu_newton(tgpu_handle h, double *x, double rel_tol, double abs_tol, double
   return guard([&] {
     Ctx *c = C(h);
     need_final(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->dg.nunk * c->dg.N, ne = (size_t)c->nunk_ext * c->dg.N;
     double *d_xs = dalloc<double>(n);
     int st = TGPU_OK;
     try {
-      h2d(c, d_xs, x, n);
+      h2d(c, d_xs, x, ne);
+      if (c->a22) copy_d(c, d_xs, a22_in(c, d_xs, A22_SUMS, 2), n);
       int it = 0;
       st = newton_device(c, d_xs, rel_tol, abs_tol, update_floor, max_iter, lin_tol, lin_max_iter, &it, final_resid);
       if (iters) *iters = it;
-      d2h(c, x, d_xs, n);
+      d2h(c, x, d_xs, ne);
     } catch (...) {
       dfree(d_xs);
       throw;
@@ -1819,7 +1915,11 @@ int tgpu_newton_solve_device(tgpu_handle h, double *d_x, double resid_tol, int m
   return guard([&] {
     int it = 0, lt = 0;
     double fr = 0.0;
-    const int st = newton_solve_device(C(h), d_x, resid_tol, max_iter, lin_tol, lin_max_iter, update_floor, &it, &fr, &lt);
+    Ctx *c = C(h);
+    need_final(c);
+    double *x = c->a22 ? const_cast<double *>(a22_in(c, d_x, A22_SUMS, 2)) : d_x;
+    const int st = newton_solve_device(c, x, resid_tol, max_iter, lin_tol, lin_max_iter, update_floor, &it, &fr, &lt);
+    a22_out(c, x, d_x);
     if (iters) *iters = it;
     if (final_resid) *final_resid = fr;
     if (lin_iters_total) *lin_iters_total = lt;
@@ -1833,13 +1933,14 @@ int tgpu_newton_solve(tgpu_handle h, double *x, double resid_tol, int max_iter, 
   return guard([&] {
     Ctx *c = C(h);
     need_final(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
-    h2d(c, c->d_newton_x, x, n);
+    const size_t n = (size_t)c->dg.nunk * c->dg.N, ne = (size_t)c->nunk_ext * c->dg.N;
+    h2d(c, c->d_newton_x, x, ne);
+    if (c->a22) copy_d(c, c->d_newton_x, a22_in(c, c->d_newton_x, A22_SUMS, 2), n);
     int it = 0, lt = 0;
     double fr = 0.0;
     const int st = newton_solve_device(c, c->d_newton_x, resid_tol, max_iter, lin_tol, lin_max_iter, update_floor,
                                        &it, &fr, &lt);
-    d2h(c, x, c->d_newton_x, n);
+    d2h(c, x, c->d_newton_x, ne);
     if (iters) *iters = it;
     if (final_resid) *final_resid = fr;
     if (lin_iters_total) *lin_iters_total = lt;
@@ -1901,7 +2002,15 @@ int tgpu_reset_stats(tgpu_handle h)
 
 int tgpu_jtv_device(tgpu_handle h, const double *d_w, double *d_out)
 {
-  return guard([&] { jtv_device(C(h), d_w, d_out); ck(cudaGetLastError(), "jtv"); return TGPU_OK; });
+  return guard([&] {
+    Ctx *c = C(h);
+    need_state(c);
+    double *o = a22_out_buf(c, d_out, 1);
+    jtv_device(c, a22_in(c, d_w, A22_EL, 0), o);
+    a22_out(c, o, d_out);
+    ck(cudaGetLastError(), "jtv");
+    return TGPU_OK;
+  });
 }
 
 int tgpu_jtv(tgpu_handle h, const double *w, double *out)
@@ -1909,9 +2018,11 @@ int tgpu_jtv(tgpu_handle h, const double *w, double *out)
   return guard([&] {
     Ctx *c = C(h);
     need_state(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->nunk_ext * c->dg.N;
     h2d(c, c->d_work, w, n);
-    jtv_device(c, c->d_work, c->d_work2);
+    double *o = a22_out_buf(c, c->d_work2, 1);
+    jtv_device(c, a22_in(c, c->d_work, A22_EL, 0), o);
+    a22_out(c, o, c->d_work2);
     d2h(c, out, c->d_work2, n);
     return TGPU_OK;
   });
@@ -1923,7 +2034,10 @@ int tgpu_adjoint_solve_device(tgpu_handle h, const double *d_g, double *d_lambda
   return guard([&] {
     int it = 0;
     double rr = 0.0;
-    const int st = adjoint_solve_device(C(h), d_g, d_lambda, tol, max_iter, &it, &rr);
+    Ctx *c = C(h);
+    double *o = a22_out_buf(c, d_lambda, 1);
+    const int st = adjoint_solve_device(c, a22_in(c, d_g, A22_ZERO, 0), o, tol, max_iter, &it, &rr);
+    a22_out(c, o, d_lambda);
     if (iters) *iters = it;
     if (relres) *relres = rr;
     return st;
@@ -1936,11 +2050,13 @@ int tgpu_adjoint_solve(tgpu_handle h, const double *g, double *lambda, double to
   return guard([&] {
     Ctx *c = C(h);
     need_state(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->nunk_ext * c->dg.N;
     h2d(c, c->d_work, g, n);
     int it = 0;
     double rr = 0.0;
-    const int st = adjoint_solve_device(c, c->d_work, c->d_work2, tol, max_iter, &it, &rr);
+    double *o = a22_out_buf(c, c->d_work2, 1);
+    const int st = adjoint_solve_device(c, a22_in(c, c->d_work, A22_ZERO, 0), o, tol, max_iter, &it, &rr);
+    a22_out(c, o, c->d_work2);
     d2h(c, lambda, c->d_work2, n);
     if (iters) *iters = it;
     if (relres) *relres = rr;
@@ -1986,7 +2102,9 @@ int tgpu_set_integration(tgpu_handle h, const double *w_fluid, const double *w_b
 int tgpu_objectives_device(tgpu_handle h, const double *d_x, double *omega_s, double *gamma_ex)
 {
   return guard([&] {
-    objectives_device(C(h), d_x, omega_s, gamma_ex);
+    Ctx *c = C(h);
+    need_integ(c);
+    objectives_device(c, a22_in(c, d_x, A22_SUMS, 0), omega_s, gamma_ex);
     return TGPU_OK;
   });
 }
@@ -1996,8 +2114,8 @@ int tgpu_objectives(tgpu_handle h, const double *x, double *omega_s, double *gam
   return guard([&] {
     Ctx *c = C(h);
     need_integ(c);
-    h2d(c, c->d_work, x, (size_t)c->dg.nunk * c->dg.N);
-    objectives_device(c, c->d_work, omega_s, gamma_ex);
+    h2d(c, c->d_work, x, (size_t)c->nunk_ext * c->dg.N);
+    objectives_device(c, a22_in(c, c->d_work, A22_SUMS, 0), omega_s, gamma_ex);
     return TGPU_OK;
   });
 }
@@ -2005,7 +2123,11 @@ int tgpu_objectives(tgpu_handle h, const double *x, double *omega_s, double *gam
 int tgpu_objective_grad_device(tgpu_handle h, const double *d_x, int kind, int icomp, double *d_gx, double *d_gv)
 {
   return guard([&] {
-    objective_grad_device(C(h), d_x, kind, icomp, d_gx, d_gv);
+    Ctx *c = C(h);
+    need_integ(c);
+    double *o = a22_out_buf(c, d_gx, 1);
+    objective_grad_device(c, a22_in(c, d_x, A22_SUMS, 0), kind, icomp, o, d_gv);
+    a22_out(c, o, d_gx);
     ck(cudaGetLastError(), "objective gradient");
     return TGPU_OK;
   });
@@ -2016,7 +2138,9 @@ int tgpu_grad_vext_device(tgpu_handle h, const double *d_x, int kind, int icomp,
 {
   return guard([&] {
     int it = 0;
-    const int st = grad_vext_device(C(h), d_x, kind, icomp, tol, max_iter, d_dF_dV, &it);
+    Ctx *c = C(h);
+    need_integ(c);
+    const int st = grad_vext_device(c, a22_in(c, d_x, A22_SUMS, 2), kind, icomp, tol, max_iter, d_dF_dV, &it);
     if (iters) *iters = it;
     return st;
   });
@@ -2029,10 +2153,10 @@ int grad_vext_host(tgpu_handle h, const double *x, int kind, int icomp, double t
   return guard([&] {
     Ctx *c = C(h);
     need_integ(c);
-    const size_t n = (size_t)c->dg.nunk * c->dg.N;
+    const size_t n = (size_t)c->nunk_ext * c->dg.N;
     h2d(c, c->d_work, x, n);
     int it = 0;
-    const int st = grad_vext_device(c, c->d_work, kind, icomp, tol, max_iter, c->d_work2, &it);
+    const int st = grad_vext_device(c, a22_in(c, c->d_work, A22_SUMS, 2), kind, icomp, tol, max_iter, c->d_work2, &it);
     d2h(c, dF_dV, c->d_work2, (size_t)c->dg.ncomp * c->dg.N);
     if (iters) *iters = it;
     return st;
