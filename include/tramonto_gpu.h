@@ -91,6 +91,19 @@ typedef struct {
   double fac_overlap[TGPU_MAXC];
   double dphi_bulk[4];       /* Dphi_Drhobar_b[0..3]: bulk dPhi/dn0..dn3 */
   double vext_max;           /* VEXT_MAX: nodes with V_ext == vext_max are zero-density rows */
+  /* two-phase interface (Type_interface = PHASE_INTERFACE, no walls): beyond the low side of an IN_BULK
+   * boundary the bulk state LBB, beyond the high side RTF (sentinels -3/-4 of offset_to_node_box,
+   * src/dft_mesh_lib.c:213-265, with constant_boundary src/dft_utils.c:90-130), and the Euler-Lagrange rows
+   * take the chemical potential betamu (the LBB/RTF mean, src/dft_thermo.c:326; src/dft_fill_EL.c:412-416) */
+  int interface;             /* 0: uniform (the fields above); 2: phase interface (the fields below) */
+  double rho_b_lbb[TGPU_MAXC], rho_b_rtf[TGPU_MAXC];
+  double dphi_lbb[4], dphi_rtf[4];   /* Dphi_Drhobar_LBB / _RTF */
+  double betamu[TGPU_MAXC];
+  /* Lconstrain_interface: the first component's density at node pin_node held at pin_value
+   * (fill_constant_density, src/dft_fill_EL.c:89-97) when pin is 1 */
+  int pin;
+  long pin_node;
+  double pin_value;
 } tgpu_geometry;
 
 /* lifecycle: create -> set_stencil/set_vext/set_zero_density/set_hard_wall -> finalize */

@@ -27,8 +27,14 @@ static void node_to_ijk(const orc_problem *p, long node, int *ijk)
 }
 
 /* offset_to_node_box (src/dft_mesh_lib.c:203-297) for one process whose box is
- * the whole mesh.  Returns a node >= 0, -1 (bulk), -2 (inside a wall) or -9
- * for a double reflection, which the reference rejects. */
+ * the whole mesh.  Returns a node >= 0, -1 (bulk), -3 / -4 (beyond the low / high
+ * bulk boundary of a phase interface), -2 (inside a wall) or -9 for a double
+ * reflection, which the reference rejects. */
+static long bulk_side(const orc_problem *p, int high)
+{
+  return p->interface == 2 ? (high ? -4 : -3) : -1;
+}
+
 static long offset_to_node(const orc_problem *p, const int *ijk, const short *off, int *reflect)
 {
   int s[3] = {0, 0, 0};
@@ -38,13 +44,13 @@ static long offset_to_node(const orc_problem *p, const int *ijk, const short *of
     reflect[i] = 0;
     if (s[i] < 0) {
       switch (p->bc[i][0]) {
-        case ORC_BC_IN_BULK: return -1;
+        case ORC_BC_IN_BULK: return bulk_side(p, 0);
         case ORC_BC_IN_WALL: return -2;
         case ORC_BC_REFLECT:
           reflect[i] = 1;
           s[i] = -s[i];
           if (s[i] >= n) {
-            if (p->bc[i][1] == ORC_BC_IN_BULK) return -1;
+            if (p->bc[i][1] == ORC_BC_IN_BULK) return bulk_side(p, 1);
             if (p->bc[i][1] == ORC_BC_IN_WALL) return -2;
             return -9;
           }
@@ -53,13 +59,13 @@ static long offset_to_node(const orc_problem *p, const int *ijk, const short *of
       }
     } else if (s[i] >= n) {
       switch (p->bc[i][1]) {
-        case ORC_BC_IN_BULK: return -1;
+        case ORC_BC_IN_BULK: return bulk_side(p, 1);
         case ORC_BC_IN_WALL: return -2;
         case ORC_BC_REFLECT:
           reflect[i] = 1;
           s[i] = 2 * (n - 1) - s[i];
           if (s[i] < 0) {
-            if (p->bc[i][0] == ORC_BC_IN_BULK) return -1;
+            if (p->bc[i][0] == ORC_BC_IN_BULK) return bulk_side(p, 0);
             if (p->bc[i][0] == ORC_BC_IN_WALL) return -2;
             return -9;
           }
@@ -603,6 +609,8 @@ static double sten_sum(pass_t *ps, int stype, int iu, long inode, const int *ijk
       double rho;
       if (jn >= 0 && !p->zero_density[(long)jc * N + jn]) rho = ps->x[(long)ju * N + jn];
       else if (jn == -1) rho = p->rho_b[jc];
+      else if (jn == -3) rho = p->rho_b_lbb[jc];
+      else if (jn == -4) rho = p->rho_b_rtf[jc];
       else rho = 0.0;
       resid_sum += fac * (weight * rho);
       if (ps->entry && jn >= 0 && !p->zero_density[(long)jc * N + jn])
@@ -641,8 +649,8 @@ static double rosen_rb(pass_t *ps, int stype, int iu, long inode, const int *ijk
       } else {
         resid = fo * weight * ps->dphi[3 * N + jn];
       }
-    } else if (jn == -1) {
-      const double *b = p->dphi_bulk;
+    } else if (jn == -1 || jn == -3 || jn == -4) {   /* :104-126 */
+      const double *b = jn == -1 ? p->dphi_bulk : (jn == -3 ? p->dphi_lbb : p->dphi_rtf);
       if (stype == ORC_DELTA) resid = fo * weight * (b[0] * p->inv_4pirsq[ic] + b[1] * p->inv_4pir[ic] + b[2]);
       else resid = fo * weight * b[3];
     } else {
@@ -692,13 +700,21 @@ static void fill_node(pass_t *ps, long inode)
         /* fill_zero_value (src/dft_fill_EL.c:224-240) */
         R = xi;
         if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, 1.0);
+      } else if (p->interface == 2 && ic == 0 && inode == p->pin_node) {
+        /* fill_constant_density (src/dft_fill_EL.c:89-96, 286-305) */
+        R = log(xi) - log(p->pin_value);
+        if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, 1.0 / xi);
       } else {
         R += log(xi);                                   /* fill_EL_ideal_gas :351-386 */
         if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, 1.0 / xi);
         double mu = 0.0;                                /* fill_EL_chem_pot :388-433 */
-        mu -= log(p->rho_b[ic]);
-        mu -= p->betamu_hs_ex[ic];
-        if (p->attraction) mu -= p->betamu_att[ic];
+        if (p->interface == 2) {
+          mu = -p->betamu[ic];                          /* :412-416 */
+        } else {
+          mu -= log(p->rho_b[ic]);
+          mu -= p->betamu_hs_ex[ic];
+          if (p->attraction) mu -= p->betamu_att[ic];
+        }
         R += mu;
         R += p->vext[(long)ic * N + inode];             /* fill_EL_ext_field :435-444 */
         R += rosen_rb(ps, ORC_DELTA, iu, inode, ijk, ic);

@@ -12,7 +12,8 @@
  *       (src/dft_fill_FMT.c:41-189, src/dft_physics_FMT1.c:79-168, src/dft_physics_FMT2.c:104-250,
  *       src/dft_physics_FMT3.c:101-265, src/dft_physics_FMT4.c:102-275)
  *   - load_euler_lagrange (src/dft_fill_EL.c:38-196, 351-444) and load_mean_field (src/dft_fill_mf.c:38-63)
- *   - offset_to_node_box (src/dft_mesh_lib.c:203-297), HW_boundary_weight (src/dft_utils.c:41-62)
+ *   - offset_to_node_box (src/dft_mesh_lib.c:203-297), HW_boundary_weight (src/dft_utils.c:41-62),
+ *     constant_boundary (src/dft_utils.c:89-110)
  *   - the hard-sphere Schur operator S = A22 - A21 A11^-1 A12 (src/dft_Schur_Epetra_Operator.cpp:86-119,
  *     src/dft_HardSphereA11_Epetra_Operator.cpp:130-197)
  * It is pinned against golden vectors produced by the reference itself
@@ -61,6 +62,16 @@ typedef struct {
   const short *sten_off[3][ORC_MAXC * ORC_MAXC];   /* [L][ndim] */
   const double *sten_w[3][ORC_MAXC * ORC_MAXC];    /* [L] */
   const double *sten_hw[3][ORC_MAXC * ORC_MAXC];   /* [L][2^ndim] or NULL */
+  /* phase interface (Type_interface = PHASE_INTERFACE): stencil points beyond the low / high
+   * bulk boundaries read the LBB / RTF states (offset_to_node_box -3 / -4), the Euler-Lagrange
+   * rows take -Betamu as their chemical potential, and with Lconstrain_interface the first
+   * density at pin_node is held at pin_value (fill_constant_density, src/dft_fill_EL.c:286-305) */
+  int interface;              /* 0: uniform, 2: phase interface */
+  double rho_b_lbb[ORC_MAXC], rho_b_rtf[ORC_MAXC];
+  double dphi_lbb[4], dphi_rtf[4];
+  double betamu[ORC_MAXC];
+  long pin_node;              /* -1: no pinned density */
+  double pin_value;
 } orc_problem;
 
 long orc_nnodes(const orc_problem *p);

@@ -46,6 +46,9 @@ class _Problem(C.Structure):
         ("sten_off", (C.POINTER(C.c_int16) * (MAXC * MAXC)) * 3),
         ("sten_w", (C.POINTER(C.c_double) * (MAXC * MAXC)) * 3),
         ("sten_hw", (C.POINTER(C.c_double) * (MAXC * MAXC)) * 3),
+        ("interface", C.c_int), ("rho_b_lbb", C.c_double * MAXC), ("rho_b_rtf", C.c_double * MAXC),
+        ("dphi_lbb", C.c_double * 4), ("dphi_rtf", C.c_double * 4), ("betamu", C.c_double * MAXC),
+        ("pin_node", C.c_long), ("pin_value", C.c_double),
     ]
 
 
@@ -78,6 +81,16 @@ class Oracle:
         for i in range(4):
             s.dphi_bulk[i] = float(prob.dphi_bulk[i])
         s.vext_max = float(prob.vext_max)
+        s.interface = int(getattr(prob, "interface", 0))
+        s.pin_node = -1
+        if s.interface:
+            for name, src in (("rho_b_lbb", prob.rho_b_lbb), ("rho_b_rtf", prob.rho_b_rtf), ("dphi_lbb", prob.dphi_lbb),
+                              ("dphi_rtf", prob.dphi_rtf), ("betamu", prob.betamu_if)):
+                arr = getattr(s, name)
+                for i, v in enumerate(np.asarray(src, np.float64)[:4]):
+                    arr[i] = float(v)
+            s.pin_node = int(prob.pin_node)
+            s.pin_value = float(prob.pin_value)
         self.N = int(np.prod([prob.nx[d] for d in range(prob.ndim)]))
         vext = np.ascontiguousarray(prob.vext, np.float64)
         zd = np.ascontiguousarray(prob.zero_density, np.int8)

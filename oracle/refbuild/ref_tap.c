@@ -78,7 +78,7 @@ int tref_setup(const char *dir)
  * Nrho_bar_s Type_func Type_attr ATTInA22Block Lhard_surf Nlists_HW Nwall
  * Type_bc[3][2] Phys2Unk_first[DENSITY,HSRHOBAR,MF_EQ] Nzone Nodes_x_box[3]
  * Max_sten_length[3] Pflag[3] Iguess Type_interface Mesh_coarsening Coarser_jac
- * Nnodes_per_el_V Type_pairPot Lcut_jac Type_CoreATT_R Type_CoreATT_CONST */
+ * Nnodes_per_el_V Type_pairPot Lcut_jac Type_CoreATT_R Type_CoreATT_CONST Lconstrain_interface Grad_dim */
 int tref_info_ints(int *o)
 {
   int k = 0, i;
@@ -96,6 +96,7 @@ int tref_info_ints(int *o)
   o[k++] = Iguess; o[k++] = Type_interface; o[k++] = Mesh_coarsening; o[k++] = Coarser_jac;
   o[k++] = Nnodes_per_el_V; o[k++] = Type_pairPot; o[k++] = Lcut_jac;
   o[k++] = Type_CoreATT_R; o[k++] = Type_CoreATT_CONST;
+  o[k++] = Lconstrain_interface; o[k++] = Grad_dim;
   return k;
 }
 
@@ -103,7 +104,8 @@ int tref_info_ints(int *o)
  * HS_diam Rho_b Betamu_hs_ex Betamu_att Inv_rad Inv_4pir Inv_4pirsq
  * Fac_overlap_hs, then Rhobar_b[10] Dphi_Drhobar_b[10], Avdw[NCOMP_MAX^2],
  * Eps_ff Sigma_ff Cut_ff [NCOMP_MAX^2 each], Temp, Jac_threshold, then YukawaK_ff Rmin_ff Rzero_ff
- * [NCOMP_MAX^2 each] */
+ * [NCOMP_MAX^2 each], Rho_b_LBB Rho_b_RTF [NCOMP_MAX each], Dphi_Drhobar_LBB Dphi_Drhobar_RTF [10 each],
+ * Betamu [NCOMP_MAX] */
 int tref_info_doubles(double *o)
 {
   int k = 0, i, j;
@@ -129,6 +131,11 @@ int tref_info_doubles(double *o)
   for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = YukawaK_ff[i][j];
   for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = Rmin_ff[i][j];
   for (i = 0; i < NCOMP_MAX; i++) for (j = 0; j < NCOMP_MAX; j++) o[k++] = Rzero_ff[i][j];
+  for (i = 0; i < NCOMP_MAX; i++) o[k++] = Rho_b_LBB[i];
+  for (i = 0; i < NCOMP_MAX; i++) o[k++] = Rho_b_RTF[i];
+  for (i = 0; i < 10; i++) o[k++] = Dphi_Drhobar_LBB[i];
+  for (i = 0; i < 10; i++) o[k++] = Dphi_Drhobar_RTF[i];
+  for (i = 0; i < NCOMP_MAX; i++) o[k++] = Betamu[i];
   return k;
 }
 

@@ -114,6 +114,10 @@ def cases():
     # mean-field stencil takes the hard-wall weights too
     c["hslj1d_wall"] = deck("HS5_FMT1_1D", dict(mf, **{"Type_attr Type_pairPot": "0 0", "Eps_ff[i][j]": "0.8333333333333334",
                                                    "Cut_ff[i][j]": "2.5", "Rho_b_0[icomp]": "0.75"}))
+    # liquid-vapor interface (BULK3: PHASE_INTERFACE between the binodal densities, the mid density pinned by
+    # Lconstrain_interface), with reflecting ends as in the example and with bulk ends (LBB / RTF sentinels)
+    c["lv1d_interface"] = deck("BULK3_FMT1_WCA_1D", {"L_Schur": SCHUR_LINSOLVE})
+    c["lv1d_bulkbc"] = deck("BULK3_FMT1_WCA_1D", {"L_Schur": SCHUR_LINSOLVE, "Type_bc(x0": "0 0"})
     # ATTInA22Block = 1: the mean field summed into the Euler-Lagrange rows (no mean-field unknowns)
     c["lj1d_a22"] = deck("LJ1_FMT1_WCA_1D", {"ATTInA22Block": "0 50 0 1 0", "L_Schur": SCHUR_LINSOLVE})
     return c

@@ -24,9 +24,11 @@ from goldens import PROD_RTOL, load, probe, rel_err
 pytestmark = pytest.mark.gpu
 
 ADJ_CASES = ["lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "mix1d_fmt4", "rough3d_fmt2", "rough3d_fmt4",
-             "hs1d_wall", "hs1d_c1", "hs1d_fmt2", "hs1d_fmt4", "hs1d_reflect", "hslj1d_wall", "lj1d_a22"]
+             "hs1d_wall", "hs1d_c1", "hs1d_fmt2", "hs1d_fmt4", "hs1d_reflect", "hslj1d_wall", "lj1d_a22",
+             "lv1d_interface", "lv1d_bulkbc"]
 # hs*1d_*: hard-wall boundary weights (hslj1d_wall also on the mean-field stencil); hs1d_reflect also a
-# reflecting boundary; lj1d_a22: the mean field summed into the Euler-Lagrange rows (ATTInA22Block = 1)
+# reflecting boundary; lj1d_a22: the mean field summed into the Euler-Lagrange rows (ATTInA22Block = 1);
+# lv1d_*: a liquid-vapour interface (bulk states on either side, a pinned density at the mid-plane)
 GRAD_RTOL = 1e-5
 FD_H = 1e-6
 

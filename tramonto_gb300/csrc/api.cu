@@ -68,19 +68,21 @@ T *upload(const std::vector<T> &h, cudaStream_t s)
 
 // One-dimensional source map of the padded box: q -> node index (with the
 // reflect bit) or a sentinel, following offset_to_node_box (src/dft_mesh_lib.c:203-297).
-std::vector<int> build_map(int n, int h, int bcl, int bcr)
+std::vector<int> build_map(int n, int h, int bcl, int bcr, bool interface)
 {
+  // bulk beyond the low side (LBB under a phase interface) and beyond the high side (RTF)
+  const int blo = tgpu::kSentBulk, bhi = interface ? tgpu::kSentBulkHi : tgpu::kSentBulk;
   std::vector<int> m(n + 2 * h);
   for (int q = 0; q < n + 2 * h; q++) {
     int s = q - h;
     int v;
     if (s < 0) {
       switch (bcl) {
-        case TGPU_BC_IN_BULK: v = tgpu::kSentBulk; break;
+        case TGPU_BC_IN_BULK: v = blo; break;
         case TGPU_BC_IN_WALL: v = tgpu::kSentWall; break;
         case TGPU_BC_REFLECT:
           s = -s;
-          if (s >= n) v = bcr == TGPU_BC_IN_BULK ? tgpu::kSentBulk : (bcr == TGPU_BC_IN_WALL ? tgpu::kSentWall : tgpu::kSentBad);
+          if (s >= n) v = bcr == TGPU_BC_IN_BULK ? bhi : (bcr == TGPU_BC_IN_WALL ? tgpu::kSentWall : tgpu::kSentBad);
           else v = s | tgpu::kReflBit;
           break;
         case TGPU_BC_PERIODIC: s += n; v = s >= 0 ? s : tgpu::kSentBad; break;
@@ -88,11 +90,11 @@ std::vector<int> build_map(int n, int h, int bcl, int bcr)
       }
     } else if (s >= n) {
       switch (bcr) {
-        case TGPU_BC_IN_BULK: v = tgpu::kSentBulk; break;
+        case TGPU_BC_IN_BULK: v = bhi; break;
         case TGPU_BC_IN_WALL: v = tgpu::kSentWall; break;
         case TGPU_BC_REFLECT:
           s = 2 * (n - 1) - s;
-          if (s < 0) v = bcl == TGPU_BC_IN_BULK ? tgpu::kSentBulk : (bcl == TGPU_BC_IN_WALL ? tgpu::kSentWall : tgpu::kSentBad);
+          if (s < 0) v = bcl == TGPU_BC_IN_BULK ? blo : (bcl == TGPU_BC_IN_WALL ? tgpu::kSentWall : tgpu::kSentBad);
           else v = s | tgpu::kReflBit;
           break;
         case TGPU_BC_PERIODIC: s -= n; v = s < n ? s : tgpu::kSentBad; break;
@@ -176,32 +178,40 @@ void need_final(Ctx *c)
 
 // Values the padded boxes take at bulk sentinels: the bulk densities (density channels) and the
 // bulk dPhi/dn combinations of the Euler-Lagrange channels (Dphi_Drhobar_b, src/dft_fill_FMT.c:104-127).
+// The padded boxes hold both sides' values, [low side channels][high side channels]: the same uniform bulk
+// twice, or the LBB and RTF states of a phase interface (Rho_b_LBB/_RTF, Dphi_Drhobar_LBB/_RTF).
 std::vector<double> bulk_values_rho(const tgpu_geometry &g)
 {
   std::vector<double> v;
-  for (int jc = 0; jc < g.ncomp; jc++) v.push_back(g.rho_b[jc]);
+  for (int side = 0; side < 2; side++)
+    for (int jc = 0; jc < g.ncomp; jc++)
+      v.push_back(g.interface == 2 ? (side ? g.rho_b_rtf[jc] : g.rho_b_lbb[jc]) : g.rho_b[jc]);
   return v;
 }
 
 std::vector<double> bulk_values_tr(const tgpu_geometry &g)
 {
   std::vector<double> v;
-  for (int ic = 0; ic < g.ncomp; ic++) {
-    const double f = g.fac_overlap[ic];
-    const double *b = g.dphi_bulk;
-    v.push_back(f * (b[0] * g.inv_4pirsq[ic] + b[1] * g.inv_4pir[ic] + b[2]));
-    for (int d = 0; d < g.ndim; d++) v.push_back(0.0);
-    v.push_back(f * b[3]);
-  }
+  for (int side = 0; side < 2; side++)
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      const double f = g.fac_overlap[ic];
+      const double *b = g.interface == 2 ? (side ? g.dphi_rtf : g.dphi_lbb) : g.dphi_bulk;
+      v.push_back(f * (b[0] * g.inv_4pirsq[ic] + b[1] * g.inv_4pir[ic] + b[2]));
+      for (int d = 0; d < g.ndim; d++) v.push_back(0.0);
+      v.push_back(f * b[3]);
+    }
   return v;
 }
 
+// bulk: [low side][high side] (2 nch values), or nch values used for both sides
 PadParams make_pad(const std::vector<double> &bulk, const std::vector<int> &sign, const std::vector<int> &zc,
                    cudaStream_t s)
 {
   PadParams p;
-  p.nch = (int)bulk.size();
-  p.bulk = upload(bulk, s);
+  p.nch = (int)sign.size();
+  std::vector<double> b2(bulk);
+  if ((int)b2.size() == p.nch) b2.insert(b2.end(), bulk.begin(), bulk.end());
+  p.bulk = upload(b2, s);
   p.sign = upload(sign, s);
   p.zc = upload(zc, s);
   return p;
@@ -1249,7 +1259,8 @@ void build_device_tables(Ctx *c)
   NP = (long)dg.P[0] * dg.P[1] * dg.P[2];
   dg.NP = NP;
   for (int d = 0; d < 3; d++) {
-    std::vector<int> m = d < nd ? build_map(dg.nx[d], dg.h[d], g.bc[d][0], g.bc[d][1]) : std::vector<int>{0};
+    std::vector<int> m = d < nd ? build_map(dg.nx[d], dg.h[d], g.bc[d][0], g.bc[d][1], g.interface == 2)
+                                : std::vector<int>{0};
     c->d_map[d] = upload(m, c->stream);
     dg.map[d] = c->d_map[d];
   }
@@ -1467,6 +1478,8 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
       if ((g.bc[d][0] == TGPU_BC_PERIODIC) != (g.bc[d][1] == TGPU_BC_PERIODIC))
         throw Error(TGPU_ERR_ARG, "periodic boundaries must be periodic on both sides");
     }
+    if (g.interface != 0 && g.interface != 2) throw Error(TGPU_ERR_UNSUPPORTED, "interface type (0 or 2)");
+    if (g.pin && g.interface != 2) throw Error(TGPU_ERR_ARG, "a pinned density needs a phase interface");
     if (g.functional < TGPU_FMT1 || g.functional > TGPU_FMT4)
       throw Error(TGPU_ERR_UNSUPPORTED, "functional outside FMT1..FMT4");
     if (g.hard_surf && g.ncomp > 2) throw Error(TGPU_ERR_UNSUPPORTED, "hard walls with more than two components");
@@ -1487,6 +1500,11 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
     dg.first_mf = g.attraction ? g.ncomp + dg.nrb : -1;
     dg.nunk = g.ncomp + dg.nrb + (g.attraction ? g.ncomp : 0);
     c->a22 = g.attraction && g.att_in_a22;
+    dg.interface = g.interface;
+    for (int i = 0; i < TGPU_MAXC; i++) dg.betamu_if[i] = g.betamu[i];
+    dg.pin_node = g.pin ? g.pin_node : -1;
+    dg.pin_value = g.pin_value;
+    if (g.pin && (g.pin_node < 0 || g.pin_node >= N)) throw Error(TGPU_ERR_ARG, "pinned node outside the mesh");
     c->nunk_ext = c->a22 ? dg.nunk - g.ncomp : dg.nunk;
     dg.functional = g.functional;
     dg.attraction = g.attraction;

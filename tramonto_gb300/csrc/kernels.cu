@@ -78,6 +78,7 @@ __global__ void k_pad(const double *__restrict__ src, T *__restrict__ dst, int n
     for (int ch = 0; ch < nch; ch++) {
       double v;
       if (sent == kSentBulk) v = bulk[ch];
+      else if (sent == kSentBulkHi) v = bulk[nch + ch];   // the high side's bulk (phase interfaces)
       else if (sent == kSentWall) v = 0.0;
       else if (sent != 0) v = __longlong_as_double(0x7ff8000000000000ULL);
       else if (no_mirror && refl) v = 0.0;
@@ -707,8 +708,14 @@ void launch_fmt_local(const double *x, double *chan, cudaStream_t s)
   k_fmt_local<<<1184, kThreads, 0, s>>>(x, chan);
 }
 
+// The pinned density of a constrained interface: R = ln rho - ln pin_value, J = 1/rho on the diagonal
+// only (fill_constant_density, src/dft_fill_EL.c:286-305)
+__device__ __forceinline__ bool pin_row(int ic, long i) { return ic == 0 && i == c_g.pin_node; }
+
+// Euler-Lagrange rows without nonlocal couplings: zero-density rows (R = rho, J = 1) and the pinned row
 __device__ __forceinline__ bool zero_row(const double *vext, const signed char *zero, int ic, long i)
 {
+  if (pin_row(ic, i)) return true;
   const long k = (long)ic * c_g.N + i;
   return zero[k] || vext[k] == c_g.vext_max;
 }
@@ -735,10 +742,15 @@ __global__ void k_assemble(const double *__restrict__ x, const double *__restric
       const double xi = x[(long)iu * N + i];
       double r;
       if (zero_row(vext, zero, ic, i)) {
-        r = xi;
+        r = pin_row(ic, i) ? log(xi) - log(c_g.pin_value) : xi;
       } else {
-        double mu = -log(c_g.rho_b[ic]) - c_g.betamu_hs_ex[ic];
-        if (c_g.attraction) mu -= c_g.betamu_att[ic];
+        double mu;
+        if (c_g.interface) {
+          mu = -c_g.betamu_if[ic];
+        } else {
+          mu = -log(c_g.rho_b[ic]) - c_g.betamu_hs_ex[ic];
+          if (c_g.attraction) mu -= c_g.betamu_att[ic];
+        }
         r = log(xi) + mu + vext[(long)ic * N + i] + tr[(long)ic * N + i];
         if (c_g.attraction) r += x[(long)(c_g.first_mf + ic) * N + i];
       }
@@ -826,7 +838,7 @@ __global__ void k_schur_combine(const double *__restrict__ x, const double *__re
     for (int ic = 0; ic < c_g.ncomp; ic++) {
       const long k = (long)ic * N + i;
       if (zero_row(vext, zero, ic, i)) {
-        y2[k] = v2[k];
+        y2[k] = pin_row(ic, i) ? v2[k] / x[(long)(c_g.first_rho + ic) * N + i] : v2[k];
       } else {
         double a21y = tr[k];
         if (c_g.attraction) a21y += ymf[k];
@@ -851,7 +863,7 @@ __global__ void k_jv_combine(const double *__restrict__ x, const double *__restr
       const int iu = c_g.first_rho + ic;
       const long k = (long)iu * N + i;
       if (zero_row(vext, zero, ic, i)) {
-        out[k] = v[k];
+        out[k] = pin_row(ic, i) ? v[k] / x[k] : v[k];
       } else {
         double r = v[k] / x[k] + tr[(long)ic * N + i];
         if (c_g.attraction) r += v[(long)(c_g.first_mf + ic) * N + i];
@@ -1028,7 +1040,7 @@ __global__ void k_jtv_local(const double *__restrict__ x, const double *__restri
       const bool zr = zero_row(vext, zero, ic, i);
       const double wel = zr ? 0.0 : w[kr];
       // density column: transposed sums already in out; add the A22 diagonal
-      out[kr] += zr ? w[kr] : w[kr] / x[kr];
+      out[kr] += (zr && !pin_row(ic, i)) ? w[kr] : w[kr] / x[kr];
       if (c_g.attraction) {
         const long km = (long)(c_g.first_mf + ic) * N + i;
         out[km] = -w[km] + wel;
@@ -1507,7 +1519,8 @@ __global__ void k_precond(const double *__restrict__ x, const double *__restrict
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     for (int ic = 0; ic < c_g.ncomp; ic++) {
       const long k = (long)ic * N + i;
-      out[k] = zero_row(vext, zero, ic, i) ? in[k] : in[k] * x[(long)(c_g.first_rho + ic) * N + i];
+      out[k] = (zero_row(vext, zero, ic, i) && !pin_row(ic, i)) ? in[k]
+                                                                 : in[k] * x[(long)(c_g.first_rho + ic) * N + i];
     }
 }
 

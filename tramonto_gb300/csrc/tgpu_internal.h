@@ -24,7 +24,7 @@ namespace tgpu {
 
 constexpr int kMaxC = TGPU_MAXC;
 constexpr int kMaxRb = 10;            // 4 + 2*3 weighted densities
-constexpr int kSentBulk = -1, kSentWall = -2, kSentBad = -9;
+constexpr int kSentBulk = -1, kSentWall = -2, kSentBulkHi = -3, kSentBad = -9;   // kSentBulk: the low side's bulk
 constexpr int kReflBit = 1 << 30;     // flag bit in a per-dimension map entry
 
 // Geometry constants visible to every kernel (one problem per launch).
@@ -34,6 +34,10 @@ struct DevGeom {
   int ncomp, nrb, nunk, first_rho, first_rb, first_mf;
   int functional, attraction, single_size, hard_surf, nlists;
   int jac_exact;                       // 1: Hessian of the energy density; 0: the reference's tables
+  int interface;                       // 2: phase interface (EL rows take betamu_if)
+  double betamu_if[kMaxC];
+  long pin_node;                       // first component's density held at pin_value there (-1: none)
+  double pin_value;
   double esize[3];
   double rho_b[kMaxC], betamu_hs_ex[kMaxC], betamu_att[kMaxC];
   double inv_rad[kMaxC], inv_4pir[kMaxC], inv_4pirsq[kMaxC], fac[kMaxC];

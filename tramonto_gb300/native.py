@@ -49,6 +49,9 @@ class Geometry(C.Structure):
         ("rho_b", C.c_double * 4), ("betamu_hs_ex", C.c_double * 4), ("betamu_att", C.c_double * 4),
         ("inv_rad", C.c_double * 4), ("inv_4pir", C.c_double * 4), ("inv_4pirsq", C.c_double * 4),
         ("fac_overlap", C.c_double * 4), ("dphi_bulk", C.c_double * 4), ("vext_max", C.c_double),
+        ("interface", C.c_int), ("rho_b_lbb", C.c_double * 4), ("rho_b_rtf", C.c_double * 4),
+        ("dphi_lbb", C.c_double * 4), ("dphi_rtf", C.c_double * 4), ("betamu", C.c_double * 4),
+        ("pin", C.c_int), ("pin_node", C.c_long), ("pin_value", C.c_double),
     ]
 
 
@@ -142,6 +145,16 @@ def geometry(p: Problem) -> Geometry:
     for i in range(4):
         g.dphi_bulk[i] = float(p.dphi_bulk[i])
     g.vext_max = float(p.vext_max)
+    g.interface = int(p.interface)
+    if p.interface:
+        for name, src in (("rho_b_lbb", p.rho_b_lbb), ("rho_b_rtf", p.rho_b_rtf), ("dphi_lbb", p.dphi_lbb),
+                          ("dphi_rtf", p.dphi_rtf), ("betamu", p.betamu_if)):
+            arr = getattr(g, name)
+            for i, v in enumerate(np.asarray(src, np.float64)[:4]):
+                arr[i] = float(v)
+    g.pin = int(p.pin_node >= 0)
+    g.pin_node = int(max(p.pin_node, 0))
+    g.pin_value = float(p.pin_value)
     return g
 
 

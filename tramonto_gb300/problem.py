@@ -48,6 +48,15 @@ class Problem:
     fac_overlap: np.ndarray = None
     dphi_bulk: np.ndarray = None   # bulk dPhi/dn0..dn3 (Dphi_Drhobar_b)
     vext_max: float = 1e300
+    # phase interface (Type_interface 2): low/high-side bulk states, the EL chemical potential, a pinned density
+    interface: int = 0
+    rho_b_lbb: np.ndarray = None
+    rho_b_rtf: np.ndarray = None
+    dphi_lbb: np.ndarray = None
+    dphi_rtf: np.ndarray = None
+    betamu_if: np.ndarray = None
+    pin_node: int = -1
+    pin_value: float = 0.0
     vext: np.ndarray = None        # [ncomp][N]
     zero_density: np.ndarray = None  # [ncomp][N] int8
     boundary_nodes: np.ndarray = None  # [nlists][N] int32, -1 = not a boundary node
@@ -123,6 +132,19 @@ def from_golden(z) -> Problem:
         fluid_masks=np.asarray(z["fluid_masks"], np.int16) if "fluid_masks" in z.files else None,
         stencils=st)
     assert p.nunk == int(ints[7]), (p.nunk, int(ints[7]))
+    if len(ints) > 45 and int(ints[36]) == 2:     # Type_interface = PHASE_INTERFACE
+        p.interface = 2
+        if nwall == 0:                            # LBB / RTF sentinels beyond bulk boundaries
+            p.rho_b_lbb, p.rho_b_rtf = np.array(d[329:329 + ncomp]), np.array(d[335:335 + ncomp])
+            p.dphi_lbb, p.dphi_rtf = np.array(d[341:345]), np.array(d[351:355])
+        else:
+            p.rho_b_lbb, p.rho_b_rtf = p.rho_b.copy(), p.rho_b.copy()
+            p.dphi_lbb, p.dphi_rtf = p.dphi_bulk.copy(), p.dphi_bulk.copy()
+        p.betamu_if = np.array(d[361:361 + ncomp])
+        if int(ints[44]):                         # Lconstrain_interface
+            gd = int(ints[45])
+            p.pin_node = int(0.5 * d[3 + gd] / d[gd])
+            p.pin_value = 0.5 * (float(d[329]) + float(d[335]))
     if "integ" in z.files:
         integ = np.asarray(z["integ"])
         vol_el, nel_v, area, fac_vol, fac_area, per_area = integ[:6]
@@ -131,5 +153,14 @@ def from_golden(z) -> Problem:
         p.w_fluid = np.asarray(z["nel_hit2"], np.float64) * unit
         p.w_bulk = np.asarray(z["nel_hit"], np.float64) * unit
         p.rhobar_b = np.array(d[55:59])
+        if p.interface:
+            # the bulk free-energy density of an interface is that of the high-side state
+            # (Rhobar_b_RTF, integrand_hs_freen_bulk, src/dft_energy_hs.c:45-60; rhobar_icomp,
+            # src/dft_thermo_hs.c:292-311); n3 n2 n1 n0 as Rhobar_b
+            rtf, hs = np.array(d[335:335 + ncomp]), p.hs_diam
+            fo = p.fac_overlap
+            area = np.pi * hs * hs * rtf * fo
+            p.rhobar_b = np.array([np.sum(np.pi * hs ** 3 / 6.0 * rtf * fo), np.sum(area),
+                                   np.sum(area * p.inv_4pir), np.sum(area * p.inv_4pirsq)])
         p.betamu = np.array(integ[6:6 + ncomp])
     return p
