@@ -562,7 +562,44 @@ typedef struct {
   double *R;            /* may be NULL */
   entry_fn entry;       /* may be NULL */
   void *ctx;
+  int izone, jzone;     /* quadrature zones of the current node's residual and Jacobian */
 } pass_t;
+
+/* Stencil[stype][zone][index] (zone 0: the sten_* tables) */
+static int zone_sten(const orc_problem *p, int zone, int stype, int index, const short **off, const double **w,
+                     const double **hw)
+{
+  if (zone == 0) {
+    *off = p->sten_off[stype][index];
+    *w = p->sten_w[stype][index];
+    *hw = p->sten_hw[stype][index];
+    return p->sten_len[stype][index];
+  }
+  *off = p->zsten_off[zone][stype][index];
+  *w = p->zsten_w[zone][stype][index];
+  *hw = p->zsten_hw[zone][stype][index];
+  return p->zsten_len[zone][stype][index];
+}
+
+/* find_jzone (src/dft_utils.c:67-86) */
+static int find_jzone(const orc_problem *p, int izone, long inode)
+{
+  enum { SAME = 0, ZONE0_FAC2 = 1, ZONES_FAC2 = 2, ALLMOSTCOARSE = 3, SECONDMOSTCOARSE = 4, FIXED_ESIZE = 5 };
+  if (p->coarser_jac != SAME && izone < p->nzone - 1) {
+    switch (p->coarser_jac) {
+      case ZONE0_FAC2: return izone == 0 ? izone + 1 : izone;
+      case ZONES_FAC2: return izone + 1;
+      case ALLMOSTCOARSE: case FIXED_ESIZE: return p->nzone - 1;
+      case SECONDMOSTCOARSE: return p->nzone - 2;
+      default: return izone;
+    }
+  }
+  if (p->coarser_jac == SAME) {
+    if (p->mesh_coarsening || p->nwall == 0 || !p->zone_flag) return izone;
+    return p->zone_flag[inode];
+  }
+  return izone;
+}
 
 static int is_dep_rb(const orc_problem *p, int k)
 {
@@ -584,10 +621,10 @@ static double sten_sum(pass_t *ps, int stype, int iu, long inode, const int *ijk
     const int ju = p->first_rho + jc;
     const int jlist = (p->nlists_hw <= 2) ? 0 : jc;
     const int index = (stype == ORC_UATT) ? icomp_pair + p->ncomp * jc : jc;
-    const int L = p->sten_len[stype][index];
-    const short *off = p->sten_off[stype][index];
-    const double *w = p->sten_w[stype][index];
-    const double *hw = p->sten_hw[stype][index];
+    const short *off;
+    const double *w, *hw;
+    /* the weighted-density and mean-field rows take their Jacobian from the residual's zone */
+    const int L = zone_sten(p, ps->izone, stype, index, &off, &w, &hw);
     for (int s = 0; s < L; s++) {
       const short *o = off + (long)s * nd;
       double weight = w[s];
@@ -626,10 +663,13 @@ static double rosen_rb(pass_t *ps, int stype, int iu, long inode, const int *ijk
   const orc_problem *p = ps->p;
   const long N = orc_nnodes(p);
   const int nd = p->ndim;
-  const int L = p->sten_len[stype][ic];
-  const short *off = p->sten_off[stype][ic];
-  const double *w = p->sten_w[stype][ic];
+  const short *off, *offJ;
+  const double *w, *hw, *wJ, *hwJ;   /* the corner weights do not enter these rows */
+  const int L = zone_sten(p, ps->izone, stype, ic, &off, &w, &hw);
+  const int LJ = zone_sten(p, ps->jzone, stype, ic, &offJ, &wJ, &hwJ);
   const double fo = p->fac_overlap[ic];
+  (void)hw;
+  (void)hwJ;
   double resid_sum = 0.0;
   int reflect[3];
   for (int s = 0; s < L; s++) {
@@ -657,27 +697,79 @@ static double rosen_rb(pass_t *ps, int stype, int iu, long inode, const int *ijk
       resid = 0.0;
     }
     resid_sum += resid;
-    if (ps->entry && jn >= 0) {
+    /* the Jacobian entries come from point s of the Jacobian zone's stencil (:144-156) */
+    const short *oj = o;
+    double weightJ = weight;
+    long jnj = jn;
+    if (ps->entry && s < LJ && ps->jzone != ps->izone) {
+      oj = offJ + (long)s * nd;
+      weightJ = wJ[s];
+      jnj = offset_to_node(p, ijk, oj, reflect);
+    }
+    if (ps->entry && s < LJ && jnj >= 0) {
       double n[10], sign[3];
       for (int d = 0; d < nd; d++) sign[d] = reflect[d] ? -1.0 : 1.0;
-      sv_to_n(p, ps->x, jn, n);
+      sv_to_n(p, ps->x, jnj, n);
       rbs t;
       if (stype == ORC_DELTA)
-        t = d2_delta(p, n, o, sign, ic);
+        t = d2_delta(p, n, oj, sign, ic);
       else
         t = d2_theta(p, n);
       const int jb = p->first_rb;
-      ps->entry(ps->ctx, iu, inode, jb + 0, jn, fo * weight * t.S3);
-      ps->entry(ps->ctx, iu, inode, jb + 1, jn, fo * weight * t.S2);
-      ps->entry(ps->ctx, iu, inode, jb + 2, jn, fo * weight * t.S1);
-      ps->entry(ps->ctx, iu, inode, jb + 3, jn, fo * weight * t.S0);
+      ps->entry(ps->ctx, iu, inode, jb + 0, jnj, fo * weightJ * t.S3);
+      ps->entry(ps->ctx, iu, inode, jb + 1, jnj, fo * weightJ * t.S2);
+      ps->entry(ps->ctx, iu, inode, jb + 2, jnj, fo * weightJ * t.S1);
+      ps->entry(ps->ctx, iu, inode, jb + 3, jnj, fo * weightJ * t.S0);
       for (int d = 0; d < nd; d++) {
-        ps->entry(ps->ctx, iu, inode, jb + 4 + d, jn, fo * weight * t.V2[d]);
-        ps->entry(ps->ctx, iu, inode, jb + 4 + nd + d, jn, fo * weight * t.V1[d]);
+        ps->entry(ps->ctx, iu, inode, jb + 4 + d, jnj, fo * weightJ * t.V2[d]);
+        ps->entry(ps->ctx, iu, inode, jb + 4 + nd + d, jnj, fo * weightJ * t.V1[d]);
       }
     }
   }
   return resid_sum;
+}
+
+/* constant_boundary (src/dft_utils.c:89-110) for the unknowns of these problems */
+static double coarse_value(const orc_problem *p, int iu, long jn)
+{
+  if (iu >= p->first_rho && iu < p->first_rho + p->ncomp) {
+    const int ic = iu - p->first_rho;
+    if (jn == -1) return p->rho_b[ic];
+    if (jn == -3) return p->rho_b_lbb[ic];
+    if (jn == -4) return p->rho_b_rtf[ic];
+    return 0.0;
+  }
+  if (iu >= p->first_rb && iu < p->first_rb + 4 + 2 * p->ndim && jn == -1) return p->rhobar_bc[iu - p->first_rb];
+  return 0.0;   /* inside a wall; (the reference leaves mean-field boundary values undefined) */
+}
+
+/* locate_neighbor_unks + load_coarse_variable (src/dft_fill_coarse.c:86-123): the two neighbours of
+ * `node` along its averaging direction, each with weight fac; with two zones a coarsened neighbour is
+ * replaced by its own neighbours (half the weight each) */
+static void coarse_terms(pass_t *ps, int iu, long row, long node, double fac, double *R)
+{
+  static const short off_pm[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+  const orc_problem *p = ps->p;
+  const long N = orc_nnodes(p);
+  int ijk[3], reflect[3];
+  node_to_ijk(p, node, ijk);
+  const int d = -p->zone_flag[node] - 1;
+  for (int loop = 0; loop < 2; loop++) {
+    const long jn = offset_to_node(p, ijk, off_pm[d + 3 * loop], reflect);
+    if (jn >= 0 && p->zone_flag[jn] < 0 && p->nzone == 2) {
+      coarse_terms(ps, iu, row, jn, 0.5 * fac, R);
+    } else if (jn < 0) {
+      *R -= fac * coarse_value(p, iu, jn);
+    } else {
+      *R -= fac * ps->x[(long)iu * N + jn];
+      if (ps->entry) ps->entry(ps->ctx, iu, row, iu, jn, -fac);
+    }
+  }
+}
+
+static int coarsened(const orc_problem *p)
+{
+  return p->zone_flag && p->mesh_coarsening && p->nwall > 0;
 }
 
 static void fill_node(pass_t *ps, long inode)
@@ -689,6 +781,20 @@ static void fill_node(pass_t *ps, long inode)
   const double *x = ps->x;
   int ijk[3];
   node_to_ijk(p, inode, ijk);
+  /* fill_resid_and_matrix (src/dft_fill_main.c:118-135): the node's zone, or an averaged row */
+  const int flag = coarsened(p) ? p->zone_flag[inode] : 0;
+  if (flag < 0) {
+    for (int iu = 0; iu < p->nunk; iu++) {   /* load_coarse_node_Ndim (src/dft_fill_coarse.c:66-84) */
+      const double fac = (iu >= p->first_rho && iu < p->first_rho + p->ncomp) ? 1.0 : -1.0;
+      double R = fac * x[(long)iu * N + inode];
+      if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, fac);
+      coarse_terms(ps, iu, inode, inode, 0.5 * fac, &R);
+      if (ps->R) ps->R[(long)iu * N + inode] = R;
+    }
+    return;
+  }
+  ps->izone = flag;
+  ps->jzone = find_jzone(p, flag, inode);
   for (int iu = 0; iu < p->nunk; iu++) {
     double R = 0.0;
     const double xi = x[(long)iu * N + inode];
@@ -768,7 +874,7 @@ static int run_pass(const orc_problem *p, const double *x, double *R, entry_fn e
   double *dphi = (double *)malloc(sizeof(double) * (size_t)nrb * (size_t)N);
   if (!dphi) return -1;
   orc_dphi(p, x, dphi);  /* FMT1stDeriv_switch over every box node (src/dft_switch_FMT.c:68-96) */
-  pass_t ps = {p, x, dphi, R, e, ctx};
+  pass_t ps = {p, x, dphi, R, e, ctx, 0, 0};
   for (long i = b; i < end; i++) fill_node(&ps, i);
   free(dphi);
   return 0;
@@ -819,6 +925,9 @@ int orc_jtv(const orc_problem *p, const double *x, const double *w, double *JTw)
  * each block product taken from the Jacobian product J v. */
 int orc_schur(const orc_problem *p, const double *x, const double *v2, double *Sv2)
 {
+  if (coarsened(p))
+    for (long i = 0; i < orc_nnodes(p); i++)
+      if (p->zone_flag[i] < 0) return -2;
   const long N = orc_nnodes(p);
   const long U = p->nunk;
   const int nrb = 4 + 2 * p->ndim;

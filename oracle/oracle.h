@@ -33,6 +33,7 @@ extern "C" {
 #endif
 
 #define ORC_MAXC 4
+#define ORC_MAXZ 5
 
 enum { ORC_DELTA = 0, ORC_THETA = 1, ORC_UATT = 2 };
 enum { ORC_BC_IN_WALL = -1, ORC_BC_IN_BULK = 0, ORC_BC_PERIODIC = 1, ORC_BC_REFLECT = 2 };
@@ -72,6 +73,19 @@ typedef struct {
   double betamu[ORC_MAXC];
   long pin_node;              /* -1: no pinned density */
   double pin_value;
+  /* quadrature zones and mesh coarsening (Nzone, Mesh_coarsening, Coarser_jac; calc_stencils
+   * src/dft_stencil.c:96-109, 229-236; set_mesh_coarsen_flag src/dft_mesh.c:2788-2850):
+   * zone_flag[N] is Mesh_coarsen_flag (NULL: zone 0 everywhere); a node with flag >= 0 fills its
+   * residual with that zone's stencils (offsets in fine-node units), its Jacobian with find_jzone's
+   * (src/dft_utils.c:67-86); flag -1/-2/-3 rows average the two neighbours along x/y/z
+   * (load_coarse_node_Ndim, src/dft_fill_coarse.c:66-123).  Zone 0 uses the sten_* tables. */
+  int nzone, mesh_coarsening, coarser_jac, nwall;
+  const int *zone_flag;
+  int zsten_len[ORC_MAXZ][3][ORC_MAXC * ORC_MAXC];
+  const short *zsten_off[ORC_MAXZ][3][ORC_MAXC * ORC_MAXC];
+  const double *zsten_w[ORC_MAXZ][3][ORC_MAXC * ORC_MAXC];
+  const double *zsten_hw[ORC_MAXZ][3][ORC_MAXC * ORC_MAXC];
+  double rhobar_bc[10];       /* Rhobar_b in solution order: constant_boundary of the rb unknowns */
 } orc_problem;
 
 long orc_nnodes(const orc_problem *p);
@@ -82,7 +96,8 @@ int orc_resid(const orc_problem *p, const double *x, double *R);
 /* Jacobian products with the reference's Jacobian entries at state x */
 int orc_jv(const orc_problem *p, const double *x, const double *v, double *Jv);
 int orc_jtv(const orc_problem *p, const double *x, const double *w, double *JTw);
-/* Schur product S v2 on the density block ([ncomp][N] in and out) */
+/* Schur product S v2 on the density block ([ncomp][N] in and out); -2 with coarsened nodes, whose
+ * unknowns the reference moves into the second block */
 int orc_schur(const orc_problem *p, const double *x, const double *v2, double *Sv2);
 /* Residual of the first `nrows` nodes only (bounded CPU samples); R is [nunk][N], other rows untouched */
 int orc_resid_rows(const orc_problem *p, const double *x, double *R, long node_begin, long node_end);

@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 MAXC = 4
+MAXZ = 5
 
 
 def build(force: bool = False) -> str:
@@ -49,6 +50,13 @@ class _Problem(C.Structure):
         ("interface", C.c_int), ("rho_b_lbb", C.c_double * MAXC), ("rho_b_rtf", C.c_double * MAXC),
         ("dphi_lbb", C.c_double * 4), ("dphi_rtf", C.c_double * 4), ("betamu", C.c_double * MAXC),
         ("pin_node", C.c_long), ("pin_value", C.c_double),
+        ("nzone", C.c_int), ("mesh_coarsening", C.c_int), ("coarser_jac", C.c_int), ("nwall", C.c_int),
+        ("zone_flag", C.POINTER(C.c_int)),
+        ("zsten_len", ((C.c_int * (MAXC * MAXC)) * 3) * MAXZ),
+        ("zsten_off", ((C.POINTER(C.c_int16) * (MAXC * MAXC)) * 3) * MAXZ),
+        ("zsten_w", ((C.POINTER(C.c_double) * (MAXC * MAXC)) * 3) * MAXZ),
+        ("zsten_hw", ((C.POINTER(C.c_double) * (MAXC * MAXC)) * 3) * MAXZ),
+        ("rhobar_bc", C.c_double * 10),
     ]
 
 
@@ -114,6 +122,29 @@ class Oracle:
                 hw = np.ascontiguousarray(hw, np.float64)
                 self._keep.append(hw)
                 s.sten_hw[stype][idx] = _dp(hw)
+        s.nzone = int(getattr(prob, "nzone", 1))
+        s.mesh_coarsening, s.coarser_jac = int(getattr(prob, "mesh_coarsening", 0)), int(getattr(prob, "coarser_jac", 0))
+        s.nwall = int(getattr(prob, "nwall", 0))
+        if getattr(prob, "zone_flag", None) is not None:
+            zf = np.ascontiguousarray(prob.zone_flag, np.int32)
+            self._keep.append(zf)
+            s.zone_flag = zf.ctypes.data_as(C.POINTER(C.c_int))
+        for zone, tabs in (getattr(prob, "zone_stencils", None) or {}).items():
+            for (stype, idx), (off, w, hw) in tabs.items():
+                off = np.ascontiguousarray(off, np.int16)
+                w = np.ascontiguousarray(w, np.float64)
+                self._keep += [off, w]
+                s.zsten_len[zone][stype][idx] = len(w)
+                s.zsten_off[zone][stype][idx] = off.ctypes.data_as(C.POINTER(C.c_int16))
+                s.zsten_w[zone][stype][idx] = _dp(w)
+                if hw is not None:
+                    hw = np.ascontiguousarray(hw, np.float64)
+                    self._keep.append(hw)
+                    s.zsten_hw[zone][stype][idx] = _dp(hw)
+        rbc = getattr(prob, "rhobar_bc", None)
+        if rbc is not None:
+            for i, v in enumerate(np.asarray(rbc, np.float64)[:10]):
+                s.rhobar_bc[i] = float(v)
         self.s = s
 
     def _vec(self, x, rows=None):

@@ -52,6 +52,7 @@ struct Mgr {
   std::vector<int> ind, dep, dens;
   bool haveLists = false;
   bool a22Diagonal = true;
+  std::vector<char> coarse;              // per global node: rows average the neighbours (block 2)
   ParamList params;
   // values of the current fill
   std::vector<double> rhs;               // [iunk][owned]
@@ -119,11 +120,22 @@ struct Schur {
     for (int u : m.ind) order1.push_back(u);
     for (int u : m.dep) order1.push_back(u);
     for (int u : m.dens) order2.push_back(u);
+    // every unknown of a coarsened node belongs to block 2 (src/dft_HardSphereLinProbMgr.cpp:119-158)
+    auto isCoarse = [&](int g) { return !m.coarse.empty() && m.coarse[g]; };
     for (int u : order1)
-      for (int g = 0; g < m.nGlobal; ++g) { gid2pos[u * m.nGlobal + g] = (int)pos2gid.size(); pos2gid.push_back(u * m.nGlobal + g); isDep.push_back(std::find(m.dep.begin(), m.dep.end(), u) != m.dep.end()); }
+      for (int g = 0; g < m.nGlobal; ++g) {
+        if (isCoarse(g)) continue;
+        gid2pos[u * m.nGlobal + g] = (int)pos2gid.size(); pos2gid.push_back(u * m.nGlobal + g); isDep.push_back(std::find(m.dep.begin(), m.dep.end(), u) != m.dep.end());
+      }
     n1 = (int)pos2gid.size();
     for (int u : order2)
-      for (int g = 0; g < m.nGlobal; ++g) { gid2pos[u * m.nGlobal + g] = (int)pos2gid.size(); pos2gid.push_back(u * m.nGlobal + g); }
+      for (int g = 0; g < m.nGlobal; ++g) {
+        if (isCoarse(g)) continue;
+        gid2pos[u * m.nGlobal + g] = (int)pos2gid.size(); pos2gid.push_back(u * m.nGlobal + g);
+      }
+    for (int g = 0; g < m.nGlobal; ++g)
+      if (isCoarse(g))
+        for (int u = 0; u < m.numUnks; ++u) { gid2pos[u * m.nGlobal + g] = (int)pos2gid.size(); pos2gid.push_back(u * m.nGlobal + g); }
     n2 = (int)pos2gid.size() - n1;
     auto init = [](Csr &c, int rows) { c.n = rows; c.ptr.assign(rows + 1, 0); c.col.clear(); c.val.clear(); };
     init(A11B, n1); init(A12, n1); init(A21, n2); init(A22, n2);
@@ -439,9 +451,13 @@ int dft_linprobmgr_setnodalcolmap(void *h, int n, int *gids)
   m.B2G.assign(gids, gids + n);
   return 0;
 }
-int dft_linprobmgr_setcoarsenednodeslist(void *, int n, int *)
+int dft_linprobmgr_setcoarsenednodeslist(void *h, int n, int *gids)
 {
-  if (n > 0) return unsupported("mesh coarsening");
+  Mgr &m = *M(h);
+  if (n <= 0) return 0;
+  m.coarse.assign(m.nGlobal, 0);
+  for (int i = 0; i < n; ++i) m.coarse[gids[i]] = 1;
+  m.a22Diagonal = false;   // A22 is not diagonal when some nodes are coarsened
   return 0;
 }
 int dft_linprobmgr_finalizeblockstructure(void *h)

@@ -215,6 +215,16 @@ int tref_get_zero_density(int *out)
   return 0;
 }
 
+/* Mesh_coarsen_flag[inode_box] (Nnodes_box): the residual zone of a node, or < 0 for a node whose
+ * rows average its neighbours (set_mesh_coarsen_flag, src/dft_mesh.c:2788-2850); -1 when unset */
+int tref_get_coarsen_flag(int *out)
+{
+  int i;
+  if (Mesh_coarsen_flag == NULL) return -1;
+  for (i = 0; i < Nnodes_box; i++) out[i] = Mesh_coarsen_flag[i];
+  return 0;
+}
+
 /* Nodes_2_boundary_wall[ilist][inode_box] for all lists (Nlists_HW * Nnodes_box) */
 int tref_get_boundary_nodes(int *out)
 {

@@ -202,6 +202,26 @@ def _child_extract(deck_lines, surfaces_from, opts, q):
                     lib.tref_stencil(isten, 0, idx, ip(off), dp(w), dp(hw) if hw is not None else None)
                     sten[(isten, idx)] = (off.reshape(L, ndim), w, None if hw is None else hw.reshape(L, nel_v))
             out["stencils"] = sten
+            # quadrature zones above 0 (coarser elements, offsets in fine-node units) and the per-node
+            # zone / coarsening flags
+            nzone = int(ints[25])
+            zsten = {}
+            for zone in range(1, nzone):
+                for isten, nidx in ((DELTA_FN_R, ncomp), (THETA_FN_R, ncomp), (THETA_PAIRPOT_RCUT, ncomp * ncomp)):
+                    for idx in range(nidx):
+                        L = lib.tref_stencil_length(isten, zone, idx)
+                        if L <= 0:
+                            continue
+                        off = np.zeros(L * ndim, np.int32)
+                        w = np.zeros(L)
+                        hw = np.zeros(L * nel_v) if lhard else None
+                        lib.tref_stencil(isten, zone, idx, ip(off), dp(w), dp(hw) if hw is not None else None)
+                        zsten[(zone, isten, idx)] = (off.reshape(L, ndim), w,
+                                                     None if hw is None else hw.reshape(L, nel_v))
+            out["zone_stencils"] = zsten
+            cf = np.zeros(nbox, np.int32)
+            if lib.tref_get_coarsen_flag(ip(cf)) == 0:
+                out["coarsen_flag"] = cf
             hit = np.zeros(ncomp * nown, np.int32)
             hit2 = np.zeros(ncomp * nown, np.int32)
             integ = np.zeros(6 + ncomp)

@@ -120,6 +120,11 @@ def cases():
     c["lv1d_bulkbc"] = deck("BULK3_FMT1_WCA_1D", {"L_Schur": SCHUR_LINSOLVE, "Type_bc(x0": "0 0"})
     # ATTInA22Block = 1: the mean field summed into the Euler-Lagrange rows (no mean-field unknowns)
     c["lj1d_a22"] = deck("LJ1_FMT1_WCA_1D", {"ATTInA22Block": "0 50 0 1 0", "L_Schur": SCHUR_LINSOLVE})
+    # mesh coarsening: HS6 (four quadrature zones at 2, 4, 5 sigma from the wall, residuals of the nodes off
+    # each zone's coarse lattice averaged from their neighbours) and HS7 (the same with a Jacobian one
+    # zone coarser than the residual near the wall)
+    c["hs1d_zones"] = deck("HS6_FMT1_1D")
+    c["hs1d_jaczones"] = deck("HS7_FMT1_1D")
     return c
 
 
@@ -167,6 +172,13 @@ def make_case(name, lines, surfaces, states=("x_newton", ("x_newton", 7, 0.02)))
         out[f"sten_{isten}_{idx}_w"] = w
         if hw is not None:
             out[f"sten_{isten}_{idx}_hw"] = hw
+    for (zone, isten, idx), (off, w, hw) in r["zone_stencils"].items():
+        out[f"zsten_{zone}_{isten}_{idx}_off"] = off.astype(np.int16)
+        out[f"zsten_{zone}_{isten}_{idx}_w"] = w
+        if hw is not None:
+            out[f"zsten_{zone}_{isten}_{idx}_hw"] = hw
+    if "coarsen_flag" in r:
+        out["coarsen_flag"] = r["coarsen_flag"]
     out["nel_hit"], out["nel_hit2"] = r["nel_hit"].astype(np.int8), r["nel_hit2"].astype(np.int8)
     out["integ"] = r["integ"]
     ind, dep, dens = block_lists(ints, nunk)

@@ -57,6 +57,15 @@ class Problem:
     betamu_if: np.ndarray = None
     pin_node: int = -1
     pin_value: float = 0.0
+    # quadrature zones / mesh coarsening (Nzone, Mesh_coarsening, Coarser_jac): per-node flag (residual
+    # zone >= 0, or -1/-2/-3: the node's rows average its neighbours along x/y/z), stencils of zones >= 1
+    nzone: int = 1
+    mesh_coarsening: int = 0
+    coarser_jac: int = 0
+    nwall: int = 0
+    zone_flag: np.ndarray = None
+    zone_stencils: dict = None
+    rhobar_bc: np.ndarray = None
     vext: np.ndarray = None        # [ncomp][N]
     zero_density: np.ndarray = None  # [ncomp][N] int8
     boundary_nodes: np.ndarray = None  # [nlists][N] int32, -1 = not a boundary node
@@ -132,6 +141,21 @@ def from_golden(z) -> Problem:
         fluid_masks=np.asarray(z["fluid_masks"], np.int16) if "fluid_masks" in z.files else None,
         stencils=st)
     assert p.nunk == int(ints[7]), (p.nunk, int(ints[7]))
+    p.nwall = nwall
+    p.rhobar_bc = np.array(d[55:65])
+    if len(ints) > 38:
+        p.nzone, p.mesh_coarsening, p.coarser_jac = int(ints[25]), int(ints[37]), int(ints[38])
+    if "coarsen_flag" in z.files:
+        p.zone_flag = np.asarray(z["coarsen_flag"], np.int32)
+    zst = {}
+    for key in z.files:
+        if key.startswith("zsten_") and key.endswith("_w"):
+            _, zone, t, idx, _ = key.split("_")
+            base = f"zsten_{zone}_{t}_{idx}"
+            zst.setdefault(int(zone), {})[(int(t), int(idx))] = (
+                np.asarray(z[base + "_off"], np.int16), np.asarray(z[key]),
+                np.asarray(z[base + "_hw"]) if base + "_hw" in z.files else None)
+    p.zone_stencils = zst
     if len(ints) > 45 and int(ints[36]) == 2:     # Type_interface = PHASE_INTERFACE
         p.interface = 2
         if nwall == 0:                            # LBB / RTF sentinels beyond bulk boundaries
