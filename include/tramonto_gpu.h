@@ -120,6 +120,21 @@ int tgpu_set_zero_density(tgpu_handle h, const signed char *flags);   /* [ncomp]
  * fluid_masks[nlists][2^ndim][N]: bit l set when the element that has the node
  * as local corner l (for that reflection pattern) is fluid (src/dft_utils.c:41-62). */
 int tgpu_set_hard_wall(tgpu_handle h, const int *boundary_nodes, const short *fluid_masks);
+/* Mesh coarsening (Nzone quadrature zones with Mesh_coarsening on; replaces the Mesh_coarsen_flag and
+ * Stencil[type][izone] reads of src/dft_fill_main.c:118-135, src/dft_fill_FMT.c:41-189 and
+ * src/dft_fill_CLSmf.c:38-171, and dft_linprobmgr_setcoarsenednodeslist, src/dft_mesh.c:516).
+ * flag[N] is Mesh_coarsen_flag: >= 0 the node's quadrature zone (< nzone, at most 5), -1/-2/-3 the
+ * node's rows average its two neighbours along x/y/z (load_coarse_node_Ndim,
+ * src/dft_fill_coarse.c:66-123).  rb_bulk[4 + 2 ndim] is Rhobar_b in solution order, the value of a
+ * weighted density beyond an IN_BULK boundary in those rows.  Zone z >= 1 stencils come from
+ * tgpu_set_zone_stencil (offsets in fine-node units, as calc_stencils scales them).  The Jacobian is the
+ * residual's derivative (the Coarser_jac option, a cheaper approximate Jacobian for the assembled
+ * matrix, has no use in the matrix-free products); the Newton step is solved on the nodes that are not
+ * coarsened, the coarsened nodes following by interpolation.  Not with phase interfaces, ATTInA22Block
+ * = 1 or the adjoint entry points. */
+int tgpu_set_zones(tgpu_handle h, int nzone, const int *flag, const double *rb_bulk);
+int tgpu_set_zone_stencil(tgpu_handle h, int zone, int type, int index, int length, const short *offsets,
+                          const double *weights, const double *hw);
 int tgpu_finalize(tgpu_handle h);
 /* Move the bulk state (chemical potential) of a finalized problem: bulk densities, excess chemical
  * potentials (hard-sphere and attraction) per component and the bulk dPhi/dn0..dn3.  The Euler-Lagrange

@@ -2,6 +2,7 @@
 // the fill, Jacobian and Schur products, the Schur-complement GMRES and the
 // damped Newton loop.  All device work is issued on the handle's stream.
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <cmath>
 #include <cstdio>
@@ -153,6 +154,18 @@ struct Ctx : tgpu_ctx {
   tgpu::ObjConst oc{};
   double *d_wf = nullptr, *d_wb = nullptr;
   double *d_obj_gx = nullptr, *d_obj_gv = nullptr, *d_obj_lam = nullptr, *d_obj_R = nullptr;
+  // quadrature zones / mesh coarsening: per-node zone (>= 0) or averaging axis (< 0), the stencils of
+  // zones >= 1, the averaged rows and the prolongation onto coarsened nodes
+  int nzone = 1;
+  std::vector<int> h_zone;
+  std::vector<double> h_rb_bulk;
+  std::vector<tgpu::DevStencil> zsten[tgpu::kMaxZone][3];
+  int *d_zone = nullptr;
+  double *d_zbuf = nullptr;      // [nrb + ncomp][N] one zone's sums
+  double *d_cbulk = nullptr;     // [nunk] value beyond an IN_BULK boundary per unknown
+  double *d_cscr = nullptr;      // [nunk][N] prolonged copies
+  tgpu::CoarseRows cr{};
+  bool coarse() const { return cr.ncoarse > 0; }
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -325,33 +338,50 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
   c->stats.kernel_launches++;
 }
 
+// Weighted-density (and mean-field) sums of the padded density channels with one zone's stencils
+// into out (rows as d_conv)
+void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, bool f32)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  const int nd = g.ndim;
+  for (int jc = 0; jc < g.ncomp; jc++) {
+    double *o_th[1] = {out};
+    conv(c, jc, 1, sten[TGPU_STEN_THETA][jc], false, o_th, 1, f32);
+    std::vector<double *> o_de;
+    o_de.push_back(out + 1 * N);
+    if (!g.single_size) {
+      o_de.push_back(out + 2 * N);
+      o_de.push_back(out + 3 * N);
+    }
+    for (int d = 0; d < nd; d++) o_de.push_back(out + (long)(4 + d) * N);
+    if (!g.single_size)
+      for (int d = 0; d < nd; d++) o_de.push_back(out + (long)(4 + nd + d) * N);
+    conv(c, jc, 1, sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), f32);
+    if (g.attraction)
+      for (int ic = 0; ic < g.ncomp; ic++) {
+        double *o_mf[1] = {out + (long)(g.nrb + ic) * N};
+        conv(c, jc, 1, sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o_mf, 1, f32);
+      }
+  }
+}
+
 // Weighted-density (and mean-field) sums of a density-shaped field
 // (`field` points at the first density row, rows N apart) into d_conv.
 void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bool zero_first = true)
 {
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
-  if (zero_first) ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * (size_t)(g.nrb + g.ncomp) * N, c->stream), "memset");
+  const size_t nrows = (size_t)(g.nrb + g.ncomp);
+  if (zero_first) ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * nrows * N, c->stream), "memset");
   pad(c, field, pp, f32);
-  const int nd = g.ndim;
-  for (int jc = 0; jc < g.ncomp; jc++) {
-    double *o_th[1] = {c->d_conv};
-    conv(c, jc, 1, c->sten[TGPU_STEN_THETA][jc], false, o_th, 1, f32);
-    std::vector<double *> o_de;
-    o_de.push_back(c->d_conv + 1 * N);
-    if (!g.single_size) {
-      o_de.push_back(c->d_conv + 2 * N);
-      o_de.push_back(c->d_conv + 3 * N);
-    }
-    for (int d = 0; d < nd; d++) o_de.push_back(c->d_conv + (long)(4 + d) * N);
-    if (!g.single_size)
-      for (int d = 0; d < nd; d++) o_de.push_back(c->d_conv + (long)(4 + nd + d) * N);
-    conv(c, jc, 1, c->sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), f32);
-    if (g.attraction)
-      for (int ic = 0; ic < g.ncomp; ic++) {
-        double *o_mf[1] = {c->d_conv + (long)(g.nrb + ic) * N};
-        conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o_mf, 1, f32);
-      }
+  forward_convs(c, c->sten, c->d_conv, f32);
+  // nodes of the coarser quadrature zones keep their own zone's sums (zero_first holds with zones)
+  for (int z = 1; z < c->nzone; z++) {
+    ck(cudaMemsetAsync(c->d_zbuf, 0, sizeof(double) * nrows * N, c->stream), "memset");
+    forward_convs(c, c->zsten[z], c->d_zbuf, f32);
+    tgpu::launch_zone_merge(c->d_zbuf, c->d_conv, (int)nrows, N, c->d_zone, z, c->stream);
+    c->stats.kernel_launches++;
   }
   if (g.hard_surf && !c->hw_targets.empty()) {
     tgpu::launch_hw_correct(field, N, 0, c->sten[TGPU_STEN_THETA].data(), c->sten[TGPU_STEN_DELTA].data(),
@@ -362,18 +392,32 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bo
   }
 }
 
+// Euler-Lagrange stencil sums of the padded channels with one zone's stencils into out ([ncomp][N])
+void transpose_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, bool f32)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const long N = g.N;
+  const int nd = g.ndim;
+  for (int ic = 0; ic < g.ncomp; ic++) {
+    double *o[1] = {out + (long)ic * N};
+    conv(c, ic * (nd + 2), 1 + nd, sten[TGPU_STEN_DELTA][ic], true, o, 1, f32);
+    conv(c, ic * (nd + 2) + nd + 1, 1, sten[TGPU_STEN_THETA][ic], true, o, 1, f32);
+  }
+}
+
 // Euler-Lagrange stencil sums over the channels in d_chan into d_tr.
 void transpose_pass(Ctx *c, const PadParams &pp, bool f32, const double *chan = nullptr, bool zero_first = true)
 {
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
-  const int nd = g.ndim;
   if (zero_first) ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
   pad(c, chan ? chan : c->d_chan, pp, f32);
-  for (int ic = 0; ic < g.ncomp; ic++) {
-    double *o[1] = {c->d_tr + (long)ic * N};
-    conv(c, ic * (nd + 2), 1 + nd, c->sten[TGPU_STEN_DELTA][ic], true, o, 1, f32);
-    conv(c, ic * (nd + 2) + nd + 1, 1, c->sten[TGPU_STEN_THETA][ic], true, o, 1, f32);
+  transpose_convs(c, c->sten, c->d_tr, f32);
+  for (int z = 1; z < c->nzone; z++) {
+    ck(cudaMemsetAsync(c->d_zbuf, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+    transpose_convs(c, c->zsten[z], c->d_zbuf, f32);
+    tgpu::launch_zone_merge(c->d_zbuf, c->d_tr, g.ncomp, N, c->d_zone, z, c->stream);
+    c->stats.kernel_launches++;
   }
 }
 
@@ -404,6 +448,7 @@ void copy_d(Ctx *c, double *dst, const double *src, size_t n)
 void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
 {
   need_final(c);
+  if (c->nzone > 1 && arith == TGPU_FILL_REFINED) arith = TGPU_FILL_FP64;   // zone sums are formed whole
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
   if (d_x != c->d_x && mode == 0)
@@ -457,6 +502,10 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
   }
   tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream);
   c->stats.kernel_launches += 2;
+  if (c->coarse()) {   // the averaged rows of coarsened nodes
+    tgpu::launch_coarse_rows(x, d_R, g.nunk, g.first_rho, g.ncomp, N, c->cr, c->d_cbulk, c->stream);
+    c->stats.kernel_launches++;
+  }
   if (mode == 0) c->have_state = true;
 }
 
@@ -482,15 +531,30 @@ struct TcScope {
   ~TcScope() { c->tc_on = prev; }
 };
 
+// With coarsened nodes the Schur complement is that of the step on the other nodes: the densities, and
+// the block-1 vector between A12 and A21, are interpolated onto the coarsened nodes, whose rows are dropped.
+const double *prolonged(Ctx *c, const double *v, int nrows)
+{
+  if (!c->coarse()) return v;
+  copy_d(c, c->d_cscr, v, (size_t)nrows * c->dg.N);
+  tgpu::launch_prolong(c->d_cscr, 0, nrows, c->dg.N, c->cr, nullptr, c->stream);
+  c->stats.kernel_launches++;
+  return c->d_cscr;
+}
+
 void schur_device(Ctx *c, const double *d_v2, double *d_y2)
 {
   need_state(c);
   TcScope tcs(c);
+  const tgpu::DevGeom &g = c->dg;
   const bool f32 = c->precision != TGPU_FP64;
-  forward_pass(c, d_v2, c->pads.rho_jac, f32);
+  const double *v2 = prolonged(c, d_v2, g.ncomp);
+  forward_pass(c, v2, c->pads.rho_jac, f32);
+  if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.N, c->cr, nullptr, c->stream);
   tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, c->stream);
   transpose_pass(c, c->pads.tr_jac, f32);
-  tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, d_v2, c->d_tr, c->d_ymf, d_y2, c->stream);
+  tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, v2, c->d_tr, c->d_ymf, d_y2, c->stream);
+  if (c->coarse()) tgpu::launch_zero_nodes(d_y2, g.ncomp, g.N, c->cr, c->stream);
   c->stats.kernel_launches += 2;
   c->stats.schur_applies++;
 }
@@ -506,6 +570,8 @@ void jv_device(Ctx *c, const double *d_v, double *d_out)
   transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_jv_combine(c->d_x, c->d_vext, c->d_zero, d_v, c->d_conv, c->d_tr, d_out, c->stream);
   c->stats.kernel_launches += 2;
+  if (c->coarse())
+    tgpu::launch_coarse_rows(d_v, d_out, c->dg.nunk, c->dg.first_rho, c->dg.ncomp, N, c->cr, nullptr, c->stream);
 }
 
 }  // namespace
@@ -523,10 +589,18 @@ namespace {
 void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
 {
   need_state(c);
-  tgpu::launch_rhs_local(c->d_x, d_b, c->d_chan, c->d_ymf, c->stream);
+  const tgpu::DevGeom &g = c->dg;
+  const double *b = d_b;
+  if (c->coarse()) {   // block-1 right-hand sides interpolated onto the coarsened nodes
+    copy_d(c, c->d_cscr, d_b, (size_t)g.nunk * g.N);
+    tgpu::launch_prolong(c->d_cscr, g.first_rb, g.nunk - g.ncomp, g.N, c->cr, nullptr, c->stream);
+    b = c->d_cscr;
+  }
+  tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, c->stream);
   TcScope tcs(c);
   transpose_pass(c, c->pads.tr_jac, c->precision != TGPU_FP64);
-  tgpu::launch_rhs_combine(c->d_vext, c->d_zero, d_b, c->d_tr, c->d_ymf, d_b2s, c->stream);
+  tgpu::launch_rhs_combine(c->d_vext, c->d_zero, b, c->d_tr, c->d_ymf, d_b2s, c->stream);
+  if (c->coarse()) tgpu::launch_zero_nodes(d_b2s, g.ncomp, g.N, c->cr, c->stream);
   c->stats.kernel_launches += 2;
 }
 
@@ -534,8 +608,19 @@ void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx
 {
   need_state(c);
   TcScope tcs(c);
-  forward_pass(c, d_x2, c->pads.rho_jac, c->precision != TGPU_FP64);
-  tgpu::launch_x1(d_b, c->d_conv, d_x2, d_dx, c->stream);
+  const tgpu::DevGeom &g = c->dg;
+  const double *x2 = prolonged(c, d_x2, g.ncomp);
+  forward_pass(c, x2, c->pads.rho_jac, c->precision != TGPU_FP64);
+  tgpu::launch_x1(d_b, c->d_conv, x2, d_dx, c->stream);
+  if (c->coarse()) tgpu::launch_prolong(d_dx, 0, g.nunk, g.N, c->cr, nullptr, c->stream);
+  c->stats.kernel_launches++;
+}
+
+// coarsened nodes' values interpolated from the others (bulk terms included)
+void coarse_state(Ctx *c, double *d_x)
+{
+  if (!c->coarse()) return;
+  tgpu::launch_prolong(d_x, 0, c->dg.nunk, c->dg.N, c->cr, c->d_cbulk, c->stream);
   c->stats.kernel_launches++;
 }
 
@@ -685,6 +770,7 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
   // With the refined residual, iterations far from the solution use FP32 sums;
   // once ||R|| falls below refine_switch the residual is FP64-accurate.
   double rprev = 1e300;
+  coarse_state(c, d_x);
   while (it < max_iter && !converged) {
     it++;
     int arith = c->fill_mode;
@@ -705,6 +791,7 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
     red_to_host(c, 1);
     const double frac = c->h_red[0];
     tgpu::launch_newton_update(d_x, d_dx, frac, rel_tol, abs_tol, c->d_partial, nb, c->d_red, c->stream);
+    coarse_state(c, d_x);
     red_to_host(c, 1);
     const double upd = std::sqrt(c->h_red[0]);
     if (!std::isfinite(upd)) throw Error(TGPU_ERR_NONFINITE, "non-finite Newton update");
@@ -742,6 +829,7 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
   int it = 0, lin_total = 0;
   double rprev = 1e300, eta = 0.1, rnorm = 1e300;
   bool converged = false;
+  coarse_state(c, d_x);
   for (;;) {
     int arith = c->fill_mode;
     const bool inexact = (arith == TGPU_FILL_MIXED || arith == TGPU_FILL_MIXED_FF || arith == TGPU_FILL_REFINED) &&
@@ -781,6 +869,7 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
     red_to_host(c, 1);
     const double frac = c->h_red[0];
     tgpu::launch_newton_update(d_x, d_dx, frac, 1.0, 1.0, c->d_partial, nb, c->d_red, c->stream);
+    coarse_state(c, d_x);
     red_to_host(c, 1);
     if (!std::isfinite(c->h_red[0])) throw Error(TGPU_ERR_NONFINITE, "non-finite Newton update");
     c->stats.kernel_launches += 6;
@@ -840,7 +929,7 @@ void adj_pad(Ctx *c, int nch)
   c->stats.kernel_launches++;
 }
 
-void jtv_device(Ctx *c, const double *d_w, double *d_out)
+void jtv_device(Ctx *c, const double *d_w_in, double *d_out)
 {
   need_state(c);
   const tgpu::DevGeom &g = c->dg;
@@ -849,21 +938,33 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
   const int nd = g.ndim;
   const int cpc = nd + 2;   // channels per component: A, B[d], C
   ck(cudaMemsetAsync(d_out, 0, sizeof(double) * (size_t)g.nunk * N, c->stream), "memset");
+  // the averaged rows of coarsened nodes are transposed apart (at the end); the stencil rows of each
+  // quadrature zone with that zone's stencils
+  const double *d_w = d_w_in;
+  if (c->coarse()) {
+    copy_d(c, c->d_cscr, d_w_in, (size_t)g.nunk * N);
+    tgpu::launch_zero_nodes(c->d_cscr, g.nunk, N, c->cr, c->stream);
+    d_w = c->d_cscr;
+  }
   // (a) density columns <- transposed weighted-density sums of the rb rows and mean-field sums of the MF rows
   {
-    tgpu::launch_adj_rb_channels(d_w, c->d_adj_chan, c->stream);
     const int nch = g.ncomp * cpc + (g.attraction ? g.ncomp : 0);
-    adj_pad(c, nch);
-    for (int jc = 0; jc < g.ncomp; jc++) {
-      double *o[1] = {d_out + (long)(g.first_rho + jc) * N};
-      const DevStencil &sd = c->sten[TGPU_STEN_DELTA][jc], &st = c->sten[TGPU_STEN_THETA][jc];
-      adj_conv(c, jc * cpc, 1 + nd, sd, sd.d_coef_adj, o, 1);
-      adj_conv(c, jc * cpc + nd + 1, 1, st, st.d_coef_fwd, o, 1);
-      if (g.attraction)
-        for (int ic = 0; ic < g.ncomp; ic++) {
-          const DevStencil &su = c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc];
-          adj_conv(c, g.ncomp * cpc + ic, 1, su, su.d_coef_fwd, o, 1);
-        }
+    for (int z = 0; z < c->nzone; z++) {
+      const std::vector<DevStencil> *sten = z == 0 ? c->sten : c->zsten[z];
+      tgpu::launch_adj_rb_channels(d_w, c->d_adj_chan, c->stream);
+      if (c->nzone > 1) tgpu::launch_zone_mask(c->d_adj_chan, nch, N, c->d_zone, z, c->stream);
+      adj_pad(c, nch);
+      for (int jc = 0; jc < g.ncomp; jc++) {
+        double *o[1] = {d_out + (long)(g.first_rho + jc) * N};
+        const DevStencil &sd = sten[TGPU_STEN_DELTA][jc], &st = sten[TGPU_STEN_THETA][jc];
+        adj_conv(c, jc * cpc, 1 + nd, sd, sd.d_coef_adj, o, 1);
+        adj_conv(c, jc * cpc + nd + 1, 1, st, st.d_coef_fwd, o, 1);
+        if (g.attraction)
+          for (int ic = 0; ic < g.ncomp; ic++) {
+            const DevStencil &su = sten[TGPU_STEN_UATT][ic + g.ncomp * jc];
+            adj_conv(c, g.ncomp * cpc + ic, 1, su, su.d_coef_fwd, o, 1);
+          }
+      }
     }
     // hard-wall boundary weights: the transpose of the forward correction
     if (g.hard_surf && !c->hw_targets.empty()) {
@@ -879,20 +980,28 @@ void jtv_device(Ctx *c, const double *d_w, double *d_out)
   }
   // (b) rb columns <- H(n) g with g gathered from the EL rows of w by the transposed delta/theta sums
   {
-    tgpu::launch_mask_rows(c->d_adj_chan, d_w, c->d_vext, c->d_zero, g.first_rho, g.ncomp, 0, c->stream);
-    adj_pad(c, g.ncomp);
     const int gst = nd + 2;   // per component: delta outputs (scalar, vector[d]) then theta
     ck(cudaMemsetAsync(c->d_adj_g, 0, sizeof(double) * (size_t)g.ncomp * gst * N, c->stream), "memset");
-    for (int ic = 0; ic < g.ncomp; ic++) {
-      double *o[tgpu::kMaxRb];
-      for (int q = 0; q < gst; q++) o[q] = c->d_adj_g + ((long)ic * gst + q) * N;
-      const DevStencil &sd = c->sten[TGPU_STEN_DELTA][ic], &st = c->sten[TGPU_STEN_THETA][ic];
-      const int vd[tgpu::kMaxRb] = {-1, 0, 1, 2};   // outputs: the scalar sum, then one per dimension
-      adj_conv(c, ic, 1, sd, sd.d_coef_adj, o, 1 + nd, vd);
-      adj_conv(c, ic, 1, st, st.d_coef_fwd, o + nd + 1, 1);
+    for (int z = 0; z < c->nzone; z++) {
+      const std::vector<DevStencil> *sten = z == 0 ? c->sten : c->zsten[z];
+      tgpu::launch_mask_rows(c->d_adj_chan, d_w, c->d_vext, c->d_zero, g.first_rho, g.ncomp, 0, c->stream);
+      if (c->nzone > 1) tgpu::launch_zone_mask(c->d_adj_chan, g.ncomp, N, c->d_zone, z, c->stream);
+      adj_pad(c, g.ncomp);
+      for (int ic = 0; ic < g.ncomp; ic++) {
+        double *o[tgpu::kMaxRb];
+        for (int q = 0; q < gst; q++) o[q] = c->d_adj_g + ((long)ic * gst + q) * N;
+        const DevStencil &sd = sten[TGPU_STEN_DELTA][ic], &st = sten[TGPU_STEN_THETA][ic];
+        const int vd[tgpu::kMaxRb] = {-1, 0, 1, 2};   // outputs: the scalar sum, then one per dimension
+        adj_conv(c, ic, 1, sd, sd.d_coef_adj, o, 1 + nd, vd);
+        adj_conv(c, ic, 1, st, st.d_coef_fwd, o + nd + 1, 1);
+      }
     }
     tgpu::launch_jtv_local(c->d_x, c->d_vext, c->d_zero, d_w, c->d_adj_g, gst, 1, d_out, c->stream);
     c->stats.kernel_launches += 4;
+  }
+  if (c->coarse()) {
+    tgpu::launch_coarse_rows_t(d_w_in, d_out, g.nunk, g.first_rho, g.ncomp, N, c->cr, c->stream);
+    c->stats.kernel_launches++;
   }
 }
 
@@ -921,6 +1030,7 @@ void schur_t_device(Ctx *c, const double *d_v2, double *d_y2)
 int adjoint_solve_device(Ctx *c, const double *d_g, double *d_lam, double tol, int maxit, int *iters, double *relres)
 {
   need_state(c);
+  if (c->coarse()) throw Error(TGPU_ERR_UNSUPPORTED, "adjoint solves with coarsened nodes");
   ensure_adjoint(c);
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
@@ -1235,6 +1345,187 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
   return L;
 }
 
+// ---- mesh coarsening: averaged rows and the prolongation onto coarsened nodes ----
+
+// One step along dimension d (s = +1 or -1) from a node under the boundary conditions: a node index,
+// -1 beyond an IN_BULK boundary or -2 inside a wall (offset_to_node_box, src/dft_mesh_lib.c:203-297,
+// for unit offsets).
+long step_node(const Ctx *c, long node, int d, int s)
+{
+  const tgpu::DevGeom &dg = c->dg;
+  long ijk[3] = {node % dg.nx[0], (node / dg.nx[0]) % dg.nx[1], node / ((long)dg.nx[0] * dg.nx[1])};
+  const long n = dg.nx[d];
+  long q = ijk[d] + s;
+  const int bl = c->g.bc[d][0], br = c->g.bc[d][1];
+  if (q < 0) {
+    if (bl == TGPU_BC_IN_BULK) return -1;
+    if (bl == TGPU_BC_IN_WALL) return -2;
+    q = bl == TGPU_BC_REFLECT ? -q : q + n;
+  } else if (q >= n) {
+    if (br == TGPU_BC_IN_BULK) return -1;
+    if (br == TGPU_BC_IN_WALL) return -2;
+    q = br == TGPU_BC_REFLECT ? 2 * (n - 1) - q : q - n;
+  }
+  if (q < 0 || q >= n) throw Error(TGPU_ERR_UNSUPPORTED, "mesh too small for its coarsening");
+  ijk[d] = q;
+  return ijk[0] + dg.nx[0] * (ijk[1] + (long)dg.nx[1] * ijk[2]);
+}
+
+// locate_neighbor_unks (src/dft_fill_coarse.c:103-123): the averaged row's terms (column, weight a) of a
+// coarsened node; with two zones a coarsened neighbour gives way to its own neighbours.  Wall columns
+// (value 0, no Jacobian entry) are left out.
+void coarse_row_terms(const Ctx *c, long node, double a, int depth, std::vector<std::pair<long, double>> &out)
+{
+  if (depth > 8) throw Error(TGPU_ERR_UNSUPPORTED, "coarsening pattern");
+  const int d = -c->h_zone[node] - 1;
+  for (int s : {1, -1}) {
+    const long j = step_node(c, node, d, s);
+    if (j >= 0 && c->h_zone[j] < 0 && c->nzone == 2) coarse_row_terms(c, j, 0.5 * a, depth + 1, out);
+    else if (j != -2) out.push_back({j, a});
+  }
+}
+
+// The values at coarsened nodes that satisfy every averaged row, as weights on the other nodes (and on the
+// bulk, column -1).  Coarsened nodes with one flag form runs along their averaging axis; each run is a
+// small linear system in its own nodes, given its outside neighbours, and runs are solved after the runs
+// they lean on (a cyclic dependence is rejected).
+void build_coarse(Ctx *c)
+{
+  const tgpu::DevGeom &dg = c->dg;
+  const long N = dg.N;
+  std::vector<int> cnode, pos(N, -1);
+  for (long i = 0; i < N; i++)
+    if (c->h_zone[i] < 0) {
+      pos[i] = (int)cnode.size();
+      cnode.push_back((int)i);
+    }
+  const int nc = (int)cnode.size();
+  c->cr.ncoarse = nc;
+  if (nc == 0) return;
+  // averaged rows
+  std::vector<int> rptr(1, 0);
+  std::vector<long> rcol;
+  std::vector<double> ra;
+  for (int k = 0; k < nc; k++) {
+    std::vector<std::pair<long, double>> t;
+    coarse_row_terms(c, cnode[k], 0.5, 0, t);
+    for (auto &e : t) {
+      rcol.push_back(e.first);
+      ra.push_back(e.second);
+    }
+    rptr.push_back((int)rcol.size());
+  }
+  // prolongation by runs
+  typedef std::vector<std::pair<long, double>> Expr;
+  std::vector<Expr> expr(nc);
+  std::vector<char> state(nc, 0);
+  std::function<void(int)> solve = [&](int k0) {
+    if (state[k0] == 2) return;
+    if (state[k0] == 1) throw Error(TGPU_ERR_UNSUPPORTED, "cyclic coarsening pattern");
+    const int flag = c->h_zone[cnode[k0]], d = -flag - 1;
+    std::vector<int> run(1, k0);
+    std::map<int, int> in_run{{k0, 0}};
+    for (size_t q = 0; q < run.size(); q++)
+      for (int s : {1, -1}) {
+        const long j = step_node(c, cnode[run[q]], d, s);
+        if (j >= 0 && c->h_zone[j] == flag && !in_run.count(pos[j])) {
+          in_run[pos[j]] = (int)run.size();
+          run.push_back(pos[j]);
+        }
+      }
+    const int m = (int)run.size();
+    if (m > 4096) throw Error(TGPU_ERR_UNSUPPORTED, "coarsening pattern");
+    for (int k : run) state[k] = 1;
+    std::vector<double> A((size_t)m * m, 0.0);
+    std::vector<long> ext;
+    std::map<long, int> ext_idx;
+    std::vector<std::vector<std::pair<int, double>>> brow(m);
+    for (int r = 0; r < m; r++) {
+      A[(size_t)r * m + r] += 1.0;
+      for (int s : {1, -1}) {
+        const long j = step_node(c, cnode[run[r]], d, s);
+        if (j == -2) continue;
+        if (j >= 0 && c->h_zone[j] == flag) {
+          A[(size_t)r * m + in_run.at(pos[j])] -= 0.5;
+          continue;
+        }
+        if (j >= 0 && c->h_zone[j] < 0) solve(pos[j]);
+        auto it = ext_idx.find(j);
+        int e;
+        if (it == ext_idx.end()) {
+          e = (int)ext.size();
+          ext_idx[j] = e;
+          ext.push_back(j);
+        } else {
+          e = it->second;
+        }
+        brow[r].push_back({e, 0.5});
+      }
+    }
+    const int E = (int)ext.size();
+    std::vector<double> X((size_t)m * E, 0.0);
+    for (int r = 0; r < m; r++)
+      for (auto &b : brow[r]) X[(size_t)r * E + b.first] += b.second;
+    // Gaussian elimination with partial pivoting on [A | X]
+    for (int col = 0; col < m; col++) {
+      int piv = col;
+      for (int r = col + 1; r < m; r++)
+        if (std::fabs(A[(size_t)r * m + col]) > std::fabs(A[(size_t)piv * m + col])) piv = r;
+      if (std::fabs(A[(size_t)piv * m + col]) < 1e-12) throw Error(TGPU_ERR_UNSUPPORTED, "singular coarsening run");
+      if (piv != col) {
+        for (int q = 0; q < m; q++) std::swap(A[(size_t)piv * m + q], A[(size_t)col * m + q]);
+        for (int q = 0; q < E; q++) std::swap(X[(size_t)piv * E + q], X[(size_t)col * E + q]);
+      }
+      for (int r = 0; r < m; r++) {
+        if (r == col) continue;
+        const double f = A[(size_t)r * m + col] / A[(size_t)col * m + col];
+        if (f == 0.0) continue;
+        for (int q = col; q < m; q++) A[(size_t)r * m + q] -= f * A[(size_t)col * m + q];
+        for (int q = 0; q < E; q++) X[(size_t)r * E + q] -= f * X[(size_t)col * E + q];
+      }
+    }
+    for (int r = 0; r < m; r++) {
+      std::map<long, double> acc;
+      const double inv = 1.0 / A[(size_t)r * m + r];
+      for (int e = 0; e < E; e++) {
+        const double w = X[(size_t)r * E + e] * inv;
+        if (w == 0.0) continue;
+        const long j = ext[e];
+        if (j >= 0 && c->h_zone[j] < 0)
+          for (auto &t : expr[pos[j]]) acc[t.first] += w * t.second;
+        else
+          acc[j] += w;
+      }
+      expr[run[r]].assign(acc.begin(), acc.end());
+    }
+    for (int k : run) state[k] = 2;
+  };
+  for (int k = 0; k < nc; k++) solve(k);
+  std::vector<int> pptr(1, 0);
+  std::vector<long> pcol;
+  std::vector<double> pw;
+  for (int k = 0; k < nc; k++) {
+    for (auto &t : expr[k]) {
+      pcol.push_back(t.first);
+      pw.push_back(t.second);
+    }
+    pptr.push_back((int)pcol.size());
+  }
+  c->cr.d_node = upload(cnode, c->stream);
+  c->cr.d_rptr = upload(rptr, c->stream);
+  c->cr.d_rcol = upload(rcol, c->stream);
+  c->cr.d_ra = upload(ra, c->stream);
+  c->cr.d_pptr = upload(pptr, c->stream);
+  c->cr.d_pcol = upload(pcol, c->stream);
+  c->cr.d_pw = upload(pw, c->stream);
+  // value beyond an IN_BULK boundary per unknown (constant_boundary, src/dft_utils.c:89-110)
+  std::vector<double> cb((size_t)dg.nunk, 0.0);
+  for (int ic = 0; ic < dg.ncomp; ic++) cb[(size_t)dg.first_rho + ic] = c->g.rho_b[ic];
+  for (int k = 0; k < dg.nrb; k++) cb[(size_t)dg.first_rb + k] = c->h_rb_bulk[k];
+  c->d_cbulk = upload(cb, c->stream);
+  c->d_cscr = dalloc<double>((size_t)dg.nunk * N);
+}
+
 void build_device_tables(Ctx *c)
 {
   tgpu_geometry &g = c->g;
@@ -1242,10 +1533,11 @@ void build_device_tables(Ctx *c)
   const int nd = g.ndim;
   // halo = largest stencil reach per dimension
   int h[3] = {0, 0, 0};
-  for (int t = 0; t < 3; t++)
-    for (auto &st : c->sten[t])
-      for (int k = 0; k < st.L; k++)
-        for (int d = 0; d < nd; d++) h[d] = std::max(h[d], std::abs((int)st.off[(size_t)k * nd + d]));
+  for (int z = 0; z < c->nzone; z++)
+    for (int t = 0; t < 3; t++)
+      for (auto &st : (z == 0 ? c->sten[t] : c->zsten[z][t]))
+        for (int k = 0; k < st.L; k++)
+          for (int d = 0; d < nd; d++) h[d] = std::max(h[d], std::abs((int)st.off[(size_t)k * nd + d]));
   long NP = 1;
   for (int d = 0; d < 3; d++) {
     dg.nx[d] = d < nd ? g.nx[d] : 1;
@@ -1264,11 +1556,9 @@ void build_device_tables(Ctx *c)
     c->d_map[d] = upload(m, c->stream);
     dg.map[d] = c->d_map[d];
   }
-  // stencil tables
-  for (int t = 0; t < 3; t++)
-    for (int idx = 0; idx < (int)c->sten[t].size(); idx++) {
-      DevStencil &st = c->sten[t][idx];
-      if (st.L == 0) continue;
+  // stencil tables; the coarser zones' stencils get the generic tables only
+  auto prep = [&](DevStencil &st, int t, int idx, bool fast) {
+      if (st.L == 0) return;
       std::vector<int> loff(st.L);
       std::vector<short> off3((size_t)st.L * 3, 0);
       for (int k = 0; k < st.L; k++) {
@@ -1332,11 +1622,11 @@ void build_device_tables(Ctx *c)
         std::vector<float> t32(tr.begin(), tr.end());
         st.d_coef_tr32 = upload(t32, c->stream);
       }
-      if (nd == 3 && (t == TGPU_STEN_THETA || t == TGPU_STEN_UATT)) {
+      if (fast && nd == 3 && (t == TGPU_STEN_THETA || t == TGPU_STEN_UATT)) {
         st.lines_fwd = build_lines(st, fwd, dg, c->stream);
         if (t == TGPU_STEN_THETA) st.lines_tr = build_lines(st, tr, dg, c->stream);
       }
-      if (nd == 3 && t == TGPU_STEN_DELTA && g.single_size) {
+      if (fast && nd == 3 && t == TGPU_STEN_DELTA && g.single_size) {
         // the forward table is [L][1 + nd] (one input), the transpose table [L][1 + nd] (one output)
         st.lines_fwd = build_lines(st, fwd, dg, c->stream, st.nout_fwd, 1);
         st.lines_tr = build_lines(st, tr, dg, c->stream, st.nin_tr, st.nin_tr);
@@ -1352,8 +1642,13 @@ void build_device_tables(Ctx *c)
           st.ff_tr.push_back(build_lines(st, col, dg, c->stream));
         }
       }
-      if (nd == 3 && t == TGPU_STEN_UATT) tgpu::tc_build_tables(st.off, fwd, st.L, dg.h[1], st.tc, c->stream);
-    }
+      if (fast && nd == 3 && t == TGPU_STEN_UATT) tgpu::tc_build_tables(st.off, fwd, st.L, dg.h[1], st.tc, c->stream);
+  };
+  for (int t = 0; t < 3; t++)
+    for (int idx = 0; idx < (int)c->sten[t].size(); idx++) prep(c->sten[t][idx], t, idx, true);
+  for (int z = 1; z < c->nzone; z++)
+    for (int t = 0; t < 3; t++)
+      for (int idx = 0; idx < (int)c->zsten[z][t].size(); idx++) prep(c->zsten[z][t][idx], t, idx, false);
   const long N = dg.N;
   // fields
   if (c->h_vext.empty()) c->h_vext.assign((size_t)g.ncomp * N, 0.0);
@@ -1549,6 +1844,15 @@ int tgpu_destroy(tgpu_handle h)
           }
         tgpu::tc_free_tables(st.tc);
       }
+    for (int z = 1; z < tgpu::kMaxZone; z++)
+      for (int t = 0; t < 3; t++)
+        for (auto &st : c->zsten[z][t]) {
+          dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
+          dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
+        }
+    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr);
+    dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
+    dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
     tgpu::tc_free_slab(c->tcslab);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);
@@ -1581,6 +1885,47 @@ int tgpu_set_stencil(tgpu_handle h, int type, int index, int length, const short
     if (index < 0 || index >= nidx) throw Error(TGPU_ERR_ARG, "stencil index");
     if (length < 0 || (length > 0 && (!offsets || !weights))) throw Error(TGPU_ERR_ARG, "stencil arrays");
     DevStencil &st = c->sten[type][index];
+    const int nd = c->g.ndim;
+    st.L = length;
+    st.off.assign(offsets, offsets + (size_t)length * nd);
+    st.w.assign(weights, weights + length);
+    if (hw) st.hw.assign(hw, hw + (size_t)length * (1 << nd));
+    else st.hw.clear();
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_zones(tgpu_handle h, int nzone, const int *flag, const double *rb_bulk)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) throw Error(TGPU_ERR_STATE, "zones are fixed after tgpu_finalize");
+    if (nzone < 1 || nzone > tgpu::kMaxZone) throw Error(TGPU_ERR_ARG, "number of zones");
+    if (!flag || !rb_bulk) throw Error(TGPU_ERR_ARG, "null zone arrays");
+    const long N = c->dg.N;
+    for (long i = 0; i < N; i++)
+      if (flag[i] >= nzone || flag[i] < -c->g.ndim) throw Error(TGPU_ERR_ARG, "zone flag");
+    c->nzone = nzone;
+    c->h_zone.assign(flag, flag + N);
+    c->h_rb_bulk.assign(rb_bulk, rb_bulk + 4 + 2 * c->g.ndim);
+    for (int z = 1; z < nzone; z++)
+      for (int t = 0; t < 3; t++) c->zsten[z][t].resize(c->sten[t].size());
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_zone_stencil(tgpu_handle h, int zone, int type, int index, int length, const short *offsets,
+                          const double *weights, const double *hw)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) throw Error(TGPU_ERR_STATE, "stencils are fixed after tgpu_finalize");
+    if (zone < 1 || zone >= c->nzone) throw Error(TGPU_ERR_ARG, "zone (set the zones first)");
+    if (type < 0 || type > 2) throw Error(TGPU_ERR_ARG, "stencil type");
+    const int nidx = type == TGPU_STEN_UATT ? c->g.ncomp * c->g.ncomp : c->g.ncomp;
+    if (index < 0 || index >= nidx) throw Error(TGPU_ERR_ARG, "stencil index");
+    if (length <= 0 || !offsets || !weights) throw Error(TGPU_ERR_ARG, "stencil arrays");
+    DevStencil &st = c->zsten[zone][type][index];
     const int nd = c->g.ndim;
     st.L = length;
     st.off.assign(offsets, offsets + (size_t)length * nd);
@@ -1680,8 +2025,28 @@ int tgpu_finalize(tgpu_handle h)
         else if (g.hard_surf && c->sten[TGPU_STEN_UATT][k].hw.empty())
           throw Error(TGPU_ERR_STATE, "hard surfaces need the attraction stencils' corner weights");
     if (g.hard_surf && c->h_bnodes.empty()) throw Error(TGPU_ERR_STATE, "hard surfaces need tgpu_set_hard_wall");
+    if (c->nzone > 1) {
+      if (g.interface) throw Error(TGPU_ERR_UNSUPPORTED, "mesh coarsening with a phase interface");
+      if (c->a22) throw Error(TGPU_ERR_UNSUPPORTED, "mesh coarsening with ATTInA22Block = 1");
+      for (int z = 1; z < c->nzone; z++)
+        for (int t = 0; t < 3; t++) {
+          if (t == TGPU_STEN_UATT && !g.attraction) continue;
+          const int nidx = t == TGPU_STEN_UATT ? g.ncomp * g.ncomp : g.ncomp;
+          for (int k = 0; k < nidx; k++)
+            if (c->zsten[z][t][k].L == 0) throw Error(TGPU_ERR_STATE, "missing stencil of a coarser zone");
+        }
+    }
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     build_device_tables(c);
+    if (c->nzone > 1) {
+      for (int t : c->hw_targets)
+        if (c->h_zone[t] > 0)
+          throw Error(TGPU_ERR_UNSUPPORTED, "hard-wall boundary nodes within reach of a coarser zone's stencils");
+      c->d_zone = upload(c->h_zone, c->stream);
+      c->d_zbuf = dalloc<double>((size_t)(c->dg.nrb + c->dg.ncomp) * c->dg.N);
+      build_coarse(c);
+      ck(cudaStreamSynchronize(c->stream), "sync");
+    }
     bool any_tc = false;
     for (auto &st : c->sten[TGPU_STEN_UATT]) any_tc = any_tc || st.tc.nplanes > 0;
     if (any_tc) c->tc_ready = tgpu::tc_make_slab(c->tcslab, c->dg, c->tc_why);

@@ -50,6 +50,19 @@ constexpr double kDensityMin = 1.e-20;   // integrands vanish at or below this d
 // Constants of the free-energy objective: per component the chemical potential
 // betamu and the bulk integrand rho_b(ln rho_b - 1) - rho_b betamu [+ rho_b betamu_att / 2],
 // and the hard-sphere energy density of the bulk weighted densities.
+// Averaged rows of coarsened nodes and the prolongation onto them (coarsen.cu)
+constexpr int kMaxZone = 5;
+struct CoarseRows {
+  int ncoarse = 0;
+  int *d_node = nullptr;                  // [ncoarse] node index of each coarsened node
+  int *d_rptr = nullptr;                  // row terms: [ncoarse + 1]
+  long *d_rcol = nullptr;                 // node index, or -1 (bulk beyond an IN_BULK boundary)
+  double *d_ra = nullptr;                 // weights a_k > 0 of fac (x_c - sum_k a_k x_k)
+  int *d_pptr = nullptr;                  // prolongation x_c = sum_e p_e x_col: [ncoarse + 1]
+  long *d_pcol = nullptr;
+  double *d_pw = nullptr;
+};
+
 struct ObjConst {
   double betamu[kMaxC];
   double bulk[kMaxC];
@@ -425,6 +438,17 @@ void launch_sten_tc(const float *pad_channel, const DevGeom &g, const TcSlab &sl
                     bool accumulate, cudaStream_t s);
 void launch_adj_rb_channels(const double *w, double *chan, cudaStream_t s);
 void launch_a11inv_t(const double *u, double *y, cudaStream_t s);
+// coarsen.cu: dst[r][i] = src[r][i] where zone[i] == z; buf[r][i] = 0 where zone[i] != z
+void launch_zone_merge(const double *src, double *dst, int nrows, long N, const int *zone, int z, cudaStream_t s);
+void launch_zone_mask(double *buf, int nrows, long N, const int *zone, int z, cudaStream_t s);
+// averaged rows at coarsened nodes (bulk: per-unknown value at -1 columns, or null for a linear product),
+// their transpose (accumulated into out), the prolongation of rows row0.. and zeroing of coarsened nodes
+void launch_coarse_rows(const double *in, double *out, int nunk, int first_rho, int ncomp, long N,
+                        const CoarseRows &cr, const double *bulk, cudaStream_t s);
+void launch_coarse_rows_t(const double *w, double *out, int nunk, int first_rho, int ncomp, long N,
+                          const CoarseRows &cr, cudaStream_t s);
+void launch_prolong(double *vec, int row0, int nrows, long N, const CoarseRows &cr, const double *bulk, cudaStream_t s);
+void launch_zero_nodes(double *vec, int nrows, long N, const CoarseRows &cr, cudaStream_t s);
 void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,
                       int mode, cudaStream_t s);
 void launch_delta_maxabs(const double *a, const double *ref, long n, double *out, double *partial, int nblocks,

@@ -85,6 +85,8 @@ def load(build_if_missing: bool = False):
         "tgpu_create": [C.POINTER(Geometry), C.c_int, C.POINTER(vp)],
         "tgpu_destroy": [vp],
         "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
+        "tgpu_set_zones": [vp, C.c_int, vp, vp],
+        "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
         "tgpu_set_jacobian_form": [vp, C.c_int],
@@ -162,6 +164,11 @@ def _ptr(a):
     return C.c_void_p(a.ctypes.data)
 
 
+def mesh_coarsened(p: Problem) -> bool:
+    """Quadrature zones that change the residual: Mesh_coarsening on, walls present, more than one zone."""
+    return bool(p.nzone > 1 and p.mesh_coarsening and p.nwall > 0 and p.zone_flag is not None)
+
+
 class Solver:
     """One problem resident on one GPU (see module doc)."""
 
@@ -187,6 +194,21 @@ class Solver:
                 bn = np.ascontiguousarray(p.boundary_nodes, np.int32)
                 fm = np.ascontiguousarray(p.fluid_masks, np.int16)
                 _check(lib.tgpu_set_hard_wall(self.h, _ptr(bn), _ptr(fm)), lib)
+            if mesh_coarsened(p):
+                # the fill reads the zones only with Mesh_coarsening on and walls present
+                # (src/dft_fill_main.c:120); the Jacobian is the residual's own derivative
+                flag = np.ascontiguousarray(p.zone_flag, np.int32)
+                rbb = np.ascontiguousarray(np.asarray(p.rhobar_bc, np.float64)[:p.nrb])
+                _check(lib.tgpu_set_zones(self.h, int(p.nzone), _ptr(flag), _ptr(rbb)), lib)
+                for zone, tabs in sorted(p.zone_stencils.items()):
+                    for (t, idx), (off, w, hw) in sorted(tabs.items()):
+                        off = np.ascontiguousarray(off, np.int16)
+                        w = np.ascontiguousarray(w, np.float64)
+                        hwp = None
+                        if hw is not None and p.hard_surf:
+                            hw = np.ascontiguousarray(hw, np.float64)
+                            hwp = _ptr(hw)
+                        _check(lib.tgpu_set_zone_stencil(self.h, zone, t, idx, len(w), _ptr(off), _ptr(w), hwp), lib)
             _check(lib.tgpu_finalize(self.h), lib)
             self.set_precision(precision)
             if p.w_fluid is not None:
