@@ -130,8 +130,8 @@ int tgpu_set_hard_wall(tgpu_handle h, const int *boundary_nodes, const short *fl
  * tgpu_set_zone_stencil (offsets in fine-node units, as calc_stencils scales them).  The Jacobian is the
  * residual's derivative (the Coarser_jac option, a cheaper approximate Jacobian for the assembled
  * matrix, has no use in the matrix-free products); the Newton step is solved on the nodes that are not
- * coarsened, the coarsened nodes following by interpolation.  Not with phase interfaces, ATTInA22Block
- * = 1 or the adjoint entry points. */
+ * coarsened, the coarsened nodes following by interpolation (the adjoint solves that step's transpose).
+ * Not with phase interfaces or ATTInA22Block = 1. */
 int tgpu_set_zones(tgpu_handle h, int nzone, const int *flag, const double *rb_bulk);
 int tgpu_set_zone_stencil(tgpu_handle h, int zone, int type, int index, int length, const short *offsets,
                           const double *weights, const double *hw);

@@ -164,6 +164,7 @@ struct Ctx : tgpu_ctx {
   double *d_zbuf = nullptr;      // [nrb + ncomp][N] one zone's sums
   double *d_cbulk = nullptr;     // [nunk] value beyond an IN_BULK boundary per unknown
   double *d_cscr = nullptr;      // [nunk][N] prolonged copies
+  double *d_cscr2 = nullptr;     // [nunk][N] the adjoint's folded right-hand side
   tgpu::CoarseRows cr{};
   bool coarse() const { return cr.ncoarse > 0; }
 };
@@ -1005,6 +1006,18 @@ void jtv_device(Ctx *c, const double *d_w_in, double *d_out)
   }
 }
 
+// The transpose of the step on the other nodes (coarsened meshes): J_r = R J E with E the prolongation
+// onto coarsened nodes and R the restriction to the other rows, so J_r^T w = E^T J^T (w, zero on
+// coarsened rows); E^T folds the coarsened columns onto the nodes they are interpolated from.
+void jtv_reduced(Ctx *c, const double *d_w, double *d_out)
+{
+  jtv_device(c, d_w, d_out);   // coarsened rows of w do not enter J_r
+  if (c->coarse()) {
+    tgpu::launch_prolong_t(d_out, 0, c->dg.nunk, c->dg.N, c->cr, c->stream);
+    c->stats.kernel_launches++;
+  }
+}
+
 // J^T lambda = g by GMRES on the transposed Schur complement
 //   S^T = A22^T - A12^T A11^-T A21^T,  right-hand side g2 - A12^T A11^-T g1,
 //   lambda1 = A11^-T (g1 - A21^T lambda2),
@@ -1019,26 +1032,34 @@ void schur_t_device(Ctx *c, const double *d_v2, double *d_y2)
   double *full = c->d_adj_v, *t = c->d_adj_t;
   ck(cudaMemsetAsync(full, 0, n * sizeof(double), c->stream), "memset");
   copy_d(c, full + (long)g.first_rho * N, d_v2, (size_t)g.ncomp * N);
-  jtv_device(c, full, t);
+  jtv_reduced(c, full, t);
   copy_d(c, d_y2, t + (long)g.first_rho * N, (size_t)g.ncomp * N);   // A22^T v2 - nothing else yet
   tgpu::launch_a11inv_t(t, full, c->stream);                           // y1 in block-1 rows, density rows 0
-  jtv_device(c, full, t);                                              // t_rho = A12^T y1
+  jtv_reduced(c, full, t);                                             // t_rho = A12^T y1
   tgpu::launch_axpby(d_y2, -1.0, t + (long)g.first_rho * N, 1.0, (long)g.ncomp * N, c->stream);
   c->stats.schur_applies++;
 }
 
-int adjoint_solve_device(Ctx *c, const double *d_g, double *d_lam, double tol, int maxit, int *iters, double *relres)
+int adjoint_solve_device(Ctx *c, const double *d_g_in, double *d_lam, double tol, int maxit, int *iters,
+                         double *relres)
 {
   need_state(c);
-  if (c->coarse()) throw Error(TGPU_ERR_UNSUPPORTED, "adjoint solves with coarsened nodes");
   ensure_adjoint(c);
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
   const size_t n = (size_t)g.nunk * N;
   double *full = c->d_adj_v, *t = c->d_adj_t;
+  // coarsened meshes: the adjoint of the step on the other nodes, right-hand side E^T g
+  const double *d_g = d_g_in;
+  if (c->coarse()) {
+    if (!c->d_cscr2) c->d_cscr2 = dalloc<double>(n);
+    copy_d(c, c->d_cscr2, d_g_in, n);
+    tgpu::launch_prolong_t(c->d_cscr2, 0, g.nunk, N, c->cr, c->stream);
+    d_g = c->d_cscr2;
+  }
   // rhs2 = g2 - A12^T A11^-T g1
   tgpu::launch_a11inv_t(d_g, full, c->stream);
-  jtv_device(c, full, t);
+  jtv_reduced(c, full, t);
   copy_d(c, c->d_b2s, d_g + (long)g.first_rho * N, (size_t)g.ncomp * N);
   tgpu::launch_axpby(c->d_b2s, -1.0, t + (long)g.first_rho * N, 1.0, (long)g.ncomp * N, c->stream);
   c->gmres_transpose = true;
@@ -1053,7 +1074,7 @@ int adjoint_solve_device(Ctx *c, const double *d_g, double *d_lam, double tol, i
   // lambda1 = A11^-T (g1 - A21^T lambda2)
   ck(cudaMemsetAsync(full, 0, n * sizeof(double), c->stream), "memset");
   copy_d(c, full + (long)g.first_rho * N, c->d_gx, (size_t)g.ncomp * N);
-  jtv_device(c, full, t);                                   // block-1 rows: A21^T lambda2
+  jtv_reduced(c, full, t);                                  // block-1 rows: A21^T lambda2
   tgpu::launch_axpby(t, 1.0, d_g, -1.0, (long)n, c->stream);  // t = g - J^T[0; lambda2] (block-1 rows used)
   tgpu::launch_a11inv_t(t, d_lam, c->stream);
   copy_d(c, d_lam + (long)g.first_rho * N, c->d_gx, (size_t)g.ncomp * N);
@@ -1850,7 +1871,7 @@ int tgpu_destroy(tgpu_handle h)
           dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
           dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
         }
-    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr);
+    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2);
     dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
     dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);

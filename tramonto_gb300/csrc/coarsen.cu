@@ -14,7 +14,7 @@
 //
 // The Newton step is solved on the other nodes only: the coarsened nodes' values follow from the rest
 // through the prolongation x_c = sum_f P_cf x_f (+ bulk terms), which satisfies every averaged row
-// exactly; prolong() applies it to whole rows of unknowns.
+// exactly; prolong() applies it to whole rows of unknowns, prolong_t() its transpose (the adjoint).
 #include "tgpu_internal.h"
 
 namespace tgpu {
@@ -96,6 +96,24 @@ __global__ void k_prolong(double *__restrict__ vec, int row0, int nrows, long N,
   row[cnode[k]] = s;
 }
 
+// transpose of the prolongation: vec[r][col_e] += p_e vec[r][c], then vec[r][c] = 0 (columns are never
+// coarsened nodes, so the adds and the reads do not meet)
+__global__ void k_prolong_t(double *__restrict__ vec, int row0, int nrows, long N, int ncoarse,
+                            const int *__restrict__ cnode, const int *__restrict__ ptr, const long *__restrict__ col,
+                            const double *__restrict__ p)
+{
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= (long)ncoarse * nrows) return;
+  const int k = (int)(t % ncoarse), r = (int)(t / ncoarse);
+  double *row = vec + (long)(row0 + r) * N;
+  const double v = row[cnode[k]];
+  for (int e = ptr[k]; e < ptr[k + 1]; e++) {
+    const long j = col[e];
+    if (j >= 0 && v != 0.0) atomicAdd(row + j, p[e] * v);
+  }
+  row[cnode[k]] = 0.0;
+}
+
 __global__ void k_zero_nodes(double *__restrict__ vec, int nrows, long N, int ncoarse, const int *__restrict__ cnode)
 {
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -142,6 +160,13 @@ void launch_prolong(double *vec, int row0, int nrows, long N, const CoarseRows &
   if (n > 0)
     k_prolong<<<nblk(n), 256, 0, s>>>(vec, row0, nrows, N, cr.ncoarse, cr.d_node, cr.d_pptr, cr.d_pcol, cr.d_pw,
                                       bulk);
+}
+
+void launch_prolong_t(double *vec, int row0, int nrows, long N, const CoarseRows &cr, cudaStream_t s)
+{
+  const long n = (long)cr.ncoarse * nrows;
+  if (n > 0)
+    k_prolong_t<<<nblk(n), 256, 0, s>>>(vec, row0, nrows, N, cr.ncoarse, cr.d_node, cr.d_pptr, cr.d_pcol, cr.d_pw);
 }
 
 void launch_zero_nodes(double *vec, int nrows, long N, const CoarseRows &cr, cudaStream_t s)

@@ -448,6 +448,7 @@ void launch_coarse_rows(const double *in, double *out, int nunk, int first_rho, 
 void launch_coarse_rows_t(const double *w, double *out, int nunk, int first_rho, int ncomp, long N,
                           const CoarseRows &cr, cudaStream_t s);
 void launch_prolong(double *vec, int row0, int nrows, long N, const CoarseRows &cr, const double *bulk, cudaStream_t s);
+void launch_prolong_t(double *vec, int row0, int nrows, long N, const CoarseRows &cr, cudaStream_t s);
 void launch_zero_nodes(double *vec, int nrows, long N, const CoarseRows &cr, cudaStream_t s);
 void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,
                       int mode, cudaStream_t s);
