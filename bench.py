@@ -74,8 +74,9 @@ def parse():
                     help="one repetition of each FP64 kernel-family timing (large workloads)")
     ap.add_argument("--products", default="fp16tc", choices=["fp16tc", "fp32"],
                     help="arithmetic of the Schur products' attraction sums")
-    ap.add_argument("--accurate-fill", default="ff", choices=["ff", "fp64"],
-                    help="arithmetic of the fills once ||R||_2 < switch: float-float or FP64 single-channel sums")
+    ap.add_argument("--accurate-fill", default="fft", choices=["ff", "fft", "fp64"],
+                    help="arithmetic of the fills once ||R||_2 < switch: float-float sums, FP64 FFT sums or "
+                         "direct FP64 sums")
     return ap.parse_args()
 
 
@@ -301,7 +302,7 @@ def main():
     x0_dev = torch.from_numpy(x0).to("cuda").contiguous()
     dx = torch.empty_like(x0_dev)
 
-    fill_mode = native.FILL_MIXED_FF if args.accurate_fill == "ff" else native.FILL_MIXED
+    fill_mode = {"ff": native.FILL_MIXED_FF, "fft": native.FILL_MIXED_FFT, "fp64": native.FILL_MIXED}[args.accurate_fill]
 
     def mixed_mode():
         s.set_precision(prod_prec)
@@ -390,6 +391,8 @@ def main():
     t_fill = timed(lambda: s.fill_device(x_mixed, R, 0), reps=rep64)
     s.set_fill_arithmetic(native.FILL_FF)
     t_fill_ff = timed(lambda: s.fill_device(x_mixed, R, 0), reps=rep64)
+    s.set_fill_arithmetic(native.FILL_FFT)
+    t_fill_fft = timed(lambda: s.fill_device(x_mixed, R, 0), reps=3)
     s.set_fill_arithmetic(native.FILL_FP32)
     t_fill32 = timed(lambda: s.fill_device(x_mixed, R, 0))
     s.set_precision(native.FP32)
@@ -404,6 +407,7 @@ def main():
     t_wca32 = s.time_stencil_sum(UATT, 0, native.FP32, reps=5)
     t_wca64 = s.time_stencil_sum(UATT, 0, native.FP64, reps=1)
     t_wca_ff = s.time_stencil_sum(UATT, 0, native.FILL_FF, reps=rep64)
+    t_wca_fft = s.time_stencil_sum(UATT, 0, native.FILL_FFT, reps=3)
     L_att = len(p.stencils[(UATT, 0)][1])
     flops_att = 2.0 * p.nnodes * L_att
     mma_flops = tc_issued_flops(p)
@@ -449,8 +453,10 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_solve, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": (("f64-accurate residual near the solution (float-float 3-D sums, rechecked in f64)"
-                       if args.accurate_fill == "ff" else "f64 residual near the solution") +
+            "dtype": ({"ff": "f64-accurate residual near the solution (float-float 3-D sums, rechecked in f64)",
+                       "fft": "f64 residual near the solution (3-D sums as f64 FFT convolutions, rechecked by the "
+                              "direct f64 sums)",
+                       "fp64": "f64 residual near the solution"}[args.accurate_fill] +
                       ("; Schur products: split-f16 x3 tensor-core attraction sums, f32 other stencil sums"
                        if args.products == "fp16tc" else "; f32 stencil sums in the Schur products")),
             "data": "synthetic",
@@ -485,8 +491,13 @@ def main():
                          "issued_mma": "3 MMAs (hi*hi, hi*lo, lo*hi) of 128x64x16 per K-step of each stencil line",
                          "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
                          "fp64_ms_per_launch": t_wca64},
-            # the other large kernel of a solve: the float-float attraction sum of the accurate fills, bound by
-            # the FP32 issue rate (12 FP32 operations per term; nominal 152 SMs x 128 lanes x clock)
+            # the attraction sum of the accurate fills: an FP64 FFT convolution by default (--accurate-fill fft;
+            # its cost is two transforms of the 192^3 box, independent of the stencil's length), else the
+            # float-float sum, bound by the FP32 issue rate (12 FP32 operations per term; nominal 152 SMs x 128
+            # lanes x clock), reported here for comparison
+            "fill_attraction_sum": {"fft_ms_per_sum": t_wca_fft,
+                                    "fft_logical_tflops": flops_att / (t_wca_fft * 1e-3) / 1e12,
+                                    "fft_vs_float_float": t_wca_ff / t_wca_fft},
             "fill_kernel": {"kernel": "k_conv_slab_ff (float-float attraction sum of the accurate fills)",
                             "bound": "fp32 issue", "ms_per_launch": t_wca_ff,
                             "achieved": 12.0 * flops_att / 2.0 / (t_wca_ff * 1e-3) / 1e12,
@@ -497,7 +508,8 @@ def main():
                             "peak_source": "nominal FP32 issue rate at the maximum SM clock",
                             "logical_tflops": flops_att / (t_wca_ff * 1e-3) / 1e12},
             "cpu_baseline": cb,
-            "breakdown_ms": {"fill_fp64": t_fill, "fill_float_float": t_fill_ff, "fill_fp32": t_fill32,
+            "breakdown_ms": {"fill_fp64": t_fill, "fill_float_float": t_fill_ff, "fill_fft": t_fill_fft,
+                             "attraction_sum_fft": t_wca_fft, "fill_fp32": t_fill32,
                              "schur_apply_fp32": t_apply32,
                              "schur_apply_fp16tc": t_apply_tc,
                              "schur_apply_fp64": t_apply64, "schur_applies_in_timed_steps": int(st["schur_applies"])},

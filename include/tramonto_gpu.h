@@ -156,13 +156,21 @@ int tgpu_set_precision(tgpu_handle h, int precision);
  *                      field (max norms).  tgpu_newton uses FP32 sums while ||R|| > switch_norm.
  * tau / switch_norm <= 0 keep the current values (defaults 1e-2 and 1.0). */
 enum { TGPU_FILL_FP64 = 0, TGPU_FILL_FP32 = 1, TGPU_FILL_REFINED = 2, TGPU_FILL_MIXED = 3, TGPU_FILL_FF = 4,
-       TGPU_FILL_MIXED_FF = 5 };
+       TGPU_FILL_MIXED_FF = 5, TGPU_FILL_FFT = 6, TGPU_FILL_MIXED_FFT = 7 };
+/* TGPU_FILL_FFT: as TGPU_FILL_FF, but in 3-D the long stencil sums (the attraction stencil; see
+ * tgpu_set_fft_threshold) are FP64 FFT convolutions of the padded channel (forward transform, product with the stencil
+ * coefficient's spectrum, inverse transform: the same sum to the FFT's rounding, ~eps log2 of the box, at a
+ * cost independent of the stencil's length); the short ones stay float-float; 1-D and 2-D problems take
+ * the direct FP64 sums.  TGPU_FILL_MIXED_FFT: FP32 sums while ||R||_2 > switch_norm, TGPU_FILL_FFT below. */
 /* TGPU_FILL_FF: as TGPU_FILL_FP64, but the 3-D single-channel stencil sums (attraction, theta) run in
  * float-float arithmetic (FP32 high/low pairs, error-free products and two-sums: ~48-bit sums, within
  * ~1e-13 of FP64); TGPU_FILL_MIXED_FF: FP32 sums while ||R||_2 > switch_norm, TGPU_FILL_FF below. */
 /* TGPU_FILL_MIXED: in tgpu_newton_solve, FP32 sums while ||R||_2 > switch_norm, FP64 below;
  * everywhere else it is the FP64 fill. */
 int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm);
+/* Stencils of at least min_points points take the FFT in TGPU_FILL_FFT; min_points < 0 (default): a cost
+ * model (direct float-float sum against the transforms) chooses. */
+int tgpu_set_fft_threshold(tgpu_handle h, int min_points);
 /* Second derivatives of the FMT energy density in J, J^T and Schur products (and so in Newton):
  *   TGPU_JAC_REFERENCE  the reference's tables, entry for entry (default): d2phi_drb2_{delta,theta}_rb_FMT*
  *                       (src/dft_physics_FMT{1,2,3,4}.c, via FMT2ndDeriv*_switch, src/dft_switch_FMT.c:122-152)
@@ -362,8 +370,9 @@ const char *tgpu_noalloc_last_error(void);
 
 /* Benchmark hook: device time (CUDA events on the handle's stream) of one
  * forward stencil sum with stencil (type, index) over the density of the last
- * fill, in TGPU_FP64, TGPU_FP32, TGPU_FP16TC or TGPU_FILL_FF (the float-float sum
- * of the accurate fills), averaged over reps launches. */
+ * fill, in TGPU_FP64, TGPU_FP32, TGPU_FP16TC, TGPU_FILL_FF (the float-float sum
+ * of the accurate fills) or TGPU_FILL_FFT (the FFT convolution, forward transform included), averaged
+ * over reps launches. */
 int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum);
 
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */

@@ -1,0 +1,68 @@
+"""FP64 stencil sums by FFT (TGPU_FILL_FFT): the accurate fill's long 3-D sums (the attraction stencil) as
+FFT convolutions, the short ones (theta, delta) as float-float sums.
+
+- At the fixture states of the 3-D reference cases (FMT1+WCA rough wall, FMT2/FMT4 rough walls) the
+  TGPU_FILL_FFT residual with every stencil sum taken by FFT (forward multi-output delta sums, transposed
+  delta and theta sums, attraction) equals the reference's to the 1e-12 of the FP64 parity tests;
+- on the 64^3 configuration-2 problem (default choice: the attraction sum by FFT) and with every sum by FFT
+  it equals the direct FP64 fill to 5e-12 at the initial state (the FFT's rounding, ~eps log2 of the box
+  times the sums' scale, against the direct sums' own ~1e-12);
+- a TGPU_FILL_MIXED_FFT Newton solve reaches ||R||_2 <= 1e-8, its residual re-evaluated by the direct
+  FP64 fill is below 1e-8 too, and its density equals the FP64 solve's to 1e-9.
+"""
+import numpy as np
+import pytest
+
+from goldens import RESID_ATOL, load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["fmt1_wca_3d", "rough3d_fmt2", "rough3d_fmt4"])
+def test_fft_fill_matches_reference_fixture(name):
+    from tramonto_gb300 import native
+    z, p = load(name)
+    s = native.Solver(p)
+    s.set_fill_arithmetic(native.FILL_FFT)
+    s.set_fft_threshold(0)   # every stencil by FFT: the multi-output delta sums and the transposed sums too
+    for k in range(len(z["states"])):
+        R = s.fill(z[f"x{k}"], mode=1)
+        err = np.abs(R - z[f"R{k}"]).max()
+        print(name, "state", k, "max |R_fft - R_ref|", err)
+        assert err <= RESID_ATOL, (name, k, err)
+    s.close()
+
+
+def test_fft_fill_matches_fp64_fill():
+    from tramonto_gb300 import native, setup
+    p, _ = setup.config2(n=64)
+    s = native.Solver(p)
+    x = setup.initial_state(s, p)
+    R64 = s.fill(x, mode=1)
+    s.set_fill_arithmetic(native.FILL_FFT)
+    for thr in (-1, 0):
+        s.set_fft_threshold(thr)
+        Rfft = s.fill(x, mode=1)
+        err = np.abs(Rfft - R64).max()
+        print("64^3 threshold", thr, ": max |R_fft - R_fp64|", err, "max |R|", np.abs(R64).max(),
+              "||R_fft - R_fp64||_2", np.linalg.norm(Rfft - R64))
+        assert err <= 5e-12
+    s.close()
+
+
+def test_mixed_fft_newton_solve():
+    from tramonto_gb300 import native, setup
+    p, _ = setup.config2(n=40)
+    s = native.Solver(p)
+    x0 = setup.initial_state(s, p)
+    x64, _, _, _ = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-10)
+    s.set_precision(native.FP16TC)
+    s.set_fill_arithmetic(native.FILL_MIXED_FFT, switch_norm=0.1)
+    xf, it, rn, li = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-6)
+    assert rn <= 1e-8
+    s.set_fill_arithmetic(native.FILL_FP64)
+    r64 = np.linalg.norm(s.fill(xf, mode=1))
+    print("mixed-FFT solve:", it, "iterations, ||R||_2", rn, "re-evaluated in FP64", r64)
+    assert r64 <= 1e-8
+    assert np.abs(xf[p.first_rho] - x64[p.first_rho]).max() <= 1e-9
+    s.close()

@@ -167,6 +167,14 @@ struct Ctx : tgpu_ctx {
   double *d_cscr2 = nullptr;     // [nunk][N] the adjoint's folded right-hand side
   tgpu::CoarseRows cr{};
   bool coarse() const { return cr.ncoarse > 0; }
+  // FP64 FFT stencil sums (TGPU_FILL_FFT): plan, work boxes, which padded channel box 0 holds the spectrum of
+  tgpu::FftPlan fft{};
+  int fft_state = 0;             // 0 not built, 1 ready, -1 not available for this problem
+  bool fft_on = false;
+  double2 *d_fbox[3] = {nullptr, nullptr, nullptr};
+  long pad_gen = 0, fft_gen = -1;
+  int fft_ch = -1;
+  int fft_min_points = -1;       // < 0: the cost model decides which stencils take the FFT
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -250,6 +258,7 @@ long nnodes(const tgpu_geometry &g)
 // Pad `nch` channels of `src` with parameter set `pp`, into the FP32 or the FP64 padded box.
 void pad(Ctx *c, const double *src, const PadParams &pp, bool f32)
 {
+  c->pad_gen++;   // the padded channels change: a cached spectrum of them is stale
   if (!f32)
     tgpu::launch_pad<double>(src, c->d_pad, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
   else
@@ -257,9 +266,106 @@ void pad(Ctx *c, const double *src, const PadParams &pp, bool f32)
   c->stats.kernel_launches++;
 }
 
+// ---- FP64 stencil sums by FFT ----------------------------------------------------
+
+// Which stencils take the FFT in TGPU_FILL_FFT: those whose direct float-float sum (measured on GB300:
+// ~5.4e-13 s per term) costs more than the transforms (~1.8e-11 s per point and log2 of the box, one per
+// coefficient plus the field's), unless tgpu_set_fft_threshold fixed a length.  At 128^3 the attraction
+// stencil (7e4 points) qualifies, theta and delta (~1e3) do not.
+bool fft_worth(const Ctx *c, const DevStencil &st, int nq)
+{
+  if (c->fft_min_points >= 0) return st.L >= c->fft_min_points;
+  const double NF = (double)c->fft.NF;
+  return (double)st.L * (double)c->dg.N * 5.4e-13 > (nq + 1) * NF * std::log2(NF) * 1.8e-11;
+}
+
+// plan, work boxes and the spectra of every zone-0 stencil coefficient (forward outputs, transpose inputs)
+void ensure_fft(Ctx *c)
+{
+  if (c->fft_state != 0) return;
+  c->fft_state = -1;
+  const tgpu::DevGeom &dg = c->dg;
+  if (dg.ndim != 3) return;
+  const int P[3] = {dg.P[0], dg.P[1], dg.P[2]};
+  if (!tgpu::fft_make_plan(c->fft, P, dg.ndim, c->stream)) return;
+  const long NF = c->fft.NF;
+  // device memory: three work boxes and one box per stencil coefficient
+  size_t nspec = 0;
+  for (int t = 0; t < 3; t++)
+    for (auto &st : c->sten[t])
+      if (st.L > 0 && fft_worth(c, st, st.nout_fwd)) nspec += st.nout_fwd + (st.d_coef_tr ? st.nin_tr : 0);
+  if (nspec == 0) return;
+  size_t free_b = 0, total_b = 0;
+  ck(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  if ((nspec + 3) * (size_t)NF * sizeof(double2) > free_b / 2) return;
+  for (auto &b : c->d_fbox) b = dalloc<double2>((size_t)NF);
+  for (int t = 0; t < 3; t++)
+    for (auto &st : c->sten[t]) {
+      if (st.L == 0 || !fft_worth(c, st, st.nout_fwd)) continue;
+      for (int side = 0; side < 2; side++) {
+        const double *coef = side == 0 ? st.d_coef_fwd : st.d_coef_tr;
+        const int nq = side == 0 ? st.nout_fwd : st.nin_tr;
+        if (!coef) continue;
+        for (int q = 0; q < nq; q++) {
+          double2 *k = dalloc<double2>((size_t)NF);
+          tgpu::launch_fft_kernel_box(st.d_off, coef, st.L, nq, q, k, c->fft, c->stream);
+          tgpu::fft3d(k, c->fft, dg.ndim, false, c->stream);
+          (side == 0 ? st.spec_fwd : st.spec_tr).push_back(k);
+        }
+      }
+    }
+  ck(cudaStreamSynchronize(c->stream), "sync");
+  c->fft_state = 1;
+}
+
+// spectrum of padded FP64 channel ch in box 0 (kept while the padded channels stay the same)
+const double2 *fft_channel(Ctx *c, int ch)
+{
+  if (c->fft_gen == c->pad_gen && c->fft_ch == ch) return c->d_fbox[0];
+  const int P[3] = {c->dg.P[0], c->dg.P[1], c->dg.P[2]};
+  tgpu::launch_fft_load(c->d_pad + (long)ch * c->dg.NP, P, c->d_fbox[0], c->fft, c->stream);
+  tgpu::fft3d(c->d_fbox[0], c->fft, c->dg.ndim, false, c->stream);
+  c->stats.kernel_launches += 1 + c->dg.ndim;
+  c->fft_gen = c->pad_gen;
+  c->fft_ch = ch;
+  return c->d_fbox[0];
+}
+
+void fft_conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
+{
+  const tgpu::DevGeom &dg = c->dg;
+  const long NF = c->fft.NF;
+  const int h[3] = {dg.h[0], dg.h[1], dg.h[2]}, nx[3] = {dg.nx[0], dg.nx[1], dg.nx[2]};
+  const double scale = 1.0 / (double)NF;
+  if (!tr) {
+    const double2 *F = fft_channel(c, ch0);
+    for (int q = 0; q < nout; q++) {
+      tgpu::launch_spec_mul(F, st.spec_fwd[q], c->d_fbox[1], NF, false, c->stream);
+      tgpu::fft3d(c->d_fbox[1], c->fft, dg.ndim, true, c->stream);
+      tgpu::launch_fft_extract(c->d_fbox[1], c->fft, h, nx, scale, outs[q], c->stream);
+      c->stats.kernel_launches += 2 + dg.ndim;
+    }
+  } else {
+    for (int k = 0; k < nin; k++) {
+      const double2 *F = fft_channel(c, ch0 + k);
+      tgpu::launch_spec_mul(F, st.spec_tr[k], c->d_fbox[2], NF, k > 0, c->stream);
+      c->stats.kernel_launches++;
+    }
+    tgpu::fft3d(c->d_fbox[2], c->fft, dg.ndim, true, c->stream);
+    tgpu::launch_fft_extract(c->d_fbox[2], c->fft, h, nx, scale, outs[0], c->stream);
+    c->stats.kernel_launches += 1 + dg.ndim;
+  }
+  c->stats.conv_launches++;
+}
+
 void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool f32)
 {
   const long NP = c->dg.NP;
+  if (!f32 && c->fft_on && c->fft_state == 1 && (tr ? (int)st.spec_tr.size() == nin && nout == 1
+                                                      : (int)st.spec_fwd.size() == nout && nin == 1)) {
+    fft_conv(c, ch0, nin, st, tr, outs, nout);
+    return;
+  }
   if (f32 && c->tc_on && !tr && nin == 1 && nout == 1 && st.tc.nplanes > 0) {
     tgpu::launch_sten_tc(c->d_pad32 + (long)ch0 * NP, c->dg, c->tcslab, st.tc, outs[0], true, c->stream);
     c->stats.conv_launches++;
@@ -495,11 +601,14 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
     }
   } else {
     const bool f32 = arith == TGPU_FILL_FP32;
-    c->ff_on = arith == TGPU_FILL_FF;
+    c->ff_on = arith == TGPU_FILL_FF || arith == TGPU_FILL_FFT;   // FFT: long stencils; float-float: the rest
+    c->fft_on = arith == TGPU_FILL_FFT;
+    if (c->fft_on) ensure_fft(c);
     forward_pass(c, rho, c->pads.rho_res, f32);
     tgpu::launch_fmt_local(x, c->d_chan, c->stream);
     transpose_pass(c, c->pads.tr_res, f32);
     c->ff_on = false;
+    c->fft_on = false;
   }
   tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream);
   c->stats.kernel_launches += 2;
@@ -515,7 +624,8 @@ void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
   // outside the Newton solve the mixed policy means the accurate (FP64) residual
   fill_arith(c, d_x, d_R, mode,
              c->fill_mode == TGPU_FILL_MIXED ? TGPU_FILL_FP64
-             : c->fill_mode == TGPU_FILL_MIXED_FF ? TGPU_FILL_FF : c->fill_mode);
+             : c->fill_mode == TGPU_FILL_MIXED_FF ? TGPU_FILL_FF
+             : c->fill_mode == TGPU_FILL_MIXED_FFT ? TGPU_FILL_FFT : c->fill_mode);
 }
 
 void need_state(Ctx *c)
@@ -833,11 +943,13 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
   coarse_state(c, d_x);
   for (;;) {
     int arith = c->fill_mode;
-    const bool inexact = (arith == TGPU_FILL_MIXED || arith == TGPU_FILL_MIXED_FF || arith == TGPU_FILL_REFINED) &&
+    const bool inexact = (arith == TGPU_FILL_MIXED || arith == TGPU_FILL_MIXED_FF || arith == TGPU_FILL_MIXED_FFT ||
+                          arith == TGPU_FILL_REFINED) &&
                          rprev > c->refine_switch;
     if (inexact) arith = TGPU_FILL_FP32;
     else if (arith == TGPU_FILL_MIXED) arith = TGPU_FILL_FP64;
     else if (arith == TGPU_FILL_MIXED_FF) arith = TGPU_FILL_FF;
+    else if (arith == TGPU_FILL_MIXED_FFT) arith = TGPU_FILL_FFT;
     fill_arith(c, d_x, d_R, 0, arith);
     tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
     red_to_host(c, 1);
@@ -1864,7 +1976,11 @@ int tgpu_destroy(tgpu_handle h)
             dfree(L.d_planes); dfree(L.d_lines); dfree(L.d_w); dfree(L.d_w_lo);
           }
         tgpu::tc_free_tables(st.tc);
+        for (auto *V : {&st.spec_fwd, &st.spec_tr})
+          for (auto &k : *V) dfree(k);
       }
+    for (auto &b : c->d_fbox) dfree(b);
+    tgpu::fft_free_plan(c->fft);
     for (int z = 1; z < tgpu::kMaxZone; z++)
       for (int t = 0; t < 3; t++)
         for (auto &st : c->zsten[z][t]) {
@@ -2102,12 +2218,35 @@ int tgpu_set_jacobian_form(tgpu_handle h, int form)
   });
 }
 
+int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    c->fft_min_points = min_points < 0 ? -1 : min_points;
+    if (c->fft_state != 0) {   // spectra are rebuilt for the new choice at the next FFT fill
+      ck(cudaStreamSynchronize(c->stream), "sync");
+      for (int t = 0; t < 3; t++)
+        for (auto &st : c->sten[t]) {
+          for (auto *V : {&st.spec_fwd, &st.spec_tr}) {
+            for (auto &k : *V) dfree(k);
+            V->clear();
+          }
+        }
+      for (auto &b : c->d_fbox) dfree(b);
+      tgpu::fft_free_plan(c->fft);
+      c->fft_state = 0;
+      c->fft_gen = -1;
+    }
+    return TGPU_OK;
+  });
+}
+
 int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch_norm)
 {
   return guard([&] {
     Ctx *c = C(h);
     if (arith != TGPU_FILL_FP64 && arith != TGPU_FILL_FP32 && arith != TGPU_FILL_REFINED && arith != TGPU_FILL_MIXED &&
-        arith != TGPU_FILL_FF && arith != TGPU_FILL_MIXED_FF)
+        arith != TGPU_FILL_FF && arith != TGPU_FILL_MIXED_FF && arith != TGPU_FILL_FFT && arith != TGPU_FILL_MIXED_FFT)
       throw Error(TGPU_ERR_ARG, "fill arithmetic");
     if (tau > 0) c->refine_tau = tau;
     if (switch_norm > 0) c->refine_switch = switch_norm;
@@ -2360,14 +2499,20 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     if (type < 0 || type > 2 || index < 0 || index >= (int)c->sten[type].size() || c->sten[type][index].L == 0)
       throw Error(TGPU_ERR_ARG, "no such stencil");
     if (reps < 1) throw Error(TGPU_ERR_ARG, "reps");
-    if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC && precision != TGPU_FILL_FF)
+    if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC && precision != TGPU_FILL_FF &&
+        precision != TGPU_FILL_FFT)
       throw Error(TGPU_ERR_ARG, "precision");
+    if (precision == TGPU_FILL_FFT) {
+      ensure_fft(c);
+      if (c->fft_state != 1) throw Error(TGPU_ERR_UNSUPPORTED, "FFT sums unavailable for this problem");
+    }
     const bool f32 = precision == TGPU_FP32 || precision == TGPU_FP16TC;
     if (precision == TGPU_FP16TC && !c->tc_ready)
       throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
-    const bool tc_prev = c->tc_on, ff_prev = c->ff_on;
+    const bool tc_prev = c->tc_on, ff_prev = c->ff_on, fft_prev = c->fft_on;
     c->tc_on = precision == TGPU_FP16TC;
-    c->ff_on = precision == TGPU_FILL_FF;
+    c->ff_on = precision == TGPU_FILL_FF || precision == TGPU_FILL_FFT;
+    c->fft_on = precision == TGPU_FILL_FFT;
     const DevStencil &st = c->sten[type][index];
     const int jc = type == TGPU_STEN_UATT ? index / c->dg.ncomp : index;
     const long N = c->dg.N;
@@ -2378,7 +2523,10 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     ck(cudaEventCreate(&c->ev1), "event");
     conv(c, jc, 1, st, false, out, 1, f32);   // warm-up
     ck(cudaEventRecord(c->ev0, c->stream), "event");
-    for (int r = 0; r < reps; r++) conv(c, jc, 1, st, false, out, 1, f32);
+    for (int r = 0; r < reps; r++) {
+      c->fft_gen = -1;   // each FFT sum transforms its field afresh
+      conv(c, jc, 1, st, false, out, 1, f32);
+    }
     ck(cudaEventRecord(c->ev1, c->stream), "event");
     ck(cudaEventSynchronize(c->ev1), "event");
     float ms = 0.f;
@@ -2388,6 +2536,7 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     c->ev0 = c->ev1 = nullptr;
     c->tc_on = tc_prev;
     c->ff_on = ff_prev;
+    c->fft_on = fft_prev;
     tc_check(c);
     *ms_per_sum = ms / reps;
     return TGPU_OK;

@@ -29,7 +29,7 @@ from .problem import Problem
 
 TGPU_OK = 0
 FP64, FP32, BF16X3, FP16TC = 0, 1, 2, 3
-FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF, FILL_MIXED_FF = 0, 1, 2, 3, 4, 5
+FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF, FILL_MIXED_FF, FILL_FFT, FILL_MIXED_FFT = 0, 1, 2, 3, 4, 5, 6, 7
 JAC_REFERENCE, JAC_EXACT = 0, 1
 STATUS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported",
           -5: "no convergence", -6: "non-finite values", -7: "domain error"}
@@ -86,6 +86,7 @@ def load(build_if_missing: bool = False):
         "tgpu_destroy": [vp],
         "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_zones": [vp, C.c_int, vp, vp],
+        "tgpu_set_fft_threshold": [vp, C.c_int],
         "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
@@ -331,9 +332,13 @@ class Solver:
         _check(self.lib.tgpu_set_jacobian_form(self.h, int(form)), self.lib)
 
     def set_fill_arithmetic(self, arith: int, tau: float = 0.0, switch_norm: float = 0.0):
-        """Residual arithmetic: FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF or FILL_MIXED_FF
-        (see include/tramonto_gpu.h)."""
+        """Residual arithmetic: FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF, FILL_MIXED_FF,
+        FILL_FFT or FILL_MIXED_FFT (see include/tramonto_gpu.h)."""
         _check(self.lib.tgpu_set_fill_arithmetic(self.h, int(arith), float(tau), float(switch_norm)), self.lib)
+
+    def set_fft_threshold(self, min_points: int):
+        """Stencils of at least min_points points take the FFT in FILL_FFT; < 0: the cost model decides."""
+        _check(self.lib.tgpu_set_fft_threshold(self.h, int(min_points)), self.lib)
 
     def set_stream(self, stream_handle: int):
         _check(self.lib.tgpu_set_stream(self.h, C.c_void_p(stream_handle)), self.lib)
