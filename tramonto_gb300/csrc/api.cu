@@ -175,6 +175,12 @@ struct Ctx : tgpu_ctx {
   long pad_gen = 0, fft_gen = -1;
   int fft_ch = -1;
   int fft_min_points = -1;       // < 0: the cost model decides which stencils take the FFT
+  bool fft_plan_ok = false;
+  // FP32 FFT sums of the long stencils in FP32 arithmetic: chosen per context by timing against the
+  // tensor-core sum (products) and the FP32 slab sum (FP32 fills): 0 undecided, 1 FFT, -1 direct
+  float2 *d_fbox32[2] = {nullptr, nullptr};
+  int fft32_tc = 0, fft32_slab = 0;
+  bool spec32_built = false;
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -288,6 +294,7 @@ void ensure_fft(Ctx *c)
   if (dg.ndim != 3) return;
   const int P[3] = {dg.P[0], dg.P[1], dg.P[2]};
   if (!tgpu::fft_make_plan(c->fft, P, dg.ndim, c->stream)) return;
+  c->fft_plan_ok = true;
   const long NF = c->fft.NF;
   // device memory: three work boxes and one box per stencil coefficient
   size_t nspec = 0;
@@ -331,6 +338,49 @@ const double2 *fft_channel(Ctx *c, int ch)
   return c->d_fbox[0];
 }
 
+// FP32 spectra of the attraction stencils (from FP64 ones) and two FP32 work boxes
+bool prepare_spec32(Ctx *c)
+{
+  if (c->spec32_built) return true;
+  ensure_fft(c);
+  if (!c->fft_plan_ok) return false;
+  const long NF = c->fft.NF;
+  double2 *tmp = dalloc<double2>((size_t)NF);
+  for (auto &st : c->sten[TGPU_STEN_UATT]) {
+    if (st.L == 0 || !st.spec_fwd32.empty()) continue;
+    for (int q = 0; q < st.nout_fwd; q++) {
+      tgpu::launch_fft_kernel_box(st.d_off, st.d_coef_fwd, st.L, st.nout_fwd, q, tmp, c->fft, c->stream);
+      tgpu::fft3d(tmp, c->fft, c->dg.ndim, false, c->stream);
+      float2 *k = dalloc<float2>((size_t)NF);
+      tgpu::launch_to_float2(tmp, k, NF, c->stream);
+      st.spec_fwd32.push_back(k);
+    }
+  }
+  ck(cudaStreamSynchronize(c->stream), "sync");
+  dfree(tmp);
+  for (auto &b : c->d_fbox32)
+    if (!b) b = dalloc<float2>((size_t)NF);
+  c->spec32_built = true;
+  return true;
+}
+
+void fft_conv32(Ctx *c, int ch0, const DevStencil &st, double *const *outs, int nout)
+{
+  const tgpu::DevGeom &dg = c->dg;
+  const long NF = c->fft.NF;
+  const int P[3] = {dg.P[0], dg.P[1], dg.P[2]}, h[3] = {dg.h[0], dg.h[1], dg.h[2]};
+  const int nx[3] = {dg.nx[0], dg.nx[1], dg.nx[2]};
+  tgpu::launch_fft_load(c->d_pad32 + (long)ch0 * dg.NP, P, c->d_fbox32[0], c->fft, c->stream);
+  tgpu::fft3d(c->d_fbox32[0], c->fft, dg.ndim, false, c->stream);
+  for (int q = 0; q < nout; q++) {
+    tgpu::launch_spec_mul(c->d_fbox32[0], st.spec_fwd32[q], c->d_fbox32[1], NF, false, c->stream);
+    tgpu::fft3d(c->d_fbox32[1], c->fft, dg.ndim, true, c->stream);
+    tgpu::launch_fft_extract(c->d_fbox32[1], c->fft, h, nx, 1.0 / (double)NF, outs[q], c->stream);
+  }
+  c->stats.kernel_launches += 1 + dg.ndim + nout * (2 + dg.ndim);
+  c->stats.conv_launches++;
+}
+
 void fft_conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
 {
   const tgpu::DevGeom &dg = c->dg;
@@ -364,6 +414,11 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
   if (!f32 && c->fft_on && c->fft_state == 1 && (tr ? (int)st.spec_tr.size() == nin && nout == 1
                                                       : (int)st.spec_fwd.size() == nout && nin == 1)) {
     fft_conv(c, ch0, nin, st, tr, outs, nout);
+    return;
+  }
+  if (f32 && !tr && nin == 1 && (int)st.spec_fwd32.size() == nout &&
+      (c->tc_on ? c->fft32_tc == 1 : c->fft32_slab == 1)) {
+    fft_conv32(c, ch0, st, outs, nout);
     return;
   }
   if (f32 && c->tc_on && !tr && nin == 1 && nout == 1 && st.tc.nplanes > 0) {
@@ -445,6 +500,38 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
   c->stats.kernel_launches++;
 }
 
+// Whether the FP32 attraction sums of the current context (tensor-core products, or FP32 slab sums) run
+// faster as FP32 FFT convolutions: timed once per context on the padded channel 0 (values do not matter;
+// the scratch output is d_tr, which every caller of forward_pass fills afterwards).
+void decide_fft32(Ctx *c)
+{
+  int &flag = c->tc_on ? c->fft32_tc : c->fft32_slab;
+  if (flag != 0) return;
+  flag = -1;
+  if (!prepare_spec32(c)) return;
+  const DevStencil &st = c->sten[TGPU_STEN_UATT][0];
+  if (st.spec_fwd32.empty()) return;
+  double *o[1] = {c->d_tr};
+  cudaEvent_t ev[4];
+  for (auto &e : ev) ck(cudaEventCreate(&e), "event");
+  flag = -1;
+  conv(c, 0, 1, st, false, o, 1, true);   // warm-up of the direct sum
+  ck(cudaEventRecord(ev[0], c->stream), "event");
+  for (int r = 0; r < 2; r++) conv(c, 0, 1, st, false, o, 1, true);
+  ck(cudaEventRecord(ev[1], c->stream), "event");
+  flag = 1;
+  conv(c, 0, 1, st, false, o, 1, true);   // warm-up of the FFT sum
+  ck(cudaEventRecord(ev[2], c->stream), "event");
+  for (int r = 0; r < 2; r++) conv(c, 0, 1, st, false, o, 1, true);
+  ck(cudaEventRecord(ev[3], c->stream), "event");
+  ck(cudaEventSynchronize(ev[3]), "event");
+  float t_direct = 0.f, t_fft = 0.f;
+  ck(cudaEventElapsedTime(&t_direct, ev[0], ev[1]), "event");
+  ck(cudaEventElapsedTime(&t_fft, ev[2], ev[3]), "event");
+  for (auto &e : ev) cudaEventDestroy(e);
+  flag = t_fft < t_direct ? 1 : -1;
+}
+
 // Weighted-density (and mean-field) sums of the padded density channels with one zone's stencils
 // into out (rows as d_conv)
 void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, bool f32)
@@ -482,6 +569,7 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bo
   const size_t nrows = (size_t)(g.nrb + g.ncomp);
   if (zero_first) ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * nrows * N, c->stream), "memset");
   pad(c, field, pp, f32);
+  if (f32 && g.attraction && g.ndim == 3) decide_fft32(c);
   forward_convs(c, c->sten, c->d_conv, f32);
   // nodes of the coarser quadrature zones keep their own zone's sums (zero_first holds with zones)
   for (int z = 1; z < c->nzone; z++) {
@@ -1978,8 +2066,10 @@ int tgpu_destroy(tgpu_handle h)
         tgpu::tc_free_tables(st.tc);
         for (auto *V : {&st.spec_fwd, &st.spec_tr})
           for (auto &k : *V) dfree(k);
+        for (auto &k : st.spec_fwd32) dfree(k);
       }
     for (auto &b : c->d_fbox) dfree(b);
+    for (auto &b : c->d_fbox32) dfree(b);
     tgpu::fft_free_plan(c->fft);
     for (int z = 1; z < tgpu::kMaxZone; z++)
       for (int t = 0; t < 3; t++)
@@ -2233,9 +2323,17 @@ int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
           }
         }
       for (auto &b : c->d_fbox) dfree(b);
+      for (auto &st : c->sten[TGPU_STEN_UATT]) {
+        for (auto &k : st.spec_fwd32) dfree(k);
+        st.spec_fwd32.clear();
+      }
+      for (auto &b : c->d_fbox32) dfree(b);
       tgpu::fft_free_plan(c->fft);
       c->fft_state = 0;
       c->fft_gen = -1;
+      c->fft_plan_ok = false;
+      c->spec32_built = false;
+      c->fft32_tc = c->fft32_slab = 0;
     }
     return TGPU_OK;
   });
@@ -2510,6 +2608,8 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     if (precision == TGPU_FP16TC && !c->tc_ready)
       throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
     const bool tc_prev = c->tc_on, ff_prev = c->ff_on, fft_prev = c->fft_on;
+    const int fft32_prev[2] = {c->fft32_tc, c->fft32_slab};
+    c->fft32_tc = c->fft32_slab = -1;   // the direct kernels of each arithmetic (tensor core, FP32 slab)
     c->tc_on = precision == TGPU_FP16TC;
     c->ff_on = precision == TGPU_FILL_FF || precision == TGPU_FILL_FFT;
     c->fft_on = precision == TGPU_FILL_FFT;
@@ -2537,6 +2637,8 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     c->tc_on = tc_prev;
     c->ff_on = ff_prev;
     c->fft_on = fft_prev;
+    c->fft32_tc = fft32_prev[0];
+    c->fft32_slab = fft32_prev[1];
     tc_check(c);
     *ms_per_sum = ms / reps;
     return TGPU_OK;

@@ -56,6 +56,7 @@ struct FftAxis {
   int n = 1, nst = 0;
   int rad[16] = {0};
   double2 *d_tw = nullptr;   // exp(-2 pi i k / n), k < n
+  float2 *d_tw32 = nullptr;  // the same rounded to FP32 (the products' FP32 transforms)
 };
 struct FftPlan {
   int F[3] = {1, 1, 1};
@@ -65,15 +66,21 @@ struct FftPlan {
 bool fft_make_plan(FftPlan &p, const int P[3], int ndim, cudaStream_t s);
 void fft_free_plan(FftPlan &p);
 void fft3d(double2 *box, const FftPlan &p, int ndim, bool inverse, cudaStream_t s);
+void fft3d(float2 *box, const FftPlan &p, int ndim, bool inverse, cudaStream_t s);
 // box <- the padded channel [P2][P1][P0], zero beyond it
 void launch_fft_load(const double *pad, const int P[3], double2 *box, const FftPlan &p, cudaStream_t s);
+void launch_fft_load(const float *pad, const int P[3], float2 *box, const FftPlan &p, cudaStream_t s);
+void launch_to_float2(const double2 *in, float2 *out, long n, cudaStream_t s);
 // box <- the correlation kernel of coefficient q of a stencil: coef[k * ncoef + q] at (-offset_k) mod F
 void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double2 *box,
                            const FftPlan &p, cudaStream_t s);
 // out = a * k (or out += a * k)
 void launch_spec_mul(const double2 *a, const double2 *k, double2 *out, long n, bool accumulate, cudaStream_t s);
+void launch_spec_mul(const float2 *a, const float2 *k, float2 *out, long n, bool accumulate, cudaStream_t s);
 // out[node] += Re(box[node + h]) * scale for the nx[0] x nx[1] x nx[2] interior
 void launch_fft_extract(const double2 *box, const FftPlan &p, const int h[3], const int nx[3], double scale,
+                        double *out, cudaStream_t s);
+void launch_fft_extract(const float2 *box, const FftPlan &p, const int h[3], const int nx[3], double scale,
                         double *out, cudaStream_t s);
 
 // Averaged rows of coarsened nodes and the prolongation onto them (coarsen.cu)
@@ -337,8 +344,10 @@ struct DevStencil {
   // float-float single-coefficient tables of a multi-channel stencil (3-D delta, one size): per forward
   // output channel and per transpose input channel, for the accurate fills
   std::vector<Lines> ff_fwd, ff_tr;
-  // FFT spectra of the correlation kernels (FP64 fills by FFT): per forward output, per transpose input
+  // FFT spectra of the correlation kernels (FP64 fills by FFT): per forward output, per transpose input;
+  // FP32 copies of the forward ones for the FP32 sums (products, FP32 fills)
   std::vector<double2 *> spec_fwd, spec_tr;
+  std::vector<float2 *> spec_fwd32;
 };
 
 }  // namespace tgpu
