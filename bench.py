@@ -273,6 +273,27 @@ def run_config5(args):
         dist.destroy_process_group()
 
 
+def fft_stream_bytes(p):
+    """Bytes an out-of-cache FP32 FFT convolution of the padded field streams (one sum)."""
+    from tramonto_gb300.problem import DELTA, THETA, UATT  # noqa: F401
+
+    def smooth(n):
+        while True:
+            m = n
+            for r in (2, 3, 5):
+                while m % r == 0:
+                    m //= r
+            if m == 1:
+                return n
+            n += 1
+    h = [max(abs(int(o[d])) for st in p.stencils.values() for o in st[0]) for d in range(3)]
+    P = [p.nx[d] + 2 * h[d] for d in range(3)]
+    NF = float(np.prod([smooth(v) for v in P]))
+    NP, N = float(np.prod(P)), float(p.nnodes)
+    box = 8.0 * NF                                   # complex FP32
+    return 4.0 * NP + box + 2 * 3 * 2 * box + 3 * box + 8.0 * N + 16.0 * N
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -408,6 +429,7 @@ def main():
     t_wca64 = s.time_stencil_sum(UATT, 0, native.FP64, reps=1)
     t_wca_ff = s.time_stencil_sum(UATT, 0, native.FILL_FF, reps=rep64)
     t_wca_fft = s.time_stencil_sum(UATT, 0, native.FILL_FFT, reps=3)
+    t_wca_fft32 = s.time_stencil_sum(UATT, 0, native.TIME_FFT32, reps=5)
     L_att = len(p.stencils[(UATT, 0)][1])
     flops_att = 2.0 * p.nnodes * L_att
     mma_flops = tc_issued_flops(p)
@@ -441,6 +463,7 @@ def main():
     e2e_s = time.perf_counter() - t0
     hbm, bf16, peak_src = peaks()
     t_dom = t_wca_tc if args.products == "fp16tc" else t_wca32
+    fft_bytes = fft_stream_bytes(p)
     ach_tf = flops_att / (t_dom * 1e-3) / 1e12
     issued_tf = mma_flops / (t_wca_tc * 1e-3) / 1e12
     if rank == 0:
@@ -476,19 +499,30 @@ def main():
             "e2e": {"value": it_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 8 * len(ladder or [0]),
                     "d2h_bytes_per_step": n * 8 * len(ladder or [0]),
                     "final_resid_norm2": rn_e2e},
-            "roofline": {"bound": "tensor",
-                         "kernel": ("attraction (WCA) stencil sum, k_sten_tc (tcgen05 split FP16 x3)"
-                                    if args.products == "fp16tc" else
-                                    "attraction (WCA) stencil sum, k_conv_slab (FP32 SIMT)"),
-                         "achieved": ach_tf, "peak": bf16, "unit": "TFLOP/s", "frac": ach_tf / bf16,
-                         "peak_source": f"{peak_src} bf16 dense",
-                         "traffic": (TC_TRAFFIC_BYTES if args.products == "fp16tc" and args.workload == "config2"
-                                     and args.n == 128 else None),
-                         "traffic_source": "profiles/k_sten_tc_wca_128.md (ncu dram bytes, one launch)",
-                         "algorithmic": f"2 x {L_att} stencil points x {p.nnodes} nodes per launch (logical)",
-                         "ms_per_launch": t_dom, "issued_mma_tflops": issued_tf,
-                         "issued_mma_frac": issued_tf / bf16,
-                         "issued_mma": "3 MMAs (hi*hi, hi*lo, lo*hi) of 128x64x16 per K-step of each stencil line",
+            # the attraction (WCA) stencil sum of the Schur products and FP32 fills: by default an FP32 FFT
+            # convolution (chosen per handle by timing it against the tensor-core and slab kernels); bound by
+            # memory streaming: its algorithmic bytes are those an out-of-cache 3-D FFT convolution streams
+            "roofline": {"bound": "hbm",
+                         "kernel": "attraction (WCA) stencil sum, FP32 FFT convolution (k_fft_load, k_fft_x / "
+                                   "k_fft_strided forward and inverse, k_spec_mul, k_fft_extract)",
+                         "achieved": fft_bytes / (t_wca_fft32 * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": fft_bytes / (t_wca_fft32 * 1e-3) / 1e9 / hbm,
+                         "peak_source": f"{peak_src} HBM copy",
+                         "traffic": None,
+                         "algorithmic": (f"{fft_bytes / 1e6:.0f} MB per sum: the padded FP32 field read and the "
+                                         "complex box written, 2 transforms x 3 axis passes reading and writing the "
+                                         "box, the spectral product (3 box streams), the interior read back and the "
+                                         "FP64 output read and written"),
+                         "ms_per_launch": t_wca_fft32,
+                         "logical_tflops": flops_att / (t_wca_fft32 * 1e-3) / 1e12,
+                         "logical": f"2 x {L_att} stencil points x {p.nnodes} nodes per sum",
+                         "tensor_core_kernel": {
+                             "kernel": "k_sten_tc (tcgen05 split FP16 x3), the direct sum it replaces",
+                             "ms_per_launch": t_wca_tc, "bound": "tensor", "achieved_logical_tflops": ach_tf,
+                             "peak": bf16, "frac": ach_tf / bf16, "issued_mma_tflops": issued_tf,
+                             "issued_mma_frac": issued_tf / bf16,
+                             "traffic": (TC_TRAFFIC_BYTES if args.workload == "config2" and args.n == 128 else None),
+                             "traffic_source": "profiles/k_sten_tc_wca_128.md (ncu dram bytes, one launch)"},
                          "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
                          "fp64_ms_per_launch": t_wca64},
             # the attraction sum of the accurate fills: an FP64 FFT convolution by default (--accurate-fill fft;
@@ -498,7 +532,7 @@ def main():
             "fill_attraction_sum": {"fft_ms_per_sum": t_wca_fft,
                                     "fft_logical_tflops": flops_att / (t_wca_fft * 1e-3) / 1e12,
                                     "fft_vs_float_float": t_wca_ff / t_wca_fft},
-            "fill_kernel": {"kernel": "k_conv_slab_ff (float-float attraction sum of the accurate fills)",
+            "float_float_attraction_sum": {"kernel": "k_conv_slab_ff (float-float attraction sum, --accurate-fill ff)",
                             "bound": "fp32 issue", "ms_per_launch": t_wca_ff,
                             "achieved": 12.0 * flops_att / 2.0 / (t_wca_ff * 1e-3) / 1e12,
                             "peak": 152 * 128 * (clk.summary().get("sm_max_mhz") or 2070.0) * 1e6 / 1e12,

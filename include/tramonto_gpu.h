@@ -371,8 +371,10 @@ const char *tgpu_noalloc_last_error(void);
 /* Benchmark hook: device time (CUDA events on the handle's stream) of one
  * forward stencil sum with stencil (type, index) over the density of the last
  * fill, in TGPU_FP64, TGPU_FP32, TGPU_FP16TC, TGPU_FILL_FF (the float-float sum
- * of the accurate fills) or TGPU_FILL_FFT (the FFT convolution, forward transform included), averaged
- * over reps launches. */
+ * of the accurate fills), TGPU_FILL_FFT (the FP64 FFT convolution, forward transform included) or
+ * TGPU_TIME_FFT32 (the FP32 FFT convolution that FP32 products and fills take where it is faster),
+ * averaged over reps launches.  TGPU_FP32 and TGPU_FP16TC time the direct kernels. */
+#define TGPU_TIME_FFT32 16
 int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum);
 
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */

@@ -2598,18 +2598,22 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
       throw Error(TGPU_ERR_ARG, "no such stencil");
     if (reps < 1) throw Error(TGPU_ERR_ARG, "reps");
     if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC && precision != TGPU_FILL_FF &&
-        precision != TGPU_FILL_FFT)
+        precision != TGPU_FILL_FFT && precision != TGPU_TIME_FFT32)
       throw Error(TGPU_ERR_ARG, "precision");
+    if (precision == TGPU_TIME_FFT32 && (type != TGPU_STEN_UATT || !prepare_spec32(c) ||
+                                         c->sten[type][index].spec_fwd32.empty()))
+      throw Error(TGPU_ERR_UNSUPPORTED, "FP32 FFT sums exist for 3-D attraction stencils only");
     if (precision == TGPU_FILL_FFT) {
       ensure_fft(c);
       if (c->fft_state != 1) throw Error(TGPU_ERR_UNSUPPORTED, "FFT sums unavailable for this problem");
     }
-    const bool f32 = precision == TGPU_FP32 || precision == TGPU_FP16TC;
+    const bool f32 = precision == TGPU_FP32 || precision == TGPU_FP16TC || precision == TGPU_TIME_FFT32;
     if (precision == TGPU_FP16TC && !c->tc_ready)
       throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
     const bool tc_prev = c->tc_on, ff_prev = c->ff_on, fft_prev = c->fft_on;
     const int fft32_prev[2] = {c->fft32_tc, c->fft32_slab};
-    c->fft32_tc = c->fft32_slab = -1;   // the direct kernels of each arithmetic (tensor core, FP32 slab)
+    // the direct kernels of each arithmetic (tensor core, FP32 slab), or the FP32 FFT
+    c->fft32_tc = c->fft32_slab = precision == TGPU_TIME_FFT32 ? 1 : -1;
     c->tc_on = precision == TGPU_FP16TC;
     c->ff_on = precision == TGPU_FILL_FF || precision == TGPU_FILL_FFT;
     c->fft_on = precision == TGPU_FILL_FFT;
