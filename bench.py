@@ -450,7 +450,7 @@ def main():
         del dx64
     # end to end through the C ABI with host buffers: copies of the state in and out inside the timed region
     mixed_mode()
-    xh = x0.copy()
+    xh = torch.from_numpy(x0.copy()).pin_memory().numpy()   # the caller's state in pinned host memory
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     it_e2e = 0
@@ -458,7 +458,8 @@ def main():
         if rb is not None:
             s.set_bulk([rb])
         xh, it_k, rn_e2e, _ = s.newton_solve(xh, resid_tol=args.resid_tol, max_iter=args.max_newton,
-                                             lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+                                             lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True,
+                                             inplace=True)
         it_e2e += it_k
     e2e_s = time.perf_counter() - t0
     hbm, bf16, peak_src = peaks()

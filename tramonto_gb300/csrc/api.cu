@@ -181,6 +181,9 @@ struct Ctx : tgpu_ctx {
   float2 *d_fbox32[2] = {nullptr, nullptr};
   int fft32_tc = 0, fft32_slab = 0;
   bool spec32_built = false;
+  // the per-node FMT Hessian scalars of the current state (products of one Newton state share them)
+  double *d_hcoef = nullptr;
+  int hcoef_form = -1;           // the Jacobian form they were made with; -1: stale
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -704,7 +707,10 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
     tgpu::launch_coarse_rows(x, d_R, g.nunk, g.first_rho, g.ncomp, N, c->cr, c->d_cbulk, c->stream);
     c->stats.kernel_launches++;
   }
-  if (mode == 0) c->have_state = true;
+  if (mode == 0) {
+    c->have_state = true;
+    c->hcoef_form = -1;   // a new state: its Hessian scalars are made at the first product
+  }
 }
 
 void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
@@ -730,6 +736,18 @@ struct TcScope {
   ~TcScope() { c->tc_on = prev; }
 };
 
+// the state's Hessian scalars for the products, made once per state and Jacobian form
+const double *hess_coef(Ctx *c)
+{
+  const int form = c->dg.jac_exact;
+  if (c->hcoef_form == form) return c->d_hcoef;
+  if (!c->d_hcoef) c->d_hcoef = dalloc<double>((size_t)tgpu::kHessCoef * c->dg.N);
+  tgpu::launch_hess_coef(c->d_x, c->d_hcoef, c->stream);
+  c->stats.kernel_launches++;
+  c->hcoef_form = form;
+  return c->d_hcoef;
+}
+
 // With coarsened nodes the Schur complement is that of the step on the other nodes: the densities, and
 // the block-1 vector between A12 and A21, are interpolated onto the coarsened nodes, whose rows are dropped.
 const double *prolonged(Ctx *c, const double *v, int nrows)
@@ -750,7 +768,7 @@ void schur_device(Ctx *c, const double *d_v2, double *d_y2)
   const double *v2 = prolonged(c, d_v2, g.ncomp);
   forward_pass(c, v2, c->pads.rho_jac, f32);
   if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.N, c->cr, nullptr, c->stream);
-  tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, c->stream);
+  tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
   transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, v2, c->d_tr, c->d_ymf, d_y2, c->stream);
   if (c->coarse()) tgpu::launch_zero_nodes(d_y2, g.ncomp, g.N, c->cr, c->stream);
@@ -765,7 +783,7 @@ void jv_device(Ctx *c, const double *d_v, double *d_out)
   const long N = c->dg.N;
   const bool f32 = c->precision != TGPU_FP64;
   forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, f32);
-  tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, c->stream);
+  tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, hess_coef(c), c->stream);
   transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_jv_combine(c->d_x, c->d_vext, c->d_zero, d_v, c->d_conv, c->d_tr, d_out, c->stream);
   c->stats.kernel_launches += 2;
@@ -777,7 +795,7 @@ void jv_device(Ctx *c, const double *d_v, double *d_out)
 
 // ---- kernels used only by the Schur rhs / back-substitution ------------------
 namespace tgpu {
-void launch_rhs_local(const double *x, const double *b, double *chan, double *ymf, cudaStream_t s);
+void launch_rhs_local(const double *x, const double *b, double *chan, double *ymf, const double *coef, cudaStream_t s);
 void launch_rhs_combine(const double *vext, const signed char *zero, const double *b, const double *tr,
                         const double *ymf, double *b2s, cudaStream_t s);
 void launch_x1(const double *b, const double *conv, const double *x2, double *dx, cudaStream_t s);
@@ -795,7 +813,7 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
     tgpu::launch_prolong(c->d_cscr, g.first_rb, g.nunk - g.ncomp, g.N, c->cr, nullptr, c->stream);
     b = c->d_cscr;
   }
-  tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, c->stream);
+  tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
   TcScope tcs(c);
   transpose_pass(c, c->pads.tr_jac, c->precision != TGPU_FP64);
   tgpu::launch_rhs_combine(c->d_vext, c->d_zero, b, c->d_tr, c->d_ymf, d_b2s, c->stream);
@@ -2077,7 +2095,7 @@ int tgpu_destroy(tgpu_handle h)
           dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
           dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
         }
-    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2);
+    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2); dfree(c->d_hcoef);
     dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
     dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);

@@ -678,6 +678,52 @@ __device__ __forceinline__ void fmt_hess_apply(const double *n, const double *y,
   fmt_hess_apply_at(n, y, z, c_g.ndim, c_g.functional, c_g.jac_exact != 0, transpose);
 }
 
+// H y at node i from the state x, with the node's Hessian scalars from coef ([kHessCoef][N], the state's, see
+// k_hess_coef) when given: the products of one Newton state then skip the FP64 evaluation of f(n3), g(n2, V2)
+__device__ __forceinline__ void hess_apply_node(const double *x, const double *coef, long i, const double *y,
+                                                double *z)
+{
+  double n[kMaxRb];
+  load_n(x, i, n);
+  if (!coef) {
+    fmt_hess_apply(n, y, z);
+    return;
+  }
+  const long N = c_g.N;
+  HessCoef c;
+  c.a = coef[i];
+  c.a2 = coef[N + i];
+  c.h13 = coef[2 * N + i];
+  c.h22 = coef[3 * N + i];
+  c.h23 = coef[4 * N + i];
+  c.h33 = coef[5 * N + i];
+  c.ff = coef[6 * N + i];
+  c.gvf1 = coef[7 * N + i];
+  c.g2vr_f = coef[8 * N + i];
+  c.g2vc_f = coef[9 * N + i];
+  c.gvv = coef[10 * N + i];
+  c.gvv_out = coef[11 * N + i];
+  fmt_hess_apply_coef(c, n, y, z, c_g.ndim, false);
+}
+
+__global__ void k_hess_coef(const double *__restrict__ x, double *__restrict__ coef)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double n[kMaxRb];
+    load_n(x, i, n);
+    const HessCoef c = fmt_hess_coef_at(n, c_g.ndim, c_g.functional, c_g.jac_exact != 0);
+    const double v[kHessCoef] = {c.a, c.a2, c.h13, c.h22, c.h23, c.h33, c.ff, c.gvf1, c.g2vr_f, c.g2vc_f, c.gvv,
+                                 c.gvv_out};
+    for (int k = 0; k < kHessCoef; k++) coef[(long)k * N + i] = v[k];
+  }
+}
+
+void launch_hess_coef(const double *x, double *coef, cudaStream_t s)
+{
+  k_hess_coef<<<1184, kThreads, 0, s>>>(x, coef);
+}
+
 // Transpose-convolution channels from a weighted-density-shaped vector q (n ordering):
 // per component A = fac (q0/4piR^2 + q1/4piR + q2), B_d = fac (q_V1d/4piR + q_V2d), C = fac q3.
 __device__ __forceinline__ void write_tr_channels(const double *q, double *chan, long i)
@@ -782,7 +828,7 @@ void launch_assemble(const double *x, const double *vext, const signed char *zer
 // Schur local step: y1 = A11^-1 u (u = A12 v in conv), then the EL-side
 // channels of H y1 for the transpose sums; y_MF = -u_MF kept for A21.
 __global__ void k_schur_local(const double *__restrict__ x, const double *__restrict__ conv,
-                              double *__restrict__ chan, double *__restrict__ ymf)
+                              double *__restrict__ chan, double *__restrict__ ymf, const double *__restrict__ coef)
 {
   const long N = c_g.N;
   const int nd = c_g.ndim;
@@ -796,37 +842,36 @@ __global__ void k_schur_local(const double *__restrict__ x, const double *__rest
     }
     y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
     for (int d = 0; d < nd; d++) { y[4 + d] = ysv[4 + nd + d]; y[4 + nd + d] = ysv[4 + d]; }
-    load_n(x, i, n);
-    fmt_hess_apply(n, y, z);
+    (void)n;
+    hess_apply_node(x, coef, i, y, z);
     write_tr_channels(z, chan, i);
     if (c_g.attraction)
       for (int ic = 0; ic < c_g.ncomp; ic++) ymf[(long)ic * N + i] = -conv[(long)(c_g.nrb + ic) * N + i];
   }
 }
 
-void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, cudaStream_t s)
+void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
+                        cudaStream_t s)
 {
-  k_schur_local<<<1184, kThreads, 0, s>>>(x, conv, chan, ymf);
+  k_schur_local<<<1184, kThreads, 0, s>>>(x, conv, chan, ymf, coef);
 }
 
 // J v local step: channels of H v_rb for the EL rows.
-__global__ void k_jv_local(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ chan)
+__global__ void k_jv_local(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ chan,
+                           const double *__restrict__ coef)
 {
   const long N = c_g.N;
-  const int nd = c_g.ndim;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-    double y[kMaxRb], n[kMaxRb], z[kMaxRb];
+    double y[kMaxRb], z[kMaxRb];
     load_n(v, i, y);
-    (void)nd;
-    load_n(x, i, n);
-    fmt_hess_apply(n, y, z);
+    hess_apply_node(x, coef, i, y, z);
     write_tr_channels(z, chan, i);
   }
 }
 
-void launch_jv_local(const double *x, const double *v, double *chan, cudaStream_t s)
+void launch_jv_local(const double *x, const double *v, double *chan, const double *coef, cudaStream_t s)
 {
-  k_jv_local<<<1184, kThreads, 0, s>>>(x, v, chan);
+  k_jv_local<<<1184, kThreads, 0, s>>>(x, v, chan, coef);
 }
 
 __global__ void k_schur_combine(const double *__restrict__ x, const double *__restrict__ vext,
@@ -896,7 +941,7 @@ void launch_jv_combine(const double *x, const double *vext, const signed char *z
 // Schur right-hand side: y1 = A11^-1 b1 from the block-1 part of a full
 // vector b, then the channels of H y1 (ComputeRHS, src/dft_Schur_Epetra_Operator.cpp:121-133).
 __global__ void k_rhs_local(const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ chan,
-                            double *__restrict__ ymf)
+                            double *__restrict__ ymf, const double *__restrict__ coef)
 {
   const long N = c_g.N;
   const int nd = c_g.ndim;
@@ -911,17 +956,17 @@ __global__ void k_rhs_local(const double *__restrict__ x, const double *__restri
     }
     y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
     for (int d = 0; d < nd; d++) { y[4 + d] = ysv[4 + nd + d]; y[4 + nd + d] = ysv[4 + d]; }
-    load_n(x, i, n);
-    fmt_hess_apply(n, y, z);
+    (void)n;
+    hess_apply_node(x, coef, i, y, z);
     write_tr_channels(z, chan, i);
     if (c_g.attraction)
       for (int ic = 0; ic < c_g.ncomp; ic++) ymf[(long)ic * N + i] = -b[(long)(c_g.first_mf + ic) * N + i];
   }
 }
 
-void launch_rhs_local(const double *x, const double *b, double *chan, double *ymf, cudaStream_t s)
+void launch_rhs_local(const double *x, const double *b, double *chan, double *ymf, const double *coef, cudaStream_t s)
 {
-  k_rhs_local<<<1184, kThreads, 0, s>>>(x, b, chan, ymf);
+  k_rhs_local<<<1184, kThreads, 0, s>>>(x, b, chan, ymf, coef);
 }
 
 __global__ void k_rhs_combine(const double *__restrict__ vext, const signed char *__restrict__ zero,

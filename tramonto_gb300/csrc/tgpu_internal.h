@@ -224,18 +224,24 @@ __host__ __device__ inline void fmt_dphi_at(const double *n, double *dphi, int n
 // src/dft_physics_FMT2.c:182-183) and FMT4's n2-row V2 entries (coefficient
 // -6 (fac^2 - 4 V2.V2 fac / n2) f for the Hessian's -6 fac (1 + 3 V2.V2/n2^2) f,
 // src/dft_physics_FMT4.c:179, fac = 1 - V2.V2/n2^2).
-__host__ __device__ inline void fmt_hess_apply_at(const double *n, const double *y, double *z, int nd, int fn,
-                                                  bool exact, bool transpose)
+// The state-dependent scalars of that matrix at one node (all zero where the White-Bear cut applies, which
+// makes z = 0); split from the product so that the products of one Newton state can reuse them.
+struct HessCoef {
+  double a, a2, h13, h22, h23, h33, ff, gvf1, g2vr_f, g2vc_f, gvv, gvv_out;
+};
+constexpr int kHessCoef = 12;
+
+__host__ __device__ inline HessCoef fmt_hess_coef_at(const double *n, int nd, int fn, bool exact)
 {
+  HessCoef c;
   if (fmt_white_bear(fn) && !(n[3] > 1.e-10)) {
-    for (int k = 0; k < 4 + 2 * nd; k++) z[k] = 0.0;
-    return;
+    c.a = c.a2 = c.h13 = c.h22 = c.h23 = c.h33 = c.ff = c.gvf1 = c.g2vr_f = c.g2vc_f = c.gvv = c.gvv_out = 0.0;
+    return c;
   }
-  double Q = 0.0, Pd = 0.0, Vy = 0.0;
+  double Q = 0.0, Pd = 0.0;
   for (int d = 0; d < nd; d++) {
     Q += n[4 + nd + d] * n[4 + nd + d];
     Pd += n[4 + d] * n[4 + nd + d];
-    Vy += n[4 + nd + d] * y[4 + nd + d];
   }
   const double a = 1.0 / (1.0 - n[3]), a2 = a * a, a3 = a2 * a;
   const FmtG g = fmt_g(n[2], Q, fn);
@@ -252,28 +258,49 @@ __host__ __device__ inline void fmt_hess_apply_at(const double *n, const double 
       g2v_row = -6.0 * (fac * fac - 4.0 * Q * fac / n[2]);
     }
   }
-  if (transpose) {
-    const double t = g2v_row;
-    g2v_row = g2v_col;
-    g2v_col = t;
-  }
-  const double h22 = g.g22 * f.f, h23 = n[1] * a2 + g.g2 * f.f1;
-  const double h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + g.g * f.f2;
-  const double h13 = n[2] * a2;
+  c.a = a;
+  c.a2 = a2;
+  c.h13 = n[2] * a2;
+  c.h22 = g.g22 * f.f;
+  c.h23 = n[1] * a2 + g.g2 * f.f1;
+  c.h33 = n[0] * a2 + 2.0 * (n[1] * n[2] - Pd) * a3 + g.g * f.f2;
+  c.ff = f.f;
+  c.gvf1 = g.gv * f.f1;
+  c.g2vr_f = g2v_row * f.f;
+  c.g2vc_f = g2v_col * f.f;
+  c.gvv = gvv;
+  c.gvv_out = gvv_out;
+  return c;
+}
+
+// z = M y from the node's scalars and its vector densities (n ordering); transpose swaps the n2-V2 entries
+__host__ __device__ inline void fmt_hess_apply_coef(const HessCoef &c, const double *n, const double *y, double *z,
+                                                    int nd, bool transpose)
+{
+  const double g2v_row = transpose ? c.g2vc_f : c.g2vr_f, g2v_col = transpose ? c.g2vr_f : c.g2vc_f;
+  double Vy = 0.0;
+  for (int d = 0; d < nd; d++) Vy += n[4 + nd + d] * y[4 + nd + d];
+  const double a = c.a, a2 = c.a2;
   double s2 = 0.0, s3 = 0.0;
   for (int d = 0; d < nd; d++) {
     const double V1 = n[4 + d], V2 = n[4 + nd + d];
     const double yV1 = y[4 + d], yV2 = y[4 + nd + d];
-    const double h3v2 = -V1 * a2 + g.gv * f.f1 * V2;    // M[n3][V2d] = M[V2d][n3]
-    s2 += g2v_row * f.f * V2 * yV2;
+    const double h3v2 = -V1 * a2 + c.gvf1 * V2;    // M[n3][V2d] = M[V2d][n3]
+    s2 += g2v_row * V2 * yV2;
     s3 += -V2 * a2 * yV1 + h3v2 * yV2;
     z[4 + d] = -V2 * a2 * y[3] - a * yV2;
-    z[4 + nd + d] = g2v_col * f.f * V2 * y[2] + h3v2 * y[3] - a * yV1 + f.f * (gvv * yV2 + gvv_out * V2 * Vy);
+    z[4 + nd + d] = g2v_col * V2 * y[2] + h3v2 * y[3] - a * yV1 + c.ff * (c.gvv * yV2 + c.gvv_out * V2 * Vy);
   }
   z[0] = a * y[3];
-  z[1] = a * y[2] + h13 * y[3];
-  z[2] = a * y[1] + h22 * y[2] + h23 * y[3] + s2;
-  z[3] = a * y[0] + h13 * y[1] + h23 * y[2] + h33 * y[3] + s3;
+  z[1] = a * y[2] + c.h13 * y[3];
+  z[2] = a * y[1] + c.h22 * y[2] + c.h23 * y[3] + s2;
+  z[3] = a * y[0] + c.h13 * y[1] + c.h23 * y[2] + c.h33 * y[3] + s3;
+}
+
+__host__ __device__ inline void fmt_hess_apply_at(const double *n, const double *y, double *z, int nd, int fn,
+                                                  bool exact, bool transpose)
+{
+  fmt_hess_apply_coef(fmt_hess_coef_at(n, nd, fn, exact), n, y, z, nd, transpose);
 }
 
 // Tensor-core form of a large 3-D single-channel stencil sum (wca_tc.cu): tiles of
@@ -429,8 +456,11 @@ constexpr int kSlabTileX = 128, kSlabTileY = 16;
 void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
                      const double *tr, double *R, cudaStream_t s);
-void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, cudaStream_t s);
-void launch_jv_local(const double *x, const double *v, double *chan, cudaStream_t s);
+// coef: the state's Hessian scalars ([kHessCoef][N], launch_hess_coef) or null to evaluate them in place
+void launch_hess_coef(const double *x, double *coef, cudaStream_t s);
+void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
+                        cudaStream_t s);
+void launch_jv_local(const double *x, const double *v, double *chan, const double *coef, cudaStream_t s);
 void launch_schur_combine(const double *x, const double *vext, const signed char *zero, const double *v2,
                           const double *tr, const double *ymf, double *y2, cudaStream_t s);
 void launch_jv_combine(const double *x, const double *vext, const signed char *zero, const double *v,

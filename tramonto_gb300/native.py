@@ -442,9 +442,16 @@ class Solver:
         return it.value, rn.value
 
     def newton_solve(self, x0, resid_tol=1e-8, max_iter=50, lin_tol=1e-8, lin_max_iter=300, update_floor=0.1,
-                     allow_noconv=False):
-        """Newton to ||R||_2 <= resid_tol (host arrays); returns (x, iterations, ||R||_2, GMRES iterations)."""
-        x = np.array(x0, np.float64, copy=True, order="C")
+                     allow_noconv=False, inplace=False):
+        """Newton to ||R||_2 <= resid_tol (host arrays); returns (x, iterations, ||R||_2, GMRES iterations).
+        inplace=True solves in x0 itself (a C-contiguous float64 array, e.g. a view of pinned host memory)."""
+        if inplace:
+            if not (isinstance(x0, np.ndarray) and x0.dtype == np.float64 and x0.flags.c_contiguous
+                    and x0.flags.writeable and x0.size == self.p.nunk * self.p.nnodes):
+                raise ValueError("inplace needs a writable C-contiguous float64 array of the state's size")
+            x = x0
+        else:
+            x = np.array(x0, np.float64, copy=True, order="C")
         it, rn, li = C.c_int(0), C.c_double(0.0), C.c_int(0)
         st = self.lib.tgpu_newton_solve(self.h, _ptr(x), resid_tol, max_iter, lin_tol, lin_max_iter, update_floor,
                                         C.byref(it), C.byref(rn), C.byref(li))
