@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = ("Newton iterations/s of a mixed-precision solve to ||R||_2 <= 1e-8, 128^3 FMT1+WCA "
-          "(tensor-core / FP32 stencil sums in the Schur products, FP64 residual)")
+          "(FP32-class stencil sums in the Schur products, FP64 residual)")
 UNIT = "Newton iter/s"
 WORKLOADS = {
     "config2": "config2: 3-D FMT1+WCA, 128^3, dx=0.1, rho_b=0.6, rough 12-3 LJ wall, periodic y,z",
@@ -481,8 +481,12 @@ def main():
                        "fft": "f64 residual near the solution (3-D sums as f64 FFT convolutions, rechecked by the "
                               "direct f64 sums)",
                        "fp64": "f64 residual near the solution"}[args.accurate_fill] +
-                      ("; Schur products: split-f16 x3 tensor-core attraction sums, f32 other stencil sums"
-                       if args.products == "fp16tc" else "; f32 stencil sums in the Schur products")),
+                      ("; Schur products: attraction sums as f32 FFT convolutions or split-f16 x3 tensor-core sums, "
+                       "whichever the handle timed faster (roofline.ms_per_launch against "
+                       "roofline.tensor_core_kernel), f32 other stencil sums"
+                       if args.products == "fp16tc" else
+                       "; Schur products: attraction sums as f32 FFT convolutions or f32 slab sums, whichever is "
+                       "faster, f32 other stencil sums")),
             "data": "synthetic",
             "config": {"workload": WORKLOADS[args.workload],
                        "step": (f"the continuation {ladder}, each rung solved to ||R||_2 <= {args.resid_tol:g}" if ladder
