@@ -178,8 +178,11 @@ struct Ctx : tgpu_ctx {
   bool fft_plan_ok = false;
   // FP32 FFT sums of the long stencils in FP32 arithmetic: chosen per context by timing against the
   // tensor-core sum (products) and the FP32 slab sum (FP32 fills): 0 undecided, 1 FFT, -1 direct
-  float2 *d_fbox32[2] = {nullptr, nullptr};
+  float2 *d_fbox32[3] = {nullptr, nullptr, nullptr};
   int fft32_tc = 0, fft32_slab = 0;
+  long fft32_gen = -1;
+  int fft32_ch = -1;
+  double *d_dscr = nullptr;      // [4 + 2 ndim][N] outputs of the timing runs that make the choices
   bool spec32_built = false;
   // the per-node FMT Hessian scalars of the current state (products of one Newton state share them)
   double *d_hcoef = nullptr;
@@ -349,16 +352,22 @@ bool prepare_spec32(Ctx *c)
   if (!c->fft_plan_ok) return false;
   const long NF = c->fft.NF;
   double2 *tmp = dalloc<double2>((size_t)NF);
-  for (auto &st : c->sten[TGPU_STEN_UATT]) {
-    if (st.L == 0 || !st.spec_fwd32.empty()) continue;
-    for (int q = 0; q < st.nout_fwd; q++) {
-      tgpu::launch_fft_kernel_box(st.d_off, st.d_coef_fwd, st.L, st.nout_fwd, q, tmp, c->fft, c->stream);
-      tgpu::fft3d(tmp, c->fft, c->dg.ndim, false, c->stream);
-      float2 *k = dalloc<float2>((size_t)NF);
-      tgpu::launch_to_float2(tmp, k, NF, c->stream);
-      st.spec_fwd32.push_back(k);
+  for (int t = 0; t < 3; t++)
+    for (auto &st : c->sten[t]) {
+      if (st.L == 0 || !st.spec_fwd32.empty()) continue;
+      for (int side = 0; side < 2; side++) {
+        const double *coef = side == 0 ? st.d_coef_fwd : st.d_coef_tr;
+        const int nq = side == 0 ? st.nout_fwd : st.nin_tr;
+        if (!coef) continue;
+        for (int q = 0; q < nq; q++) {
+          tgpu::launch_fft_kernel_box(st.d_off, coef, st.L, nq, q, tmp, c->fft, c->stream);
+          tgpu::fft3d(tmp, c->fft, c->dg.ndim, false, c->stream);
+          float2 *k = dalloc<float2>((size_t)NF);
+          tgpu::launch_to_float2(tmp, k, NF, c->stream);
+          (side == 0 ? st.spec_fwd32 : st.spec_tr32).push_back(k);
+        }
+      }
     }
-  }
   ck(cudaStreamSynchronize(c->stream), "sync");
   dfree(tmp);
   for (auto &b : c->d_fbox32)
@@ -367,21 +376,56 @@ bool prepare_spec32(Ctx *c)
   return true;
 }
 
-void fft_conv32(Ctx *c, int ch0, const DevStencil &st, double *const *outs, int nout)
+// spectrum of padded FP32 channel ch in FP32 box 0 (kept while the padded channels stay the same)
+const float2 *fft_channel32(Ctx *c, int ch)
+{
+  if (c->fft32_gen == c->pad_gen && c->fft32_ch == ch) return c->d_fbox32[0];
+  const tgpu::DevGeom &dg = c->dg;
+  const int P[3] = {dg.P[0], dg.P[1], dg.P[2]};
+  tgpu::launch_fft_load(c->d_pad32 + (long)ch * dg.NP, P, c->d_fbox32[0], c->fft, c->stream);
+  tgpu::fft3d(c->d_fbox32[0], c->fft, dg.ndim, false, c->stream);
+  c->stats.kernel_launches += 1 + dg.ndim;
+  c->fft32_gen = c->pad_gen;
+  c->fft32_ch = ch;
+  return c->d_fbox32[0];
+}
+
+void fft_conv32(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
 {
   const tgpu::DevGeom &dg = c->dg;
   const long NF = c->fft.NF;
-  const int P[3] = {dg.P[0], dg.P[1], dg.P[2]}, h[3] = {dg.h[0], dg.h[1], dg.h[2]};
-  const int nx[3] = {dg.nx[0], dg.nx[1], dg.nx[2]};
-  tgpu::launch_fft_load(c->d_pad32 + (long)ch0 * dg.NP, P, c->d_fbox32[0], c->fft, c->stream);
-  tgpu::fft3d(c->d_fbox32[0], c->fft, dg.ndim, false, c->stream);
-  for (int q = 0; q < nout; q++) {
-    tgpu::launch_spec_mul(c->d_fbox32[0], st.spec_fwd32[q], c->d_fbox32[1], NF, false, c->stream);
-    tgpu::fft3d(c->d_fbox32[1], c->fft, dg.ndim, true, c->stream);
-    tgpu::launch_fft_extract(c->d_fbox32[1], c->fft, h, nx, 1.0 / (double)NF, outs[q], c->stream);
+  const int h[3] = {dg.h[0], dg.h[1], dg.h[2]}, nx[3] = {dg.nx[0], dg.nx[1], dg.nx[2]};
+  const double scale = 1.0 / (double)NF;
+  if (!tr) {
+    const float2 *F = fft_channel32(c, ch0);
+    for (int q = 0; q < nout; q++) {
+      tgpu::launch_spec_mul(F, st.spec_fwd32[q], c->d_fbox32[1], NF, false, c->stream);
+      tgpu::fft3d(c->d_fbox32[1], c->fft, dg.ndim, true, c->stream);
+      tgpu::launch_fft_extract(c->d_fbox32[1], c->fft, h, nx, scale, outs[q], c->stream);
+      c->stats.kernel_launches += 2 + dg.ndim;
+    }
+  } else {
+    for (int k = 0; k < nin; k++) {
+      const float2 *F = fft_channel32(c, ch0 + k);
+      tgpu::launch_spec_mul(F, st.spec_tr32[k], c->d_fbox32[2], NF, k > 0, c->stream);
+      c->stats.kernel_launches++;
+    }
+    tgpu::fft3d(c->d_fbox32[2], c->fft, dg.ndim, true, c->stream);
+    tgpu::launch_fft_extract(c->d_fbox32[2], c->fft, h, nx, scale, outs[0], c->stream);
+    c->stats.kernel_launches += 1 + dg.ndim;
   }
-  c->stats.kernel_launches += 1 + dg.ndim + nout * (2 + dg.ndim);
   c->stats.conv_launches++;
+}
+
+// FP32 FFT for this sum: the attraction stencil by its context's choice (tensor-core products or FP32 slab
+// sums), the short stencils by their own (decide_fft32_sten)
+bool use_fft32(const Ctx *c, const DevStencil &st, bool tr, int nin, int nout)
+{
+  if (tr) return (int)st.spec_tr32.size() == nin && nout == 1 && st.fft32_tr == 1;
+  if ((int)st.spec_fwd32.size() != nout || nin != 1) return false;
+  if (&st >= c->sten[TGPU_STEN_UATT].data() && &st < c->sten[TGPU_STEN_UATT].data() + c->sten[TGPU_STEN_UATT].size())
+    return c->tc_on ? c->fft32_tc == 1 : c->fft32_slab == 1;
+  return st.fft32_fwd == 1;
 }
 
 void fft_conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
@@ -419,9 +463,8 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
     fft_conv(c, ch0, nin, st, tr, outs, nout);
     return;
   }
-  if (f32 && !tr && nin == 1 && (int)st.spec_fwd32.size() == nout &&
-      (c->tc_on ? c->fft32_tc == 1 : c->fft32_slab == 1)) {
-    fft_conv32(c, ch0, st, outs, nout);
+  if (f32 && c->spec32_built && use_fft32(c, st, tr, nin, nout)) {
+    fft_conv32(c, ch0, nin, st, tr, outs, nout);
     return;
   }
   if (f32 && c->tc_on && !tr && nin == 1 && nout == 1 && st.tc.nplanes > 0) {
@@ -535,6 +578,39 @@ void decide_fft32(Ctx *c)
   flag = t_fft < t_direct ? 1 : -1;
 }
 
+// The same choice for one short stencil (theta, delta) and direction: its FP32 slab / point sum against the
+// FP32 FFT, timed once on the padded channels ch0.. into d_dscr.  The FFT runs after the first reuse the
+// field's transform when it is the one the forward sums share (the channel's spectrum stays cached).
+void decide_fft32_sten(Ctx *c, DevStencil &st, bool tr, int ch0, int nin, int nout)
+{
+  int &flag = tr ? st.fft32_tr : st.fft32_fwd;
+  if (flag != 0) return;
+  flag = -1;
+  if (!prepare_spec32(c)) return;
+  if (tr ? (int)st.spec_tr32.size() != nin : (int)st.spec_fwd32.size() != nout) return;
+  const long N = c->dg.N;
+  if (!c->d_dscr) c->d_dscr = dalloc<double>((size_t)tgpu::kMaxRb * N);
+  double *o[tgpu::kMaxRb];
+  for (int q = 0; q < nout; q++) o[q] = c->d_dscr + (long)q * N;
+  cudaEvent_t ev[4];
+  for (auto &e : ev) ck(cudaEventCreate(&e), "event");
+  conv(c, ch0, nin, st, tr, o, nout, true);   // warm-up of the direct sum
+  ck(cudaEventRecord(ev[0], c->stream), "event");
+  for (int r = 0; r < 2; r++) conv(c, ch0, nin, st, tr, o, nout, true);
+  ck(cudaEventRecord(ev[1], c->stream), "event");
+  flag = 1;
+  conv(c, ch0, nin, st, tr, o, nout, true);   // warm-up of the FFT sum
+  ck(cudaEventRecord(ev[2], c->stream), "event");
+  for (int r = 0; r < 2; r++) conv(c, ch0, nin, st, tr, o, nout, true);
+  ck(cudaEventRecord(ev[3], c->stream), "event");
+  ck(cudaEventSynchronize(ev[3]), "event");
+  float t_direct = 0.f, t_fft = 0.f;
+  ck(cudaEventElapsedTime(&t_direct, ev[0], ev[1]), "event");
+  ck(cudaEventElapsedTime(&t_fft, ev[2], ev[3]), "event");
+  for (auto &e : ev) cudaEventDestroy(e);
+  flag = t_fft < t_direct ? 1 : -1;
+}
+
 // Weighted-density (and mean-field) sums of the padded density channels with one zone's stencils
 // into out (rows as d_conv)
 void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, bool f32)
@@ -573,6 +649,11 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bo
   if (zero_first) ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * nrows * N, c->stream), "memset");
   pad(c, field, pp, f32);
   if (f32 && g.attraction && g.ndim == 3) decide_fft32(c);
+  if (f32 && g.ndim == 3)
+    for (int jc = 0; jc < g.ncomp; jc++) {
+      decide_fft32_sten(c, c->sten[TGPU_STEN_THETA][jc], false, jc, 1, 1);
+      decide_fft32_sten(c, c->sten[TGPU_STEN_DELTA][jc], false, jc, 1, c->sten[TGPU_STEN_DELTA][jc].nout_fwd);
+    }
   forward_convs(c, c->sten, c->d_conv, f32);
   // nodes of the coarser quadrature zones keep their own zone's sums (zero_first holds with zones)
   for (int z = 1; z < c->nzone; z++) {
@@ -610,6 +691,12 @@ void transpose_pass(Ctx *c, const PadParams &pp, bool f32, const double *chan = 
   const long N = g.N;
   if (zero_first) ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
   pad(c, chan ? chan : c->d_chan, pp, f32);
+  if (f32 && g.ndim == 3)
+    for (int ic = 0; ic < g.ncomp; ic++) {
+      const int base = ic * (g.ndim + 2);
+      decide_fft32_sten(c, c->sten[TGPU_STEN_DELTA][ic], true, base, 1 + g.ndim, 1);
+      decide_fft32_sten(c, c->sten[TGPU_STEN_THETA][ic], true, base + g.ndim + 1, 1, 1);
+    }
   transpose_convs(c, c->sten, c->d_tr, f32);
   for (int z = 1; z < c->nzone; z++) {
     ck(cudaMemsetAsync(c->d_zbuf, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
@@ -2084,9 +2171,11 @@ int tgpu_destroy(tgpu_handle h)
         tgpu::tc_free_tables(st.tc);
         for (auto *V : {&st.spec_fwd, &st.spec_tr})
           for (auto &k : *V) dfree(k);
-        for (auto &k : st.spec_fwd32) dfree(k);
+        for (auto *V : {&st.spec_fwd32, &st.spec_tr32})
+          for (auto &k : *V) dfree(k);
       }
     for (auto &b : c->d_fbox) dfree(b);
+    dfree(c->d_dscr);
     for (auto &b : c->d_fbox32) dfree(b);
     tgpu::fft_free_plan(c->fft);
     for (int z = 1; z < tgpu::kMaxZone; z++)
@@ -2341,10 +2430,14 @@ int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
           }
         }
       for (auto &b : c->d_fbox) dfree(b);
-      for (auto &st : c->sten[TGPU_STEN_UATT]) {
-        for (auto &k : st.spec_fwd32) dfree(k);
-        st.spec_fwd32.clear();
-      }
+      for (int t = 0; t < 3; t++)
+        for (auto &st : c->sten[t]) {
+          for (auto *V : {&st.spec_fwd32, &st.spec_tr32}) {
+            for (auto &k : *V) dfree(k);
+            V->clear();
+          }
+          st.fft32_fwd = st.fft32_tr = 0;
+        }
       for (auto &b : c->d_fbox32) dfree(b);
       tgpu::fft_free_plan(c->fft);
       c->fft_state = 0;
@@ -2352,6 +2445,7 @@ int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
       c->fft_plan_ok = false;
       c->spec32_built = false;
       c->fft32_tc = c->fft32_slab = 0;
+      c->fft32_gen = -1;
     }
     return TGPU_OK;
   });

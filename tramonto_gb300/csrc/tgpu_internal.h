@@ -374,7 +374,8 @@ struct DevStencil {
   // FFT spectra of the correlation kernels (FP64 fills by FFT): per forward output, per transpose input;
   // FP32 copies of the forward ones for the FP32 sums (products, FP32 fills)
   std::vector<double2 *> spec_fwd, spec_tr;
-  std::vector<float2 *> spec_fwd32;
+  std::vector<float2 *> spec_fwd32, spec_tr32;
+  int fft32_fwd = 0, fft32_tr = 0;      // short stencils: FP32 FFT (1) or slab (-1) sums, 0 undecided
 };
 
 }  // namespace tgpu
