@@ -2740,7 +2740,7 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
     conv(c, jc, 1, st, false, out, 1, f32);   // warm-up
     ck(cudaEventRecord(c->ev0, c->stream), "event");
     for (int r = 0; r < reps; r++) {
-      c->fft_gen = -1;   // each FFT sum transforms its field afresh
+      c->fft_gen = c->fft32_gen = -1;   // each FFT sum transforms its field afresh
       conv(c, jc, 1, st, false, out, 1, f32);
     }
     ck(cudaEventRecord(c->ev1, c->stream), "event");
