@@ -5,7 +5,7 @@
 // every F_d >= P_d (the padded extent: i + h + o stays inside [0, P)).  So one forward transform of the
 // padded channel, a pointwise product with the kernel's spectrum (computed once per stencil coefficient)
 // and one inverse transform give a sum whose cost does not depend on the stencil's length: for the
-// 71 831-point attraction stencil at 128^3 that is ~2 transforms of 192^3 against 1.5e11 terms.
+// 71 831-point attraction stencil at 128^3 that is ~2 transforms of 180^3 against 1.5e11 terms.
 // Rounding: FP64 FFTs with tabulated twiddles keep the error near eps log2(NF) of the sum's scale.
 //
 // Each axis is a batch of 1-D transforms.  A CTA loads kFftLines lines and the twiddle table into shared
