@@ -1,19 +1,22 @@
 """Benchmark of the nonlocal-density Newton path on one GB300.
 
-Workload (BASELINE configuration 2): 3-D FMT1 + WCA Lennard-Jones fluid
+Workload (configuration 2): 3-D FMT1 + WCA Lennard-Jones fluid
 (eps=1, r_c=2.5 sigma, kT*=1.2), sigma=1, 128^3 nodes at dx=0.1 sigma,
 rho_b=0.6, periodic in y and z, a rough 12-3 LJ wall (eps_w=1, 16x16 patches
 of U(-0.5,0.5) sigma heights, seeded) on the low-x side, bulk on the high-x side.
 
 A step is one Newton solve from the initial state (rho_b exp(-V) with its own
 weighted densities) to ||R||_2 <= 1e-8: residual fills (FP32 stencil sums while
-||R||_2 > 0.1, FP64 after), Schur-complement GMRES whose products sum the 3-D
-attraction stencil on the tensor cores (tcgen05, split FP16 x3, FP32
-accumulation) and the other stencils in FP32 (inexact Newton,
-Eisenstat-Walker tolerances), and the damped update.  The value is Newton iterations per second over the K timed solves; the
-plain FP64 path (FP64 residual and products) is timed per iteration beside it.  The inputs (12 unknowns x 128^3
-doubles = 201 MB, plus the 200+ MB of padded fields) exceed the 129 MB L2, so
-no explicit flush is done between steps.
+||R||_2 > 0.1, FP64-accurate after: the attraction sum as an FP64 FFT
+convolution, the short stencils as float-float sums), Schur-complement GMRES
+whose products take the 3-D attraction sum as an FP32 FFT convolution or on
+the tensor cores (tcgen05, split FP16 x3), whichever the handle timed faster,
+and the other stencils in FP32 (inexact Newton, Eisenstat-Walker tolerances),
+and the damped update.  The value is Newton iterations per second over the K
+timed solves; the plain FP64 path (FP64 residual and products) is timed per
+iteration beside it.  The inputs (12 unknowns x 128^3 doubles = 201 MB, plus
+the 200+ MB of padded fields) exceed the 129 MB L2, so no explicit flush is
+done between steps.
 
 `--impl reference` times the reference's CPU algorithm (the C oracle under
 oracle/, a restatement of the reference's fill) on the host cores on a bounded
