@@ -171,6 +171,9 @@ int tgpu_set_fill_arithmetic(tgpu_handle h, int arith, double tau, double switch
 /* Stencils of at least min_points points take the FFT in TGPU_FILL_FFT; min_points < 0 (default): a cost
  * model (direct float-float sum against the transforms) chooses. */
 int tgpu_set_fft_threshold(tgpu_handle h, int min_points);
+/* FP32 stencil sums (products, FP32 fills) as FP32 FFT convolutions: -1 (default) each sum's first use times
+ * the FFT against its direct kernel and keeps the faster; 0 never; 1 always (3-D problems). */
+int tgpu_set_fft32_policy(tgpu_handle h, int policy);
 /* Second derivatives of the FMT energy density in J, J^T and Schur products (and so in Newton):
  *   TGPU_JAC_REFERENCE  the reference's tables, entry for entry (default): d2phi_drb2_{delta,theta}_rb_FMT*
  *                       (src/dft_physics_FMT{1,2,3,4}.c, via FMT2ndDeriv*_switch, src/dft_switch_FMT.c:122-152)

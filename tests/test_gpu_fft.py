@@ -8,7 +8,11 @@ FFT convolutions, the short ones (theta, delta) as float-float sums.
   it equals the direct FP64 fill to 5e-12 at the initial state (the FFT's rounding, ~eps log2 of the box
   times the sums' scale, against the direct sums' own ~1e-12);
 - a TGPU_FILL_MIXED_FFT Newton solve reaches ||R||_2 <= 1e-8, its residual re-evaluated by the direct
-  FP64 fill is below 1e-8 too, and its density equals the FP64 solve's to 1e-9.
+  FP64 fill is below 1e-8 too, and its density equals the FP64 solve's to 1e-9;
+- with every FP32 sum forced onto FP32 FFTs (tgpu_set_fft32_policy 1) the Schur product equals the FP64 one to
+  1e-5, its nonlocal part (S v2 less the local v2 / rho) too, and J v to 1e-5 (relative to their max norms), an FP32 fill equals the FP64 fill to 1e-4, and the mixed
+  solve still reaches the FP64 solve's density to 1e-9; with the direct kernels forced (policy 0) the products
+  are the slab / tensor-core ones.
 """
 import numpy as np
 import pytest
@@ -64,5 +68,42 @@ def test_mixed_fft_newton_solve():
     r64 = np.linalg.norm(s.fill(xf, mode=1))
     print("mixed-FFT solve:", it, "iterations, ||R||_2", rn, "re-evaluated in FP64", r64)
     assert r64 <= 1e-8
+    assert np.abs(xf[p.first_rho] - x64[p.first_rho]).max() <= 1e-9
+    s.close()
+
+
+@pytest.mark.parametrize("policy", [1, 0])
+def test_fp32_fft_products(policy):
+    from tramonto_gb300 import native, setup
+    from goldens import rel_err
+    p, _ = setup.config2(n=40)
+    s = native.Solver(p)
+    x0 = setup.initial_state(s, p)
+    x64, _, _, _ = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-10)
+    s.fill(x64)
+    rng = np.random.default_rng(4)
+    v2 = rng.standard_normal((p.ncomp, p.nnodes))
+    v = rng.standard_normal((p.nunk, p.nnodes))
+    S64, J64 = s.schur(v2), s.jv(v)
+    s.set_precision(native.FP16TC)
+    s.set_fft32_policy(policy)
+    S32, J32 = s.schur(v2), s.jv(v)
+    # the nonlocal part of S v2 (the local A22 v2 = v2 / rho on live rows dominates the max norm near the wall)
+    rho = x64[p.first_rho:p.first_rho + p.ncomp]
+    live = (np.asarray(p.zero_density).reshape(rho.shape) == 0) & (np.asarray(p.vext).reshape(rho.shape) < p.vext_max)
+    local = np.where(live, v2 / np.where(live, rho, 1.0), v2)
+    nl64, nl32 = S64 - local, S32 - local
+    print("policy", policy, "Schur rel", rel_err(S32, S64), "nonlocal part rel", rel_err(nl32, nl64),
+          "Jv rel", rel_err(J32, J64))
+    assert rel_err(S32, S64) <= 1e-5 and rel_err(J32, J64) <= 1e-5
+    assert rel_err(nl32, nl64) <= 1e-5
+    s.set_fill_arithmetic(native.FILL_FP32)
+    R32 = s.fill(x64, mode=1)
+    s.set_fill_arithmetic(native.FILL_FP64)
+    R64 = s.fill(x64, mode=1)
+    assert np.abs(R32 - R64).max() <= 1e-4 * max(1.0, np.abs(R64).max())
+    s.set_fill_arithmetic(native.FILL_MIXED_FFT, switch_norm=0.1)
+    xf, it, rn, _ = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-6)
+    assert rn <= 1e-8
     assert np.abs(xf[p.first_rho] - x64[p.first_rho]).max() <= 1e-9
     s.close()

@@ -2415,6 +2415,24 @@ int tgpu_set_jacobian_form(tgpu_handle h, int form)
   });
 }
 
+int tgpu_set_fft32_policy(tgpu_handle h, int policy)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    if (policy < -1 || policy > 1) throw Error(TGPU_ERR_ARG, "policy");
+    int v = 0;
+    if (policy != -1) {
+      v = policy == 1 ? 1 : -1;
+      if (v == 1 && !prepare_spec32(c)) throw Error(TGPU_ERR_UNSUPPORTED, "FP32 FFT sums unavailable for this problem");
+    }
+    c->fft32_tc = c->fft32_slab = v;
+    for (int t = 0; t < 3; t++)
+      for (auto &st : c->sten[t]) st.fft32_fwd = st.fft32_tr = v;
+    return TGPU_OK;
+  });
+}
+
 int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
 {
   return guard([&] {

@@ -88,6 +88,7 @@ def load(build_if_missing: bool = False):
         "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_zones": [vp, C.c_int, vp, vp],
         "tgpu_set_fft_threshold": [vp, C.c_int],
+        "tgpu_set_fft32_policy": [vp, C.c_int],
         "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
@@ -340,6 +341,10 @@ class Solver:
     def set_fft_threshold(self, min_points: int):
         """Stencils of at least min_points points take the FFT in FILL_FFT; < 0: the cost model decides."""
         _check(self.lib.tgpu_set_fft_threshold(self.h, int(min_points)), self.lib)
+
+    def set_fft32_policy(self, policy: int):
+        """FP32 sums as FP32 FFT convolutions: -1 timed choice (default), 0 never, 1 always."""
+        _check(self.lib.tgpu_set_fft32_policy(self.h, int(policy)), self.lib)
 
     def set_stream(self, stream_handle: int):
         _check(self.lib.tgpu_set_stream(self.h, C.c_void_p(stream_handle)), self.lib)
