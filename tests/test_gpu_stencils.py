@@ -101,3 +101,11 @@ def test_attraction_stencils_of_other_pair_potentials(name, pp, ndim, h):
     else:
         assert np.array_equal(wh.view(np.uint64), wd.view(np.uint64))
         assert np.array_equal(hh.view(np.uint64), hd.view(np.uint64))
+
+
+@pytest.mark.parametrize("name", ["sten3d_dx010", "sten3d_dx008"])
+def test_device_builder_matches_reference_tables_of_the_3d_workloads(name):
+    """The GPU builder's tables of the 128^3 (dx 0.1) and 256^3 (dx 0.08) workloads against the reference's
+    calc_stencils at the same element sizes (tests/golden/make_stencil_golden.py)."""
+    from test_stencils_3d_cpu import CASES, compare, workload_tables
+    compare(name, workload_tables(CASES[name][0], device=True))
