@@ -13,14 +13,18 @@ whose products take the 3-D attraction sum as an FP32 FFT convolution or on
 the tensor cores (tcgen05, split FP16 x3), whichever the handle timed faster,
 and the other stencils in FP32 (inexact Newton, Eisenstat-Walker tolerances),
 and the damped update.  The value is Newton iterations per second over the K
-timed solves; the plain FP64 path (FP64 residual and products) is timed per
-iteration beside it.  The inputs (12 unknowns x 128^3 doubles = 201 MB, plus
+timed solves.  Beside it: the plain FP64 path (every sum FP64-accurate in fills
+and products, the long ones as FP64 FFT convolutions, same driver and target)
+timed over a whole solve, and continued to ||R||_2 <= 1e-10 as the reference
+solution for the mixed solution's maximum density error; and one iteration
+with direct FP64 sums.  The inputs (12 unknowns x 128^3 doubles = 201 MB, plus
 the 200+ MB of padded fields) exceed the 129 MB L2, so no explicit flush is
 done between steps.
 
-`--impl reference` times the reference's CPU algorithm (the C oracle under
-oracle/, a restatement of the reference's fill) on the host cores on a bounded
-sample of the same workload and prints the same metric.
+`--impl reference` times the reference's fill algorithm (the C oracle under
+oracle/, a restatement of the reference's fill, on the reference's own stencil
+tables and bulk constants) on the host cores on a bounded sample of the same
+workload and prints the same metric with its cost model.
 """
 from __future__ import annotations
 
@@ -65,13 +69,19 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=128, help="grid of the config2 workload")
     ap.add_argument("--workload", default="config2", choices=["config2", "config4", "config5"])
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=1,
+                    help="Newton iterations timed with direct FP64 stencil sums (0: skip)")
     ap.add_argument("--lin-tol", type=float, default=1e-6)
     ap.add_argument("--lin-maxit", type=int, default=200)
     ap.add_argument("--resid-tol", type=float, default=1e-8)
     ap.add_argument("--max-newton", type=int, default=40)
     ap.add_argument("--switch", type=float, default=0.1)
-    ap.add_argument("--cpu-sample-planes", type=int, default=2)
+    ap.add_argument("--cpu-sample-planes", type=int, default=0,
+                    help="z-planes of the CPU sample (0: 2 for the GPU arm's one-core baseline, a quarter of the host "
+                         "threads for the reference arm)")
+    ap.add_argument("--k-gmres", type=float, default=7.43,
+                    help="GMRES iterations per Newton iteration for the reference arm's cost model (the GPU arm "
+                         "prints its own as gmres_iters_per_newton_iter)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--light", action="store_true",
                     help="one repetition of each FP64 kernel-family timing (large workloads)")
@@ -130,7 +140,7 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_sten_tc launch at 128^3 (ncu, profiles/)
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_sten_tc launch at 128^3 (ncu, one launch)
 TC_TRAFFIC_BYTES = 47.724e6 + 0.538e6
 
 
@@ -202,34 +212,79 @@ def cpu_baseline(p, x, k_gmres, planes, threads=1):
             "t_fill_s": t_fill}
 
 
+def workload_config(args, ladder=None):
+    """The `config` dict of both arms' JSON lines (the same dict, built from the command line alone)."""
+    if args.workload == "config4":
+        grid, dx, rho_b = [256] * 3, 0.08, 0.7
+    else:
+        grid, dx, rho_b = [args.n] * 3, 0.1, 0.6
+    return {"workload": WORKLOADS[args.workload],
+            "step": (f"the continuation {ladder}, each rung solved to ||R||_2 <= {args.resid_tol:g}" if ladder
+                     else f"one Newton solve from the initial state to ||R||_2 <= {args.resid_tol:g}"),
+            "grid": grid, "dx": dx, "seed": 1234, "rho_b": rho_b, "continuation": ladder, "kT": 1.2, "rcut": 2.5,
+            "lin_tol_floor": args.lin_tol, "fp32_until_resid": args.switch, "inputs_exceed_l2": True,
+            "l2_flush": "none (working set > L2)"}
+
+
 def run_reference(args):
-    """Reference arm: the reference's CPU algorithm on the host cores."""
-    from tramonto_gb300 import setup
+    """Reference arm: the reference's fill algorithm (the C oracle, a restatement of it) on all host cores.
+
+    Nothing from the product package is imported: the problem comes from oracle/workload.py (the reference's own
+    stencil tables and bulk constants, the workload's seeded wall field).  Each step is one residual fill of a
+    sample of z-planes of the 128^3 grid at the state the GPU arm's solves start from (densities and their own
+    weighted densities and mean field); ms_per_step is its measured time.  The Newton-iteration rate is the
+    cost model of the reference's own CPU path: (1 + k) fills per Newton iteration (the assembled Jacobian of
+    the 128^3 problem holds ~1e11 entries, so its GMRES cannot run here), k = the GPU arm's GMRES iterations per
+    Newton iteration (--k-gmres), the full fill = the sample's time scaled by the node count."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    p, meta = make_problem(args)
-    # initial state on the host: densities rho_b exp(-V), weighted densities from the oracle's sums
+    if args.workload != "config2":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm times the 128^3 workload only"}))
+        return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import orc
+    import workload
+    p = workload.config2_problem(args.n)
     o = orc.Oracle(p)
-    x = np.zeros((p.nunk, p.nnodes))
-    rho = p.rho_b[0] * np.exp(-np.minimum(p.vext[0], 50.0))
-    rho[p.zero_density[0] != 0] = 0.0
-    x[0] = rho
     threads = os.cpu_count() or 1
-    k_gmres = 7.4    # GMRES iterations per Newton iteration of the GPU solve (bench.py default run)
-    steps = []
-    for _ in range(max(1, args.steps)):
-        cb = cpu_baseline(p, x, k_gmres, planes=max(threads, args.cpu_sample_planes), threads=threads)
-        steps.append(cb["value"])
-    v = float(np.median(steps))
+    planes = args.cpu_sample_planes if args.cpu_sample_planes > 0 else max(2, threads // 4)
+    t0 = time.perf_counter()
+    x = workload.initial_state(p, o, planes, threads)
+    t_state = time.perf_counter() - t0
+    ranges = workload.plane_ranges(p, range(planes), threads)
+    nodes = sum(e - b for b, e in ranges)
+
+    def step():
+        from concurrent.futures import ThreadPoolExecutor
+        t = time.perf_counter()
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda r: o.resid_rows(x, r[0], r[1]), ranges))
+        return time.perf_counter() - t
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(max(1, args.steps))]
+    t_sample = float(np.median(times))
+    t_fill = t_sample * p.nnodes / nodes
+    k = args.k_gmres
+    v = 1.0 / ((1.0 + k) * t_fill)
+    sample = (f"oracle residual fill of {planes} z-planes ({nodes} of {p.nnodes} nodes) on {threads} threads, "
+              f"median {t_sample:.2f} s per step; Newton iteration = (1 + k) full fills, k = {k:g}")
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+           "warmup": args.warmup, "ms_per_step": t_sample * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOADS[args.workload], "inputs_exceed_l2": True},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
-           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": workload_config(args),
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "model": {"step": "one residual fill of the sampled z-planes (ms_per_step is its measured time)",
+                     "sample_fraction": nodes / p.nnodes, "full_fill_s": t_fill,
+                     "newton_iteration": "(1 + k) full fills", "k": k,
+                     "k_source": "GMRES iterations per Newton iteration of the GPU arm's solve "
+                                 "(its gmres_iters_per_newton_iter), passed as --k-gmres",
+                     "state_setup_s": t_state,
+                     "inputs": "stencil tables and bulk constants from the reference's own set-up "
+                               "(tests/golden/sten3d_dx010.npz), seeded wall field"}}
     print(json.dumps(out))
 
 
@@ -334,19 +389,19 @@ def main():
 
     ladder = meta.get("ladder")
 
-    def solve():
+    def solve(xt=dx, resid_tol=None, lin_tol=None):
         """One step: a Newton solve from the initial state, or the continuation along the workload's ladder of
         bulk densities (each rung warm-started from the previous solution); totals over the rungs."""
-        dx.copy_(x0_dev)
+        xt.copy_(x0_dev)
+        kw = dict(resid_tol=resid_tol or args.resid_tol, max_iter=args.max_newton, lin_tol=lin_tol or args.lin_tol,
+                  lin_max_iter=args.lin_maxit, allow_noconv=True)
         if not ladder:
-            return s.newton_solve_device(dx, resid_tol=args.resid_tol, max_iter=args.max_newton,
-                                         lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+            return s.newton_solve_device(xt, **kw)
         it_t = li_t = 0
         rn = float("inf")
         for rb in ladder:
             s.set_bulk([rb])
-            it, rn, li = s.newton_solve_device(dx, resid_tol=args.resid_tol, max_iter=args.max_newton,
-                                               lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+            it, rn, li = s.newton_solve_device(xt, **kw)
             it_t += it
             li_t += li
         return it_t, rn, li_t
@@ -436,21 +491,43 @@ def main():
     L_att = len(p.stencils[(UATT, 0)][1])
     flops_att = 2.0 * p.nnodes * L_att
     mma_flops = tc_issued_flops(p)
-    # plain FP64 Newton iterations (FP64 residual and FP64 Schur products) from the initial state
+    # The plain FP64 path: every sum FP64-accurate in the fills and in the Schur products (the long 3-D sums as
+    # FP64 FFT convolutions, the short ones in float-float arithmetic), the same Newton driver and target, timed
+    # over a whole solve; then continued to ||R||_2 <= 1e-10 with tight linear solves as the FP64 solution the
+    # mixed solution's density is compared with.
+    s.set_precision(native.FP64_FFT)
+    s.set_fill_arithmetic(native.FILL_FFT)
+    x64 = torch.empty_like(dx)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    it64, rn64, li64 = solve(x64)
+    b.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = a.elapsed_time(b) / max(1, it64)
+    progress(f"plain FP64 solve: {it64} Newton iterations, {li64} GMRES, {fp64_ms:.1f} ms per iteration")
+    s.newton_solve_device(x64, resid_tol=1e-10, max_iter=args.max_newton, lin_tol=1e-10, lin_max_iter=args.lin_maxit,
+                          allow_noconv=True)
+    rho = slice(p.first_rho, p.first_rho + p.ncomp)
+    dens_err = float((x_mixed[rho] - x64[rho]).abs().max().item())
+    dens_max = float(x64[rho].abs().max().item())
+    progress(f"max |rho_mixed - rho_fp64| = {dens_err:.2e} (max rho {dens_max:.3f})")
+    del x64
+    # the same iteration with direct FP64 stencil sums (no FFT, no float-float) in fills and products
+    s.set_precision(native.FP64)
     s.set_fill_arithmetic(native.FILL_FP64)
-    fp64_ms = None
+    direct_ms = None
     if args.fp64_steps > 0:
-        dx64 = x0_dev.clone()
-        s.newton_device(dx64, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        dxd = x0_dev.clone()
+        s.newton_device(dxd, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
         torch.cuda.synchronize()
         a.record(stream)
         for _ in range(args.fp64_steps):
-            s.newton_device(dx64, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
+            s.newton_device(dxd, max_iter=1, lin_tol=args.lin_tol, lin_max_iter=args.lin_maxit, allow_noconv=True)
         b.record(stream)
         torch.cuda.synchronize()
-        fp64_ms = a.elapsed_time(b) / args.fp64_steps
-        del dx64
+        direct_ms = a.elapsed_time(b) / args.fp64_steps
+        del dxd
     # end to end through the C ABI with host buffers: copies of the state in and out inside the timed region
     mixed_mode()
     xh = torch.from_numpy(x0.copy()).pin_memory().numpy()   # the caller's state in pinned host memory
@@ -474,7 +551,7 @@ def main():
         cb = None
         if not args.no_cpu_baseline:
             k = max(1.0, lin_iters / max(1, iters))
-            cb = cpu_baseline(p, x_mixed.cpu().numpy(), k, planes=args.cpu_sample_planes, threads=1)
+            cb = cpu_baseline(p, x_mixed.cpu().numpy(), k, planes=args.cpu_sample_planes or 2, threads=1)
             cb.pop("t_fill_s", None)
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -491,14 +568,7 @@ def main():
                        "; Schur products: attraction sums as f32 FFT convolutions or f32 slab sums, whichever is "
                        "faster, f32 other stencil sums")),
             "data": "synthetic",
-            "config": {"workload": WORKLOADS[args.workload],
-                       "step": (f"the continuation {ladder}, each rung solved to ||R||_2 <= {args.resid_tol:g}" if ladder
-                                else f"one Newton solve from the initial state to ||R||_2 <= {args.resid_tol:g}"),
-                       "grid": meta["grid"], "dx": meta["dx"], "seed": meta["seed"],
-                       "rho_b": (ladder or [meta["rho_b"]])[-1], "continuation": ladder, "kT": 1.2, "rcut": 2.5,
-                       "lin_tol_floor": args.lin_tol,
-                       "fp32_until_resid": args.switch, "inputs_exceed_l2": True,
-                       "l2_flush": "none (working set > L2)"},
+            "config": workload_config(args, ladder),
             "newton_iters_per_step": iters / args.steps, "ms_per_newton_iter": ms_per_iter,
             "gmres_iters_per_newton_iter": lin_iters / max(1, iters), "final_resid_norm2": max(final_r),
             "final_resid_norm2_fp64_recheck": resid_fp64, "accurate_fill": args.accurate_fill,
@@ -530,7 +600,8 @@ def main():
                              "peak": bf16, "frac": ach_tf / bf16, "issued_mma_tflops": issued_tf,
                              "issued_mma_frac": issued_tf / bf16,
                              "traffic": (TC_TRAFFIC_BYTES if args.workload == "config2" and args.n == 128 else None),
-                             "traffic_source": "profiles/k_sten_tc_wca_128.md (ncu dram bytes, one launch)"},
+                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
+                                               "128^3"},
                          "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
                          "fp64_ms_per_launch": t_wca64},
             # the attraction sum of the accurate fills: an FP64 FFT convolution by default (--accurate-fill fft;
@@ -555,8 +626,18 @@ def main():
                              "schur_apply_fp32": t_apply32,
                              "schur_apply_fp16tc": t_apply_tc,
                              "schur_apply_fp64": t_apply64, "schur_applies_in_timed_steps": int(st["schur_applies"])},
-            "plain_fp64": {"ms_per_newton_iter": fp64_ms,
-                           "speedup_mixed_vs_fp64_per_iter": (fp64_ms / ms_per_iter) if fp64_ms else None},
+            "plain_fp64": {"ms_per_newton_iter": fp64_ms, "newton_iters": it64, "gmres_iters": li64,
+                           "final_resid_norm2": rn64,
+                           "arithmetic": "FP64-accurate fills and Schur products: long 3-D sums as FP64 FFT "
+                                         "convolutions, short ones in float-float arithmetic",
+                           "speedup_mixed_vs_fp64_per_iter": fp64_ms / ms_per_iter,
+                           "speedup_mixed_vs_fp64_per_solve": (fp64_ms * it64) / ms_per_solve},
+            "plain_fp64_direct_sums": {"ms_per_newton_iter": direct_ms,
+                                       "speedup_mixed_vs_direct_per_iter": (direct_ms / ms_per_iter)
+                                       if direct_ms else None},
+            "max_density_err_vs_fp64": dens_err,
+            "density_err_reference": "the FP64 path's solution continued to ||R||_2 <= 1e-10 (linear tolerance "
+                                     f"1e-10); max density {dens_max:.4f}",
             "setup_s": t_setup,
         }
         print(json.dumps(out))

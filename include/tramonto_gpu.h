@@ -65,7 +65,7 @@ enum { TGPU_JAC_REFERENCE = 0, TGPU_JAC_EXACT = 1 };
 /* stencil types (reference Stencil ids, src/dft_globals_const.h:152-161) */
 enum { TGPU_STEN_DELTA = 0, TGPU_STEN_THETA = 1, TGPU_STEN_UATT = 2 };
 /* arithmetic of the stencil convolutions */
-enum { TGPU_FP64 = 0, TGPU_FP32 = 1, TGPU_BF16X3 = 2, TGPU_FP16TC = 3 };
+enum { TGPU_FP64 = 0, TGPU_FP32 = 1, TGPU_BF16X3 = 2, TGPU_FP16TC = 3, TGPU_FP64_FFT = 4 };
 
 #define TGPU_MAXC 4
 
@@ -145,7 +145,9 @@ int tgpu_set_bulk_state(tgpu_handle h, const double *rho_b, const double *betamu
                         const double *dphi_bulk);
 /* Arithmetic of the Jacobian / Schur products: TGPU_FP64, TGPU_FP32 (stencil sums in FP32), or
  * TGPU_FP16TC (as TGPU_FP32, but the 3-D attraction sums on the tensor cores: FP16 inputs scaled by
- * powers of two, FP32 accumulation; TGPU_ERR_UNSUPPORTED when the problem has none).  The residual
+ * powers of two, FP32 accumulation; TGPU_ERR_UNSUPPORTED when the problem has none), or TGPU_FP64_FFT
+ * (FP64-accurate sums as TGPU_FILL_FFT forms them: in 3-D the long stencils as FP64 FFT convolutions, the
+ * short ones in float-float arithmetic; 1-D and 2-D problems take the direct FP64 sums).  The residual
  * fill's arithmetic is set by tgpu_set_fill_arithmetic. */
 int tgpu_set_precision(tgpu_handle h, int precision);
 /* Arithmetic of the residual fill:
@@ -359,7 +361,11 @@ double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double
  * until exit): the padded box (nx + 2*reach per dimension, multiplied) may
  * not exceed TGPU_NOALLOC_MAX_PADDED points, nor the stencil
  * TGPU_NOALLOC_MAX_STENCIL points, nor any padded extent 4096; larger inputs
- * return TGPU_ERR_ARG with a message in tgpu_noalloc_last_error().  The first
+ * return TGPU_ERR_ARG with a message in tgpu_noalloc_last_error().  A stencil
+ * that reaches past what the boundary rules can map (a periodic reach longer
+ * than the box, or a mirrored point beyond the far side when that side is
+ * periodic or reflecting) returns TGPU_ERR_UNSUPPORTED.  These checks run on
+ * the host before any device work.  The first
  * call on a device looks up the device addresses of those arrays (make that
  * first call before any stream capture).  Every call shares the arrays and
  * rewrites what it reads; calls whose work overlaps on the GPU race.  Returns

@@ -30,6 +30,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "libtramonto_ref.so")
+# the reference checkout, read in place: TRAMONTO_REFERENCE overrides the default location
 REFERENCE = os.environ.get("TRAMONTO_REFERENCE", "/root/reference")
 
 # stencil type ids of the reference (src/dft_globals_const.h:152-161)

@@ -21,8 +21,11 @@ The reference tree must be present (it is read in place, never copied).
 """
 from __future__ import annotations
 
+import atexit
 import os
+import shutil
 import sys
+import tempfile
 
 import numpy as np
 import scipy.sparse as sp
@@ -55,7 +58,8 @@ MF_UNKNOWNS = "0 50 0 0 0"      # NL_Solver Max_NL_iter Physics_scaling ATTInA22
 
 
 def cases():
-    tmp = os.path.join(ROOT, "_work", "golden_surfaces")
+    tmp = tempfile.mkdtemp(prefix="golden_surfaces_")     # surface files of the edited decks, removed at exit
+    atexit.register(shutil.rmtree, tmp, True)
     c = {}
     # 1-D FMT1 hard sphere against a hard wall (the reference's HS5 example as is)
     c["hs1d_wall"] = deck("HS5_FMT1_1D")

@@ -13,7 +13,9 @@ size and its zone-0 tables are kept:
     sten3d_dx010.npz   delta (844 points), theta (1015) and attraction (71 831) at dx = 0.1
     sten3d_dx008.npz   the same at dx = 0.08 (attraction: 137 299 points)
 
-Offsets are stored as int8 (every reach is below 32 nodes), weights as float64.
+Offsets are stored as int8 (every reach is below 32 nodes), weights as float64; the
+reference's set-up scalars of the deck (bulk state rho_b = 0.6: weighted densities,
+dPhi/dn, excess chemical potentials) are kept with them (info_ints, info_doubles).
 Run from the repository root with the reference tree present (read in place):
 
     python tests/golden/make_stencil_golden.py
@@ -56,8 +58,11 @@ def make(name, esize, edge):
         t0 = time.time()
         r = tref.extract(deck(esize, edge, surf), surf, newton=False, fill_states=())
     d = r["info_doubles"]
+    # the reference's set-up scalars of the same deck (rho_b = 0.6): bulk weighted densities, dPhi/dn and the
+    # excess chemical potentials (its own thermo, src/dft_thermo_hs.c:226-334, src/dft_thermo_att.c:44-63)
     out = {"esize": np.float64(esize), "kT": np.float64(KT), "hs_diam": np.float64(d[7]),
-           "sigma_ff": np.float64(d[147]), "eps_ff": np.float64(d[111]), "cut_ff": np.float64(d[183])}
+           "sigma_ff": np.float64(d[147]), "eps_ff": np.float64(d[111]), "cut_ff": np.float64(d[183]),
+           "info_ints": r["info_ints"], "info_doubles": d}
     for (isten, idx), (off, w, _hw) in r["stencils"].items():
         assert np.abs(off).max() < 128
         out[f"sten_{isten}_{idx}_off"] = off.astype(np.int8)

@@ -47,3 +47,22 @@ def test_errors_without_gpu_are_status_codes(lib):
     h = ctypes.c_void_p()
     assert lib.tgpu_create(None, 0, ctypes.byref(h)) == -1
     assert b"null" in lib.tgpu_last_error()
+
+
+@pytest.mark.parametrize("bc,reach,n", [((1, 1), 50, 30), ((2, 2), 50, 30), ((2, 1), 12, 10)],
+                         ids=["periodic-reach-past-box", "reflect-both-sides", "reflect-then-periodic"])
+def test_noalloc_rejects_stencils_that_reach_past_the_box(lib, bc, reach, n):
+    """A padded position the boundary rules cannot map (a periodic reach longer than the box, a mirrored point
+    beyond a periodic or reflecting far side) is TGPU_ERR_UNSUPPORTED, decided on the host before any device
+    work (the field pointers here are never read)."""
+    import numpy as np
+    lib.tgpu_stencil_sum_noalloc.restype = ctypes.c_int
+    lib.tgpu_noalloc_last_error.restype = ctypes.c_char_p
+    nx = np.array([n, 1, 1], np.int32)
+    bcs = np.array(bc, np.int32)
+    off = np.array([[-reach], [0], [reach]], np.int16)
+    w = np.ones(3)
+    rc = lib.tgpu_stencil_sum_noalloc(1, ctypes.c_void_p(nx.ctypes.data), ctypes.c_void_p(bcs.ctypes.data),
+                                      ctypes.c_double(0.0), 3, ctypes.c_void_p(off.ctypes.data),
+                                      ctypes.c_void_p(w.ctypes.data), ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    assert rc == -4 and b"reaches past the box" in lib.tgpu_noalloc_last_error()

@@ -12,7 +12,9 @@ FFT convolutions, the short ones (theta, delta) as float-float sums.
 - with every FP32 sum forced onto FP32 FFTs (tgpu_set_fft32_policy 1) the Schur product equals the FP64 one to
   1e-5, its nonlocal part (S v2 less the local v2 / rho) too, and J v to 1e-5 (relative to their max norms), an FP32 fill equals the FP64 fill to 1e-4, and the mixed
   solve still reaches the FP64 solve's density to 1e-9; with the direct kernels forced (policy 0) the products
-  are the slab / tensor-core ones.
+  are the slab / tensor-core ones;
+- TGPU_FP64_FFT products (J v and the Schur product with the sums of TGPU_FILL_FFT) equal the reference's
+  assembled products on the 3-D fixtures to 1e-12 (every sum by FFT) and the direct FP64 products at 64^3 to 1e-11.
 """
 import numpy as np
 import pytest
@@ -106,4 +108,46 @@ def test_fp32_fft_products(policy):
     xf, it, rn, _ = s.newton_solve(x0, resid_tol=1e-8, lin_tol=1e-6)
     assert rn <= 1e-8
     assert np.abs(xf[p.first_rho] - x64[p.first_rho]).max() <= 1e-9
+    s.close()
+
+
+@pytest.mark.parametrize("name", ["fmt1_wca_3d", "rough3d_fmt2", "rough3d_fmt4"])
+def test_fp64_fft_products_match_reference_fixture(name):
+    """TGPU_FP64_FFT products (every 3-D sum by FP64 FFT with threshold 0) against the reference's assembled
+    J v and Schur product, to the 1e-12 of the FP64 parity tests."""
+    from tramonto_gb300 import native
+    from goldens import PROD_RTOL, probe, rel_err
+    z, p = load(name)
+    s = native.Solver(p)
+    s.set_precision(native.FP64_FFT)
+    s.set_fft_threshold(0)
+    N = p.nunk * p.nnodes
+    for k in range(len(z["states"])):
+        x = z[f"x{k}"]
+        s.fill(x)
+        Jv = s.jv(probe(N, 0).reshape(x.shape))
+        S = s.schur(probe(p.ncomp * p.nnodes, 2).reshape(p.ncomp, p.nnodes))
+        print(name, k, "Jv rel", rel_err(Jv, z[f"Jv{k}"]), "Sv rel", rel_err(S, z[f"schur_Sv{k}"]))
+        assert rel_err(Jv, z[f"Jv{k}"]) <= PROD_RTOL
+        assert rel_err(S, z[f"schur_Sv{k}"]) <= PROD_RTOL
+    s.close()
+
+
+def test_fp64_fft_products_match_fp64_products():
+    """At 64^3 (default choice: the attraction sum by FP64 FFT, theta and delta in float-float) the Schur
+    product and J v equal the direct FP64 ones to 1e-11 of their max norms."""
+    from tramonto_gb300 import native, setup
+    from goldens import rel_err
+    p, _ = setup.config2(n=64)
+    s = native.Solver(p)
+    x = setup.initial_state(s, p)
+    s.fill(x)
+    rng = np.random.default_rng(8)
+    v2 = rng.standard_normal((p.ncomp, p.nnodes))
+    v = rng.standard_normal((p.nunk, p.nnodes))
+    S64, J64 = s.schur(v2), s.jv(v)
+    s.set_precision(native.FP64_FFT)
+    S, J = s.schur(v2), s.jv(v)
+    print("64^3 FP64-FFT products: Schur rel", rel_err(S, S64), "Jv rel", rel_err(J, J64))
+    assert rel_err(S, S64) <= 1e-11 and rel_err(J, J64) <= 1e-11
     s.close()

@@ -58,3 +58,17 @@ def test_config2_uses_the_pinned_tables():
         off, w, _ = p.stencils[(t, 0)]
         assert np.array_equal(off, z[f"sten_{t}_0_off"].astype(np.int16))
         assert np.abs(w - z[f"sten_{t}_0_w"]).max() <= 1e-14 * np.abs(z[f"sten_{t}_0_w"]).max()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_bulk_constants_of_the_workload_match_reference(name):
+    """Bulk weighted densities, dPhi/dn and excess chemical potentials at rho_b = 0.6 with the pinned tables
+    against the reference's own thermo of the same deck."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = z["info_doubles"]
+    uat = {0: (None, z[f"sten_{UATT}_0_w"])}
+    b = setup.bulk_constants(0, [HS_DIAM], [0.6], True, uat, 1)
+    assert np.allclose(b["rhobar_b"], d[55:59], rtol=1e-14, atol=0)
+    assert np.allclose(b["dphi_bulk"], d[65:69], rtol=1e-14, atol=1e-15)
+    assert np.allclose(b["betamu_hs_ex"], d[19:20], rtol=1e-13)
+    assert np.allclose(b["betamu_att"], d[25:26], rtol=1e-13)

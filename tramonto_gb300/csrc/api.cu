@@ -186,6 +186,8 @@ struct Ctx : tgpu_ctx {
   bool spec32_built = false;
   // the per-node FMT Hessian scalars of the current state (products of one Newton state share them)
   double *d_hcoef = nullptr;
+  // domain flags of the last fill (tgpu::kDomainN3 | tgpu::kDomainRho), set by its local kernels
+  unsigned *d_domain = nullptr;
   int hcoef_form = -1;           // the Jacobian form they were made with; -1: stale
 };
 
@@ -742,9 +744,11 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
   const double *rho = x + (long)g.first_rho * N;
   const size_t nrho = (size_t)g.ncomp * N, nconv = (size_t)(g.nrb + g.ncomp) * N;
   const size_t nchan = (size_t)g.ncomp * (g.ndim + 2) * N, ntr = (size_t)g.ncomp * N;
+  if (!c->d_domain) c->d_domain = dalloc<unsigned>(1);
+  ck(cudaMemsetAsync(c->d_domain, 0, sizeof(unsigned), c->stream), "memset");
   if (arith == TGPU_FILL_REFINED) {
     ensure_refs(c);
-    tgpu::launch_fmt_local(x, c->d_chan, c->stream);
+    tgpu::launch_fmt_local(x, c->d_chan, c->stream, c->d_domain);
     bool refresh = !c->have_ref;
     if (!refresh) {
       const int nb = tgpu::reduce_blocks((long)nchan);
@@ -783,12 +787,12 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
     c->fft_on = arith == TGPU_FILL_FFT;
     if (c->fft_on) ensure_fft(c);
     forward_pass(c, rho, c->pads.rho_res, f32);
-    tgpu::launch_fmt_local(x, c->d_chan, c->stream);
+    tgpu::launch_fmt_local(x, c->d_chan, c->stream, c->d_domain);
     transpose_pass(c, c->pads.tr_res, f32);
     c->ff_on = false;
     c->fft_on = false;
   }
-  tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream);
+  tgpu::launch_assemble(x, c->d_vext, c->d_zero, c->d_conv, c->d_tr, d_R, c->stream, c->d_domain);
   c->stats.kernel_launches += 2;
   if (c->coarse()) {   // the averaged rows of coarsened nodes
     tgpu::launch_coarse_rows(x, d_R, g.nunk, g.first_rho, g.ncomp, N, c->cr, c->d_cbulk, c->stream);
@@ -809,19 +813,49 @@ void fill_device(Ctx *c, const double *d_x, double *d_R, int mode)
              : c->fill_mode == TGPU_FILL_MIXED_FFT ? TGPU_FILL_FFT : c->fill_mode);
 }
 
+// TGPU_ERR_DOMAIN when the last fill took log(1 - n3) or 1/(1 - n3)^k at n3 >= 1, or log(rho) of rho <= 0 on a
+// live Euler-Lagrange row (the reference evaluates them unguarded, calc_FMT_derivatives src/dft_fill_FMT.c:362-366,
+// fill_EL_ideal_gas src/dft_fill_EL.c:358, and its Newton fails on the NaN); waits for the stream
+void check_domain(Ctx *c)
+{
+  if (!c->d_domain) return;
+  unsigned f = 0;
+  ck(cudaMemcpyAsync(&f, c->d_domain, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "d2h");
+  ck(cudaStreamSynchronize(c->stream), "sync");
+  if (f & tgpu::kDomainN3) throw Error(TGPU_ERR_DOMAIN, "n3 >= 1 at some node: log(1 - n3) and 1/(1 - n3) undefined");
+  if (f & tgpu::kDomainRho) throw Error(TGPU_ERR_DOMAIN, "density <= 0 on a live Euler-Lagrange row: log(rho) undefined");
+}
+
 void need_state(Ctx *c)
 {
   need_final(c);
   if (!c->have_state) throw Error(TGPU_ERR_STATE, "no Jacobian state: call tgpu_fill with mode 0 first");
 }
 
-// Jacobian / Schur products run their 3-D attraction sums on the tensor cores in TGPU_FP16TC
+// Arithmetic of the Jacobian / Schur products: TGPU_FP16TC runs the 3-D attraction sums on the tensor cores;
+// TGPU_FP64_FFT keeps every sum FP64-accurate but takes the long 3-D ones as FP64 FFT convolutions and the
+// short ones in float-float arithmetic (the sums of TGPU_FILL_FFT)
 struct TcScope {
   Ctx *c;
-  bool prev;
-  explicit TcScope(Ctx *c_) : c(c_), prev(c_->tc_on) { c->tc_on = c->precision == TGPU_FP16TC && c->tc_ready; }
-  ~TcScope() { c->tc_on = prev; }
+  bool prev_tc, prev_ff, prev_fft;
+  explicit TcScope(Ctx *c_) : c(c_), prev_tc(c_->tc_on), prev_ff(c_->ff_on), prev_fft(c_->fft_on)
+  {
+    c->tc_on = c->precision == TGPU_FP16TC && c->tc_ready;
+    if (c->precision == TGPU_FP64_FFT) {
+      c->ff_on = c->fft_on = true;
+      ensure_fft(c);
+    }
+  }
+  ~TcScope()
+  {
+    c->tc_on = prev_tc;
+    c->ff_on = prev_ff;
+    c->fft_on = prev_fft;
+  }
 };
+
+// whether the products' stencil sums run in FP32 arithmetic
+bool prod_f32(const Ctx *c) { return c->precision == TGPU_FP32 || c->precision == TGPU_FP16TC; }
 
 // the state's Hessian scalars for the products, made once per state and Jacobian form
 const double *hess_coef(Ctx *c)
@@ -851,7 +885,7 @@ void schur_device(Ctx *c, const double *d_v2, double *d_y2)
   need_state(c);
   TcScope tcs(c);
   const tgpu::DevGeom &g = c->dg;
-  const bool f32 = c->precision != TGPU_FP64;
+  const bool f32 = prod_f32(c);
   const double *v2 = prolonged(c, d_v2, g.ncomp);
   forward_pass(c, v2, c->pads.rho_jac, f32);
   if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.N, c->cr, nullptr, c->stream);
@@ -868,7 +902,7 @@ void jv_device(Ctx *c, const double *d_v, double *d_out)
   need_state(c);
   TcScope tcs(c);
   const long N = c->dg.N;
-  const bool f32 = c->precision != TGPU_FP64;
+  const bool f32 = prod_f32(c);
   forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, f32);
   tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, hess_coef(c), c->stream);
   transpose_pass(c, c->pads.tr_jac, f32);
@@ -902,7 +936,7 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
   }
   tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
   TcScope tcs(c);
-  transpose_pass(c, c->pads.tr_jac, c->precision != TGPU_FP64);
+  transpose_pass(c, c->pads.tr_jac, prod_f32(c));
   tgpu::launch_rhs_combine(c->d_vext, c->d_zero, b, c->d_tr, c->d_ymf, d_b2s, c->stream);
   if (c->coarse()) tgpu::launch_zero_nodes(d_b2s, g.ncomp, g.N, c->cr, c->stream);
   c->stats.kernel_launches += 2;
@@ -914,7 +948,7 @@ void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx
   TcScope tcs(c);
   const tgpu::DevGeom &g = c->dg;
   const double *x2 = prolonged(c, d_x2, g.ncomp);
-  forward_pass(c, x2, c->pads.rho_jac, c->precision != TGPU_FP64);
+  forward_pass(c, x2, c->pads.rho_jac, prod_f32(c));
   tgpu::launch_x1(d_b, c->d_conv, x2, d_dx, c->stream);
   if (c->coarse()) tgpu::launch_prolong(d_dx, 0, g.nunk, g.N, c->cr, nullptr, c->stream);
   c->stats.kernel_launches++;
@@ -1082,6 +1116,7 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
     fill_arith(c, d_x, d_R, 0, arith);
     tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
     red_to_host(c, 1);
+    check_domain(c);
     rnorm = std::sqrt(c->h_red[0]);
     rprev = rnorm;
     if (!std::isfinite(rnorm)) throw Error(TGPU_ERR_NONFINITE, "non-finite residual in Newton");
@@ -1146,6 +1181,7 @@ int newton_solve_device(Ctx *c, double *d_x, double resid_tol, int max_iter, dou
     fill_arith(c, d_x, d_R, 0, arith);
     tgpu::launch_norm2(d_R, n, c->d_partial, nb, c->d_red, c->stream);
     red_to_host(c, 1);
+    check_domain(c);
     rnorm = std::sqrt(c->h_red[0]);
     if (!std::isfinite(rnorm)) throw Error(TGPU_ERR_NONFINITE, "non-finite residual in Newton");
     if (inexact && rnorm <= c->refine_switch) {
@@ -2184,7 +2220,7 @@ int tgpu_destroy(tgpu_handle h)
           dfree(st.d_loff); dfree(st.d_loff_neg); dfree(st.d_off); dfree(st.d_w); dfree(st.d_hw);
           dfree(st.d_coef_fwd); dfree(st.d_coef_fwd32); dfree(st.d_coef_tr); dfree(st.d_coef_tr32); dfree(st.d_coef_adj);
         }
-    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2); dfree(c->d_hcoef);
+    dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2); dfree(c->d_hcoef); dfree(c->d_domain);
     dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
     dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
@@ -2394,7 +2430,7 @@ int tgpu_set_precision(tgpu_handle h, int precision)
 {
   return guard([&] {
     Ctx *c = C(h);
-    if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC)
+    if (precision != TGPU_FP64 && precision != TGPU_FP32 && precision != TGPU_FP16TC && precision != TGPU_FP64_FFT)
       throw Error(TGPU_ERR_UNSUPPORTED, "precision");
     if (precision == TGPU_FP16TC && !c->tc_ready)
       throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
@@ -2517,6 +2553,7 @@ int tgpu_fill_device(tgpu_handle h, const double *d_x, double *d_R, int mode)
     fill_device(c, a22_in(c, d_x, A22_SUMS, 0), R, mode);
     a22_out(c, R, d_R);
     ck(cudaGetLastError(), "fill launch");
+    check_domain(c);
     return TGPU_OK;
   });
 }
@@ -2534,6 +2571,7 @@ int tgpu_fill(tgpu_handle h, const double *x, double *R, int mode)
     a22_out(c, Rd, c->d_work2);
     d2h(c, R, c->d_work2, n);
     ck(cudaGetLastError(), "fill launch");
+    check_domain(c);
     return TGPU_OK;
   });
 }

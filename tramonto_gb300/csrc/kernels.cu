@@ -739,19 +739,21 @@ __device__ __forceinline__ void write_tr_channels(const double *q, double *chan,
   }
 }
 
-__global__ void k_fmt_local(const double *__restrict__ x, double *__restrict__ chan)
+// domain: when non-null, bit kDomainN3 is set where n3 >= 1 (log(1 - n3) and 1/(1 - n3)^k are taken here)
+__global__ void k_fmt_local(const double *__restrict__ x, double *__restrict__ chan, unsigned *__restrict__ domain)
 {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < c_g.N; i += (long)gridDim.x * blockDim.x) {
     double n[kMaxRb], dphi[kMaxRb];
     load_n(x, i, n);
+    if (domain && n[3] >= 1.0) atomicOr(domain, kDomainN3);
     fmt_dphi(n, dphi);
     write_tr_channels(dphi, chan, i);
   }
 }
 
-void launch_fmt_local(const double *x, double *chan, cudaStream_t s)
+void launch_fmt_local(const double *x, double *chan, cudaStream_t s, unsigned *domain)
 {
-  k_fmt_local<<<1184, kThreads, 0, s>>>(x, chan);
+  k_fmt_local<<<1184, kThreads, 0, s>>>(x, chan, domain);
 }
 
 // The pinned density of a constrained interface: R = ln rho - ln pin_value, J = 1/rho on the diagonal
@@ -777,9 +779,10 @@ __device__ __forceinline__ bool dep_rb(int k, int *src, double *c)
   return false;
 }
 
+// domain: when non-null, bit kDomainRho is set where a live Euler-Lagrange row takes log(rho) of rho <= 0
 __global__ void k_assemble(const double *__restrict__ x, const double *__restrict__ vext,
                            const signed char *__restrict__ zero, const double *__restrict__ conv,
-                           const double *__restrict__ tr, double *__restrict__ R)
+                           const double *__restrict__ tr, double *__restrict__ R, unsigned *__restrict__ domain)
 {
   const long N = c_g.N;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
@@ -797,6 +800,7 @@ __global__ void k_assemble(const double *__restrict__ x, const double *__restric
           mu = -log(c_g.rho_b[ic]) - c_g.betamu_hs_ex[ic];
           if (c_g.attraction) mu -= c_g.betamu_att[ic];
         }
+        if (domain && xi <= 0.0) atomicOr(domain, kDomainRho);
         r = log(xi) + mu + vext[(long)ic * N + i] + tr[(long)ic * N + i];
         if (c_g.attraction) r += x[(long)(c_g.first_mf + ic) * N + i];
       }
@@ -820,9 +824,9 @@ __global__ void k_assemble(const double *__restrict__ x, const double *__restric
 }
 
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
-                     const double *tr, double *R, cudaStream_t s)
+                     const double *tr, double *R, cudaStream_t s, unsigned *domain)
 {
-  k_assemble<<<1184, kThreads, 0, s>>>(x, vext, zero, conv, tr, R);
+  k_assemble<<<1184, kThreads, 0, s>>>(x, vext, zero, conv, tr, R, domain);
 }
 
 // Schur local step: y1 = A11^-1 u (u = A12 v in conv), then the EL-side

@@ -64,7 +64,6 @@ __global__ void k_na_pad(const double *__restrict__ field, double bulk, Geo g, c
     double v;
     if (sent == kSentBulk) v = bulk;
     else if (sent == kSentWall) v = 0.0;
-    else if (sent != 0) v = __longlong_as_double(0x7ff8000000000000ULL);
     else v = field[idx[0] + (long)g.nx[0] * (idx[1] + (long)g.nx[1] * idx[2])];
     pad[p] = v;
   }
@@ -115,8 +114,10 @@ int device_ptrs(int dev, DevPtrs **out)
   return TGPU_OK;
 }
 
-// one padded dimension: q -> node (with reflect bit) or sentinel, as offset_to_node_box
-void fill_map(int n, int h, int bcl, int bcr, int *m)
+// one padded dimension: q -> node (with reflect bit) or sentinel, as offset_to_node_box; false when a
+// padded position has no node to read: a periodic reach longer than the box, or a mirrored position that
+// falls past the far side without a bulk or wall rule there
+bool fill_map(int n, int h, int bcl, int bcr, int *m)
 {
   for (int q = 0; q < n + 2 * h; q++) {
     int s = q - h, v;
@@ -137,8 +138,10 @@ void fill_map(int n, int h, int bcl, int bcr, int *m)
     } else {
       v = s;
     }
+    if (v == kSentBad) return false;
     m[q] = v;
   }
+  return true;
 }
 
 }  // namespace
@@ -154,6 +157,10 @@ int tgpu_stencil_sum_noalloc(int ndim, const int *nx, const int *bc, double bulk
   if (ndim < 1 || ndim > 3 || !nx || !bc || !d_field || !d_out) return fail(TGPU_ERR_ARG, "null or bad argument");
   if (length < 0 || length > kStenMax) return fail(TGPU_ERR_ARG, "stencil longer than TGPU_NOALLOC_MAX_STENCIL");
   if (length > 0 && (!offsets || !weights)) return fail(TGPU_ERR_ARG, "null stencil arrays");
+  for (int d = 0; d < ndim; d++)
+    for (int k = 0; k < 2; k++)
+      if (bc[2 * d + k] < TGPU_BC_IN_WALL || bc[2 * d + k] > TGPU_BC_REFLECT)
+        return fail(TGPU_ERR_UNSUPPORTED, "boundary condition");
   Geo g{};
   g.ndim = ndim;
   int h[3] = {0, 0, 0};
@@ -163,23 +170,41 @@ int tgpu_stencil_sum_noalloc(int ndim, const int *nx, const int *bc, double bulk
       h[d] = o < 0 ? (h[d] > -o ? h[d] : -o) : (h[d] > o ? h[d] : o);
     }
   g.N = 1;
+  long NP = 1;
   for (int d = 0; d < 3; d++) {
     g.nx[d] = d < ndim ? nx[d] : 1;
     if (g.nx[d] < 1) return fail(TGPU_ERR_ARG, "nx must be positive");
+    if (g.nx[d] > kMapMax) return fail(TGPU_ERR_ARG, "padded extent above 4096 in a dimension");
     g.h[d] = d < ndim ? h[d] : 0;
-    g.P[d] = g.nx[d] + 2 * g.h[d];
-    if (g.P[d] > kMapMax) return fail(TGPU_ERR_ARG, "padded extent above 4096 in a dimension");
+    const long P = (long)g.nx[d] + 2L * g.h[d];
+    if (P > kMapMax) return fail(TGPU_ERR_ARG, "padded extent above 4096 in a dimension");
+    g.P[d] = (int)P;
+    NP *= P;
     g.N *= g.nx[d];
   }
+  if (NP > kPadMax) return fail(TGPU_ERR_ARG, "padded box larger than TGPU_NOALLOC_MAX_PADDED points");
+  g.NP = NP;
   g.pstride[0] = 1;
   g.pstride[1] = g.P[0];
   g.pstride[2] = (long)g.P[0] * g.P[1];
-  g.NP = (long)g.P[0] * g.P[1] * g.P[2];
-  if (g.NP > kPadMax) return fail(TGPU_ERR_ARG, "padded box larger than TGPU_NOALLOC_MAX_PADDED points");
-  for (int d = 0; d < ndim; d++)
-    for (int k = 0; k < 2; k++)
-      if (bc[2 * d + k] < TGPU_BC_IN_WALL || bc[2 * d + k] > TGPU_BC_REFLECT)
-        return fail(TGPU_ERR_UNSUPPORTED, "boundary condition");
+  // host-side staging of the maps and offsets (host memory, reused per thread); the maps are checked before
+  // any device work, so a rejected call leaves the device untouched
+  static thread_local int h_map[3 * kMapMax];
+  static thread_local int h_loff[kStenMax];
+  for (int d = 0; d < 3; d++) {
+    if (d >= ndim) {
+      h_map[d * kMapMax] = 0;
+    } else if (!fill_map(g.nx[d], g.h[d], bc[2 * d], bc[2 * d + 1], h_map + d * kMapMax)) {
+      return fail(TGPU_ERR_UNSUPPORTED,
+                  "stencil reaches past the box: a periodic reach longer than the box, or a mirrored point beyond "
+                  "the far side without a bulk or wall boundary there");
+    }
+  }
+  for (int k = 0; k < length; k++) {
+    long o = 0;
+    for (int d = 0; d < ndim; d++) o += (long)offsets[(long)k * ndim + d] * g.pstride[d];
+    h_loff[k] = (int)o;
+  }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(TGPU_ERR_CUDA, cudaGetErrorString(e));
@@ -187,27 +212,16 @@ int tgpu_stencil_sum_noalloc(int ndim, const int *nx, const int *bc, double bulk
   int st = device_ptrs(dev, &dp);
   if (st != TGPU_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // host-side staging of the maps and offsets (host memory, reused per thread)
-  static thread_local int h_map[3 * kMapMax];
-  static thread_local int h_loff[kStenMax];
-  for (int d = 0; d < 3; d++) {
-    if (d < ndim) fill_map(g.nx[d], g.h[d], bc[2 * d], bc[2 * d + 1], h_map + d * kMapMax);
-    else h_map[d * kMapMax] = 0;
-  }
-  for (int k = 0; k < length; k++) {
-    long o = 0;
-    for (int d = 0; d < ndim; d++) o += (long)offsets[(long)k * ndim + d] * g.pstride[d];
-    h_loff[k] = (int)o;
-  }
   if ((e = cudaMemcpyAsync(dp->map, h_map, sizeof(int) * 3 * kMapMax, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
       (length > 0 && (e = cudaMemcpyAsync(dp->loff, h_loff, sizeof(int) * length, cudaMemcpyHostToDevice, s)) != cudaSuccess) ||
       (length > 0 && (e = cudaMemcpyAsync(dp->w, weights, sizeof(double) * length, cudaMemcpyHostToDevice, s)) != cudaSuccess))
     return fail(TGPU_ERR_CUDA, cudaGetErrorString(e));
   k_na_pad<<<592, 256, 0, s>>>(d_field, bulk_value, g, dp->map, dp->pad);
   k_na_sum<<<(unsigned)((g.N + 255) / 256), 256, 0, s>>>(dp->pad, dp->loff, dp->w, length, g, d_out);
+  // a launch that could not start reports here, before the wait
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail(TGPU_ERR_CUDA, cudaGetErrorString(e));
   // the host tables above are reused by the next call: wait for the copies to land
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail(TGPU_ERR_CUDA, cudaGetErrorString(e));
-  if ((e = cudaGetLastError()) != cudaSuccess) return fail(TGPU_ERR_CUDA, cudaGetErrorString(e));
   return TGPU_OK;
 }
 

@@ -454,9 +454,11 @@ void launch_conv_slab_ff(const float *in_hi, const float *in_lo, long in_total, 
                          const int4 *lines, const float *lw, const float *lw_lo, double *out, int pitch, int ncols,
                          int max_rows, int max_lines, int max_w, int nx, int ny, int nz, cudaStream_t s);
 constexpr int kSlabTileX = 128, kSlabTileY = 16;
-void launch_fmt_local(const double *x, double *chan, cudaStream_t s);
+// domain flags of a fill (launch_fmt_local / launch_assemble with a non-null flag word)
+constexpr unsigned kDomainN3 = 1u, kDomainRho = 2u;
+void launch_fmt_local(const double *x, double *chan, cudaStream_t s, unsigned *domain = nullptr);
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
-                     const double *tr, double *R, cudaStream_t s);
+                     const double *tr, double *R, cudaStream_t s, unsigned *domain = nullptr);
 // coef: the state's Hessian scalars ([kHessCoef][N], launch_hess_coef) or null to evaluate them in place
 void launch_hess_coef(const double *x, double *coef, cudaStream_t s);
 void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
