@@ -83,6 +83,11 @@ def parse():
                     help="GMRES iterations per Newton iteration for the reference arm's cost model (the GPU arm "
                          "prints its own as gmres_iters_per_newton_iter)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fft32-policy", type=int, default=-1, choices=[-1, 0, 1],
+                    help="FP32 sums as FP32 FFT convolutions: -1 chosen by timing each sum's first use (default), "
+                         "1 always, 0 never (profiler runs fix the choice, since their timings are not the real ones)")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 solve and the density error (launch lists and profiles)")
     ap.add_argument("--light", action="store_true",
                     help="one repetition of each FP64 kernel-family timing (large workloads)")
     ap.add_argument("--products", default="fp16tc", choices=["fp16tc", "fp32"],
@@ -387,6 +392,9 @@ def main():
         s.set_precision(prod_prec)
         s.set_fill_arithmetic(fill_mode, switch_norm=args.switch)
 
+    if args.fft32_policy != -1:
+        s.set_fft32_policy(args.fft32_policy)
+
     ladder = meta.get("ladder")
 
     def solve(xt=dx, resid_tol=None, lin_tol=None):
@@ -425,6 +433,7 @@ def main():
     final_r = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("timed_solves")   # the launch list's window (ncu --nvtx-include timed_solves/)
         e0.record(stream)
         for _ in range(args.steps):
             it, rn, li = solve()
@@ -433,8 +442,10 @@ def main():
             final_r.append(rn)
             progress(f"timed solve: {it} Newton iterations, {li} GMRES, ||R||_2 = {rn:.2e}")
         e1.record(stream)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
     st = s.stats()
+    choices = {name: s.fft32_choice(t, 0) for name, t in (("theta", THETA), ("delta", DELTA), ("attraction", UATT))}
     ms_total = e0.elapsed_time(e1)
     # one replica per rank: Newton iterations of all ranks over the slowest rank's time
     _, ms_total, value = ranks.whole_job_rate(max(1, iters), ms_total, device="cuda")
@@ -495,24 +506,26 @@ def main():
     # FP64 FFT convolutions, the short ones in float-float arithmetic), the same Newton driver and target, timed
     # over a whole solve; then continued to ||R||_2 <= 1e-10 with tight linear solves as the FP64 solution the
     # mixed solution's density is compared with.
-    s.set_precision(native.FP64_FFT)
-    s.set_fill_arithmetic(native.FILL_FFT)
-    x64 = torch.empty_like(dx)
+    fp64_ms = it64 = li64 = rn64 = dens_err = dens_max = None
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    a.record(stream)
-    it64, rn64, li64 = solve(x64)
-    b.record(stream)
-    torch.cuda.synchronize()
-    fp64_ms = a.elapsed_time(b) / max(1, it64)
-    progress(f"plain FP64 solve: {it64} Newton iterations, {li64} GMRES, {fp64_ms:.1f} ms per iteration")
-    s.newton_solve_device(x64, resid_tol=1e-10, max_iter=args.max_newton, lin_tol=1e-10, lin_max_iter=args.lin_maxit,
-                          allow_noconv=True)
-    rho = slice(p.first_rho, p.first_rho + p.ncomp)
-    dens_err = float((x_mixed[rho] - x64[rho]).abs().max().item())
-    dens_max = float(x64[rho].abs().max().item())
-    progress(f"max |rho_mixed - rho_fp64| = {dens_err:.2e} (max rho {dens_max:.3f})")
-    del x64
+    if not args.no_plain:
+        s.set_precision(native.FP64_FFT)
+        s.set_fill_arithmetic(native.FILL_FFT)
+        x64 = torch.empty_like(dx)
+        torch.cuda.synchronize()
+        a.record(stream)
+        it64, rn64, li64 = solve(x64)
+        b.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = a.elapsed_time(b) / max(1, it64)
+        progress(f"plain FP64 solve: {it64} Newton iterations, {li64} GMRES, {fp64_ms:.1f} ms per iteration")
+        s.newton_solve_device(x64, resid_tol=1e-10, max_iter=args.max_newton, lin_tol=1e-10, lin_max_iter=args.lin_maxit,
+                              allow_noconv=True)
+        rho = slice(p.first_rho, p.first_rho + p.ncomp)
+        dens_err = float((x_mixed[rho] - x64[rho]).abs().max().item())
+        dens_max = float(x64[rho].abs().max().item())
+        progress(f"max |rho_mixed - rho_fp64| = {dens_err:.2e} (max rho {dens_max:.3f})")
+        del x64
     # the same iteration with direct FP64 stencil sums (no FFT, no float-float) in fills and products
     s.set_precision(native.FP64)
     s.set_fill_arithmetic(native.FILL_FP64)
@@ -573,6 +586,7 @@ def main():
             "gmres_iters_per_newton_iter": lin_iters / max(1, iters), "final_resid_norm2": max(final_r),
             "final_resid_norm2_fp64_recheck": resid_fp64, "accurate_fill": args.accurate_fill,
             "gpu_launches": int(st["kernel_launches"]),
+            "fp32_sum_choices": choices,
             "clocks": clk.summary(),
             "e2e": {"value": it_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 8 * len(ladder or [0]),
                     "d2h_bytes_per_step": n * 8 * len(ladder or [0]),
@@ -626,18 +640,19 @@ def main():
                              "schur_apply_fp32": t_apply32,
                              "schur_apply_fp16tc": t_apply_tc,
                              "schur_apply_fp64": t_apply64, "schur_applies_in_timed_steps": int(st["schur_applies"])},
-            "plain_fp64": {"ms_per_newton_iter": fp64_ms, "newton_iters": it64, "gmres_iters": li64,
-                           "final_resid_norm2": rn64,
-                           "arithmetic": "FP64-accurate fills and Schur products: long 3-D sums as FP64 FFT "
-                                         "convolutions, short ones in float-float arithmetic",
-                           "speedup_mixed_vs_fp64_per_iter": fp64_ms / ms_per_iter,
-                           "speedup_mixed_vs_fp64_per_solve": (fp64_ms * it64) / ms_per_solve},
+            "plain_fp64": None if fp64_ms is None else {
+                "ms_per_newton_iter": fp64_ms, "newton_iters": it64, "gmres_iters": li64, "final_resid_norm2": rn64,
+                "arithmetic": "FP64-accurate fills and Schur products: 3-D stencil sums as FP64 FFT convolutions "
+                              "where the cost model finds them cheaper than float-float direct sums",
+                "speedup_mixed_vs_fp64_per_iter": fp64_ms / ms_per_iter,
+                "speedup_mixed_vs_fp64_per_solve": (fp64_ms * it64) / ms_per_solve},
             "plain_fp64_direct_sums": {"ms_per_newton_iter": direct_ms,
                                        "speedup_mixed_vs_direct_per_iter": (direct_ms / ms_per_iter)
                                        if direct_ms else None},
             "max_density_err_vs_fp64": dens_err,
-            "density_err_reference": "the FP64 path's solution continued to ||R||_2 <= 1e-10 (linear tolerance "
-                                     f"1e-10); max density {dens_max:.4f}",
+            "density_err_reference": None if dens_max is None else
+                ("the FP64 path's solution continued to ||R||_2 <= 1e-10 (linear tolerance 1e-10); max density "
+                 f"{dens_max:.4f}"),
             "setup_s": t_setup,
         }
         print(json.dumps(out))

@@ -176,6 +176,12 @@ int tgpu_set_fft_threshold(tgpu_handle h, int min_points);
 /* FP32 stencil sums (products, FP32 fills) as FP32 FFT convolutions: -1 (default) each sum's first use times
  * the FFT against its direct kernel and keeps the faster; 0 never; 1 always (3-D problems). */
 int tgpu_set_fft32_policy(tgpu_handle h, int policy);
+/* The choices of that policy so far, for stencil (type, index): choice[0] forward, choice[1] transposed sums
+ * (1 FFT, -1 direct kernel, 0 not yet decided); ms[4] the timed direct and FFT sums behind them (forward direct,
+ * forward FFT, transposed direct, transposed FFT; 0 where not timed).  For the attraction stencil the forward
+ * choice is the one of the current product arithmetic (tensor-core products for TGPU_FP16TC, else the FP32 slab
+ * kernel).  No reference counterpart (a benchmark and diagnostics hook). */
+int tgpu_fft32_choice(tgpu_handle h, int type, int index, int *choice, double *ms);
 /* Second derivatives of the FMT energy density in J, J^T and Schur products (and so in Newton):
  *   TGPU_JAC_REFERENCE  the reference's tables, entry for entry (default): d2phi_drb2_{delta,theta}_rb_FMT*
  *                       (src/dft_physics_FMT{1,2,3,4}.c, via FMT2ndDeriv*_switch, src/dft_switch_FMT.c:122-152)

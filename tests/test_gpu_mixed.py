@@ -47,7 +47,9 @@ def test_refined_fill_matches_fp64_fill():
     R32 = s.fill(x1)
     s.close()
     assert st["fp64_refreshes"] == 0
-    assert np.abs(Rref - R64).max() <= 1e-10, np.abs(Rref - R64).max()
+    # FP32 sums of a change of relative size 1e-4: their rounding is ~1e-7 of the change's sums (FP32 FFT sums
+    # carry it relative to the sums' max norm, ~3e-7), against residual terms of O(1..10)
+    assert np.abs(Rref - R64).max() <= 3e-10, np.abs(Rref - R64).max()
     assert np.abs(R32 - R64).max() > np.abs(Rref - R64).max()
 
 

@@ -114,6 +114,8 @@ struct PadParams {
   double *bulk = nullptr;
   int *sign = nullptr, *zc = nullptr;
   int nch = 0;
+  std::vector<double> h_bulk;      // host copies: [low side channels][high side channels]
+  std::vector<int> h_sign, h_zc;
 };
 
 }  // namespace
@@ -180,10 +182,16 @@ struct Ctx : tgpu_ctx {
   // tensor-core sum (products) and the FP32 slab sum (FP32 fills): 0 undecided, 1 FFT, -1 direct
   float2 *d_fbox32[3] = {nullptr, nullptr, nullptr};
   int fft32_tc = 0, fft32_slab = 0;
+  float t32_att[2][2] = {{0.f, 0.f}, {0.f, 0.f}};   // [slab context, tensor-core context][direct, FFT] ms
   long fft32_gen = -1;
   int fft32_ch = -1;
   double *d_dscr = nullptr;      // [4 + 2 ndim][N] outputs of the timing runs that make the choices
   bool spec32_built = false;
+  // the channels of the last pad(): the padded box is written only when a direct kernel needs it (FFT sums read
+  // the channels through the boundary maps)
+  const double *pad_src = nullptr;
+  const PadParams *pad_pp = nullptr;
+  bool pad_f32 = false, pad_pending = false;
   // the per-node FMT Hessian scalars of the current state (products of one Newton state share them)
   double *d_hcoef = nullptr;
   // domain flags of the last fill (tgpu::kDomainN3 | tgpu::kDomainRho), set by its local kernels
@@ -250,6 +258,9 @@ PadParams make_pad(const std::vector<double> &bulk, const std::vector<int> &sign
   p.bulk = upload(b2, s);
   p.sign = upload(sign, s);
   p.zc = upload(zc, s);
+  p.h_bulk = b2;
+  p.h_sign = sign;
+  p.h_zc = zc;
   return p;
 }
 
@@ -269,28 +280,83 @@ long nnodes(const tgpu_geometry &g)
 
 // ---- stencil passes --------------------------------------------------------
 
-// Pad `nch` channels of `src` with parameter set `pp`, into the FP32 or the FP64 padded box.
+// Pad `nch` channels of `src` with parameter set `pp`, into the FP32 or the FP64 padded box: recorded here, written
+// by materialize() before the first direct kernel that reads the box (src must stay unchanged until then)
 void pad(Ctx *c, const double *src, const PadParams &pp, bool f32)
 {
   c->pad_gen++;   // the padded channels change: a cached spectrum of them is stale
-  if (!f32)
-    tgpu::launch_pad<double>(src, c->d_pad, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
+  c->pad_src = src;
+  c->pad_pp = &pp;
+  c->pad_f32 = f32;
+  c->pad_pending = true;
+}
+
+void materialize(Ctx *c)
+{
+  if (!c->pad_pending) return;
+  const PadParams &pp = *c->pad_pp;
+  if (!c->pad_f32)
+    tgpu::launch_pad<double>(c->pad_src, c->d_pad, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
   else
-    tgpu::launch_pad<float>(src, c->d_pad32, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
+    tgpu::launch_pad<float>(c->pad_src, c->d_pad32, pp.nch, pp.bulk, pp.sign, pp.zc, c->d_zero, false, c->stream);
   c->stats.kernel_launches++;
+  c->pad_pending = false;
+}
+
+// channel ch of the last pad() as the FFT's mapped source
+tgpu::MapSrc map_src(const Ctx *c, int ch)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const PadParams &pp = *c->pad_pp;
+  tgpu::MapSrc m;
+  m.src = c->pad_src + (long)ch * g.N;
+  m.ndim = g.ndim;
+  for (int d = 0; d < 3; d++) {
+    m.nx[d] = g.nx[d];
+    m.map[d] = g.map[d];
+  }
+  m.bulk_lo = pp.h_bulk[ch];
+  m.bulk_hi = pp.h_bulk[pp.nch + ch];
+  m.signmask = pp.h_sign[ch];
+  m.zc = pp.h_zc[ch];
+  m.zero = c->d_zero;
+  m.N = g.N;
+  return m;
 }
 
 // ---- FP64 stencil sums by FFT ----------------------------------------------------
 
-// Which stencils take the FFT in TGPU_FILL_FFT: those whose direct float-float sum (measured on GB300:
-// ~5.4e-13 s per term) costs more than the transforms (~1.8e-11 s per point and log2 of the box, one per
-// coefficient plus the field's), unless tgpu_set_fft_threshold fixed a length.  At 128^3 the attraction
-// stencil (7e4 points) qualifies, theta and delta (~1e3) do not.
+// Which stencils take the FFT in TGPU_FILL_FFT (and TGPU_FP64_FFT products): those whose direct float-float sums
+// (measured on GB300: ~5.4e-13 s per term and output) cost more than the transforms (one per coefficient plus the
+// field's; measured ~8e-12 s per half-spectrum point and log2 of the box: 0.26 ms for the 180 x 128 x 128 box of
+// the 128^3 workload), unless tgpu_set_fft_threshold fixed a length.  At 128^3 every stencil qualifies: the
+// attraction stencil (7e4 points), theta (1015) and delta (844 points, four outputs).
 bool fft_worth(const Ctx *c, const DevStencil &st, int nq)
 {
   if (c->fft_min_points >= 0) return st.L >= c->fft_min_points;
-  const double NF = (double)c->fft.NF;
-  return (double)st.L * (double)c->dg.N * 5.4e-13 > (nq + 1) * NF * std::log2(NF) * 1.8e-11;
+  const double NR = (double)c->fft.NR, NH = (double)c->fft.NH;
+  return (double)st.L * (double)c->dg.N * nq * 5.4e-13 > (nq + 1) * NH * std::log2(NR) * 8.0e-12;
+}
+
+// the plan's geometry: padded extents, mesh, reach, and the dimensions periodic at both ends (left unpadded)
+void plan_geometry_args(const Ctx *c, int P[3], int nx[3], int h[3], int per[3])
+{
+  const tgpu::DevGeom &dg = c->dg;
+  for (int d = 0; d < 3; d++) {
+    P[d] = dg.P[d];
+    nx[d] = dg.nx[d];
+    h[d] = dg.h[d];
+    per[d] = d < dg.ndim && c->g.bc[d][0] == TGPU_BC_PERIODIC && c->g.bc[d][1] == TGPU_BC_PERIODIC;
+  }
+}
+
+// spectrum (FP64 half spectrum) of coefficient q of a stencil's forward (side 0) or transposed (side 1) table
+void kernel_spectrum(Ctx *c, const DevStencil &st, int side, int q, double *rbox, double2 *spec)
+{
+  const double *coef = side == 0 ? st.d_coef_fwd : st.d_coef_tr;
+  const int nq = side == 0 ? st.nout_fwd : st.nin_tr;
+  tgpu::launch_fft_kernel_box(st.d_off, coef, st.L, nq, q, rbox, c->fft, c->stream);
+  tgpu::rfft_forward_box(rbox, spec, c->fft, c->stream);
 }
 
 // plan, work boxes and the spectra of every zone-0 stencil coefficient (forward outputs, transpose inputs)
@@ -300,11 +366,12 @@ void ensure_fft(Ctx *c)
   c->fft_state = -1;
   const tgpu::DevGeom &dg = c->dg;
   if (dg.ndim != 3) return;
-  const int P[3] = {dg.P[0], dg.P[1], dg.P[2]};
-  if (!tgpu::fft_make_plan(c->fft, P, dg.ndim, c->stream)) return;
+  int P[3], nx[3], h[3], per[3];
+  plan_geometry_args(c, P, nx, h, per);
+  if (!tgpu::fft_make_plan(c->fft, P, nx, h, per, dg.ndim, c->stream)) return;
   c->fft_plan_ok = true;
-  const long NF = c->fft.NF;
-  // device memory: three work boxes and one box per stencil coefficient
+  const long NH = c->fft.NH, NR = c->fft.NR;
+  // device memory: three work spectra and one spectrum per stencil coefficient
   size_t nspec = 0;
   for (int t = 0; t < 3; t++)
     for (auto &st : c->sten[t])
@@ -312,8 +379,9 @@ void ensure_fft(Ctx *c)
   if (nspec == 0) return;
   size_t free_b = 0, total_b = 0;
   ck(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-  if ((nspec + 3) * (size_t)NF * sizeof(double2) > free_b / 2) return;
-  for (auto &b : c->d_fbox) b = dalloc<double2>((size_t)NF);
+  if ((nspec + 3) * (size_t)NH * sizeof(double2) + (size_t)NR * sizeof(double) > free_b / 2) return;
+  for (auto &b : c->d_fbox) b = dalloc<double2>((size_t)NH);
+  double *rbox = dalloc<double>((size_t)NR);
   for (int t = 0; t < 3; t++)
     for (auto &st : c->sten[t]) {
       if (st.L == 0 || !fft_worth(c, st, st.nout_fwd)) continue;
@@ -322,14 +390,14 @@ void ensure_fft(Ctx *c)
         const int nq = side == 0 ? st.nout_fwd : st.nin_tr;
         if (!coef) continue;
         for (int q = 0; q < nq; q++) {
-          double2 *k = dalloc<double2>((size_t)NF);
-          tgpu::launch_fft_kernel_box(st.d_off, coef, st.L, nq, q, k, c->fft, c->stream);
-          tgpu::fft3d(k, c->fft, dg.ndim, false, c->stream);
+          double2 *k = dalloc<double2>((size_t)NH);
+          kernel_spectrum(c, st, side, q, rbox, k);
           (side == 0 ? st.spec_fwd : st.spec_tr).push_back(k);
         }
       }
     }
   ck(cudaStreamSynchronize(c->stream), "sync");
+  dfree(rbox);
   c->fft_state = 1;
 }
 
@@ -337,23 +405,22 @@ void ensure_fft(Ctx *c)
 const double2 *fft_channel(Ctx *c, int ch)
 {
   if (c->fft_gen == c->pad_gen && c->fft_ch == ch) return c->d_fbox[0];
-  const int P[3] = {c->dg.P[0], c->dg.P[1], c->dg.P[2]};
-  tgpu::launch_fft_load(c->d_pad + (long)ch * c->dg.NP, P, c->d_fbox[0], c->fft, c->stream);
-  tgpu::fft3d(c->d_fbox[0], c->fft, c->dg.ndim, false, c->stream);
-  c->stats.kernel_launches += 1 + c->dg.ndim;
+  tgpu::rfft_forward_mapped(map_src(c, ch), c->d_fbox[0], c->fft, c->stream);
+  c->stats.kernel_launches += 3;
   c->fft_gen = c->pad_gen;
   c->fft_ch = ch;
   return c->d_fbox[0];
 }
 
-// FP32 spectra of the attraction stencils (from FP64 ones) and two FP32 work boxes
+// FP32 spectra of the stencils (from FP64 ones) and three FP32 work spectra
 bool prepare_spec32(Ctx *c)
 {
   if (c->spec32_built) return true;
   ensure_fft(c);
   if (!c->fft_plan_ok) return false;
-  const long NF = c->fft.NF;
-  double2 *tmp = dalloc<double2>((size_t)NF);
+  const long NH = c->fft.NH, NR = c->fft.NR;
+  double2 *tmp = dalloc<double2>((size_t)NH);
+  double *rbox = dalloc<double>((size_t)NR);
   for (int t = 0; t < 3; t++)
     for (auto &st : c->sten[t]) {
       if (st.L == 0 || !st.spec_fwd32.empty()) continue;
@@ -362,18 +429,18 @@ bool prepare_spec32(Ctx *c)
         const int nq = side == 0 ? st.nout_fwd : st.nin_tr;
         if (!coef) continue;
         for (int q = 0; q < nq; q++) {
-          tgpu::launch_fft_kernel_box(st.d_off, coef, st.L, nq, q, tmp, c->fft, c->stream);
-          tgpu::fft3d(tmp, c->fft, c->dg.ndim, false, c->stream);
-          float2 *k = dalloc<float2>((size_t)NF);
-          tgpu::launch_to_float2(tmp, k, NF, c->stream);
+          kernel_spectrum(c, st, side, q, rbox, tmp);
+          float2 *k = dalloc<float2>((size_t)NH);
+          tgpu::launch_to_float2(tmp, k, NH, c->stream);
           (side == 0 ? st.spec_fwd32 : st.spec_tr32).push_back(k);
         }
       }
     }
   ck(cudaStreamSynchronize(c->stream), "sync");
   dfree(tmp);
+  dfree(rbox);
   for (auto &b : c->d_fbox32)
-    if (!b) b = dalloc<float2>((size_t)NF);
+    if (!b) b = dalloc<float2>((size_t)NH);
   c->spec32_built = true;
   return true;
 }
@@ -382,11 +449,8 @@ bool prepare_spec32(Ctx *c)
 const float2 *fft_channel32(Ctx *c, int ch)
 {
   if (c->fft32_gen == c->pad_gen && c->fft32_ch == ch) return c->d_fbox32[0];
-  const tgpu::DevGeom &dg = c->dg;
-  const int P[3] = {dg.P[0], dg.P[1], dg.P[2]};
-  tgpu::launch_fft_load(c->d_pad32 + (long)ch * dg.NP, P, c->d_fbox32[0], c->fft, c->stream);
-  tgpu::fft3d(c->d_fbox32[0], c->fft, dg.ndim, false, c->stream);
-  c->stats.kernel_launches += 1 + dg.ndim;
+  tgpu::rfft_forward_mapped(map_src(c, ch), c->d_fbox32[0], c->fft, c->stream);
+  c->stats.kernel_launches += 3;
   c->fft32_gen = c->pad_gen;
   c->fft32_ch = ch;
   return c->d_fbox32[0];
@@ -394,27 +458,23 @@ const float2 *fft_channel32(Ctx *c, int ch)
 
 void fft_conv32(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
 {
-  const tgpu::DevGeom &dg = c->dg;
-  const long NF = c->fft.NF;
-  const int h[3] = {dg.h[0], dg.h[1], dg.h[2]}, nx[3] = {dg.nx[0], dg.nx[1], dg.nx[2]};
-  const double scale = 1.0 / (double)NF;
+  const long NH = c->fft.NH;
+  const double scale = 1.0 / (double)c->fft.NR;
   if (!tr) {
     const float2 *F = fft_channel32(c, ch0);
     for (int q = 0; q < nout; q++) {
-      tgpu::launch_spec_mul(F, st.spec_fwd32[q], c->d_fbox32[1], NF, false, c->stream);
-      tgpu::fft3d(c->d_fbox32[1], c->fft, dg.ndim, true, c->stream);
-      tgpu::launch_fft_extract(c->d_fbox32[1], c->fft, h, nx, scale, outs[q], c->stream);
-      c->stats.kernel_launches += 2 + dg.ndim;
+      tgpu::launch_spec_mul(F, st.spec_fwd32[q], c->d_fbox32[1], NH, false, c->stream);
+      tgpu::rfft_inverse(c->d_fbox32[1], c->fft, scale, outs[q], true, c->stream);
+      c->stats.kernel_launches += 4;
     }
   } else {
     for (int k = 0; k < nin; k++) {
       const float2 *F = fft_channel32(c, ch0 + k);
-      tgpu::launch_spec_mul(F, st.spec_tr32[k], c->d_fbox32[2], NF, k > 0, c->stream);
+      tgpu::launch_spec_mul(F, st.spec_tr32[k], c->d_fbox32[2], NH, k > 0, c->stream);
       c->stats.kernel_launches++;
     }
-    tgpu::fft3d(c->d_fbox32[2], c->fft, dg.ndim, true, c->stream);
-    tgpu::launch_fft_extract(c->d_fbox32[2], c->fft, h, nx, scale, outs[0], c->stream);
-    c->stats.kernel_launches += 1 + dg.ndim;
+    tgpu::rfft_inverse(c->d_fbox32[2], c->fft, scale, outs[0], true, c->stream);
+    c->stats.kernel_launches += 3;
   }
   c->stats.conv_launches++;
 }
@@ -432,27 +492,23 @@ bool use_fft32(const Ctx *c, const DevStencil &st, bool tr, int nin, int nout)
 
 void fft_conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
 {
-  const tgpu::DevGeom &dg = c->dg;
-  const long NF = c->fft.NF;
-  const int h[3] = {dg.h[0], dg.h[1], dg.h[2]}, nx[3] = {dg.nx[0], dg.nx[1], dg.nx[2]};
-  const double scale = 1.0 / (double)NF;
+  const long NH = c->fft.NH;
+  const double scale = 1.0 / (double)c->fft.NR;
   if (!tr) {
     const double2 *F = fft_channel(c, ch0);
     for (int q = 0; q < nout; q++) {
-      tgpu::launch_spec_mul(F, st.spec_fwd[q], c->d_fbox[1], NF, false, c->stream);
-      tgpu::fft3d(c->d_fbox[1], c->fft, dg.ndim, true, c->stream);
-      tgpu::launch_fft_extract(c->d_fbox[1], c->fft, h, nx, scale, outs[q], c->stream);
-      c->stats.kernel_launches += 2 + dg.ndim;
+      tgpu::launch_spec_mul(F, st.spec_fwd[q], c->d_fbox[1], NH, false, c->stream);
+      tgpu::rfft_inverse(c->d_fbox[1], c->fft, scale, outs[q], true, c->stream);
+      c->stats.kernel_launches += 4;
     }
   } else {
     for (int k = 0; k < nin; k++) {
       const double2 *F = fft_channel(c, ch0 + k);
-      tgpu::launch_spec_mul(F, st.spec_tr[k], c->d_fbox[2], NF, k > 0, c->stream);
+      tgpu::launch_spec_mul(F, st.spec_tr[k], c->d_fbox[2], NH, k > 0, c->stream);
       c->stats.kernel_launches++;
     }
-    tgpu::fft3d(c->d_fbox[2], c->fft, dg.ndim, true, c->stream);
-    tgpu::launch_fft_extract(c->d_fbox[2], c->fft, h, nx, scale, outs[0], c->stream);
-    c->stats.kernel_launches += 1 + dg.ndim;
+    tgpu::rfft_inverse(c->d_fbox[2], c->fft, scale, outs[0], true, c->stream);
+    c->stats.kernel_launches += 3;
   }
   c->stats.conv_launches++;
 }
@@ -469,6 +525,7 @@ void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const
     fft_conv32(c, ch0, nin, st, tr, outs, nout);
     return;
   }
+  materialize(c);   // the direct kernels below read the padded box
   if (f32 && c->tc_on && !tr && nin == 1 && nout == 1 && st.tc.nplanes > 0) {
     tgpu::launch_sten_tc(c->d_pad32 + (long)ch0 * NP, c->dg, c->tcslab, st.tc, outs[0], true, c->stream);
     c->stats.conv_launches++;
@@ -578,6 +635,8 @@ void decide_fft32(Ctx *c)
   ck(cudaEventElapsedTime(&t_fft, ev[2], ev[3]), "event");
   for (auto &e : ev) cudaEventDestroy(e);
   flag = t_fft < t_direct ? 1 : -1;
+  c->t32_att[c->tc_on ? 1 : 0][0] = 0.5f * t_direct;
+  c->t32_att[c->tc_on ? 1 : 0][1] = 0.5f * t_fft;
 }
 
 // The same choice for one short stencil (theta, delta) and direction: its FP32 slab / point sum against the
@@ -611,6 +670,8 @@ void decide_fft32_sten(Ctx *c, DevStencil &st, bool tr, int ch0, int nin, int no
   ck(cudaEventElapsedTime(&t_fft, ev[2], ev[3]), "event");
   for (auto &e : ev) cudaEventDestroy(e);
   flag = t_fft < t_direct ? 1 : -1;
+  st.t32[tr ? 1 : 0][0] = 0.5f * t_direct;
+  st.t32[tr ? 1 : 0][1] = 0.5f * t_fft;
 }
 
 // Weighted-density (and mean-field) sums of the padded density channels with one zone's stencils
@@ -889,7 +950,7 @@ void schur_device(Ctx *c, const double *d_v2, double *d_y2)
   const double *v2 = prolonged(c, d_v2, g.ncomp);
   forward_pass(c, v2, c->pads.rho_jac, f32);
   if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.N, c->cr, nullptr, c->stream);
-  tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
+  tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, hess_coef(c), c->stream, f32);
   transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, v2, c->d_tr, c->d_ymf, d_y2, c->stream);
   if (c->coarse()) tgpu::launch_zero_nodes(d_y2, g.ncomp, g.N, c->cr, c->stream);
@@ -904,7 +965,7 @@ void jv_device(Ctx *c, const double *d_v, double *d_out)
   const long N = c->dg.N;
   const bool f32 = prod_f32(c);
   forward_pass(c, d_v + (long)c->dg.first_rho * N, c->pads.rho_jac, f32);
-  tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, hess_coef(c), c->stream);
+  tgpu::launch_jv_local(c->d_x, d_v, c->d_chan, hess_coef(c), c->stream, f32);
   transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_jv_combine(c->d_x, c->d_vext, c->d_zero, d_v, c->d_conv, c->d_tr, d_out, c->stream);
   c->stats.kernel_launches += 2;
@@ -2500,6 +2561,29 @@ int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
       c->spec32_built = false;
       c->fft32_tc = c->fft32_slab = 0;
       c->fft32_gen = -1;
+    }
+    return TGPU_OK;
+  });
+}
+
+int tgpu_fft32_choice(tgpu_handle h, int type, int index, int *choice, double *ms)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (type < 0 || type > 2 || index < 0 || index >= (int)c->sten[type].size() || !choice || !ms)
+      throw Error(TGPU_ERR_ARG, "no such stencil");
+    const DevStencil &st = c->sten[type][index];
+    if (type == TGPU_STEN_UATT) {
+      const int ctx = c->precision == TGPU_FP16TC ? 1 : 0;
+      choice[0] = ctx ? c->fft32_tc : c->fft32_slab;
+      choice[1] = 0;
+      ms[0] = c->t32_att[ctx][0];
+      ms[1] = c->t32_att[ctx][1];
+      ms[2] = ms[3] = 0.0;
+    } else {
+      choice[0] = st.fft32_fwd;
+      choice[1] = st.fft32_tr;
+      for (int k = 0; k < 4; k++) ms[k] = st.t32[k / 2][k % 2];
     }
     return TGPU_OK;
   });

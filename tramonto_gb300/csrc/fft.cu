@@ -1,21 +1,32 @@
-// FP64 three-dimensional FFTs for the stencil sums of the accurate fills.
+// Three-dimensional real-to-complex FFTs for the stencil sums (FP64 in the accurate fills and FP64-accurate
+// products, FP32 in the FP32 products and fills).
 //
-// A stencil sum out(i) = sum_o c(o) f(i + h + o) over the padded box is a correlation; with the kernel
-// g[(-o) mod F] = c(o) it is the circular convolution (f * g)(i + h), exact for interior outputs when
-// every F_d >= P_d (the padded extent: i + h + o stays inside [0, P)).  So one forward transform of the
-// padded channel, a pointwise product with the kernel's spectrum (computed once per stencil coefficient)
-// and one inverse transform give a sum whose cost does not depend on the stencil's length: for the
-// 71 831-point attraction stencil at 128^3 that is ~2 transforms of 180^3 against 1.5e11 terms.
-// Rounding: FP64 FFTs with tabulated twiddles keep the error near eps log2(NF) of the sum's scale.
+// A stencil sum out(i) = sum_o c(o) f(i + o) over the mesh, with the reference's boundary rules, is a
+// correlation.  Along a periodic dimension of n nodes it is exactly the circular correlation of period n; along
+// any other dimension the padded channel (the field extended by the boundary rules over the stencil's reach h)
+// is transformed on a length F >= P = n + 2h, where the circular correlation equals the sum for every interior
+// output.  So the transform box is [F2][F1][F0] with F_d = n_d on periodic dimensions (when n_d is a product of
+// 2, 3 and 5) and the smallest such F_d >= P_d elsewhere; with the correlation kernel g[(-o) mod F] = c(o)
+// (points that wrap onto the same position add up, as the reference folds a stencil wider than a periodic box),
+// one forward transform of the field, a product with the kernel's spectrum and one inverse transform give the
+// sum at a cost that does not depend on the stencil's length.  At 128^3 with the attraction reach of 25 nodes
+// that is a 180 x 128 x 128 box: 2.9e6 points against 5.8e6 for a box padded in every dimension.
 //
-// Each axis is a batch of 1-D transforms.  A CTA loads kFftLines lines and the twiddle table into shared
-// memory (coalesced:
-// consecutive lines along x for the y and z axes, whole contiguous lines for x), runs the stages of a
-// mixed-radix Stockham autosort FFT there (radices 2, 3, 4, 5; the iteration of Govindaraju, Lloyd,
-// Dotsenko, Smith and Manferdelli, "High performance discrete Fourier transforms on graphics
-// processors", SC 2008: butterfly j reads j + r n/R, multiplies by W_{Ns R}^{r (j mod Ns)}, takes an
-// R-point DFT and writes (j / Ns) Ns R + (j mod Ns) + r Ns), and writes the lines back in place.
-// The inverse uses conjugate twiddles; its 1/NF goes into the extraction.
+// The field is real, so only the half spectrum k0 < F0/2 + 1 is kept ([F2][F1][F0/2 + 1] complex): along x two
+// real lines are packed as the real and imaginary parts of one complex line, transformed together and split
+// by Hermitian symmetry (A[k] = (Z[k] + conj Z[-k]) / 2, B[k] = (Z[k] - conj Z[-k]) / 2i); the inverse packs
+// two half-spectrum lines as Z = A + iB (extended by conjugate symmetry) and returns them as the real and
+// imaginary parts of one inverse transform.  The x passes read the padded channel directly and write the
+// interior outputs directly (no load or extraction pass); the y and z passes are batches of complex transforms
+// over the half-spectrum box.
+//
+// Each 1-D transform runs in shared memory as a mixed-radix Stockham autosort FFT (radices 2, 3, 4, 5; the
+// iteration of Govindaraju, Lloyd, Dotsenko, Smith and Manferdelli, "High performance discrete Fourier
+// transforms on graphics processors", SC 2008: butterfly j reads j + r n/R, multiplies by
+// W_{Ns R}^{r (j mod Ns)}, takes an R-point DFT and writes (j / Ns) Ns R + (j mod Ns) + r Ns).  The 3- and
+// 5-point DFTs use the symmetric forms that share the sums and differences of mirrored inputs (two real
+// multiplications per output pair instead of a full complex product per term).  Twiddles are tabulated on
+// the host in extended precision.  The inverse uses conjugate twiddles; its 1/(F0 F1 F2) is applied on output.
 #include <cmath>
 #include <vector>
 
@@ -25,16 +36,26 @@ namespace tgpu {
 
 namespace {
 
-constexpr int kFftLines = 8;
+constexpr int kFftLines = 8;     // complex lines per CTA tile
 constexpr int kFftThreads = 256;
-constexpr int kFftMaxN = 432;   // two ping-pong tiles of kFftLines lines and the twiddles fit in shared memory
+constexpr int kFftMaxN = 432;    // two ping-pong tiles of kFftLines lines and the twiddles fit in shared memory
 
 struct Stages {
   int nst;
   int rad[16];
 };
 
-// complex arithmetic on double2 (FP64 sums of the accurate fills) and float2 (FP32 sums of the products)
+template <class C>
+struct Real;
+template <>
+struct Real<double2> {
+  using T = double;
+};
+template <>
+struct Real<float2> {
+  using T = float;
+};
+
 template <class C>
 __device__ __forceinline__ C cmul(C a, C b)
 {
@@ -60,37 +81,58 @@ __device__ __forceinline__ C twiddle(const C *tw, int k, int inv)
   return w;
 }
 
-// R-point DFT of v in place (forward: exp(-2 pi i r k / R); inverse: conjugate); R known at compile time so
-// that v stays in registers
-template <int R, class C>
-__device__ __forceinline__ void dft_small(C *v, const C *tw, int n, int inv)
+// a + s (-i b) for the forward transform (s = +1), a + s (i b) for the inverse
+template <class C>
+__device__ __forceinline__ C add_mi(C a, C b, int inv)
 {
+  return inv ? C{a.x - b.y, a.y + b.x} : C{a.x + b.y, a.y - b.x};
+}
+template <class C>
+__device__ __forceinline__ C sub_mi(C a, C b, int inv)
+{
+  return inv ? C{a.x + b.y, a.y - b.x} : C{a.x - b.y, a.y + b.x};
+}
+
+// R-point DFT of v in place (forward: exp(-2 pi i r k / R); inverse: conjugate); R known at compile time so that
+// v stays in registers
+template <int R, class C>
+__device__ __forceinline__ void dft_small(C *v, int inv)
+{
+  using T = typename Real<C>::T;
   if (R == 2) {
     const C a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
+  } else if (R == 3) {
+    // y1,2 = v0 - (v1 + v2)/2 -/+ i (sqrt 3 / 2)(v1 - v2)
+    const T s3 = (T)0.86602540378443864676;
+    const C a = cadd(v[1], v[2]), b = csub(v[1], v[2]);
+    const C m = C{v[0].x - (T)0.5 * a.x, v[0].y - (T)0.5 * a.y};
+    const C s = C{s3 * b.x, s3 * b.y};
+    v[0] = cadd(v[0], a);
+    v[1] = add_mi(m, s, inv);
+    v[2] = sub_mi(m, s, inv);
   } else if (R == 4) {
-    const C y0 = cadd(v[0], v[2]), y1 = csub(v[0], v[2]), y2 = cadd(v[1], v[3]);
-    C y3 = csub(v[1], v[3]);
-    y3 = inv ? C{-y3.y, y3.x} : C{y3.y, -y3.x};   // times +i (inverse) or -i
+    const C y0 = cadd(v[0], v[2]), y1 = csub(v[0], v[2]), y2 = cadd(v[1], v[3]), y3 = csub(v[1], v[3]);
     v[0] = cadd(y0, y2);
     v[2] = csub(y0, y2);
-    v[1] = cadd(y1, y3);
-    v[3] = csub(y1, y3);
+    v[1] = add_mi(y1, y3, inv);
+    v[3] = sub_mi(y1, y3, inv);
   } else {
-    C w[R];   // W_R^m from the table: W_n^(m n / R)
-#pragma unroll
-    for (int m = 0; m < R; m++) w[m] = twiddle(tw, m * (n / R), inv);
-    C o[R];
-#pragma unroll
-    for (int k = 0; k < R; k++) {
-      C s = v[0];
-#pragma unroll
-      for (int r = 1; r < R; r++) s = cadd(s, cmul(v[r], w[(r * k) % R]));
-      o[k] = s;
-    }
-#pragma unroll
-    for (int k = 0; k < R; k++) v[k] = o[k];
+    // 5 points: with a1 = v1 + v4, b1 = v1 - v4, a2 = v2 + v3, b2 = v2 - v3,
+    // y1,4 = v0 + c1 a1 + c2 a2 -/+ i (s1 b1 + s2 b2),  y2,3 = v0 + c2 a1 + c1 a2 -/+ i (s2 b1 - s1 b2)
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+    const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+    const C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]), a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    const C m1 = C{v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y};
+    const C m2 = C{v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y};
+    const C n1 = C{s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y};
+    const C n2 = C{s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y};
+    v[0] = C{v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y};
+    v[1] = add_mi(m1, n1, inv);
+    v[4] = sub_mi(m1, n1, inv);
+    v[2] = add_mi(m2, n2, inv);
+    v[3] = sub_mi(m2, n2, inv);
   }
 }
 
@@ -107,16 +149,18 @@ __device__ __forceinline__ void fft_stage(const C *in, C *out, int n, int ls, in
 #pragma unroll
     for (int r = 0; r < R; r++) v[r] = src[j + r * nb];
     const int k = j % Ns;
+    if (Ns > 1) {
 #pragma unroll
-    for (int r = 1; r < R; r++) v[r] = cmul(v[r], twiddle(tw, r * k * step, inv));
-    dft_small<R, C>(v, tw, n, inv);
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], twiddle(tw, r * k * step, inv));
+    }
+    dft_small<R, C>(v, inv);
     const int idx = (j / Ns) * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; r++) dst[idx + r * Ns] = v[r];
   }
 }
 
-// stages of one tile of kFftLines lines (line stride ls) from buf0; returns the buffer holding the result
+// stages of one tile of nlines lines (line stride ls) from buf0; returns the buffer holding the result
 template <class C>
 __device__ C *fft_tile(C *buf0, C *buf1, int n, int ls, int nlines, const Stages &st, const C *tw, int inv)
 {
@@ -139,33 +183,135 @@ __device__ C *fft_tile(C *buf0, C *buf1, int n, int ls, int nlines, const Stages
   return in;
 }
 
-// axis 0: lines along x (contiguous), kFftLines consecutive lines per CTA
-template <class C>
-__global__ void __launch_bounds__(kFftThreads) k_fft_x(C *box, int F0, long nlines_total, Stages st,
-                                                     const C *__restrict__ tw_g, int inv)
+// Geometry of the real box as the x passes see it: where a line's values come from (forward) or go to (inverse)
+struct XGeom {
+  int F0, F1, Fh;            // transform lengths along x and y, half-spectrum length along x
+  long nlines;               // real lines F1 * F2
+  // forward source: element (x, y, z) of the box is the source at padded position (x + off0, y + off1, z + off2)
+  // when x < ext0, y < ext1, z < ext2, else 0
+  int off[3], ext[3];
+  // inverse destination: box position p holds output node p - e (interior nodes only)
+  int e[3], nx[3];
+};
+
+// Sources of the forward x pass: element (x, y, z) of the real box (x < ext0, y < ext1, z < ext2; 0 beyond)
+// at padded position (x + off0, y + off1, z + off2)
+template <class T>
+struct BoxSrc {   // a padded channel, or a real box [F2][F1][F0] (off 0)
+  const T *p;
+  long sy, sz;
+  __device__ __forceinline__ T operator()(const XGeom &g, int x, int y, int z) const
+  {
+    return p[(long)(z + g.off[2]) * sz + (long)(y + g.off[1]) * sy + x + g.off[0]];
+  }
+};
+template <class T>
+struct MappedSrc {   // the unpadded channel through the boundary maps (the padded box's values, computed)
+  MapSrc m;
+  __device__ __forceinline__ T operator()(const XGeom &g, int x, int y, int z) const
+  {
+    const int q[3] = {x + g.off[0], y + g.off[1], z + g.off[2]};
+    int idx[3] = {0, 0, 0}, refl = 0;
+    for (int d = 0; d < m.ndim; d++) {
+      const int v = m.map[d][q[d]];
+      if (v < 0) {   // the first out-of-range dimension decides (the reference's order)
+        if (v == kSentBulk) return (T)m.bulk_lo;
+        if (v == kSentBulkHi) return (T)m.bulk_hi;
+        if (v == kSentWall) return (T)0;
+        return (T)__longlong_as_double(0x7ff8000000000000ULL);   // no node to read (as the padded box holds)
+      }
+      if (v & kReflBit) refl |= 1 << d;
+      idx[d] = v & ~kReflBit;
+    }
+    const long node = idx[0] + (long)m.nx[0] * (idx[1] + (long)m.nx[1] * idx[2]);
+    if (m.zc >= 0 && m.zero[(long)m.zc * m.N + node]) return (T)0;
+    const double v = m.src[node];
+    return (T)((__popc(refl & m.signmask) & 1) ? -v : v);
+  }
+};
+
+// x pass of the forward transform: two real lines per complex line, split into two half-spectrum lines
+template <class T, class C, class Src>
+__global__ void __launch_bounds__(kFftThreads) k_rfft_x(Src src, XGeom g, Stages st, const C *__restrict__ tw_g,
+                                                      C *__restrict__ spec)
 {
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
-  const int n = F0, ls = n + 1;
+  const int n = g.F0, ls = n + 1;
   C *b0 = sm, *b1 = sm + kFftLines * ls, *tw = b1 + kFftLines * ls;
   for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
-  const long l0 = (long)blockIdx.x * kFftLines;
-  const int nl = (int)min((long)kFftLines, nlines_total - l0);
-  for (int q = threadIdx.x; q < nl * n; q += blockDim.x) {
-    const int l = q / n, e = q - l * n;
-    b0[l * ls + e] = box[(l0 + l) * n + e];
+  const long pair0 = (long)blockIdx.x * kFftLines;
+  const long npairs = (g.nlines + 1) / 2;
+  const int np = (int)min((long)kFftLines, npairs - pair0);
+  for (int q = threadIdx.x; q < np * n; q += blockDim.x) {
+    const int l = q / n, x = q - l * n;
+    T v[2] = {0, 0};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const long L = 2 * (pair0 + l) + h;
+      if (L >= g.nlines) break;
+      const int y = (int)(L % g.F1), z = (int)(L / g.F1);
+      if (x < g.ext[0] && y < g.ext[1] && z < g.ext[2]) v[h] = src(g, x, y, z);
+    }
+    b0[l * ls + x] = C{v[0], v[1]};
   }
   __syncthreads();
-  const C *res = fft_tile<C>(b0, b1, n, ls, nl, st, tw, inv);
-  for (int q = threadIdx.x; q < nl * n; q += blockDim.x) {
-    const int l = q / n, e = q - l * n;
-    box[(l0 + l) * n + e] = res[l * ls + e];
+  const C *res = fft_tile<C>(b0, b1, n, ls, np, st, tw, 0);
+  using R = T;
+  for (int q = threadIdx.x; q < np * g.Fh; q += blockDim.x) {
+    const int l = q / g.Fh, k = q - l * g.Fh;
+    const C Z = res[l * ls + k], Zm = res[l * ls + (k == 0 ? 0 : n - k)];
+    const long L = 2 * (pair0 + l);
+    spec[L * g.Fh + k] = C{(R)0.5 * (Z.x + Zm.x), (R)0.5 * (Z.y - Zm.y)};
+    if (L + 1 < g.nlines) spec[(L + 1) * g.Fh + k] = C{(R)0.5 * (Z.y + Zm.y), (R)0.5 * (Zm.x - Z.x)};
   }
 }
 
-// axes 1 and 2: lines of element stride es; a CTA takes kFftLines consecutive x at one (outer) index
+// x pass of the inverse transform: two half-spectrum lines as one complex line, written out as the real outputs
+// of the interior nodes (out[node] = scale * value, or += when accumulate)
 template <class C>
-__global__ void __launch_bounds__(kFftThreads) k_fft_strided(C *box, int F0, int n, long es, long outer_stride,
+__global__ void __launch_bounds__(kFftThreads) k_irfft_x(const C *__restrict__ spec, XGeom g, Stages st,
+                                                       const C *__restrict__ tw_g, double scale,
+                                                       double *__restrict__ out, int accumulate)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *sm = reinterpret_cast<C *>(smraw);
+  const int n = g.F0, ls = n + 1;
+  C *b0 = sm, *b1 = sm + kFftLines * ls, *tw = b1 + kFftLines * ls;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
+  const long pair0 = (long)blockIdx.x * kFftLines;
+  const long npairs = (g.nlines + 1) / 2;
+  const int np = (int)min((long)kFftLines, npairs - pair0);
+  for (int q = threadIdx.x; q < np * n; q += blockDim.x) {
+    const int l = q / n, k = q - l * n;
+    const long L = 2 * (pair0 + l);
+    const bool up = k < g.Fh;
+    const int kk = up ? k : n - k;
+    const C A = spec[L * g.Fh + kk];
+    const C B = L + 1 < g.nlines ? spec[(L + 1) * g.Fh + kk] : C{0, 0};
+    // Z = A + iB on the stored half; conj(A) + i conj(B) on the mirrored half
+    b0[l * ls + k] = up ? C{A.x - B.y, A.y + B.x} : C{A.x + B.y, B.x - A.y};
+  }
+  __syncthreads();
+  const C *res = fft_tile<C>(b0, b1, n, ls, np, st, tw, 1);
+  const int nx0 = g.nx[0];
+  for (int q = threadIdx.x; q < np * 2 * nx0; q += blockDim.x) {
+    const int lh = q / nx0, x = q - lh * nx0;
+    const int l = lh >> 1, h = lh & 1;
+    const long L = 2 * (pair0 + l) + h;
+    if (L >= g.nlines) continue;
+    const int y = (int)(L % g.F1) - g.e[1], z = (int)(L / g.F1) - g.e[2];
+    if (y < 0 || y >= g.nx[1] || z < 0 || z >= g.nx[2]) continue;
+    const C r = res[l * ls + x + g.e[0]];
+    const double v = scale * (double)(h ? r.y : r.x);
+    double *o = out + ((long)z * g.nx[1] + y) * nx0 + x;
+    *o = accumulate ? *o + v : v;
+  }
+}
+
+// y and z passes: lines of element stride es; a CTA takes kFftLines consecutive x at one (outer) index
+template <class C>
+__global__ void __launch_bounds__(kFftThreads) k_fft_strided(C *box, int X, int n, long es, long outer_stride,
                                                            Stages st, const C *__restrict__ tw_g, int inv)
 {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -173,10 +319,10 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(C *box, int F0, int
   const int ls = n + 1;
   C *b0 = sm, *b1 = sm + kFftLines * ls, *tw = b1 + kFftLines * ls;
   for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
-  const int xblocks = (F0 + kFftLines - 1) / kFftLines;
+  const int xblocks = (X + kFftLines - 1) / kFftLines;
   const int x0 = (blockIdx.x % xblocks) * kFftLines;
   const long base = (long)(blockIdx.x / xblocks) * outer_stride + x0;
-  const int nl = min(kFftLines, F0 - x0);
+  const int nl = min(kFftLines, X - x0);
   for (int q = threadIdx.x; q < kFftLines * n; q += blockDim.x) {
     const int e = q / kFftLines, l = q - e * kFftLines;
     if (l < nl) b0[l * ls + e] = box[base + e * es + l];
@@ -189,29 +335,17 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(C *box, int F0, int
   }
 }
 
-template <class T, class C>
-__global__ void k_fft_load(const T *__restrict__ pad, int P0, int P1, int P2, C *__restrict__ box, int F0, int F1,
-                           long NF)
-{
-  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < NF; q += (long)gridDim.x * blockDim.x) {
-    const int x = (int)(q % F0);
-    const long r = q / F0;
-    const int y = (int)(r % F1), z = (int)(r / F1);
-    T v = 0;
-    if (x < P0 && y < P1 && z < P2) v = pad[((long)z * P1 + y) * P0 + x];
-    box[q] = C{v, 0};
-  }
-}
-
+// correlation kernel of coefficient q of a stencil in the real box: coef[k * ncoef + q] added at (-offset_k) mod F
+// (offsets that wrap onto the same position add up)
 __global__ void k_fft_kernel_box(const short *__restrict__ off3, const double *__restrict__ coef, int L, int ncoef,
-                                 int q, double2 *__restrict__ box, int F0, int F1, int F2)
+                                 int q, double *__restrict__ box, int F0, int F1, int F2)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= L) return;
   const int x = ((-(int)off3[3 * k]) % F0 + F0) % F0;
   const int y = ((-(int)off3[3 * k + 1]) % F1 + F1) % F1;
   const int z = ((-(int)off3[3 * k + 2]) % F2 + F2) % F2;
-  box[((long)z * F1 + y) * F0 + x] = make_double2(coef[(long)k * ncoef + q], 0.0);
+  atomicAdd(box + ((long)z * F1 + y) * F0 + x, coef[(long)k * ncoef + q]);
 }
 
 template <class C>
@@ -223,18 +357,6 @@ __global__ void k_spec_mul(const C *__restrict__ a, const C *__restrict__ k, C *
   }
 }
 
-template <class C>
-__global__ void k_fft_extract(const C *__restrict__ box, int F0, int F1, int h0, int h1, int h2, int nx0, int nx1,
-                              long N, double scale, double *__restrict__ out)
-{
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % nx0);
-    const long r = i / nx0;
-    const int y = (int)(r % nx1), z = (int)(r / nx1);
-    out[i] += (double)box[((long)(z + h2) * F1 + (y + h1)) * F0 + (x + h0)].x * scale;
-  }
-}
-
 __global__ void k_to_float2(const double2 *__restrict__ in, float2 *__restrict__ out, long n)
 {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -243,16 +365,18 @@ __global__ void k_to_float2(const double2 *__restrict__ in, float2 *__restrict__
 
 int grid_for(long n) { return (int)std::min<long>((n + 255) / 256, 152L * 16); }
 
-// smallest F >= P that is a product of 2, 3, 5, and its radix list (4s first)
-bool choose(int P, int &F, Stages &st)
+bool smooth(int F)
 {
-  for (F = std::max(P, 1); F <= kFftMaxN; F++) {
-    int m = F;
-    for (int r : {2, 3, 5})
-      while (m % r == 0) m /= r;
-    if (m == 1) break;
-  }
-  if (F > kFftMaxN) return false;
+  int m = F;
+  for (int r : {2, 3, 5})
+    while (m % r == 0) m /= r;
+  return m == 1;
+}
+
+// radix list of a length (4s first)
+bool stages_of(int F, Stages &st)
+{
+  if (F < 1 || F > kFftMaxN || !smooth(F)) return false;
   int m = F;
   st.nst = 0;
   while (m % 4 == 0) { st.rad[st.nst++] = 4; m /= 4; }
@@ -262,61 +386,123 @@ bool choose(int P, int &F, Stages &st)
   return st.nst <= 16;
 }
 
+Stages stages(const FftAxis &a)
+{
+  Stages st{};
+  st.nst = a.nst;
+  for (int k = 0; k < a.nst; k++) st.rad[k] = a.rad[k];
+  return st;
+}
+
 template <class C>
 size_t tile_smem(int n)
 {
   return sizeof(C) * (2 * (size_t)kFftLines * (n + 1) + n);
 }
 
-template <class C>
-void set_smem_limits(const FftPlan &p, int ndim)
+template <class T, class C>
+void set_smem_limits(const FftPlan &p)
 {
-  size_t sx = tile_smem<C>(p.F[0]), ss = 0;
-  for (int d = 1; d < ndim; d++) ss = std::max(ss, tile_smem<C>(p.F[d]));
-  cudaFuncSetAttribute(k_fft_x<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx);
-  if (ss) cudaFuncSetAttribute(k_fft_strided<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss);
+  const int sx = (int)tile_smem<C>(p.F[0]);
+  cudaFuncSetAttribute(k_rfft_x<T, C, BoxSrc<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+  cudaFuncSetAttribute(k_rfft_x<T, C, MappedSrc<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+  cudaFuncSetAttribute(k_irfft_x<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+  const int ss = (int)std::max(tile_smem<C>(p.F[1]), tile_smem<C>(p.F[2]));
+  cudaFuncSetAttribute(k_fft_strided<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss);
+}
+
+XGeom xgeom(const FftPlan &p)
+{
+  XGeom g{};
+  g.F0 = p.F[0];
+  g.F1 = p.F[1];
+  g.Fh = p.Fh;
+  g.nlines = (long)p.F[1] * p.F[2];
+  for (int d = 0; d < 3; d++) {
+    g.off[d] = p.off[d];
+    g.ext[d] = p.ext[d];
+    g.e[d] = p.h[d] - p.off[d];
+    g.nx[d] = p.nx[d];
+  }
+  return g;
+}
+
+// forward y and z passes (inverse: z then y) over the half-spectrum box
+template <class C>
+void yz_passes(C *spec, const FftPlan &p, bool inverse, const C *const *tw, cudaStream_t s)
+{
+  const int X = p.Fh;
+  const int xblocks = (X + kFftLines - 1) / kFftLines;
+  for (int k = 0; k < 2; k++) {
+    const int d = inverse ? 2 - k : 1 + k;
+    const int n = p.F[d];
+    if (n == 1) continue;
+    const long es = d == 1 ? (long)X : (long)X * p.F[1];
+    const long outer = d == 1 ? (long)X * p.F[1] : (long)X;   // axis 1: outer index z; axis 2: outer index y
+    const long nouter = d == 1 ? p.F[2] : p.F[1];
+    k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, tile_smem<C>(n), s>>>(
+        spec, X, n, es, outer, stages(p.ax[d]), tw[d], inverse ? 1 : 0);
+  }
+}
+
+template <class T, class C, class Src>
+void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, const C *const *tw, cudaStream_t s)
+{
+  XGeom g = xgeom(p);
+  if (!padded)   // a real box [F2][F1][F0]
+    for (int d = 0; d < 3; d++) {
+      g.off[d] = 0;
+      g.ext[d] = p.F[d];
+    }
+  const long npairs = (g.nlines + 1) / 2;
+  k_rfft_x<T, C, Src><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
+      src, g, stages(p.ax[0]), tw[0], spec);
+  yz_passes<C>(spec, p, false, tw, s);
 }
 
 template <class C>
-void fft3d_impl(C *box, const FftPlan &p, int ndim, bool inverse, const C *const *tw, cudaStream_t s)
+void rfft_inverse_impl(C *spec, const FftPlan &p, double scale, double *out, bool accumulate, const C *const *tw,
+                       cudaStream_t s)
 {
-  const int F0 = p.F[0], F1 = p.F[1], F2 = p.F[2];
-  for (int d = 0; d < ndim; d++) {
-    const FftAxis &a = p.ax[d];
-    Stages st{};
-    st.nst = a.nst;
-    for (int k = 0; k < a.nst; k++) st.rad[k] = a.rad[k];
-    const size_t sm = tile_smem<C>(a.n);
-    if (d == 0) {
-      const long nl = (long)F1 * F2;
-      k_fft_x<C><<<(unsigned)((nl + kFftLines - 1) / kFftLines), kFftThreads, sm, s>>>(box, F0, nl, st, tw[d],
-                                                                                       inverse ? 1 : 0);
-    } else {
-      const int xblocks = (F0 + kFftLines - 1) / kFftLines;
-      const long es = d == 1 ? (long)F0 : (long)F0 * F1;
-      const long outer = d == 1 ? (long)F0 * F1 : (long)F0;   // axis 1: outer index z; axis 2: outer index y
-      const long nouter = d == 1 ? F2 : F1;
-      k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, sm, s>>>(box, F0, a.n, es, outer, st, tw[d],
-                                                                             inverse ? 1 : 0);
-    }
-  }
+  yz_passes<C>(spec, p, true, tw, s);
+  const XGeom g = xgeom(p);
+  const long npairs = (g.nlines + 1) / 2;
+  k_irfft_x<C><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
+      spec, g, stages(p.ax[0]), tw[0], scale, out, accumulate ? 1 : 0);
 }
 
 }  // namespace
 
-bool fft_make_plan(FftPlan &p, const int P[3], int ndim, cudaStream_t s)
+bool fft_make_plan(FftPlan &p, const int P[3], const int nx[3], const int h[3], const int periodic[3], int ndim,
+                   cudaStream_t s)
 {
-  p.NF = 1;
+  p.NR = 1;
   for (int d = 0; d < 3; d++) {
     FftAxis &a = p.ax[d];
+    p.P[d] = d < ndim ? P[d] : 1;
+    p.nx[d] = d < ndim ? nx[d] : 1;
+    p.h[d] = d < ndim ? h[d] : 0;
     if (d >= ndim) {
       p.F[d] = 1;
+      p.off[d] = 0;
+      p.ext[d] = 1;
       a.n = 1;
       a.nst = 0;
       continue;
     }
     Stages st{};
-    if (!choose(P[d], p.F[d], st)) return false;
+    if (periodic[d] && stages_of(nx[d], st)) {   // the period itself: no padding
+      p.F[d] = nx[d];
+      p.off[d] = h[d];
+      p.ext[d] = nx[d];
+    } else {
+      int F = P[d];
+      while (F <= kFftMaxN && !smooth(F)) F++;
+      if (!stages_of(F, st)) return false;
+      p.F[d] = F;
+      p.off[d] = 0;
+      p.ext[d] = P[d];
+    }
     a.n = p.F[d];
     a.nst = st.nst;
     for (int k = 0; k < st.nst; k++) a.rad[k] = st.rad[k];
@@ -333,10 +519,12 @@ bool fft_make_plan(FftPlan &p, const int P[3], int ndim, cudaStream_t s)
     cudaMemcpyAsync(a.d_tw, tw.data(), sizeof(double2) * a.n, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(a.d_tw32, tw32.data(), sizeof(float2) * a.n, cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);   // the host tables go out of scope
-    p.NF *= p.F[d];
+    p.NR *= p.F[d];
   }
-  set_smem_limits<double2>(p, ndim);
-  set_smem_limits<float2>(p, ndim);
+  p.Fh = p.F[0] / 2 + 1;
+  p.NH = (long)p.Fh * p.F[1] * p.F[2];
+  set_smem_limits<double, double2>(p);
+  set_smem_limits<float, float2>(p);
   return true;
 }
 
@@ -350,32 +538,52 @@ void fft_free_plan(FftPlan &p)
   }
 }
 
-void fft3d(double2 *box, const FftPlan &p, int ndim, bool inverse, cudaStream_t s)
+void rfft_forward(const double *pad, double2 *spec, const FftPlan &p, cudaStream_t s)
 {
   const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
-  fft3d_impl<double2>(box, p, ndim, inverse, tw, s);
+  rfft_forward_impl<double, double2>(BoxSrc<double>{pad, p.P[0], (long)p.P[0] * p.P[1]}, true, spec, p, tw, s);
 }
 
-void fft3d(float2 *box, const FftPlan &p, int ndim, bool inverse, cudaStream_t s)
+void rfft_forward(const float *pad, float2 *spec, const FftPlan &p, cudaStream_t s)
 {
   const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
-  fft3d_impl<float2>(box, p, ndim, inverse, tw, s);
+  rfft_forward_impl<float, float2>(BoxSrc<float>{pad, p.P[0], (long)p.P[0] * p.P[1]}, true, spec, p, tw, s);
 }
 
-void launch_fft_load(const double *pad, const int P[3], double2 *box, const FftPlan &p, cudaStream_t s)
+void rfft_forward_mapped(const MapSrc &m, double2 *spec, const FftPlan &p, cudaStream_t s)
 {
-  k_fft_load<double, double2><<<grid_for(p.NF), 256, 0, s>>>(pad, P[0], P[1], P[2], box, p.F[0], p.F[1], p.NF);
+  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
+  rfft_forward_impl<double, double2>(MappedSrc<double>{m}, true, spec, p, tw, s);
 }
 
-void launch_fft_load(const float *pad, const int P[3], float2 *box, const FftPlan &p, cudaStream_t s)
+void rfft_forward_mapped(const MapSrc &m, float2 *spec, const FftPlan &p, cudaStream_t s)
 {
-  k_fft_load<float, float2><<<grid_for(p.NF), 256, 0, s>>>(pad, P[0], P[1], P[2], box, p.F[0], p.F[1], p.NF);
+  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
+  rfft_forward_impl<float, float2>(MappedSrc<float>{m}, true, spec, p, tw, s);
 }
 
-void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double2 *box,
+void rfft_forward_box(const double *box, double2 *spec, const FftPlan &p, cudaStream_t s)
+{
+  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
+  rfft_forward_impl<double, double2>(BoxSrc<double>{box, p.F[0], (long)p.F[0] * p.F[1]}, false, spec, p, tw, s);
+}
+
+void rfft_inverse(double2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
+{
+  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
+  rfft_inverse_impl<double2>(spec, p, scale, out, accumulate, tw, s);
+}
+
+void rfft_inverse(float2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
+{
+  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
+  rfft_inverse_impl<float2>(spec, p, scale, out, accumulate, tw, s);
+}
+
+void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double *box,
                            const FftPlan &p, cudaStream_t s)
 {
-  cudaMemsetAsync(box, 0, sizeof(double2) * p.NF, s);
+  cudaMemsetAsync(box, 0, sizeof(double) * p.NR, s);
   if (L > 0) k_fft_kernel_box<<<(L + 255) / 256, 256, 0, s>>>(off3, coef, L, ncoef, q, box, p.F[0], p.F[1], p.F[2]);
 }
 
@@ -392,22 +600,6 @@ void launch_spec_mul(const double2 *a, const double2 *k, double2 *out, long n, b
 void launch_spec_mul(const float2 *a, const float2 *k, float2 *out, long n, bool accumulate, cudaStream_t s)
 {
   k_spec_mul<float2><<<grid_for(n), 256, 0, s>>>(a, k, out, n, accumulate ? 1 : 0);
-}
-
-void launch_fft_extract(const double2 *box, const FftPlan &p, const int h[3], const int nx[3], double scale,
-                        double *out, cudaStream_t s)
-{
-  const long N = (long)nx[0] * nx[1] * nx[2];
-  k_fft_extract<double2><<<grid_for(N), 256, 0, s>>>(box, p.F[0], p.F[1], h[0], h[1], h[2], nx[0], nx[1], N, scale,
-                                                     out);
-}
-
-void launch_fft_extract(const float2 *box, const FftPlan &p, const int h[3], const int nx[3], double scale,
-                        double *out, cudaStream_t s)
-{
-  const long N = (long)nx[0] * nx[1] * nx[2];
-  k_fft_extract<float2><<<grid_for(N), 256, 0, s>>>(box, p.F[0], p.F[1], h[0], h[1], h[2], nx[0], nx[1], N, scale,
-                                                    out);
 }
 
 }  // namespace tgpu

@@ -706,6 +706,38 @@ __device__ __forceinline__ void hess_apply_node(const double *x, const double *c
   fmt_hess_apply_coef(c, n, y, z, c_g.ndim, false);
 }
 
+// the same in arithmetic T from the state's Hessian scalars (coef must be given)
+template <class T>
+__device__ __forceinline__ void hess_apply_node_t(const double *x, const double *coef, long i, const T *y, T *z)
+{
+  const long N = c_g.N;
+  const int nd = c_g.ndim;
+  const double *rb = x + (long)c_g.first_rb * N;
+  T n[kMaxRb];
+  n[0] = (T)rb[3 * N + i];
+  n[1] = (T)rb[2 * N + i];
+  n[2] = (T)rb[1 * N + i];
+  n[3] = (T)rb[i];
+  for (int d = 0; d < nd; d++) {
+    n[4 + d] = (T)rb[(4 + nd + d) * N + i];
+    n[4 + nd + d] = (T)rb[(4 + d) * N + i];
+  }
+  HessCoefT<T> c;
+  c.a = (T)coef[i];
+  c.a2 = (T)coef[N + i];
+  c.h13 = (T)coef[2 * N + i];
+  c.h22 = (T)coef[3 * N + i];
+  c.h23 = (T)coef[4 * N + i];
+  c.h33 = (T)coef[5 * N + i];
+  c.ff = (T)coef[6 * N + i];
+  c.gvf1 = (T)coef[7 * N + i];
+  c.g2vr_f = (T)coef[8 * N + i];
+  c.g2vc_f = (T)coef[9 * N + i];
+  c.gvv = (T)coef[10 * N + i];
+  c.gvv_out = (T)coef[11 * N + i];
+  fmt_hess_apply_coef(c, n, y, z, nd, false);
+}
+
 __global__ void k_hess_coef(const double *__restrict__ x, double *__restrict__ coef)
 {
   const long N = c_g.N;
@@ -725,17 +757,19 @@ void launch_hess_coef(const double *x, double *coef, cudaStream_t s)
 }
 
 // Transpose-convolution channels from a weighted-density-shaped vector q (n ordering):
-// per component A = fac (q0/4piR^2 + q1/4piR + q2), B_d = fac (q_V1d/4piR + q_V2d), C = fac q3.
-__device__ __forceinline__ void write_tr_channels(const double *q, double *chan, long i)
+// per component A = fac (q0/4piR^2 + q1/4piR + q2), B_d = fac (q_V1d/4piR + q_V2d), C = fac q3
+// (formed in the arithmetic of q, stored in FP64)
+template <class T>
+__device__ __forceinline__ void write_tr_channels(const T *q, double *chan, long i)
 {
   const int nd = c_g.ndim;
   const long N = c_g.N;
   for (int ic = 0; ic < c_g.ncomp; ic++) {
-    const double f = c_g.fac[ic];
+    const T f = (T)c_g.fac[ic], i4pr = (T)c_g.inv_4pir[ic], i4pr2 = (T)c_g.inv_4pirsq[ic];
     const long base = (long)ic * (nd + 2);
-    chan[base * N + i] = f * (q[0] * c_g.inv_4pirsq[ic] + q[1] * c_g.inv_4pir[ic] + q[2]);
-    for (int d = 0; d < nd; d++) chan[(base + 1 + d) * N + i] = f * (q[4 + d] * c_g.inv_4pir[ic] + q[4 + nd + d]);
-    chan[(base + nd + 1) * N + i] = f * q[3];
+    chan[base * N + i] = (double)(f * (q[0] * i4pr2 + q[1] * i4pr + q[2]));
+    for (int d = 0; d < nd; d++) chan[(base + 1 + d) * N + i] = (double)(f * (q[4 + d] * i4pr + q[4 + nd + d]));
+    chan[(base + nd + 1) * N + i] = (double)(f * q[3]);
   }
 }
 
@@ -831,23 +865,25 @@ void launch_assemble(const double *x, const double *vext, const signed char *zer
 
 // Schur local step: y1 = A11^-1 u (u = A12 v in conv), then the EL-side
 // channels of H y1 for the transpose sums; y_MF = -u_MF kept for A21.
+// T = double, or float for FP32 products (then coef must hold the state's Hessian scalars)
+template <class T>
 __global__ void k_schur_local(const double *__restrict__ x, const double *__restrict__ conv,
                               double *__restrict__ chan, double *__restrict__ ymf, const double *__restrict__ coef)
 {
   const long N = c_g.N;
   const int nd = c_g.ndim;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-    double ysv[kMaxRb], y[kMaxRb], n[kMaxRb], z[kMaxRb];
+    T ysv[kMaxRb], y[kMaxRb], z[kMaxRb];
     for (int k = 0; k < c_g.nrb; k++) {
       int src;
       double c;
-      if (dep_rb(k, &src, &c)) ysv[k] = -c * conv[(long)src * N + i];   // -u_dep - B u_ind, u_dep = 0
-      else ysv[k] = -conv[(long)k * N + i];
+      if (dep_rb(k, &src, &c)) ysv[k] = (T)(-c * conv[(long)src * N + i]);   // -u_dep - B u_ind, u_dep = 0
+      else ysv[k] = (T)(-conv[(long)k * N + i]);
     }
     y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
     for (int d = 0; d < nd; d++) { y[4 + d] = ysv[4 + nd + d]; y[4 + nd + d] = ysv[4 + d]; }
-    (void)n;
-    hess_apply_node(x, coef, i, y, z);
+    if constexpr (sizeof(T) == sizeof(double)) hess_apply_node(x, coef, i, y, z);
+    else hess_apply_node_t<T>(x, coef, i, y, z);
     write_tr_channels(z, chan, i);
     if (c_g.attraction)
       for (int ic = 0; ic < c_g.ncomp; ic++) ymf[(long)ic * N + i] = -conv[(long)(c_g.nrb + ic) * N + i];
@@ -855,27 +891,39 @@ __global__ void k_schur_local(const double *__restrict__ x, const double *__rest
 }
 
 void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
-                        cudaStream_t s)
+                        cudaStream_t s, bool f32)
 {
-  k_schur_local<<<1184, kThreads, 0, s>>>(x, conv, chan, ymf, coef);
+  if (f32 && coef) k_schur_local<float><<<1184, kThreads, 0, s>>>(x, conv, chan, ymf, coef);
+  else k_schur_local<double><<<1184, kThreads, 0, s>>>(x, conv, chan, ymf, coef);
 }
 
 // J v local step: channels of H v_rb for the EL rows.
+template <class T>
 __global__ void k_jv_local(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ chan,
                            const double *__restrict__ coef)
 {
   const long N = c_g.N;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-    double y[kMaxRb], z[kMaxRb];
-    load_n(v, i, y);
-    hess_apply_node(x, coef, i, y, z);
+    T z[kMaxRb];
+    if constexpr (sizeof(T) == sizeof(double)) {
+      double y[kMaxRb];
+      load_n(v, i, y);
+      hess_apply_node(x, coef, i, y, z);
+    } else {
+      double yd[kMaxRb];
+      T y[kMaxRb];
+      load_n(v, i, yd);
+      for (int k = 0; k < c_g.nrb; k++) y[k] = (T)yd[k];
+      hess_apply_node_t<T>(x, coef, i, y, z);
+    }
     write_tr_channels(z, chan, i);
   }
 }
 
-void launch_jv_local(const double *x, const double *v, double *chan, const double *coef, cudaStream_t s)
+void launch_jv_local(const double *x, const double *v, double *chan, const double *coef, cudaStream_t s, bool f32)
 {
-  k_jv_local<<<1184, kThreads, 0, s>>>(x, v, chan, coef);
+  if (f32 && coef) k_jv_local<float><<<1184, kThreads, 0, s>>>(x, v, chan, coef);
+  else k_jv_local<double><<<1184, kThreads, 0, s>>>(x, v, chan, coef);
 }
 
 __global__ void k_schur_combine(const double *__restrict__ x, const double *__restrict__ vext,
@@ -1624,7 +1672,9 @@ __global__ void k_newton_update(double *__restrict__ x, const double *__restrict
     for (int iu = 0; iu < c_g.nunk; iu++) {
       const long k = (long)iu * N + i;
       const double xo = x[k], d = dx[k];
-      const double t = (frac * d) / (rel * xo + abs_tol);
+      // the weighted update norm is a convergence test (<= 1): its quotients in FP32 (an FP64 division per
+      // unknown made this kernel FP64-bound), their squares summed in FP64
+      const double t = (double)((float)(frac * d) / (float)(rel * xo + abs_tol));
       s = fma(t, t, s);
       const bool is_rho = iu >= c_g.first_rho && iu < c_g.first_rho + c_g.ncomp;
       if (is_rho && xo + frac * d < 1.e-99) x[k] = 0.1 * xo;

@@ -50,38 +50,57 @@ constexpr double kDensityMin = 1.e-20;   // integrands vanish at or below this d
 // Constants of the free-energy objective: per component the chemical potential
 // betamu and the bulk integrand rho_b(ln rho_b - 1) - rho_b betamu [+ rho_b betamu_att / 2],
 // and the hard-sphere energy density of the bulk weighted densities.
-// FP64 3-D FFTs for the stencil sums of the accurate fills (fft.cu): complex box [F2][F1][F0] with F_d >= the
-// padded box; each axis's length is a product of radices 2, 3, 4, 5
+// 3-D real-to-complex FFTs for the stencil sums (fft.cu): real box [F2][F1][F0] with F_d = n_d on periodic
+// dimensions (no padding) and F_d >= the padded extent elsewhere, half spectrum [F2][F1][F0/2 + 1]; each axis's
+// length is a product of radices 2, 3, 4, 5
 struct FftAxis {
   int n = 1, nst = 0;
   int rad[16] = {0};
   double2 *d_tw = nullptr;   // exp(-2 pi i k / n), k < n
-  float2 *d_tw32 = nullptr;  // the same rounded to FP32 (the products' FP32 transforms)
+  float2 *d_tw32 = nullptr;  // the same rounded to FP32 (the FP32 transforms)
 };
 struct FftPlan {
   int F[3] = {1, 1, 1};
-  long NF = 0;
+  int Fh = 1;                // F[0] / 2 + 1
+  int P[3] = {1, 1, 1}, nx[3] = {1, 1, 1}, h[3] = {0, 0, 0};
+  int off[3] = {0, 0, 0};    // first padded index the box holds along d (h on an unpadded periodic dimension)
+  int ext[3] = {1, 1, 1};    // padded extent the box holds (zeros beyond it)
+  long NR = 0;               // real box points
+  long NH = 0;               // half-spectrum points
   FftAxis ax[3];
 };
-bool fft_make_plan(FftPlan &p, const int P[3], int ndim, cudaStream_t s);
+bool fft_make_plan(FftPlan &p, const int P[3], const int nx[3], const int h[3], const int periodic[3], int ndim,
+                   cudaStream_t s);
+// One channel of a field read through the per-dimension boundary maps (the values a padded box would hold:
+// bulk values at bulk sentinels, 0 inside walls, mirrored nodes with the sign flips of signmask, 0 at the
+// zero-density nodes of component zc >= 0)
+struct MapSrc {
+  const double *src = nullptr;    // the channel [N]
+  int ndim = 3, nx[3] = {1, 1, 1};
+  const int *map[3] = {nullptr, nullptr, nullptr};
+  double bulk_lo = 0.0, bulk_hi = 0.0;
+  int signmask = 0, zc = -1;
+  const signed char *zero = nullptr;
+  long N = 0;
+};
+void rfft_forward_mapped(const MapSrc &m, double2 *spec, const FftPlan &p, cudaStream_t s);
+void rfft_forward_mapped(const MapSrc &m, float2 *spec, const FftPlan &p, cudaStream_t s);
 void fft_free_plan(FftPlan &p);
-void fft3d(double2 *box, const FftPlan &p, int ndim, bool inverse, cudaStream_t s);
-void fft3d(float2 *box, const FftPlan &p, int ndim, bool inverse, cudaStream_t s);
-// box <- the padded channel [P2][P1][P0], zero beyond it
-void launch_fft_load(const double *pad, const int P[3], double2 *box, const FftPlan &p, cudaStream_t s);
-void launch_fft_load(const float *pad, const int P[3], float2 *box, const FftPlan &p, cudaStream_t s);
+// half spectrum of a padded channel [P2][P1][P0]
+void rfft_forward(const double *pad, double2 *spec, const FftPlan &p, cudaStream_t s);
+void rfft_forward(const float *pad, float2 *spec, const FftPlan &p, cudaStream_t s);
+// half spectrum of a real box [F2][F1][F0]
+void rfft_forward_box(const double *box, double2 *spec, const FftPlan &p, cudaStream_t s);
+// out[node] (+)= scale * (inverse transform of spec) at the interior nodes; spec is overwritten
+void rfft_inverse(double2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
+void rfft_inverse(float2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
 void launch_to_float2(const double2 *in, float2 *out, long n, cudaStream_t s);
-// box <- the correlation kernel of coefficient q of a stencil: coef[k * ncoef + q] at (-offset_k) mod F
-void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double2 *box,
+// real box <- the correlation kernel of coefficient q of a stencil: coef[k * ncoef + q] added at (-offset_k) mod F
+void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double *box,
                            const FftPlan &p, cudaStream_t s);
 // out = a * k (or out += a * k)
 void launch_spec_mul(const double2 *a, const double2 *k, double2 *out, long n, bool accumulate, cudaStream_t s);
 void launch_spec_mul(const float2 *a, const float2 *k, float2 *out, long n, bool accumulate, cudaStream_t s);
-// out[node] += Re(box[node + h]) * scale for the nx[0] x nx[1] x nx[2] interior
-void launch_fft_extract(const double2 *box, const FftPlan &p, const int h[3], const int nx[3], double scale,
-                        double *out, cudaStream_t s);
-void launch_fft_extract(const float2 *box, const FftPlan &p, const int h[3], const int nx[3], double scale,
-                        double *out, cudaStream_t s);
 
 // Averaged rows of coarsened nodes and the prolongation onto them (coarsen.cu)
 constexpr int kMaxZone = 5;
@@ -226,9 +245,11 @@ __host__ __device__ inline void fmt_dphi_at(const double *n, double *dphi, int n
 // src/dft_physics_FMT4.c:179, fac = 1 - V2.V2/n2^2).
 // The state-dependent scalars of that matrix at one node (all zero where the White-Bear cut applies, which
 // makes z = 0); split from the product so that the products of one Newton state can reuse them.
-struct HessCoef {
-  double a, a2, h13, h22, h23, h33, ff, gvf1, g2vr_f, g2vc_f, gvv, gvv_out;
+template <class T>
+struct HessCoefT {
+  T a, a2, h13, h22, h23, h33, ff, gvf1, g2vr_f, g2vc_f, gvv, gvv_out;
 };
+using HessCoef = HessCoefT<double>;
 constexpr int kHessCoef = 12;
 
 __host__ __device__ inline HessCoef fmt_hess_coef_at(const double *n, int nd, int fn, bool exact)
@@ -274,18 +295,20 @@ __host__ __device__ inline HessCoef fmt_hess_coef_at(const double *n, int nd, in
 }
 
 // z = M y from the node's scalars and its vector densities (n ordering); transpose swaps the n2-V2 entries
-__host__ __device__ inline void fmt_hess_apply_coef(const HessCoef &c, const double *n, const double *y, double *z,
-                                                    int nd, bool transpose)
+// T = double, or float for the products of FP32 arithmetic (coefficients of the state rounded once)
+template <class T>
+__host__ __device__ inline void fmt_hess_apply_coef(const HessCoefT<T> &c, const T *n, const T *y, T *z, int nd,
+                                                    bool transpose)
 {
-  const double g2v_row = transpose ? c.g2vc_f : c.g2vr_f, g2v_col = transpose ? c.g2vr_f : c.g2vc_f;
-  double Vy = 0.0;
+  const T g2v_row = transpose ? c.g2vc_f : c.g2vr_f, g2v_col = transpose ? c.g2vr_f : c.g2vc_f;
+  T Vy = 0;
   for (int d = 0; d < nd; d++) Vy += n[4 + nd + d] * y[4 + nd + d];
-  const double a = c.a, a2 = c.a2;
-  double s2 = 0.0, s3 = 0.0;
+  const T a = c.a, a2 = c.a2;
+  T s2 = 0, s3 = 0;
   for (int d = 0; d < nd; d++) {
-    const double V1 = n[4 + d], V2 = n[4 + nd + d];
-    const double yV1 = y[4 + d], yV2 = y[4 + nd + d];
-    const double h3v2 = -V1 * a2 + c.gvf1 * V2;    // M[n3][V2d] = M[V2d][n3]
+    const T V1 = n[4 + d], V2 = n[4 + nd + d];
+    const T yV1 = y[4 + d], yV2 = y[4 + nd + d];
+    const T h3v2 = -V1 * a2 + c.gvf1 * V2;    // M[n3][V2d] = M[V2d][n3]
     s2 += g2v_row * V2 * yV2;
     s3 += -V2 * a2 * yV1 + h3v2 * yV2;
     z[4 + d] = -V2 * a2 * y[3] - a * yV2;
@@ -376,6 +399,7 @@ struct DevStencil {
   std::vector<double2 *> spec_fwd, spec_tr;
   std::vector<float2 *> spec_fwd32, spec_tr32;
   int fft32_fwd = 0, fft32_tr = 0;      // short stencils: FP32 FFT (1) or slab (-1) sums, 0 undecided
+  float t32[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [forward, transposed][direct, FFT] ms of the timing that decided
 };
 
 }  // namespace tgpu
@@ -462,8 +486,10 @@ void launch_assemble(const double *x, const double *vext, const signed char *zer
 // coef: the state's Hessian scalars ([kHessCoef][N], launch_hess_coef) or null to evaluate them in place
 void launch_hess_coef(const double *x, double *coef, cudaStream_t s);
 void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
-                        cudaStream_t s);
-void launch_jv_local(const double *x, const double *v, double *chan, const double *coef, cudaStream_t s);
+                        cudaStream_t s, bool f32 = false);
+// f32: the per-node Hessian in FP32 arithmetic (FP32 products)
+void launch_jv_local(const double *x, const double *v, double *chan, const double *coef, cudaStream_t s,
+                     bool f32 = false);
 void launch_schur_combine(const double *x, const double *vext, const signed char *zero, const double *v2,
                           const double *tr, const double *ymf, double *y2, cudaStream_t s);
 void launch_jv_combine(const double *x, const double *vext, const signed char *zero, const double *v,

@@ -89,6 +89,7 @@ def load(build_if_missing: bool = False):
         "tgpu_set_zones": [vp, C.c_int, vp, vp],
         "tgpu_set_fft_threshold": [vp, C.c_int],
         "tgpu_set_fft32_policy": [vp, C.c_int],
+        "tgpu_fft32_choice": [vp, C.c_int, C.c_int, ip, dp],
         "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
@@ -345,6 +346,15 @@ class Solver:
     def set_fft32_policy(self, policy: int):
         """FP32 sums as FP32 FFT convolutions: -1 timed choice (default), 0 never, 1 always."""
         _check(self.lib.tgpu_set_fft32_policy(self.h, int(policy)), self.lib)
+
+    def fft32_choice(self, stype: int, index: int = 0) -> dict:
+        """The FP32 sums' timed choice for a stencil: forward / transposed (1 FFT, -1 direct, 0 undecided) and the
+        timed milliseconds per sum behind them."""
+        ch = (C.c_int * 2)()
+        ms = (C.c_double * 4)()
+        _check(self.lib.tgpu_fft32_choice(self.h, stype, index, ch, ms), self.lib)
+        return {"forward": ch[0], "transposed": ch[1], "ms_direct_fwd": ms[0], "ms_fft_fwd": ms[1],
+                "ms_direct_tr": ms[2], "ms_fft_tr": ms[3]}
 
     def set_stream(self, stream_handle: int):
         _check(self.lib.tgpu_set_stream(self.h, C.c_void_p(stream_handle)), self.lib)
