@@ -9,6 +9,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "tgpu_internal.h"
@@ -181,6 +182,9 @@ struct Ctx : tgpu_ctx {
   // FP32 FFT sums of the long stencils in FP32 arithmetic: chosen per context by timing against the
   // tensor-core sum (products) and the FP32 slab sum (FP32 fills): 0 undecided, 1 FFT, -1 direct
   float2 *d_fbox32[3] = {nullptr, nullptr, nullptr};
+  // spectra of a transposed sum's input channels (each transformed once, summed by one inverse)
+  std::vector<double2 *> d_trbox;
+  std::vector<float2 *> d_trbox32;
   int fft32_tc = 0, fft32_slab = 0;
   float t32_att[2][2] = {{0.f, 0.f}, {0.f, 0.f}};   // [slab context, tensor-core context][direct, FFT] ms
   long fft32_gen = -1;
@@ -456,27 +460,66 @@ const float2 *fft_channel32(Ctx *c, int ch)
   return c->d_fbox32[0];
 }
 
+// spectrum of channel ch of the last pad() into box (not cached)
+template <class C>
+const C *channel_into(Ctx *c, int ch, C *box)
+{
+  tgpu::rfft_forward_mapped(map_src(c, ch), box, c->fft, c->stream);
+  c->stats.kernel_launches += 3;
+  return box;
+}
+
+template <class C>
+std::vector<C *> &tr_boxes(Ctx *c);
+template <>
+std::vector<double2 *> &tr_boxes<double2>(Ctx *c) { return c->d_trbox; }
+template <>
+std::vector<float2 *> &tr_boxes<float2>(Ctx *c) { return c->d_trbox32; }
+
+// transposed sum: out += the inverse of sum_t (spectrum of channel chs[t]) * kern[t], over channels of the last
+// pad(), in one inverse transform
+template <class C>
+void fft_tr_sum(Ctx *c, const int *chs, const C *const *kern, int n, double *out)
+{
+  if (n > tgpu::fft_max_terms()) throw Error(TGPU_ERR_UNSUPPORTED, "too many channels for one FFT transposed sum");
+  std::vector<C *> &boxes = tr_boxes<C>(c);
+  while ((int)boxes.size() < n) boxes.push_back(dalloc<C>((size_t)c->fft.NH));
+  std::vector<const C *> a(n);
+  for (int t = 0; t < n; t++) a[t] = channel_into(c, chs[t], boxes[t]);
+  C *work = std::is_same<C, float2>::value ? (C *)c->d_fbox32[2] : (C *)c->d_fbox[2];
+  tgpu::rfft_inverse_products(a.data(), kern, n, work, c->fft, 1.0 / (double)c->fft.NR, out, true, c->stream);
+  c->stats.kernel_launches += 3;
+  c->stats.conv_launches++;
+}
+
+// FFT sums with the stencil's spectra `spec` (FP32 or FP64): forward, one inverse per output of the field's spectrum
+// times the output's kernel; transposed, one inverse of the channels' spectra times their kernels
+template <class C>
+void fft_conv_impl(Ctx *c, int ch0, int nin, const std::vector<C *> &spec, bool tr, double *const *outs, int nout,
+                   C *const *fbox, const C *(*channel)(Ctx *, int))
+{
+  if (!tr) {
+    const C *F = channel(c, ch0);
+    for (int q = 0; q < nout; q++) {
+      const C *a[1] = {F}, *k[1] = {spec[q]};
+      tgpu::rfft_inverse_products(a, k, 1, fbox[1], c->fft, 1.0 / (double)c->fft.NR, outs[q], true, c->stream);
+      c->stats.kernel_launches += 3;
+    }
+    c->stats.conv_launches++;
+  } else {
+    std::vector<int> chs(nin);
+    std::vector<const C *> k(nin);
+    for (int t = 0; t < nin; t++) {
+      chs[t] = ch0 + t;
+      k[t] = spec[t];
+    }
+    fft_tr_sum<C>(c, chs.data(), k.data(), nin, outs[0]);
+  }
+}
+
 void fft_conv32(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
 {
-  const long NH = c->fft.NH;
-  const double scale = 1.0 / (double)c->fft.NR;
-  if (!tr) {
-    const float2 *F = fft_channel32(c, ch0);
-    for (int q = 0; q < nout; q++) {
-      tgpu::launch_spec_mul(F, st.spec_fwd32[q], c->d_fbox32[1], NH, false, c->stream);
-      tgpu::rfft_inverse(c->d_fbox32[1], c->fft, scale, outs[q], true, c->stream);
-      c->stats.kernel_launches += 4;
-    }
-  } else {
-    for (int k = 0; k < nin; k++) {
-      const float2 *F = fft_channel32(c, ch0 + k);
-      tgpu::launch_spec_mul(F, st.spec_tr32[k], c->d_fbox32[2], NH, k > 0, c->stream);
-      c->stats.kernel_launches++;
-    }
-    tgpu::rfft_inverse(c->d_fbox32[2], c->fft, scale, outs[0], true, c->stream);
-    c->stats.kernel_launches += 3;
-  }
-  c->stats.conv_launches++;
+  fft_conv_impl<float2>(c, ch0, nin, tr ? st.spec_tr32 : st.spec_fwd32, tr, outs, nout, c->d_fbox32, fft_channel32);
 }
 
 // FP32 FFT for this sum: the attraction stencil by its context's choice (tensor-core products or FP32 slab
@@ -492,25 +535,7 @@ bool use_fft32(const Ctx *c, const DevStencil &st, bool tr, int nin, int nout)
 
 void fft_conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout)
 {
-  const long NH = c->fft.NH;
-  const double scale = 1.0 / (double)c->fft.NR;
-  if (!tr) {
-    const double2 *F = fft_channel(c, ch0);
-    for (int q = 0; q < nout; q++) {
-      tgpu::launch_spec_mul(F, st.spec_fwd[q], c->d_fbox[1], NH, false, c->stream);
-      tgpu::rfft_inverse(c->d_fbox[1], c->fft, scale, outs[q], true, c->stream);
-      c->stats.kernel_launches += 4;
-    }
-  } else {
-    for (int k = 0; k < nin; k++) {
-      const double2 *F = fft_channel(c, ch0 + k);
-      tgpu::launch_spec_mul(F, st.spec_tr[k], c->d_fbox[2], NH, k > 0, c->stream);
-      c->stats.kernel_launches++;
-    }
-    tgpu::rfft_inverse(c->d_fbox[2], c->fft, scale, outs[0], true, c->stream);
-    c->stats.kernel_launches += 3;
-  }
-  c->stats.conv_launches++;
+  fft_conv_impl<double2>(c, ch0, nin, tr ? st.spec_tr : st.spec_fwd, tr, outs, nout, c->d_fbox, fft_channel);
 }
 
 void conv(Ctx *c, int ch0, int nin, const DevStencil &st, bool tr, double *const *outs, int nout, bool f32)
@@ -734,7 +759,8 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bo
   }
 }
 
-// Euler-Lagrange stencil sums of the padded channels with one zone's stencils into out ([ncomp][N])
+// Euler-Lagrange stencil sums of the padded channels with one zone's stencils into out ([ncomp][N]); where both the
+// delta and the theta sums of a component take FFTs, their 2 + ndim channels share one inverse transform
 void transpose_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, bool f32)
 {
   const tgpu::DevGeom &g = c->dg;
@@ -742,8 +768,28 @@ void transpose_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, b
   const int nd = g.ndim;
   for (int ic = 0; ic < g.ncomp; ic++) {
     double *o[1] = {out + (long)ic * N};
-    conv(c, ic * (nd + 2), 1 + nd, sten[TGPU_STEN_DELTA][ic], true, o, 1, f32);
-    conv(c, ic * (nd + 2) + nd + 1, 1, sten[TGPU_STEN_THETA][ic], true, o, 1, f32);
+    const DevStencil &sd = sten[TGPU_STEN_DELTA][ic], &st = sten[TGPU_STEN_THETA][ic];
+    const int base = ic * (nd + 2);
+    int chs[tgpu::kMaxRb];
+    for (int t = 0; t < nd + 2; t++) chs[t] = base + t;
+    if (sten == c->sten && f32 && c->spec32_built && use_fft32(c, sd, true, 1 + nd, 1) &&
+        use_fft32(c, st, true, 1, 1)) {
+      const float2 *k[tgpu::kMaxRb];
+      for (int t = 0; t <= nd; t++) k[t] = sd.spec_tr32[t];
+      k[nd + 1] = st.spec_tr32[0];
+      fft_tr_sum<float2>(c, chs, k, nd + 2, o[0]);
+      continue;
+    }
+    if (sten == c->sten && !f32 && c->fft_on && c->fft_state == 1 && (int)sd.spec_tr.size() == 1 + nd &&
+        st.spec_tr.size() == 1) {
+      const double2 *k[tgpu::kMaxRb];
+      for (int t = 0; t <= nd; t++) k[t] = sd.spec_tr[t];
+      k[nd + 1] = st.spec_tr[0];
+      fft_tr_sum<double2>(c, chs, k, nd + 2, o[0]);
+      continue;
+    }
+    conv(c, base, 1 + nd, sd, true, o, 1, f32);
+    conv(c, base + nd + 1, 1, st, true, o, 1, f32);
   }
 }
 
@@ -2274,6 +2320,8 @@ int tgpu_destroy(tgpu_handle h)
     for (auto &b : c->d_fbox) dfree(b);
     dfree(c->d_dscr);
     for (auto &b : c->d_fbox32) dfree(b);
+    for (auto &b : c->d_trbox) dfree(b);
+    for (auto &b : c->d_trbox32) dfree(b);
     tgpu::fft_free_plan(c->fft);
     for (int z = 1; z < tgpu::kMaxZone; z++)
       for (int t = 0; t < 3; t++)
@@ -2554,6 +2602,10 @@ int tgpu_set_fft_threshold(tgpu_handle h, int min_points)
           st.fft32_fwd = st.fft32_tr = 0;
         }
       for (auto &b : c->d_fbox32) dfree(b);
+      for (auto &b : c->d_trbox) dfree(b);
+      for (auto &b : c->d_trbox32) dfree(b);
+      c->d_trbox.clear();
+      c->d_trbox32.clear();
       tgpu::fft_free_plan(c->fft);
       c->fft_state = 0;
       c->fft_gen = -1;

@@ -27,6 +27,8 @@
 // 5-point DFTs use the symmetric forms that share the sums and differences of mirrored inputs (two real
 // multiplications per output pair instead of a full complex product per term).  Twiddles are tabulated on
 // the host in extended precision.  The inverse uses conjugate twiddles; its 1/(F0 F1 F2) is applied on output.
+// The spectral products (one kernel spectrum per output, or the sum of channel-times-kernel products of a
+// transposed sum) are formed while the first inverse pass loads its lines.
 #include <cmath>
 #include <vector>
 
@@ -309,10 +311,21 @@ __global__ void __launch_bounds__(kFftThreads) k_irfft_x(const C *__restrict__ s
   }
 }
 
-// y and z passes: lines of element stride es; a CTA takes kFftLines consecutive x at one (outer) index
+// spectral products formed by a pass as it loads its lines: value = sum_t a_t * k_t (n = 0: the input itself)
+constexpr int kMaxTerms = 6;
 template <class C>
-__global__ void __launch_bounds__(kFftThreads) k_fft_strided(C *box, int X, int n, long es, long outer_stride,
-                                                           Stages st, const C *__restrict__ tw_g, int inv)
+struct Terms {
+  const C *a[kMaxTerms];
+  const C *k[kMaxTerms];
+  int n;
+};
+
+// y and z passes: lines of element stride es; a CTA takes kFftLines consecutive x at one (outer) index; reads `in`
+// (or the products of `terms`) and writes `out` (in place when out == in)
+template <class C>
+__global__ void __launch_bounds__(kFftThreads) k_fft_strided(const C *in, C *out, Terms<C> terms, int X, int n,
+                                                           long es, long outer_stride, Stages st,
+                                                           const C *__restrict__ tw_g, int inv)
 {
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
@@ -325,13 +338,22 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(C *box, int X, int 
   const int nl = min(kFftLines, X - x0);
   for (int q = threadIdx.x; q < kFftLines * n; q += blockDim.x) {
     const int e = q / kFftLines, l = q - e * kFftLines;
-    if (l < nl) b0[l * ls + e] = box[base + e * es + l];
+    if (l >= nl) continue;
+    const long idx = base + e * es + l;
+    C v;
+    if (terms.n == 0) {
+      v = in[idx];
+    } else {
+      v = cmul(terms.a[0][idx], terms.k[0][idx]);
+      for (int t = 1; t < terms.n; t++) v = cadd(v, cmul(terms.a[t][idx], terms.k[t][idx]));
+    }
+    b0[l * ls + e] = v;
   }
   __syncthreads();
   const C *res = fft_tile<C>(b0, b1, n, ls, nl, st, tw, inv);
   for (int q = threadIdx.x; q < kFftLines * n; q += blockDim.x) {
     const int e = q / kFftLines, l = q - e * kFftLines;
-    if (l < nl) box[base + e * es + l] = res[l * ls + e];
+    if (l < nl) out[base + e * es + l] = res[l * ls + e];
   }
 }
 
@@ -348,12 +370,14 @@ __global__ void k_fft_kernel_box(const short *__restrict__ off3, const double *_
   atomicAdd(box + ((long)z * F1 + y) * F0 + x, coef[(long)k * ncoef + q]);
 }
 
+// the products of `t` as a spectrum (a box without y or z passes to form them in)
 template <class C>
-__global__ void k_spec_mul(const C *__restrict__ a, const C *__restrict__ k, C *__restrict__ out, long n, int accumulate)
+__global__ void k_spec_terms(Terms<C> t, C *__restrict__ out, long n)
 {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const C p = cmul(a[i], k[i]);
-    out[i] = accumulate ? cadd(out[i], p) : p;
+    C v = cmul(t.a[0][i], t.k[0][i]);
+    for (int j = 1; j < t.n; j++) v = cadd(v, cmul(t.a[j][i], t.k[j][i]));
+    out[i] = v;
   }
 }
 
@@ -427,22 +451,18 @@ XGeom xgeom(const FftPlan &p)
   return g;
 }
 
-// forward y and z passes (inverse: z then y) over the half-spectrum box
+// one y (d = 1) or z (d = 2) pass over the half-spectrum box
 template <class C>
-void yz_passes(C *spec, const FftPlan &p, bool inverse, const C *const *tw, cudaStream_t s)
+void strided_pass(const C *in, C *out, const Terms<C> &terms, const FftPlan &p, int d, bool inverse, const C *tw,
+                  cudaStream_t s)
 {
-  const int X = p.Fh;
+  const int X = p.Fh, n = p.F[d];
   const int xblocks = (X + kFftLines - 1) / kFftLines;
-  for (int k = 0; k < 2; k++) {
-    const int d = inverse ? 2 - k : 1 + k;
-    const int n = p.F[d];
-    if (n == 1) continue;
-    const long es = d == 1 ? (long)X : (long)X * p.F[1];
-    const long outer = d == 1 ? (long)X * p.F[1] : (long)X;   // axis 1: outer index z; axis 2: outer index y
-    const long nouter = d == 1 ? p.F[2] : p.F[1];
-    k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, tile_smem<C>(n), s>>>(
-        spec, X, n, es, outer, stages(p.ax[d]), tw[d], inverse ? 1 : 0);
-  }
+  const long es = d == 1 ? (long)X : (long)X * p.F[1];
+  const long outer = d == 1 ? (long)X * p.F[1] : (long)X;   // axis 1: outer index z; axis 2: outer index y
+  const long nouter = d == 1 ? p.F[2] : p.F[1];
+  k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, tile_smem<C>(n), s>>>(
+      in, out, terms, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
 }
 
 template <class T, class C, class Src>
@@ -457,14 +477,24 @@ void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, c
   const long npairs = (g.nlines + 1) / 2;
   k_rfft_x<T, C, Src><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
       src, g, stages(p.ax[0]), tw[0], spec);
-  yz_passes<C>(spec, p, false, tw, s);
+  const Terms<C> none{};
+  for (int d = 1; d <= 2; d++)
+    if (p.F[d] > 1) strided_pass<C>(spec, spec, none, p, d, false, tw[d], s);
 }
 
+// inverse of the products in `terms`, formed by the first inverse pass into `spec` (the work box)
 template <class C>
-void rfft_inverse_impl(C *spec, const FftPlan &p, double scale, double *out, bool accumulate, const C *const *tw,
-                       cudaStream_t s)
+void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double scale, double *out, bool accumulate,
+                       const C *const *tw, cudaStream_t s)
 {
-  yz_passes<C>(spec, p, true, tw, s);
+  const Terms<C> none{};
+  bool pending = true;   // products not formed yet
+  for (int d = 2; d >= 1; d--) {
+    if (p.F[d] == 1) continue;
+    strided_pass<C>(spec, spec, pending ? terms : none, p, d, true, tw[d], s);
+    pending = false;
+  }
+  if (pending) k_spec_terms<C><<<grid_for(p.NH), 256, 0, s>>>(terms, spec, p.NH);
   const XGeom g = xgeom(p);
   const long npairs = (g.nlines + 1) / 2;
   k_irfft_x<C><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
@@ -568,17 +598,33 @@ void rfft_forward_box(const double *box, double2 *spec, const FftPlan &p, cudaSt
   rfft_forward_impl<double, double2>(BoxSrc<double>{box, p.F[0], (long)p.F[0] * p.F[1]}, false, spec, p, tw, s);
 }
 
-void rfft_inverse(double2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
+template <class C>
+Terms<C> make_terms(const C *const *a, const C *const *k, int n)
 {
-  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
-  rfft_inverse_impl<double2>(spec, p, scale, out, accumulate, tw, s);
+  Terms<C> t{};
+  t.n = n;
+  for (int j = 0; j < n; j++) {
+    t.a[j] = a[j];
+    t.k[j] = k[j];
+  }
+  return t;
 }
 
-void rfft_inverse(float2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
+void rfft_inverse_products(const double2 *const *a, const double2 *const *k, int nterms, double2 *work,
+                           const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
+{
+  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
+  rfft_inverse_impl<double2>(make_terms(a, k, nterms), work, p, scale, out, accumulate, tw, s);
+}
+
+void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
+                           const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
 {
   const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
-  rfft_inverse_impl<float2>(spec, p, scale, out, accumulate, tw, s);
+  rfft_inverse_impl<float2>(make_terms(a, k, nterms), work, p, scale, out, accumulate, tw, s);
 }
+
+int fft_max_terms() { return kMaxTerms; }
 
 void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double *box,
                            const FftPlan &p, cudaStream_t s)
@@ -590,16 +636,6 @@ void launch_fft_kernel_box(const short *off3, const double *coef, int L, int nco
 void launch_to_float2(const double2 *in, float2 *out, long n, cudaStream_t s)
 {
   k_to_float2<<<grid_for(n), 256, 0, s>>>(in, out, n);
-}
-
-void launch_spec_mul(const double2 *a, const double2 *k, double2 *out, long n, bool accumulate, cudaStream_t s)
-{
-  k_spec_mul<double2><<<grid_for(n), 256, 0, s>>>(a, k, out, n, accumulate ? 1 : 0);
-}
-
-void launch_spec_mul(const float2 *a, const float2 *k, float2 *out, long n, bool accumulate, cudaStream_t s)
-{
-  k_spec_mul<float2><<<grid_for(n), 256, 0, s>>>(a, k, out, n, accumulate ? 1 : 0);
 }
 
 }  // namespace tgpu

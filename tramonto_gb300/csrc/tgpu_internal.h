@@ -91,16 +91,17 @@ void rfft_forward(const double *pad, double2 *spec, const FftPlan &p, cudaStream
 void rfft_forward(const float *pad, float2 *spec, const FftPlan &p, cudaStream_t s);
 // half spectrum of a real box [F2][F1][F0]
 void rfft_forward_box(const double *box, double2 *spec, const FftPlan &p, cudaStream_t s);
-// out[node] (+)= scale * (inverse transform of spec) at the interior nodes; spec is overwritten
-void rfft_inverse(double2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
-void rfft_inverse(float2 *spec, const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
+// out[node] (+)= scale * inverse transform of sum_t a_t k_t (nterms <= fft_max_terms() spectral products, formed by
+// the first inverse pass) at the interior nodes; work holds the half spectrum in between
+void rfft_inverse_products(const double2 *const *a, const double2 *const *k, int nterms, double2 *work,
+                           const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
+void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
+                           const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
+int fft_max_terms();
 void launch_to_float2(const double2 *in, float2 *out, long n, cudaStream_t s);
 // real box <- the correlation kernel of coefficient q of a stencil: coef[k * ncoef + q] added at (-offset_k) mod F
 void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double *box,
                            const FftPlan &p, cudaStream_t s);
-// out = a * k (or out += a * k)
-void launch_spec_mul(const double2 *a, const double2 *k, double2 *out, long n, bool accumulate, cudaStream_t s);
-void launch_spec_mul(const float2 *a, const float2 *k, float2 *out, long n, bool accumulate, cudaStream_t s);
 
 // Averaged rows of coarsened nodes and the prolongation onto them (coarsen.cu)
 constexpr int kMaxZone = 5;
