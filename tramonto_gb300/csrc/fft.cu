@@ -30,6 +30,7 @@
 // The spectral products (one kernel spectrum per output, or the sum of channel-times-kernel products of a
 // transposed sum) are formed while the first inverse pass loads its lines.
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "tgpu_internal.h"
@@ -45,6 +46,9 @@ constexpr int kFftMaxN = 432;    // two ping-pong tiles of kFftLines lines and t
 struct Stages {
   int nst;
   int rad[16];
+  int Ns[16];                    // product of the earlier radices (one-warp-per-line passes)
+  int step[16];                  // twiddle stride n / (Ns R)
+  unsigned magic[16];            // ceil(2^32 / Ns), 0 when Ns = 1: j / Ns = umulhi(j, magic) for j < 2^16
 };
 
 template <class C>
@@ -357,6 +361,176 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(const C *in, C *out
   }
 }
 
+// ---- FP32 passes: one warp per line ------------------------------------------------------------------------
+// The FP32 passes are bound by latency and instruction issue, not arithmetic: here a warp owns a line, so the
+// stages of a line synchronise only the warp (the block synchronises around its coalesced loads and stores), and
+// the butterflies index without runtime divisions (j / Ns by a precomputed 32-bit reciprocal).  The FP64 passes
+// keep the block tile above: FP64 issue slots are the bound there, and spreading a stage's butterflies over the
+// whole block leaves fewer of them on partly filled warps (at 180 points a warp per line leaves up to 28 of 64
+// lane slots of a stage idle).
+constexpr int kWLines = 16;   // lines (one warp each) per CTA
+
+template <int R, class C>
+__device__ __forceinline__ void warp_stage(const C *src, C *dst, int n, int Ns, int step, unsigned magic,
+                                           const C *tw, int inv, int lane)
+{
+  const int nb = n / R;
+  for (int j = lane; j < nb; j += 32) {
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = src[j + r * nb];
+    const int q = Ns == 1 ? j : (int)__umulhi((unsigned)j, magic);   // j / Ns
+    const int k = j - q * Ns;
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], twiddle(tw, r * k * step, inv));
+    }
+    dft_small<R, C>(v, inv);
+    const int idx = q * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) dst[idx + r * Ns] = v[r];
+  }
+}
+
+// every stage of one line (this warp's buffers b0, b1); returns the buffer that holds the result
+template <class C>
+__device__ __forceinline__ C *warp_fft(C *b0, C *b1, int n, const Stages &st, const C *tw, int inv, int lane)
+{
+  C *in = b0, *out = b1;
+  for (int s = 0; s < st.nst; s++) {
+    switch (st.rad[s]) {
+      case 2: warp_stage<2, C>(in, out, n, st.Ns[s], st.step[s], st.magic[s], tw, inv, lane); break;
+      case 3: warp_stage<3, C>(in, out, n, st.Ns[s], st.step[s], st.magic[s], tw, inv, lane); break;
+      case 4: warp_stage<4, C>(in, out, n, st.Ns[s], st.step[s], st.magic[s], tw, inv, lane); break;
+      default: warp_stage<5, C>(in, out, n, st.Ns[s], st.step[s], st.magic[s], tw, inv, lane); break;
+    }
+    __syncwarp();
+    C *t = in;
+    in = out;
+    out = t;
+  }
+  return in;
+}
+
+// forward x pass: each warp packs two real lines into one complex line, transforms it and splits it
+template <class T, class C, class Src>
+__global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(Src src, XGeom g, Stages st, const C *__restrict__ tw_g,
+                                                        C *__restrict__ spec)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *sm = reinterpret_cast<C *>(smraw);
+  const int n = g.F0, ls = n + 1;
+  C *tw = sm + 2 * kWLines * ls;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long L = 2 * ((long)blockIdx.x * kWLines + w);
+  if (L >= g.nlines) return;
+  C *b0 = sm + w * ls, *b1 = sm + (kWLines + w) * ls;
+  const bool two = L + 1 < g.nlines;
+  const int y0 = (int)(L % g.F1), z0 = (int)(L / g.F1);
+  const int y1 = (int)((L + 1) % g.F1), z1 = (int)((L + 1) / g.F1);
+  const bool r0 = y0 < g.ext[1] && z0 < g.ext[2], r1 = two && y1 < g.ext[1] && z1 < g.ext[2];
+  for (int x = lane; x < n; x += 32) {
+    T a = 0, b = 0;
+    if (x < g.ext[0]) {
+      if (r0) a = src(g, x, y0, z0);
+      if (r1) b = src(g, x, y1, z1);
+    }
+    b0[x] = C{a, b};
+  }
+  __syncwarp();
+  const C *res = warp_fft<C>(b0, b1, n, st, tw, 0, lane);
+  for (int k = lane; k < g.Fh; k += 32) {
+    const C Z = res[k], Zm = res[k == 0 ? 0 : n - k];
+    spec[L * g.Fh + k] = C{(T)0.5 * (Z.x + Zm.x), (T)0.5 * (Z.y - Zm.y)};
+    if (two) spec[(L + 1) * g.Fh + k] = C{(T)0.5 * (Z.y + Zm.y), (T)0.5 * (Zm.x - Z.x)};
+  }
+}
+
+// inverse x pass: each warp packs two half-spectrum lines into one complex line and writes the real and
+// imaginary parts of its inverse as the outputs of the interior nodes
+template <class C>
+__global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(const C *__restrict__ spec, XGeom g, Stages st,
+                                                         const C *__restrict__ tw_g, double scale,
+                                                         double *__restrict__ out, int accumulate)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *sm = reinterpret_cast<C *>(smraw);
+  const int n = g.F0, ls = n + 1;
+  C *tw = sm + 2 * kWLines * ls;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long L = 2 * ((long)blockIdx.x * kWLines + w);
+  if (L >= g.nlines) return;
+  C *b0 = sm + w * ls, *b1 = sm + (kWLines + w) * ls;
+  const bool two = L + 1 < g.nlines;
+  for (int k = lane; k < n; k += 32) {
+    const bool up = k < g.Fh;
+    const int kk = up ? k : n - k;
+    const C A = spec[L * g.Fh + kk];
+    const C B = two ? spec[(L + 1) * g.Fh + kk] : C{0, 0};
+    b0[k] = up ? C{A.x - B.y, A.y + B.x} : C{A.x + B.y, B.x - A.y};
+  }
+  __syncwarp();
+  const C *res = warp_fft<C>(b0, b1, n, st, tw, 1, lane);
+  const int nx0 = g.nx[0];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    if (h == 1 && !two) break;
+    const int y = (int)((L + h) % g.F1) - g.e[1], z = (int)((L + h) / g.F1) - g.e[2];
+    if (y < 0 || y >= g.nx[1] || z < 0 || z >= g.nx[2]) continue;
+    double *o = out + ((long)z * g.nx[1] + y) * nx0;
+    for (int x = lane; x < nx0; x += 32) {
+      const C r = res[x + g.e[0]];
+      const double v = scale * (double)(h ? r.y : r.x);
+      o[x] = accumulate ? o[x] + v : v;
+    }
+  }
+}
+
+// y and z passes: kWLines consecutive x at one outer index, one warp per line
+template <class C>
+__global__ void __launch_bounds__(32 * kWLines) k_fft_stridedw(const C *in, C *out, Terms<C> terms, int X, int n,
+                                                             long es, long outer_stride, Stages st,
+                                                             const C *__restrict__ tw_g, int inv)
+{
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C *sm = reinterpret_cast<C *>(smraw);
+  const int ls = n + 1;
+  C *tw = sm + 2 * kWLines * ls;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
+  const int xblocks = (X + kWLines - 1) / kWLines;
+  const int x0 = (blockIdx.x % xblocks) * kWLines;
+  const long base = (long)(blockIdx.x / xblocks) * outer_stride + x0;
+  const int nl = min(kWLines, X - x0);
+  for (int q = threadIdx.x; q < kWLines * n; q += blockDim.x) {
+    const int e = q / kWLines, l = q % kWLines;
+    if (l >= nl) continue;
+    const long idx = base + e * es + l;
+    C v;
+    if (terms.n == 0) {
+      v = in[idx];
+    } else {
+      v = cmul(terms.a[0][idx], terms.k[0][idx]);
+      for (int t = 1; t < terms.n; t++) v = cadd(v, cmul(terms.a[t][idx], terms.k[t][idx]));
+    }
+    sm[l * ls + e] = v;
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // every warp runs its line (beyond nl on stale data, never stored) so that all results sit in the same buffer
+  C *b0 = sm + w * ls;
+  const C *res = warp_fft<C>(b0, sm + (kWLines + w) * ls, n, st, tw, inv, lane);
+  const int rofs = (int)(res - b0);   // 0 or kWLines * ls
+  __syncthreads();
+  for (int q = threadIdx.x; q < kWLines * n; q += blockDim.x) {
+    const int e = q / kWLines, l = q % kWLines;
+    if (l < nl) out[base + e * es + l] = sm[rofs + l * ls + e];
+  }
+}
+
 // correlation kernel of coefficient q of a stencil in the real box: coef[k * ncoef + q] added at (-offset_k) mod F
 // (offsets that wrap onto the same position add up)
 __global__ void k_fft_kernel_box(const short *__restrict__ off3, const double *__restrict__ coef, int L, int ncoef,
@@ -414,9 +588,18 @@ Stages stages(const FftAxis &a)
 {
   Stages st{};
   st.nst = a.nst;
-  for (int k = 0; k < a.nst; k++) st.rad[k] = a.rad[k];
+  int Ns = 1;
+  for (int k = 0; k < a.nst; k++) {
+    st.rad[k] = a.rad[k];
+    st.Ns[k] = Ns;
+    st.step[k] = a.n / (Ns * a.rad[k]);
+    st.magic[k] = Ns == 1 ? 0u : (unsigned)((((unsigned long long)1 << 32) + Ns - 1) / Ns);
+    Ns *= a.rad[k];
+  }
   return st;
 }
+
+size_t wtile_smem(int n) { return sizeof(float2) * (2 * (size_t)kWLines * (n + 1) + n); }
 
 template <class C>
 size_t tile_smem(int n)
@@ -433,6 +616,13 @@ void set_smem_limits(const FftPlan &p)
   cudaFuncSetAttribute(k_irfft_x<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
   const int ss = (int)std::max(tile_smem<C>(p.F[1]), tile_smem<C>(p.F[2]));
   cudaFuncSetAttribute(k_fft_strided<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss);
+  if (std::is_same<C, float2>::value) {
+    const int wx = (int)wtile_smem(p.F[0]), ws = (int)std::max(wtile_smem(p.F[1]), wtile_smem(p.F[2]));
+    cudaFuncSetAttribute(k_rfft_xw<float, float2, BoxSrc<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
+    cudaFuncSetAttribute(k_rfft_xw<float, float2, MappedSrc<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
+    cudaFuncSetAttribute(k_irfft_xw<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
+    cudaFuncSetAttribute(k_fft_stridedw<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);
+  }
 }
 
 XGeom xgeom(const FftPlan &p)
@@ -461,8 +651,14 @@ void strided_pass(const C *in, C *out, const Terms<C> &terms, const FftPlan &p, 
   const long es = d == 1 ? (long)X : (long)X * p.F[1];
   const long outer = d == 1 ? (long)X * p.F[1] : (long)X;   // axis 1: outer index z; axis 2: outer index y
   const long nouter = d == 1 ? p.F[2] : p.F[1];
-  k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, tile_smem<C>(n), s>>>(
-      in, out, terms, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+  if constexpr (std::is_same<C, float2>::value) {
+    const int xb = (X + kWLines - 1) / kWLines;
+    k_fft_stridedw<C><<<(unsigned)(xb * nouter), 32 * kWLines, wtile_smem(n), s>>>(
+        in, out, terms, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+  } else {
+    k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, tile_smem<C>(n), s>>>(
+        in, out, terms, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+  }
 }
 
 template <class T, class C, class Src>
@@ -475,8 +671,12 @@ void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, c
       g.ext[d] = p.F[d];
     }
   const long npairs = (g.nlines + 1) / 2;
-  k_rfft_x<T, C, Src><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
-      src, g, stages(p.ax[0]), tw[0], spec);
+  if constexpr (std::is_same<C, float2>::value)
+    k_rfft_xw<T, C, Src><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
+        src, g, stages(p.ax[0]), tw[0], spec);
+  else
+    k_rfft_x<T, C, Src><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
+        src, g, stages(p.ax[0]), tw[0], spec);
   const Terms<C> none{};
   for (int d = 1; d <= 2; d++)
     if (p.F[d] > 1) strided_pass<C>(spec, spec, none, p, d, false, tw[d], s);
@@ -497,8 +697,12 @@ void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double 
   if (pending) k_spec_terms<C><<<grid_for(p.NH), 256, 0, s>>>(terms, spec, p.NH);
   const XGeom g = xgeom(p);
   const long npairs = (g.nlines + 1) / 2;
-  k_irfft_x<C><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
-      spec, g, stages(p.ax[0]), tw[0], scale, out, accumulate ? 1 : 0);
+  if constexpr (std::is_same<C, float2>::value)
+    k_irfft_xw<C><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
+        spec, g, stages(p.ax[0]), tw[0], scale, out, accumulate ? 1 : 0);
+  else
+    k_irfft_x<C><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
+        spec, g, stages(p.ax[0]), tw[0], scale, out, accumulate ? 1 : 0);
 }
 
 }  // namespace
