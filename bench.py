@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -147,6 +148,9 @@ class ClockSampler:
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_sten_tc launch at 128^3 (ncu, one launch)
 TC_TRAFFIC_BYTES = 47.724e6 + 0.538e6
+# the same for one launch of the FP32 y/z FFT pass (k_fft_stridedw<float2>) at 128^3, mean of three launches
+# (ncu flushes the caches before each profiled launch, so the box is read from DRAM there)
+FFT32_PASS_TRAFFIC_BYTES = 11.951e6 + 2.803e6
 
 
 def tc_issued_flops(p):
@@ -334,27 +338,6 @@ def run_config5(args):
     print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
-
-
-def fft_stream_bytes(p):
-    """Bytes an out-of-cache FP32 FFT convolution of the padded field streams (one sum)."""
-    from tramonto_gb300.problem import DELTA, THETA, UATT  # noqa: F401
-
-    def smooth(n):
-        while True:
-            m = n
-            for r in (2, 3, 5):
-                while m % r == 0:
-                    m //= r
-            if m == 1:
-                return n
-            n += 1
-    h = [max(abs(int(o[d])) for st in p.stencils.values() for o in st[0]) for d in range(3)]
-    P = [p.nx[d] + 2 * h[d] for d in range(3)]
-    NF = float(np.prod([smooth(v) for v in P]))
-    NP, N = float(np.prod(P)), float(p.nnodes)
-    box = 8.0 * NF                                   # complex FP32
-    return 4.0 * NP + box + 2 * 3 * 2 * box + 3 * box + 8.0 * N + 16.0 * N
 
 
 def main():
@@ -557,7 +540,13 @@ def main():
     e2e_s = time.perf_counter() - t0
     hbm, bf16, peak_src = peaks()
     t_dom = t_wca_tc if args.products == "fp16tc" else t_wca32
-    fft_bytes = fft_stream_bytes(p)
+    # the launch list's leading kernel: one y or z pass of the FP32 FFT sums over the half spectrum
+    t_pass_y, nh, nr = s.time_fft_pass(native.FP32, 1, reps=20)
+    t_pass_z, _, _ = s.time_fft_pass(native.FP32, 2, reps=20)
+    t_pass = 0.5 * (t_pass_y + t_pass_z)
+    pass_bytes = 2.0 * nh * 8.0                          # the half spectrum (complex FP32) read and written
+    t_pass64, _, _ = s.time_fft_pass(native.FP64, 1, reps=10)
+    fft_flops = 2 * 2.5 * nr * math.log2(nr) + 6.0 * nh  # two real transforms and the spectral product
     ach_tf = flops_att / (t_dom * 1e-3) / 1e12
     issued_tf = mma_flops / (t_wca_tc * 1e-3) / 1e12
     if rank == 0:
@@ -591,23 +580,29 @@ def main():
             "e2e": {"value": it_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * 8 * len(ladder or [0]),
                     "d2h_bytes_per_step": n * 8 * len(ladder or [0]),
                     "final_resid_norm2": rn_e2e},
-            # the attraction (WCA) stencil sum of the Schur products and FP32 fills: by default an FP32 FFT
-            # convolution (chosen per handle by timing it against the tensor-core and slab kernels); bound by
-            # memory streaming: its algorithmic bytes are those an out-of-cache 3-D FFT convolution streams
+            # the largest share of the timed solve's launch list: the y and z passes of the FP32 FFT stencil sums
+            # (every stencil sum of the Schur products and FP32 fills), each reading and writing the half spectrum
             "roofline": {"bound": "hbm",
-                         "kernel": "attraction (WCA) stencil sum, FP32 FFT convolution (k_fft_load, k_fft_x / "
-                                   "k_fft_strided forward and inverse, k_spec_mul, k_fft_extract)",
-                         "achieved": fft_bytes / (t_wca_fft32 * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
-                         "frac": fft_bytes / (t_wca_fft32 * 1e-3) / 1e9 / hbm,
-                         "peak_source": f"{peak_src} HBM copy",
-                         "traffic": None,
-                         "algorithmic": (f"{fft_bytes / 1e6:.0f} MB per sum: the padded FP32 field read and the "
-                                         "complex box written, 2 transforms x 3 axis passes reading and writing the "
-                                         "box, the spectral product (3 box streams), the interior read back and the "
-                                         "FP64 output read and written"),
-                         "ms_per_launch": t_wca_fft32,
-                         "logical_tflops": flops_att / (t_wca_fft32 * 1e-3) / 1e12,
-                         "logical": f"2 x {L_att} stencil points x {p.nnodes} nodes per sum",
+                         "kernel": "k_fft_stridedw<float2>: one y or z pass of the FP32 FFT stencil sums (one warp "
+                                   "per line, 16 lines per CTA) over the half spectrum",
+                         "achieved": pass_bytes / (t_pass * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": pass_bytes / (t_pass * 1e-3) / 1e9 / hbm,
+                         "peak_source": f"{peak_src} HBM copy (burst: the pass is timed alone)",
+                         "traffic": (FFT32_PASS_TRAFFIC_BYTES if args.workload == "config2" and args.n == 128
+                                     else None),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch at 128^3",
+                         "algorithmic": f"{pass_bytes / 1e6:.1f} MB per pass: the {nh}-point complex FP32 half "
+                                        "spectrum read and written once",
+                         "ms_per_launch": t_pass, "ms_per_launch_y": t_pass_y, "ms_per_launch_z": t_pass_z,
+                         "fp64_pass_ms_per_launch": t_pass64,
+                         "fft32_attraction_sum": {
+                             "ms_per_sum": t_wca_fft32,
+                             "fft_flops": fft_flops,
+                             "fft_tflops": (fft_flops / (t_wca_fft32 * 1e-3) / 1e12) if fft_flops else None,
+                             "counted": "2 x 2.5 NR log2 NR for the real forward and inverse transforms of the "
+                                        f"{nr}-point box, 6 per half-spectrum point for the product",
+                             "logical_tflops": flops_att / (t_wca_fft32 * 1e-3) / 1e12,
+                             "logical": f"2 x {L_att} stencil points x {p.nnodes} nodes per sum"},
                          "tensor_core_kernel": {
                              "kernel": "k_sten_tc (tcgen05 split FP16 x3), the direct sum it replaces",
                              "ms_per_launch": t_wca_tc, "bound": "tensor", "achieved_logical_tflops": ach_tf,
@@ -619,9 +614,9 @@ def main():
                          "fp32_slab_ms_per_launch": t_wca32, "fp32_slab_tflops": flops_att / (t_wca32 * 1e-3) / 1e12,
                          "fp64_ms_per_launch": t_wca64},
             # the attraction sum of the accurate fills: an FP64 FFT convolution by default (--accurate-fill fft;
-            # its cost is two transforms of the 192^3 box, independent of the stencil's length), else the
-            # float-float sum, bound by the FP32 issue rate (12 FP32 operations per term; nominal 152 SMs x 128
-            # lanes x clock), reported here for comparison
+            # its cost is two real transforms of the 180 x 128 x 128 box, independent of the stencil's length),
+            # else the float-float sum, bound by the FP32 issue rate (12 FP32 operations per term; nominal 152 SMs
+            # x 128 lanes x clock), reported here for comparison
             "fill_attraction_sum": {"fft_ms_per_sum": t_wca_fft,
                                     "fft_logical_tflops": flops_att / (t_wca_fft * 1e-3) / 1e12,
                                     "fft_vs_float_float": t_wca_ff / t_wca_fft},

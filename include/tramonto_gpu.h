@@ -392,6 +392,13 @@ const char *tgpu_noalloc_last_error(void);
 #define TGPU_TIME_FFT32 16
 int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum);
 
+/* Benchmark hook: device time (CUDA events on the handle's stream) of one forward y (axis 1) or z (axis 2) pass of
+ * the 3-D FFT sums over a half-spectrum work box, TGPU_FP32 or TGPU_FP64, averaged over reps; box_points receives
+ * the half spectrum's size (each pass reads and writes it once), real_points the real transform box's (either may
+ * be NULL).  No reference counterpart. */
+int tgpu_time_fft_pass(tgpu_handle h, int precision, int axis, int reps, double *ms_per_pass, long *box_points,
+                       long *real_points);
+
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */
 typedef struct {
   double fill_ms, schur_ms, conv_ms, gmres_ms;

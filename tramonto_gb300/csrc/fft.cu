@@ -231,8 +231,8 @@ struct MappedSrc {   // the unpadded channel through the boundary maps (the padd
     }
     const long node = idx[0] + (long)m.nx[0] * (idx[1] + (long)m.nx[1] * idx[2]);
     if (m.zc >= 0 && m.zero[(long)m.zc * m.N + node]) return (T)0;
-    const double v = m.src[node];
-    return (T)((__popc(refl & m.signmask) & 1) ? -v : v);
+    const T v = to_arith<T>(m.src[node]);
+    return (__popc(refl & m.signmask) & 1) ? -v : v;
   }
 };
 
@@ -482,9 +482,10 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(const C *__restrict__
     const int y = (int)((L + h) % g.F1) - g.e[1], z = (int)((L + h) / g.F1) - g.e[2];
     if (y < 0 || y >= g.nx[1] || z < 0 || z >= g.nx[2]) continue;
     double *o = out + ((long)z * g.nx[1] + y) * nx0;
+    const float sc = (float)scale;
     for (int x = lane; x < nx0; x += 32) {
       const C r = res[x + g.e[0]];
-      const double v = scale * (double)(h ? r.y : r.x);
+      const double v = (double)(sc * (h ? r.y : r.x));   // scaled in FP32
       o[x] = accumulate ? o[x] + v : v;
     }
   }
@@ -829,6 +830,18 @@ void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int n
 }
 
 int fft_max_terms() { return kMaxTerms; }
+
+void fft_pass(double2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s)
+{
+  const Terms<double2> none{};
+  strided_pass<double2>(spec, spec, none, p, d, inverse, p.ax[d].d_tw, s);
+}
+
+void fft_pass(float2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s)
+{
+  const Terms<float2> none{};
+  strided_pass<float2>(spec, spec, none, p, d, inverse, p.ax[d].d_tw32, s);
+}
 
 void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double *box,
                            const FftPlan &p, cudaStream_t s)

@@ -714,27 +714,27 @@ __device__ __forceinline__ void hess_apply_node_t(const double *x, const double 
   const int nd = c_g.ndim;
   const double *rb = x + (long)c_g.first_rb * N;
   T n[kMaxRb];
-  n[0] = (T)rb[3 * N + i];
-  n[1] = (T)rb[2 * N + i];
-  n[2] = (T)rb[1 * N + i];
-  n[3] = (T)rb[i];
+  n[0] = to_arith<T>(rb[3 * N + i]);
+  n[1] = to_arith<T>(rb[2 * N + i]);
+  n[2] = to_arith<T>(rb[1 * N + i]);
+  n[3] = to_arith<T>(rb[i]);
   for (int d = 0; d < nd; d++) {
-    n[4 + d] = (T)rb[(4 + nd + d) * N + i];
-    n[4 + nd + d] = (T)rb[(4 + d) * N + i];
+    n[4 + d] = to_arith<T>(rb[(4 + nd + d) * N + i]);
+    n[4 + nd + d] = to_arith<T>(rb[(4 + d) * N + i]);
   }
   HessCoefT<T> c;
-  c.a = (T)coef[i];
-  c.a2 = (T)coef[N + i];
-  c.h13 = (T)coef[2 * N + i];
-  c.h22 = (T)coef[3 * N + i];
-  c.h23 = (T)coef[4 * N + i];
-  c.h33 = (T)coef[5 * N + i];
-  c.ff = (T)coef[6 * N + i];
-  c.gvf1 = (T)coef[7 * N + i];
-  c.g2vr_f = (T)coef[8 * N + i];
-  c.g2vc_f = (T)coef[9 * N + i];
-  c.gvv = (T)coef[10 * N + i];
-  c.gvv_out = (T)coef[11 * N + i];
+  c.a = to_arith<T>(coef[i]);
+  c.a2 = to_arith<T>(coef[N + i]);
+  c.h13 = to_arith<T>(coef[2 * N + i]);
+  c.h22 = to_arith<T>(coef[3 * N + i]);
+  c.h23 = to_arith<T>(coef[4 * N + i]);
+  c.h33 = to_arith<T>(coef[5 * N + i]);
+  c.ff = to_arith<T>(coef[6 * N + i]);
+  c.gvf1 = to_arith<T>(coef[7 * N + i]);
+  c.g2vr_f = to_arith<T>(coef[8 * N + i]);
+  c.g2vc_f = to_arith<T>(coef[9 * N + i]);
+  c.gvv = to_arith<T>(coef[10 * N + i]);
+  c.gvv_out = to_arith<T>(coef[11 * N + i]);
   fmt_hess_apply_coef(c, n, y, z, nd, false);
 }
 
@@ -765,11 +765,11 @@ __device__ __forceinline__ void write_tr_channels(const T *q, double *chan, long
   const int nd = c_g.ndim;
   const long N = c_g.N;
   for (int ic = 0; ic < c_g.ncomp; ic++) {
-    const T f = (T)c_g.fac[ic], i4pr = (T)c_g.inv_4pir[ic], i4pr2 = (T)c_g.inv_4pirsq[ic];
+    const T f = to_arith<T>(c_g.fac[ic]), i4pr = to_arith<T>(c_g.inv_4pir[ic]), i4pr2 = to_arith<T>(c_g.inv_4pirsq[ic]);
     const long base = (long)ic * (nd + 2);
-    chan[base * N + i] = (double)(f * (q[0] * i4pr2 + q[1] * i4pr + q[2]));
-    for (int d = 0; d < nd; d++) chan[(base + 1 + d) * N + i] = (double)(f * (q[4 + d] * i4pr + q[4 + nd + d]));
-    chan[(base + nd + 1) * N + i] = (double)(f * q[3]);
+    chan[base * N + i] = to_f64(f * (q[0] * i4pr2 + q[1] * i4pr + q[2]));
+    for (int d = 0; d < nd; d++) chan[(base + 1 + d) * N + i] = to_f64(f * (q[4 + d] * i4pr + q[4 + nd + d]));
+    chan[(base + nd + 1) * N + i] = to_f64(f * q[3]);
   }
 }
 
@@ -877,16 +877,18 @@ __global__ void k_schur_local(const double *__restrict__ x, const double *__rest
     for (int k = 0; k < c_g.nrb; k++) {
       int src;
       double c;
-      if (dep_rb(k, &src, &c)) ysv[k] = (T)(-c * conv[(long)src * N + i]);   // -u_dep - B u_ind, u_dep = 0
-      else ysv[k] = (T)(-conv[(long)k * N + i]);
+      if (dep_rb(k, &src, &c)) ysv[k] = -to_arith<T>(c) * to_arith<T>(conv[(long)src * N + i]);   // -u_dep - B u_ind
+      else ysv[k] = -to_arith<T>(conv[(long)k * N + i]);
     }
     y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
     for (int d = 0; d < nd; d++) { y[4 + d] = ysv[4 + nd + d]; y[4 + nd + d] = ysv[4 + d]; }
     if constexpr (sizeof(T) == sizeof(double)) hess_apply_node(x, coef, i, y, z);
     else hess_apply_node_t<T>(x, coef, i, y, z);
     write_tr_channels(z, chan, i);
-    if (c_g.attraction)
-      for (int ic = 0; ic < c_g.ncomp; ic++) ymf[(long)ic * N + i] = -conv[(long)(c_g.nrb + ic) * N + i];
+    if (c_g.attraction)   // the sign flipped on the integer pipe
+      for (int ic = 0; ic < c_g.ncomp; ic++)
+        ymf[(long)ic * N + i] =
+            __longlong_as_double(__double_as_longlong(conv[(long)(c_g.nrb + ic) * N + i]) ^ (long long)0x8000000000000000ull);
   }
 }
 
@@ -913,7 +915,7 @@ __global__ void k_jv_local(const double *__restrict__ x, const double *__restric
       double yd[kMaxRb];
       T y[kMaxRb];
       load_n(v, i, yd);
-      for (int k = 0; k < c_g.nrb; k++) y[k] = (T)yd[k];
+      for (int k = 0; k < c_g.nrb; k++) y[k] = to_arith<T>(yd[k]);
       hess_apply_node_t<T>(x, coef, i, y, z);
     }
     write_tr_channels(z, chan, i);
@@ -1662,32 +1664,43 @@ void launch_newton_frac(const double *x, const double *dx, double floor_frac, do
   k_min_final<<<1, kThreads, 0, s>>>(partial, nblocks, result);
 }
 
+// partial != null: also the weighted update norm (a convergence test, <= 1): its quotients in FP32 and its squares
+// summed in FP32 per thread (FP64 divisions per unknown made this kernel FP64-bound); the residual-targeted Newton
+// needs no norm and skips it
 __global__ void k_newton_update(double *__restrict__ x, const double *__restrict__ dx, double frac, double rel,
                                 double abs_tol, double *__restrict__ partial)
 {
   __shared__ double sh[32];
   const long N = c_g.N;
-  double s = 0.0;
+  const bool norm = partial != nullptr;
+  float s = 0.0f;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     for (int iu = 0; iu < c_g.nunk; iu++) {
       const long k = (long)iu * N + i;
       const double xo = x[k], d = dx[k];
-      // the weighted update norm is a convergence test (<= 1): its quotients in FP32 (an FP64 division per
-      // unknown made this kernel FP64-bound), their squares summed in FP64
-      const double t = (double)((float)(frac * d) / (float)(rel * xo + abs_tol));
-      s = fma(t, t, s);
+      const double xn = fma(frac, d, xo);
+      if (norm) {
+        float t = (float)(frac * d) / (float)fma(rel, xo, abs_tol);
+        if (fabsf(t) > 1.0e18f) t = 1.0e18f;   // any term above 1 fails the test; NaN passes through to the check
+        s = fmaf(t, t, s);
+      }
       const bool is_rho = iu >= c_g.first_rho && iu < c_g.first_rho + c_g.ncomp;
-      if (is_rho && xo + frac * d < 1.e-99) x[k] = 0.1 * xo;
-      else if (iu == c_g.first_rb && xo + frac * d > 1.0) x[k] = xo + 0.5 * (1.0 - xo);
-      else x[k] = xo + frac * d;
+      if (is_rho && xn < 1.e-99) x[k] = 0.1 * xo;
+      else if (iu == c_g.first_rb && xn > 1.0) x[k] = xo + 0.5 * (1.0 - xo);
+      else x[k] = xn;
     }
-  s = block_sum(s, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (!norm) return;
+  const double sb = block_sum((double)s, sh);
+  if (threadIdx.x == 0) partial[blockIdx.x] = sb;
 }
 
 void launch_newton_update(double *x, const double *dx, double frac, double rel, double abs_tol, double *partial,
                           int nblocks, double *result, cudaStream_t s)
 {
+  if (!partial) {
+    k_newton_update<<<nblocks, kThreads, 0, s>>>(x, dx, frac, rel, abs_tol, nullptr);
+    return;
+  }
   k_newton_update<<<nblocks, kThreads, 0, s>>>(x, dx, frac, rel, abs_tol, partial);
   k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
 }

@@ -22,6 +22,16 @@
 
 namespace tgpu {
 
+// an FP64 value in arithmetic T, and back (conversions between FP64 and FP32 by the hardware: the same
+// conversions done with integer operations on the two 32-bit halves measured slower in the FP32 products)
+template <class T>
+__host__ __device__ __forceinline__ T to_arith(double x)
+{
+  return (T)x;
+}
+__host__ __device__ __forceinline__ double to_f64(float x) { return (double)x; }
+__host__ __device__ __forceinline__ double to_f64(double x) { return x; }
+
 constexpr int kMaxC = TGPU_MAXC;
 constexpr int kMaxRb = 10;            // 4 + 2*3 weighted densities
 constexpr int kSentBulk = -1, kSentWall = -2, kSentBulkHi = -3, kSentBad = -9;   // kSentBulk: the low side's bulk
@@ -98,6 +108,9 @@ void rfft_inverse_products(const double2 *const *a, const double2 *const *k, int
 void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
                            const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
 int fft_max_terms();
+// one y (d = 1) or z (d = 2) pass over a half spectrum, in place (benchmark hook)
+void fft_pass(double2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s);
+void fft_pass(float2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s);
 void launch_to_float2(const double2 *in, float2 *out, long n, cudaStream_t s);
 // real box <- the correlation kernel of coefficient q of a stencil: coef[k * ncoef + q] added at (-offset_k) mod F
 void launch_fft_kernel_box(const short *off3, const double *coef, int L, int ncoef, int q, double *box,

@@ -90,6 +90,7 @@ def load(build_if_missing: bool = False):
         "tgpu_set_fft_threshold": [vp, C.c_int],
         "tgpu_set_fft32_policy": [vp, C.c_int],
         "tgpu_fft32_choice": [vp, C.c_int, C.c_int, ip, dp],
+        "tgpu_time_fft_pass": [vp, C.c_int, C.c_int, C.c_int, dp, C.POINTER(C.c_long), C.POINTER(C.c_long)],
         "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
@@ -480,6 +481,14 @@ class Solver:
                                                update_floor, C.byref(it), C.byref(rn), C.byref(li))
         _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
         return it.value, rn.value, li.value
+
+    def time_fft_pass(self, precision, axis=1, reps=20):
+        """Device milliseconds of one y (axis 1) or z (axis 2) pass of the FFT sums, the half spectrum's size and the
+        real box's size."""
+        ms, pts, real = C.c_double(0.0), C.c_long(0), C.c_long(0)
+        _check(self.lib.tgpu_time_fft_pass(self.h, precision, axis, reps, C.byref(ms), C.byref(pts), C.byref(real)),
+               self.lib)
+        return ms.value, pts.value, real.value
 
     def time_stencil_sum(self, stype, index, precision, reps=5) -> float:
         """Device milliseconds of one forward stencil sum (benchmark hook)."""
