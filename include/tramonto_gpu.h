@@ -399,6 +399,13 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
 int tgpu_time_fft_pass(tgpu_handle h, int precision, int axis, int reps, double *ms_per_pass, long *box_points,
                        long *real_points);
 
+/* Diagnostics hook: the limit (try-wait attempts) of the tensor-core stencil sum's pipeline waits; spins <= 0
+ * restores the default.  A wait that runs out stops the kernel's pipeline, which drains the copies and MMAs it
+ * started (those waits keep the default limit), frees its tensor memory and leaves an error flag that the call
+ * reports as TGPU_ERR_CUDA ("a bounded wait ran out").  A tiny limit makes the waits run out on purpose, to
+ * exercise that path.  No reference counterpart. */
+int tgpu_set_tc_wait_limit(tgpu_handle h, long spins);
+
 /* Timing of the device work of the last call, per kernel family (ms), for benchmarks. */
 typedef struct {
   double fill_ms, schur_ms, conv_ms, gmres_ms;

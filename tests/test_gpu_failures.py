@@ -7,7 +7,10 @@
 - TGPU_ERR_NONFINITE: NaN in the external field at set-up, NaN in one density of a Newton state, a NaN right-hand
   side of the Schur solve;
 - TGPU_ERR_NOCONV: the GMRES cap (one iteration to 1e-14) and the Newton cap (one iteration to 1e-14; the
-  reference's newton_solver returns -iter when Max_NL_iter is reached, src/dft_newton.c:186-192).
+  reference's newton_solver returns -iter when Max_NL_iter is reached, src/dft_newton.c:186-192);
+- TGPU_ERR_CUDA from the tensor-core stencil sum when its pipeline's mbarrier waits are limited to one attempt
+  (tgpu_set_tc_wait_limit): the waits run out, the kernel drains the copies and MMAs it started (those waits keep
+  their default limit), frees its tensor memory and leaves a flag that the product reports.
 
 After each failure the handle stays usable: the next fill of the fixture's state equals the reference's residual.
 """
@@ -106,4 +109,27 @@ def test_iteration_caps():
     st, msg = _status(lambda: s.newton_solve(x1, resid_tol=1e-14, max_iter=1))
     assert st == ERR_NOCONV
     _still_usable(s, z)
+    s.close()
+
+
+def test_tensor_core_waits_that_run_out_are_reported():
+    import ctypes as C
+    from tramonto_gb300 import native, setup
+    from goldens import rel_err
+    p, _ = setup.config2(n=40)
+    s = native.Solver(p)
+    s.set_fft32_policy(0)          # the direct tensor-core sum, not the FP32 FFT
+    x = setup.initial_state(s, p)
+    s.fill(x, mode=0)
+    v2 = np.random.default_rng(6).standard_normal((p.ncomp, p.nnodes))
+    ref = s.schur(v2)              # FP64
+    s.set_precision(native.FP16TC)
+    ok = s.schur(v2)
+    assert rel_err(ok, ref) <= 1e-4
+    assert s.lib.tgpu_set_tc_wait_limit(s.h, C.c_long(1)) == 0
+    st, msg = _status(lambda: s.schur(v2))
+    assert st == -2 and "bounded wait ran out" in msg
+    assert s.lib.tgpu_set_tc_wait_limit(s.h, C.c_long(0)) == 0
+    again = s.schur(v2)            # default limit: the context and the handle still work
+    assert rel_err(again, ref) <= 1e-4 and np.abs(again - ok).max() <= 1e-12 * np.abs(ok).max()
     s.close()

@@ -2952,6 +2952,17 @@ int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int
   });
 }
 
+int tgpu_set_tc_wait_limit(tgpu_handle h, long spins)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    if (!c->tc_ready) throw Error(TGPU_ERR_UNSUPPORTED, "tensor-core sums unavailable: " + c->tc_why);
+    c->tcslab.spin = spins > 0 ? spins : 0;
+    return TGPU_OK;
+  });
+}
+
 int tgpu_time_fft_pass(tgpu_handle h, int precision, int axis, int reps, double *ms_per_pass, long *box_points,
                        long *real_points)
 {

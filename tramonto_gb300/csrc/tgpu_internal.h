@@ -372,6 +372,7 @@ struct TcSlab {                   // per problem: the FP16 copy of a padded chan
   void *d_slab = nullptr;         // FP16 [high, low][Zp][G][Yp][8]
   float *d_scale = nullptr;       // [0] field scale, [1] max |field| (bits)
   int *d_err = nullptr;           // nonzero after a bounded wait ran out
+  long spin = 0;                  // limit of the pipeline's waits (0: the kernel's default)
   int G = 0, Yp = 0, Zp = 0, R = 0, hy = 0, hz = 0, nring = 0, nsm = 1;
 };
 

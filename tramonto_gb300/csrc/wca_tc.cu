@@ -84,10 +84,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
-// bounded wait for the phase with the given parity to complete
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+// bounded wait for the phase with the given parity to complete (limit: try_wait attempts)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long limit = kSpin)
 {
-  for (long i = 0; i < kSpin; i++) {
+  for (long i = 0; i < limit; i++) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -167,6 +167,7 @@ struct TcArgs {
   double *out;
   int accumulate;
   int *err;
+  long spin;              // limit of the pipeline's waits (the drain before exit always uses kSpin)
 };
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar)
@@ -256,13 +257,13 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
       for (int pi = 0; pi < np && ok; pi++) {
         const int4 pl = P.planes[p_begin + pi];
         const int s = pi & 1;
-        if (pi >= 2 && !mbar_wait(pempty + 8 * s, ((pi >> 1) - 1) & 1)) { ok = false; break; }
+        if (pi >= 2 && !mbar_wait(pempty + 8 * s, ((pi >> 1) - 1) & 1, P.spin)) { ok = false; break; }
         mbar_expect_tx(pfull + 8 * s, plane_bytes);
         tma_load_5d(plane[s], &tmap, 0, y0, x0 / 8, z + pl.x + P.hz, 0, pfull + 8 * s);
         armed[s]++;
         for (int rj = 0; rj < pl.z; rj++, ri++) {
           const int bs = ri % nring;
-          if (ri >= nring && !mbar_wait(bempty + 8 * bs, ((ri / nring) - 1) & 1)) { ok = false; break; }
+          if (ri >= nring && !mbar_wait(bempty + 8 * bs, ((ri / nring) - 1) & 1, P.spin)) { ok = false; break; }
           if (*abort_flag) { ok = false; break; }
           mbar_expect_tx(bfull + 8 * bs, kTableBytes);
           bulk_load(ring + bs * kTableBytes, P.tables + (size_t)(pl.y + rj) * kRecHalfs, kTableBytes, bfull + 8 * bs);
@@ -288,11 +289,11 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
       for (int pi = 0; pi < np && ok; pi++) {
         const int4 pl = P.planes[p_begin + pi];
         const int s = pi & 1;
-        if (!mbar_wait(pfull + 8 * s, (pi >> 1) & 1)) { ok = false; break; }
+        if (!mbar_wait(pfull + 8 * s, (pi >> 1) & 1, P.spin)) { ok = false; break; }
         used[s]++;
         for (int rj = 0; rj < pl.z && ok; rj++, ri++) {
           const int bs = ri % nring;
-          if (!mbar_wait(bfull + 8 * bs, (ri / nring) & 1)) { ok = false; break; }
+          if (!mbar_wait(bfull + 8 * bs, (ri / nring) & 1, P.spin)) { ok = false; break; }
           if (*abort_flag) { ok = false; break; }
           used[2 + bs]++;
           tc_fence_after();
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
           for (int j = 0; j < hd.w; j++, bi++) {
             const int chunk = bi / kChunk, cb = chunk % kAccBufs;
             const bool chunk_start = bi % kChunk == 0;
-            if (chunk_start && chunk >= kAccBufs && !mbar_wait(aempty + 8 * cb, ((chunk / kAccBufs) - 1) & 1)) {
+            if (chunk_start && chunk >= kAccBufs && !mbar_wait(aempty + 8 * cb, ((chunk / kAccBufs) - 1) & 1, P.spin)) {
               ok = false;
               break;
             }
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
       bool got = false;
       for (int it = 0; it < 4 && !got; it++) {
         if (*abort_flag) break;
-        got = mbar_wait(afull + 8 * cb, (c / kAccBufs) & 1);
+        got = mbar_wait(afull + 8 * cb, (c / kAccBufs) & 1, P.spin);
       }
       got = __all_sync(0xffffffffu, got);
       if (!got) { ok = false; break; }
@@ -393,14 +394,14 @@ __global__ void __launch_bounds__(192, 1) k_sten_tc(const __grid_constant__ CUte
     }
   }
   // every MMA has completed before TMEM is freed; copies started but not consumed land before exit
-  if (threadIdx.x == 0) mbar_wait(accb, 0);
+  if (threadIdx.x == 0) mbar_wait(accb, 0, kSpin);
   tc_fence_before();
   __syncthreads();
   if (threadIdx.x == 0)
     for (int i = 0; i < 2 + nring; i++)
       if (armed[i] > used[i]) {
         const uint32_t bar = i < 2 ? pfull + 8 * i : bfull + 8 * (i - 2);
-        mbar_wait(bar, (armed[i] - 1) & 1);
+        mbar_wait(bar, (armed[i] - 1) & 1, kSpin);
       }
   __syncthreads();
   if (warp == 0) {
@@ -637,6 +638,7 @@ void launch_sten_tc(const float *pad_channel, const DevGeom &g, const TcSlab &sl
   a.out = out;
   a.accumulate = accumulate ? 1 : 0;
   a.err = sl.d_err;
+  a.spin = sl.spin > 0 ? sl.spin : kSpin;
   const int tiles = ((g.nx[0] + kTcN - 1) / kTcN) * ((g.nx[1] + kTcM - 1) / kTcM) * g.nx[2];
   const int ns = accumulate ? t.split_for(tiles, sl.nsm) : 1;
   a.nsplit = ns;

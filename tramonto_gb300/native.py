@@ -90,6 +90,7 @@ def load(build_if_missing: bool = False):
         "tgpu_set_fft_threshold": [vp, C.c_int],
         "tgpu_set_fft32_policy": [vp, C.c_int],
         "tgpu_fft32_choice": [vp, C.c_int, C.c_int, ip, dp],
+        "tgpu_set_tc_wait_limit": [vp, C.c_long],
         "tgpu_time_fft_pass": [vp, C.c_int, C.c_int, C.c_int, dp, C.POINTER(C.c_long), C.POINTER(C.c_long)],
         "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
