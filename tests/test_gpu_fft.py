@@ -151,3 +151,22 @@ def test_fp64_fft_products_match_fp64_products():
     print("64^3 FP64-FFT products: Schur rel", rel_err(S, S64), "Jv rel", rel_err(J, J64))
     assert rel_err(S, S64) <= 1e-11 and rel_err(J, J64) <= 1e-11
     s.close()
+
+
+def test_fft_sums_follow_a_moved_bulk_state():
+    """After tgpu_set_bulk_state (the continuation in the chemical potential) the FFT sums read the new bulk values
+    at the bulk boundary as the direct sums do: FP64-FFT fill = direct FP64 fill to 5e-12, FP32 fill to 1e-4."""
+    from tramonto_gb300 import native, setup
+    p, _ = setup.config2(n=40)
+    s = native.Solver(p)
+    x = setup.initial_state(s, p, max_enhancement=1.0)
+    s.set_bulk([0.66])
+    R64 = s.fill(x, mode=1)
+    s.set_fill_arithmetic(native.FILL_FFT)
+    Rf = s.fill(x, mode=1)
+    s.set_fill_arithmetic(native.FILL_FP32)
+    R32 = s.fill(x, mode=1)
+    print("moved bulk: |R_fft - R_fp64|", np.abs(Rf - R64).max(), "|R_fp32 - R_fp64|", np.abs(R32 - R64).max())
+    assert np.abs(Rf - R64).max() <= 5e-12
+    assert np.abs(R32 - R64).max() <= 1e-4 * max(1.0, np.abs(R64).max())
+    s.close()

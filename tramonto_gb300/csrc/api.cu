@@ -2450,6 +2450,8 @@ int tgpu_set_bulk_state(tgpu_handle h, const double *rho_b, const double *betamu
                        c->stream), "h2d");
     ck(cudaMemcpyAsync(c->pads.tr_res.bulk, bt.data(), bt.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream),
        "h2d");
+    c->pads.rho_res.h_bulk = br;   // the host copies the FFT sums read the boundary values from
+    c->pads.tr_res.h_bulk = bt;
     tgpu::upload_geom(dg, c->stream);
     g_geom_owner = c;
     c->have_state = false;
