@@ -348,6 +348,73 @@ double tgpu_pairpot_att(double r, const tgpu_pairpot *pp);
 /* r of the minimum of the cut-and-shifted LJ 12-6 potential, located by the
  * search of pairPot_find_rmin (src/dft_pairPot.c:98-152) */
 double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0);
+
+/* ---- Surfaces and their external fields (set-up; src/dft_surfaces.c setup_surface, src/dft_mesh.c
+ * boundary flags, src/dft_vext.c setup_external_field_n and setup_integrated_LJ_walls) ----
+ * The mesh is the reference's: Nodes_x = Size_x/Esize_x + 1 (Size_x/Esize_x when both ends are
+ * periodic), Elements_x = Size_x/Esize_x, node i at -Size_x/2 + i Esize_x, node and element index
+ * x fastest.  Each wall is a surface of one wall type placed at wall_pos (WallPos, dft_surfaces.dat).
+ * An element belongs to a wall when the surface test of its type (Surf_type) holds at the element
+ * centre (the reference's surface_*_inSurfaceTest), with the distance adjustment of the type's
+ * linear and periodic overlays (surface_linear_offset, surface_periodic_offset).  A node has zero
+ * density when no element around it is fluid for some wall (elements beyond an IN_WALL face count
+ * for no wall, beyond an IN_BULK face as fluid) or one wall owns all of them (src/dft_mesh.c:1060-1145).
+ * Walls of an integrated type (Ipot_wf_n = 5, Type_vext = VEXT_PAIR_POTENTIAL with the LJ 12-6 cut and
+ * shifted pair potential) add, at every other node, the wall-fluid potential integrated over each of
+ * their elements, their periodic and reflected images and, on IN_WALL / LAST_NODE faces, the element's
+ * copies beyond the face (max cut / Esize of them), in the reference's order, each sum stopped at
+ * vext_max once reached (setup_integrated_LJ_walls, src/dft_vext.c:671-865, integrate_potential and
+ * get_wt_from_sten, src/dft_vext_integrated.c:42-200).  Zero-density nodes hold vext_max, and a node
+ * whose field reaches vext_max has zero density (src/dft_vext.c:150-167).
+ * Not built (TGPU_ERR_UNSUPPORTED): roughness patches, angle cutouts, Lhard_surf, semi-permeable
+ * walls, atomic and single-element surfaces, 2-D slit pores of orientation 0, pair potentials
+ * other than LJ 12-6, Ipot_wf_n other than 0, 1 and 5. */
+#define TGPU_SURF_MAXWALLS 16
+#define TGPU_SURF_MAXTYPES 4
+#define TGPU_SURF_MAXFNC 4
+/* Surf_type values (src/dft_globals_const.h surface ids): planar wall, finite block, cylinder (2-D) /
+ * sphere (3-D), finite cylinder (3-D), cylindrical pore (2-D) / spherical cavity (3-D), slit pore (2-D) /
+ * finite cylindrical pore (3-D) */
+enum { TGPU_SURF_PLANAR = 0, TGPU_SURF_BLOCK = 1, TGPU_SURF_COLLOID = 2, TGPU_SURF_FINITE_CYL = 5,
+       TGPU_SURF_PORE = 7, TGPU_SURF_FINITE_PORE = 8 };
+/* Ipot_wf_n values: no wall-fluid term and hard walls (elements and zero density only), integrated LJ */
+enum { TGPU_VEXT_NONE = 0, TGPU_VEXT_HARD = 1, TGPU_VEXT_INTEGRATED = 5 };
+/* the reference's other boundary codes, read by the surface builder only */
+enum { TGPU_BC_LAST_NODE = 3, TGPU_BC_LAST_NODE_RESTART = 4 };
+typedef struct {
+  int surf_type, orientation;          /* Surf_type, Orientation */
+  double param[3];                     /* WallParam, WallParam_2, WallParam_3 */
+  int nperiodic;                       /* periodic overlays: offset += amplitude cos(2 pi (x - origin)/wavelength) */
+  int periodic_orient[TGPU_SURF_MAXFNC];
+  double amplitude[TGPU_SURF_MAXFNC], wavelength[TGPU_SURF_MAXFNC], periodic_origin[TGPU_SURF_MAXFNC];
+  int nlinear;                         /* linear overlays: offset += slope (x - origin) between origin and end */
+  int linear_orient[TGPU_SURF_MAXFNC];
+  double slope[TGPU_SURF_MAXFNC], linear_origin[TGPU_SURF_MAXFNC], linear_end[TGPU_SURF_MAXFNC];
+  int ipot_wf;                         /* TGPU_VEXT_* (Ipot_wf_n) */
+  double sigma_wf[TGPU_MAXC], eps_wf[TGPU_MAXC], cut_wf[TGPU_MAXC];   /* eps in kT */
+} tgpu_wall_type;
+typedef struct {
+  int ndim;
+  double size[3], esize[3];            /* Size_x, Esize_x */
+  int bc[3][2];                        /* Type_bc, TGPU_BC_* */
+  int ncomp;
+  double vext_max;                     /* VEXT_MAX */
+  int apply_offset[3];                 /* Lapply_offset (radius, half-length, -) of the pore and cylinder tests */
+  int ntypes;
+  tgpu_wall_type type[TGPU_SURF_MAXTYPES];
+  int nwalls;
+  int wall_type[TGPU_SURF_MAXWALLS];
+  double wall_pos[TGPU_SURF_MAXWALLS][3];
+} tgpu_surface_spec;
+/* nodes and elements per dimension of the spec's mesh (unused dims 1); TGPU_ERR_ARG when Size_x is
+ * not a multiple of Esize_x */
+int tgpu_surface_mesh(const tgpu_surface_spec *s, int *nodes, int *elements);
+/* the surface set-up on the GPU: vext [ncomp][nodes], zero [ncomp][nodes] (1 = zero density) and, when
+ * wall_el is not NULL, the walls of each element as a bit mask [elements].  Host buffers; the
+ * _device variant takes device buffers (current device, default stream, synchronised). */
+int tgpu_surface_field_host(const tgpu_surface_spec *s, double *vext, signed char *zero, unsigned short *wall_el);
+int tgpu_surface_field_device(const tgpu_surface_spec *s, double *d_vext, signed char *d_zero,
+                              unsigned short *d_wall_el);
 /* the WCA attraction u_att(r) in kT (uLJ12_6_ATT_CS, src/dft_pairPot_LJ12_6.c:128-168) */
 double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double rmin);
 
@@ -372,8 +439,7 @@ double tgpu_uatt(double r, double sigma, double eps_over_kT, double rcut, double
  * than the box, or a mirrored point beyond the far side when that side is
  * periodic or reflecting) returns TGPU_ERR_UNSUPPORTED.  These checks run on
  * the host before any device work.  The first
- * call on a device looks up the device addresses of those arrays (make that
- * first call before any stream capture).  Every call shares the arrays and
+ * call on a device looks up the device addresses of those arrays.  Every call shares the arrays and
  * rewrites what it reads; calls whose work overlaps on the GPU race.  Returns
  * after the sum is complete on `stream` (NULL: the legacy default stream). */
 #define TGPU_NOALLOC_MAX_PADDED 2097152

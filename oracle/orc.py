@@ -22,14 +22,38 @@ MAXZ = 5
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h"))):
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "surfaces.c")]
+    deps = srcs + [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "..", "include", "tramonto_gpu.h")]
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(f) for f in deps):
         os.makedirs(BUILD, exist_ok=True)
         tmp = LIB + f".tmp{os.getpid()}"
-        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-o", tmp, src, "-lm"], check=True)
+        # no contraction of multiply-adds: the surface restatement keeps the reference's operations
+        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-ffp-contract=off", "-o", tmp, *srcs, "-lm"],
+                       check=True)
         os.replace(tmp, LIB)
     return LIB
+
+
+def surface_field(spec):
+    """The restatement of the reference's surface set-up (oracle/surfaces.c) for a tramonto_gb300.surfaces
+    SurfaceSpec: (V_ext [ncomp][nodes], zero flags [ncomp][nodes] int8, element wall masks uint16)."""
+    lib = C.CDLL(build())
+    nodes, els = [1, 1, 1], [1, 1, 1]
+    for d in range(spec.ndim):
+        nodes[d] = int(np.floor(spec.size[d] / spec.esize[d] + 1.0 + 0.5))
+        els[d] = nodes[d] - 1
+        if spec.bc[d][0] == 1 and spec.bc[d][1] == 1:
+            nodes[d] -= 1
+    n, ne = int(np.prod(nodes)), int(np.prod(els))
+    vext = np.zeros((spec.ncomp, n))
+    zero = np.zeros((spec.ncomp, n), np.int8)
+    wall_el = np.zeros(ne, np.uint16)
+    fn = lib.oracle_surface_field
+    fn.argtypes = [C.c_void_p] * 4
+    fn.restype = C.c_int
+    if fn(C.addressof(spec), vext.ctypes.data, zero.ctypes.data, wall_el.ctypes.data) != 0:
+        raise ValueError("the surface restatement does not cover this spec")
+    return vext, zero, wall_el
 
 
 class _Problem(C.Structure):

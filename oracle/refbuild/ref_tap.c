@@ -344,3 +344,28 @@ int tref_energy(double *omega_s, double *ads, double *ads_b)
   }
   return 0;
 }
+
+/* Surfaces: ints Nwall Nwall_type Nlists_HW Nelements_box Nwall_Images, WallType[Nwall];
+ * doubles WallPos[Nwall][3], then Sigma_wf Eps_wf Cut_wf [Ncomp][Nwall_type] each (effective values
+ * after mixing and scaling), then WallPos_Images[Nwall_Images][3] */
+int tref_wall_info(int *oi, double *od)
+{
+  int k = 0, j = 0, i, w, d;
+  oi[k++] = Nwall; oi[k++] = Nwall_type; oi[k++] = Nlists_HW; oi[k++] = Nelements_box; oi[k++] = Nwall_Images;
+  for (w = 0; w < Nwall; w++) oi[k++] = WallType[w];
+  for (w = 0; w < Nwall; w++) for (d = 0; d < 3; d++) od[j++] = d < Ndim ? WallPos[d][w] : 0.0;
+  for (i = 0; i < Ncomp; i++) for (w = 0; w < Nwall_type; w++) od[j++] = Sigma_wf[i][w];
+  for (i = 0; i < Ncomp; i++) for (w = 0; w < Nwall_type; w++) od[j++] = Eps_wf[i][w];
+  for (i = 0; i < Ncomp; i++) for (w = 0; w < Nwall_type; w++) od[j++] = Cut_wf[i][w];
+  for (w = 0; w < Nwall_Images; w++) for (d = 0; d < 3; d++) od[j++] = d < Ndim ? WallPos_Images[w][d] : 0.0;
+  return k;
+}
+
+/* Wall_elems[Nlists_HW-1][iel_box] (the last wall that owns each element, -1 for fluid) */
+int tref_wall_elems(int *out)
+{
+  int e;
+  if (Wall_elems == NULL) return -1;
+  for (e = 0; e < Nelements_box; e++) out[e] = Wall_elems[Nlists_HW - 1][e];
+  return 0;
+}

@@ -179,6 +179,22 @@ def _child_extract(deck_lines, surfaces_from, opts, q):
             zt = np.zeros(ncomp * nbox, np.int32)
             lib.tref_get_zero_density(ip(zt))
             out["zero_density"] = zt.reshape(ncomp, nbox)
+            if int(ints[15]) > 0:   # Nwall: the surfaces (positions, images, wall-fluid parameters, elements)
+                wi = np.zeros(64, np.int32)
+                wd = np.zeros(4096, np.float64)
+                lib.tref_wall_info(ip(wi), dp(wd))
+                nwall, ntype, _, nel, nimg = (int(v) for v in wi[:5])
+                out["wall_type"] = wi[5:5 + nwall].copy()
+                k = 0
+                out["wall_pos"] = wd[k:k + 3 * nwall].reshape(nwall, 3).copy()
+                k += 3 * nwall
+                for key in ("sigma_wf", "eps_wf", "cut_wf"):
+                    out[key] = wd[k:k + ncomp * ntype].reshape(ncomp, ntype).copy()
+                    k += ncomp * ntype
+                out["wall_images"] = wd[k:k + 3 * nimg].reshape(nimg, 3).copy()
+                we = np.zeros(nel, np.int32)
+                if lib.tref_wall_elems(ip(we)) == 0:
+                    out["wall_elems"] = we
             if lhard and nlists > 0:
                 bn = np.zeros(nlists * nbox, np.int32)
                 if lib.tref_get_boundary_nodes(ip(bn)) == 0:

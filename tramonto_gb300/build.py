@@ -20,8 +20,10 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr",
            "-diag-suppress", "550,177"]
-# stencils.cu: the host and device stencil builders must perform the same IEEE operations
-FILE_FLAGS = {"stencils.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
+# stencils.cu: the host and device stencil builders must perform the same IEEE operations;
+# surfaces.cu: positions, distances and rule choices with the reference's operations
+FILE_FLAGS = {"stencils.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+              "surfaces.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:

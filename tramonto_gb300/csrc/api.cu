@@ -2222,6 +2222,10 @@ void build_device_tables(Ctx *c)
 
 }  // namespace
 
+namespace tgpu {
+void set_last_error(const std::string &text) { g_last_error = text; }
+}  // namespace tgpu
+
 extern "C" {
 
 const char *tgpu_last_error(void) { return g_last_error.c_str(); }

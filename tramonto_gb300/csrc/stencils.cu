@@ -777,6 +777,11 @@ int make_stencil(bool device, int type, int ndim, const double *esize, double hs
 
 }  // namespace
 
+namespace tgpu {
+// the n-point Gauss-Legendre rule on [0,1] of the stencil builder, for the other set-up code
+void gauss_rule01(int n, double *x, double *w) { gauss01(n, x, w); }
+}  // namespace tgpu
+
 extern "C" {
 
 double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0)

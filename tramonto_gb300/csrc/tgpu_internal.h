@@ -569,4 +569,10 @@ void launch_check_finite(const double *x, long n, double *partial, int nblocks, 
 
 int reduce_blocks(long n);
 
+// the n-point Gauss-Legendre rule mapped to [0,1] (nodes ascending, weights summing to 1; stencils.cu)
+void gauss_rule01(int n, double *x, double *w);
+
+// the text tgpu_last_error() returns (api.cu), for entry points outside api.cu
+void set_last_error(const std::string &text);
+
 }  // namespace tgpu

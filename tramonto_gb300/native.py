@@ -121,6 +121,8 @@ def load(build_if_missing: bool = False):
         "tgpu_grad_omega_vext": [vp, vp, C.c_double, C.c_int, vp, ip],
         "tgpu_grad_gamma_vext": [vp, vp, C.c_int, C.c_double, C.c_int, vp, ip],
         "tgpu_grad_epsw": [vp, vp, C.c_int, C.c_int, vp, C.c_double, C.c_int, dp, ip],
+        "tgpu_surface_mesh": [vp, ip, ip],
+        "tgpu_surface_field_host": [vp, vp, vp, vp], "tgpu_surface_field_device": [vp, vp, vp, vp],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)

@@ -1,0 +1,308 @@
+"""Surfaces and their external fields, built on the GPU (tgpu_surface_field_*, csrc/surfaces.cu).
+
+A reference user describes walls in the input deck (dft_input.dat: mesh, boundaries, the surface
+and wall-fluid sections) and their positions in dft_surfaces.dat.  :func:`read_deck` reads those
+sections into a :class:`SurfaceSpec`; :func:`surface_field` returns the external field V_ext/kT
+[ncomp][nodes], the zero-density flags [ncomp][nodes] and the walls of every element, as the
+reference's set-up computes them (setup_surface, src/dft_surfaces.c:39; setup_external_field_n,
+src/dft_vext.c:38; setup_integrated_LJ_walls, src/dft_vext.c:671).  :func:`problem_fields` gives
+them in the layout build_problem takes.
+
+The deck is read by the labels of its '@' lines, as the reference's input reader reads fields in
+order (src/dft_input.c): the wall-fluid parameters follow its mixing rules (Lorentz-Berthelot for
+Mix_type 0, src/dft_potential_params.c:120-125; the deck's values for Mix_type 1).  Parts of the
+deck this path does not build (roughness, angle cutouts, Lhard_surf, 9-3 walls of Ipot_wf_n 2 and 3,
+pair potentials other than LJ 12-6, a positive Temp or Length_ref) raise NotImplementedError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import native
+
+MAXC, MAXWALLS, MAXTYPES, MAXFNC = 4, 16, 4, 4
+SURF_PLANAR, SURF_BLOCK, SURF_COLLOID, SURF_FINITE_CYL, SURF_PORE, SURF_FINITE_PORE = 0, 1, 2, 5, 7, 8
+VEXT_NONE, VEXT_HARD, VEXT_INTEGRATED = 0, 1, 5
+BC_IN_WALL, BC_IN_BULK, BC_PERIODIC, BC_REFLECT, BC_LAST_NODE, BC_LAST_NODE_RESTART = -1, 0, 1, 2, 3, 4
+
+
+class WallType(C.Structure):
+    _fields_ = [("surf_type", C.c_int), ("orientation", C.c_int), ("param", C.c_double * 3),
+                ("nperiodic", C.c_int), ("periodic_orient", C.c_int * MAXFNC), ("amplitude", C.c_double * MAXFNC),
+                ("wavelength", C.c_double * MAXFNC), ("periodic_origin", C.c_double * MAXFNC),
+                ("nlinear", C.c_int), ("linear_orient", C.c_int * MAXFNC), ("slope", C.c_double * MAXFNC),
+                ("linear_origin", C.c_double * MAXFNC), ("linear_end", C.c_double * MAXFNC),
+                ("ipot_wf", C.c_int), ("sigma_wf", C.c_double * MAXC), ("eps_wf", C.c_double * MAXC),
+                ("cut_wf", C.c_double * MAXC)]
+
+
+class SurfaceSpec(C.Structure):
+    """tgpu_surface_spec (include/tramonto_gpu.h)."""
+    _fields_ = [("ndim", C.c_int), ("size", C.c_double * 3), ("esize", C.c_double * 3),
+                ("bc", (C.c_int * 2) * 3), ("ncomp", C.c_int), ("vext_max", C.c_double),
+                ("apply_offset", C.c_int * 3), ("ntypes", C.c_int), ("type", WallType * MAXTYPES),
+                ("nwalls", C.c_int), ("wall_type", C.c_int * MAXWALLS), ("wall_pos", (C.c_double * 3) * MAXWALLS)]
+
+    def mesh(self):
+        """(nodes[3], elements[3]) of the spec's mesh (unused dimensions 1)."""
+        lib = native.load()
+        nodes, els = (C.c_int * 3)(), (C.c_int * 3)()
+        native._check(lib.tgpu_surface_mesh(C.byref(self), nodes, els), lib)
+        return list(nodes), list(els)
+
+
+def make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=10.0, apply_offset=(0, 0, 0)):
+    """A SurfaceSpec from plain values: bc [(lo, hi)] per dimension; types a list of dicts (surf_type,
+    orientation, param, ipot_wf, sigma_wf, eps_wf, cut_wf per component, optional periodic / linear
+    lists of (orientation, amplitude, wavelength, origin) / (orientation, slope, origin, end));
+    walls a list of (type index, position)."""
+    s = SurfaceSpec()
+    s.ndim, s.ncomp, s.vext_max = int(ndim), int(ncomp), float(vext_max)
+    for d in range(3):
+        s.size[d] = float(size[d]) if d < ndim else 0.0
+        s.esize[d] = float(esize[d]) if d < ndim else 0.0
+        lo, hi = bc[d] if d < ndim else (BC_IN_BULK, BC_IN_BULK)
+        s.bc[d][0], s.bc[d][1] = int(lo), int(hi)
+        s.apply_offset[d] = int(apply_offset[d])
+    if len(types) > MAXTYPES or len(walls) > MAXWALLS or ncomp > MAXC:
+        raise ValueError("too many wall types, walls or components")
+    s.ntypes = len(types)
+    for t, T in enumerate(types):
+        o = s.type[t]
+        o.surf_type, o.orientation = int(T["surf_type"]), int(T.get("orientation", 0))
+        for k, v in enumerate(T.get("param", (0.0, 0.0, 0.0))[:3]):
+            o.param[k] = float(v)
+        per = T.get("periodic", [])
+        lin = T.get("linear", [])
+        if len(per) > MAXFNC or len(lin) > MAXFNC:
+            raise ValueError("too many overlay functions")
+        o.nperiodic = len(per)
+        for i, (ori, amp, wl, org) in enumerate(per):
+            o.periodic_orient[i], o.amplitude[i], o.wavelength[i], o.periodic_origin[i] = int(ori), amp, wl, org
+        o.nlinear = len(lin)
+        for i, (ori, sl, org, end) in enumerate(lin):
+            o.linear_orient[i], o.slope[i], o.linear_origin[i], o.linear_end[i] = int(ori), sl, org, end
+        o.ipot_wf = int(T.get("ipot_wf", VEXT_HARD))
+        for c in range(ncomp):
+            o.sigma_wf[c] = float(T.get("sigma_wf", [0.0] * ncomp)[c])
+            o.eps_wf[c] = float(T.get("eps_wf", [0.0] * ncomp)[c])
+            o.cut_wf[c] = float(T.get("cut_wf", [0.0] * ncomp)[c])
+    s.nwalls = len(walls)
+    for w, (t, pos) in enumerate(walls):
+        s.wall_type[w] = int(t)
+        for d in range(3):
+            s.wall_pos[w][d] = float(pos[d]) if d < len(pos) else 0.0
+    return s
+
+
+def surface_field(spec: SurfaceSpec):
+    """V_ext/kT [ncomp][nodes], zero-density flags [ncomp][nodes] (int8) and the wall bit mask of every
+    element [elements] (uint16), computed on the GPU."""
+    nodes, els = spec.mesh()
+    n, ne = int(np.prod(nodes)), int(np.prod(els))
+    vext = np.zeros((spec.ncomp, n))
+    zero = np.zeros((spec.ncomp, n), np.int8)
+    wall_el = np.zeros(ne, np.uint16)
+    lib = native.load()
+    native._check(lib.tgpu_surface_field_host(C.byref(spec), vext.ctypes.data, zero.ctypes.data,
+                                              wall_el.ctypes.data), lib)
+    return vext, zero, wall_el
+
+
+# ---- reading the surface part of a reference input deck ----------------------------------------------
+
+def _deck_fields(text):
+    """[(values, label)] of the '@' lines: values are the leading numeric tokens (n/a as None)."""
+    out = []
+    for line in text.splitlines():
+        if not line.startswith("@"):
+            continue
+        toks = line[1:].split()
+        vals, k = [], 0
+        for k, t in enumerate(toks):
+            if t.lower() == "n/a":
+                vals.append(None)
+                continue
+            try:
+                vals.append(float(t))
+            except ValueError:
+                break
+        else:
+            k = len(toks)
+        out.append((vals, " ".join(toks[k:])))
+    return out
+
+
+class _Deck:
+    def __init__(self, text):
+        self.fields = _deck_fields(text)
+
+    def get(self, key, n=None):
+        """the values of the one line whose label starts with key (or, for a key in parentheses, holds it)"""
+        if key.startswith("("):
+            hits = [v for v, lab in self.fields if key[1:-1] in lab]
+        else:
+            hits = [v for v, lab in self.fields if lab.startswith(key)]
+        if len(hits) != 1:
+            raise KeyError(f"deck label {key!r} matched {len(hits)} lines")
+        v = hits[0]
+        return v if n is None else v[:n]
+
+
+def read_deck(input_path, surfaces_path=None):
+    """A SurfaceSpec from a reference input deck (dft_input.dat) and its wall positions
+    (dft_surfaces.dat beside it unless surfaces_path is given)."""
+    with open(input_path) as f:
+        dk = _Deck(f.read())
+    if surfaces_path is None:
+        surfaces_path = os.path.join(os.path.dirname(os.path.abspath(input_path)), "dft_surfaces.dat")
+    length_ref, _, temp, _, vext_max = dk.get("Length_ref", 5)
+    if (length_ref is not None and length_ref > 0) or (temp is not None and temp > 0):
+        raise NotImplementedError("dimensioned units (Length_ref or Temp > 0)")
+    ndim = int(dk.get("Ndim", 1)[0])
+    size = dk.get("Size_x", ndim)
+    esize = dk.get("Esize_x", ndim)
+    bc = [tuple(int(v) for v in dk.get(f"Type_bc(x{d}", 2)) for d in range(ndim)]
+    ntypes, nwalls, _, auto_center, auto_size = (int(v) for v in dk.get("Nwall_types Nwall", 5))
+    if auto_size:
+        raise NotImplementedError("Lauto_size")
+    surf = [int(v) for v in dk.get("Surf_type", ntypes)]
+    orient = [int(v) for v in dk.get("Orientation[iwall_type]", ntypes)]
+    p1 = dk.get("WallParam[", ntypes)
+    p2 = dk.get("WallParam2", ntypes)
+    p3 = dk.get("WallParam3", ntypes)
+    apply = [int(v) for v in dk.get("Lapply_of", 3)]
+    if any(int(v) for v in dk.get("Lrough_surf", ntypes)):
+        raise NotImplementedError("roughness patches")
+    nper = [int(v) for v in dk.get("Nperiodic_overlay", ntypes)]
+    nlin = [int(v) for v in dk.get("Nlinear_overlay", ntypes)]
+    if any(int(v) for v in dk.get("LangleCutout", ntypes)):
+        raise NotImplementedError("angle cutouts")
+
+    def per_type(key, counts):
+        if sum(counts) == 0:
+            return [[] for _ in counts]
+        # a line with fewer values than functions: the reference's read of the missing ones fails and
+        # leaves its zero-initialised arrays unchanged
+        vals = list(dk.get(key, sum(counts)))
+        vals += [0.0] * (sum(counts) - len(vals))
+        out, k = [], 0
+        for c in counts:
+            out.append(vals[k:k + c])
+            k += c
+        return out
+
+    p_or = per_type("OrientationPeriodic", nper)
+    p_amp = per_type("Amplitude[", nper)
+    p_wl = per_type("Period[", nper)
+    p_org = per_type("Origin[iwall_type]", nper)
+    l_or = per_type("OrientationLinear", nlin)
+    l_sl = per_type("Slope[", nlin)
+    l_org = per_type("Origin_linear", nlin)
+    l_end = per_type("Endpoint_linear", nlin)
+    ipot = [int(v) for v in dk.get("(Ipot_wf_n)", ntypes)]
+    if int(dk.get("Lhard_surf", 1)[0]):
+        raise NotImplementedError("Lhard_surf")
+    tvext = [int(v) for v in dk.get("Type_vext[", ntypes)]
+    potid = [int(v) for v in dk.get("Vext_PotentialID", ntypes)]
+    ncomp, mix = (int(v) for v in dk.get("Ncomp Mix_type", 2))
+    for t in range(ntypes):
+        if ipot[t] not in (VEXT_NONE, VEXT_HARD, VEXT_INTEGRATED):
+            raise NotImplementedError(f"Ipot_wf_n = {ipot[t]}")
+        if ipot[t] == VEXT_INTEGRATED and (tvext[t] != 1 or potid[t] != 0):
+            raise NotImplementedError("integrated walls other than the LJ 12-6 pair potential")
+    nff = ncomp if mix == 0 else ncomp * ncomp
+    nww = ntypes if mix == 0 else ntypes * ntypes
+    if mix == 0:
+        sff = dk.get("Sigma_ff", nff)
+        eff = dk.get("Eps_ff", nff)
+        cff = dk.get("Cut_ff", nff)
+        sww = dk.get("Sigma_ww", nww)
+        eww = dk.get("Eps_ww", nww)
+        cww = dk.get("Cut_ww", nww)
+        # Lorentz-Berthelot (src/dft_potential_params.c:120-125)
+        swf = [[0.5 * (sff[i] + sww[t]) for i in range(ncomp)] for t in range(ntypes)]
+        ewf = [[math.sqrt(eff[i] * eww[t]) for i in range(ncomp)] for t in range(ntypes)]
+        cwf = [[0.5 * (cff[i] + cww[t]) for i in range(ncomp)] for t in range(ntypes)]
+    else:
+        nwf = ncomp * ntypes
+        s_in, e_in, c_in = dk.get("Sigma_wf", nwf), dk.get("Eps_wf", nwf), dk.get("Cut_wf", nwf)
+        swf = [[s_in[i * ntypes + t] for i in range(ncomp)] for t in range(ntypes)]
+        ewf = [[e_in[i * ntypes + t] for i in range(ncomp)] for t in range(ntypes)]
+        cwf = [[c_in[i * ntypes + t] for i in range(ncomp)] for t in range(ntypes)]
+    types = []
+    for t in range(ntypes):
+        types.append(dict(surf_type=surf[t], orientation=orient[t], param=(p1[t], p2[t], p3[t]), ipot_wf=ipot[t],
+                          sigma_wf=swf[t], eps_wf=ewf[t], cut_wf=cwf[t],
+                          periodic=[(int(p_or[t][i]), p_amp[t][i], p_wl[t][i], p_org[t][i]) for i in range(nper[t])],
+                          linear=[(int(l_or[t][i]), l_sl[t][i], l_org[t][i], l_end[t][i]) for i in range(nlin[t])]))
+    with open(surfaces_path) as f:
+        toks = f.read().split()
+    walls, k = [], 0
+    for _ in range(nwalls):
+        wt = int(toks[k])
+        pos = [float(toks[k + 2 + d]) for d in range(ndim)]
+        walls.append((wt, pos))
+        k += 2 + ndim + 1          # type, link, position, Elec_param_w
+    if auto_center:
+        lo = [min(w[1][d] for w in walls) for d in range(ndim)]
+        hi = [max(w[1][d] for w in walls) for d in range(ndim)]
+        walls = [(t, [p[d] - 0.5 * (hi[d] + lo[d]) for d in range(ndim)]) for t, p in walls]
+    return make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=vext_max, apply_offset=apply)
+
+
+def problem_fields(spec: SurfaceSpec):
+    """(vext, zero_density) for build_problem: V_ext/kT [ncomp][nodes] and int8 flags."""
+    vext, zero, _ = surface_field(spec)
+    return vext, zero
+
+
+def spec_arrays(spec: SurfaceSpec) -> dict:
+    """The spec as named numpy arrays (for storing next to results); spec_from_arrays inverts it."""
+    nt, nw = spec.ntypes, spec.nwalls
+    a = {"ndim": np.int32(spec.ndim), "size": np.array(spec.size[:]), "esize": np.array(spec.esize[:]),
+         "bc": np.array([[spec.bc[d][0], spec.bc[d][1]] for d in range(3)], np.int32),
+         "ncomp": np.int32(spec.ncomp), "vext_max": np.float64(spec.vext_max),
+         "apply_offset": np.array(spec.apply_offset[:], np.int32),
+         "wall_type": np.array(spec.wall_type[:nw], np.int32),
+         "wall_pos": np.array([spec.wall_pos[w][:] for w in range(nw)]).reshape(nw, 3)}
+    for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf"):
+        a["t_" + f] = np.array([getattr(spec.type[t], f) for t in range(nt)], np.int32)
+    for f in ("periodic_orient", "linear_orient"):
+        a["t_" + f] = np.array([getattr(spec.type[t], f)[:] for t in range(nt)], np.int32).reshape(nt, MAXFNC)
+    for f, n in (("param", 3), ("amplitude", MAXFNC), ("wavelength", MAXFNC), ("periodic_origin", MAXFNC),
+                 ("slope", MAXFNC), ("linear_origin", MAXFNC), ("linear_end", MAXFNC), ("sigma_wf", MAXC),
+                 ("eps_wf", MAXC), ("cut_wf", MAXC)):
+        a["t_" + f] = np.array([getattr(spec.type[t], f)[:] for t in range(nt)]).reshape(nt, n)
+    return a
+
+
+def spec_from_arrays(a) -> SurfaceSpec:
+    s = SurfaceSpec()
+    s.ndim, s.ncomp, s.vext_max = int(a["ndim"]), int(a["ncomp"]), float(a["vext_max"])
+    for d in range(3):
+        s.size[d], s.esize[d] = float(a["size"][d]), float(a["esize"][d])
+        s.bc[d][0], s.bc[d][1] = int(a["bc"][d][0]), int(a["bc"][d][1])
+        s.apply_offset[d] = int(a["apply_offset"][d])
+    nt = len(a["t_surf_type"])
+    s.ntypes = nt
+    for t in range(nt):
+        o = s.type[t]
+        for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf"):
+            setattr(o, f, int(a["t_" + f][t]))
+        for f in ("periodic_orient", "linear_orient", "param", "amplitude", "wavelength", "periodic_origin", "slope",
+                  "linear_origin", "linear_end", "sigma_wf", "eps_wf", "cut_wf"):
+            arr = getattr(o, f)
+            for i, v in enumerate(a["t_" + f][t]):
+                arr[i] = v
+    nw = len(a["wall_type"])
+    s.nwalls = nw
+    for w in range(nw):
+        s.wall_type[w] = int(a["wall_type"][w])
+        for d in range(3):
+            s.wall_pos[w][d] = float(a["wall_pos"][w][d])
+    return s
