@@ -366,9 +366,14 @@ double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0
  * vext_max once reached (setup_integrated_LJ_walls, src/dft_vext.c:671-865, integrate_potential and
  * get_wt_from_sten, src/dft_vext_integrated.c:42-200).  Zero-density nodes hold vext_max, and a node
  * whose field reaches vext_max has zero density (src/dft_vext.c:150-167).
+ * Walls of Ipot_wf_n 2 and 3 add, at every other node, a potential of the distance X_wall from the node
+ * to the wall's surface (or centre) as the surface test measures it with the overlay adjustment of the
+ * node's element (src/dft_surfaces.c:400-430): a 1-D wall form (Type_vext 0) or the LJ 12-6 pair
+ * potential (Type_vext 1), a node with X_wall <= 0.001 holding vext_max (setup_vext_XRSurf,
+ * src/dft_vext.c:364-436); wall images add nothing (their X_wall is 1000, beyond every cut).
  * Not built (TGPU_ERR_UNSUPPORTED): roughness patches, angle cutouts, Lhard_surf, semi-permeable
  * walls, atomic and single-element surfaces, 2-D slit pores of orientation 0, pair potentials
- * other than LJ 12-6, Ipot_wf_n other than 0, 1 and 5. */
+ * other than LJ 12-6, the charged (LINEAR) and Yukawa 1-D forms, Ipot_wf_n 4. */
 #define TGPU_SURF_MAXWALLS 16
 #define TGPU_SURF_MAXTYPES 4
 #define TGPU_SURF_MAXFNC 4
@@ -377,8 +382,15 @@ double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0
  * finite cylindrical pore (3-D) */
 enum { TGPU_SURF_PLANAR = 0, TGPU_SURF_BLOCK = 1, TGPU_SURF_COLLOID = 2, TGPU_SURF_FINITE_CYL = 5,
        TGPU_SURF_PORE = 7, TGPU_SURF_FINITE_PORE = 8 };
-/* Ipot_wf_n values: no wall-fluid term and hard walls (elements and zero density only), integrated LJ */
-enum { TGPU_VEXT_NONE = 0, TGPU_VEXT_HARD = 1, TGPU_VEXT_INTEGRATED = 5 };
+/* Ipot_wf_n values: no wall-fluid term and hard walls (elements and zero density only), a potential of the
+ * distance from the node to the surface or to the surface's centre, integrated LJ */
+enum { TGPU_VEXT_NONE = 0, TGPU_VEXT_HARD = 1, TGPU_VEXT_DIST_TO_SURF = 2, TGPU_VEXT_DIST_TO_CENTER = 3,
+       TGPU_VEXT_INTEGRATED = 5 };
+/* Vext_PotentialID values of the 1-D wall forms (src/dft_vext_1D.c): 9-3 cut and shifted, its variant
+ * without the 2 pi sigma^3 / 3 factor, 9-3 without the shift, the shifted-distance form, the 9 repulsion,
+ * the attractive exponential */
+enum { TGPU_WALL1D_LJ93_CS = 0, TGPU_WALL1D_LJ93_V2_CS = 1, TGPU_WALL1D_LJ93_NOCS = 2,
+       TGPU_WALL1D_LJ93_SHIFTX_CS = 3, TGPU_WALL1D_REPULSIVE9 = 4, TGPU_WALL1D_EXP_ATT = 5 };
 /* the reference's other boundary codes, read by the surface builder only */
 enum { TGPU_BC_LAST_NODE = 3, TGPU_BC_LAST_NODE_RESTART = 4 };
 typedef struct {
@@ -391,6 +403,9 @@ typedef struct {
   int linear_orient[TGPU_SURF_MAXFNC];
   double slope[TGPU_SURF_MAXFNC], linear_origin[TGPU_SURF_MAXFNC], linear_end[TGPU_SURF_MAXFNC];
   int ipot_wf;                         /* TGPU_VEXT_* (Ipot_wf_n) */
+  int type_vext;                       /* Type_vext: 0 a 1-D wall form (VEXT_DEFINED), 1 the pair potential */
+  int pot_id;                          /* Vext_PotentialID: a TGPU_WALL1D_* form, or 0 (LJ 12-6) for type_vext 1 */
+  double rho_w;                        /* Rho_w: the 1-D forms' prefactor is eps_wf rho_w */
   double sigma_wf[TGPU_MAXC], eps_wf[TGPU_MAXC], cut_wf[TGPU_MAXC];   /* eps in kT */
 } tgpu_wall_type;
 typedef struct {
@@ -399,6 +414,7 @@ typedef struct {
   int bc[3][2];                        /* Type_bc, TGPU_BC_* */
   int ncomp;
   double vext_max;                     /* VEXT_MAX */
+  double sigma_ff[TGPU_MAXC];          /* Sigma_ff[i][i] (the shifted 9-3 form) */
   int apply_offset[3];                 /* Lapply_offset (radius, half-length, -) of the pore and cylinder tests */
   int ntypes;
   tgpu_wall_type type[TGPU_SURF_MAXTYPES];

@@ -189,6 +189,122 @@ static int or_in_surface(const tgpu_surface_spec *s, const tgpu_wall_type *T, co
   }
 }
 
+/* delx_vext of the surface tests (the same src/dft_surfaces_*.c functions) */
+static double or_surface_dist(const tgpu_surface_spec *s, const tgpu_wall_type *T, const double *wp, const double *xt,
+                              double adj, int flag_X_to_center)
+{
+  int nd = s->ndim, idim;
+  double radius, halflength, r12, x12, sq;
+  switch (T->surf_type) {
+    case TGPU_SURF_PLANAR: {
+      double halfwidth = T->param[0];
+      halfwidth += adj - OR_ROFF;
+      x12 = fabs(wp[T->orientation] - xt[T->orientation]);
+      return flag_X_to_center ? x12 : x12 - halfwidth;
+    }
+    case TGPU_SURF_BLOCK: {
+      int in = 1;
+      double rsq_surface = 0.0, rsq_center = 0.0;
+      for (idim = 0; idim < nd; idim++) {
+        double halfwidth = T->param[idim] + adj - OR_ROFF, xtest;
+        x12 = fabs(wp[idim] - xt[idim]);
+        if (x12 > halfwidth) in = 0;
+        xtest = x12 - halfwidth;
+        if (xtest > 0) {
+          rsq_surface += xtest * xtest;
+          rsq_center += x12 * x12;
+        }
+      }
+      if (in) return 0.0;
+      return flag_X_to_center ? sqrt(rsq_center) : sqrt(rsq_surface);
+    }
+    case TGPU_SURF_COLLOID:
+    case TGPU_SURF_PORE:
+      radius = T->param[0] + adj - OR_ROFF;
+      sq = 0.0;
+      for (idim = 0; idim < nd; idim++) {
+        x12 = wp[idim] - xt[idim];
+        sq += x12 * x12;
+      }
+      r12 = sqrt(sq);
+      if (T->surf_type == TGPU_SURF_PORE) return radius - r12;
+      return flag_X_to_center ? r12 : r12 - radius;
+    default: {
+      double xtest[3], delr_sq = 0.0, delr_sq_center = 0.0;
+      int dim[3];
+      if (s->apply_offset[0]) radius = T->param[0] + adj - OR_ROFF;
+      else radius = T->param[0] - OR_ROFF;
+      if (s->apply_offset[1]) halflength = T->param[1] + adj - OR_ROFF;
+      else halflength = T->param[1] - OR_ROFF;
+      if (nd == 3) {
+        switch (T->orientation) {
+          case 2: dim[0] = 0; dim[1] = 1; dim[2] = 2; break;
+          case 1: dim[0] = 2; dim[1] = 0; dim[2] = 1; break;
+          default: dim[0] = 1; dim[1] = 2; dim[2] = 0; break;
+        }
+      } else {
+        dim[0] = 0; dim[1] = 1; dim[2] = 1;
+      }
+      for (idim = 0; idim < 3; idim++) xtest[idim] = xt[dim[idim]];
+      sq = 0.0;
+      for (idim = 0; idim < nd - 1; idim++) {
+        double dx = xtest[idim] - wp[dim[idim]];
+        sq = sq + dx * dx;
+      }
+      r12 = sqrt(sq);
+      x12 = fabs(wp[dim[nd - 1]] - xtest[nd - 1]);
+      if (T->surf_type == TGPU_SURF_FINITE_CYL) {
+        if (r12 > radius) delr_sq += (r12 - radius) * (r12 - radius);
+        if (x12 > halflength) delr_sq += (x12 - halflength) * (x12 - halflength);
+        if (r12 > radius) delr_sq_center += (r12) * (r12);
+        if (x12 > halflength) delr_sq_center += (x12) * (x12);
+        return flag_X_to_center ? sqrt(delr_sq_center) : sqrt(delr_sq);
+      }
+      if (x12 > halflength) delr_sq += (x12 - halflength) * (x12 - halflength);
+      if (r12 < radius) delr_sq += (radius - r12) * (radius - r12);
+      return sqrt(delr_sq);
+    }
+  }
+}
+
+static double or_ulj(double r, double sigma, double eps, double rcut);
+
+/* Vext_1D (src/dft_switch_vext1D.c:42-80 with src/dft_vext_1D.c) or the LJ 12-6 pair potential */
+static double or_vext_1d(const tgpu_surface_spec *s, const tgpu_wall_type *T, int icomp, double x)
+{
+  double prefac = T->eps_wf[icomp] * T->rho_w, sigma = T->sigma_wf[icomp], cut = T->cut_wf[icomp];
+  if (T->type_vext == 1) return or_ulj(x, sigma, T->eps_wf[icomp], cut);
+  switch (T->pot_id) {
+    case TGPU_WALL1D_LJ93_CS:
+      if (x <= cut)
+        return prefac * (2.0 * OR_PI / 3.0) * (pow(sigma, 3)) *
+               ((2.0 / 15.0) * (pow(sigma / x, 9) - pow(sigma / cut, 9)) - (pow(sigma / x, 3) - pow(sigma / cut, 3)));
+      return 0.0;
+    case TGPU_WALL1D_LJ93_V2_CS:
+      if (x <= cut)
+        return prefac * ((2.0 / 15.0) * (pow(sigma / x, 9) - pow(sigma / cut, 9)) - (pow(sigma / x, 3) - pow(sigma / cut, 3)));
+      return 0.0;
+    case TGPU_WALL1D_LJ93_NOCS:
+      if (x <= cut)
+        return prefac * (2.0 * OR_PI / 3.0) * ((2.0 / 15.0) * pow(sigma, 12) / pow(x, 9) - pow(sigma, 6) / pow(x, 3));
+      return 0.0;
+    case TGPU_WALL1D_LJ93_SHIFTX_CS: {
+      double delta = 0.5 * (s->sigma_ff[icomp] - 1), xmax = cut + delta, xmin = xmax - 0.5;
+      if (x <= xmin) return s->vext_max;
+      if (x <= xmax)
+        return prefac * ((2.0 / 15.0) * (pow(sigma / (x - delta), 9) - pow(sigma / cut, 9)) -
+                         (pow(sigma / (x - delta), 3) - pow(sigma / cut, 3)));
+      return 0.0;
+    }
+    case TGPU_WALL1D_REPULSIVE9:
+      if (x <= cut) return prefac * (2.0 * OR_PI / 3.0) * pow(sigma, 3) * ((2.0 / 15.0) * pow(sigma / x, 9));
+      return 0.0;
+    default:
+      if (x <= cut) return -prefac * exp(-x / sigma);
+      return 0.0;
+  }
+}
+
 static double or_ulj(double r, double sigma, double eps, double rcut)
 {
   double u;
@@ -332,8 +448,8 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
 {
   or_mesh m;
   int nd = s->ndim, nw = s->nwalls, iwall, idim, i, icomp, ncorner;
-  int nimg, *real, (*touch)[3][2];
-  double (*wpos)[3];
+  int nimg, k_img, *real, (*touch)[3][2];
+  double (*wpos)[3], *xwall;
   unsigned short *wall_el;
   long iel, inode;
   signed char *zero0;
@@ -370,9 +486,17 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
     }
   }
 
-  /* wall elements and touched faces */
+  /* wall elements and touched faces; X_wall when a wall type is distance-based */
   wall_el = calloc((size_t)m.nels, sizeof(unsigned short));
   touch = calloc((size_t)nw + 1, sizeof(*touch));
+  xwall = NULL;
+  for (i = 0; i < s->ntypes; i++)
+    if (s->type[i].ipot_wf == TGPU_VEXT_DIST_TO_SURF || s->type[i].ipot_wf == TGPU_VEXT_DIST_TO_CENTER) {
+      long k;
+      xwall = malloc((size_t)m.nnodes * nw * sizeof(double));
+      for (k = 0; k < m.nnodes * nw; k++) xwall[k] = 1000.0;
+      break;
+    }
   for (iwall = 0; iwall < nw; iwall++) {
     const tgpu_wall_type *T = &s->type[s->wall_type[iwall]];
     for (iel = 0; iel < m.nels; iel++) {
@@ -385,6 +509,25 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
         xtest[idim] = (-0.5 * s->size[idim] + s->esize[idim] * ijk[idim]) + 0.5 * s->esize[idim];
       }
       adj = or_overlay(T, nd, xtest);
+      if (xwall) {   /* X_wall from the nodes of this element (src/dft_surfaces.c:400-430) */
+        int imax[3] = {1, 1, 1}, ix[3];
+        for (idim = 0; idim < nd; idim++)
+          if (ijk[idim] == m.nodes[idim] - 2 && s->bc[idim][1] != TGPU_BC_PERIODIC) imax[idim] = 2;
+        for (ix[2] = 0; ix[2] < imax[2]; ix[2]++)
+          for (ix[1] = 0; ix[1] < imax[1]; ix[1]++)
+            for (ix[0] = 0; ix[0] < imax[0]; ix[0]++) {
+              double xt[3] = {0.0, 0.0, 0.0}, delx;
+              long node = 0, stride = 1;
+              for (idim = 0; idim < nd; idim++) {
+                xt[idim] = (-0.5 * s->size[idim] + s->esize[idim] * ijk[idim]) + ix[idim] * s->esize[idim];
+                node += (ijk[idim] + ix[idim]) * stride;
+                stride *= m.nodes[idim];
+              }
+              delx = or_surface_dist(s, T, s->wall_pos[iwall], xt, adj, T->ipot_wf == TGPU_VEXT_DIST_TO_CENTER);
+              if (delx > 0.0) xwall[node * nw + iwall] = delx < xwall[node * nw + iwall] ? delx : xwall[node * nw + iwall];
+              else xwall[node * nw + iwall] = 0.0;
+            }
+      }
       if (or_in_surface(s, T, s->wall_pos[iwall], xtest, adj)) {
         wall_el[iel] |= (unsigned short)(1u << iwall);
         for (idim = 0; idim < nd; idim++) {
@@ -427,11 +570,28 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
     for (inode = 0; inode < m.nnodes; inode++)
       vext[icomp * m.nnodes + inode] = zero0[inode] ? s->vext_max : 0.0;
 
-  /* setup_integrated_LJ_walls for each wall of integrated type */
-  for (iwall = 0; iwall < nw; iwall++) {
-    const tgpu_wall_type *T = &s->type[s->wall_type[iwall]];
+  /* the walls and their images in image order (setup_external_field_n, src/dft_vext.c:108-140):
+   * setup_vext_XRSurf for every image of a distance-based type, setup_integrated_LJ_walls for every real
+   * wall of integrated type */
+  for (k_img = 0; k_img < nimg; k_img++) {
+    const tgpu_wall_type *T = &s->type[s->wall_type[real[k_img]]];
     double max_cut = 0.0;
-    if (T->ipot_wf != TGPU_VEXT_INTEGRATED) continue;
+    iwall = k_img;
+    if (T->ipot_wf == TGPU_VEXT_DIST_TO_SURF || T->ipot_wf == TGPU_VEXT_DIST_TO_CENTER) {
+      for (icomp = 0; icomp < s->ncomp; icomp++)
+        for (inode = 0; inode < m.nnodes; inode++) {
+          double *V = &vext[icomp * m.nnodes + inode], xORr;
+          if (zero0[inode]) continue;
+          xORr = k_img < nw ? xwall[inode * nw + k_img] : 1000.0;
+          if (fabs(*V - s->vext_max) > 1.e-6) {
+            if (xORr > 0.001) *V += or_vext_1d(s, T, icomp, xORr);
+            else *V = s->vext_max;
+          }
+          if (*V >= s->vext_max) *V = s->vext_max;
+        }
+      continue;
+    }
+    if (T->ipot_wf != TGPU_VEXT_INTEGRATED || k_img >= nw) continue;
     for (icomp = 0; icomp < s->ncomp; icomp++)
       if (max_cut < T->cut_wf[icomp]) max_cut = T->cut_wf[icomp];
     for (iel = 0; iel < m.nels; iel++) {
@@ -523,6 +683,7 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
   if (wall_el_out) memcpy(wall_el_out, wall_el, (size_t)m.nels * sizeof(unsigned short));
   free(wall_el);
   free(touch);
+  free(xwall);
   free(zero0);
   free(wpos);
   free(real);

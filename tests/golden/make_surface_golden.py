@@ -26,8 +26,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import tref  # noqa: E402
 from tramonto_gb300 import surfaces  # noqa: E402
 
-# deck -> fixture name: every GEOM example whose surfaces the GPU builder covers (no roughness, angle
-# cutouts or Lhard_surf; integrated LJ 12-6 walls), small enough for the reference to set up in a minute
+# deck -> fixture name: the example decks whose surfaces the GPU builder covers (no roughness, angle cutouts
+# or Lhard_surf), small enough for the reference to set up in about two minutes: every such GEOM deck with
+# integrated LJ 12-6 walls, and decks of the distance-based 9-3 walls in 1-D, 2-D and 3-D
 DECKS = {
     "GEOM25_CYL_PORE_2D": "surf_cylpore2d",
     "GEOM31_TAPERED_CYLPORE_3D": "surf_taperedpore3d",
@@ -42,6 +43,14 @@ DECKS = {
     "GEOM35_PLANE_PERIODIC_3D": "surf_plane3d_periodic",
     "GEOM37_WEDGE_LINEAR_2D": "surf_wedge2d",
     "GEOM38_WEDGE_3D": "surf_wedge3d",
+    # distance-based walls (Ipot_wf_n 2: the 9-3 cut-and-shifted form of the distance to the surface)
+    "GEOM32_PLANE_PERIODIC_2D": "surf_lj93_plane2d_cosx",
+    "GEOM33_PLANE_PERIODIC2_2D": "surf_lj93_plane2d_cosy",
+    "LJ1_FMT1_WCA_1D": "surf_lj93_1d",
+    "MIX2_FMT1_WCA_1D": "surf_lj93_mix1d",
+    "CONT1_FMT1_WCA_1D": "surf_lj93_cont1d",
+    "BC1_FMT1_WCA_ELEC_2D": "surf_lj93_2d_three",
+    "BC7_FMT1_WCA_ELEC_3D": "surf_lj93_3d_three",
 }
 
 

@@ -71,7 +71,7 @@ def test_noalloc_rejects_stencils_that_reach_past_the_box(lib, bc, reach, n):
 def test_surface_spec_errors_before_device_work(lib):
     """The surface builder checks its spec on the host: a mesh without a positive element size is
     TGPU_ERR_ARG, options it does not build (a 1-D sphere, a 2-D slit pore of orientation 0,
-    Ipot_wf_n 2) TGPU_ERR_UNSUPPORTED; tgpu_surface_mesh gives the reference's node and element counts."""
+    Ipot_wf_n 4) TGPU_ERR_UNSUPPORTED; tgpu_surface_mesh gives the reference's node and element counts."""
     import numpy as np
     from tramonto_gb300 import surfaces
     lj = dict(sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0])
@@ -89,7 +89,7 @@ def test_surface_spec_errors_before_device_work(lib):
                             [dict(surf_type=surfaces.SURF_FINITE_PORE, orientation=0, param=(1.0, 2.0, 0),
                                   ipot_wf=5, **lj)]), -4),
         (surfaces.make_spec(2, (9.4, 10.0), (0.2, 0.2), [(1, 1), (-1, 3)], 1, [(0, (0.0, 0.0))],
-                            [dict(surf_type=surfaces.SURF_PLANAR, param=(1.0, 0, 0), ipot_wf=2, **lj)]), -4),
+                            [dict(surf_type=surfaces.SURF_PLANAR, param=(1.0, 0, 0), ipot_wf=4, **lj)]), -4),
     ]
     v = np.zeros(4096)
     z = np.zeros(4096, np.int8)

@@ -1,8 +1,9 @@
 """Surfaces and their external fields built on the GPU (tgpu_surface_field_*) against the reference's own
-set-up of its GEOM example decks (tests/golden/surf_*.npz: cylindrical pores in 2-D and 3-D, a tapered
-3-D pore with linear overlays, blocks, cylinders, spheres, periodic-overlay and wedge planes; reflecting,
-last-node, in-wall and in-bulk boundaries) and against the oracle's restatement on specs with periodic
-images and several walls.
+set-up of its example decks (tests/golden/surf_*.npz: integrated LJ walls of cylindrical pores in 2-D and
+3-D, a tapered 3-D pore with linear overlays, blocks, cylinders, spheres, periodic-overlay and wedge planes;
+distance-based 9-3 walls in 1-D, 2-D and 3-D; reflecting, last-node, in-wall and in-bulk boundaries) and
+against the oracle's restatement on specs with periodic images, several walls, every 1-D wall form and the
+distances to surfaces and to centres.
 
 Bars: wall elements and zero-density flags identical; V_ext/kT within 1e-10 of the reference's (the
 kernel forms powers as products and sums the Gauss points of an element over the lanes of a warp, in
@@ -57,7 +58,30 @@ def _periodic_specs():
                              [dict(surf_type=surfaces.SURF_FINITE_PORE, orientation=2, param=(1.0, 1.5, 0.0),
                                    ipot_wf=5, sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0],
                                    linear=[(2, 0.2, 0.0, 1.5)])], apply_offset=(1, 0, 0))
-    return {"periodic2d": s2, "periodic3d": s3, "reflect_periodic_pore3d": s3p}
+    # distance-based walls: every 1-D form and the pair potential, distances to surfaces and to centres
+    lj1 = dict(sigma_wf=[1.0, 0.8], eps_wf=[1.2, 0.6], cut_wf=[2.5, 2.2], rho_w=0.9)
+    sd2 = surfaces.make_spec(2, (8.0, 6.0), (0.2, 0.25), [(-1, -1), (1, 1)], 2,
+                             [(0, (-3.0, 0.0)), (1, (3.0, 0.0)), (2, (0.5, 1.0)), (3, (-0.5, -1.5))],
+                             [dict(surf_type=surfaces.SURF_PLANAR, orientation=0, param=(1.0, 0, 0), ipot_wf=2,
+                                   pot_id=surfaces.WALL1D_LJ93_CS, periodic=[(1, 0.3, 3.0, 0.0)], **lj1),
+                              dict(surf_type=surfaces.SURF_PLANAR, orientation=0, param=(1.0, 0, 0), ipot_wf=2,
+                                   pot_id=surfaces.WALL1D_LJ93_SHIFTX_CS, **lj1),
+                              dict(surf_type=surfaces.SURF_COLLOID, param=(0.8, 0, 0), ipot_wf=3, type_vext=1, **lj1),
+                              dict(surf_type=surfaces.SURF_BLOCK, param=(0.6, 0.4, 0), ipot_wf=2,
+                                   pot_id=surfaces.WALL1D_EXP_ATT, **lj1)], sigma_ff=[1.0, 1.3])
+    sd3 = surfaces.make_spec(3, (5.0, 4.0, 4.0), (0.25, 0.25, 0.25), [(0, 0), (1, 1), (2, 2)], 1,
+                             [(0, (0.0, 0.0, 0.0)), (1, (1.5, 1.0, 1.0)), (2, (-1.5, 0.0, 0.0))],
+                             [dict(surf_type=surfaces.SURF_FINITE_PORE, orientation=0, param=(1.5, 1.0, 0), ipot_wf=2,
+                                   pot_id=surfaces.WALL1D_LJ93_V2_CS, sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0]),
+                              dict(surf_type=surfaces.SURF_FINITE_CYL, orientation=2, param=(0.5, 0.75, 0), ipot_wf=3,
+                                   pot_id=surfaces.WALL1D_REPULSIVE9, sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0]),
+                              dict(surf_type=surfaces.SURF_PORE, param=(2.4, 0, 0), ipot_wf=2,
+                                   pot_id=surfaces.WALL1D_LJ93_NOCS, sigma_wf=[1.0], eps_wf=[0.5], cut_wf=[2.5])])
+    # an integrated planar wall in 1-D (the 2 pi rho dz out-of-line integral) with a face copy region
+    si1 = surfaces.make_spec(1, (8.0,), (0.1,), [(-1, 0)], 2, [(0, (-3.5,))],
+                             [dict(surf_type=surfaces.SURF_PLANAR, orientation=0, param=(0.5, 0, 0), ipot_wf=5, **lj)])
+    return {"periodic2d": s2, "periodic3d": s3, "reflect_periodic_pore3d": s3p, "distance_walls2d": sd2,
+            "distance_walls3d": sd3, "integrated1d": si1}
 
 
 @pytest.mark.parametrize("case", list(_periodic_specs()))

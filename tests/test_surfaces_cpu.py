@@ -1,6 +1,7 @@
 """Surfaces and their external fields on the CPU: the oracle's restatement (oracle/surfaces.c) against
-the reference's own set-up of its GEOM example decks (tests/golden/surf_*.npz, made by
-tests/golden/make_surface_golden.py), and the deck reader of tramonto_gb300.surfaces.
+the reference's own set-up of its example decks (tests/golden/surf_*.npz, made by
+tests/golden/make_surface_golden.py: integrated LJ walls of the GEOM decks, distance-based 9-3 walls in
+1-D, 2-D and 3-D), and the deck reader of tramonto_gb300.surfaces.
 
 Bars: wall elements and zero-density flags identical; V_ext/kT within 1e-10 of the reference's
 (powers by pow() as the reference, Gauss nodes computed rather than tabulated: differences of a few
@@ -19,7 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
 FIXTURES = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(HERE, "golden", "surf_*.npz")))
 # the fixtures the oracle restates in a few seconds (its loops are the reference's, one thread)
-ORACLE_FIXTURES = ["surf_cylpore2d", "surf_block2d", "surf_cyl2d", "surf_plane2d_periodic", "surf_sphere3d"]
+ORACLE_FIXTURES = ["surf_cylpore2d", "surf_block2d", "surf_cyl2d", "surf_plane2d_periodic", "surf_sphere3d",
+                   "surf_lj93_plane2d_cosx", "surf_lj93_plane2d_cosy", "surf_lj93_1d", "surf_lj93_mix1d",
+                   "surf_lj93_cont1d", "surf_lj93_2d_three", "surf_lj93_3d_three"]
 V_TOL = 1e-10
 
 

@@ -49,6 +49,8 @@ enum { kModeId = 0, kModeAdd = 1, kModeSub = 2 };
 struct Image {
   int mode[3];
   double pic[3], prc[3];
+  int ishift[3];   // lattice form: element e maps to e + ishift (periodic shift) or ishift - 1 - e (mirror)
+  int lattice;     // 1 when every mapped corner is a lattice point (the offset table applies)
 };
 
 struct Mesh {
@@ -162,6 +164,68 @@ __device__ bool in_surface(const tgpu_wall_type &T, int ndim, const int *apply, 
   }
   if (st == TGPU_SURF_FINITE_CYL) return r12 <= radius && x12 <= halflength;
   return r12 >= radius && x12 <= halflength;
+}
+
+// delx_vext of the surface tests: the distance from x to the surface (or, to_center, to its centre or
+// axis) that the walls of Ipot_wf_n 2 and 3 use
+__device__ double surface_dist(const tgpu_wall_type &T, int ndim, const int *apply, const double *w, const double *x,
+                               double adj, bool to_center)
+{
+  const int st = T.surf_type;
+  if (st == TGPU_SURF_PLANAR) {
+    double hw = T.param[0];
+    hw += adj - kRoff;
+    const double x12 = fabs(w[T.orientation] - x[T.orientation]);
+    return to_center ? x12 : x12 - hw;
+  }
+  if (st == TGPU_SURF_BLOCK) {
+    bool in = true;
+    double rs = 0.0, rc = 0.0;
+    for (int d = 0; d < ndim; d++) {
+      const double hw = T.param[d] + adj - kRoff;
+      const double x12 = fabs(w[d] - x[d]);
+      if (x12 > hw) in = false;
+      const double xt = x12 - hw;
+      if (xt > 0) {
+        rs += xt * xt;
+        rc += x12 * x12;
+      }
+    }
+    if (in) return 0.0;
+    return to_center ? sqrt(rc) : sqrt(rs);
+  }
+  if (st == TGPU_SURF_COLLOID || st == TGPU_SURF_PORE) {
+    const double radius = T.param[0] + adj - kRoff;
+    double q = 0.0;
+    for (int d = 0; d < ndim; d++) {
+      const double x12 = w[d] - x[d];
+      q += x12 * x12;
+    }
+    const double r12 = sqrt(q);
+    if (st == TGPU_SURF_PORE) return radius - r12;
+    return to_center ? r12 : r12 - radius;
+  }
+  const double radius = apply[0] ? T.param[0] + adj - kRoff : T.param[0] - kRoff;
+  const double halflength = apply[1] ? T.param[1] + adj - kRoff : T.param[1] - kRoff;
+  double r12, x12;
+  if (ndim == 3) {
+    cyl_dists(T.orientation, x, w, r12, x12);
+  } else {
+    const double dx = x[0] - w[0];
+    r12 = sqrt(0.0 + dx * dx);
+    x12 = fabs(w[1] - x[1]);
+  }
+  double dsq = 0.0, csq = 0.0;
+  if (st == TGPU_SURF_FINITE_CYL) {
+    if (r12 > radius) dsq += (r12 - radius) * (r12 - radius);
+    if (x12 > halflength) dsq += (x12 - halflength) * (x12 - halflength);
+    if (r12 > radius) csq += r12 * r12;
+    if (x12 > halflength) csq += x12 * x12;
+    return to_center ? sqrt(csq) : sqrt(dsq);
+  }
+  if (x12 > halflength) dsq += (x12 - halflength) * (x12 - halflength);
+  if (r12 < radius) dsq += (radius - r12) * (radius - r12);
+  return sqrt(dsq);
 }
 
 // position of node index i along d (node_to_position, src/dft_mesh_lib.c:579-620)
@@ -308,10 +372,10 @@ __device__ double wall_weight(int ndim, double r, const PotParams &P, int ngpu, 
   return 2.0 * temp * P.cut * zmax;
 }
 
-// integrate_potential (src/dft_vext_integrated.c:42-155): the element with lower corner w seen from
-// the node at f, Gauss points spread over the lanes; every lane returns the element's sum
-__device__ double integrate_element(const Mesh &m, const double *w, const double *f, const PotParams &P, int near,
-                                    int lane)
+// integrate_potential (src/dft_vext_integrated.c:42-155): the element with lower corner w seen from the
+// node at f, the Gauss points t0, t0 + step, ... of the rule the distance class `near` selects
+__device__ double integrate_points(const Mesh &m, const double *w, const double *f, const PotParams &P, int near,
+                                   int t0, int step)
 {
   const Rules &G = d_rules;
   const int ngp = near == 0 ? 6 : 3;
@@ -323,7 +387,7 @@ __device__ double integrate_element(const Mesh &m, const double *w, const double
   if (m.ndim > 1) total *= ngp;
   if (m.ndim > 2) total *= ngp;
   double part = 0.0;
-  for (int t = lane; t < total; t += 32) {
+  for (int t = t0; t < total; t += step) {
     if (m.ndim == 3) {
       const int ig = t / (ngp * ngp), jg = (t / ngp) % ngp, kg = t % ngp;
       const double p0 = w[0] + gp[ig] * m.esize[0];
@@ -349,8 +413,77 @@ __device__ double integrate_element(const Mesh &m, const double *w, const double
       part += weight * gw[t] * m.vol_el;
     }
   }
+  return part;
+}
+
+// the same over the lanes of a warp; a butterfly sum leaves the element's value in every lane
+__device__ double integrate_element_warp(const Mesh &m, const double *w, const double *f, const PotParams &P, int near,
+                                         int lane)
+{
+  double part = integrate_points(m, w, f, P, near, lane, 32);
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   return part;
+}
+
+// ---- the offset table of an integrated wall type ---------------------------------------------------
+// The element integral depends on the node and the element's lower corner only through their lattice
+// offset delta (the corner of every image and face copy of an element is a lattice point when the
+// images are periodic shifts or mirrors about the box faces).  One table per wall type holds, for
+// every delta within (max_cut / Esize + 2) elements, a code and the integral per component:
+//   code 0   beyond the reach test; 1..3 the Gauss rule of the distance class (r^2 < 4, < 16, else);
+//   code 4   r^2 within 1e-9 (relative) of 4, 16 or max_cut^2: the reference's decision there depends
+//            on the rounding of its absolute positions, so the table holds the integral under all three
+//            rules and an item picks one (or none) by r^2 computed from the positions the reference
+//            computes.
+// Tabulated integrals are formed with the node at the origin; they differ from the reference's,
+// formed at absolute positions, by rounding.  K is [rule][ncomp][n]: rule 0..2 (only the code's rule is
+// filled for codes 1..3).
+constexpr unsigned char kCodeSkip = 0, kCodeAmbiguous = 4;
+constexpr double kAmbiguousTol = 1e-9;
+
+struct OffTable {
+  int R[3], W[3];
+  long n;
+  const unsigned char *code;
+  const double *K;           // [3][ncomp][n]
+  int ncomp;
+};
+
+__global__ void k_vext_table(Mesh m, PotParams P0, PotParams P1, PotParams P2, PotParams P3, int ncomp, double thr,
+                             OffTable t, unsigned char *code, double *K)
+{
+  const int lane = threadIdx.x & 31;
+  const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+  const PotParams P[4] = {P0, P1, P2, P3};
+  for (long i = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5; i < t.n; i += nwarps) {
+    long r = i;
+    double w[3] = {0.0, 0.0, 0.0};
+    const double f[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < 3; d++) {
+      const int delta = (int)(r % t.W[d]) - t.R[d];
+      r /= t.W[d];
+      if (d < m.ndim) w[d] = delta * m.esize[d];
+    }
+    double r2 = 0.0;
+    for (int d = 0; d < m.ndim; d++) r2 += (w[d] - f[d]) * (w[d] - f[d]);
+    unsigned char c0;
+    if (fabs(r2 - thr) <= kAmbiguousTol * thr || fabs(r2 - 4.0) <= kAmbiguousTol * 4.0 ||
+        fabs(r2 - 16.0) <= kAmbiguousTol * 16.0) {
+      c0 = kCodeAmbiguous;
+    } else if (!(r2 < thr)) {
+      c0 = kCodeSkip;
+    } else {
+      c0 = (unsigned char)(1 + (r2 < 4.0 ? 0 : (r2 < 16.0 ? 1 : 2)));
+    }
+    for (int rule = 0; rule < 3; rule++) {
+      const bool want = c0 == kCodeAmbiguous || c0 == rule + 1;
+      for (int c = 0; c < ncomp; c++) {
+        const double v = want ? integrate_element_warp(m, w, f, P[c], rule, lane) : 0.0;
+        if (lane == 0) K[((long)rule * ncomp + c) * t.n + i] = v;
+      }
+    }
+    if (lane == 0) code[i] = c0;
+  }
 }
 
 constexpr int kMaxIv = 28;
@@ -407,58 +540,162 @@ struct NodeState {
   }
 };
 
-// every image and copy of one wall element, in the reference's order (src/dft_vext.c:727-858)
-__device__ void add_element(const Mesh &m, const int *ije, const Image *img, int nimg, double max_cut, double thr,
-                            const PotParams *P, const double *f, NodeState &S, int lane)
+// The items of one wall element for one node — every image and face copy, in the reference's order
+// (src/dft_vext.c:727-858) — summed in order per component, with the largest running sum: the node's
+// clipped sum reaches vext_max inside this element exactly when its value before it plus that peak does.
+__device__ void element_items(const Mesh &m, const int *ije, const Image *img, int nimg, double max_cut, double thr,
+                              const PotParams *P, const NodeState &S, const int *ijk_f, const double *f,
+                              const OffTable &t, double *sum, double *peak)
 {
-  double center[3] = {0.0, 0.0, 0.0};
-  for (int d = 0; d < m.ndim; d++) center[d] = node_pos(m, d, ije[d]) + 0.5 * m.esize[d];
-  int nghost = 0, gd = 0;
-  double del = 0.0;
+  for (int c = 0; c < S.ncomp; c++) {
+    sum[c] = 0.0;
+    peak[c] = -1.0e300;
+  }
+  // face copies: the reference tests |centre -/+ Esize/2 +/- Size/2| < 1e-6, i.e. the first or last element
+  // along a dimension (Esize is far above 1e-6); the last dimension that holds decides
+  int nghost = 0, gd = 0, gstep = 0;
   for (int d = 0; d < m.ndim; d++) {
-    if (bc_face_wall(m.bc[d][0]) && fabs(center[d] - 0.5 * m.esize[d] + m.size[d] / 2.) < 1.e-6) {
+    if (bc_face_wall(m.bc[d][0]) && ije[d] == 0) {
       nghost = (int)(max_cut / m.esize[d]);
-      del = -m.esize[d];
       gd = d;
-    } else if (bc_face_wall(m.bc[d][1]) && fabs(center[d] + 0.5 * m.esize[d] - m.size[d] / 2) < 1.e-6) {
+      gstep = -1;
+    } else if (bc_face_wall(m.bc[d][1]) && ije[d] == m.els[d] - 1) {
       nghost = (int)(max_cut / m.esize[d]);
-      del = m.esize[d];
       gd = d;
+      gstep = 1;
     }
   }
   for (int k = 0; k < nimg; k++) {
     const Image &I = img[k];
-    double w[3] = {0.0, 0.0, 0.0}, save[3];
-    for (int d = 0; d < m.ndim; d++) {
-      if (I.mode[d] == kModeId) {
-        w[d] = center[d];
-      } else {
-        const double delta = center[d] - I.prc[d];
-        w[d] = I.mode[d] == kModeAdd ? I.pic[d] + delta : I.pic[d] - delta;
-      }
-    }
-    for (int d = 0; d < m.ndim; d++) {
-      w[d] -= 0.5 * m.esize[d];
-      save[d] = w[d];
-    }
+    int ci[3] = {0, 0, 0};
+    for (int d = 0; d < m.ndim; d++)
+      ci[d] = I.mode[d] == kModeId ? ije[d] : (I.mode[d] == kModeAdd ? ije[d] + I.ishift[d] : I.ishift[d] - 1 - ije[d]);
     for (int g = 0; g <= nghost; g++) {
-      if (g > 0) w[gd] = save[gd] + g * del;
-      double r2 = 0.0;
-      for (int d = 0; d < m.ndim; d++) r2 += (w[d] - f[d]) * (w[d] - f[d]);
-      if (!(r2 < thr)) continue;
-      const int near = r2 < 4.0 ? 0 : (r2 < 16.0 ? 1 : 2);
+      unsigned char code = kCodeAmbiguous;
+      long idx = 0;
+      if (I.lattice) {
+        bool inside = true;
+        for (int d = 2; d >= 0; d--) {
+          const int delta = d < m.ndim ? ci[d] + (d == gd ? g * gstep : 0) - ijk_f[d] : 0;
+          if (delta < -t.R[d] || delta > t.R[d]) inside = false;
+          idx = idx * t.W[d] + (delta + t.R[d]);
+        }
+        if (!inside) continue;
+        code = t.code[idx];
+      }
+      if (code == kCodeSkip) continue;
+      int rule = code - 1;
+      double w[3] = {0.0, 0.0, 0.0};
+      if (code == kCodeAmbiguous) {
+        // the item's lower corner as the reference computes it (src/dft_vext.c:741-790)
+        for (int d = 0; d < m.ndim; d++) {
+          const double center = node_pos(m, d, ije[d]) + 0.5 * m.esize[d];
+          if (I.mode[d] == kModeId) {
+            w[d] = center;
+          } else {
+            const double delta = center - I.prc[d];
+            w[d] = I.mode[d] == kModeAdd ? I.pic[d] + delta : I.pic[d] - delta;
+          }
+          w[d] -= 0.5 * m.esize[d];
+          if (g > 0 && d == gd) w[d] = w[d] + g * (gstep * m.esize[d]);
+        }
+        double r2 = 0.0;
+        for (int d = 0; d < m.ndim; d++) r2 += (w[d] - f[d]) * (w[d] - f[d]);
+        if (!(r2 < thr)) continue;
+        rule = r2 < 4.0 ? 0 : (r2 < 16.0 ? 1 : 2);
+      }
       for (int c = 0; c < S.ncomp; c++) {
-        if (!S.live[c] || !(S.V[c] < S.vmax || S.V[c] == 0.0)) continue;
-        S.V[c] += integrate_element(m, w, f, P[c], near, lane);
-        if (S.V[c] >= S.vmax) S.V[c] = S.vmax;
+        if (!S.live[c]) continue;
+        // an image off the lattice (a wall mirrored about a face it lies beyond) is integrated here
+        const double v = I.lattice ? t.K[((long)rule * t.ncomp + c) * t.n + idx] : integrate_points(m, w, f, P[c], rule, 0, 1);
+        sum[c] += v;
+        peak[c] = fmax(peak[c], sum[c]);
       }
     }
   }
 }
 
+// the 1-D wall forms (src/dft_vext_1D.c:40-230) and the LJ 12-6 pair potential at distance x
+__device__ double wall_1d(const tgpu_wall_type &T, int c, double sigma_ff, double vmax, double x)
+{
+  const double sigma = T.sigma_wf[c], cut = T.cut_wf[c];
+  if (T.type_vext == 1) {
+    const double q = sigma / cut, q2 = q * q, q6 = q2 * q2 * q2;
+    return lj_cs(x, sigma, T.eps_wf[c], cut, q6, q6 * q6);
+  }
+  const double prefac = T.eps_wf[c] * T.rho_w;
+  const double s3 = sigma * sigma * sigma;
+  auto p3 = [](double a) { return a * a * a; };
+  switch (T.pot_id) {
+    case TGPU_WALL1D_LJ93_CS:
+      if (x > cut) return 0.0;
+      return prefac * (2.0 * kPi / 3.0) * s3 *
+             ((2.0 / 15.0) * (p3(p3(sigma / x)) - p3(p3(sigma / cut))) - (p3(sigma / x) - p3(sigma / cut)));
+    case TGPU_WALL1D_LJ93_V2_CS:
+      if (x > cut) return 0.0;
+      return prefac * ((2.0 / 15.0) * (p3(p3(sigma / x)) - p3(p3(sigma / cut))) - (p3(sigma / x) - p3(sigma / cut)));
+    case TGPU_WALL1D_LJ93_NOCS:
+      if (x > cut) return 0.0;
+      return prefac * (2.0 * kPi / 3.0) * ((2.0 / 15.0) * (p3(s3) * s3) / p3(p3(x)) - (s3 * s3) / p3(x));
+    case TGPU_WALL1D_LJ93_SHIFTX_CS: {
+      const double delta = 0.5 * (sigma_ff - 1);
+      const double xmax = cut + delta, xmin = xmax - 0.5;
+      if (x <= xmin) return vmax;
+      if (x > xmax) return 0.0;
+      const double q = sigma / (x - delta);
+      return prefac * ((2.0 / 15.0) * (p3(p3(q)) - p3(p3(sigma / cut))) - (p3(q) - p3(sigma / cut)));
+    }
+    case TGPU_WALL1D_REPULSIVE9:
+      if (x > cut) return 0.0;
+      return prefac * (2.0 * kPi / 3.0) * s3 * ((2.0 / 15.0) * p3(p3(sigma / x)));
+    default:   // TGPU_WALL1D_EXP_ATT
+      if (x > cut) return 0.0;
+      return -prefac * exp(-x / sigma);
+  }
+}
+
+// setup_vext_XRSurf (src/dft_vext.c:364-436) for one real wall at one node: X_wall from the surface test at
+// the node with the overlay adjustment of the element the reference tests the node from (its own lower
+// corner element, the last element along a dimension for the far nodes; src/dft_surfaces.c:400-430)
+__device__ void add_xr_wall(const tgpu_surface_spec &s, const Mesh &m, int iw, const int *ijk, NodeState &S)
+{
+  const tgpu_wall_type &T = s.type[s.wall_type[iw]];
+  double xc[3] = {0.0, 0.0, 0.0}, xt[3] = {0.0, 0.0, 0.0};
+  for (int d = 0; d < m.ndim; d++) {
+    const int e = min(ijk[d], m.els[d] - 1);
+    const double p = node_pos(m, d, e);
+    xc[d] = p + 0.5 * m.esize[d];
+    xt[d] = p + (ijk[d] - e) * m.esize[d];
+  }
+  const double adj = overlay_adjust(T, m.ndim, xc);
+  const double delx = surface_dist(T, m.ndim, s.apply_offset, s.wall_pos[iw], xt, adj,
+                                   T.ipot_wf == TGPU_VEXT_DIST_TO_CENTER);
+  const double xw = delx > 0.0 ? fmin(delx, 1000.0) : 0.0;
+  for (int c = 0; c < S.ncomp; c++) {
+    if (!S.live[c]) continue;
+    if (fabs(S.V[c] - S.vmax) > 1.e-6) {
+      if (xw > 0.001) S.V[c] += wall_1d(T, c, s.sigma_ff[c], S.vmax, xw);
+      else S.V[c] = S.vmax;
+    }
+    if (S.V[c] >= S.vmax) S.V[c] = S.vmax;
+  }
+}
+
+struct Tables {
+  OffTable t[TGPU_SURF_MAXTYPES];
+};
+
+// the wall-fluid parameters of component c of a wall type, with (sigma/cut)^6 and ^12 as products
+__host__ __device__ inline PotParams pot_params(const tgpu_wall_type &T, int c)
+{
+  const double q = T.sigma_wf[c] / T.cut_wf[c], q2 = q * q, q6 = q2 * q2 * q2;
+  return PotParams{T.sigma_wf[c], T.eps_wf[c], T.cut_wf[c], q6, q6 * q6};
+}
+
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_vext_integrated(tgpu_surface_spec s, Mesh m, const Image *img, const int *img_first, const int *img_count,
-                  const unsigned short *wall_el, const unsigned char *zero0, double *vext, signed char *zero)
+                  Tables tabs, const unsigned short *wall_el, const unsigned char *zero0, double *vext,
+                  signed char *zero)
 {
   const int lane = threadIdx.x & 31;
   const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
@@ -481,15 +718,19 @@ k_vext_integrated(tgpu_surface_spec s, Mesh m, const Image *img, const int *img_
     }
     for (int iw = 0; iw < s.nwalls && !z0; iw++) {
       const tgpu_wall_type &T = s.type[s.wall_type[iw]];
+      if (T.ipot_wf == TGPU_VEXT_DIST_TO_SURF || T.ipot_wf == TGPU_VEXT_DIST_TO_CENTER) {
+        add_xr_wall(s, m, iw, ijk, S);
+        continue;
+      }
       if (T.ipot_wf != TGPU_VEXT_INTEGRATED) continue;
-      if (S.frozen()) break;
+      if (S.frozen()) continue;
       double max_cut = 0.0;
       PotParams P[TGPU_MAXC];
       for (int c = 0; c < s.ncomp; c++) {
         if (max_cut < T.cut_wf[c]) max_cut = T.cut_wf[c];
-        const double q = T.sigma_wf[c] / T.cut_wf[c], q2 = q * q, q6 = q2 * q2 * q2;
-        P[c] = {T.sigma_wf[c], T.eps_wf[c], T.cut_wf[c], q6, q6 * q6};
+        P[c] = pot_params(T, c);
       }
+      const OffTable &tab = tabs.t[s.wall_type[iw]];
       const double thr = (max_cut + 0.0) * max_cut + 0.0;
       const Image *wimg = img + img_first[iw];
       const int nimg = img_count[iw];
@@ -509,16 +750,25 @@ k_vext_integrated(tgpu_surface_spec s, Mesh m, const Image *img, const int *img_
                   const long row = ((long)z * m.els[1] + y) * m.els[0];
                   const bool cand = x <= hi[0][ix] && ((wall_el[row + x] >> iw) & 1);
                   unsigned mask = __ballot_sync(0xffffffffu, cand);
+                  if (!mask) continue;
+                  double sum[TGPU_MAXC], peak[TGPU_MAXC];
+                  if (cand) {
+                    const int ije[3] = {x, y, z};
+                    element_items(m, ije, wimg, nimg, max_cut, thr, P, S, ijk, f, tab, sum, peak);
+                  }
+                  // the elements of this chunk in ascending order
                   while (mask) {
                     const int b = __ffs(mask) - 1;
                     mask &= mask - 1;
-                    const int ije[3] = {x0 + b, y, z};
-                    add_element(m, ije, wimg, nimg, max_cut, thr, P, f, S, lane);
-                    if (S.frozen()) {
-                      stop = true;
-                      break;
+                    for (int c = 0; c < s.ncomp; c++) {
+                      const double sb = __shfl_sync(0xffffffffu, cand ? sum[c] : 0.0, b);
+                      const double pb = __shfl_sync(0xffffffffu, cand ? peak[c] : 0.0, b);
+                      if (!S.live[c] || !(S.V[c] < S.vmax || S.V[c] == 0.0)) continue;
+                      if (S.V[c] + pb >= S.vmax) S.V[c] = S.vmax;
+                      else S.V[c] += sb;
                     }
                   }
+                  if (S.frozen()) stop = true;
                 }
     }
     if (lane == 0) {
@@ -602,9 +852,14 @@ int check_spec(const tgpu_surface_spec *s)
       default:
         return TGPU_ERR_UNSUPPORTED;
     }
-    if (T.ipot_wf != TGPU_VEXT_NONE && T.ipot_wf != TGPU_VEXT_HARD && T.ipot_wf != TGPU_VEXT_INTEGRATED)
+    if (T.ipot_wf != TGPU_VEXT_NONE && T.ipot_wf != TGPU_VEXT_HARD && T.ipot_wf != TGPU_VEXT_INTEGRATED &&
+        T.ipot_wf != TGPU_VEXT_DIST_TO_SURF && T.ipot_wf != TGPU_VEXT_DIST_TO_CENTER)
       return TGPU_ERR_UNSUPPORTED;
-    if (T.ipot_wf == TGPU_VEXT_INTEGRATED)
+    if (T.ipot_wf == TGPU_VEXT_INTEGRATED && (T.type_vext != 1 || T.pot_id != 0)) return TGPU_ERR_UNSUPPORTED;
+    if ((T.ipot_wf == TGPU_VEXT_DIST_TO_SURF || T.ipot_wf == TGPU_VEXT_DIST_TO_CENTER) &&
+        !(T.type_vext == 1 ? T.pot_id == 0 : (T.pot_id >= TGPU_WALL1D_LJ93_CS && T.pot_id <= TGPU_WALL1D_EXP_ATT)))
+      return TGPU_ERR_UNSUPPORTED;
+    if (T.ipot_wf >= TGPU_VEXT_DIST_TO_SURF)
       for (int c = 0; c < s->ncomp; c++)
         if (!(T.cut_wf[c] > 0.0) || !(T.sigma_wf[c] > 0.0)) return TGPU_ERR_ARG;
   }
@@ -679,6 +934,17 @@ bool make_images(const tgpu_surface_spec *s, std::vector<Image> &out, std::vecto
           return false;
         }
       }
+      // the lattice form of the map: centre + (pic - prc) is element e + (pic - prc)/Esize; the mirror
+      // (pic + prc) - centre has its lower corner at element (pic + prc + Size)/Esize - 1 - e
+      I.lattice = 1;
+      for (int d = 0; d < nd; d++) {
+        if (I.mode[d] == kModeId) continue;
+        const double q = I.mode[d] == kModeAdd ? (I.pic[d] - I.prc[d]) / s->esize[d]
+                                               : (I.pic[d] + I.prc[d] + s->size[d]) / s->esize[d];
+        const double qr = std::nearbyint(q);
+        if (std::fabs(q - qr) > 1e-9 * std::max(1.0, std::fabs(q)) || std::fabs(qr) > 1e8) I.lattice = 0;
+        I.ishift[d] = I.lattice ? (int)qr : 0;
+      }
       out.push_back(I);
       count[w]++;
     }
@@ -743,6 +1009,39 @@ int surface_field(const tgpu_surface_spec *s, double *d_vext, signed char *d_zer
     ok = ok && cudaMemcpy(dcount, count.data(), s->nwalls * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
   }
   ok = ok && cudaMemcpyToSymbol(d_rules, &R, sizeof(Rules)) == cudaSuccess;
+  // the offset tables of the integrated wall types that some wall uses
+  Tables tabs{};
+  for (int t = 0; t < s->ntypes && ok; t++) {
+    const tgpu_wall_type &T = s->type[t];
+    bool used = false;
+    for (int w = 0; w < s->nwalls; w++) used |= s->wall_type[w] == t;
+    if (!used || T.ipot_wf != TGPU_VEXT_INTEGRATED) continue;
+    double max_cut = 0.0;
+    PotParams P[4] = {};
+    for (int c = 0; c < s->ncomp; c++) {
+      if (max_cut < T.cut_wf[c]) max_cut = T.cut_wf[c];
+      P[c] = pot_params(T, c);
+    }
+    OffTable &tb = tabs.t[t];
+    tb.n = 1;
+    for (int d = 0; d < 3; d++) {
+      tb.R[d] = d < m.ndim ? (int)(max_cut / m.esize[d]) + 2 : 0;
+      tb.W[d] = 2 * tb.R[d] + 1;
+      tb.n *= tb.W[d];
+    }
+    unsigned char *code = dev_alloc<unsigned char>(owned, tb.n);
+    double *K = dev_alloc<double>(owned, (size_t)tb.n * s->ncomp * 3);
+    tb.ncomp = s->ncomp;
+    if (!code || !K) {
+      release();
+      return fail(TGPU_ERR_CUDA, "surface field: device allocation failed");
+    }
+    tb.code = code;
+    tb.K = K;
+    const double thr = (max_cut + 0.0) * max_cut + 0.0;
+    const long bt = std::min<long>((tb.n + kWarpsPerBlock - 1) / kWarpsPerBlock, 152L * 64);
+    k_vext_table<<<(int)bt, 32 * kWarpsPerBlock>>>(m, P[0], P[1], P[2], P[3], s->ncomp, thr, tb, code, K);
+  }
   if (ok) {
     const int tb = 256;
     const long be = std::min<long>((m.nels + tb - 1) / tb, 152L * 16);
@@ -750,7 +1049,8 @@ int surface_field(const tgpu_surface_spec *s, double *d_vext, signed char *d_zer
     k_surf_elements<<<(int)be, tb>>>(*s, m, wall_el, touch);
     k_surf_zero<<<(int)bn, tb>>>(m, s->nwalls, wall_el, touch, zero0);
     const long bw = std::min<long>((m.nnodes + kWarpsPerBlock - 1) / kWarpsPerBlock, 152L * 64);
-    k_vext_integrated<<<(int)bw, 32 * kWarpsPerBlock>>>(*s, m, dimg, dfirst, dcount, wall_el, zero0, d_vext, d_zero);
+    k_vext_integrated<<<(int)bw, 32 * kWarpsPerBlock>>>(*s, m, dimg, dfirst, dcount, tabs, wall_el, zero0, d_vext,
+                                                        d_zero);
     ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
   }
   release();

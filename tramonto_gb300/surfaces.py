@@ -11,8 +11,8 @@ them in the layout build_problem takes.
 The deck is read by the labels of its '@' lines, as the reference's input reader reads fields in
 order (src/dft_input.c): the wall-fluid parameters follow its mixing rules (Lorentz-Berthelot for
 Mix_type 0, src/dft_potential_params.c:120-125; the deck's values for Mix_type 1).  Parts of the
-deck this path does not build (roughness, angle cutouts, Lhard_surf, 9-3 walls of Ipot_wf_n 2 and 3,
-pair potentials other than LJ 12-6, a positive Temp or Length_ref) raise NotImplementedError.
+deck this path does not build (roughness, angle cutouts, Lhard_surf, the charged and Yukawa 1-D wall
+forms, pair potentials other than LJ 12-6, a positive Temp or Length_ref) raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -26,7 +26,8 @@ from . import native
 
 MAXC, MAXWALLS, MAXTYPES, MAXFNC = 4, 16, 4, 4
 SURF_PLANAR, SURF_BLOCK, SURF_COLLOID, SURF_FINITE_CYL, SURF_PORE, SURF_FINITE_PORE = 0, 1, 2, 5, 7, 8
-VEXT_NONE, VEXT_HARD, VEXT_INTEGRATED = 0, 1, 5
+VEXT_NONE, VEXT_HARD, VEXT_DIST_TO_SURF, VEXT_DIST_TO_CENTER, VEXT_INTEGRATED = 0, 1, 2, 3, 5
+WALL1D_LJ93_CS, WALL1D_LJ93_V2_CS, WALL1D_LJ93_NOCS, WALL1D_LJ93_SHIFTX_CS, WALL1D_REPULSIVE9, WALL1D_EXP_ATT = range(6)
 BC_IN_WALL, BC_IN_BULK, BC_PERIODIC, BC_REFLECT, BC_LAST_NODE, BC_LAST_NODE_RESTART = -1, 0, 1, 2, 3, 4
 
 
@@ -36,15 +37,15 @@ class WallType(C.Structure):
                 ("wavelength", C.c_double * MAXFNC), ("periodic_origin", C.c_double * MAXFNC),
                 ("nlinear", C.c_int), ("linear_orient", C.c_int * MAXFNC), ("slope", C.c_double * MAXFNC),
                 ("linear_origin", C.c_double * MAXFNC), ("linear_end", C.c_double * MAXFNC),
-                ("ipot_wf", C.c_int), ("sigma_wf", C.c_double * MAXC), ("eps_wf", C.c_double * MAXC),
-                ("cut_wf", C.c_double * MAXC)]
+                ("ipot_wf", C.c_int), ("type_vext", C.c_int), ("pot_id", C.c_int), ("rho_w", C.c_double),
+                ("sigma_wf", C.c_double * MAXC), ("eps_wf", C.c_double * MAXC), ("cut_wf", C.c_double * MAXC)]
 
 
 class SurfaceSpec(C.Structure):
     """tgpu_surface_spec (include/tramonto_gpu.h)."""
     _fields_ = [("ndim", C.c_int), ("size", C.c_double * 3), ("esize", C.c_double * 3),
                 ("bc", (C.c_int * 2) * 3), ("ncomp", C.c_int), ("vext_max", C.c_double),
-                ("apply_offset", C.c_int * 3), ("ntypes", C.c_int), ("type", WallType * MAXTYPES),
+                ("sigma_ff", C.c_double * MAXC), ("apply_offset", C.c_int * 3), ("ntypes", C.c_int), ("type", WallType * MAXTYPES),
                 ("nwalls", C.c_int), ("wall_type", C.c_int * MAXWALLS), ("wall_pos", (C.c_double * 3) * MAXWALLS)]
 
     def mesh(self):
@@ -55,13 +56,16 @@ class SurfaceSpec(C.Structure):
         return list(nodes), list(els)
 
 
-def make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=10.0, apply_offset=(0, 0, 0)):
+def make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=10.0, apply_offset=(0, 0, 0), sigma_ff=None):
     """A SurfaceSpec from plain values: bc [(lo, hi)] per dimension; types a list of dicts (surf_type,
-    orientation, param, ipot_wf, sigma_wf, eps_wf, cut_wf per component, optional periodic / linear
-    lists of (orientation, amplitude, wavelength, origin) / (orientation, slope, origin, end));
-    walls a list of (type index, position)."""
+    orientation, param, ipot_wf, type_vext (default 1 for integrated walls, else 0), pot_id, rho_w, sigma_wf,
+    eps_wf, cut_wf per component, optional periodic / linear lists of (orientation, amplitude, wavelength,
+    origin) / (orientation, slope, origin, end)); walls a list of (type index, position); sigma_ff the
+    fluid diameters Sigma_ff[i][i]."""
     s = SurfaceSpec()
     s.ndim, s.ncomp, s.vext_max = int(ndim), int(ncomp), float(vext_max)
+    for c in range(ncomp):
+        s.sigma_ff[c] = float(sigma_ff[c]) if sigma_ff is not None else 1.0
     for d in range(3):
         s.size[d] = float(size[d]) if d < ndim else 0.0
         s.esize[d] = float(esize[d]) if d < ndim else 0.0
@@ -87,6 +91,9 @@ def make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=10.0, apply_o
         for i, (ori, sl, org, end) in enumerate(lin):
             o.linear_orient[i], o.slope[i], o.linear_origin[i], o.linear_end[i] = int(ori), sl, org, end
         o.ipot_wf = int(T.get("ipot_wf", VEXT_HARD))
+        o.type_vext = int(T.get("type_vext", 1 if o.ipot_wf == VEXT_INTEGRATED else 0))
+        o.pot_id = int(T.get("pot_id", 0))
+        o.rho_w = float(T.get("rho_w", 1.0))
         for c in range(ncomp):
             o.sigma_wf[c] = float(T.get("sigma_wf", [0.0] * ncomp)[c])
             o.eps_wf[c] = float(T.get("eps_wf", [0.0] * ncomp)[c])
@@ -211,12 +218,17 @@ def read_deck(input_path, surfaces_path=None):
     potid = [int(v) for v in dk.get("Vext_PotentialID", ntypes)]
     ncomp, mix = (int(v) for v in dk.get("Ncomp Mix_type", 2))
     for t in range(ntypes):
-        if ipot[t] not in (VEXT_NONE, VEXT_HARD, VEXT_INTEGRATED):
+        if ipot[t] not in (VEXT_NONE, VEXT_HARD, VEXT_DIST_TO_SURF, VEXT_DIST_TO_CENTER, VEXT_INTEGRATED):
             raise NotImplementedError(f"Ipot_wf_n = {ipot[t]}")
         if ipot[t] == VEXT_INTEGRATED and (tvext[t] != 1 or potid[t] != 0):
             raise NotImplementedError("integrated walls other than the LJ 12-6 pair potential")
+        if ipot[t] in (VEXT_DIST_TO_SURF, VEXT_DIST_TO_CENTER) and (potid[t] != 0 if tvext[t] == 1 else potid[t] > 5):
+            raise NotImplementedError("distance-based walls other than the 1-D forms 0-5 and the LJ 12-6 pair potential")
     nff = ncomp if mix == 0 else ncomp * ncomp
     nww = ntypes if mix == 0 else ntypes * ntypes
+    sff_all = dk.get("Sigma_ff", nff)
+    sigma_ff = [sff_all[i] if mix == 0 else sff_all[i * ncomp + i] for i in range(ncomp)]
+    rho_w = dk.get("Rho_w", ntypes)
     if mix == 0:
         sff = dk.get("Sigma_ff", nff)
         eff = dk.get("Eps_ff", nff)
@@ -237,6 +249,7 @@ def read_deck(input_path, surfaces_path=None):
     types = []
     for t in range(ntypes):
         types.append(dict(surf_type=surf[t], orientation=orient[t], param=(p1[t], p2[t], p3[t]), ipot_wf=ipot[t],
+                          type_vext=tvext[t], pot_id=potid[t], rho_w=rho_w[t],
                           sigma_wf=swf[t], eps_wf=ewf[t], cut_wf=cwf[t],
                           periodic=[(int(p_or[t][i]), p_amp[t][i], p_wl[t][i], p_org[t][i]) for i in range(nper[t])],
                           linear=[(int(l_or[t][i]), l_sl[t][i], l_org[t][i], l_end[t][i]) for i in range(nlin[t])]))
@@ -252,7 +265,8 @@ def read_deck(input_path, surfaces_path=None):
         lo = [min(w[1][d] for w in walls) for d in range(ndim)]
         hi = [max(w[1][d] for w in walls) for d in range(ndim)]
         walls = [(t, [p[d] - 0.5 * (hi[d] + lo[d]) for d in range(ndim)]) for t, p in walls]
-    return make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=vext_max, apply_offset=apply)
+    return make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=vext_max, apply_offset=apply,
+                     sigma_ff=sigma_ff)
 
 
 def problem_fields(spec: SurfaceSpec):
@@ -270,8 +284,10 @@ def spec_arrays(spec: SurfaceSpec) -> dict:
          "apply_offset": np.array(spec.apply_offset[:], np.int32),
          "wall_type": np.array(spec.wall_type[:nw], np.int32),
          "wall_pos": np.array([spec.wall_pos[w][:] for w in range(nw)]).reshape(nw, 3)}
-    for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf"):
+    a["sigma_ff"] = np.array(spec.sigma_ff[:])
+    for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf", "type_vext", "pot_id"):
         a["t_" + f] = np.array([getattr(spec.type[t], f) for t in range(nt)], np.int32)
+    a["t_rho_w"] = np.array([spec.type[t].rho_w for t in range(nt)])
     for f in ("periodic_orient", "linear_orient"):
         a["t_" + f] = np.array([getattr(spec.type[t], f)[:] for t in range(nt)], np.int32).reshape(nt, MAXFNC)
     for f, n in (("param", 3), ("amplitude", MAXFNC), ("wavelength", MAXFNC), ("periodic_origin", MAXFNC),
@@ -288,12 +304,18 @@ def spec_from_arrays(a) -> SurfaceSpec:
         s.size[d], s.esize[d] = float(a["size"][d]), float(a["esize"][d])
         s.bc[d][0], s.bc[d][1] = int(a["bc"][d][0]), int(a["bc"][d][1])
         s.apply_offset[d] = int(a["apply_offset"][d])
+    for c, v in enumerate(a["sigma_ff"] if "sigma_ff" in a else [1.0] * MAXC):
+        s.sigma_ff[c] = float(v)
     nt = len(a["t_surf_type"])
     s.ntypes = nt
     for t in range(nt):
         o = s.type[t]
         for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf"):
             setattr(o, f, int(a["t_" + f][t]))
+        # arrays stored before the distance-based walls: integrated LJ 12-6 walls (Type_vext 1, potential 0)
+        o.type_vext = int(a["t_type_vext"][t]) if "t_type_vext" in a else 1
+        o.pot_id = int(a["t_pot_id"][t]) if "t_pot_id" in a else 0
+        o.rho_w = float(a["t_rho_w"][t]) if "t_rho_w" in a else 1.0
         for f in ("periodic_orient", "linear_orient", "param", "amplitude", "wavelength", "periodic_origin", "slope",
                   "linear_origin", "linear_end", "sigma_wf", "eps_wf", "cut_wf"):
             arr = getattr(o, f)
