@@ -378,31 +378,46 @@ def gaussian_random_field(nx, esize, corr_len=1.0, seed=4321):
 def pore_vext(nx, esize, hs_diam, eps_w, field, pore_radius=5.0, grf_amplitude=0.5, vext_max=10.0):
     """V_ext/kT of a cylindrical pore along z (axis at the box centre in x, y) and its eps_w derivative.
 
-    Species i sees amplitude * field plus a soft cut-and-shifted 9-3 shell eps_w f_i(d) (the form of
-    Vext_LJ9_3_CS, src/dft_vext_1D.c:42-56) of the distance d = R - r from the pore surface, with
-    sigma_wf = (sigma_i + 1)/2 and cut 2.5 sigma_wf.  Nodes with d <= 0 or V >= vext_max hold vext_max
-    (zero-density rows).  Returns (V [ncomp][N], dV/deps_w [ncomp][N], zero-density flags [ncomp][N])."""
-    x = (np.arange(nx[0]) - (nx[0] - 1) / 2) * esize[0]
-    y = (np.arange(nx[1]) - (nx[1] - 1) / 2) * esize[1]
-    r = np.sqrt(x[None, None, :] ** 2 + y[None, :, None] ** 2) * np.ones((nx[2], 1, 1))
-    d = (pore_radius - r).reshape(-1)
+    The pore is the reference's own surface: a cylindrical pore (Surf_type 8, orientation z, radius
+    pore_radius, unbounded length; surface_cylindricalPore3D_inSurfaceTest,
+    src/dft_surfaces_cylindricalPore3D.c:38-96) whose wall acts through the cut-and-shifted 9-3 form of
+    the distance to its surface (Ipot_wf_n 2, Vext_LJ9_3_CS, src/dft_vext_1D.c:42-56) with prefactor
+    eps_w, sigma_wf = (sigma_i + 1)/2 and cut 2.5 sigma_wf — built on the GPU by the surface builder
+    (tramonto_gb300.surfaces), zero-density nodes by the reference's element rule.  Species i also sees
+    grf_amplitude * field.  Nodes whose field reaches vext_max hold vext_max (zero-density rows).  Returns
+    (V [ncomp][N], dV/deps_w [ncomp][N], zero-density flags [ncomp][N])."""
+    from . import surfaces
+    nx = tuple(int(v) for v in nx)
+    size = ((nx[0] - 1) * esize[0], (nx[1] - 1) * esize[1], nx[2] * esize[2])
+    swf = [0.5 * (sig + 1.0) for sig in hs_diam]
+    spec = surfaces.make_spec(
+        3, size, esize, [(BC_IN_WALL, BC_IN_WALL), (BC_IN_WALL, BC_IN_WALL), (BC_PERIODIC, BC_PERIODIC)], len(hs_diam),
+        [(0, (0.0, 0.0, 0.0))],
+        [dict(surf_type=surfaces.SURF_FINITE_PORE, orientation=2, param=(pore_radius, 1.0e6, 0.0),
+              ipot_wf=surfaces.VEXT_DIST_TO_SURF, type_vext=0, pot_id=surfaces.WALL1D_LJ93_CS, rho_w=1.0,
+              sigma_wf=swf, eps_wf=[eps_w] * len(hs_diam), cut_wf=[2.5 * v for v in swf])],
+        vext_max=vext_max, sigma_ff=list(hs_diam))
+    nodes, _ = spec.mesh()
+    if tuple(nodes) != nx:
+        raise ValueError(f"pore mesh {nodes} differs from {nx}")
+    shell, zero, _ = surfaces.surface_field(spec)
     g = grf_amplitude * np.asarray(field).reshape(-1)
     vs, ds, zs = [], [], []
-    for sig in hs_diam:
-        swf = 0.5 * (sig + 1.0)
-        v, de, _ = lj93_wall_1d(d, eps_w, swf, 2.5 * swf, vext_max=np.inf)
-        v = np.where(d > 0, v + g, vext_max)
-        zero = (d <= 0) | (v >= vext_max)
-        vs.append(np.where(zero, vext_max, v))
-        ds.append(np.where(zero, 0.0, de))
-        zs.append(zero)
+    for i in range(len(hs_diam)):
+        live = zero[i] == 0
+        v = np.where(live, shell[i] + g, vext_max)
+        z = ~live | (v >= vext_max)
+        vs.append(np.where(z, vext_max, v))
+        ds.append(np.where(z, 0.0, shell[i] / eps_w))
+        zs.append(z)
     return np.array(vs), np.array(ds), np.array(zs, np.int8)
 
 
 def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0, eps_w=0.5):
     """3-D binary White-Bear (FMT3) hard spheres (sigma 1 and 0.5, rho_b 0.3 and 0.6) in a cylindrical pore
-    of radius 5 along z with a soft 9-3 shell of strength eps_w; V_ext += 0.5 kT * Gaussian random field
-    (correlation length 1).  Walls outside the box in x and y, periodic in z."""
+    of radius 5 along z (the reference's cylindrical pore surface, built on the GPU) with a soft 9-3 wall of
+    strength eps_w; V_ext += 0.5 kT * Gaussian random field (correlation length 1).  Walls outside the box
+    in x and y, periodic in z."""
     es = (esize,) * 3
     field = gaussian_random_field(nx, es, 1.0, seed)
     vext, dv_deps, zd = pore_vext(nx, es, [1.0, 0.5], eps_w, field, pore_radius)
@@ -410,7 +425,8 @@ def config3(nx=(96, 96, 64), esize=0.1, seed=4321, pore_radius=5.0, eps_w=0.5):
                       hs_diam=[1.0, 0.5], rho_b=[0.3, 0.6], functional=FMT3, vext=vext, zero_density=zd)
     return p, dict(grid=list(nx), dx=esize, seed=seed, pore_radius=pore_radius, rho_b=[0.3, 0.6], eps_w=eps_w,
                    functional="FMT3", field="0.5 kT Gaussian random field, correlation length 1",
-                   shell="eps_w * 9-3 cut-and-shifted, sigma_wf=(sigma_i+1)/2, cut 2.5 sigma_wf",
+                   shell="eps_w * 9-3 cut-and-shifted of the distance to the cylindrical pore surface (Ipot_wf_n 2), "
+                         "sigma_wf=(sigma_i+1)/2, cut 2.5 sigma_wf, built on the GPU",
                    grf=field, dv_deps=dv_deps)
 
 
