@@ -371,11 +371,22 @@ double tgpu_lj_rmin(double sigma, double eps_over_kT, double rcut, double esize0
  * node's element (src/dft_surfaces.c:400-430): a 1-D wall form (Type_vext 0) or the LJ 12-6 pair
  * potential (Type_vext 1), a node with X_wall <= 0.001 holding vext_max (setup_vext_XRSurf,
  * src/dft_vext.c:364-436); wall images add nothing (their X_wall is 1000, beyond every cut).
- * Not built (TGPU_ERR_UNSUPPORTED): roughness patches, angle cutouts, Lhard_surf, semi-permeable
- * walls, atomic and single-element surfaces, 2-D slit pores of orientation 0, pair potentials
- * other than LJ 12-6, the charged (LINEAR) and Yukawa 1-D forms, Ipot_wf_n 4. */
+ * Roughness (Lrough_surf): the surface test's distance adjustment adds the height of the patch that
+ * holds the element centre — patches of the planar, cylinder (2-D) and cylinder / pore (3-D) surfaces as
+ * surface_*_roughness (src/dft_surfacesAdjust_roughness.c) — from the table Rough_precalc[type][100][100]
+ * that the reference fills with the C library's rand() after srand(135649), for every wall type in
+ * order (src/dft_setup_params.c:303-331); the library fills it with a restatement of glibc's rand()
+ * (the additive feedback generator of random_r), so surfaces match a reference built on glibc.  A patch
+ * index of 100 or more is TGPU_ERR_ARG (the reference exits there).
+ * Angle cutouts (LangleCutout_surf; surface_angleCutout2D and surface_angleCutout3D_cyl,
+ * src/dft_surfacesAdjust_angleCutout.c:40-139) restrict planar, cylinder, sphere and pore surfaces to a
+ * wedge of angles about the wall centre (blocks have none); angle_start == angle_end is TGPU_ERR_ARG
+ * (the reference leaves its test undefined there).
+ * Not built (TGPU_ERR_UNSUPPORTED): Lhard_surf, semi-permeable walls, atomic and single-element
+ * surfaces, 2-D slit pores of orientation 0, pair potentials other than LJ 12-6, the charged (LINEAR) and
+ * Yukawa 1-D forms, Ipot_wf_n 4. */
 #define TGPU_SURF_MAXWALLS 16
-#define TGPU_SURF_MAXTYPES 4
+#define TGPU_SURF_MAXTYPES 16
 #define TGPU_SURF_MAXFNC 4
 /* Surf_type values (src/dft_globals_const.h surface ids): planar wall, finite block, cylinder (2-D) /
  * sphere (3-D), finite cylinder (3-D), cylindrical pore (2-D) / spherical cavity (3-D), slit pore (2-D) /
@@ -402,6 +413,13 @@ typedef struct {
   int nlinear;                         /* linear overlays: offset += slope (x - origin) between origin and end */
   int linear_orient[TGPU_SURF_MAXFNC];
   double slope[TGPU_SURF_MAXFNC], linear_origin[TGPU_SURF_MAXFNC], linear_end[TGPU_SURF_MAXFNC];
+  int cutout;                          /* LangleCutout_surf: the surface keeps only the elements whose angle
+                                          about the wall centre lies in [angle_start, angle_end] (degrees;
+                                          wrapping past 360 when angle_end < angle_start) */
+  double angle_start, angle_end;       /* Angle_start, Angle_end */
+  int rough;                           /* Lrough_surf: roughness patches of rough_length, heights in
+                                          [-rough_max/2, rough_max/2) */
+  double rough_max, rough_length;      /* Rough_param_max, Rough_length */
   int ipot_wf;                         /* TGPU_VEXT_* (Ipot_wf_n) */
   int type_vext;                       /* Type_vext: 0 a 1-D wall form (VEXT_DEFINED), 1 the pair potential */
   int pot_id;                          /* Vext_PotentialID: a TGPU_WALL1D_* form, or 0 (LJ 12-6) for type_vext 1 */
@@ -429,6 +447,8 @@ int tgpu_surface_mesh(const tgpu_surface_spec *s, int *nodes, int *elements);
  * wall_el is not NULL, the walls of each element as a bit mask [elements].  Host buffers; the
  * _device variant takes device buffers (current device, default stream, synchronised). */
 int tgpu_surface_field_host(const tgpu_surface_spec *s, double *vext, signed char *zero, unsigned short *wall_el);
+/* the roughness patch heights the builder uses, [ntypes][100][100] (host only, no GPU) */
+int tgpu_surface_rough_table(const tgpu_surface_spec *s, double *out);
 int tgpu_surface_field_device(const tgpu_surface_spec *s, double *d_vext, signed char *d_zero,
                               unsigned short *d_wall_el);
 /* the WCA attraction u_att(r) in kT (uLJ12_6_ATT_CS, src/dft_pairPot_LJ12_6.c:128-168) */

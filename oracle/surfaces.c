@@ -95,7 +95,119 @@ static void or_node_pos(const tgpu_surface_spec *s, const or_mesh *m, long inode
   }
 }
 
-static double or_overlay(const tgpu_wall_type *T, int ndim, const double *x)
+/* Rough_precalc (src/dft_setup_params.c:303-331): the C library's rand() after srand(135649), every wall
+ * type in order; [ntypes][100][100] */
+#define OR_ROUGH 100
+static double *or_rough_tables(const tgpu_surface_spec *s)
+{
+  int t, i, any = 0;
+  double *tab = calloc((size_t)(s->ntypes > 0 ? s->ntypes : 1) * OR_ROUGH * OR_ROUGH, sizeof(double));
+  for (t = 0; t < s->ntypes; t++) any |= s->type[t].rough;
+  if (!any) return tab;
+  srand(135649);
+  for (t = 0; t < s->ntypes; t++)
+    for (i = 0; i < OR_ROUGH * OR_ROUGH; i++) {
+      int irand = rand() % 2147483647;
+      tab[(size_t)t * OR_ROUGH * OR_ROUGH + i] = s->type[t].rough_max * (-0.5 + (((double)irand) / ((double)2147483647)));
+    }
+  return tab;
+}
+
+/* surface_planar_roughness, surface_cylinder2D_roughness, surface_cylinder3D_roughness
+ * (src/dft_surfacesAdjust_roughness.c:38-180); returns 0 and sets *bad for a patch index >= 100 */
+static double or_rough(const tgpu_surface_spec *s, const tgpu_wall_type *T, const double *x, const double *wp,
+                       const double *tab, int *bad)
+{
+  int st = T->surf_type, nd = s->ndim, rb[2] = {0, 0}, idim, ib = 0;
+  if (!T->rough || nd < 2) return 0.0;
+  if (st == TGPU_SURF_PLANAR || st == TGPU_SURF_BLOCK) {
+    int orientation = st == TGPU_SURF_PLANAR ? T->orientation : 0;
+    for (idim = 0; idim < nd; idim++) {
+      if (idim != orientation) {
+        rb[ib] = (int)((x[idim] + 0.5 * s->size[idim]) / T->rough_length);
+        if (rb[ib] >= OR_ROUGH) { *bad = 1; return 0.0; }
+        ib++;
+      }
+    }
+  } else if (nd == 2 && (st == TGPU_SURF_COLLOID || st == TGPU_SURF_PORE || st == TGPU_SURF_FINITE_PORE)) {
+    double vecB[2], rsq = 0.0, r, angle, angle_deg, angle_block = asin(T->rough_length / T->param[0]);
+    for (idim = 0; idim < nd; idim++) {
+      vecB[idim] = x[idim] - wp[idim];
+      rsq += vecB[idim] * vecB[idim];
+    }
+    r = sqrt(rsq);
+    angle = acos(vecB[0] / r);
+    angle_deg = 180. * angle / OR_PI;
+    if (x[1] < wp[1]) angle_deg = 360 - angle_deg;
+    angle = angle_deg * OR_PI / 180.;
+    rb[0] = (int)(angle / angle_block);
+  } else if (nd == 3 && (st == TGPU_SURF_FINITE_CYL || st == TGPU_SURF_FINITE_PORE)) {
+    double xtest[3], vecB[3], rsq = 0.0, r, angle, angle_deg, angle_block;
+    int dim[3], test_cos;
+    switch (T->orientation) {
+      case 2: xtest[0] = x[0]; dim[0] = 0; xtest[1] = x[1]; dim[1] = 1; xtest[2] = x[2]; dim[2] = 2; test_cos = 1; break;
+      case 1: xtest[0] = x[2]; dim[0] = 2; xtest[1] = x[0]; dim[1] = 0; xtest[2] = x[1]; dim[2] = 1; test_cos = 0; break;
+      default: xtest[0] = x[1]; dim[0] = 1; xtest[1] = x[2]; dim[1] = 2; xtest[2] = x[0]; dim[2] = 0; test_cos = 2; break;
+    }
+    angle_block = asin(T->rough_length / T->param[0]);
+    for (idim = 0; idim < nd - 1; idim++) {
+      vecB[idim] = xtest[idim] - wp[dim[idim]];
+      rsq += vecB[idim] * vecB[idim];
+    }
+    r = sqrt(rsq);
+    angle = acos(vecB[0] / r);
+    angle_deg = 180. * angle / OR_PI;
+    if (x[test_cos] < wp[test_cos]) angle_deg = 360 - angle_deg;
+    angle = OR_PI * angle_deg / 180;
+    rb[0] = (int)(angle / angle_block);
+    rb[1] = (int)((x[T->orientation] + 0.5 * s->size[T->orientation]) / T->rough_length);
+  } else {
+    return 0.0;
+  }
+  if (rb[0] >= OR_ROUGH || rb[1] >= OR_ROUGH) { *bad = 1; return 0.0; }
+  return tab[rb[0] * OR_ROUGH + rb[1]];
+}
+
+/* surface_angleCutout2D / surface_angleCutout3D_cyl (src/dft_surfacesAdjust_angleCutout.c:40-139) with
+ * the choice of setup_surface (src/dft_surfaces.c:246-330); spheres and spherical cavities have no
+ * orientation set (0) */
+static int or_angle_test(const tgpu_surface_spec *s, const tgpu_wall_type *T, const double *x, const double *wp)
+{
+  int nd = s->ndim, idim, angle_test = 1, dim[3], idim_testCos = 1, orientation;
+  double vecB[3], xtest[3], rsq = 0.0, r, angle, angle_deg;
+  if (!T->cutout || nd < 2 || T->surf_type == TGPU_SURF_BLOCK) return 1;
+  if (nd == 2) {
+    for (idim = 0; idim < nd; idim++) {
+      vecB[idim] = x[idim] - wp[idim];
+      rsq += vecB[idim] * vecB[idim];
+    }
+  } else {
+    orientation = (T->surf_type == TGPU_SURF_FINITE_CYL || T->surf_type == TGPU_SURF_FINITE_PORE) ? T->orientation : 0;
+    switch (orientation) {
+      case 2: xtest[0] = x[0]; dim[0] = 0; xtest[1] = x[1]; dim[1] = 1; idim_testCos = 1; break;
+      case 1: xtest[0] = x[2]; dim[0] = 2; xtest[1] = x[0]; dim[1] = 0; idim_testCos = 0; break;
+      default: xtest[0] = x[1]; dim[0] = 1; xtest[1] = x[2]; dim[1] = 2; idim_testCos = 2; break;
+    }
+    for (idim = 0; idim < nd - 1; idim++) {
+      vecB[idim] = xtest[idim] - wp[dim[idim]];
+      rsq += vecB[idim] * vecB[idim];
+    }
+  }
+  r = sqrt(rsq);
+  angle = acos(vecB[0] / r);
+  angle_deg = 180. * angle / OR_PI;
+  if (x[idim_testCos] < wp[idim_testCos]) angle_deg = 360 - angle_deg;
+  if (T->angle_end > T->angle_start) {
+    angle_test = 1;
+    if (angle_deg < T->angle_start || angle_deg > T->angle_end) angle_test = 0;
+  } else if (T->angle_end < T->angle_start) {
+    angle_test = 0;
+    if (angle_deg > T->angle_start || angle_deg < T->angle_end) angle_test = 1;
+  }
+  return angle_test;
+}
+
+static double or_overlay(const tgpu_wall_type *T, int ndim, const double *x, double dist_roughness)
 {
   double dist_periodic = 0.0, dist_linear = 0.0, adj = 0.0;
   int i, use_per = 0, use_lin = 0, forced = 0;
@@ -124,7 +236,7 @@ static double or_overlay(const tgpu_wall_type *T, int ndim, const double *x)
     }
     dist_linear = offset;
   }
-  adj += (0.0 + dist_periodic + dist_linear);
+  adj += (dist_roughness + dist_periodic + dist_linear);
   return adj;
 }
 
@@ -449,7 +561,8 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
   or_mesh m;
   int nd = s->ndim, nw = s->nwalls, iwall, idim, i, icomp, ncorner;
   int nimg, k_img, *real, (*touch)[3][2];
-  double (*wpos)[3], *xwall;
+  double (*wpos)[3], *xwall, *rough;
+  int bad_rough = 0;
   unsigned short *wall_el;
   long iel, inode;
   signed char *zero0;
@@ -486,6 +599,7 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
     }
   }
 
+  rough = or_rough_tables(s);
   /* wall elements and touched faces; X_wall when a wall type is distance-based */
   wall_el = calloc((size_t)m.nels, sizeof(unsigned short));
   touch = calloc((size_t)nw + 1, sizeof(*touch));
@@ -508,7 +622,9 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
         r /= m.els[idim];
         xtest[idim] = (-0.5 * s->size[idim] + s->esize[idim] * ijk[idim]) + 0.5 * s->esize[idim];
       }
-      adj = or_overlay(T, nd, xtest);
+      adj = or_overlay(T, nd, xtest,
+                       or_rough(s, T, xtest, s->wall_pos[iwall], rough + (size_t)s->wall_type[iwall] * OR_ROUGH * OR_ROUGH,
+                                &bad_rough));
       if (xwall) {   /* X_wall from the nodes of this element (src/dft_surfaces.c:400-430) */
         int imax[3] = {1, 1, 1}, ix[3];
         for (idim = 0; idim < nd; idim++)
@@ -528,7 +644,7 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
               else xwall[node * nw + iwall] = 0.0;
             }
       }
-      if (or_in_surface(s, T, s->wall_pos[iwall], xtest, adj)) {
+      if (or_in_surface(s, T, s->wall_pos[iwall], xtest, adj) && or_angle_test(s, T, xtest, s->wall_pos[iwall])) {
         wall_el[iel] |= (unsigned short)(1u << iwall);
         for (idim = 0; idim < nd; idim++) {
           int nadd = s->bc[idim][1] == TGPU_BC_PERIODIC ? 0 : 1;
@@ -684,6 +800,8 @@ int oracle_surface_field(const tgpu_surface_spec *s, double *vext, signed char *
   free(wall_el);
   free(touch);
   free(xwall);
+  free(rough);
+  if (bad_rough) return -1;
   free(zero0);
   free(wpos);
   free(real);

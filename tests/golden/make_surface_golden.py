@@ -28,7 +28,8 @@ from tramonto_gb300 import surfaces  # noqa: E402
 
 # deck -> fixture name: the example decks whose surfaces the GPU builder covers (no roughness, angle cutouts
 # or Lhard_surf), small enough for the reference to set up in about two minutes: every such GEOM deck with
-# integrated LJ 12-6 walls, and decks of the distance-based 9-3 walls in 1-D, 2-D and 3-D
+# integrated LJ 12-6 walls, decks of the distance-based 9-3 walls in 1-D, 2-D and 3-D, rough surfaces and
+# angle cutouts
 DECKS = {
     "GEOM25_CYL_PORE_2D": "surf_cylpore2d",
     "GEOM31_TAPERED_CYLPORE_3D": "surf_taperedpore3d",
@@ -51,6 +52,24 @@ DECKS = {
     "CONT1_FMT1_WCA_1D": "surf_lj93_cont1d",
     "BC1_FMT1_WCA_ELEC_2D": "surf_lj93_2d_three",
     "BC7_FMT1_WCA_ELEC_3D": "surf_lj93_3d_three",
+    # roughness patches (Rough_precalc from the C library's rand() after srand(135649))
+    "GEOM1_PLANE_ROUGH_2D": "surf_rough_plane2d",
+    "GEOM3_PLANE_ROUGH_3D": "surf_rough_plane3d",
+    "GEOM6_PLANE_ROUGH_VEXTINT_2D": "surf_rough_vextint2d",
+    "GEOM7_PLANE_ROUGH_VEXTINT_3D": "surf_rough_vextint3d",
+    "GEOM13_CYL_ROUGH_2D": "surf_rough_cyl2d",
+    "GEOM21_CYL_ROUGH_3D": "surf_rough_cyl3d",
+    "GEOM26_CYL_PORE_ROUGH_2D": "surf_rough_cylpore2d",
+    # angle cutouts (wedges of cylinders, pores and slits; two and twelve wall types)
+    "GEOM14_CYL_WEDGECUTOUT_2D": "surf_cut_cyl2d",
+    "GEOM15_CYL_WEDGE2TYPES_2D": "surf_cut_cyl2d_twelve",
+    "GEOM16_CYL_WEDGE2TYPES_REFLECT_2D": "surf_cut_cyl2d_reflect",
+    "GEOM22_CYL_WEDGE2TYPES_3D": "surf_cut_cyl3d",
+    "GEOM27_CYL_PORE_WEDGE2TYPES_2D": "surf_cut_cylpore2d",
+    "GEOM28_CYLPORE_WEDGE2TYPES_3D": "surf_cut_cylpore3d",
+    "GEOM29_SLITPORE_2D": "surf_cut_slitpore2d",
+    "GEOM30_TAPERED_SLITPORE_2D": "surf_cut_taperedslit2d",
+    "GEOM36_PLANE_NOTCH_2D": "surf_cut_notch2d",
 }
 
 

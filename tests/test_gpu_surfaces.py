@@ -80,8 +80,27 @@ def _periodic_specs():
     # an integrated planar wall in 1-D (the 2 pi rho dz out-of-line integral) with a face copy region
     si1 = surfaces.make_spec(1, (8.0,), (0.1,), [(-1, 0)], 2, [(0, (-3.5,))],
                              [dict(surf_type=surfaces.SURF_PLANAR, orientation=0, param=(0.5, 0, 0), ipot_wf=5, **lj)])
+    # rough 3-D cylindrical pore (integrated) next to a rough slit pore wall in 2-D (distance-based)
+    sr3 = surfaces.make_spec(3, (4.0, 4.0, 5.0), (0.25, 0.25, 0.25), [(-1, -1), (-1, -1), (1, 1)], 1, [(0, (0.0, 0.0, 0.0))],
+                             [dict(surf_type=surfaces.SURF_FINITE_PORE, orientation=2, param=(1.5, 1.75, 0.0), ipot_wf=5,
+                                   rough=1, rough_max=0.4, rough_length=0.5, sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0])])
+    sr2 = surfaces.make_spec(2, (6.0, 8.0), (0.2, 0.2), [(-1, -1), (1, 1)], 2, [(0, (0.0, 0.0))],
+                             [dict(surf_type=surfaces.SURF_FINITE_PORE, orientation=1, param=(1.5, 3.0, 0.0), ipot_wf=2,
+                                   rough=1, rough_max=0.5, rough_length=0.3, pot_id=surfaces.WALL1D_LJ93_CS, **lj1)])
+    # angle cutouts of a 3-D sphere (no orientation: the wedge about x) and of a spherical cavity, and a 2-D
+    # wedge that wraps past 360 degrees
+    sc3 = surfaces.make_spec(3, (4.0, 4.0, 4.0), (0.25, 0.25, 0.25), [(2, 2), (2, 2), (2, 2)], 1,
+                             [(0, (0.0, 0.0, 0.0)), (1, (0.0, 0.0, 0.0))],
+                             [dict(surf_type=surfaces.SURF_COLLOID, param=(1.0, 0, 0), ipot_wf=5, cutout=1,
+                                   angle_start=30.0, angle_end=200.0, sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0]),
+                              dict(surf_type=surfaces.SURF_PORE, param=(1.8, 0, 0), ipot_wf=5, cutout=1,
+                                   angle_start=300.0, angle_end=60.0, sigma_wf=[1.0], eps_wf=[0.5], cut_wf=[2.0])])
+    sc2 = surfaces.make_spec(2, (6.0, 6.0), (0.2, 0.2), [(-1, -1), (1, 1)], 2, [(0, (0.0, 0.0))],
+                             [dict(surf_type=surfaces.SURF_COLLOID, param=(1.2, 0, 0), ipot_wf=5, cutout=1,
+                                   angle_start=250.0, angle_end=80.0, **lj)])
     return {"periodic2d": s2, "periodic3d": s3, "reflect_periodic_pore3d": s3p, "distance_walls2d": sd2,
-            "distance_walls3d": sd3, "integrated1d": si1}
+            "distance_walls3d": sd3, "integrated1d": si1, "rough_pore3d": sr3, "rough_slit2d": sr2,
+            "cutout_sphere3d": sc3, "cutout_wrap2d": sc2}
 
 
 @pytest.mark.parametrize("case", list(_periodic_specs()))

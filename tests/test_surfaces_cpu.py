@@ -22,7 +22,8 @@ FIXTURES = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os
 # the fixtures the oracle restates in a few seconds (its loops are the reference's, one thread)
 ORACLE_FIXTURES = ["surf_cylpore2d", "surf_block2d", "surf_cyl2d", "surf_plane2d_periodic", "surf_sphere3d",
                    "surf_lj93_plane2d_cosx", "surf_lj93_plane2d_cosy", "surf_lj93_1d", "surf_lj93_mix1d",
-                   "surf_lj93_cont1d", "surf_lj93_2d_three", "surf_lj93_3d_three"]
+                   "surf_lj93_cont1d", "surf_lj93_2d_three", "surf_lj93_3d_three", "surf_rough_plane2d",
+                   "surf_rough_plane3d", "surf_rough_cylpore2d", "surf_cut_notch2d", "surf_cut_cylpore2d"]
 V_TOL = 1e-10
 
 
@@ -162,7 +163,29 @@ def test_read_deck_of_own_text(tmp_path):
 
 
 def test_read_deck_refuses_what_is_not_built(tmp_path):
-    (tmp_path / "dft_input.dat").write_text(DECK.replace("@ 0 0 \tLrough_surf", "@ 1 0 \tLrough_surf"))
+    (tmp_path / "dft_input.dat").write_text(DECK.replace("@ 0 \tLhard_surf", "@ 1 \tLhard_surf"))
     (tmp_path / "dft_surfaces.dat").write_text(" 0 0 -2.0 1.0 0.\n 1 0 1.0 -1.0 0.\n 1 1 3.0 0.0 0.\n")
     with pytest.raises(NotImplementedError):
         surfaces.read_deck(str(tmp_path / "dft_input.dat"))
+
+
+def test_rough_table_is_the_c_library_rand():
+    """the builder's roughness patch heights equal Rough_precalc as the reference fills it: rand() % (2^31 - 1)
+    after srand(135649), every wall type in order (here the C library's own rand(), when it is glibc)"""
+    import ctypes
+    try:
+        libc = ctypes.CDLL("libc.so.6")
+        libc.gnu_get_libc_version
+    except (OSError, AttributeError):
+        pytest.skip("not glibc")
+    lj = dict(sigma_wf=[1.0], eps_wf=[1.0], cut_wf=[2.0])
+    spec = surfaces.make_spec(2, (10.0, 10.0), (0.25, 0.25), [(-1, -1), (1, 1)], 1, [(0, (0.0, 0.0)), (1, (3.0, 0.0))],
+                              [dict(surf_type=surfaces.SURF_PLANAR, param=(1.0, 0, 0), rough=1, rough_max=0.5,
+                                    rough_length=0.5, **lj),
+                               dict(surf_type=surfaces.SURF_COLLOID, param=(1.0, 0, 0), rough=1, rough_max=0.3,
+                                    rough_length=0.4, **lj)])
+    tab = surfaces.rough_table(spec)
+    libc.srand(135649)
+    r = np.array([libc.rand() % 2147483647 for _ in range(20000)], np.float64).reshape(2, 100, 100)
+    assert np.array_equal(tab[0], 0.5 * (-0.5 + r[0] / 2147483647.0))
+    assert np.array_equal(tab[1], 0.3 * (-0.5 + r[1] / 2147483647.0))

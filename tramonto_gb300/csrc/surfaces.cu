@@ -77,10 +77,89 @@ __host__ __device__ inline bool bc_face_wall(int b)
 
 // ---- surface tests (src/dft_surfaces_*.c, *_inSurfaceTest) ----------------------------------------
 
+constexpr int kRoughBlocks = 100;          // MAX_ROUGH_BLOCK
+constexpr unsigned kErrRoughBlock = 1u;    // a roughness patch index beyond the table (the reference exits)
+
+// Roughness (src/dft_surfacesAdjust_roughness.c): the height of the patch of the table `rough`
+// ([100][100] of this wall type) that holds the element centre x; w is the wall's position.
+__device__ double rough_planar(const tgpu_surface_spec &s, const tgpu_wall_type &T, int orientation, const double *x,
+                               const double *rough, unsigned *err)
+{
+  int rb[2] = {0, 0}, ib = 0;
+  for (int d = 0; d < s.ndim; d++) {
+    if (d == orientation) continue;
+    rb[ib] = (int)((x[d] + 0.5 * s.size[d]) / T.rough_length);
+    if (rb[ib] >= kRoughBlocks) { atomicOr(err, kErrRoughBlock); rb[ib] = 0; }
+    ib++;
+  }
+  return rough[rb[0] * kRoughBlocks + rb[1]];
+}
+
+__device__ double rough_cylinder2d(const tgpu_wall_type &T, const double *x, const double *w, const double *rough,
+                                   unsigned *err)
+{
+  const double angle_block = asin(T.rough_length / T.param[0]);
+  double vec[2], rsq = 0.0;
+  for (int d = 0; d < 2; d++) {
+    vec[d] = x[d] - w[d];
+    rsq += vec[d] * vec[d];
+  }
+  const double r = sqrt(rsq);
+  double deg = 180. * acos(vec[0] / r) / kPi;
+  if (x[1] < w[1]) deg = 360 - deg;
+  const double angle = deg * kPi / 180.;
+  int rb0 = (int)(angle / angle_block);
+  if (rb0 >= kRoughBlocks) { atomicOr(err, kErrRoughBlock); rb0 = 0; }
+  return rough[rb0 * kRoughBlocks];
+}
+
+__device__ double rough_cylinder3d(const tgpu_surface_spec &s, const tgpu_wall_type &T, const double *x,
+                                   const double *w, const double *rough, unsigned *err)
+{
+  int dim[3], test_cos;
+  const int o = T.orientation;
+  if (o == 2) { dim[0] = 0; dim[1] = 1; dim[2] = 2; test_cos = 1; }
+  else if (o == 1) { dim[0] = 2; dim[1] = 0; dim[2] = 1; test_cos = 0; }
+  else { dim[0] = 1; dim[1] = 2; dim[2] = 0; test_cos = 2; }
+  const double angle_block = asin(T.rough_length / T.param[0]);
+  double vec[2], rsq = 0.0;
+  for (int i = 0; i < 2; i++) {
+    vec[i] = x[dim[i]] - w[dim[i]];
+    rsq += vec[i] * vec[i];
+  }
+  const double r = sqrt(rsq);
+  double deg = 180. * acos(vec[0] / r) / kPi;
+  if (x[test_cos] < w[test_cos]) deg = 360 - deg;
+  const double angle = kPi * deg / 180;
+  int rb0 = (int)(angle / angle_block);
+  int rb1 = (int)((x[o] + 0.5 * s.size[o]) / T.rough_length);
+  if (rb0 >= kRoughBlocks || rb1 >= kRoughBlocks) { atomicOr(err, kErrRoughBlock); rb0 = rb1 = 0; }
+  return rough[rb0 * kRoughBlocks + rb1];
+}
+
+// the roughness height of this surface at x (the fp_roughness choice of setup_surface,
+// src/dft_surfaces.c:246-330; blocks use the planar patches with orientation 0, the orientation their
+// geometry record leaves unset)
+__device__ double rough_adjust(const tgpu_surface_spec &s, const tgpu_wall_type &T, const double *x, const double *w,
+                               const double *rough, unsigned *err)
+{
+  if (!T.rough || s.ndim < 2) return 0.0;
+  switch (T.surf_type) {
+    case TGPU_SURF_PLANAR: return rough_planar(s, T, T.orientation, x, rough, err);
+    case TGPU_SURF_BLOCK: return rough_planar(s, T, 0, x, rough, err);
+    case TGPU_SURF_COLLOID:
+    case TGPU_SURF_PORE: return s.ndim == 2 ? rough_cylinder2d(T, x, w, rough, err) : 0.0;
+    case TGPU_SURF_FINITE_CYL: return rough_cylinder3d(s, T, x, w, rough, err);
+    case TGPU_SURF_FINITE_PORE:
+      return s.ndim == 3 ? rough_cylinder3d(s, T, x, w, rough, err) : rough_cylinder2d(T, x, w, rough, err);
+    default: return 0.0;
+  }
+}
+
 // the distance adjustment of the overlays the reference applies to this surface (the fp_periodic and
 // fp_linear choices of setup_surface, src/dft_surfaces.c:246-330, and the forced orientations of
-// src/dft_setup_params.c:681-790)
-__device__ double overlay_adjust(const tgpu_wall_type &T, int ndim, const double *x)
+// src/dft_setup_params.c:681-790), after the roughness height dr
+__device__ double overlay_adjust(const tgpu_wall_type &T, int ndim, const double *x, double dr)
 {
   const int st = T.surf_type;
   bool per = false, lin = false, forced = false;
@@ -103,7 +182,7 @@ __device__ double overlay_adjust(const tgpu_wall_type &T, int ndim, const double
     }
   }
   double adj = 0.0;
-  adj += (0.0 + dp + dl);
+  adj += (dr + dp + dl);
   return adj;
 }
 
@@ -234,10 +313,49 @@ __device__ __forceinline__ double node_pos(const Mesh &m, int d, int i)
   return -0.5 * m.size[d] + m.esize[d] * (double)i;
 }
 
+// the wedge test of an angle cutout (surface_angleCutout2D / surface_angleCutout3D_cyl): the angle of the
+// element centre x about the wall centre w in the plane across axis `o` (3-D), in degrees over [0, 360)
+__device__ bool angle_cutout(const tgpu_surface_spec &s, const tgpu_wall_type &T, const double *x, const double *w)
+{
+  double vec[2], rsq = 0.0;
+  int test_cos = 1;
+  if (s.ndim == 2) {
+    for (int d = 0; d < 2; d++) {
+      vec[d] = x[d] - w[d];
+      rsq += vec[d] * vec[d];
+    }
+  } else {
+    // spheres and spherical cavities keep the orientation their geometry record leaves at 0
+    const int o = (T.surf_type == TGPU_SURF_FINITE_CYL || T.surf_type == TGPU_SURF_FINITE_PORE) ? T.orientation : 0;
+    int dim[3];
+    if (o == 2) { dim[0] = 0; dim[1] = 1; dim[2] = 2; test_cos = 1; }
+    else if (o == 1) { dim[0] = 2; dim[1] = 0; dim[2] = 1; test_cos = 0; }
+    else { dim[0] = 1; dim[1] = 2; dim[2] = 0; test_cos = 2; }
+    for (int i = 0; i < 2; i++) {
+      vec[i] = x[dim[i]] - w[dim[i]];
+      rsq += vec[i] * vec[i];
+    }
+  }
+  const double r = sqrt(rsq);
+  double deg = 180. * acos(vec[0] / r) / kPi;
+  if (x[test_cos] < w[test_cos]) deg = 360 - deg;
+  if (T.angle_end > T.angle_start) return !(deg < T.angle_start || deg > T.angle_end);
+  return deg > T.angle_start || deg < T.angle_end;
+}
+
+__device__ bool has_cutout(const tgpu_surface_spec &s, const tgpu_wall_type &T)
+{
+  // planar walls (2-D and 3-D), cylinders / spheres, finite cylinders and pores (src/dft_surfaces.c:246-330)
+  return T.cutout && s.ndim > 1 && T.surf_type != TGPU_SURF_BLOCK &&
+         !(T.surf_type == TGPU_SURF_PLANAR && s.ndim == 3);
+}
+
 // ---- k_surf_elements ------------------------------------------------------------------------------
 
-__global__ void k_surf_elements(tgpu_surface_spec s, Mesh m, unsigned short *wall_el, unsigned *touch)
+__global__ void k_surf_elements(const tgpu_surface_spec *__restrict__ sp, Mesh m, const double *rough,
+                                unsigned short *wall_el, unsigned *touch, unsigned *err)
 {
+  const tgpu_surface_spec &s = *sp;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < m.nels; e += (long)gridDim.x * blockDim.x) {
     int ijk[3] = {0, 0, 0};
     long r = e;
@@ -250,8 +368,11 @@ __global__ void k_surf_elements(tgpu_surface_spec s, Mesh m, unsigned short *wal
     unsigned short bits = 0;
     for (int iw = 0; iw < s.nwalls; iw++) {
       const tgpu_wall_type &T = s.type[s.wall_type[iw]];
-      const double adj = overlay_adjust(T, m.ndim, x);
+      const double dr = rough_adjust(s, T, x, s.wall_pos[iw], rough + (long)s.wall_type[iw] * kRoughBlocks * kRoughBlocks,
+                                     err);
+      const double adj = overlay_adjust(T, m.ndim, x, dr);
       if (!in_surface(T, m.ndim, s.apply_offset, s.wall_pos[iw], x, adj)) continue;
+      if (has_cutout(s, T) && !angle_cutout(s, T, x, s.wall_pos[iw])) continue;
       bits |= (unsigned short)(1u << iw);
       unsigned t = 0;
       for (int d = 0; d < m.ndim; d++) {
@@ -657,7 +778,8 @@ __device__ double wall_1d(const tgpu_wall_type &T, int c, double sigma_ff, doubl
 // setup_vext_XRSurf (src/dft_vext.c:364-436) for one real wall at one node: X_wall from the surface test at
 // the node with the overlay adjustment of the element the reference tests the node from (its own lower
 // corner element, the last element along a dimension for the far nodes; src/dft_surfaces.c:400-430)
-__device__ void add_xr_wall(const tgpu_surface_spec &s, const Mesh &m, int iw, const int *ijk, NodeState &S)
+__device__ void add_xr_wall(const tgpu_surface_spec &s, const Mesh &m, int iw, const int *ijk, const double *rough,
+                            unsigned *err, NodeState &S)
 {
   const tgpu_wall_type &T = s.type[s.wall_type[iw]];
   double xc[3] = {0.0, 0.0, 0.0}, xt[3] = {0.0, 0.0, 0.0};
@@ -667,7 +789,9 @@ __device__ void add_xr_wall(const tgpu_surface_spec &s, const Mesh &m, int iw, c
     xc[d] = p + 0.5 * m.esize[d];
     xt[d] = p + (ijk[d] - e) * m.esize[d];
   }
-  const double adj = overlay_adjust(T, m.ndim, xc);
+  const double dr = rough_adjust(s, T, xc, s.wall_pos[iw], rough + (long)s.wall_type[iw] * kRoughBlocks * kRoughBlocks,
+                                 err);
+  const double adj = overlay_adjust(T, m.ndim, xc, dr);
   const double delx = surface_dist(T, m.ndim, s.apply_offset, s.wall_pos[iw], xt, adj,
                                    T.ipot_wf == TGPU_VEXT_DIST_TO_CENTER);
   const double xw = delx > 0.0 ? fmin(delx, 1000.0) : 0.0;
@@ -693,10 +817,11 @@ __host__ __device__ inline PotParams pot_params(const tgpu_wall_type &T, int c)
 }
 
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-k_vext_integrated(tgpu_surface_spec s, Mesh m, const Image *img, const int *img_first, const int *img_count,
-                  Tables tabs, const unsigned short *wall_el, const unsigned char *zero0, double *vext,
-                  signed char *zero)
+k_vext_integrated(const tgpu_surface_spec *__restrict__ sp, Mesh m, const Image *img, const int *img_first,
+                  const int *img_count, Tables tabs, const double *rough, unsigned *err, const unsigned short *wall_el,
+                  const unsigned char *zero0, double *vext, signed char *zero)
 {
+  const tgpu_surface_spec &s = *sp;
   const int lane = threadIdx.x & 31;
   const long nwarps = ((long)gridDim.x * blockDim.x) >> 5;
   for (long n = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5; n < m.nnodes; n += nwarps) {
@@ -719,7 +844,7 @@ k_vext_integrated(tgpu_surface_spec s, Mesh m, const Image *img, const int *img_
     for (int iw = 0; iw < s.nwalls && !z0; iw++) {
       const tgpu_wall_type &T = s.type[s.wall_type[iw]];
       if (T.ipot_wf == TGPU_VEXT_DIST_TO_SURF || T.ipot_wf == TGPU_VEXT_DIST_TO_CENTER) {
-        add_xr_wall(s, m, iw, ijk, S);
+        add_xr_wall(s, m, iw, ijk, rough, err, S);
         continue;
       }
       if (T.ipot_wf != TGPU_VEXT_INTEGRATED) continue;
@@ -852,6 +977,19 @@ int check_spec(const tgpu_surface_spec *s)
       default:
         return TGPU_ERR_UNSUPPORTED;
     }
+    if (T.cutout && !(T.angle_start != T.angle_end)) return TGPU_ERR_ARG;
+    // the reference gives 3-D planar walls the 2-D wedge test, which writes past its 2-vector there
+    if (T.cutout && T.surf_type == TGPU_SURF_PLANAR && s->ndim == 3) return TGPU_ERR_UNSUPPORTED;
+    if (T.rough && s->ndim > 1) {
+      if (!(T.rough_length > 0.0)) return TGPU_ERR_ARG;
+      // the reference exits when a patch is longer than the radius (or a quarter of a cylinder's length)
+      const bool cyl = T.surf_type == TGPU_SURF_FINITE_CYL || T.surf_type == TGPU_SURF_FINITE_PORE ||
+                       ((T.surf_type == TGPU_SURF_COLLOID || T.surf_type == TGPU_SURF_PORE) && s->ndim == 2);
+      if (cyl && T.rough_length > T.param[0]) return TGPU_ERR_ARG;
+      if ((T.surf_type == TGPU_SURF_FINITE_CYL || (T.surf_type == TGPU_SURF_FINITE_PORE && s->ndim == 3)) &&
+          T.rough_length > (T.param[1] - kRoff) / 2.)
+        return TGPU_ERR_ARG;
+    }
     if (T.ipot_wf != TGPU_VEXT_NONE && T.ipot_wf != TGPU_VEXT_HARD && T.ipot_wf != TGPU_VEXT_INTEGRATED &&
         T.ipot_wf != TGPU_VEXT_DIST_TO_SURF && T.ipot_wf != TGPU_VEXT_DIST_TO_CENTER)
       return TGPU_ERR_UNSUPPORTED;
@@ -859,9 +997,12 @@ int check_spec(const tgpu_surface_spec *s)
     if ((T.ipot_wf == TGPU_VEXT_DIST_TO_SURF || T.ipot_wf == TGPU_VEXT_DIST_TO_CENTER) &&
         !(T.type_vext == 1 ? T.pot_id == 0 : (T.pot_id >= TGPU_WALL1D_LJ93_CS && T.pot_id <= TGPU_WALL1D_EXP_ATT)))
       return TGPU_ERR_UNSUPPORTED;
+    // a component with sigma_wf = cut_wf = 0 (values a deck leaves unset) sees nothing of the wall, as in the
+    // reference; negative or non-finite values are refused
     if (T.ipot_wf >= TGPU_VEXT_DIST_TO_SURF)
       for (int c = 0; c < s->ncomp; c++)
-        if (!(T.cut_wf[c] > 0.0) || !(T.sigma_wf[c] > 0.0)) return TGPU_ERR_ARG;
+        if (!(T.cut_wf[c] >= 0.0) || !(T.sigma_wf[c] >= 0.0) || (T.cut_wf[c] > 0.0) != (T.sigma_wf[c] > 0.0))
+          return TGPU_ERR_ARG;
   }
   return TGPU_OK;
 }
@@ -952,6 +1093,54 @@ bool make_images(const tgpu_surface_spec *s, std::vector<Image> &out, std::vecto
   return (int)out.size() <= kMaxImages;
 }
 
+// glibc's rand() after srand(seed): the additive feedback generator of random_r (TYPE_3, degree 31,
+// separation 3).  The state starts from seed by r_i = 16807 r_{i-1} mod (2^31 - 1) (Schrage's method),
+// i = 1..30, repeats r_0..r_2 as r_31..r_33, then runs r_i = r_{i-31} + r_{i-3} (mod 2^32); the first 310
+// values are discarded and each later value gives r_i >> 1.
+struct GlibcRand {
+  std::vector<unsigned> r;
+  size_t k = 0;
+  explicit GlibcRand(unsigned seed)
+  {
+    if (seed == 0) seed = 1;
+    r.resize(34);
+    r[0] = seed;
+    for (int i = 1; i < 31; i++) {
+      const long hi = (long)(int)r[i - 1] / 127773, lo = (long)(int)r[i - 1] % 127773;
+      long word = 16807 * lo - 2836 * hi;
+      if (word < 0) word += 2147483647;
+      r[i] = (unsigned)word;
+    }
+    for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+    for (int i = 34; i < 344; i++) r.push_back(r[i - 31] + r[i - 3]);
+    k = r.size();
+  }
+  int next()
+  {
+    const unsigned v = r[k - 31] + r[k - 3];
+    r.push_back(v);
+    k++;
+    return (int)(v >> 1);
+  }
+};
+
+// Rough_precalc[type][100][100] of src/dft_setup_params.c:303-331 (irand = rand() % (2^31 - 1))
+std::vector<double> rough_tables(const tgpu_surface_spec *s)
+{
+  std::vector<double> out((size_t)std::max(s->ntypes, 1) * kRoughBlocks * kRoughBlocks, 0.0);
+  bool any = false;
+  for (int t = 0; t < s->ntypes; t++) any |= s->type[t].rough != 0;
+  if (!any) return out;
+  GlibcRand g(135649u);
+  const int range = 2147483647;
+  for (int t = 0; t < s->ntypes; t++)
+    for (int i = 0; i < kRoughBlocks * kRoughBlocks; i++) {
+      const int irand = g.next() % range;
+      out[(size_t)t * kRoughBlocks * kRoughBlocks + i] = s->type[t].rough_max * (-0.5 + ((double)irand) / ((double)range));
+    }
+  return out;
+}
+
 void fill_rules(Rules &R)
 {
   tgpu::gauss_rule01(6, R.g6x, R.g6w);
@@ -993,15 +1182,21 @@ int surface_field(const tgpu_surface_spec *s, double *d_vext, signed char *d_zer
     for (void *p : owned) cudaFree(p);
   };
   unsigned short *wall_el = d_wall_el ? d_wall_el : dev_alloc<unsigned short>(owned, m.nels);
-  unsigned *touch = dev_alloc<unsigned>(owned, TGPU_SURF_MAXWALLS);
+  unsigned *touch = dev_alloc<unsigned>(owned, TGPU_SURF_MAXWALLS + 1);   // [nwalls] face flags, then the error word
+  unsigned *err = touch ? touch + TGPU_SURF_MAXWALLS : nullptr;
+  const std::vector<double> rtab = rough_tables(s);
+  double *rough = dev_alloc<double>(owned, rtab.size());
   unsigned char *zero0 = dev_alloc<unsigned char>(owned, m.nnodes);
+  tgpu_surface_spec *dspec = dev_alloc<tgpu_surface_spec>(owned, 1);
   Image *dimg = dev_alloc<Image>(owned, img.size());
   int *dfirst = dev_alloc<int>(owned, TGPU_SURF_MAXWALLS), *dcount = dev_alloc<int>(owned, TGPU_SURF_MAXWALLS);
-  if (!wall_el || !touch || !zero0 || !dimg || !dfirst || !dcount) {
+  if (!wall_el || !touch || !zero0 || !dimg || !dfirst || !dcount || !rough || !dspec) {
     release();
     return fail(TGPU_ERR_CUDA, "surface field: device allocation failed");
   }
-  bool ok = cudaMemset(touch, 0, TGPU_SURF_MAXWALLS * sizeof(unsigned)) == cudaSuccess;
+  bool ok = cudaMemset(touch, 0, (TGPU_SURF_MAXWALLS + 1) * sizeof(unsigned)) == cudaSuccess;
+  ok = ok && cudaMemcpy(dspec, s, sizeof(tgpu_surface_spec), cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaMemcpy(rough, rtab.data(), rtab.size() * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess;
   if (!img.empty())
     ok = ok && cudaMemcpy(dimg, img.data(), img.size() * sizeof(Image), cudaMemcpyHostToDevice) == cudaSuccess;
   if (s->nwalls > 0) {
@@ -1046,12 +1241,18 @@ int surface_field(const tgpu_surface_spec *s, double *d_vext, signed char *d_zer
     const int tb = 256;
     const long be = std::min<long>((m.nels + tb - 1) / tb, 152L * 16);
     const long bn = std::min<long>((m.nnodes + tb - 1) / tb, 152L * 16);
-    k_surf_elements<<<(int)be, tb>>>(*s, m, wall_el, touch);
+    k_surf_elements<<<(int)be, tb>>>(dspec, m, rough, wall_el, touch, err);
     k_surf_zero<<<(int)bn, tb>>>(m, s->nwalls, wall_el, touch, zero0);
     const long bw = std::min<long>((m.nnodes + kWarpsPerBlock - 1) / kWarpsPerBlock, 152L * 64);
-    k_vext_integrated<<<(int)bw, 32 * kWarpsPerBlock>>>(*s, m, dimg, dfirst, dcount, tabs, wall_el, zero0, d_vext,
-                                                        d_zero);
+    k_vext_integrated<<<(int)bw, 32 * kWarpsPerBlock>>>(dspec, m, dimg, dfirst, dcount, tabs, rough, err, wall_el,
+                                                        zero0, d_vext, d_zero);
     ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+  }
+  unsigned herr = 0;
+  if (ok) ok = cudaMemcpy(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost) == cudaSuccess;
+  if (ok && herr) {
+    release();
+    return fail(TGPU_ERR_ARG, "surface field: a roughness patch index reaches 100 (MAX_ROUGH_BLOCK)");
   }
   release();
   return ok ? TGPU_OK : fail(TGPU_ERR_CUDA, "surface field: a CUDA call failed");
@@ -1070,6 +1271,14 @@ int tgpu_surface_mesh(const tgpu_surface_spec *s, int *nodes, int *elements)
     nodes[d] = m.nodes[d];
     elements[d] = m.els[d];
   }
+  return TGPU_OK;
+}
+
+int tgpu_surface_rough_table(const tgpu_surface_spec *s, double *out)
+{
+  if (!s || !out || s->ntypes < 0 || s->ntypes > TGPU_SURF_MAXTYPES) return TGPU_ERR_ARG;
+  const std::vector<double> t = rough_tables(s);
+  std::copy(t.begin(), t.begin() + (size_t)s->ntypes * kRoughBlocks * kRoughBlocks, out);
   return TGPU_OK;
 }
 

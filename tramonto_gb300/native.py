@@ -123,6 +123,7 @@ def load(build_if_missing: bool = False):
         "tgpu_grad_epsw": [vp, vp, C.c_int, C.c_int, vp, C.c_double, C.c_int, dp, ip],
         "tgpu_surface_mesh": [vp, ip, ip],
         "tgpu_surface_field_host": [vp, vp, vp, vp], "tgpu_surface_field_device": [vp, vp, vp, vp],
+        "tgpu_surface_rough_table": [vp, vp],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)

@@ -11,8 +11,8 @@ them in the layout build_problem takes.
 The deck is read by the labels of its '@' lines, as the reference's input reader reads fields in
 order (src/dft_input.c): the wall-fluid parameters follow its mixing rules (Lorentz-Berthelot for
 Mix_type 0, src/dft_potential_params.c:120-125; the deck's values for Mix_type 1).  Parts of the
-deck this path does not build (roughness, angle cutouts, Lhard_surf, the charged and Yukawa 1-D wall
-forms, pair potentials other than LJ 12-6, a positive Temp or Length_ref) raise NotImplementedError.
+deck this path does not build (Lhard_surf, the charged and Yukawa 1-D wall forms, pair potentials other
+than LJ 12-6, a positive Temp or Length_ref) raise NotImplementedError.
 """
 from __future__ import annotations
 
@@ -24,7 +24,7 @@ import numpy as np
 
 from . import native
 
-MAXC, MAXWALLS, MAXTYPES, MAXFNC = 4, 16, 4, 4
+MAXC, MAXWALLS, MAXTYPES, MAXFNC = 4, 16, 16, 4
 SURF_PLANAR, SURF_BLOCK, SURF_COLLOID, SURF_FINITE_CYL, SURF_PORE, SURF_FINITE_PORE = 0, 1, 2, 5, 7, 8
 VEXT_NONE, VEXT_HARD, VEXT_DIST_TO_SURF, VEXT_DIST_TO_CENTER, VEXT_INTEGRATED = 0, 1, 2, 3, 5
 WALL1D_LJ93_CS, WALL1D_LJ93_V2_CS, WALL1D_LJ93_NOCS, WALL1D_LJ93_SHIFTX_CS, WALL1D_REPULSIVE9, WALL1D_EXP_ATT = range(6)
@@ -37,6 +37,8 @@ class WallType(C.Structure):
                 ("wavelength", C.c_double * MAXFNC), ("periodic_origin", C.c_double * MAXFNC),
                 ("nlinear", C.c_int), ("linear_orient", C.c_int * MAXFNC), ("slope", C.c_double * MAXFNC),
                 ("linear_origin", C.c_double * MAXFNC), ("linear_end", C.c_double * MAXFNC),
+                ("cutout", C.c_int), ("angle_start", C.c_double), ("angle_end", C.c_double),
+                ("rough", C.c_int), ("rough_max", C.c_double), ("rough_length", C.c_double),
                 ("ipot_wf", C.c_int), ("type_vext", C.c_int), ("pot_id", C.c_int), ("rho_w", C.c_double),
                 ("sigma_wf", C.c_double * MAXC), ("eps_wf", C.c_double * MAXC), ("cut_wf", C.c_double * MAXC)]
 
@@ -90,6 +92,12 @@ def make_spec(ndim, size, esize, bc, ncomp, walls, types, vext_max=10.0, apply_o
         o.nlinear = len(lin)
         for i, (ori, sl, org, end) in enumerate(lin):
             o.linear_orient[i], o.slope[i], o.linear_origin[i], o.linear_end[i] = int(ori), sl, org, end
+        o.cutout = int(T.get("cutout", 0))
+        o.angle_start = float(T.get("angle_start", 0.0))
+        o.angle_end = float(T.get("angle_end", 0.0))
+        o.rough = int(T.get("rough", 0))
+        o.rough_max = float(T.get("rough_max", 0.0))
+        o.rough_length = float(T.get("rough_length", 0.0))
         o.ipot_wf = int(T.get("ipot_wf", VEXT_HARD))
         o.type_vext = int(T.get("type_vext", 1 if o.ipot_wf == VEXT_INTEGRATED else 0))
         o.pot_id = int(T.get("pot_id", 0))
@@ -123,12 +131,18 @@ def surface_field(spec: SurfaceSpec):
 # ---- reading the surface part of a reference input deck ----------------------------------------------
 
 def _deck_fields(text):
-    """[(values, label)] of the '@' lines: values are the leading numeric tokens (n/a as None)."""
+    """[(values, label)] of the '@' records: the text from one '@' to the next (the reference's reader
+    continues a list of values onto the following lines); values are the leading numeric tokens (n/a as
+    None), the label the rest."""
     out = []
+    records = []
     for line in text.splitlines():
-        if not line.startswith("@"):
-            continue
-        toks = line[1:].split()
+        if line.startswith("@"):
+            records.append(line[1:])
+        elif records:
+            records[-1] += " " + line
+    for rec in records:
+        toks = rec.split()
         vals, k = [], 0
         for k, t in enumerate(toks):
             if t.lower() == "n/a":
@@ -156,8 +170,24 @@ class _Deck:
             hits = [v for v, lab in self.fields if lab.startswith(key)]
         if len(hits) != 1:
             raise KeyError(f"deck label {key!r} matched {len(hits)} lines")
-        v = hits[0]
-        return v if n is None else v[:n]
+        return self._take(hits[0], n)
+
+    @staticmethod
+    def _take(v, n):
+        # a line with fewer values than asked for: the reference's reads of the missing ones fail and leave
+        # its zero-initialised arrays unchanged
+        if n is None:
+            return v
+        v = [0.0 if x is None else x for x in v[:n]]
+        return v + [0.0] * (n - len(v))
+
+    def after(self, key, k, n):
+        """the values of the k-th '@' line after the one labelled key: the reference reads these lines in
+        order, and some decks leave them unlabelled"""
+        idx = [i for i, (_, lab) in enumerate(self.fields) if lab.startswith(key)]
+        if len(idx) != 1:
+            raise KeyError(f"deck label {key!r} matched {len(idx)} lines")
+        return self._take(self.fields[idx[0] + k][0], n)
 
 
 def read_deck(input_path, surfaces_path=None):
@@ -183,20 +213,19 @@ def read_deck(input_path, surfaces_path=None):
     p2 = dk.get("WallParam2", ntypes)
     p3 = dk.get("WallParam3", ntypes)
     apply = [int(v) for v in dk.get("Lapply_of", 3)]
-    if any(int(v) for v in dk.get("Lrough_surf", ntypes)):
-        raise NotImplementedError("roughness patches")
+    rough = [int(v) for v in dk.get("Lrough_surf", ntypes)]
+    rough_max = dk.get("rough_param_max", ntypes) if any(rough) else [0.0] * ntypes
+    rough_len = dk.get("Rough_length", ntypes) if any(rough) else [0.0] * ntypes
     nper = [int(v) for v in dk.get("Nperiodic_overlay", ntypes)]
     nlin = [int(v) for v in dk.get("Nlinear_overlay", ntypes)]
-    if any(int(v) for v in dk.get("LangleCutout", ntypes)):
-        raise NotImplementedError("angle cutouts")
+    cutout = [int(v) for v in dk.get("LangleCutout", ntypes)]
+    a_start = dk.get("Angle_start", ntypes) if any(cutout) else [0.0] * ntypes
+    a_end = dk.get("Angle_end", ntypes) if any(cutout) else [0.0] * ntypes
 
     def per_type(key, counts):
         if sum(counts) == 0:
             return [[] for _ in counts]
-        # a line with fewer values than functions: the reference's read of the missing ones fails and
-        # leaves its zero-initialised arrays unchanged
-        vals = list(dk.get(key, sum(counts)))
-        vals += [0.0] * (sum(counts) - len(vals))
+        vals = dk.get(key, sum(counts))
         out, k = [], 0
         for c in counts:
             out.append(vals[k:k + c])
@@ -229,27 +258,30 @@ def read_deck(input_path, surfaces_path=None):
     sff_all = dk.get("Sigma_ff", nff)
     sigma_ff = [sff_all[i] if mix == 0 else sff_all[i * ncomp + i] for i in range(ncomp)]
     rho_w = dk.get("Rho_w", ntypes)
+    # after Rho_w: Sigma_ww, Eps_ww, Cut_ww, EpsYukawa_ww, YukawaK_ww, Sigma_wf, Eps_wf, Cut_wf (src/dft_input.c)
     if mix == 0:
         sff = dk.get("Sigma_ff", nff)
         eff = dk.get("Eps_ff", nff)
         cff = dk.get("Cut_ff", nff)
-        sww = dk.get("Sigma_ww", nww)
-        eww = dk.get("Eps_ww", nww)
-        cww = dk.get("Cut_ww", nww)
+        sww = dk.after("Rho_w", 1, nww)
+        eww = dk.after("Rho_w", 2, nww)
+        cww = dk.after("Rho_w", 3, nww)
         # Lorentz-Berthelot (src/dft_potential_params.c:120-125)
         swf = [[0.5 * (sff[i] + sww[t]) for i in range(ncomp)] for t in range(ntypes)]
         ewf = [[math.sqrt(eff[i] * eww[t]) for i in range(ncomp)] for t in range(ntypes)]
         cwf = [[0.5 * (cff[i] + cww[t]) for i in range(ncomp)] for t in range(ntypes)]
     else:
         nwf = ncomp * ntypes
-        s_in, e_in, c_in = dk.get("Sigma_wf", nwf), dk.get("Eps_wf", nwf), dk.get("Cut_wf", nwf)
+        s_in, e_in, c_in = dk.after("Rho_w", 6, nwf), dk.after("Rho_w", 7, nwf), dk.after("Rho_w", 8, nwf)
         swf = [[s_in[i * ntypes + t] for i in range(ncomp)] for t in range(ntypes)]
         ewf = [[e_in[i * ntypes + t] for i in range(ncomp)] for t in range(ntypes)]
         cwf = [[c_in[i * ntypes + t] for i in range(ncomp)] for t in range(ntypes)]
     types = []
     for t in range(ntypes):
         types.append(dict(surf_type=surf[t], orientation=orient[t], param=(p1[t], p2[t], p3[t]), ipot_wf=ipot[t],
-                          type_vext=tvext[t], pot_id=potid[t], rho_w=rho_w[t],
+                          type_vext=tvext[t], pot_id=potid[t], rho_w=rho_w[t], rough=rough[t],
+                          cutout=cutout[t], angle_start=a_start[t], angle_end=a_end[t],
+                          rough_max=rough_max[t], rough_length=rough_len[t],
                           sigma_wf=swf[t], eps_wf=ewf[t], cut_wf=cwf[t],
                           periodic=[(int(p_or[t][i]), p_amp[t][i], p_wl[t][i], p_org[t][i]) for i in range(nper[t])],
                           linear=[(int(l_or[t][i]), l_sl[t][i], l_org[t][i], l_end[t][i]) for i in range(nlin[t])]))
@@ -269,6 +301,14 @@ def read_deck(input_path, surfaces_path=None):
                      sigma_ff=sigma_ff)
 
 
+def rough_table(spec: SurfaceSpec):
+    """The roughness patch heights [ntypes][100][100] the builder uses (Rough_precalc)."""
+    out = np.zeros((max(spec.ntypes, 1), 100, 100))
+    lib = native.load()
+    native._check(lib.tgpu_surface_rough_table(C.byref(spec), out.ctypes.data), lib)
+    return out[:spec.ntypes]
+
+
 def problem_fields(spec: SurfaceSpec):
     """(vext, zero_density) for build_problem: V_ext/kT [ncomp][nodes] and int8 flags."""
     vext, zero, _ = surface_field(spec)
@@ -285,9 +325,11 @@ def spec_arrays(spec: SurfaceSpec) -> dict:
          "wall_type": np.array(spec.wall_type[:nw], np.int32),
          "wall_pos": np.array([spec.wall_pos[w][:] for w in range(nw)]).reshape(nw, 3)}
     a["sigma_ff"] = np.array(spec.sigma_ff[:])
-    for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf", "type_vext", "pot_id"):
+    for f in ("surf_type", "orientation", "nperiodic", "nlinear", "ipot_wf", "type_vext", "pot_id", "rough",
+              "cutout"):
         a["t_" + f] = np.array([getattr(spec.type[t], f) for t in range(nt)], np.int32)
-    a["t_rho_w"] = np.array([spec.type[t].rho_w for t in range(nt)])
+    for f in ("rho_w", "rough_max", "rough_length", "angle_start", "angle_end"):
+        a["t_" + f] = np.array([getattr(spec.type[t], f) for t in range(nt)])
     for f in ("periodic_orient", "linear_orient"):
         a["t_" + f] = np.array([getattr(spec.type[t], f)[:] for t in range(nt)], np.int32).reshape(nt, MAXFNC)
     for f, n in (("param", 3), ("amplitude", MAXFNC), ("wavelength", MAXFNC), ("periodic_origin", MAXFNC),
@@ -316,6 +358,12 @@ def spec_from_arrays(a) -> SurfaceSpec:
         o.type_vext = int(a["t_type_vext"][t]) if "t_type_vext" in a else 1
         o.pot_id = int(a["t_pot_id"][t]) if "t_pot_id" in a else 0
         o.rho_w = float(a["t_rho_w"][t]) if "t_rho_w" in a else 1.0
+        o.cutout = int(a["t_cutout"][t]) if "t_cutout" in a else 0
+        o.angle_start = float(a["t_angle_start"][t]) if "t_angle_start" in a else 0.0
+        o.angle_end = float(a["t_angle_end"][t]) if "t_angle_end" in a else 0.0
+        o.rough = int(a["t_rough"][t]) if "t_rough" in a else 0
+        o.rough_max = float(a["t_rough_max"][t]) if "t_rough_max" in a else 0.0
+        o.rough_length = float(a["t_rough_length"][t]) if "t_rough_length" in a else 0.0
         for f in ("periodic_orient", "linear_orient", "param", "amplitude", "wavelength", "periodic_origin", "slope",
                   "linear_origin", "linear_end", "sigma_wf", "eps_wf", "cut_wf"):
             arr = getattr(o, f)
