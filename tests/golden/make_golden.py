@@ -129,6 +129,15 @@ def cases():
     # zone coarser than the residual near the wall)
     c["hs1d_zones"] = deck("HS6_FMT1_1D")
     c["hs1d_jaczones"] = deck("HS7_FMT1_1D")
+    # MIX1's hard wall (boundary weights, one surface list per component size) with three and four hard-sphere
+    # components of different diameters (FMT1, and FMT3 for the four)
+    mix = {"Mass[i]": "1. 1. 1. 1.", "Charge[i]": "0. 0. 0. 0.", "Pol[i]": "0. 0. 0. 0.",
+           "Eps_ff[i][j]": "0. 0. 0. 0.", "Cut_ff[i][j]": "0. 0. 0. 0.", "Bond_ff[i][j]": "1. 1. 1. 1."}
+    c["mix3_hw1d"] = deck("MIX1_FMT1_1D", dict(mix, **{"Ncomp Mix_type": "3 0", "Sigma_ff[i][j]": "1. 0.8 0.6",
+                                                      "Rho_b_0[icomp]": "0.25 0.2 0.3"}))
+    c["mix4_hw1d_fmt3"] = deck("MIX1_FMT1_1D", dict(mix, **{"Type_func (": "2 0", "Ncomp Mix_type": "4 0",
+                                                           "Sigma_ff[i][j]": "1. 0.85 0.7 0.55",
+                                                           "Rho_b_0[icomp]": "0.15 0.15 0.2 0.2"}))
     return c
 
 

@@ -10,7 +10,7 @@ GOLDEN = os.path.join(HERE, "golden")
 CASES = ["hs1d_wall", "hs1d_reflect", "lj1d_mf", "mix1d_fmt3", "fmt1_wca_3d", "hs1d_c1",
          "hs1d_fmt2", "hs1d_fmt4", "mix1d_fmt4", "rough3d_fmt2", "rough3d_fmt4",
          "lj1d_sigzero", "lj1d_jdc", "yuk1d_mf", "exp1d_mf", "sw1d_mf", "hslj1d_wall", "lj1d_a22",
-         "lv1d_interface", "lv1d_bulkbc", "hs1d_zones", "hs1d_jaczones"]
+         "lv1d_interface", "lv1d_bulkbc", "hs1d_zones", "hs1d_jaczones", "mix3_hw1d", "mix4_hw1d_fmt3"]
 
 # The reference fills in IEEE FP64 with its own summation order; any other
 # order differs by rounding.  Residual entries are compared with an absolute

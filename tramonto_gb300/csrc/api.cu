@@ -2249,7 +2249,6 @@ int tgpu_create(const tgpu_geometry *geom, int device, tgpu_handle *out)
     if (g.pin && g.interface != 2) throw Error(TGPU_ERR_ARG, "a pinned density needs a phase interface");
     if (g.functional < TGPU_FMT1 || g.functional > TGPU_FMT4)
       throw Error(TGPU_ERR_UNSUPPORTED, "functional outside FMT1..FMT4");
-    if (g.hard_surf && g.ncomp > 2) throw Error(TGPU_ERR_UNSUPPORTED, "hard walls with more than two components");
     const long N = nnodes(g);
     if (N > (1L << 31) / 4) throw Error(TGPU_ERR_ARG, "mesh too large for 32-bit stencil offsets");
     ck(cudaSetDevice(device), "cudaSetDevice");

@@ -1257,10 +1257,10 @@ struct HwStencil {
   const double *w, *hw;
 };
 
-// The hard-wall stencils of up to two components: theta and delta per component, the mean-field
-// stencils per (output component, input component) pair
+// The hard-wall stencils: theta and delta per component, the mean-field stencils per (output component,
+// input component) pair (ua[ic + kMaxC jc])
 struct HwSet {
-  HwStencil th[2], de[2], ua[4];
+  HwStencil th[kMaxC], de[kMaxC], ua[kMaxC * kMaxC];
 };
 
 // kind 0: theta -> n3; 1: delta -> n2 [n1 n0] V2 [V1]; 2: mean field -> row orow (no prefactor)
@@ -1318,34 +1318,34 @@ __global__ void k_hw_correct(const double *__restrict__ field, long fcs, int ffi
   const int nc = c_g.ncomp;
   double acc[kMaxRb + kMaxC];
   for (int k = 0; k < kMaxRb + kMaxC; k++) acc[k] = 0.0;
-  for (int jc = 0; jc < nc && jc < 2; jc++) {
+  for (int jc = 0; jc < nc; jc++) {
     const int jlist = (c_g.nlists <= 2) ? 0 : jc;
     if (do_fmt) {
       hw_apply(hs.th[jc], 0, 0, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
       hw_apply(hs.de[jc], 1, 0, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
     }
     if (do_mf)
-      for (int ic = 0; ic < nc && ic < 2; ic++)
-        hw_apply(hs.ua[ic + 2 * jc], 2, c_g.nrb + ic, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
+      for (int ic = 0; ic < nc; ic++)
+        hw_apply(hs.ua[ic + kMaxC * jc], 2, c_g.nrb + ic, jc, jlist, ijk, field, fcs, ffirst, zero, bnodes, fmask, acc);
   }
   if (do_fmt)
     for (int k = 0; k < c_g.nrb; k++) conv[(long)k * c_g.N + i] += acc[k];
   if (do_mf)
-    for (int ic = 0; ic < nc && ic < 2; ic++) conv[(long)(c_g.nrb + ic) * c_g.N + i] += acc[c_g.nrb + ic];
+    for (int ic = 0; ic < nc; ic++) conv[(long)(c_g.nrb + ic) * c_g.N + i] += acc[c_g.nrb + ic];
 }
 
 static HwSet hw_set(const DevStencil *theta, const DevStencil *delta, const DevStencil *uatt, int ncomp)
 {
   HwSet h{};
-  for (int c = 0; c < 2 && c < ncomp; c++) {
+  for (int c = 0; c < kMaxC && c < ncomp; c++) {
     if (theta && theta[c].L) h.th[c] = {theta[c].L, theta[c].d_off, theta[c].d_w, theta[c].d_hw};
     if (delta && delta[c].L) h.de[c] = {delta[c].L, delta[c].d_off, delta[c].d_w, delta[c].d_hw};
   }
   if (uatt)
-    for (int jc = 0; jc < 2 && jc < ncomp; jc++)
-      for (int ic = 0; ic < 2 && ic < ncomp; ic++) {
+    for (int jc = 0; jc < kMaxC && jc < ncomp; jc++)
+      for (int ic = 0; ic < kMaxC && ic < ncomp; ic++) {
         const DevStencil &u = uatt[ic + ncomp * jc];
-        if (u.L && u.d_hw) h.ua[ic + 2 * jc] = {u.L, u.d_off, u.d_w, u.d_hw};
+        if (u.L && u.d_hw) h.ua[ic + kMaxC * jc] = {u.L, u.d_off, u.d_w, u.d_hw};
       }
   return h;
 }
@@ -1477,7 +1477,7 @@ __global__ void k_hw_correct_t(const double *__restrict__ w, const double *__res
   int ijk[3];
   node_ijk(i, ijk);
   const int nc = c_g.ncomp;
-  for (int jc = 0; jc < nc && jc < 2; jc++) {
+  for (int jc = 0; jc < nc; jc++) {
     const int jlist = (c_g.nlists <= 2) ? 0 : jc;
     if (do_fmt) {
       const double *W = w + (long)c_g.first_rb * N + i;   // adjoint rb rows at i, N apart
@@ -1485,8 +1485,8 @@ __global__ void k_hw_correct_t(const double *__restrict__ w, const double *__res
       hw_apply_t(hs.de[jc], 1, jc, jlist, ijk, W, zero, bnodes, fmask, out);
     }
     if (do_mf)
-      for (int ic = 0; ic < nc && ic < 2; ic++)
-        hw_apply_t(hs.ua[ic + 2 * jc], 2, jc, jlist, ijk, mfw + (long)ic * N + i, zero, bnodes, fmask, out);
+      for (int ic = 0; ic < nc; ic++)
+        hw_apply_t(hs.ua[ic + kMaxC * jc], 2, jc, jlist, ijk, mfw + (long)ic * N + i, zero, bnodes, fmask, out);
   }
 }
 
