@@ -485,7 +485,15 @@ void fft_tr_sum(Ctx *c, const int *chs, const C *const *kern, int n, double *out
   std::vector<C *> &boxes = tr_boxes<C>(c);
   while ((int)boxes.size() < n) boxes.push_back(dalloc<C>((size_t)c->fft.NH));
   std::vector<const C *> a(n);
-  for (int t = 0; t < n; t++) a[t] = channel_into(c, chs[t], boxes[t]);
+  if constexpr (std::is_same<C, float2>::value) {   // the channels' spectra in one launch per pass
+    std::vector<tgpu::MapSrc> ms(n);
+    for (int t = 0; t < n; t++) ms[t] = map_src(c, chs[t]);
+    tgpu::rfft_forward_mapped_batch(ms.data(), n, boxes.data(), c->fft, c->stream);
+    c->stats.kernel_launches += 3;
+    for (int t = 0; t < n; t++) a[t] = boxes[t];
+  } else {
+    for (int t = 0; t < n; t++) a[t] = channel_into(c, chs[t], boxes[t]);
+  }
   C *work = std::is_same<C, float2>::value ? (C *)c->d_fbox32[2] : (C *)c->d_fbox[2];
   tgpu::rfft_inverse_products(a.data(), kern, n, work, c->fft, 1.0 / (double)c->fft.NR, out, true, c->stream);
   c->stats.kernel_launches += 3;
@@ -500,10 +508,18 @@ void fft_conv_impl(Ctx *c, int ch0, int nin, const std::vector<C *> &spec, bool 
 {
   if (!tr) {
     const C *F = channel(c, ch0);
-    for (int q = 0; q < nout; q++) {
-      const C *a[1] = {F}, *k[1] = {spec[q]};
-      tgpu::rfft_inverse_products(a, k, 1, fbox[1], c->fft, 1.0 / (double)c->fft.NR, outs[q], true, c->stream);
+    if constexpr (std::is_same<C, float2>::value) {   // every output in one launch per pass
+      std::vector<C *> &work = tr_boxes<C>(c);
+      while ((int)work.size() < nout) work.push_back(dalloc<C>((size_t)c->fft.NH));
+      tgpu::rfft_inverse_batch(F, spec.data(), nout, work.data(), c->fft, 1.0 / (double)c->fft.NR, outs, true,
+                               c->stream);
       c->stats.kernel_launches += 3;
+    } else {
+      for (int q = 0; q < nout; q++) {
+        const C *a[1] = {F}, *k[1] = {spec[q]};
+        tgpu::rfft_inverse_products(a, k, 1, fbox[1], c->fft, 1.0 / (double)c->fft.NR, outs[q], true, c->stream);
+        c->stats.kernel_launches += 3;
+      }
     }
     c->stats.conv_launches++;
   } else {
