@@ -724,7 +724,6 @@ void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, boo
   const int nd = g.ndim;
   for (int jc = 0; jc < g.ncomp; jc++) {
     double *o_th[1] = {out};
-    conv(c, jc, 1, sten[TGPU_STEN_THETA][jc], false, o_th, 1, f32);
     std::vector<double *> o_de;
     o_de.push_back(out + 1 * N);
     if (!g.single_size) {
@@ -734,6 +733,37 @@ void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, boo
     for (int d = 0; d < nd; d++) o_de.push_back(out + (long)(4 + d) * N);
     if (!g.single_size)
       for (int d = 0; d < nd; d++) o_de.push_back(out + (long)(4 + nd + d) * N);
+    // every sum of this density by FP32 FFT: all their inverse transforms in one launch per pass
+    if (f32 && sten == c->sten && c->spec32_built) {
+      const DevStencil &sth = sten[TGPU_STEN_THETA][jc], &sde = sten[TGPU_STEN_DELTA][jc];
+      bool all = use_fft32(c, sth, false, 1, 1) && use_fft32(c, sde, false, 1, (int)o_de.size());
+      if (g.attraction)
+        for (int ic = 0; ic < g.ncomp; ic++) all = all && use_fft32(c, sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, 1, 1);
+      if (all) {
+        std::vector<const float2 *> ks;
+        std::vector<double *> os;
+        ks.push_back(sth.spec_fwd32[0]);
+        os.push_back(out);
+        for (size_t q = 0; q < o_de.size(); q++) {
+          ks.push_back(sde.spec_fwd32[q]);
+          os.push_back(o_de[q]);
+        }
+        if (g.attraction)
+          for (int ic = 0; ic < g.ncomp; ic++) {
+            ks.push_back(sten[TGPU_STEN_UATT][ic + g.ncomp * jc].spec_fwd32[0]);
+            os.push_back(out + (long)(g.nrb + ic) * N);
+          }
+        const float2 *F = fft_channel32(c, jc);
+        std::vector<float2 *> &work = tr_boxes<float2>(c);
+        while (work.size() < ks.size()) work.push_back(dalloc<float2>((size_t)c->fft.NH));
+        tgpu::rfft_inverse_batch(F, ks.data(), (int)ks.size(), work.data(), c->fft, 1.0 / (double)c->fft.NR,
+                                 os.data(), true, c->stream);
+        c->stats.kernel_launches += 3 * ((ks.size() + tgpu::fft_max_batch() - 1) / tgpu::fft_max_batch());
+        c->stats.conv_launches++;
+        continue;
+      }
+    }
+    conv(c, jc, 1, sten[TGPU_STEN_THETA][jc], false, o_th, 1, f32);
     conv(c, jc, 1, sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), f32);
     if (g.attraction)
       for (int ic = 0; ic < g.ncomp; ic++) {
