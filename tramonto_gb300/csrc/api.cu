@@ -485,14 +485,12 @@ void fft_tr_sum(Ctx *c, const int *chs, const C *const *kern, int n, double *out
   std::vector<C *> &boxes = tr_boxes<C>(c);
   while ((int)boxes.size() < n) boxes.push_back(dalloc<C>((size_t)c->fft.NH));
   std::vector<const C *> a(n);
-  if constexpr (std::is_same<C, float2>::value) {   // the channels' spectra in one launch per pass
+  {   // the channels' spectra in one launch per pass
     std::vector<tgpu::MapSrc> ms(n);
     for (int t = 0; t < n; t++) ms[t] = map_src(c, chs[t]);
     tgpu::rfft_forward_mapped_batch(ms.data(), n, boxes.data(), c->fft, c->stream);
     c->stats.kernel_launches += 3;
     for (int t = 0; t < n; t++) a[t] = boxes[t];
-  } else {
-    for (int t = 0; t < n; t++) a[t] = channel_into(c, chs[t], boxes[t]);
   }
   C *work = std::is_same<C, float2>::value ? (C *)c->d_fbox32[2] : (C *)c->d_fbox[2];
   tgpu::rfft_inverse_products(a.data(), kern, n, work, c->fft, 1.0 / (double)c->fft.NR, out, true, c->stream);
@@ -508,18 +506,12 @@ void fft_conv_impl(Ctx *c, int ch0, int nin, const std::vector<C *> &spec, bool 
 {
   if (!tr) {
     const C *F = channel(c, ch0);
-    if constexpr (std::is_same<C, float2>::value) {   // every output in one launch per pass
+    {   // every output in one launch per pass
       std::vector<C *> &work = tr_boxes<C>(c);
       while ((int)work.size() < nout) work.push_back(dalloc<C>((size_t)c->fft.NH));
       tgpu::rfft_inverse_batch(F, spec.data(), nout, work.data(), c->fft, 1.0 / (double)c->fft.NR, outs, true,
                                c->stream);
       c->stats.kernel_launches += 3;
-    } else {
-      for (int q = 0; q < nout; q++) {
-        const C *a[1] = {F}, *k[1] = {spec[q]};
-        tgpu::rfft_inverse_products(a, k, 1, fbox[1], c->fft, 1.0 / (double)c->fft.NR, outs[q], true, c->stream);
-        c->stats.kernel_launches += 3;
-      }
     }
     c->stats.conv_launches++;
   } else {
@@ -733,7 +725,37 @@ void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, boo
     for (int d = 0; d < nd; d++) o_de.push_back(out + (long)(4 + d) * N);
     if (!g.single_size)
       for (int d = 0; d < nd; d++) o_de.push_back(out + (long)(4 + nd + d) * N);
-    // every sum of this density by FP32 FFT: all their inverse transforms in one launch per pass
+    // every sum of this density by FFT (FP64 accurate fills, or FP32): all their inverse transforms in one launch
+    // per pass
+    if (!f32 && sten == c->sten && c->fft_on && c->fft_state == 1) {
+      const DevStencil &sth = sten[TGPU_STEN_THETA][jc], &sde = sten[TGPU_STEN_DELTA][jc];
+      bool all = sth.spec_fwd.size() == 1 && sde.spec_fwd.size() == o_de.size();
+      if (g.attraction)
+        for (int ic = 0; ic < g.ncomp; ic++) all = all && sten[TGPU_STEN_UATT][ic + g.ncomp * jc].spec_fwd.size() == 1;
+      if (all) {
+        std::vector<const double2 *> ks;
+        std::vector<double *> os;
+        ks.push_back(sth.spec_fwd[0]);
+        os.push_back(out);
+        for (size_t q = 0; q < o_de.size(); q++) {
+          ks.push_back(sde.spec_fwd[q]);
+          os.push_back(o_de[q]);
+        }
+        if (g.attraction)
+          for (int ic = 0; ic < g.ncomp; ic++) {
+            ks.push_back(sten[TGPU_STEN_UATT][ic + g.ncomp * jc].spec_fwd[0]);
+            os.push_back(out + (long)(g.nrb + ic) * N);
+          }
+        const double2 *F = fft_channel(c, jc);
+        std::vector<double2 *> &work = tr_boxes<double2>(c);
+        while (work.size() < ks.size()) work.push_back(dalloc<double2>((size_t)c->fft.NH));
+        tgpu::rfft_inverse_batch(F, ks.data(), (int)ks.size(), work.data(), c->fft, 1.0 / (double)c->fft.NR,
+                                 os.data(), true, c->stream);
+        c->stats.kernel_launches += 3 * ((ks.size() + tgpu::fft_max_batch() - 1) / tgpu::fft_max_batch());
+        c->stats.conv_launches++;
+        continue;
+      }
+    }
     if (f32 && sten == c->sten && c->spec32_built) {
       const DevStencil &sth = sten[TGPU_STEN_THETA][jc], &sde = sten[TGPU_STEN_DELTA][jc];
       bool all = use_fft32(c, sth, false, 1, 1) && use_fft32(c, sde, false, 1, (int)o_de.size());

@@ -236,11 +236,43 @@ struct MappedSrc {   // the unpadded channel through the boundary maps (the padd
   }
 };
 
+// spectral products formed by a pass as it loads its lines: value = sum_t a_t * k_t (n = 0: the input itself)
+constexpr int kMaxTerms = 6;
+template <class C>
+struct Terms {
+  const C *a[kMaxTerms];
+  const C *k[kMaxTerms];
+  int n;
+};
+
+// up to kMaxBatch transforms of one plan in one launch (blockIdx.y selects the transform)
+constexpr int kMaxBatch = 8;
+template <class C>
+struct PassBatch {
+  const C *in[kMaxBatch];
+  C *out[kMaxBatch];
+  Terms<C> terms[kMaxBatch];
+};
+
+template <class Src, class C>
+struct SrcBatch {
+  Src src[kMaxBatch];
+  C *spec[kMaxBatch];
+};
+
+template <class C>
+struct OutBatch {
+  const C *spec[kMaxBatch];
+  double *out[kMaxBatch];
+};
+
 // x pass of the forward transform: two real lines per complex line, split into two half-spectrum lines
 template <class T, class C, class Src>
-__global__ void __launch_bounds__(kFftThreads) k_rfft_x(Src src, XGeom g, Stages st, const C *__restrict__ tw_g,
-                                                      C *__restrict__ spec)
+__global__ void __launch_bounds__(kFftThreads) k_rfft_x(SrcBatch<Src, C> sb, XGeom g, Stages st,
+                                                      const C *__restrict__ tw_g)
 {
+  const Src &src = sb.src[blockIdx.y];
+  C *__restrict__ spec = sb.spec[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
   const int n = g.F0, ls = n + 1;
@@ -276,10 +308,11 @@ __global__ void __launch_bounds__(kFftThreads) k_rfft_x(Src src, XGeom g, Stages
 // x pass of the inverse transform: two half-spectrum lines as one complex line, written out as the real outputs
 // of the interior nodes (out[node] = scale * value, or += when accumulate)
 template <class C>
-__global__ void __launch_bounds__(kFftThreads) k_irfft_x(const C *__restrict__ spec, XGeom g, Stages st,
-                                                       const C *__restrict__ tw_g, double scale,
-                                                       double *__restrict__ out, int accumulate)
+__global__ void __launch_bounds__(kFftThreads) k_irfft_x(OutBatch<C> ob, XGeom g, Stages st,
+                                                       const C *__restrict__ tw_g, double scale, int accumulate)
 {
+  const C *__restrict__ spec = ob.spec[blockIdx.y];
+  double *__restrict__ out = ob.out[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
   const int n = g.F0, ls = n + 1;
@@ -315,31 +348,16 @@ __global__ void __launch_bounds__(kFftThreads) k_irfft_x(const C *__restrict__ s
   }
 }
 
-// spectral products formed by a pass as it loads its lines: value = sum_t a_t * k_t (n = 0: the input itself)
-constexpr int kMaxTerms = 6;
-template <class C>
-struct Terms {
-  const C *a[kMaxTerms];
-  const C *k[kMaxTerms];
-  int n;
-};
-
-// up to kMaxBatch transforms of one plan in one launch (blockIdx.y selects the transform)
-constexpr int kMaxBatch = 8;
-template <class C>
-struct PassBatch {
-  const C *in[kMaxBatch];
-  C *out[kMaxBatch];
-  Terms<C> terms[kMaxBatch];
-};
-
 // y and z passes: lines of element stride es; a CTA takes kFftLines consecutive x at one (outer) index; reads `in`
 // (or the products of `terms`) and writes `out` (in place when out == in)
 template <class C>
-__global__ void __launch_bounds__(kFftThreads) k_fft_strided(const C *in, C *out, Terms<C> terms, int X, int n,
-                                                           long es, long outer_stride, Stages st,
-                                                           const C *__restrict__ tw_g, int inv)
+__global__ void __launch_bounds__(kFftThreads) k_fft_strided(PassBatch<C> pb, int X, int n, long es,
+                                                           long outer_stride, Stages st, const C *__restrict__ tw_g,
+                                                           int inv)
 {
+  const C *in = pb.in[blockIdx.y];
+  C *out = pb.out[blockIdx.y];
+  const Terms<C> &terms = pb.terms[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
   const int ls = n + 1;
@@ -422,12 +440,6 @@ __device__ __forceinline__ C *warp_fft(C *b0, C *b1, int n, const Stages &st, co
 }
 
 // forward x pass: each warp packs two real lines into one complex line, transforms it and splits it
-template <class Src, class C>
-struct SrcBatch {
-  Src src[kMaxBatch];
-  C *spec[kMaxBatch];
-};
-
 template <class T, class C, class Src>
 __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, XGeom g, Stages st,
                                                         const C *__restrict__ tw_g)
@@ -467,12 +479,6 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
 
 // inverse x pass: each warp packs two half-spectrum lines into one complex line and writes the real and
 // imaginary parts of its inverse as the outputs of the interior nodes
-template <class C>
-struct OutBatch {
-  const C *spec[kMaxBatch];
-  double *out[kMaxBatch];
-};
-
 template <class C>
 __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom g, Stages st,
                                                          const C *__restrict__ tw_g, double scale, int accumulate)
@@ -669,17 +675,25 @@ XGeom xgeom(const FftPlan &p)
   return g;
 }
 
-// one y (d = 1) or z (d = 2) pass of nb FP32 transforms of the plan in one launch
-void strided_pass_batch(const PassBatch<float2> &pb, int nb, const FftPlan &p, int d, bool inverse, const float2 *tw,
+// one y (d = 1) or z (d = 2) pass of nb transforms of the plan in one launch: FP32 one warp per line, FP64 the
+// block tile
+template <class C>
+void strided_pass_batch(const PassBatch<C> &pb, int nb, const FftPlan &p, int d, bool inverse, const C *tw,
                         cudaStream_t s)
 {
   const int X = p.Fh, n = p.F[d];
   const long es = d == 1 ? (long)X : (long)X * p.F[1];
   const long outer = d == 1 ? (long)X * p.F[1] : (long)X;   // axis 1: outer index z; axis 2: outer index y
   const long nouter = d == 1 ? p.F[2] : p.F[1];
-  const int xb = (X + kWLines - 1) / kWLines;
-  k_fft_stridedw<float2><<<dim3((unsigned)(xb * nouter), (unsigned)nb), 32 * kWLines, wtile_smem(n), s>>>(
-      pb, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+  if constexpr (std::is_same<C, float2>::value) {
+    const int xb = (X + kWLines - 1) / kWLines;
+    k_fft_stridedw<float2><<<dim3((unsigned)(xb * nouter), (unsigned)nb), 32 * kWLines, wtile_smem(n), s>>>(
+        pb, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+  } else {
+    const int xblocks = (X + kFftLines - 1) / kFftLines;
+    k_fft_strided<C><<<dim3((unsigned)(xblocks * nouter), (unsigned)nb), kFftThreads, tile_smem<C>(n), s>>>(
+        pb, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+  }
 }
 
 // one y (d = 1) or z (d = 2) pass over the half-spectrum box
@@ -687,21 +701,11 @@ template <class C>
 void strided_pass(const C *in, C *out, const Terms<C> &terms, const FftPlan &p, int d, bool inverse, const C *tw,
                   cudaStream_t s)
 {
-  const int X = p.Fh, n = p.F[d];
-  const int xblocks = (X + kFftLines - 1) / kFftLines;
-  const long es = d == 1 ? (long)X : (long)X * p.F[1];
-  const long outer = d == 1 ? (long)X * p.F[1] : (long)X;   // axis 1: outer index z; axis 2: outer index y
-  const long nouter = d == 1 ? p.F[2] : p.F[1];
-  if constexpr (std::is_same<C, float2>::value) {
-    PassBatch<float2> pb{};
-    pb.in[0] = in;
-    pb.out[0] = out;
-    pb.terms[0] = terms;
-    strided_pass_batch(pb, 1, p, d, inverse, tw, s);
-  } else {
-    k_fft_strided<C><<<(unsigned)(xblocks * nouter), kFftThreads, tile_smem<C>(n), s>>>(
-        in, out, terms, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
-  }
+  PassBatch<C> pb{};
+  pb.in[0] = in;
+  pb.out[0] = out;
+  pb.terms[0] = terms;
+  strided_pass_batch<C>(pb, 1, p, d, inverse, tw, s);
 }
 
 template <class T, class C, class Src>
@@ -720,9 +724,13 @@ void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, c
     sb.spec[0] = spec;
     k_rfft_xw<T, C, Src><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
         sb, g, stages(p.ax[0]), tw[0]);
-  } else
+  } else {
+    SrcBatch<Src, C> sb{};
+    sb.src[0] = src;
+    sb.spec[0] = spec;
     k_rfft_x<T, C, Src><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
-        src, g, stages(p.ax[0]), tw[0], spec);
+        sb, g, stages(p.ax[0]), tw[0]);
+  }
   const Terms<C> none{};
   for (int d = 1; d <= 2; d++)
     if (p.F[d] > 1) strided_pass<C>(spec, spec, none, p, d, false, tw[d], s);
@@ -749,39 +757,48 @@ void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double 
     ob.out[0] = out;
     k_irfft_xw<C><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
         ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
-  } else
+  } else {
+    OutBatch<C> ob{};
+    ob.spec[0] = spec;
+    ob.out[0] = out;
     k_irfft_x<C><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
-        spec, g, stages(p.ax[0]), tw[0], scale, out, accumulate ? 1 : 0);
+        ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+  }
 }
 
-// nb forward transforms of mapped channels in one launch per pass (FP32)
-void rfft_forward_mapped_batch_impl(const MapSrc *m, int nb, float2 *const *spec, const FftPlan &p, cudaStream_t s)
+// nb forward transforms of mapped channels in one launch per pass
+template <class T, class C>
+void rfft_forward_mapped_batch_impl(const MapSrc *m, int nb, C *const *spec, const FftPlan &p, const C *const *tw,
+                                    cudaStream_t s)
 {
   const XGeom g = xgeom(p);
   const long npairs = (g.nlines + 1) / 2;
-  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
-  SrcBatch<MappedSrc<float>, float2> sb{};
-  PassBatch<float2> pb{};
+  SrcBatch<MappedSrc<T>, C> sb{};
+  PassBatch<C> pb{};
   for (int b = 0; b < nb; b++) {
-    sb.src[b] = MappedSrc<float>{m[b]};
+    sb.src[b] = MappedSrc<T>{m[b]};
     sb.spec[b] = spec[b];
     pb.in[b] = spec[b];
     pb.out[b] = spec[b];
   }
-  k_rfft_xw<float, float2, MappedSrc<float>>
-      <<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
-          sb, g, stages(p.ax[0]), tw[0]);
+  if constexpr (std::is_same<C, float2>::value)
+    k_rfft_xw<T, C, MappedSrc<T>>
+        <<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
+            sb, g, stages(p.ax[0]), tw[0]);
+  else
+    k_rfft_x<T, C, MappedSrc<T>><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
+                                   tile_smem<C>(p.F[0]), s>>>(sb, g, stages(p.ax[0]), tw[0]);
   for (int d = 1; d <= 2; d++)
-    if (p.F[d] > 1) strided_pass_batch(pb, nb, p, d, false, tw[d], s);
+    if (p.F[d] > 1) strided_pass_batch<C>(pb, nb, p, d, false, tw[d], s);
 }
 
-// nb inverse transforms (FP32), output b the inverse of a * k[b] (formed by the first inverse pass in work[b])
-void rfft_inverse_batch_impl(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,
-                             double scale, double *const *out, bool accumulate, cudaStream_t s)
+// nb inverse transforms, output b the inverse of a * k[b] (formed by the first inverse pass in work[b])
+template <class C>
+void rfft_inverse_batch_impl(const C *a, const C *const *k, int nb, C *const *work, const FftPlan &p, double scale,
+                             double *const *out, bool accumulate, const C *const *tw, cudaStream_t s)
 {
-  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
-  PassBatch<float2> pb{}, plain{};
-  OutBatch<float2> ob{};
+  PassBatch<C> pb{}, plain{};
+  OutBatch<C> ob{};
   for (int b = 0; b < nb; b++) {
     pb.in[b] = plain.in[b] = work[b];
     pb.out[b] = plain.out[b] = work[b];
@@ -794,15 +811,19 @@ void rfft_inverse_batch_impl(const float2 *a, const float2 *const *k, int nb, fl
   bool pending = true;
   for (int d = 2; d >= 1; d--) {
     if (p.F[d] == 1) continue;
-    strided_pass_batch(pending ? pb : plain, nb, p, d, true, tw[d], s);
+    strided_pass_batch<C>(pending ? pb : plain, nb, p, d, true, tw[d], s);
     pending = false;
   }
   if (pending)
-    for (int b = 0; b < nb; b++) k_spec_terms<float2><<<grid_for(p.NH), 256, 0, s>>>(pb.terms[b], work[b], p.NH);
+    for (int b = 0; b < nb; b++) k_spec_terms<C><<<grid_for(p.NH), 256, 0, s>>>(pb.terms[b], work[b], p.NH);
   const XGeom g = xgeom(p);
   const long npairs = (g.nlines + 1) / 2;
-  k_irfft_xw<float2><<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines,
-                        wtile_smem(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+  if constexpr (std::is_same<C, float2>::value)
+    k_irfft_xw<C><<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines,
+                    wtile_smem(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+  else
+    k_irfft_x<C><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
+                   tile_smem<C>(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
 }
 
 }  // namespace
@@ -933,15 +954,34 @@ int fft_max_batch() { return kMaxBatch; }
 
 void rfft_forward_mapped_batch(const MapSrc *m, int nb, float2 *const *spec, const FftPlan &p, cudaStream_t s)
 {
+  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
   for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
-    rfft_forward_mapped_batch_impl(m + b0, std::min(kMaxBatch, nb - b0), spec + b0, p, s);
+    rfft_forward_mapped_batch_impl<float, float2>(m + b0, std::min(kMaxBatch, nb - b0), spec + b0, p, tw, s);
+}
+
+void rfft_forward_mapped_batch(const MapSrc *m, int nb, double2 *const *spec, const FftPlan &p, cudaStream_t s)
+{
+  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
+  for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
+    rfft_forward_mapped_batch_impl<double, double2>(m + b0, std::min(kMaxBatch, nb - b0), spec + b0, p, tw, s);
 }
 
 void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,
                         double scale, double *const *out, bool accumulate, cudaStream_t s)
 {
+  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
   for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
-    rfft_inverse_batch_impl(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0, accumulate, s);
+    rfft_inverse_batch_impl<float2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0,
+                                    accumulate, tw, s);
+}
+
+void rfft_inverse_batch(const double2 *a, const double2 *const *k, int nb, double2 *const *work, const FftPlan &p,
+                        double scale, double *const *out, bool accumulate, cudaStream_t s)
+{
+  const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
+  for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
+    rfft_inverse_batch_impl<double2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0,
+                                     accumulate, tw, s);
 }
 
 void fft_pass(double2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s)

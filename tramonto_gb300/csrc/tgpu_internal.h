@@ -112,7 +112,10 @@ int fft_max_terms();
 // channels into spec[b]; inverse transforms out[b] (+)= scale * inverse of a * k[b] (work[b] the half spectra)
 int fft_max_batch();
 void rfft_forward_mapped_batch(const MapSrc *m, int nb, float2 *const *spec, const FftPlan &p, cudaStream_t s);
+void rfft_forward_mapped_batch(const MapSrc *m, int nb, double2 *const *spec, const FftPlan &p, cudaStream_t s);
 void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,
+                        double scale, double *const *out, bool accumulate, cudaStream_t s);
+void rfft_inverse_batch(const double2 *a, const double2 *const *k, int nb, double2 *const *work, const FftPlan &p,
                         double scale, double *const *out, bool accumulate, cudaStream_t s);
 // one y (d = 1) or z (d = 2) pass over a half spectrum, in place (benchmark hook)
 void fft_pass(double2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s);
