@@ -76,7 +76,7 @@ def dense_jacobian(oracle, x):
     return J
 
 
-def make_manager(L, p, z, hardsphere=True):
+def make_manager(L, p, z, hardsphere=True, a22_diagonal=True):
     N, nunk = p.nnodes, p.nunk
     h = (L.dft_hardsphere_lin_prob_mgr_create if hardsphere else L.dft_basic_lin_prob_mgr_create)(nunk, None, None)
     assert h
@@ -85,7 +85,7 @@ def make_manager(L, p, z, hardsphere=True):
                         ("setdensityequationids", "blk_dens")):
             a, ptr = ints(z[key])
             assert getattr(L, "dft_hardsphere_lin_prob_mgr_" + fn)(h, len(a), ptr) == 0
-        assert L.dft_hardsphere_lin_prob_mgr_seta22blockisdiagonal(h, 1) == 0
+        assert L.dft_hardsphere_lin_prob_mgr_seta22blockisdiagonal(h, 1 if a22_diagonal else 0) == 0
     assert L.dft_linprobmgr_finalizeblockstructure(h) == -1      # maps not set yet
     g, gp = ints(np.arange(N))
     assert L.dft_linprobmgr_setnodalrowmap(h, N, gp) == 0

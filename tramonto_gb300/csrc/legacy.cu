@@ -7,7 +7,8 @@
 // solves through the Schur complement as dft_HardSphereLinProbMgr does
 // (src/dft_HardSphereLinProbMgr.cpp:345-428): block 1 = independent then dependent non-local
 // unknowns, block 2 = densities; A11 = [-I 0; B -I] (dft_HardSphereA11_Epetra_Operator.cpp:130-197,
-// checked at set-up), S = A22 - A21 A11^-1 A12, GMRES on S with diag(A22) as left preconditioner,
+// checked at set-up), S = A22 - A21 A11^-1 A12, GMRES on S with diag(A22) as left preconditioner (ILU(2) of
+// A22 when the caller says A22 is not diagonal, as the reference),
 // then x1 = A11^-1 (b1 - A12 x2).  The basic manager runs GMRES on the whole matrix with its
 // diagonal as left preconditioner.  GMRES orthogonalises by classical Gram-Schmidt applied twice
 // (one batched dot-product kernel per pass) and stops on ||M^-1 r|| <= tol ||M^-1 b||.
@@ -56,6 +57,35 @@ __global__ void k_axpby(double *__restrict__ y, double a, const double *__restri
 {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     y[i] = a * x[i] + b * y[i];
+}
+
+// y <- U^-1 L^-1 y with the incomplete factors of A22 (L unit lower, strict part stored; U upper with its
+// diagonal first in each row), level by level in one CTA: the rows of a level depend only on earlier levels
+__global__ void __launch_bounds__(1024) k_ilu_solve(int nlev_l, const int *__restrict__ lp, const int *__restrict__ lr,
+                                                    const long *__restrict__ Lrp, const int *__restrict__ Lci,
+                                                    const double *__restrict__ Lva, int nlev_u,
+                                                    const int *__restrict__ up, const int *__restrict__ ur,
+                                                    const long *__restrict__ Urp, const int *__restrict__ Uci,
+                                                    const double *__restrict__ Uva, double *__restrict__ y)
+{
+  for (int l = 0; l < nlev_l; l++) {
+    for (int q = lp[l] + threadIdx.x; q < lp[l + 1]; q += blockDim.x) {
+      const int r = lr[q];
+      double v = y[r];
+      for (long k = Lrp[r]; k < Lrp[r + 1]; k++) v -= Lva[k] * y[Lci[k]];
+      y[r] = v;
+    }
+    __syncthreads();
+  }
+  for (int l = 0; l < nlev_u; l++) {
+    for (int q = up[l] + threadIdx.x; q < up[l + 1]; q += blockDim.x) {
+      const int r = ur[q];
+      double v = y[r];
+      for (long k = Urp[r] + 1; k < Urp[r + 1]; k++) v -= Uva[k] * y[Uci[k]];
+      y[r] = v / Uva[Urp[r]];
+    }
+    __syncthreads();
+  }
 }
 
 __global__ void k_divide(double *__restrict__ y, const double *__restrict__ d, long n)
@@ -138,6 +168,12 @@ struct Mgr {
   cudaStream_t s = nullptr;
   DevCsr dJ, dB, dA12, dA21, dA22;
   double *d_prec = nullptr;      // preconditioner diagonal (A22 or J)
+  // ILU(2) of a non-diagonal A22 (the reference's Ifpack "ILU", level-of-fill 2,
+  // src/dft_A22Matrix_Epetra_Operator.cpp:110-140) and the level sets of its triangular solves
+  bool ilu = false;
+  DevCsr dL, dU;
+  int nlev_l = 0, nlev_u = 0;
+  int *d_lp = nullptr, *d_lr = nullptr, *d_up = nullptr, *d_ur = nullptr;
   double *d_x = nullptr, *d_b = nullptr, *d_t1 = nullptr, *d_t2 = nullptr, *d_t3 = nullptr;
   double *d_V = nullptr, *d_partial = nullptr, *d_h = nullptr;
   int kdim = 0;
@@ -185,6 +221,13 @@ void free_dev(Mgr *m)
   free_csr(m->dA12);
   free_csr(m->dA21);
   free_csr(m->dA22);
+  free_csr(m->dL);
+  free_csr(m->dU);
+  for (int **p : {&m->d_lp, &m->d_lr, &m->d_up, &m->d_ur}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  m->ilu = false;
   for (double **p : {&m->d_prec, &m->d_x, &m->d_b, &m->d_t1, &m->d_t2, &m->d_t3, &m->d_V, &m->d_partial, &m->d_h}) {
     cudaFree(*p);
     *p = nullptr;
@@ -207,6 +250,93 @@ bool upload_csr(const HostCsr &h, DevCsr &d, cudaStream_t s, std::string *why)
       return false;
   }
   return ck(cudaStreamSynchronize(s), why);
+}
+
+// ILU(p) by levels of fill (Saad, Iterative Methods for Sparse Linear Systems, 2nd ed., Algorithm 10.5): row i of
+// A is eliminated with the U rows of its earlier columns in increasing column order; a fill entry gets level
+// lev(i,k) + lev(k,j) + 1 and is kept at level <= p (original entries have level 0).  L is unit lower (its strict
+// part stored), U upper with the diagonal first in each row.  false on a zero pivot.
+bool ilu_levels(const HostCsr &A, int p, HostCsr &L, HostCsr &U)
+{
+  const int n = (int)A.rp.size() - 1;
+  std::vector<std::vector<int>> ulev(n);     // level of each stored U entry
+  std::vector<double> w(n, 0.0);
+  std::vector<int> lev(n, -1);               // -1: column absent from the working row
+  std::vector<int> cols;
+  for (int i = 0; i < n; i++) {
+    cols.clear();
+    for (long k = A.rp[i]; k < A.rp[i + 1]; k++) {
+      const int c = A.ci[k];
+      if (lev[c] < 0) cols.push_back(c);
+      lev[c] = 0;
+      w[c] += A.va[k];
+    }
+    if (lev[i] < 0) {   // keep the diagonal in the pattern
+      lev[i] = 0;
+      cols.push_back(i);
+    }
+    std::sort(cols.begin(), cols.end());
+    // eliminate the columns below i in increasing order; fill may add columns between the current and i
+    for (size_t q = 0; q < cols.size() && cols[q] < i; q++) {
+      const int k = cols[q];
+      const double piv = U.va[U.rp[k]];
+      w[k] /= piv;
+      const double f = w[k];
+      for (long e = U.rp[k] + 1; e < U.rp[k + 1]; e++) {
+        const int j = U.ci[e];
+        const int nl = lev[k] + ulev[k][e - U.rp[k]] + 1;
+        if (lev[j] < 0) {
+          if (nl > p) continue;
+          lev[j] = nl;
+          w[j] = 0.0;
+          cols.insert(std::upper_bound(cols.begin() + q + 1, cols.end(), j), j);
+        } else if (nl < lev[j]) {
+          lev[j] = nl;
+        }
+        w[j] -= f * U.va[e];
+      }
+    }
+    if (w[i] == 0.0) return false;
+    std::vector<int> &ul = ulev[i];
+    U.add(i, w[i]);
+    ul.push_back(lev[i]);
+    for (int c : cols) {
+      if (c < i) L.add(c, w[c]);
+      else if (c > i) {
+        U.add(c, w[c]);
+        ul.push_back(lev[c]);
+      }
+    }
+    L.end_row();
+    U.end_row();
+    for (int c : cols) {
+      w[c] = 0.0;
+      lev[c] = -1;
+    }
+  }
+  return true;
+}
+
+// level sets of a triangular solve: a row's level is one more than the deepest row it reads (lower: forward
+// order; upper: backward order)
+void tri_levels(const HostCsr &T, bool lower, std::vector<int> &ptr, std::vector<int> &rows)
+{
+  const int n = (int)T.rp.size() - 1;
+  std::vector<int> lv(n, 0);
+  int nl = 0;
+  for (int t = 0; t < n; t++) {
+    const int r = lower ? t : n - 1 - t;
+    int l = 0;
+    for (long k = T.rp[r] + (lower ? 0 : 1); k < T.rp[r + 1]; k++) l = std::max(l, lv[T.ci[k]] + 1);
+    lv[r] = l;
+    nl = std::max(nl, l + 1);
+  }
+  ptr.assign(nl + 1, 0);
+  for (int r = 0; r < n; r++) ptr[lv[r] + 1]++;
+  for (int l = 0; l < nl; l++) ptr[l + 1] += ptr[l];
+  rows.assign(n, 0);
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int r = 0; r < n; r++) rows[fill[lv[r]]++] = r;
 }
 
 void spmv(Mgr *m, const DevCsr &A, const double *x, double *y, double alpha, double beta)
@@ -259,11 +389,21 @@ void schur(Mgr *m, const double *v2, double *y2)
   spmv(m, m->dA21, m->d_t2, y2, -1.0, 1.0);
 }
 
+// y <- M^-1 y: the incomplete factors of a non-diagonal A22, else the diagonal
+void precondition(Mgr *m, double *y)
+{
+  if (m->ilu)
+    k_ilu_solve<<<1, 1024, 0, m->s>>>(m->nlev_l, m->d_lp, m->d_lr, m->dL.rp, m->dL.ci, m->dL.va, m->nlev_u, m->d_up,
+                                      m->d_ur, m->dU.rp, m->dU.ci, m->dU.va, y);
+  else
+    k_divide<<<592, kThreads, 0, m->s>>>(y, m->d_prec, m->nvec);
+}
+
 void apply_op(Mgr *m, const double *v, double *y)
 {
   if (m->hardsphere) schur(m, v, y);
   else spmv(m, m->dJ, v, y, 1.0, 0.0);
-  k_divide<<<592, kThreads, 0, m->s>>>(y, m->d_prec, m->nvec);
+  precondition(m, y);
 }
 
 // batched dots h[j] = <V_j, w>, j < k, back on the host
@@ -478,6 +618,26 @@ int setup_solver(Mgr *m)
     if (!upload_csr(B, m->dB, m->s, &why) || !upload_csr(A12, m->dA12, m->s, &why) ||
         !upload_csr(A21, m->dA21, m->s, &why) || !upload_csr(A22, m->dA22, m->s, &why))
       return fail(kErrCuda, why);
+    if (!m->a22_diagonal) {   // the reference preconditions a non-diagonal A22 with ILU(2)
+      HostCsr L, U;
+      if (!ilu_levels(A22, 2, L, U)) return fail(kErrUnsup, "zero pivot in the incomplete factorisation of A22");
+      std::vector<int> lp, lr, up, ur;
+      tri_levels(L, true, lp, lr);
+      tri_levels(U, false, up, ur);
+      m->nlev_l = (int)lp.size() - 1;
+      m->nlev_u = (int)up.size() - 1;
+      m->d_lp = dalloc<int>(lp.size(), &why);
+      m->d_lr = dalloc<int>(lr.size(), &why);
+      m->d_up = dalloc<int>(up.size(), &why);
+      m->d_ur = dalloc<int>(ur.size(), &why);
+      if (!upload_csr(L, m->dL, m->s, &why) || !upload_csr(U, m->dU, m->s, &why) || !m->d_lp || !m->d_lr ||
+          !m->d_up || !m->d_ur || !ck(cudaMemcpy(m->d_lp, lp.data(), lp.size() * sizeof(int), cudaMemcpyHostToDevice), &why) ||
+          !ck(cudaMemcpy(m->d_lr, lr.data(), lr.size() * sizeof(int), cudaMemcpyHostToDevice), &why) ||
+          !ck(cudaMemcpy(m->d_up, up.data(), up.size() * sizeof(int), cudaMemcpyHostToDevice), &why) ||
+          !ck(cudaMemcpy(m->d_ur, ur.data(), ur.size() * sizeof(int), cudaMemcpyHostToDevice), &why))
+        return fail(kErrCuda, why);
+      m->ilu = true;
+    }
     m->d_t1 = dalloc<double>(n1, &why);
     m->d_t2 = dalloc<double>(n1, &why);
   } else {
@@ -538,7 +698,7 @@ int solve(Mgr *m)
     // rhs2 = M^-1 (b2 - A21 A11^-1 b1)
     a11_inverse(m, d_b1, m->d_t2);
     spmv(m, m->dA21, m->d_t2, d_rhs2, -1.0, 1.0);
-    k_divide<<<592, kThreads, 0, m->s>>>(d_rhs2, m->d_prec, n2);
+    precondition(m, d_rhs2);
     st = gmres(m, d_rhs2, d_x2);
     if (st != kOk && st != kErrNoconv) return st;
     // x1 = A11^-1 (b1 - A12 x2)
