@@ -99,3 +99,48 @@ def test_stable_branches_match_natural_continuation(branch):
         n_nat = float(isotherm.adsorption(p, x)[0])
         assert abs(n_nat - r["N"]) <= 1e-7 * abs(r["N"]), (r["betamu"], n_nat, r["N"])
     s.close()
+
+
+def test_turning_point_solver_locks_onto_the_condensation_fold(branch):
+    """The Moore-Spence bordering algorithm (isotherm.turning_point, the reference's turning_point_alg) started
+    from the arclength point next to the condensation turning point converges to a state with ||R||_2 <= 1e-9
+    whose Jacobian has the null vector y (||J y|| / ||y|| <= 1e-6), at a beta mu at or beyond every arclength point
+    of that stretch of the branch (the fold is the branch's local maximum of beta mu), and at the maximum of a
+    quadratic fit beta mu(N) through the five arclength points around it (5e-4 in beta mu, 1e-2 relative in N: the
+    fit's own error over points ~0.02 apart in arclength)."""
+    from tramonto_gb300 import isotherm
+    recs, _ = branch
+    k = _turning_points(recs)[0]
+    rec = isotherm.turning_point(_spec(), recs[k]["x"], recs[k]["betamu"], tol=1e-9)
+    near = [r["betamu"] for r in recs[max(1, k - 5):k + 6]]
+    print("fold:", rec["betamu"], "arclength max:", max(near), "iterations", rec["iters"], "||R||", rec["resid"],
+          "||Jy||/||y||", rec["jy_rel"])
+    assert rec["converged"]
+    assert rec["resid"] <= 1e-9
+    assert rec["betamu"] >= max(near) - 1e-9
+    pts = recs[k - 2:k + 3]
+    c2, c1, c0 = np.polyfit([r["N"] for r in pts], [r["betamu"] for r in pts], 2)
+    n_fit, mu_fit = -c1 / (2 * c2), c0 - c1 * c1 / (4 * c2)
+    print("quadratic fit: beta mu", mu_fit, "N", n_fit, " turning point: N", rec["N"])
+    assert abs(rec["betamu"] - mu_fit) <= 5e-4 and abs(rec["N"] - n_fit) <= 1e-2 * n_fit
+    assert rec["jy_rel"] <= 1e-6
+
+
+def test_turning_point_continuation_in_the_wall_strength(branch):
+    """Continuation of the condensation fold in the wall strength eps_w (LOCA's turning-point continuation,
+    zero order with con_lib's step control), both ways from eps_w = 1: every requested point converges
+    (||R||_2 <= 1e-9, ||J y|| / ||y|| <= 1e-6), the fold stays the same one (N within 0.1 of the eps_w = 1
+    fold; the branch's next fold is at N ~ 2), and a weaker wall attraction moves it to a higher beta mu,
+    nearly linearly (the second difference of beta mu is below a tenth of the first)."""
+    from tramonto_gb300 import isotherm
+    recs, _ = branch
+    k = _turning_points(recs)[0]
+    for eps in ([1.0, 0.99, 0.98, 0.97], [1.0, 1.01, 1.02, 1.03]):
+        out = isotherm.turning_point_continuation(_spec(), recs[k]["x"], recs[k]["betamu"], eps)
+        print([(r["eps_w"], round(r["betamu"], 6), round(r["N"], 5), r["iters"], r["substeps"]) for r in out])
+        assert len(out) == 4 and all(r["converged"] and r["resid"] <= 1e-9 and r["jy_rel"] <= 1e-6 for r in out)
+        mus = np.array([r["betamu"] for r in out])
+        assert all(abs(r["N"] - out[0]["N"]) <= 0.1 for r in out)
+        d1 = np.diff(mus) * np.sign(eps[1] - eps[0])
+        assert np.all(d1 < 0)
+        assert np.max(np.abs(np.diff(d1))) <= 0.1 * np.min(np.abs(d1))

@@ -224,3 +224,193 @@ def arclength(spec, rho_b0, n_steps, ds=0.02, ds_min=1e-5, ds_max=0.2, direction
         return recs, x
     finally:
         s.close()
+
+
+def _tp_solver(s, p, x, mu, y=None, tol=1e-9, max_iter=40, perturb=1e-6, lin_tol=1e-12, log=None):
+    """Moore-Spence turning-point iterations on a live solver (see turning_point); returns (x, mu, y,
+    iterations, ||R||_2, ||J y|| / ||y||, converged)."""
+    r0 = p.first_rho
+    live = _live_rows(p)[0]
+    R_mu = np.zeros(s.shape)
+    R_mu[r0][live] = -1.0
+    n_unk = float(s.shape[0] * s.shape[1])
+
+    def lt(v):                     # ltransnorm with phi = ones: the mean of v over all unknowns
+        return float(v.sum()) / n_unk
+
+    def lin(rhs):
+        return s.solve(rhs, tol=lin_tol, max_iter=2000)[0]
+
+    def djy(v, h, Jy):
+        """(J(x + h v) y - J(x) y) / h; where x + h v leaves the functional's domain (a density <= 0 next to
+        a wall, where v is large) the backward difference, then steps 16 and 256 times smaller, are taken."""
+        for hh in (h, -h, h / 16, -h / 16, h / 256, -h / 256):
+            try:
+                s.fill(x + hh * v, mode=0)
+            except native.TgpuError as err:
+                if err.status != native.TGPU_ERR_DOMAIN:
+                    raise
+                continue
+            return (s.jv(y) - Jy) / hh
+        raise native.TgpuError(native.TGPU_ERR_DOMAIN, "no finite-difference step inside the domain")
+
+    rn, jy_rel = float("inf"), float("inf")
+    R = None
+    for it in range(max_iter + 1):
+        if R is None:                            # (a later iteration's residual comes from the update below)
+            s.set_chemical_potential([mu])
+            R = s.fill(x, mode=0)
+        rn = float(np.linalg.norm(R))
+        a = lin(R)                               # J a = R (a = -dx of a Newton step)
+        b = lin(R_mu)                            # J b = dR/dmu
+        if y is None:                            # first iteration: the null vector guess is b, normalised
+            y = b / lt(b)
+        else:
+            y = y / lt(y)
+        Jy = s.jv(y)
+        jy_rel = float(np.linalg.norm(Jy) / max(np.linalg.norm(y), 1e-300))
+        if log is not None:
+            log(it, mu, rn, jy_rel)
+        if it > 0 and rn <= tol and abs(dmu) <= 1e-10 * (1.0 + abs(mu)) and r_upd <= 1.0:
+            return x, mu, y, it, rn, jy_rel, True
+        if it == max_iter:
+            break
+        xnorm = float(np.sqrt(np.sum(x * x)))
+        ha = perturb * (perturb + xnorm / max(float(np.sqrt(np.sum(a * a))), 1e-300))
+        hb = perturb * (perturb + xnorm / max(float(np.sqrt(np.sum(b * b))), 1e-300))
+        dJy_a = djy(a, ha, Jy)
+        dJy_b = djy(b, hb, Jy)
+        s.fill(x, mode=0)                        # back to the Jacobian at x for the last two solves
+        # the reference's linear_solver_conwrap solves with the negated right-hand side of
+        # calc_rhs_continuation, so these are its c and d
+        c = lin(dJy_a)                           # TP_CONT_SOL3 (AGS_option 0): J c = (d/dx J y) a
+        d = lin(dJy_b)                           # TP_CONT_SOL4: J d = (d/dx J y) b (J does not depend on beta mu)
+        den = lt(d)
+        if den == 0.0 or not np.isfinite(den):
+            break
+        dmu = (1.0 - lt(c)) / den
+        y_new = c + dmu * d
+        # the null vector's scaled update (reltol 1e-6, abstol 1e-9; converged below 1)
+        r_upd = float(np.sqrt(np.mean(((y_new - y) / (np.abs(y_new) * 1e-6 + 1e-9)) ** 2)))
+        dx = -a - dmu * b
+        rho, drho = x[r0], dx[r0]                # the density-positivity fraction of update_solution
+        neg = live & (drho < -0.9 * rho)
+        f = min(1.0, float(np.min(-0.9 * rho[neg] / drho[neg]))) if neg.any() else 1.0
+        # an update that leaves the functional's domain (a packing fraction n3 >= 1) is halved until the
+        # residual can be taken again; eight halvings without success end the solve unconverged
+        R = None
+        for _ in range(9):
+            s.set_chemical_potential([mu + f * dmu])
+            try:
+                R = s.fill(x + f * dx, mode=0)
+                break
+            except native.TgpuError as err:
+                if err.status != native.TGPU_ERR_DOMAIN:
+                    raise
+                f *= 0.5
+        if R is None:
+            break
+        x = x + f * dx
+        mu = mu + f * dmu
+        y = y_new
+    return x, mu, y, max_iter, rn, jy_rel, False
+
+
+def turning_point(spec, x0, mu0, y0=None, mixed=False, tol=1e-9, max_iter=40, perturb=1e-6, log=None):
+    """A turning point (spinodal) of the beta mu branch of a one-component pore problem, located by the
+    reference's Moore-Spence bordering algorithm (turning_point_alg, src/loca_bord.c:164-420, AGS_option 0).
+
+    Unknowns: the state x, beta mu and the null vector y of the Jacobian J, normalised by <y, phi>/n = 1 with
+    phi = ones (calc_scale_vec_conwrap, src/dft_continuation.c:501-528; ltransnorm, src/loca_util.c:209).
+    Each iteration solves four systems with J at x,
+        J a = R,   J b = dR/dmu,   J c = (J(x + h_a a) y - J(x) y)/h_a,   J d = (J(x + h_b b) y - J(x) y)/h_b
+    (h_v = perturb (perturb + |x|/|v|); the right-hand sides of calc_rhs_continuation TP_CONT_SOL2-4,
+    src/loca_bord.c:1352-1520, negated as its linear solver takes them; beta mu enters R linearly, dR/dmu = -1
+    on the live Euler-Lagrange rows, so J does not depend on it), then
+        dmu = (1 - <c, phi>/n) / (<d, phi>/n),   y <- c + dmu d,   x <- x - a - dmu b,   mu <- mu + dmu,
+    with the density-positivity fraction of update_solution on the state update.  Starts from a state
+    (x0, mu0) near the fold (e.g. an arclength point where the tangent's mu component changes sign); y0, a
+    null vector guess (the previous fold's), is optional.  Returns a record: beta mu, N, ||R||_2,
+    ||J y|| / ||y||, iterations, converged, and the state and null vector."""
+    p = setup.slit_pore(spec)
+    if p.ncomp != 1:
+        raise ValueError("one component")
+    s = native.Solver(p)
+    try:
+        set_mode(s, mixed)
+        x = np.array(x0, np.float64)
+        live = _live_rows(p)[0]
+        rho = x[p.first_rho]
+        rho[~live] = 0.0                         # rows that are zero-density rows at this wall strength
+        fresh = live & ~(rho > 0.0)              # rows that are live only at this wall strength: the ideal gas
+        rho[fresh] = np.exp(float(mu0) - np.asarray(p.vext, np.float64).reshape(-1)[fresh])
+        x, mu, y, it, rn, jy, ok = _tp_solver(s, p, x, float(mu0), y0, tol, max_iter, perturb,
+                                              1e-6 if mixed else 1e-12, log)
+        return dict(betamu=mu, N=float(adsorption(p, x)[0]), resid=rn, jy_rel=jy, iters=it, converged=ok, x=x, y=y)
+    finally:
+        s.close()
+
+
+def _off_fold(x, y, offset):
+    """x + s y with |s y| = offset |x|, on the side that keeps every positive entry of x above half its value
+    (the other side, or a smaller offset, when one does not)."""
+    scale = offset * float(np.linalg.norm(x)) / max(float(np.linalg.norm(y)), 1e-300)
+    pos = x > 0
+    for s in (scale, -scale, 0.25 * scale, -0.25 * scale):
+        xs = x + s * y
+        if np.all(xs[pos] >= 0.5 * x[pos]):
+            return xs
+    return x
+
+
+def turning_point_continuation(spec, x0, mu0, eps_values, tol=1e-9, max_iter=25, first_step=0.002, max_step=0.01,
+                               step_ctrl=0.5, min_step=1e-5, restart_offset=0.01, log=None):
+    """Zero-order continuation of a turning point in the wall strength eps_w (LOCA's
+    TURNING_POINT_CONTINUATION: each step re-solves the turning-point system from the previous fold's
+    state, beta mu and null vector, src/loca_lib.c:582-640) with con_lib's step control
+    (src/loca_lib.c:440-512): a converged step of `its` Newton iterations multiplies the step by
+    1 + step_ctrl ((max_iter - its) / (max_iter - 1))^2 (simple_step_control, src/loca_lib.c:1007-1033) up to
+    max_step, a failed one halves it and retries from the last converged fold, down to min_step.  The
+    steps start from eps_values[0] (solved from x0, mu0) and land on every requested value; one record per
+    requested eps_w, "substeps" counting the turning-point solves that reached it.  Small steps matter: the
+    Moore-Spence iteration converges only near its fold, and a step that is too long may converge on
+    another fold of the same branch.  Each step restarts a distance restart_offset ||x|| along the null vector
+    from the last fold, where the branch passes (x_f + s y at beta mu_f + O(s^2)): at the fold itself J is
+    singular to rounding, a = J^-1 R and b = J^-1 dR/dmu carry null components of order |R| / sigma_min that
+    the update -a - dmu b must cancel to that relative precision, which the finite-difference second
+    derivatives cannot give, whereas off the fold J is nonsingular by O(s) (as at an arclength point next to
+    the fold).  log(eps_w, record), when given, sees every turning-point solve."""
+    out = []
+    x, mu, y = np.array(x0, np.float64), float(mu0), None
+    e_cur, step = None, float(first_step)
+    for e in eps_values:
+        e = float(e)
+        n_sub, rec = 0, None
+        while True:
+            if e_cur is None:
+                target = e
+            else:
+                target = e if abs(e - e_cur) <= step else e_cur + np.copysign(step, e - e_cur)
+            rec = turning_point(dict(spec, eps_w=target), _off_fold(x, y, restart_offset) if e_cur is not None else x,
+                                mu, y, tol=tol, max_iter=max_iter)
+            n_sub += 1
+            if log is not None:
+                log(target, rec)
+            if rec["converged"]:
+                x, mu, y = rec["x"], rec["betamu"], rec["y"]
+                if e_cur is not None:
+                    f = (max_iter - rec["iters"]) / (max_iter - 1.0)
+                    step = min(step * (1.0 + step_ctrl * f * f), max_step)
+                e_cur = target
+                if target == e:
+                    break
+                continue
+            step *= 0.5
+            if e_cur is None or step < min_step:
+                break
+        rec["eps_w"] = e
+        rec["substeps"] = n_sub
+        out.append(rec)
+        if not rec["converged"]:
+            break
+    return out

@@ -28,6 +28,7 @@ from . import build as _build
 from .problem import Problem
 
 TGPU_OK = 0
+TGPU_ERR_DOMAIN = -7
 FP64, FP32, BF16X3, FP16TC, FP64_FFT = 0, 1, 2, 3, 4
 FILL_FP64, FILL_FP32, FILL_REFINED, FILL_MIXED, FILL_FF, FILL_MIXED_FF, FILL_FFT, FILL_MIXED_FFT = 0, 1, 2, 3, 4, 5, 6, 7
 TIME_FFT32 = 16   # time_stencil_sum: the FP32 FFT convolution

@@ -459,12 +459,13 @@ def slit_pore_vext(ndim, nx, esize, eps_w=1.0, sigma_w=1.0, cut_w=3.0, pattern=0
 
 def slit_pore(spec, rho_b=None):
     """One configuration-5 problem: FMT1 + WCA (eps = 1, r_c = 2.5, kT* = spec.get("kT", 1.2)) in a slit pore
-    (spec from config5); walls beyond both x ends, periodic y in 2-D."""
+    (spec from config5); walls beyond both x ends, periodic y in 2-D, of strength spec.get("eps_w", 1.0) (the
+    zero-density rows follow from the field at that strength)."""
     ndim, nx, dx = spec["ndim"], tuple(spec["nx"]), spec["dx"]
     es = (dx,) * ndim
     kT = float(spec.get("kT", 1.2))
     bc = [(BC_IN_WALL, BC_IN_WALL)] + [(BC_PERIODIC, BC_PERIODIC)] * (ndim - 1)
-    vext = slit_pore_vext(ndim, nx, es)
+    vext = slit_pore_vext(ndim, nx, es, eps_w=float(spec.get("eps_w", 1.0)))
     return build_problem(ndim, nx, es, tuple(bc), hs_diam=[1.0], rho_b=[spec["rho_b"] if rho_b is None else rho_b],
                          functional=FMT1, attraction=True, sigma=[[1.0]], eps=[[1.0 / kT]], rcut=[[2.5]], vext=vext)
 
