@@ -125,14 +125,26 @@ int tgpu_set_hard_wall(tgpu_handle h, const int *boundary_nodes, const short *fl
  * src/dft_fill_CLSmf.c:38-171, and dft_linprobmgr_setcoarsenednodeslist, src/dft_mesh.c:516).
  * flag[N] is Mesh_coarsen_flag: >= 0 the node's quadrature zone (< nzone, at most 5), -1/-2/-3 the
  * node's rows average its two neighbours along x/y/z (load_coarse_node_Ndim,
- * src/dft_fill_coarse.c:66-123).  rb_bulk[4 + 2 ndim] is Rhobar_b in solution order, the value of a
- * weighted density beyond an IN_BULK boundary in those rows.  Zone z >= 1 stencils come from
+ * src/dft_fill_coarse.c:66-123), TGPU_FLAG_1DBC the node's rows copy the node with the same coordinate
+ * along the tgpu_set_1d_boundary dimension and 0 along the others (L1D_bc: load_coarse_node_1dim,
+ * src/dft_fill_coarse.c:37-64; set_mesh_coarsen_flag, src/dft_mesh.c:2835-2841), TGPU_FLAG_BULK /
+ * TGPU_FLAG_PB the node's Euler-Lagrange rows hold the bulk density (BULK_ZONE: fill_bulk_density,
+ * src/dft_fill_EL.c:265-284) / the ideal gas in the external field without hard-sphere or attraction
+ * terms (PB_ZONE, src/dft_fill_EL.c:132-161, 405-410; no charges here), its other rows zone 0's
+ * stencils (the reference indexes its stencil table with the negative flag there).  rb_bulk[4 + 2 ndim]
+ * is Rhobar_b in solution order, the value of a weighted density beyond an IN_BULK boundary in averaged
+ * rows; with a phase interface rb_bulk[2][4 + 2 ndim] holds Rhobar_b_LBB then Rhobar_b_RTF (the low and
+ * the high side), the densities there Rho_b_LBB / _RTF.  Zone z >= 1 stencils come from
  * tgpu_set_zone_stencil (offsets in fine-node units, as calc_stencils scales them).  The Jacobian is the
  * residual's derivative (the Coarser_jac option, a cheaper approximate Jacobian for the assembled
  * matrix, has no use in the matrix-free products); the Newton step is solved on the nodes that are not
  * coarsened, the coarsened nodes following by interpolation (the adjoint solves that step's transpose).
- * Not with phase interfaces or ATTInA22Block = 1. */
+ * With two zones the reference's averaged row next to a 1-D boundary, BULK_ZONE or PB_ZONE node reads past
+ * its offset table; that pattern is TGPU_ERR_UNSUPPORTED. */
+enum { TGPU_FLAG_PB = -777, TGPU_FLAG_BULK = -888, TGPU_FLAG_1DBC = -999 };
 int tgpu_set_zones(tgpu_handle h, int nzone, const int *flag, const double *rb_bulk);
+/* L1D_bc's dimension (Dim_1Dbc = Grad_dim, src/dft_input.c:1474-1477), 0 unless set; before finalize. */
+int tgpu_set_1d_boundary(tgpu_handle h, int dim);
 int tgpu_set_zone_stencil(tgpu_handle h, int zone, int type, int index, int length, const short *offsets,
                           const double *weights, const double *hw);
 int tgpu_finalize(tgpu_handle h);

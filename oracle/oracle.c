@@ -739,7 +739,12 @@ static double coarse_value(const orc_problem *p, int iu, long jn)
     if (jn == -4) return p->rho_b_rtf[ic];
     return 0.0;
   }
-  if (iu >= p->first_rb && iu < p->first_rb + 4 + 2 * p->ndim && jn == -1) return p->rhobar_bc[iu - p->first_rb];
+  if (iu >= p->first_rb && iu < p->first_rb + 4 + 2 * p->ndim) {
+    const int k = iu - p->first_rb;
+    if (jn == -1) return p->rhobar_bc[k];
+    if (jn == -3) return p->rhobar_lbb[k];
+    if (jn == -4) return p->rhobar_rtf[k];
+  }
   return 0.0;   /* inside a wall; (the reference leaves mean-field boundary values undefined) */
 }
 
@@ -756,7 +761,7 @@ static void coarse_terms(pass_t *ps, int iu, long row, long node, double fac, do
   const int d = -p->zone_flag[node] - 1;
   for (int loop = 0; loop < 2; loop++) {
     const long jn = offset_to_node(p, ijk, off_pm[d + 3 * loop], reflect);
-    if (jn >= 0 && p->zone_flag[jn] < 0 && p->nzone == 2) {
+    if (jn >= 0 && p->zone_flag[jn] < 0 && p->zone_flag[jn] >= -3 && p->nzone == 2) {
       coarse_terms(ps, iu, row, jn, 0.5 * fac, R);
     } else if (jn < 0) {
       *R -= fac * coarse_value(p, iu, jn);
@@ -767,10 +772,17 @@ static void coarse_terms(pass_t *ps, int iu, long row, long node, double fac, do
   }
 }
 
+/* the fill reads Mesh_coarsen_flag with Mesh_coarsening on and walls present, or with L1D_bc
+ * (src/dft_fill_main.c:120) */
 static int coarsened(const orc_problem *p)
 {
-  return p->zone_flag && p->mesh_coarsening && p->nwall > 0;
+  return p->zone_flag && ((p->mesh_coarsening && p->nwall > 0) || p->l1d_bc);
 }
+
+enum { FLAG_PBELEC = -777, FLAG_BULK = -888, FLAG_1DBC = -999 };
+
+/* a row that averages neighbours or copies the 1-D line (not BULK_ZONE / PB_ZONE nodes) */
+static int averaged_flag(int flag) { return flag < 0 && flag != FLAG_BULK && flag != FLAG_PBELEC; }
 
 static void fill_node(pass_t *ps, long inode)
 {
@@ -783,7 +795,23 @@ static void fill_node(pass_t *ps, long inode)
   node_to_ijk(p, inode, ijk);
   /* fill_resid_and_matrix (src/dft_fill_main.c:118-135): the node's zone, or an averaged row */
   const int flag = coarsened(p) ? p->zone_flag[inode] : 0;
-  if (flag < 0) {
+  if (flag == FLAG_1DBC) {
+    /* load_coarse_node_1dim (src/dft_fill_coarse.c:37-64): x(node) - x(the node on the line through the
+     * origin along Grad_dim with the same Grad_dim coordinate), for every unknown */
+    int jk[3] = {0, 0, 0};
+    jk[p->dim_1dbc] = ijk[p->dim_1dbc];
+    const long jn = jk[0] + (long)p->nx[0] * (jk[1] + (long)p->nx[1] * jk[2]);
+    for (int iu = 0; iu < p->nunk; iu++) {
+      const double R = x[(long)iu * N + inode] - x[(long)iu * N + jn];
+      if (ps->entry) {
+        ps->entry(ps->ctx, iu, inode, iu, inode, 1.0);
+        ps->entry(ps->ctx, iu, inode, iu, jn, -1.0);
+      }
+      if (ps->R) ps->R[(long)iu * N + inode] = R;
+    }
+    return;
+  }
+  if (averaged_flag(flag)) {
     for (int iu = 0; iu < p->nunk; iu++) {   /* load_coarse_node_Ndim (src/dft_fill_coarse.c:66-84) */
       const double fac = (iu >= p->first_rho && iu < p->first_rho + p->ncomp) ? 1.0 : -1.0;
       double R = fac * x[(long)iu * N + inode];
@@ -793,8 +821,9 @@ static void fill_node(pass_t *ps, long inode)
     }
     return;
   }
-  ps->izone = flag;
-  ps->jzone = find_jzone(p, flag, inode);
+  ps->izone = flag < 0 ? 0 : flag;
+  ps->jzone = find_jzone(p, ps->izone, inode);
+  if (ps->jzone < 0) ps->jzone = 0;
   for (int iu = 0; iu < p->nunk; iu++) {
     double R = 0.0;
     const double xi = x[(long)iu * N + inode];
@@ -806,6 +835,15 @@ static void fill_node(pass_t *ps, long inode)
         /* fill_zero_value (src/dft_fill_EL.c:224-240) */
         R = xi;
         if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, 1.0);
+      } else if (flag == FLAG_BULK) {
+        /* fill_bulk_density (src/dft_fill_EL.c:69-80, 265-284) */
+        R = log(xi) - log(p->rho_b[ic]);
+        if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, 1.0 / xi);
+      } else if (flag == FLAG_PBELEC) {
+        /* ideal gas, chemical potential without the excess terms, external field; no hard-sphere or
+         * attraction terms (src/dft_fill_EL.c:132-161, 405-410) */
+        R = log(xi) + (p->interface == 2 ? -p->betamu[ic] : -log(p->rho_b[ic])) + p->vext[(long)ic * N + inode];
+        if (ps->entry) ps->entry(ps->ctx, iu, inode, iu, inode, 1.0 / xi);
       } else if (p->interface == 2 && ic == 0 && inode == p->pin_node) {
         /* fill_constant_density (src/dft_fill_EL.c:89-96, 286-305) */
         R = log(xi) - log(p->pin_value);
@@ -927,7 +965,7 @@ int orc_schur(const orc_problem *p, const double *x, const double *v2, double *S
 {
   if (coarsened(p))
     for (long i = 0; i < orc_nnodes(p); i++)
-      if (p->zone_flag[i] < 0) return -2;
+      if (averaged_flag(p->zone_flag[i])) return -2;
   const long N = orc_nnodes(p);
   const long U = p->nunk;
   const int nrb = 4 + 2 * p->ndim;

@@ -86,6 +86,14 @@ typedef struct {
   const double *zsten_w[ORC_MAXZ][3][ORC_MAXC * ORC_MAXC];
   const double *zsten_hw[ORC_MAXZ][3][ORC_MAXC * ORC_MAXC];
   double rhobar_bc[10];       /* Rhobar_b in solution order: constant_boundary of the rb unknowns */
+  /* L1D_bc (src/dft_mesh.c:165-185, 2835-2841): nodes flagged -999 hold every unknown equal to the node
+   * with the same coordinate along dim_1dbc and 0 along the others (load_coarse_node_1dim,
+   * src/dft_fill_coarse.c:37-64).  Flags -888 (BULK_ZONE) and -777 (PB_ZONE) keep the bulk density, or
+   * the ideal gas in the external field, in the Euler-Lagrange rows (fill_bulk_density
+   * src/dft_fill_EL.c:265-284; the FLAG_PBELEC branches :132, :405-410); their other rows take zone 0's
+   * stencils (the reference indexes its stencil table with the negative flag there). */
+  int l1d_bc, dim_1dbc;
+  double rhobar_lbb[10], rhobar_rtf[10];   /* Rhobar_b_LBB / _RTF (phase interface) in solution order */
 } orc_problem;
 
 long orc_nnodes(const orc_problem *p);

@@ -81,6 +81,8 @@ class _Problem(C.Structure):
         ("zsten_w", ((C.POINTER(C.c_double) * (MAXC * MAXC)) * 3) * MAXZ),
         ("zsten_hw", ((C.POINTER(C.c_double) * (MAXC * MAXC)) * 3) * MAXZ),
         ("rhobar_bc", C.c_double * 10),
+        ("l1d_bc", C.c_int), ("dim_1dbc", C.c_int),
+        ("rhobar_lbb", C.c_double * 10), ("rhobar_rtf", C.c_double * 10),
     ]
 
 
@@ -149,6 +151,7 @@ class Oracle:
         s.nzone = int(getattr(prob, "nzone", 1))
         s.mesh_coarsening, s.coarser_jac = int(getattr(prob, "mesh_coarsening", 0)), int(getattr(prob, "coarser_jac", 0))
         s.nwall = int(getattr(prob, "nwall", 0))
+        s.l1d_bc, s.dim_1dbc = int(getattr(prob, "l1d_bc", 0)), int(getattr(prob, "dim_1dbc", 0))
         if getattr(prob, "zone_flag", None) is not None:
             zf = np.ascontiguousarray(prob.zone_flag, np.int32)
             self._keep.append(zf)
@@ -169,6 +172,17 @@ class Oracle:
         if rbc is not None:
             for i, v in enumerate(np.asarray(rbc, np.float64)[:10]):
                 s.rhobar_bc[i] = float(v)
+        if s.interface == 2:
+            # Rhobar_b_LBB / _RTF (rhobar_icomp of the two bulk states, src/dft_thermo_hs.c:292-311)
+            for dst, rho in ((s.rhobar_lbb, prob.rho_b_lbb), (s.rhobar_rtf, prob.rho_b_rtf)):
+                for ic in range(prob.ncomp):
+                    d = float(prob.hs_diam[ic])
+                    vol, area = np.pi * d * d * d / 6.0, np.pi * d * d
+                    f = float(prob.fac_overlap[ic]) * float(rho[ic])
+                    dst[0] += f * vol
+                    dst[1] += f * area
+                    dst[2] += f * area * float(prob.inv_4pir[ic])
+                    dst[3] += f * area * float(prob.inv_4pirsq[ic])
         self.s = s
 
     def _vec(self, x, rows=None):

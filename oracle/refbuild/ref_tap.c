@@ -78,7 +78,8 @@ int tref_setup(const char *dir)
  * Nrho_bar_s Type_func Type_attr ATTInA22Block Lhard_surf Nlists_HW Nwall
  * Type_bc[3][2] Phys2Unk_first[DENSITY,HSRHOBAR,MF_EQ] Nzone Nodes_x_box[3]
  * Max_sten_length[3] Pflag[3] Iguess Type_interface Mesh_coarsening Coarser_jac
- * Nnodes_per_el_V Type_pairPot Lcut_jac Type_CoreATT_R Type_CoreATT_CONST Lconstrain_interface Grad_dim */
+ * Nnodes_per_el_V Type_pairPot Lcut_jac Type_CoreATT_R Type_CoreATT_CONST Lconstrain_interface Grad_dim
+ * L1D_bc Dim_1Dbc */
 int tref_info_ints(int *o)
 {
   int k = 0, i;
@@ -97,6 +98,7 @@ int tref_info_ints(int *o)
   o[k++] = Nnodes_per_el_V; o[k++] = Type_pairPot; o[k++] = Lcut_jac;
   o[k++] = Type_CoreATT_R; o[k++] = Type_CoreATT_CONST;
   o[k++] = Lconstrain_interface; o[k++] = Grad_dim;
+  o[k++] = L1D_bc; o[k++] = Dim_1Dbc;
   return k;
 }
 

@@ -79,12 +79,15 @@ def cases():
         "Esize_x(idim)": "0.05", "ATTInA22Block": MF_UNKNOWNS, "L_Schur": SCHUR_LINSOLVE})
     # 3-D FMT1 + WCA, LJ 9-3 planar wall at x=0, bulk at the far x end, periodic y and z
     surf3d = write_surfaces(os.path.join(tmp, "fmt1_wca_3d"), " 0 0 -1.5 0.0 0.0  0.0\n")
-    c["fmt1_wca_3d"] = deck("GEOM3_PLANE_ROUGH_3D", {
-        "Size_x(idim)": "3.0 5.5 5.5", "Esize_x(idim)": "0.25 0.25 0.25",
-        "Type_bc(x0": "-1 0", "Type_bc(x1": "1 1", "Type_bc(x2": "1 1",
-        "Nwall_types Nwall Nlink": "1 1 1 0 0", "Xtest_reflect_TF": "0 0 0",
-        "Lrough_surf": "0", "Lapply_offest": "0 0 0", "Cut_ff[i][j]": "2.5", "Rho_b_0[icomp]": "0.6",
-        "ATTInA22Block": "0 20 0 0 0", "L_Schur": "1 0 100"}, surfaces=surf3d)
+    wca3d = {"Size_x(idim)": "3.0 5.5 5.5", "Esize_x(idim)": "0.25 0.25 0.25",
+             "Type_bc(x0": "-1 0", "Type_bc(x1": "1 1", "Type_bc(x2": "1 1",
+             "Nwall_types Nwall Nlink": "1 1 1 0 0", "Xtest_reflect_TF": "0 0 0",
+             "Lrough_surf": "0", "Lapply_offest": "0 0 0", "Cut_ff[i][j]": "2.5", "Rho_b_0[icomp]": "0.6",
+             "ATTInA22Block": "0 20 0 0 0", "L_Schur": "1 0 100"}
+    c["fmt1_wca_3d"] = deck("GEOM3_PLANE_ROUGH_3D", wca3d, surfaces=surf3d)
+    # the same with L1D_bc: every node within 1 sigma of either x end holds the values of the node with the same x
+    # on the line y = z = 0 (the one row of such nodes that is filled)
+    c["fmt1_wca_3d_1dbc"] = deck("GEOM3_PLANE_ROUGH_3D", dict(wca3d, **{"L1D_bc": "1 1.0"}), surfaces=surf3d)
     # 1-D HS5 with the zero-dimensional-crossover Rosenfeld functional (FMT2) and the
     # White-Bear functional with the same vector correction (FMT4)
     c["hs1d_fmt2"] = deck("HS5_FMT1_1D", {"Type_func (": "1 0"})
@@ -129,6 +132,12 @@ def cases():
     # zone coarser than the residual near the wall)
     c["hs1d_zones"] = deck("HS6_FMT1_1D")
     c["hs1d_jaczones"] = deck("HS7_FMT1_1D")
+    # the LJ1 fluid (FMT1 + WCA at a 9-3 wall) with HS6's four zones at 2, 4, 5 sigma from the wall, the mean field
+    # as its own unknown and summed into the Euler-Lagrange rows (ATTInA22Block = 1)
+    zones = {"Nzone (Coarsens": "4", "Rmax_zone": "2. 4. 5.", "Mesh_coarsening": "1"}
+    c["lj1d_zones"] = deck("LJ1_FMT1_WCA_1D", dict(zones, **mf))
+    c["lj1d_zones_a22"] = deck("LJ1_FMT1_WCA_1D", dict(zones, **{"ATTInA22Block": "0 50 0 1 0",
+                                                                 "L_Schur": SCHUR_LINSOLVE}))
     # MIX1's hard wall (boundary weights, one surface list per component size) with three and four hard-sphere
     # components of different diameters (FMT1, and FMT3 for the four)
     mix = {"Mass[i]": "1. 1. 1. 1.", "Charge[i]": "0. 0. 0. 0.", "Pol[i]": "0. 0. 0. 0.",

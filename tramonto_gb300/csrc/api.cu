@@ -160,12 +160,14 @@ struct Ctx : tgpu_ctx {
   // quadrature zones / mesh coarsening: per-node zone (>= 0) or averaging axis (< 0), the stencils of
   // zones >= 1, the averaged rows and the prolongation onto coarsened nodes
   int nzone = 1;
-  std::vector<int> h_zone;
-  std::vector<double> h_rb_bulk;
+  std::vector<int> h_zone;       // Mesh_coarsen_flag as given (zones, averaging axes, 1-D boundary / bulk / PB flags)
+  std::vector<double> h_rb_bulk; // Rhobar_b beyond IN_BULK boundaries: [low side][high side]
+  int dim_1dbc = 0;              // L1D_bc: nodes flagged kFlag1dbc copy the line through the origin along it
   std::vector<tgpu::DevStencil> zsten[tgpu::kMaxZone][3];
-  int *d_zone = nullptr;
+  int *d_zone = nullptr;         // the stencil zone of every node (BULK/PB nodes 0, averaged rows < 0)
+  signed char *d_rowkind = nullptr;   // BULK_ZONE (1) / PB_ZONE (2) Euler-Lagrange rows, when any
   double *d_zbuf = nullptr;      // [nrb + ncomp][N] one zone's sums
-  double *d_cbulk = nullptr;     // [nunk] value beyond an IN_BULK boundary per unknown
+  double *d_cbulk = nullptr;     // [2][nunk] value beyond the low / high IN_BULK boundary per unknown
   double *d_cscr = nullptr;      // [nunk][N] prolonged copies
   double *d_cscr2 = nullptr;     // [nunk][N] the adjoint's folded right-hand side
   tgpu::CoarseRows cr{};
@@ -1050,7 +1052,7 @@ const double *prolonged(Ctx *c, const double *v, int nrows)
 {
   if (!c->coarse()) return v;
   copy_d(c, c->d_cscr, v, (size_t)nrows * c->dg.N);
-  tgpu::launch_prolong(c->d_cscr, 0, nrows, c->dg.N, c->cr, nullptr, c->stream);
+  tgpu::launch_prolong(c->d_cscr, 0, nrows, c->dg.nunk, c->dg.N, c->cr, nullptr, c->stream);
   c->stats.kernel_launches++;
   return c->d_cscr;
 }
@@ -1063,7 +1065,7 @@ void schur_device(Ctx *c, const double *d_v2, double *d_y2)
   const bool f32 = prod_f32(c);
   const double *v2 = prolonged(c, d_v2, g.ncomp);
   forward_pass(c, v2, c->pads.rho_jac, f32);
-  if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.N, c->cr, nullptr, c->stream);
+  if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.nunk, g.N, c->cr, nullptr, c->stream);
   tgpu::launch_schur_local(c->d_x, c->d_conv, c->d_chan, c->d_ymf, hess_coef(c), c->stream, f32);
   transpose_pass(c, c->pads.tr_jac, f32);
   tgpu::launch_schur_combine(c->d_x, c->d_vext, c->d_zero, v2, c->d_tr, c->d_ymf, d_y2, c->stream);
@@ -1106,7 +1108,7 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
   const double *b = d_b;
   if (c->coarse()) {   // block-1 right-hand sides interpolated onto the coarsened nodes
     copy_d(c, c->d_cscr, d_b, (size_t)g.nunk * g.N);
-    tgpu::launch_prolong(c->d_cscr, g.first_rb, g.nunk - g.ncomp, g.N, c->cr, nullptr, c->stream);
+    tgpu::launch_prolong(c->d_cscr, g.first_rb, g.nunk - g.ncomp, g.nunk, g.N, c->cr, nullptr, c->stream);
     b = c->d_cscr;
   }
   tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
@@ -1125,7 +1127,7 @@ void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx
   const double *x2 = prolonged(c, d_x2, g.ncomp);
   forward_pass(c, x2, c->pads.rho_jac, prod_f32(c));
   tgpu::launch_x1(d_b, c->d_conv, x2, d_dx, c->stream);
-  if (c->coarse()) tgpu::launch_prolong(d_dx, 0, g.nunk, g.N, c->cr, nullptr, c->stream);
+  if (c->coarse()) tgpu::launch_prolong(d_dx, 0, g.nunk, g.nunk, g.N, c->cr, nullptr, c->stream);
   c->stats.kernel_launches++;
 }
 
@@ -1133,7 +1135,7 @@ void schur_x1_device(Ctx *c, const double *d_b, const double *d_x2, double *d_dx
 void coarse_state(Ctx *c, double *d_x)
 {
   if (!c->coarse()) return;
-  tgpu::launch_prolong(d_x, 0, c->dg.nunk, c->dg.N, c->cr, c->d_cbulk, c->stream);
+  tgpu::launch_prolong(d_x, 0, c->dg.nunk, c->dg.nunk, c->dg.N, c->cr, c->d_cbulk, c->stream);
   c->stats.kernel_launches++;
 }
 
@@ -1648,6 +1650,18 @@ void a22_mf_sums(Ctx *c, const double *x, bool jac, double *mf)
       double *o[1] = {mf + (long)ic * N};
       conv(c, jc, 1, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, o, 1, false);
     }
+  // nodes of the coarser quadrature zones take their own zone's sums (load_mean_field with the node's
+  // zone, src/dft_fill_EL.c:156-159)
+  for (int z = 1; z < c->nzone; z++) {
+    ck(cudaMemsetAsync(c->d_zbuf, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+    for (int jc = 0; jc < g.ncomp; jc++)
+      for (int ic = 0; ic < g.ncomp; ic++) {
+        double *o[1] = {c->d_zbuf + (long)ic * N};
+        conv(c, jc, 1, c->zsten[z][TGPU_STEN_UATT][ic + g.ncomp * jc], false, o, 1, false);
+      }
+    tgpu::launch_zone_merge(c->d_zbuf, mf, g.ncomp, N, c->d_zone, z, c->stream);
+    c->stats.kernel_launches++;
+  }
   if (g.hard_surf && !c->hw_targets.empty()) {
     tgpu::launch_hw_correct(x + (long)g.first_rho * N, N, 0, nullptr, nullptr, c->sten[TGPU_STEN_UATT].data(),
                             g.ncomp, false, true, c->d_hw_targets, (int)c->hw_targets.size(), c->d_zero,
@@ -1668,9 +1682,13 @@ const double *a22_in(Ctx *c, const double *ext, int how, int slot)
   copy_d(c, in, ext, (size_t)c->nunk_ext * N);
   double *mf = in + (long)g.first_mf * N;
   if (how == A22_ZERO) ck(cudaMemsetAsync(mf, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
-  else if (how == A22_EL)   // C^T w: the EL rows, except zero-density rows (they hold no mean field)
+  else if (how == A22_EL) {  // C^T w: the EL rows, except rows that hold no mean field (zero-density rows,
+                            // averaged rows of coarsened nodes)
     tgpu::launch_mask_rows(mf, ext, c->d_vext, c->d_zero, g.first_rho, g.ncomp, 0, c->stream);
-  else a22_mf_sums(c, in, how == A22_JAC_SUMS, mf);
+    if (c->coarse()) tgpu::launch_zero_nodes(mf, g.ncomp, N, c->cr, c->stream);
+  } else {
+    a22_mf_sums(c, in, how == A22_JAC_SUMS, mf);
+  }
   return in;
 }
 
@@ -1884,10 +1902,11 @@ DevStencil::Lines build_lines(const DevStencil &st, const std::vector<double> &c
 // ---- mesh coarsening: averaged rows and the prolongation onto coarsened nodes ----
 
 // One step along dimension d (s = +1 or -1) from a node under the boundary conditions: a node index,
-// -1 beyond an IN_BULK boundary or -2 inside a wall (offset_to_node_box, src/dft_mesh_lib.c:203-297,
-// for unit offsets).
+// -1 beyond an IN_BULK boundary (-3 beyond the high one of a phase interface, the RTF state) or -2 inside
+// a wall (offset_to_node_box, src/dft_mesh_lib.c:203-297, for unit offsets).
 long step_node(const Ctx *c, long node, int d, int s)
 {
+  const long bulk_hi = c->g.interface == 2 ? tgpu::kSentBulkHi : tgpu::kSentBulk;
   const tgpu::DevGeom &dg = c->dg;
   long ijk[3] = {node % dg.nx[0], (node / dg.nx[0]) % dg.nx[1], node / ((long)dg.nx[0] * dg.nx[1])};
   const long n = dg.nx[d];
@@ -1898,7 +1917,7 @@ long step_node(const Ctx *c, long node, int d, int s)
     if (bl == TGPU_BC_IN_WALL) return -2;
     q = bl == TGPU_BC_REFLECT ? -q : q + n;
   } else if (q >= n) {
-    if (br == TGPU_BC_IN_BULK) return -1;
+    if (br == TGPU_BC_IN_BULK) return bulk_hi;
     if (br == TGPU_BC_IN_WALL) return -2;
     q = br == TGPU_BC_REFLECT ? 2 * (n - 1) - q : q - n;
   }
@@ -1907,18 +1926,64 @@ long step_node(const Ctx *c, long node, int d, int s)
   return ijk[0] + dg.nx[0] * (ijk[1] + (long)dg.nx[1] * ijk[2]);
 }
 
+// Flags of Mesh_coarsen_flag beyond zones and averaging axes (src/dft_mesh.c:2788-2850)
+constexpr int kFlagPB = TGPU_FLAG_PB, kFlagBulk = TGPU_FLAG_BULK, kFlag1dbc = TGPU_FLAG_1DBC;
+
+// a node whose rows are not filled but follow other nodes: averaged along an axis, or the 1-D boundary copy
+inline bool coarse_flag(int f) { return f == kFlag1dbc || (f < 0 && f >= -3); }
+
+// the node on the line through the origin along dim_1dbc with the same coordinate along it
+// (load_coarse_node_1dim, src/dft_fill_coarse.c:43-45)
+long line_node(const Ctx *c, long node)
+{
+  const tgpu::DevGeom &dg = c->dg;
+  const long ijk[3] = {node % dg.nx[0], (node / dg.nx[0]) % dg.nx[1], node / ((long)dg.nx[0] * dg.nx[1])};
+  long jk[3] = {0, 0, 0};
+  jk[c->dim_1dbc] = ijk[c->dim_1dbc];
+  return jk[0] + dg.nx[0] * (jk[1] + (long)dg.nx[1] * jk[2]);
+}
+
 // locate_neighbor_unks (src/dft_fill_coarse.c:103-123): the averaged row's terms (column, weight a) of a
 // coarsened node; with two zones a coarsened neighbour gives way to its own neighbours.  Wall columns
-// (value 0, no Jacobian entry) are left out.
+// (value 0, no Jacobian entry) are left out.  With two zones the reference recurses into a neighbour with
+// a 1-D boundary, BULK_ZONE or PB_ZONE flag as if the flag were an axis (reading past its offset table), so
+// that pattern is refused.
 void coarse_row_terms(const Ctx *c, long node, double a, int depth, std::vector<std::pair<long, double>> &out)
 {
   if (depth > 8) throw Error(TGPU_ERR_UNSUPPORTED, "coarsening pattern");
   const int d = -c->h_zone[node] - 1;
   for (int s : {1, -1}) {
     const long j = step_node(c, node, d, s);
-    if (j >= 0 && c->h_zone[j] < 0 && c->nzone == 2) coarse_row_terms(c, j, 0.5 * a, depth + 1, out);
-    else if (j != -2) out.push_back({j, a});
+    if (j >= 0 && c->h_zone[j] < 0 && c->nzone == 2) {
+      if (c->h_zone[j] < -3)
+        throw Error(TGPU_ERR_UNSUPPORTED, "with two zones, an averaged node next to a 1-D boundary, BULK_ZONE or "
+                                          "PB_ZONE node");
+      coarse_row_terms(c, j, 0.5 * a, depth + 1, out);
+    } else if (j != -2) {
+      out.push_back({j, a});
+    }
   }
+}
+
+// Values beyond the low and the high IN_BULK boundary per unknown (constant_boundary, src/dft_utils.c:
+// 89-110): the bulk densities (Rho_b, or Rho_b_LBB / _RTF of a phase interface) and Rhobar_b; mean-field
+// unknowns 0 (the reference leaves them undefined there).  Called again when the bulk state moves.
+void upload_cbulk(Ctx *c)
+{
+  const tgpu::DevGeom &dg = c->dg;
+  const tgpu_geometry &g = c->g;
+  const int nrb = dg.nrb;
+  std::vector<double> cb(2 * (size_t)dg.nunk, 0.0);
+  for (int side = 0; side < 2; side++) {
+    double *o = cb.data() + (size_t)side * dg.nunk;
+    for (int ic = 0; ic < dg.ncomp; ic++)
+      o[dg.first_rho + ic] = g.interface == 2 ? (side ? g.rho_b_rtf[ic] : g.rho_b_lbb[ic]) : g.rho_b[ic];
+    const size_t off = c->h_rb_bulk.size() >= 2 * (size_t)nrb ? (size_t)side * nrb : 0;
+    for (int k = 0; k < nrb && off + k < c->h_rb_bulk.size(); k++) o[dg.first_rb + k] = c->h_rb_bulk[off + k];
+  }
+  if (!c->d_cbulk) c->d_cbulk = dalloc<double>(cb.size());
+  ck(cudaMemcpyAsync(c->d_cbulk, cb.data(), cb.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
+  ck(cudaStreamSynchronize(c->stream), "sync");
 }
 
 // The values at coarsened nodes that satisfy every averaged row, as weights on the other nodes (and on the
@@ -1931,20 +1996,28 @@ void build_coarse(Ctx *c)
   const long N = dg.N;
   std::vector<int> cnode, pos(N, -1);
   for (long i = 0; i < N; i++)
-    if (c->h_zone[i] < 0) {
+    if (coarse_flag(c->h_zone[i])) {
       pos[i] = (int)cnode.size();
       cnode.push_back((int)i);
     }
   const int nc = (int)cnode.size();
   c->cr.ncoarse = nc;
   if (nc == 0) return;
-  // averaged rows
+  // averaged rows fac (x_c - sum_k a_k x_k), and the 1-D boundary rows x_c - x_line (fac 1 on every unknown)
   std::vector<int> rptr(1, 0);
   std::vector<long> rcol;
   std::vector<double> ra;
+  std::vector<signed char> ckind(nc, 0);
   for (int k = 0; k < nc; k++) {
     std::vector<std::pair<long, double>> t;
-    coarse_row_terms(c, cnode[k], 0.5, 0, t);
+    if (c->h_zone[cnode[k]] == kFlag1dbc) {
+      const long ln = line_node(c, cnode[k]);
+      if (c->h_zone[ln] == kFlag1dbc) throw Error(TGPU_ERR_ARG, "a 1-D boundary node on its own line");
+      t.push_back({ln, 1.0});
+      ckind[k] = 1;
+    } else {
+      coarse_row_terms(c, cnode[k], 0.5, 0, t);
+    }
     for (auto &e : t) {
       rcol.push_back(e.first);
       ra.push_back(e.second);
@@ -1958,6 +2031,18 @@ void build_coarse(Ctx *c)
   std::function<void(int)> solve = [&](int k0) {
     if (state[k0] == 2) return;
     if (state[k0] == 1) throw Error(TGPU_ERR_UNSUPPORTED, "cyclic coarsening pattern");
+    if (c->h_zone[cnode[k0]] == kFlag1dbc) {   // the line node's value (its own prolongation when averaged)
+      const long ln = line_node(c, cnode[k0]);
+      state[k0] = 1;
+      if (coarse_flag(c->h_zone[ln])) {
+        solve(pos[ln]);
+        expr[k0] = expr[pos[ln]];
+      } else {
+        expr[k0].assign(1, {ln, 1.0});
+      }
+      state[k0] = 2;
+      return;
+    }
     const int flag = c->h_zone[cnode[k0]], d = -flag - 1;
     std::vector<int> run(1, k0);
     std::map<int, int> in_run{{k0, 0}};
@@ -1985,7 +2070,7 @@ void build_coarse(Ctx *c)
           A[(size_t)r * m + in_run.at(pos[j])] -= 0.5;
           continue;
         }
-        if (j >= 0 && c->h_zone[j] < 0) solve(pos[j]);
+        if (j >= 0 && coarse_flag(c->h_zone[j])) solve(pos[j]);
         auto it = ext_idx.find(j);
         int e;
         if (it == ext_idx.end()) {
@@ -2027,7 +2112,7 @@ void build_coarse(Ctx *c)
         const double w = X[(size_t)r * E + e] * inv;
         if (w == 0.0) continue;
         const long j = ext[e];
-        if (j >= 0 && c->h_zone[j] < 0)
+        if (j >= 0 && coarse_flag(c->h_zone[j]))
           for (auto &t : expr[pos[j]]) acc[t.first] += w * t.second;
         else
           acc[j] += w;
@@ -2054,11 +2139,8 @@ void build_coarse(Ctx *c)
   c->cr.d_pptr = upload(pptr, c->stream);
   c->cr.d_pcol = upload(pcol, c->stream);
   c->cr.d_pw = upload(pw, c->stream);
-  // value beyond an IN_BULK boundary per unknown (constant_boundary, src/dft_utils.c:89-110)
-  std::vector<double> cb((size_t)dg.nunk, 0.0);
-  for (int ic = 0; ic < dg.ncomp; ic++) cb[(size_t)dg.first_rho + ic] = c->g.rho_b[ic];
-  for (int k = 0; k < dg.nrb; k++) cb[(size_t)dg.first_rb + k] = c->h_rb_bulk[k];
-  c->d_cbulk = upload(cb, c->stream);
+  c->cr.d_kind = upload(ckind, c->stream);
+  upload_cbulk(c);
   c->d_cscr = dalloc<double>((size_t)dg.nunk * N);
 }
 
@@ -2401,7 +2483,7 @@ int tgpu_destroy(tgpu_handle h)
         }
     dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2); dfree(c->d_hcoef); dfree(c->d_domain);
     dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
-    dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw);
+    dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw); dfree(c->cr.d_kind); dfree(c->d_rowkind);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
     tgpu::tc_free_slab(c->tcslab);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);
@@ -2452,13 +2534,28 @@ int tgpu_set_zones(tgpu_handle h, int nzone, const int *flag, const double *rb_b
     if (nzone < 1 || nzone > tgpu::kMaxZone) throw Error(TGPU_ERR_ARG, "number of zones");
     if (!flag || !rb_bulk) throw Error(TGPU_ERR_ARG, "null zone arrays");
     const long N = c->dg.N;
-    for (long i = 0; i < N; i++)
-      if (flag[i] >= nzone || flag[i] < -c->g.ndim) throw Error(TGPU_ERR_ARG, "zone flag");
+    for (long i = 0; i < N; i++) {
+      const int f = flag[i];
+      if (!((f >= -c->g.ndim && f < nzone) || f == kFlag1dbc || f == kFlagBulk || f == kFlagPB))
+        throw Error(TGPU_ERR_ARG, "zone flag");
+    }
     c->nzone = nzone;
     c->h_zone.assign(flag, flag + N);
-    c->h_rb_bulk.assign(rb_bulk, rb_bulk + 4 + 2 * c->g.ndim);
+    const int nrb = 4 + 2 * c->g.ndim;
+    c->h_rb_bulk.assign(rb_bulk, rb_bulk + (c->g.interface == 2 ? 2 : 1) * nrb);
     for (int z = 1; z < nzone; z++)
       for (int t = 0; t < 3; t++) c->zsten[z][t].resize(c->sten[t].size());
+    return TGPU_OK;
+  });
+}
+
+int tgpu_set_1d_boundary(tgpu_handle h, int dim)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    if (c->finalized) throw Error(TGPU_ERR_STATE, "zones are fixed after tgpu_finalize");
+    if (dim < 0 || dim >= c->g.ndim) throw Error(TGPU_ERR_ARG, "dimension");
+    c->dim_1dbc = dim;
     return TGPU_OK;
   });
 }
@@ -2516,6 +2613,20 @@ int tgpu_set_bulk_state(tgpu_handle h, const double *rho_b, const double *betamu
       g.betamu_att[ic] = dg.betamu_att[ic] = betamu_att[ic];
     }
     for (int k = 0; k < 4; k++) g.dphi_bulk[k] = dg.dphi_bulk[k] = dphi_bulk[k];
+    if (c->coarse() && g.interface != 2) {
+      // Rhobar_b of the new bulk state for the averaged rows next to IN_BULK boundaries (rhobar_icomp,
+      // src/dft_thermo_hs.c:292-311; the diameter from 1/R)
+      std::fill(c->h_rb_bulk.begin(), c->h_rb_bulk.end(), 0.0);
+      for (int ic = 0; ic < g.ncomp; ic++) {
+        const double d = 2.0 / g.inv_rad[ic], vol = M_PI * d * d * d / 6.0, area = M_PI * d * d;
+        const double f = g.fac_overlap[ic] * g.rho_b[ic];
+        c->h_rb_bulk[0] += f * vol;
+        c->h_rb_bulk[1] += f * area;
+        c->h_rb_bulk[2] += f * area * g.inv_4pir[ic];
+        c->h_rb_bulk[3] += f * area * g.inv_4pirsq[ic];
+      }
+      upload_cbulk(c);
+    }
     const std::vector<double> br = bulk_values_rho(g), bt = bulk_values_tr(g);
     ck(cudaMemcpyAsync(c->pads.rho_res.bulk, br.data(), br.size() * sizeof(double), cudaMemcpyHostToDevice,
                        c->stream), "h2d");
@@ -2577,8 +2688,6 @@ int tgpu_finalize(tgpu_handle h)
           throw Error(TGPU_ERR_STATE, "hard surfaces need the attraction stencils' corner weights");
     if (g.hard_surf && c->h_bnodes.empty()) throw Error(TGPU_ERR_STATE, "hard surfaces need tgpu_set_hard_wall");
     if (c->nzone > 1) {
-      if (g.interface) throw Error(TGPU_ERR_UNSUPPORTED, "mesh coarsening with a phase interface");
-      if (c->a22) throw Error(TGPU_ERR_UNSUPPORTED, "mesh coarsening with ATTInA22Block = 1");
       for (int z = 1; z < c->nzone; z++)
         for (int t = 0; t < 3; t++) {
           if (t == TGPU_STEN_UATT && !g.attraction) continue;
@@ -2589,12 +2698,28 @@ int tgpu_finalize(tgpu_handle h)
     }
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     build_device_tables(c);
-    if (c->nzone > 1) {
+    if (!c->h_zone.empty()) {
       for (int t : c->hw_targets)
         if (c->h_zone[t] > 0)
           throw Error(TGPU_ERR_UNSUPPORTED, "hard-wall boundary nodes within reach of a coarser zone's stencils");
-      c->d_zone = upload(c->h_zone, c->stream);
-      c->d_zbuf = dalloc<double>((size_t)(c->dg.nrb + c->dg.ncomp) * c->dg.N);
+      // stencil zone per node: BULK_ZONE / PB_ZONE nodes fill their other rows with zone 0's stencils (the
+      // reference indexes its stencil table with the negative flag there); their Euler-Lagrange rows by kind
+      std::vector<int> zone(c->h_zone);
+      std::vector<signed char> kind(zone.size(), 0);
+      bool any_kind = false;
+      for (size_t i = 0; i < zone.size(); i++)
+        if (zone[i] == kFlagBulk || zone[i] == kFlagPB) {
+          kind[i] = zone[i] == kFlagBulk ? 1 : 2;
+          zone[i] = 0;
+          any_kind = true;
+        }
+      c->d_zone = upload(zone, c->stream);
+      if (any_kind) {
+        c->d_rowkind = upload(kind, c->stream);
+        c->dg.rowkind = c->d_rowkind;
+        tgpu::upload_geom(c->dg, c->stream);
+      }
+      if (c->nzone > 1) c->d_zbuf = dalloc<double>((size_t)(c->dg.nrb + c->dg.ncomp) * c->dg.N);
       build_coarse(c);
       ck(cudaStreamSynchronize(c->stream), "sync");
     }

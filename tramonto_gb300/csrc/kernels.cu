@@ -794,12 +794,44 @@ void launch_fmt_local(const double *x, double *chan, cudaStream_t s, unsigned *d
 // only (fill_constant_density, src/dft_fill_EL.c:286-305)
 __device__ __forceinline__ bool pin_row(int ic, long i) { return ic == 0 && i == c_g.pin_node; }
 
-// Euler-Lagrange rows without nonlocal couplings: zero-density rows (R = rho, J = 1) and the pinned row
+__device__ __forceinline__ int row_kind(long i) { return c_g.rowkind ? c_g.rowkind[i] : 0; }
+
+// Euler-Lagrange rows without nonlocal couplings: zero-density rows (R = rho, J = 1), the pinned row and
+// the rows of BULK_ZONE / PB_ZONE nodes
 __device__ __forceinline__ bool zero_row(const double *vext, const signed char *zero, int ic, long i)
 {
   if (pin_row(ic, i)) return true;
   const long k = (long)ic * c_g.N + i;
-  return zero[k] || vext[k] == c_g.vext_max;
+  return zero[k] || vext[k] == c_g.vext_max || row_kind(i) != 0;
+}
+
+// Of those, the rows R = ln rho - ln c with J = 1/rho: the pinned row (c = pin_value), a BULK_ZONE node's
+// (c = rho_b: fill_bulk_density, src/dft_fill_EL.c:69-80, 265-284) and a PB_ZONE node's (the ideal gas in
+// the external field, chemical potential without the excess terms and no hard-sphere or attraction terms:
+// ln c = -mu0 - V_ext, src/dft_fill_EL.c:132-161, 405-410); zero-density rows come first
+__device__ __forceinline__ bool log_row(const double *vext, const signed char *zero, int ic, long i)
+{
+  if (pin_row(ic, i)) return true;
+  const long k = (long)ic * c_g.N + i;
+  return !(zero[k] || vext[k] == c_g.vext_max) && row_kind(i) != 0;
+}
+
+__device__ __forceinline__ double log_row_c(const double *vext, int ic, long i)
+{
+  const int kind = row_kind(i);   // the bulk and PB rows come before the pinned row (src/dft_fill_EL.c:69-97)
+  if (kind == 1) return log(c_g.rho_b[ic]);
+  if (kind == 2) {
+    const double mu0 = c_g.interface ? -c_g.betamu_if[ic] : -log(c_g.rho_b[ic]);
+    return -(mu0 + vext[(long)ic * c_g.N + i]);
+  }
+  return log(c_g.pin_value);
+}
+
+// Euler-Lagrange rows that hold +V_ext: the full rows and the PB_ZONE rows
+__device__ __forceinline__ bool vext_row(const double *vext, const signed char *zero, int ic, long i)
+{
+  if (!zero_row(vext, zero, ic, i)) return true;
+  return row_kind(i) == 2 && log_row(vext, zero, ic, i);
 }
 
 // dependent weighted densities (one particle size): n1 = n2/4piR, n0 = n2/4piR^2, V1 = V2/4piR
@@ -825,7 +857,12 @@ __global__ void k_assemble(const double *__restrict__ x, const double *__restric
       const double xi = x[(long)iu * N + i];
       double r;
       if (zero_row(vext, zero, ic, i)) {
-        r = pin_row(ic, i) ? log(xi) - log(c_g.pin_value) : xi;
+        if (log_row(vext, zero, ic, i)) {
+          if (domain && xi <= 0.0) atomicOr(domain, kDomainRho);
+          r = log(xi) - log_row_c(vext, ic, i);
+        } else {
+          r = xi;
+        }
       } else {
         double mu;
         if (c_g.interface) {
@@ -937,7 +974,7 @@ __global__ void k_schur_combine(const double *__restrict__ x, const double *__re
     for (int ic = 0; ic < c_g.ncomp; ic++) {
       const long k = (long)ic * N + i;
       if (zero_row(vext, zero, ic, i)) {
-        y2[k] = pin_row(ic, i) ? v2[k] / x[(long)(c_g.first_rho + ic) * N + i] : v2[k];
+        y2[k] = log_row(vext, zero, ic, i) ? v2[k] / x[(long)(c_g.first_rho + ic) * N + i] : v2[k];
       } else {
         double a21y = tr[k];
         if (c_g.attraction) a21y += ymf[k];
@@ -962,7 +999,7 @@ __global__ void k_jv_combine(const double *__restrict__ x, const double *__restr
       const int iu = c_g.first_rho + ic;
       const long k = (long)iu * N + i;
       if (zero_row(vext, zero, ic, i)) {
-        out[k] = pin_row(ic, i) ? v[k] / x[k] : v[k];
+        out[k] = log_row(vext, zero, ic, i) ? v[k] / x[k] : v[k];
       } else {
         double r = v[k] / x[k] + tr[(long)ic * N + i];
         if (c_g.attraction) r += v[(long)(c_g.first_mf + ic) * N + i];
@@ -1139,7 +1176,7 @@ __global__ void k_jtv_local(const double *__restrict__ x, const double *__restri
       const bool zr = zero_row(vext, zero, ic, i);
       const double wel = zr ? 0.0 : w[kr];
       // density column: transposed sums already in out; add the A22 diagonal
-      out[kr] += (zr && !pin_row(ic, i)) ? w[kr] : w[kr] / x[kr];
+      out[kr] += (zr && !log_row(vext, zero, ic, i)) ? w[kr] : w[kr] / x[kr];
       if (c_g.attraction) {
         const long km = (long)(c_g.first_mf + ic) * N + i;
         out[km] = -w[km] + wel;
@@ -1618,8 +1655,9 @@ __global__ void k_precond(const double *__restrict__ x, const double *__restrict
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     for (int ic = 0; ic < c_g.ncomp; ic++) {
       const long k = (long)ic * N + i;
-      out[k] = (zero_row(vext, zero, ic, i) && !pin_row(ic, i)) ? in[k]
-                                                                 : in[k] * x[(long)(c_g.first_rho + ic) * N + i];
+      out[k] = (zero_row(vext, zero, ic, i) && !log_row(vext, zero, ic, i))
+                   ? in[k]
+                   : in[k] * x[(long)(c_g.first_rho + ic) * N + i];
     }
 }
 
@@ -1893,7 +1931,8 @@ void launch_objective_grad(const double *x, const double *vext, const double *sa
   k_objective_grad<<<1184, kThreads, 0, s>>>(x, vext, satt, wf, wb, oc, kind, icomp, gx, gv, chan);
 }
 
-// dF/dV_ext = dF/dV|_x - lambda on the Euler-Lagrange rows (which hold +V_ext), 0 on zero-density rows
+// dF/dV_ext = dF/dV|_x - lambda on the Euler-Lagrange rows that hold +V_ext (full rows and PB_ZONE rows),
+// dF/dV|_x elsewhere
 __global__ void k_vext_sens(const double *__restrict__ lam, const double *__restrict__ gv,
                             const double *__restrict__ vext, const signed char *__restrict__ zero,
                             double *__restrict__ out)
@@ -1902,7 +1941,7 @@ __global__ void k_vext_sens(const double *__restrict__ lam, const double *__rest
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     for (int ic = 0; ic < c_g.ncomp; ic++) {
       const long k = (long)ic * N + i;
-      out[k] = zero_row(vext, zero, ic, i) ? gv[k] : gv[k] - lam[(long)(c_g.first_rho + ic) * N + i];
+      out[k] = vext_row(vext, zero, ic, i) ? gv[k] - lam[(long)(c_g.first_rho + ic) * N + i] : gv[k];
     }
 }
 

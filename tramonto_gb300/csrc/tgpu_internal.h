@@ -48,6 +48,8 @@ struct DevGeom {
   double betamu_if[kMaxC];
   long pin_node;                       // first component's density held at pin_value there (-1: none)
   double pin_value;
+  const signed char *rowkind;          // per node: 0, or the Euler-Lagrange row of a BULK_ZONE (1) / PB_ZONE (2)
+                                       // node (nullptr: none)
   double esize[3];
   double rho_b[kMaxC], betamu_hs_ex[kMaxC], betamu_att[kMaxC];
   double inv_rad[kMaxC], inv_4pir[kMaxC], inv_4pirsq[kMaxC], fac[kMaxC];
@@ -131,11 +133,12 @@ struct CoarseRows {
   int ncoarse = 0;
   int *d_node = nullptr;                  // [ncoarse] node index of each coarsened node
   int *d_rptr = nullptr;                  // row terms: [ncoarse + 1]
-  long *d_rcol = nullptr;                 // node index, or -1 (bulk beyond an IN_BULK boundary)
+  long *d_rcol = nullptr;                 // node index, or -1 / -3 (bulk beyond the low / high IN_BULK boundary)
   double *d_ra = nullptr;                 // weights a_k > 0 of fac (x_c - sum_k a_k x_k)
   int *d_pptr = nullptr;                  // prolongation x_c = sum_e p_e x_col: [ncoarse + 1]
   long *d_pcol = nullptr;
   double *d_pw = nullptr;
+  signed char *d_kind = nullptr;          // [ncoarse] 1: a 1-D boundary row x_c - x_line (fac 1 on every unknown)
 };
 
 struct ObjConst {
@@ -567,7 +570,8 @@ void launch_coarse_rows(const double *in, double *out, int nunk, int first_rho, 
                         const CoarseRows &cr, const double *bulk, cudaStream_t s);
 void launch_coarse_rows_t(const double *w, double *out, int nunk, int first_rho, int ncomp, long N,
                           const CoarseRows &cr, cudaStream_t s);
-void launch_prolong(double *vec, int row0, int nrows, long N, const CoarseRows &cr, const double *bulk, cudaStream_t s);
+void launch_prolong(double *vec, int row0, int nrows, int nunk, long N, const CoarseRows &cr, const double *bulk,
+                    cudaStream_t s);
 void launch_prolong_t(double *vec, int row0, int nrows, long N, const CoarseRows &cr, cudaStream_t s);
 void launch_zero_nodes(double *vec, int nrows, long N, const CoarseRows &cr, cudaStream_t s);
 void launch_mask_rows(double *out, const double *w, const double *vext, const signed char *zero, int first, int nrows,

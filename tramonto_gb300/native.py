@@ -87,7 +87,7 @@ def load(build_if_missing: bool = False):
         "tgpu_create": [C.POINTER(Geometry), C.c_int, C.POINTER(vp)],
         "tgpu_destroy": [vp],
         "tgpu_set_stencil": [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp],
-        "tgpu_set_zones": [vp, C.c_int, vp, vp],
+        "tgpu_set_zones": [vp, C.c_int, vp, vp], "tgpu_set_1d_boundary": [vp, C.c_int],
         "tgpu_set_fft_threshold": [vp, C.c_int],
         "tgpu_set_fft32_policy": [vp, C.c_int],
         "tgpu_fft32_choice": [vp, C.c_int, C.c_int, ip, dp],
@@ -175,8 +175,27 @@ def _ptr(a):
 
 
 def mesh_coarsened(p: Problem) -> bool:
-    """Quadrature zones that change the residual: Mesh_coarsening on, walls present, more than one zone."""
-    return bool(p.nzone > 1 and p.mesh_coarsening and p.nwall > 0 and p.zone_flag is not None)
+    """Flags that change the residual, read as the fill reads them: with Mesh_coarsening on and walls present, or
+    with L1D_bc (src/dft_fill_main.c:120)."""
+    if p.zone_flag is None:
+        return False
+    return bool((p.mesh_coarsening and p.nwall > 0) or p.l1d_bc)
+
+
+def _rhobar_bulk(p: Problem):
+    """Rhobar_b beyond IN_BULK boundaries in solution order; [LBB, RTF] with a phase interface (rhobar_icomp,
+    src/dft_thermo_hs.c:292-311)."""
+    nrb = p.nrb
+    if p.interface != 2:
+        return np.ascontiguousarray(np.asarray(p.rhobar_bc, np.float64)[:nrb])
+    out = np.zeros((2, nrb))
+    for side, rho in enumerate((p.rho_b_lbb, p.rho_b_rtf)):
+        for ic in range(p.ncomp):
+            d = float(p.hs_diam[ic])
+            vol, area = np.pi * d * d * d / 6.0, np.pi * d * d
+            f = float(p.fac_overlap[ic]) * float(rho[ic])
+            out[side, :4] += [f * vol, f * area, f * area * p.inv_4pir[ic], f * area * p.inv_4pirsq[ic]]
+    return np.ascontiguousarray(out.reshape(-1))
 
 
 class Solver:
@@ -208,8 +227,10 @@ class Solver:
                 # the fill reads the zones only with Mesh_coarsening on and walls present
                 # (src/dft_fill_main.c:120); the Jacobian is the residual's own derivative
                 flag = np.ascontiguousarray(p.zone_flag, np.int32)
-                rbb = np.ascontiguousarray(np.asarray(p.rhobar_bc, np.float64)[:p.nrb])
-                _check(lib.tgpu_set_zones(self.h, int(p.nzone), _ptr(flag), _ptr(rbb)), lib)
+                rbb = _rhobar_bulk(p)
+                if p.l1d_bc:
+                    _check(lib.tgpu_set_1d_boundary(self.h, int(p.dim_1dbc)), lib)
+                _check(lib.tgpu_set_zones(self.h, int(max(p.nzone, 1)), _ptr(flag), _ptr(rbb)), lib)
                 for zone, tabs in sorted(p.zone_stencils.items()):
                     for (t, idx), (off, w, hw) in sorted(tabs.items()):
                         off = np.ascontiguousarray(off, np.int16)

@@ -64,6 +64,8 @@ class Problem:
     coarser_jac: int = 0
     nwall: int = 0
     zone_flag: np.ndarray = None
+    l1d_bc: int = 0                  # L1D_bc: nodes flagged -999 copy the line through the origin along dim_1dbc
+    dim_1dbc: int = 0
     zone_stencils: dict = None
     rhobar_bc: np.ndarray = None
     vext: np.ndarray = None        # [ncomp][N]
@@ -147,6 +149,8 @@ def from_golden(z) -> Problem:
         p.nzone, p.mesh_coarsening, p.coarser_jac = int(ints[25]), int(ints[37]), int(ints[38])
     if "coarsen_flag" in z.files:
         p.zone_flag = np.asarray(z["coarsen_flag"], np.int32)
+    if len(ints) > 47:
+        p.l1d_bc, p.dim_1dbc = int(ints[46]), int(ints[47])
     zst = {}
     for key in z.files:
         if key.startswith("zsten_") and key.endswith("_w"):
