@@ -148,9 +148,10 @@ class ClockSampler:
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_sten_tc launch at 128^3 (ncu, one launch)
 TC_TRAFFIC_BYTES = 47.724e6 + 0.538e6
-# the same for one launch of the FP32 y/z FFT pass (k_fft_stridedw<float2>) at 128^3, mean of three launches
-# (ncu flushes the caches before each profiled launch, so the box is read from DRAM there)
-FFT32_PASS_TRAFFIC_BYTES = 11.951e6 + 2.803e6
+# DRAM bytes per algorithmic byte of the FP32 y/z FFT pass launches (k_fft_stridedw<float2>) of a timed solve at
+# 128^3: ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the launches, divided by their algorithmic
+# bytes (ncu flushes the caches before each profiled launch, so every launch reads from DRAM there)
+FFT32_PASS_TRAFFIC_BYTES_PER_BYTE = (27604.527e6 + 3098.825e6) / (512 * 99.893e6)
 
 
 def tc_issued_flops(p):
@@ -428,6 +429,12 @@ def main():
         torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
     st = s.stats()
+    # the roofline kernel in one more solve, the same as a timed one: a CUDA event pair on the solver's stream around
+    # every FP32 y/z FFT pass launch gives its average launch duration and algorithmic bytes per launch
+    s.pass_timer_begin()
+    solve(torch.empty_like(dx))
+    torch.cuda.synchronize()
+    pt_launches, pt_ms, pt_bytes, pt_transforms = s.pass_timer_end()
     choices = {name: s.fft32_choice(t, 0) for name, t in (("theta", THETA), ("delta", DELTA), ("attraction", UATT))}
     ms_total = e0.elapsed_time(e1)
     # one replica per rank: Newton iterations of all ranks over the slowest rank's time
@@ -545,6 +552,9 @@ def main():
     t_pass_z, _, _ = s.time_fft_pass(native.FP32, 2, reps=20)
     t_pass = 0.5 * (t_pass_y + t_pass_z)
     pass_bytes = 2.0 * nh * 8.0                          # the half spectrum (complex FP32) read and written
+    pt_launches = max(1, pt_launches)
+    launch_ms, launch_bytes = pt_ms / pt_launches, pt_bytes / pt_launches
+    launch_gbs = launch_bytes / (launch_ms * 1e-3) / 1e9
     t_pass64, _, _ = s.time_fft_pass(native.FP64, 1, reps=10)
     fft_flops = 2 * 2.5 * nr * math.log2(nr) + 6.0 * nh  # two real transforms and the spectral product
     ach_tf = flops_att / (t_dom * 1e-3) / 1e12
@@ -583,17 +593,25 @@ def main():
             # the largest share of the timed solve's launch list: the y and z passes of the FP32 FFT stencil sums
             # (every stencil sum of the Schur products and FP32 fills), each reading and writing the half spectrum
             "roofline": {"bound": "hbm",
-                         "kernel": "k_fft_stridedw<float2>: one y or z pass of the FP32 FFT stencil sums (one warp "
-                                   "per line, 16 lines per CTA) over the half spectrum",
-                         "achieved": pass_bytes / (t_pass * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
-                         "frac": pass_bytes / (t_pass * 1e-3) / 1e9 / hbm,
-                         "peak_source": f"{peak_src} HBM copy (burst: the pass is timed alone)",
-                         "traffic": (FFT32_PASS_TRAFFIC_BYTES if args.workload == "config2" and args.n == 128
-                                     else None),
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch at 128^3",
-                         "algorithmic": f"{pass_bytes / 1e6:.1f} MB per pass: the {nh}-point complex FP32 half "
-                                        "spectrum read and written once",
-                         "ms_per_launch": t_pass, "ms_per_launch_y": t_pass_y, "ms_per_launch_z": t_pass_z,
+                         "kernel": "k_fft_stridedw<float2>: the y and z passes of the FP32 FFT stencil sums (one warp "
+                                   "per line, 16 lines per CTA), each launch a batch of transforms over the half "
+                                   "spectrum",
+                         "achieved": launch_gbs, "peak": hbm, "unit": "GB/s", "frac": launch_gbs / hbm,
+                         "peak_source": f"{peak_src} HBM copy (burst)",
+                         "measured": f"CUDA events around each of the {pt_launches} launches of one solve like the "
+                                     "timed ones",
+                         "ms_per_launch": launch_ms, "launches_per_solve": pt_launches,
+                         "transforms_per_launch": pt_transforms / pt_launches,
+                         "algorithmic": f"{launch_bytes / 1e6:.1f} MB per launch on average: per transform the "
+                                        f"{nh}-point complex FP32 half spectrum ({nh * 8 / 1e6:.1f} MB) written once "
+                                        "and read once, or the two operands of each spectral product read",
+                         "traffic": (FFT32_PASS_TRAFFIC_BYTES_PER_BYTE * launch_bytes
+                                     if args.workload == "config2" and args.n == 128 else None),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over the launches of a "
+                                           "timed solve at 128^3, per algorithmic byte, times this launch average",
+                         "single_transform_pass": {"ms_y": t_pass_y, "ms_z": t_pass_z,
+                                                   "achieved_gbs": pass_bytes / (t_pass * 1e-3) / 1e9,
+                                                   "note": "one transform per launch, 768 CTAs: 1.26 waves"},
                          "fp64_pass_ms_per_launch": t_pass64,
                          "fft32_attraction_sum": {
                              "ms_per_sum": t_wca_fft32,

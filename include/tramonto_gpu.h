@@ -506,6 +506,12 @@ const char *tgpu_noalloc_last_error(void);
 #define TGPU_TIME_FFT32 16
 int tgpu_time_stencil_sum(tgpu_handle h, int type, int index, int precision, int reps, double *ms_per_sum);
 
+/* Times every launch of the FP32 y/z FFT pass kernel (the solves' leading kernel) between begin and end with a CUDA
+ * event pair on its stream: launches, summed duration, algorithmic bytes (per transform the complex FP32 half
+ * spectrum written once and read once, or each spectral product's two operands read) and transforms.  The
+ * timer is process-wide; the events add gaps between launches, not to them. */
+int tgpu_pass_timer_begin(tgpu_handle h);
+int tgpu_pass_timer_end(tgpu_handle h, long *launches, double *ms_total, double *bytes_total, long *transforms);
 /* Benchmark hook: device time (CUDA events on the handle's stream) of one forward y (axis 1) or z (axis 2) pass of
  * the 3-D FFT sums over a half-spectrum work box, TGPU_FP32 or TGPU_FP64, averaged over reps; box_points receives
  * the half spectrum's size (each pass reads and writes it once), real_points the real transform box's (either may

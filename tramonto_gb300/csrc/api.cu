@@ -3195,6 +3195,30 @@ int tgpu_time_fft_pass(tgpu_handle h, int precision, int axis, int reps, double 
   });
 }
 
+int tgpu_pass_timer_begin(tgpu_handle h)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    long nl = 0;
+    tgpu::pass_timer_collect(&nl, nullptr, nullptr, nullptr);   // drop an earlier unread window
+    tgpu::pass_timer_enable(true);
+    return TGPU_OK;
+  });
+}
+
+int tgpu_pass_timer_end(tgpu_handle h, long *launches, double *ms_total, double *bytes_total, long *transforms)
+{
+  return guard([&] {
+    Ctx *c = C(h);
+    need_final(c);
+    tgpu::pass_timer_enable(false);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    tgpu::pass_timer_collect(launches, ms_total, bytes_total, transforms);
+    return TGPU_OK;
+  });
+}
+
 int tgpu_get_stats(tgpu_handle h, tgpu_stats *out)
 {
   return guard([&] { *out = C(h)->stats; return TGPU_OK; });

@@ -42,6 +42,7 @@ namespace {
 constexpr int kFftLines = 8;     // complex lines per CTA tile
 constexpr int kFftThreads = 256;
 constexpr int kFftMaxN = 432;    // two ping-pong tiles of kFftLines lines and the twiddles fit in shared memory
+constexpr int kBlockLoadBatch = 4;   // global loads a thread issues before storing them to the tile
 
 struct Stages {
   int nst;
@@ -367,18 +368,29 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(PassBatch<C> pb, in
   const int x0 = (blockIdx.x % xblocks) * kFftLines;
   const long base = (long)(blockIdx.x / xblocks) * outer_stride + x0;
   const int nl = min(kFftLines, X - x0);
-  for (int q = threadIdx.x; q < kFftLines * n; q += blockDim.x) {
-    const int e = q / kFftLines, l = q - e * kFftLines;
-    if (l >= nl) continue;
-    const long idx = base + e * es + l;
-    C v;
-    if (terms.n == 0) {
-      v = in[idx];
-    } else {
-      v = cmul(terms.a[0][idx], terms.k[0][idx]);
-      for (int t = 1; t < terms.n; t++) v = cadd(v, cmul(terms.a[t][idx], terms.k[t][idx]));
+  const int total = kFftLines * n;
+  for (int q0 = threadIdx.x; q0 < total; q0 += kBlockLoadBatch * blockDim.x) {   // loads first, then stores
+    C v[kBlockLoadBatch];
+#pragma unroll
+    for (int b = 0; b < kBlockLoadBatch; b++) {
+      const int q = q0 + b * blockDim.x;
+      const int e = q / kFftLines, l = q - e * kFftLines;
+      v[b] = C{0, 0};
+      if (q < total && l < nl) {
+        const long idx = base + e * es + l;
+        if (terms.n == 0) {
+          v[b] = in[idx];
+        } else {
+          v[b] = cmul(terms.a[0][idx], terms.k[0][idx]);
+          for (int t = 1; t < terms.n; t++) v[b] = cadd(v[b], cmul(terms.a[t][idx], terms.k[t][idx]));
+        }
+      }
     }
-    b0[l * ls + e] = v;
+#pragma unroll
+    for (int b = 0; b < kBlockLoadBatch; b++) {
+      const int q = q0 + b * blockDim.x;
+      if (q < total) b0[(q % kFftLines) * ls + q / kFftLines] = v[b];
+    }
   }
   __syncthreads();
   const C *res = fft_tile<C>(b0, b1, n, ls, nl, st, tw, inv);
@@ -396,6 +408,7 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(PassBatch<C> pb, in
 // whole block leaves fewer of them on partly filled warps (at 180 points a warp per line leaves up to 28 of 64
 // lane slots of a stage idle).
 constexpr int kWLines = 16;   // lines (one warp each) per CTA
+constexpr int kLoadBatch = 4; // global loads a thread issues before it stores them to shared memory
 
 template <int R, class C>
 __device__ __forceinline__ void warp_stage(const C *src, C *dst, int n, int Ns, int step, unsigned magic,
@@ -460,13 +473,21 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
   const int y0 = (int)(L % g.F1), z0 = (int)(L / g.F1);
   const int y1 = (int)((L + 1) % g.F1), z1 = (int)((L + 1) / g.F1);
   const bool r0 = y0 < g.ext[1] && z0 < g.ext[2], r1 = two && y1 < g.ext[1] && z1 < g.ext[2];
-  for (int x = lane; x < n; x += 32) {
-    T a = 0, b = 0;
-    if (x < g.ext[0]) {
-      if (r0) a = src(g, x, y0, z0);
-      if (r1) b = src(g, x, y1, z1);
+  for (int x0 = lane; x0 < n; x0 += 32 * kLoadBatch) {
+    T a[kLoadBatch], b[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; u++) {
+      const int x = x0 + 32 * u;
+      a[u] = 0;
+      b[u] = 0;
+      if (x < g.ext[0]) {
+        if (r0) a[u] = src(g, x, y0, z0);
+        if (r1) b[u] = src(g, x, y1, z1);
+      }
     }
-    b0[x] = C{a, b};
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; u++)
+      if (x0 + 32 * u < n) b0[x0 + 32 * u] = C{a[u], b[u]};
   }
   __syncwarp();
   const C *res = warp_fft<C>(b0, b1, n, st, tw, 0, lane);
@@ -496,12 +517,25 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom
   if (L >= g.nlines) return;
   C *b0 = sm + w * ls, *b1 = sm + (kWLines + w) * ls;
   const bool two = L + 1 < g.nlines;
-  for (int k = lane; k < n; k += 32) {
-    const bool up = k < g.Fh;
-    const int kk = up ? k : n - k;
-    const C A = spec[L * g.Fh + kk];
-    const C B = two ? spec[(L + 1) * g.Fh + kk] : C{0, 0};
-    b0[k] = up ? C{A.x - B.y, A.y + B.x} : C{A.x + B.y, B.x - A.y};
+  for (int k0 = lane; k0 < n; k0 += 32 * kLoadBatch) {
+    C A[kLoadBatch], B[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; u++) {
+      const int k = k0 + 32 * u;
+      const int kk = k < g.Fh ? k : n - k;
+      A[u] = C{0, 0};
+      B[u] = C{0, 0};
+      if (k < n) {
+        A[u] = spec[L * g.Fh + kk];
+        if (two) B[u] = spec[(L + 1) * g.Fh + kk];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; u++) {
+      const int k = k0 + 32 * u;
+      if (k < n)
+        b0[k] = k < g.Fh ? C{A[u].x - B[u].y, A[u].y + B[u].x} : C{A[u].x + B[u].y, B[u].x - A[u].y};
+    }
   }
   __syncwarp();
   const C *res = warp_fft<C>(b0, b1, n, st, tw, 1, lane);
@@ -539,18 +573,31 @@ __global__ void __launch_bounds__(32 * kWLines) k_fft_stridedw(PassBatch<C> pb, 
   const int x0 = (blockIdx.x % xblocks) * kWLines;
   const long base = (long)(blockIdx.x / xblocks) * outer_stride + x0;
   const int nl = min(kWLines, X - x0);
-  for (int q = threadIdx.x; q < kWLines * n; q += blockDim.x) {
-    const int e = q / kWLines, l = q % kWLines;
-    if (l >= nl) continue;
-    const long idx = base + e * es + l;
-    C v;
-    if (terms.n == 0) {
-      v = in[idx];
-    } else {
-      v = cmul(terms.a[0][idx], terms.k[0][idx]);
-      for (int t = 1; t < terms.n; t++) v = cadd(v, cmul(terms.a[t][idx], terms.k[t][idx]));
+  // loads in groups of kLoadBatch per thread, all issued before any shared-memory store (the pass is bound by
+  // global-load latency)
+  const int total = kWLines * n;
+  for (int q0 = threadIdx.x; q0 < total; q0 += kLoadBatch * blockDim.x) {
+    C v[kLoadBatch];
+#pragma unroll
+    for (int b = 0; b < kLoadBatch; b++) {
+      const int q = q0 + b * blockDim.x;
+      const int e = q / kWLines, l = q % kWLines;
+      v[b] = C{0, 0};
+      if (q < total && l < nl) {
+        const long idx = base + e * es + l;
+        if (terms.n == 0) {
+          v[b] = in[idx];
+        } else {
+          v[b] = cmul(terms.a[0][idx], terms.k[0][idx]);
+          for (int t = 1; t < terms.n; t++) v[b] = cadd(v[b], cmul(terms.a[t][idx], terms.k[t][idx]));
+        }
+      }
     }
-    sm[l * ls + e] = v;
+#pragma unroll
+    for (int b = 0; b < kLoadBatch; b++) {
+      const int q = q0 + b * blockDim.x;
+      if (q < total) sm[(q % kWLines) * ls + q / kWLines] = v[b];
+    }
   }
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -675,6 +722,17 @@ XGeom xgeom(const FftPlan &p)
   return g;
 }
 
+// Optional timing of every FP32 y/z pass launch (the solves' leading kernel): a CUDA event pair around each launch
+// on its own stream and the launch's algorithmic bytes (per transform the half spectrum written once and read once,
+// or the two operands of each spectral product read); collected and reset by pass_timer_collect.
+struct PassTimer {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;   // begin, end of each launch
+  std::vector<double> bytes;
+  std::vector<int> fields;
+};
+PassTimer g_pass_timer;
+
 // one y (d = 1) or z (d = 2) pass of nb transforms of the plan in one launch: FP32 one warp per line, FP64 the
 // block tile
 template <class C>
@@ -687,8 +745,24 @@ void strided_pass_batch(const PassBatch<C> &pb, int nb, const FftPlan &p, int d,
   const long nouter = d == 1 ? p.F[2] : p.F[1];
   if constexpr (std::is_same<C, float2>::value) {
     const int xb = (X + kWLines - 1) / kWLines;
+    const bool timed = g_pass_timer.on;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (timed) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, s);
+    }
     k_fft_stridedw<float2><<<dim3((unsigned)(xb * nouter), (unsigned)nb), 32 * kWLines, wtile_smem(n), s>>>(
         pb, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+    if (timed) {
+      cudaEventRecord(e1, s);
+      double units = 0.0;   // half spectra moved
+      for (int b = 0; b < nb; b++) units += 1.0 + (pb.terms[b].n > 0 ? 2.0 * pb.terms[b].n : 1.0);
+      g_pass_timer.ev.push_back(e0);
+      g_pass_timer.ev.push_back(e1);
+      g_pass_timer.bytes.push_back(units * (double)p.NH * sizeof(float2));
+      g_pass_timer.fields.push_back(nb);
+    }
   } else {
     const int xblocks = (X + kFftLines - 1) / kFftLines;
     k_fft_strided<C><<<dim3((unsigned)(xblocks * nouter), (unsigned)nb), kFftThreads, tile_smem<C>(n), s>>>(
@@ -1006,6 +1080,34 @@ void launch_fft_kernel_box(const short *off3, const double *coef, int L, int nco
 void launch_to_float2(const double2 *in, float2 *out, long n, cudaStream_t s)
 {
   k_to_float2<<<grid_for(n), 256, 0, s>>>(in, out, n);
+}
+
+void pass_timer_enable(bool on)
+{
+  g_pass_timer.on = on;
+}
+
+void pass_timer_collect(long *launches, double *ms_total, double *bytes_total, long *fields_total)
+{
+  double ms = 0.0, bytes = 0.0;
+  long fields = 0;
+  const size_t nl = g_pass_timer.bytes.size();
+  for (size_t i = 0; i < nl; i++) {
+    float t = 0.f;
+    cudaEventSynchronize(g_pass_timer.ev[2 * i + 1]);
+    cudaEventElapsedTime(&t, g_pass_timer.ev[2 * i], g_pass_timer.ev[2 * i + 1]);
+    ms += t;
+    bytes += g_pass_timer.bytes[i];
+    fields += g_pass_timer.fields[i];
+  }
+  for (cudaEvent_t e : g_pass_timer.ev) cudaEventDestroy(e);
+  g_pass_timer.ev.clear();
+  g_pass_timer.bytes.clear();
+  g_pass_timer.fields.clear();
+  if (launches) *launches = (long)nl;
+  if (ms_total) *ms_total = ms;
+  if (bytes_total) *bytes_total = bytes;
+  if (fields_total) *fields_total = fields;
 }
 
 }  // namespace tgpu

@@ -113,6 +113,9 @@ int fft_max_terms();
 // several FP32 transforms of one plan per launch (blockIdx.y selects the transform): forward transforms of nb mapped
 // channels into spec[b]; inverse transforms out[b] (+)= scale * inverse of a * k[b] (work[b] the half spectra)
 int fft_max_batch();
+// per-launch CUDA-event timing of the FP32 y/z FFT passes (off unless enabled; collect reads and resets)
+void pass_timer_enable(bool on);
+void pass_timer_collect(long *launches, double *ms_total, double *bytes_total, long *fields_total);
 void rfft_forward_mapped_batch(const MapSrc *m, int nb, float2 *const *spec, const FftPlan &p, cudaStream_t s);
 void rfft_forward_mapped_batch(const MapSrc *m, int nb, double2 *const *spec, const FftPlan &p, cudaStream_t s);
 void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,

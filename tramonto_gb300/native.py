@@ -93,6 +93,8 @@ def load(build_if_missing: bool = False):
         "tgpu_fft32_choice": [vp, C.c_int, C.c_int, ip, dp],
         "tgpu_set_tc_wait_limit": [vp, C.c_long],
         "tgpu_time_fft_pass": [vp, C.c_int, C.c_int, C.c_int, dp, C.POINTER(C.c_long), C.POINTER(C.c_long)],
+        "tgpu_pass_timer_begin": [vp],
+        "tgpu_pass_timer_end": [vp, C.POINTER(C.c_long), dp, dp, C.POINTER(C.c_long)],
         "tgpu_set_zone_stencil": [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp],
         "tgpu_set_vext": [vp, vp], "tgpu_set_zero_density": [vp, vp], "tgpu_set_hard_wall": [vp, vp, vp],
         "tgpu_finalize": [vp], "tgpu_set_precision": [vp, C.c_int], "tgpu_set_stream": [vp, vp],
@@ -507,6 +509,17 @@ class Solver:
                                                update_floor, C.byref(it), C.byref(rn), C.byref(li))
         _check(st, self.lib, ok=(0, -5) if allow_noconv else (0,))
         return it.value, rn.value, li.value
+
+    def pass_timer_begin(self):
+        """Start timing every FP32 y/z FFT pass launch (CUDA events on its stream)."""
+        _check(self.lib.tgpu_pass_timer_begin(self.h), self.lib)
+
+    def pass_timer_end(self):
+        """Stop the pass timer: (launches, summed ms, algorithmic bytes, transforms)."""
+        nl, nt = C.c_long(), C.c_long()
+        ms, by = C.c_double(), C.c_double()
+        _check(self.lib.tgpu_pass_timer_end(self.h, C.byref(nl), C.byref(ms), C.byref(by), C.byref(nt)), self.lib)
+        return int(nl.value), float(ms.value), float(by.value), int(nt.value)
 
     def time_fft_pass(self, precision, axis=1, reps=20):
         """Device milliseconds of one y (axis 1) or z (axis 2) pass of the FFT sums, the half spectrum's size and the
