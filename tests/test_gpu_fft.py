@@ -13,6 +13,9 @@ FFT convolutions, the short ones (theta, delta) as float-float sums.
   1e-5, its nonlocal part (S v2 less the local v2 / rho) too, and J v to 1e-5 (relative to their max norms), an FP32 fill equals the FP64 fill to 1e-4, and the mixed
   solve still reaches the FP64 solve's density to 1e-9; with the direct kernels forced (policy 0) the products
   are the slab / tensor-core ones;
+- FP32 Schur products whose every sum is an FP32 FFT keep their sums, channels and transposed sums in FP32 storage;
+  with the timed choices (policy -1) the first product makes the choices in FP64 storage, the next ones run in
+  FP32 storage and equal it to 1e-6 (the same FP32 sums; only the last sum A21 y rounds in FP32);
 - TGPU_FP64_FFT products (J v and the Schur product with the sums of TGPU_FILL_FFT) equal the reference's
   assembled products on the 3-D fixtures to 1e-12 (every sum by FFT) and the direct FP64 products at 64^3 to 1e-11.
 """
@@ -169,4 +172,23 @@ def test_fft_sums_follow_a_moved_bulk_state():
     print("moved bulk: |R_fft - R_fp64|", np.abs(Rf - R64).max(), "|R_fp32 - R_fp64|", np.abs(R32 - R64).max())
     assert np.abs(Rf - R64).max() <= 5e-12
     assert np.abs(R32 - R64).max() <= 1e-4 * max(1.0, np.abs(R64).max())
+    s.close()
+
+
+def test_fp32_storage_schur_product_equals_the_fp64_storage_one():
+    from tramonto_gb300 import native, setup
+    from goldens import rel_err
+    p, _ = setup.config2(n=40)
+    s = native.Solver(p)
+    x0 = setup.initial_state(s, p)
+    s.fill(x0)
+    rng = np.random.default_rng(11)
+    v2 = rng.standard_normal((p.ncomp, p.nnodes))
+    S64 = s.schur(v2)
+    s.set_precision(native.FP32)
+    first = s.schur(v2)     # makes the timed FFT / direct choices (FP64 storage)
+    again = s.schur(v2)     # FP32 storage when every sum took the FFT
+    print("first vs again", rel_err(again, first), "vs FP64", rel_err(again, S64))
+    assert rel_err(again, first) <= 1e-6
+    assert rel_err(again, S64) <= 1e-5
     s.close()

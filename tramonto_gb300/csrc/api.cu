@@ -196,6 +196,7 @@ struct Ctx : tgpu_ctx {
   // the channels of the last pad(): the padded box is written only when a direct kernel needs it (FFT sums read
   // the channels through the boundary maps)
   const double *pad_src = nullptr;
+  const float *pad_src32 = nullptr;   // FP32 channels of the last pad32() (read through the boundary maps only)
   const PadParams *pad_pp = nullptr;
   bool pad_f32 = false, pad_pending = false;
   // the per-node FMT Hessian scalars of the current state (products of one Newton state share them)
@@ -203,6 +204,13 @@ struct Ctx : tgpu_ctx {
   // domain flags of the last fill (tgpu::kDomainN3 | tgpu::kDomainRho), set by its local kernels
   unsigned *d_domain = nullptr;
   int hcoef_form = -1;           // the Jacobian form they were made with; -1: stale
+  // FP32 storage of the FP32 Schur products whose every stencil sum is an FP32 FFT (3-D, one zone, no hard-wall
+  // corrections or coarsened nodes): the sums, channels, transposed sums, -u_MF and the state's Hessian scalars
+  // with its weighted densities ([kHessCoef + nrb][N]) in FP32; store32 routes the FFT sums' outputs and inputs
+  // there while such a product runs
+  bool store32 = false;
+  float *d_conv32 = nullptr, *d_chan32 = nullptr, *d_tr32 = nullptr, *d_ymf32 = nullptr, *d_hcoef32 = nullptr;
+  int hcoef32_form = -1;
 };
 
 // The geometry lives in one __constant__ block per device; the handle that
@@ -292,13 +300,26 @@ void pad(Ctx *c, const double *src, const PadParams &pp, bool f32)
 {
   c->pad_gen++;   // the padded channels change: a cached spectrum of them is stale
   c->pad_src = src;
+  c->pad_src32 = nullptr;
   c->pad_pp = &pp;
   c->pad_f32 = f32;
   c->pad_pending = true;
 }
 
+// FP32 channels for the FP32 FFT sums, which read them through the boundary maps (no padded box is made)
+void pad32(Ctx *c, const float *src, const PadParams &pp)
+{
+  c->pad_gen++;
+  c->pad_src = nullptr;
+  c->pad_src32 = src;
+  c->pad_pp = &pp;
+  c->pad_f32 = true;
+  c->pad_pending = false;
+}
+
 void materialize(Ctx *c)
 {
+  if (c->pad_src32) throw Error(TGPU_ERR_STATE, "an FP32-storage product needs a direct stencil sum");
   if (!c->pad_pending) return;
   const PadParams &pp = *c->pad_pp;
   if (!c->pad_f32)
@@ -315,7 +336,8 @@ tgpu::MapSrc map_src(const Ctx *c, int ch)
   const tgpu::DevGeom &g = c->dg;
   const PadParams &pp = *c->pad_pp;
   tgpu::MapSrc m;
-  m.src = c->pad_src + (long)ch * g.N;
+  if (c->pad_src32) m.src32 = c->pad_src32 + (long)ch * g.N;
+  else m.src = c->pad_src + (long)ch * g.N;
   m.ndim = g.ndim;
   for (int d = 0; d < 3; d++) {
     m.nx[d] = g.nx[d];
@@ -495,6 +517,15 @@ void fft_tr_sum(Ctx *c, const int *chs, const C *const *kern, int n, double *out
     for (int t = 0; t < n; t++) a[t] = boxes[t];
   }
   C *work = std::is_same<C, float2>::value ? (C *)c->d_fbox32[2] : (C *)c->d_fbox[2];
+  if constexpr (std::is_same<C, float2>::value) {
+    if (c->store32) {   // the FP32 shadow of the transposed-sum output
+      tgpu::rfft_inverse_products(a.data(), kern, n, work, c->fft, 1.0 / (double)c->fft.NR,
+                                  c->d_tr32 + (out - c->d_tr), true, c->stream);
+      c->stats.kernel_launches += 3;
+      c->stats.conv_launches++;
+      return;
+    }
+  }
   tgpu::rfft_inverse_products(a.data(), kern, n, work, c->fft, 1.0 / (double)c->fft.NR, out, true, c->stream);
   c->stats.kernel_launches += 3;
   c->stats.conv_launches++;
@@ -780,13 +811,21 @@ void forward_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, boo
         const float2 *F = fft_channel32(c, jc);
         std::vector<float2 *> &work = tr_boxes<float2>(c);
         while (work.size() < ks.size()) work.push_back(dalloc<float2>((size_t)c->fft.NH));
-        tgpu::rfft_inverse_batch(F, ks.data(), (int)ks.size(), work.data(), c->fft, 1.0 / (double)c->fft.NR,
-                                 os.data(), true, c->stream);
+        if (c->store32) {   // the FP32 shadows of the sums
+          std::vector<float *> os32;
+          for (double *o : os) os32.push_back(c->d_conv32 + (o - c->d_conv));
+          tgpu::rfft_inverse_batch(F, ks.data(), (int)ks.size(), work.data(), c->fft, 1.0 / (double)c->fft.NR,
+                                   os32.data(), true, c->stream);
+        } else {
+          tgpu::rfft_inverse_batch(F, ks.data(), (int)ks.size(), work.data(), c->fft, 1.0 / (double)c->fft.NR,
+                                   os.data(), true, c->stream);
+        }
         c->stats.kernel_launches += 3 * ((ks.size() + tgpu::fft_max_batch() - 1) / tgpu::fft_max_batch());
         c->stats.conv_launches++;
         continue;
       }
     }
+    if (c->store32) throw Error(TGPU_ERR_STATE, "an FP32-storage product needs a direct stencil sum");
     conv(c, jc, 1, sten[TGPU_STEN_THETA][jc], false, o_th, 1, f32);
     conv(c, jc, 1, sten[TGPU_STEN_DELTA][jc], false, o_de.data(), (int)o_de.size(), f32);
     if (g.attraction)
@@ -804,7 +843,10 @@ void forward_pass(Ctx *c, const double *field, const PadParams &pp, bool f32, bo
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
   const size_t nrows = (size_t)(g.nrb + g.ncomp);
-  if (zero_first) ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * nrows * N, c->stream), "memset");
+  if (zero_first) {
+    if (c->store32) ck(cudaMemsetAsync(c->d_conv32, 0, sizeof(float) * nrows * N, c->stream), "memset");
+    else ck(cudaMemsetAsync(c->d_conv, 0, sizeof(double) * nrows * N, c->stream), "memset");
+  }
   pad(c, field, pp, f32);
   if (f32 && g.attraction && g.ndim == 3) decide_fft32(c);
   if (f32 && g.ndim == 3)
@@ -858,6 +900,7 @@ void transpose_convs(Ctx *c, const std::vector<DevStencil> *sten, double *out, b
       fft_tr_sum<double2>(c, chs, k, nd + 2, o[0]);
       continue;
     }
+    if (c->store32) throw Error(TGPU_ERR_STATE, "an FP32-storage product needs a direct stencil sum");
     conv(c, base, 1 + nd, sd, true, o, 1, f32);
     conv(c, base + nd + 1, 1, st, true, o, 1, f32);
   }
@@ -868,8 +911,13 @@ void transpose_pass(Ctx *c, const PadParams &pp, bool f32, const double *chan = 
 {
   const tgpu::DevGeom &g = c->dg;
   const long N = g.N;
-  if (zero_first) ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
-  pad(c, chan ? chan : c->d_chan, pp, f32);
+  if (c->store32) {
+    if (zero_first) ck(cudaMemsetAsync(c->d_tr32, 0, sizeof(float) * (size_t)g.ncomp * N, c->stream), "memset");
+    pad32(c, c->d_chan32, pp);
+  } else {
+    if (zero_first) ck(cudaMemsetAsync(c->d_tr, 0, sizeof(double) * (size_t)g.ncomp * N, c->stream), "memset");
+    pad(c, chan ? chan : c->d_chan, pp, f32);
+  }
   if (f32 && g.ndim == 3)
     for (int ic = 0; ic < g.ncomp; ic++) {
       const int base = ic * (g.ndim + 2);
@@ -978,6 +1026,7 @@ void fill_arith(Ctx *c, const double *d_x, double *d_R, int mode, int arith)
   if (mode == 0) {
     c->have_state = true;
     c->hcoef_form = -1;   // a new state: its Hessian scalars are made at the first product
+    c->hcoef32_form = -1;
   }
 }
 
@@ -1057,12 +1106,68 @@ const double *prolonged(Ctx *c, const double *v, int nrows)
   return c->d_cscr;
 }
 
+// The FP32 Schur product with FP32 storage: every stencil sum an FP32 FFT (the choices already made by timing), in
+// 3-D, with one quadrature zone, no hard-wall corrections and no coarsened nodes
+bool schur_store32_ok(Ctx *c)
+{
+  const tgpu::DevGeom &g = c->dg;
+  if (!prod_f32(c) || !c->spec32_built || g.ndim != 3 || c->nzone != 1 || !c->hw_targets.empty() || c->coarse())
+    return false;
+  const int nde = 1 + (g.single_size ? 0 : 2) + g.ndim * (g.single_size ? 1 : 2);
+  for (int jc = 0; jc < g.ncomp; jc++) {
+    const DevStencil &sth = c->sten[TGPU_STEN_THETA][jc], &sde = c->sten[TGPU_STEN_DELTA][jc];
+    if (!use_fft32(c, sth, false, 1, 1) || !use_fft32(c, sde, false, 1, nde)) return false;
+    if (!use_fft32(c, sde, true, 1 + g.ndim, 1) || !use_fft32(c, sth, true, 1, 1)) return false;
+    if (g.attraction)
+      for (int ic = 0; ic < g.ncomp; ic++)
+        if (!use_fft32(c, c->sten[TGPU_STEN_UATT][ic + g.ncomp * jc], false, 1, 1)) return false;
+  }
+  return true;
+}
+
+void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
+{
+  const tgpu::DevGeom &g = c->dg;
+  const size_t N = (size_t)g.N;
+  if (!c->d_conv32) {
+    c->d_conv32 = dalloc<float>((size_t)(g.nrb + g.ncomp) * N);
+    c->d_chan32 = dalloc<float>((size_t)g.ncomp * (g.ndim + 2) * N);
+    c->d_tr32 = dalloc<float>((size_t)g.ncomp * N);
+    c->d_ymf32 = dalloc<float>((size_t)g.ncomp * N);
+    c->d_hcoef32 = dalloc<float>((size_t)(tgpu::kHessCoef + g.nrb) * N);
+  }
+  if (c->hcoef32_form != g.jac_exact) {
+    tgpu::launch_hess_coef32(c->d_x, c->d_hcoef32, c->stream);
+    c->stats.kernel_launches++;
+    c->hcoef32_form = g.jac_exact;
+  }
+  c->store32 = true;
+  try {
+    forward_pass(c, d_v2, c->pads.rho_jac, true);
+    tgpu::launch_schur_local32(g.ndim, c->d_conv32, c->d_hcoef32, c->d_chan32, c->d_ymf32, c->stream);
+    transpose_pass(c, c->pads.tr_jac, true);
+  } catch (...) {
+    c->store32 = false;
+    c->pad_src32 = nullptr;
+    throw;
+  }
+  c->store32 = false;
+  c->pad_src32 = nullptr;
+  tgpu::launch_schur_combine32(c->d_x, c->d_vext, c->d_zero, d_v2, c->d_tr32, c->d_ymf32, d_y2, c->stream);
+  c->stats.kernel_launches += 2;
+  c->stats.schur_applies++;
+}
+
 void schur_device(Ctx *c, const double *d_v2, double *d_y2)
 {
   need_state(c);
   TcScope tcs(c);
   const tgpu::DevGeom &g = c->dg;
   const bool f32 = prod_f32(c);
+  if (f32 && schur_store32_ok(c)) {
+    schur_device_store32(c, d_v2, d_y2);
+    return;
+  }
   const double *v2 = prolonged(c, d_v2, g.ncomp);
   forward_pass(c, v2, c->pads.rho_jac, f32);
   if (c->coarse()) tgpu::launch_prolong(c->d_conv, 0, g.nrb + g.ncomp, g.nunk, g.N, c->cr, nullptr, c->stream);
@@ -2484,6 +2589,7 @@ int tgpu_destroy(tgpu_handle h)
     dfree(c->d_zone); dfree(c->d_zbuf); dfree(c->d_cbulk); dfree(c->d_cscr); dfree(c->d_cscr2); dfree(c->d_hcoef); dfree(c->d_domain);
     dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
     dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw); dfree(c->cr.d_kind); dfree(c->d_rowkind);
+    dfree(c->d_conv32); dfree(c->d_chan32); dfree(c->d_tr32); dfree(c->d_ymf32); dfree(c->d_hcoef32);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
     tgpu::tc_free_slab(c->tcslab);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);

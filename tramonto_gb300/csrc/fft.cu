@@ -232,7 +232,7 @@ struct MappedSrc {   // the unpadded channel through the boundary maps (the padd
     }
     const long node = idx[0] + (long)m.nx[0] * (idx[1] + (long)m.nx[1] * idx[2]);
     if (m.zc >= 0 && m.zero[(long)m.zc * m.N + node]) return (T)0;
-    const T v = to_arith<T>(m.src[node]);
+    const T v = m.src32 ? (T)m.src32[node] : to_arith<T>(m.src[node]);
     return (__popc(refl & m.signmask) & 1) ? -v : v;
   }
 };
@@ -265,6 +265,7 @@ template <class C>
 struct OutBatch {
   const C *spec[kMaxBatch];
   double *out[kMaxBatch];
+  float *out32[kMaxBatch];   // FP32 outputs (the FP32 transforms; used instead of out when set)
 };
 
 // x pass of the forward transform: two real lines per complex line, split into two half-spectrum lines
@@ -506,6 +507,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom
 {
   const C *__restrict__ spec = ob.spec[blockIdx.y];
   double *__restrict__ out = ob.out[blockIdx.y];
+  float *__restrict__ out32 = ob.out32[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
   const int n = g.F0, ls = n + 1;
@@ -545,8 +547,17 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom
     if (h == 1 && !two) break;
     const int y = (int)((L + h) % g.F1) - g.e[1], z = (int)((L + h) / g.F1) - g.e[2];
     if (y < 0 || y >= g.nx[1] || z < 0 || z >= g.nx[2]) continue;
-    double *o = out + ((long)z * g.nx[1] + y) * nx0;
     const float sc = (float)scale;
+    if (out32) {
+      float *o = out32 + ((long)z * g.nx[1] + y) * nx0;
+      for (int x = lane; x < nx0; x += 32) {
+        const C r = res[x + g.e[0]];
+        const float v = sc * (h ? r.y : r.x);
+        o[x] = accumulate ? o[x] + v : v;
+      }
+      continue;
+    }
+    double *o = out + ((long)z * g.nx[1] + y) * nx0;
     for (int x = lane; x < nx0; x += 32) {
       const C r = res[x + g.e[0]];
       const double v = (double)(sc * (h ? r.y : r.x));   // scaled in FP32
@@ -812,8 +823,8 @@ void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, c
 
 // inverse of the products in `terms`, formed by the first inverse pass into `spec` (the work box)
 template <class C>
-void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double scale, double *out, bool accumulate,
-                       const C *const *tw, cudaStream_t s)
+void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double scale, double *out, float *out32,
+                       bool accumulate, const C *const *tw, cudaStream_t s)
 {
   const Terms<C> none{};
   bool pending = true;   // products not formed yet
@@ -829,6 +840,7 @@ void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double 
     OutBatch<C> ob{};
     ob.spec[0] = spec;
     ob.out[0] = out;
+    ob.out32[0] = out32;
     k_irfft_xw<C><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
         ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
   } else {
@@ -869,7 +881,8 @@ void rfft_forward_mapped_batch_impl(const MapSrc *m, int nb, C *const *spec, con
 // nb inverse transforms, output b the inverse of a * k[b] (formed by the first inverse pass in work[b])
 template <class C>
 void rfft_inverse_batch_impl(const C *a, const C *const *k, int nb, C *const *work, const FftPlan &p, double scale,
-                             double *const *out, bool accumulate, const C *const *tw, cudaStream_t s)
+                             double *const *out, float *const *out32, bool accumulate, const C *const *tw,
+                             cudaStream_t s)
 {
   PassBatch<C> pb{}, plain{};
   OutBatch<C> ob{};
@@ -880,7 +893,8 @@ void rfft_inverse_batch_impl(const C *a, const C *const *k, int nb, C *const *wo
     pb.terms[b].k[0] = k[b];
     pb.terms[b].n = 1;
     ob.spec[b] = work[b];
-    ob.out[b] = out[b];
+    ob.out[b] = out ? out[b] : nullptr;
+    ob.out32[b] = out32 ? out32[b] : nullptr;
   }
   bool pending = true;
   for (int d = 2; d >= 1; d--) {
@@ -1013,14 +1027,21 @@ void rfft_inverse_products(const double2 *const *a, const double2 *const *k, int
                            const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
 {
   const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
-  rfft_inverse_impl<double2>(make_terms(a, k, nterms), work, p, scale, out, accumulate, tw, s);
+  rfft_inverse_impl<double2>(make_terms(a, k, nterms), work, p, scale, out, nullptr, accumulate, tw, s);
 }
 
 void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
                            const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s)
 {
   const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
-  rfft_inverse_impl<float2>(make_terms(a, k, nterms), work, p, scale, out, accumulate, tw, s);
+  rfft_inverse_impl<float2>(make_terms(a, k, nterms), work, p, scale, out, nullptr, accumulate, tw, s);
+}
+
+void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
+                           const FftPlan &p, double scale, float *out, bool accumulate, cudaStream_t s)
+{
+  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
+  rfft_inverse_impl<float2>(make_terms(a, k, nterms), work, p, scale, nullptr, out, accumulate, tw, s);
 }
 
 int fft_max_terms() { return kMaxTerms; }
@@ -1045,7 +1066,16 @@ void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 
 {
   const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
   for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
-    rfft_inverse_batch_impl<float2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0,
+    rfft_inverse_batch_impl<float2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0, nullptr,
+                                    accumulate, tw, s);
+}
+
+void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,
+                        double scale, float *const *out, bool accumulate, cudaStream_t s)
+{
+  const float2 *tw[3] = {p.ax[0].d_tw32, p.ax[1].d_tw32, p.ax[2].d_tw32};
+  for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
+    rfft_inverse_batch_impl<float2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, nullptr, out + b0,
                                     accumulate, tw, s);
 }
 
@@ -1054,7 +1084,7 @@ void rfft_inverse_batch(const double2 *a, const double2 *const *k, int nb, doubl
 {
   const double2 *tw[3] = {p.ax[0].d_tw, p.ax[1].d_tw, p.ax[2].d_tw};
   for (int b0 = 0; b0 < nb; b0 += kMaxBatch)
-    rfft_inverse_batch_impl<double2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0,
+    rfft_inverse_batch_impl<double2>(a, k + b0, std::min(kMaxBatch, nb - b0), work + b0, p, scale, out + b0, nullptr,
                                      accumulate, tw, s);
 }
 

@@ -936,6 +936,91 @@ void launch_schur_local(const double *x, const double *conv, double *chan, doubl
   else k_schur_local<double><<<1184, kThreads, 0, s>>>(x, conv, chan, ymf, coef);
 }
 
+// FP32 storage for the FP32 Schur products: the state's Hessian scalars and weighted densities (n order) as FP32
+// rows [kHessCoef + nrb][N], made once per state; with the stencil sums, channels and transposed sums also held
+// in FP32 the local step converts nothing (conversions between FP64 and FP32 run on GB300's FP64 pipe).
+__global__ void k_hess_coef32(const double *__restrict__ x, float *__restrict__ coef)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    double n[kMaxRb];
+    load_n(x, i, n);
+    const HessCoef c = fmt_hess_coef_at(n, c_g.ndim, c_g.functional, c_g.jac_exact != 0);
+    const double v[kHessCoef] = {c.a, c.a2, c.h13, c.h22, c.h23, c.h33, c.ff, c.gvf1, c.g2vr_f, c.g2vc_f, c.gvv,
+                                 c.gvv_out};
+    for (int k = 0; k < kHessCoef; k++) coef[(long)k * N + i] = (float)v[k];
+    for (int k = 0; k < c_g.nrb; k++) coef[(long)(kHessCoef + k) * N + i] = (float)n[k];
+  }
+}
+
+void launch_hess_coef32(const double *x, float *coef, cudaStream_t s)
+{
+  k_hess_coef32<<<1184, kThreads, 0, s>>>(x, coef);
+}
+
+// k_schur_local with every operand in FP32 storage (conv [nrb + ncomp][N] the stencil sums of A12 v, chan the
+// transposed-sum channels, ymf = -u_MF); ND the dimension, so that the per-node arrays stay in registers, and the
+// per-component constants converted once per thread
+template <int ND>
+__global__ void k_schur_local32(const float *__restrict__ conv, const float *__restrict__ coef,
+                                float *__restrict__ chan, float *__restrict__ ymf)
+{
+  constexpr int NRB = 4 + 2 * ND;
+  const long N = c_g.N;
+  int src_k[NRB];
+  float dep_c[NRB];
+  bool dep[NRB];
+#pragma unroll
+  for (int k = 0; k < NRB; k++) {
+    double cd = 0.0;
+    dep[k] = dep_rb(k, &src_k[k], &cd);
+    dep_c[k] = (float)cd;
+  }
+  const int ncomp = c_g.ncomp;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    float ysv[NRB], y[NRB], z[NRB], n[NRB];
+#pragma unroll
+    for (int k = 0; k < NRB; k++)
+      ysv[k] = dep[k] ? -dep_c[k] * conv[(long)src_k[k] * N + i] : -conv[(long)k * N + i];   // -u_dep - B u_ind
+    y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
+#pragma unroll
+    for (int d = 0; d < ND; d++) { y[4 + d] = ysv[4 + ND + d]; y[4 + ND + d] = ysv[4 + d]; }
+#pragma unroll
+    for (int k = 0; k < NRB; k++) n[k] = coef[(long)(kHessCoef + k) * N + i];
+    HessCoefT<float> hc;
+    hc.a = coef[i];
+    hc.a2 = coef[N + i];
+    hc.h13 = coef[2 * N + i];
+    hc.h22 = coef[3 * N + i];
+    hc.h23 = coef[4 * N + i];
+    hc.h33 = coef[5 * N + i];
+    hc.ff = coef[6 * N + i];
+    hc.gvf1 = coef[7 * N + i];
+    hc.g2vr_f = coef[8 * N + i];
+    hc.g2vc_f = coef[9 * N + i];
+    hc.gvv = coef[10 * N + i];
+    hc.gvv_out = coef[11 * N + i];
+    fmt_hess_apply_coef(hc, n, y, z, ND, false);
+    for (int ic = 0; ic < ncomp; ic++) {
+      const float fc = (float)c_g.fac[ic], i4pr = (float)c_g.inv_4pir[ic], i4pr2 = (float)c_g.inv_4pirsq[ic];
+      const long base = (long)ic * (ND + 2);
+      chan[base * N + i] = fc * (z[0] * i4pr2 + z[1] * i4pr + z[2]);
+#pragma unroll
+      for (int d = 0; d < ND; d++) chan[(base + 1 + d) * N + i] = fc * (z[4 + d] * i4pr + z[4 + ND + d]);
+      chan[(base + ND + 1) * N + i] = fc * z[3];
+    }
+    if (c_g.attraction)
+      for (int ic = 0; ic < ncomp; ic++) ymf[(long)ic * N + i] = -conv[(long)(NRB + ic) * N + i];
+  }
+}
+
+void launch_schur_local32(int ndim, const float *conv, const float *coef, float *chan, float *ymf, cudaStream_t s)
+{
+  if (ndim == 3) k_schur_local32<3><<<1184, kThreads, 0, s>>>(conv, coef, chan, ymf);
+  else if (ndim == 2) k_schur_local32<2><<<1184, kThreads, 0, s>>>(conv, coef, chan, ymf);
+  else k_schur_local32<1><<<1184, kThreads, 0, s>>>(conv, coef, chan, ymf);
+}
+
 // J v local step: channels of H v_rb for the EL rows.
 template <class T>
 __global__ void k_jv_local(const double *__restrict__ x, const double *__restrict__ v, double *__restrict__ chan,
@@ -987,6 +1072,31 @@ void launch_schur_combine(const double *x, const double *vext, const signed char
                           const double *tr, const double *ymf, double *y2, cudaStream_t s)
 {
   k_schur_combine<<<1184, kThreads, 0, s>>>(x, vext, zero, v2, tr, ymf, y2);
+}
+
+// k_schur_combine with the transposed sums and -u_MF in FP32 storage
+__global__ void k_schur_combine32(const double *__restrict__ x, const double *__restrict__ vext,
+                                  const signed char *__restrict__ zero, const double *__restrict__ v2,
+                                  const float *__restrict__ tr, const float *__restrict__ ymf, double *__restrict__ y2)
+{
+  const long N = c_g.N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    for (int ic = 0; ic < c_g.ncomp; ic++) {
+      const long k = (long)ic * N + i;
+      if (zero_row(vext, zero, ic, i)) {
+        y2[k] = log_row(vext, zero, ic, i) ? v2[k] / x[(long)(c_g.first_rho + ic) * N + i] : v2[k];
+      } else {
+        float a21y = tr[k];
+        if (c_g.attraction) a21y += ymf[k];
+        y2[k] = v2[k] / x[(long)(c_g.first_rho + ic) * N + i] - (double)a21y;
+      }
+    }
+}
+
+void launch_schur_combine32(const double *x, const double *vext, const signed char *zero, const double *v2,
+                            const float *tr, const float *ymf, double *y2, cudaStream_t s)
+{
+  k_schur_combine32<<<1184, kThreads, 0, s>>>(x, vext, zero, v2, tr, ymf, y2);
 }
 
 __global__ void k_jv_combine(const double *__restrict__ x, const double *__restrict__ vext,

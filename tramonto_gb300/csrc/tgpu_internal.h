@@ -88,6 +88,7 @@ bool fft_make_plan(FftPlan &p, const int P[3], const int nx[3], const int h[3], 
 // zero-density nodes of component zc >= 0)
 struct MapSrc {
   const double *src = nullptr;    // the channel [N]
+  const float *src32 = nullptr;   // the channel in FP32 (read instead of src when set; FP32 transforms only)
   int ndim = 3, nx[3] = {1, 1, 1};
   const int *map[3] = {nullptr, nullptr, nullptr};
   double bulk_lo = 0.0, bulk_hi = 0.0;
@@ -109,19 +110,23 @@ void rfft_inverse_products(const double2 *const *a, const double2 *const *k, int
                            const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
 void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
                            const FftPlan &p, double scale, double *out, bool accumulate, cudaStream_t s);
+void rfft_inverse_products(const float2 *const *a, const float2 *const *k, int nterms, float2 *work,
+                           const FftPlan &p, double scale, float *out, bool accumulate, cudaStream_t s);
 int fft_max_terms();
 // several FP32 transforms of one plan per launch (blockIdx.y selects the transform): forward transforms of nb mapped
 // channels into spec[b]; inverse transforms out[b] (+)= scale * inverse of a * k[b] (work[b] the half spectra)
 int fft_max_batch();
-// per-launch CUDA-event timing of the FP32 y/z FFT passes (off unless enabled; collect reads and resets)
-void pass_timer_enable(bool on);
-void pass_timer_collect(long *launches, double *ms_total, double *bytes_total, long *fields_total);
 void rfft_forward_mapped_batch(const MapSrc *m, int nb, float2 *const *spec, const FftPlan &p, cudaStream_t s);
 void rfft_forward_mapped_batch(const MapSrc *m, int nb, double2 *const *spec, const FftPlan &p, cudaStream_t s);
 void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,
                         double scale, double *const *out, bool accumulate, cudaStream_t s);
+void rfft_inverse_batch(const float2 *a, const float2 *const *k, int nb, float2 *const *work, const FftPlan &p,
+                        double scale, float *const *out, bool accumulate, cudaStream_t s);
 void rfft_inverse_batch(const double2 *a, const double2 *const *k, int nb, double2 *const *work, const FftPlan &p,
                         double scale, double *const *out, bool accumulate, cudaStream_t s);
+// per-launch CUDA-event timing of the FP32 y/z FFT passes (off unless enabled; collect reads and resets)
+void pass_timer_enable(bool on);
+void pass_timer_collect(long *launches, double *ms_total, double *bytes_total, long *fields_total);
 // one y (d = 1) or z (d = 2) pass over a half spectrum, in place (benchmark hook)
 void fft_pass(double2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s);
 void fft_pass(float2 *spec, const FftPlan &p, int d, bool inverse, cudaStream_t s);
@@ -515,6 +520,12 @@ void launch_assemble(const double *x, const double *vext, const signed char *zer
                      const double *tr, double *R, cudaStream_t s, unsigned *domain = nullptr);
 // coef: the state's Hessian scalars ([kHessCoef][N], launch_hess_coef) or null to evaluate them in place
 void launch_hess_coef(const double *x, double *coef, cudaStream_t s);
+// FP32 storage variants of the FP32 Schur product: the state's Hessian scalars and weighted densities as FP32 rows
+// [kHessCoef + nrb][N]; the local step and the combination on FP32 sums, channels and transposed sums
+void launch_hess_coef32(const double *x, float *coef, cudaStream_t s);
+void launch_schur_local32(int ndim, const float *conv, const float *coef, float *chan, float *ymf, cudaStream_t s);
+void launch_schur_combine32(const double *x, const double *vext, const signed char *zero, const double *v2,
+                            const float *tr, const float *ymf, double *y2, cudaStream_t s);
 void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
                         cudaStream_t s, bool f32 = false);
 // f32: the per-node Hessian in FP32 arithmetic (FP32 products)
