@@ -1089,9 +1089,10 @@ const double *hess_coef(Ctx *c)
   const int form = c->dg.jac_exact;
   if (c->hcoef_form == form) return c->d_hcoef;
   if (!c->d_hcoef) c->d_hcoef = dalloc<double>((size_t)tgpu::kHessCoef * c->dg.N);
-  tgpu::launch_hess_coef(c->d_x, c->d_hcoef, c->stream);
+  tgpu::launch_hess_coef(c->d_x, c->d_hcoef, c->stream, c->d_hcoef32);   // with the FP32 table once it exists
   c->stats.kernel_launches++;
   c->hcoef_form = form;
+  if (c->d_hcoef32) c->hcoef32_form = form;
   return c->d_hcoef;
 }
 
@@ -1137,9 +1138,13 @@ void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
     c->d_hcoef32 = dalloc<float>((size_t)(tgpu::kHessCoef + g.nrb) * N);
   }
   if (c->hcoef32_form != g.jac_exact) {
-    tgpu::launch_hess_coef32(c->d_x, c->d_hcoef32, c->stream);
-    c->stats.kernel_launches++;
-    c->hcoef32_form = g.jac_exact;
+    if (c->hcoef_form != g.jac_exact) {
+      hess_coef(c);   // both tables in one pass (the FP64 one serves the Schur right-hand side)
+    } else {
+      tgpu::launch_hess_coef32(c->d_x, c->d_hcoef32, c->stream);
+      c->stats.kernel_launches++;
+      c->hcoef32_form = g.jac_exact;
+    }
   }
   c->store32 = true;
   try {

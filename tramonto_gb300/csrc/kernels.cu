@@ -738,7 +738,8 @@ __device__ __forceinline__ void hess_apply_node_t(const double *x, const double 
   fmt_hess_apply_coef(c, n, y, z, nd, false);
 }
 
-__global__ void k_hess_coef(const double *__restrict__ x, double *__restrict__ coef)
+// coef32, when given, receives the FP32 table of k_hess_coef32 in the same pass
+__global__ void k_hess_coef(const double *__restrict__ x, double *__restrict__ coef, float *__restrict__ coef32)
 {
   const long N = c_g.N;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
@@ -748,12 +749,16 @@ __global__ void k_hess_coef(const double *__restrict__ x, double *__restrict__ c
     const double v[kHessCoef] = {c.a, c.a2, c.h13, c.h22, c.h23, c.h33, c.ff, c.gvf1, c.g2vr_f, c.g2vc_f, c.gvv,
                                  c.gvv_out};
     for (int k = 0; k < kHessCoef; k++) coef[(long)k * N + i] = v[k];
+    if (coef32) {
+      for (int k = 0; k < kHessCoef; k++) coef32[(long)k * N + i] = (float)v[k];
+      for (int k = 0; k < c_g.nrb; k++) coef32[(long)(kHessCoef + k) * N + i] = (float)n[k];
+    }
   }
 }
 
-void launch_hess_coef(const double *x, double *coef, cudaStream_t s)
+void launch_hess_coef(const double *x, double *coef, cudaStream_t s, float *coef32)
 {
-  k_hess_coef<<<1184, kThreads, 0, s>>>(x, coef);
+  k_hess_coef<<<1184, kThreads, 0, s>>>(x, coef, coef32);
 }
 
 // Transpose-convolution channels from a weighted-density-shaped vector q (n ordering):

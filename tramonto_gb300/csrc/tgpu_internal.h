@@ -519,7 +519,7 @@ void launch_fmt_local(const double *x, double *chan, cudaStream_t s, unsigned *d
 void launch_assemble(const double *x, const double *vext, const signed char *zero, const double *conv,
                      const double *tr, double *R, cudaStream_t s, unsigned *domain = nullptr);
 // coef: the state's Hessian scalars ([kHessCoef][N], launch_hess_coef) or null to evaluate them in place
-void launch_hess_coef(const double *x, double *coef, cudaStream_t s);
+void launch_hess_coef(const double *x, double *coef, cudaStream_t s, float *coef32 = nullptr);
 // FP32 storage variants of the FP32 Schur product: the state's Hessian scalars and weighted densities as FP32 rows
 // [kHessCoef + nrb][N]; the local step and the combination on FP32 sums, channels and transposed sums
 void launch_hess_coef32(const double *x, float *coef, cudaStream_t s);
