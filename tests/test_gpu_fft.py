@@ -192,3 +192,34 @@ def test_fp32_storage_schur_product_equals_the_fp64_storage_one():
     assert rel_err(again, first) <= 1e-6
     assert rel_err(again, S64) <= 1e-5
     s.close()
+
+
+@pytest.mark.parametrize("n", [96, 128])
+def test_fp32_fft_codelet_lengths(n):
+    """The compile-time codelets of the FP32 passes (y/z lengths 96 and 128, x lengths 150 and 180 at 96^3 and
+    128^3): with every FP32 sum an FFT the Schur product's nonlocal part and J v equal the FP64 products to 1e-5 of
+    their max norms, and the FP32 fill the FP64 fill to 1e-4."""
+    from tramonto_gb300 import native, setup
+    from goldens import rel_err
+    p, _ = setup.config2(n=n)
+    s = native.Solver(p)
+    x = setup.initial_state(s, p)
+    s.fill(x)
+    rng = np.random.default_rng(n)
+    v2 = rng.standard_normal((p.ncomp, p.nnodes))
+    v = rng.standard_normal((p.nunk, p.nnodes))
+    S64, J64 = s.schur(v2), s.jv(v)
+    s.set_precision(native.FP32)
+    s.set_fft32_policy(1)
+    S32, J32 = s.schur(v2), s.jv(v)
+    rho = x[p.first_rho:p.first_rho + p.ncomp]
+    live = (np.asarray(p.zero_density).reshape(rho.shape) == 0) & (np.asarray(p.vext).reshape(rho.shape) < p.vext_max)
+    local = np.where(live, v2 / np.where(live, rho, 1.0), v2)
+    print(n, "nonlocal Schur rel", rel_err(S32 - local, S64 - local), "Jv rel", rel_err(J32, J64))
+    assert rel_err(S32 - local, S64 - local) <= 1e-5 and rel_err(J32, J64) <= 1e-5
+    s.set_fill_arithmetic(native.FILL_FP32)
+    R32 = s.fill(x, mode=1)
+    s.set_fill_arithmetic(native.FILL_FP64)
+    R64 = s.fill(x, mode=1)
+    assert np.abs(R32 - R64).max() <= 1e-4 * max(1.0, np.abs(R64).max())
+    s.close()

@@ -453,8 +453,87 @@ __device__ __forceinline__ C *warp_fft(C *b0, C *b1, int n, const Stages &st, co
   return in;
 }
 
+// ---- compile-time codelets of the warp passes for the common lengths ------------------------------------------
+// The passes are bound by instruction issue; for the lengths the 3-D workloads use, the stages' radices, strides,
+// twiddle steps and the direction are template constants (no runtime switch, division or direction selects).  The
+// radices of N in stage order (fours first, then 2, 3, 5; any order gives the DFT in natural order):
+__host__ __device__ constexpr int ct_radix(int n, int s)
+{
+  for (int k = 0; n > 1; k++) {
+    const int r = n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : 0;
+    if (r == 0) return 0;
+    if (k == s) return r;
+    n /= r;
+  }
+  return 0;
+}
+__host__ __device__ constexpr int ct_ns(int n, int s)   // product of the radices before stage s
+{
+  int p = 1;
+  for (int k = 0; k < s; k++) p *= ct_radix(n, k);
+  return p;
+}
+__host__ __device__ constexpr bool ct_factors(int n)    // n a product of 2, 3, 5
+{
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  while (n % 5 == 0) n /= 5;
+  return n == 1;
+}
+
+template <int R, int N, int NS, bool INV, class C>
+__device__ __forceinline__ void warp_stage_ct(const C *src, C *dst, const C *tw, int lane)
+{
+  constexpr int nb = N / R, step = N / (NS * R);
+#pragma unroll
+  for (int j0 = 0; j0 < nb; j0 += 32) {
+    const int j = j0 + lane;
+    if (nb % 32 != 0 && j >= nb) break;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = src[j + r * nb];
+    const int q = j / NS, k = j - q * NS;
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        C w = tw[r * k * step];
+        if (INV) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    dft_small<R, C>(v, INV ? 1 : 0);
+    const int idx = q * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) dst[idx + r * NS] = v[r];
+  }
+}
+
+// the stages from S on, ping-ponging between the warp's two line buffers; returns the buffer with the result
+template <int N, int S, bool INV, class C>
+struct WarpFftCt {
+  static __device__ __forceinline__ C *run(C *in, C *out, const C *tw, int lane)
+  {
+    constexpr int R = ct_radix(N, S);
+    if constexpr (R == 0) {
+      return in;
+    } else {
+      warp_stage_ct<R, N, ct_ns(N, S), INV, C>(in, out, tw, lane);
+      __syncwarp();
+      return WarpFftCt<N, S + 1, INV, C>::run(out, in, tw, lane);
+    }
+  }
+};
+
+// warp_fft for the lengths with codelets (N = 0: the run-time stages)
+template <int N, bool INV, class C>
+__device__ __forceinline__ C *warp_fft_n(C *b0, C *b1, int n, const Stages &st, const C *tw, int lane)
+{
+  if constexpr (N == 0) return warp_fft<C>(b0, b1, n, st, tw, INV ? 1 : 0, lane);
+  else return WarpFftCt<N, 0, INV, C>::run(b0, b1, tw, lane);
+}
+
 // forward x pass: each warp packs two real lines into one complex line, transforms it and splits it
-template <class T, class C, class Src>
+template <class T, class C, class Src, int NC = 0>
 __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, XGeom g, Stages st,
                                                         const C *__restrict__ tw_g)
 {
@@ -462,7 +541,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
   C *__restrict__ spec = sb.spec[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
-  const int n = g.F0, ls = n + 1;
+  const int n = NC ? NC : g.F0, ls = n + 1;
   C *tw = sm + 2 * kWLines * ls;
   for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
   __syncthreads();
@@ -491,7 +570,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
       if (x0 + 32 * u < n) b0[x0 + 32 * u] = C{a[u], b[u]};
   }
   __syncwarp();
-  const C *res = warp_fft<C>(b0, b1, n, st, tw, 0, lane);
+  const C *res = warp_fft_n<NC, false, C>(b0, b1, n, st, tw, lane);
   for (int k = lane; k < g.Fh; k += 32) {
     const C Z = res[k], Zm = res[k == 0 ? 0 : n - k];
     spec[L * g.Fh + k] = C{(T)0.5 * (Z.x + Zm.x), (T)0.5 * (Z.y - Zm.y)};
@@ -501,7 +580,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
 
 // inverse x pass: each warp packs two half-spectrum lines into one complex line and writes the real and
 // imaginary parts of its inverse as the outputs of the interior nodes
-template <class C>
+template <class C, int NC = 0>
 __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom g, Stages st,
                                                          const C *__restrict__ tw_g, double scale, int accumulate)
 {
@@ -510,7 +589,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom
   float *__restrict__ out32 = ob.out32[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
-  const int n = g.F0, ls = n + 1;
+  const int n = NC ? NC : g.F0, ls = n + 1;
   C *tw = sm + 2 * kWLines * ls;
   for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
   __syncthreads();
@@ -540,7 +619,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom
     }
   }
   __syncwarp();
-  const C *res = warp_fft<C>(b0, b1, n, st, tw, 1, lane);
+  const C *res = warp_fft_n<NC, true, C>(b0, b1, n, st, tw, lane);
   const int nx0 = g.nx[0];
 #pragma unroll
   for (int h = 0; h < 2; h++) {
@@ -567,11 +646,12 @@ __global__ void __launch_bounds__(32 * kWLines) k_irfft_xw(OutBatch<C> ob, XGeom
 }
 
 // y and z passes: kWLines consecutive x at one outer index, one warp per line
-template <class C>
-__global__ void __launch_bounds__(32 * kWLines) k_fft_stridedw(PassBatch<C> pb, int X, int n, long es,
+template <class C, int NC, bool INV>
+__global__ void __launch_bounds__(32 * kWLines) k_fft_stridedw(PassBatch<C> pb, int X, int n_rt, long es,
                                                              long outer_stride, Stages st,
-                                                             const C *__restrict__ tw_g, int inv)
+                                                             const C *__restrict__ tw_g)
 {
+  const int n = NC ? NC : n_rt;
   const C *in = pb.in[blockIdx.y];
   C *out = pb.out[blockIdx.y];
   const Terms<C> &terms = pb.terms[blockIdx.y];
@@ -614,7 +694,7 @@ __global__ void __launch_bounds__(32 * kWLines) k_fft_stridedw(PassBatch<C> pb, 
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // every warp runs its line (beyond nl on stale data, never stored) so that all results sit in the same buffer
   C *b0 = sm + w * ls;
-  const C *res = warp_fft<C>(b0, sm + (kWLines + w) * ls, n, st, tw, inv, lane);
+  const C *res = warp_fft_n<NC, INV, C>(b0, sm + (kWLines + w) * ls, n, st, tw, lane);
   const int rofs = (int)(res - b0);   // 0 or kWLines * ls
   __syncthreads();
   for (int q = threadIdx.x; q < kWLines * n; q += blockDim.x) {
@@ -693,6 +773,22 @@ Stages stages(const FftAxis &a)
 
 size_t wtile_smem(int n) { return sizeof(float2) * (2 * (size_t)kWLines * (n + 1) + n); }
 
+// f(std::integral_constant<int, N>) for the lengths with codelets (the y/z lengths 96, 128, 256 and the x lengths
+// 150, 180, 320 of the 96^3, 128^3 and 256^3 workloads), f(std::integral_constant<int, 0>) otherwise
+template <class F>
+void with_length(int n, F &&f)
+{
+  switch (n) {
+    case 96: f(std::integral_constant<int, 96>{}); return;
+    case 128: f(std::integral_constant<int, 128>{}); return;
+    case 150: f(std::integral_constant<int, 150>{}); return;
+    case 180: f(std::integral_constant<int, 180>{}); return;
+    case 256: f(std::integral_constant<int, 256>{}); return;
+    case 320: f(std::integral_constant<int, 320>{}); return;
+    default: f(std::integral_constant<int, 0>{}); return;
+  }
+}
+
 template <class C>
 size_t tile_smem(int n)
 {
@@ -710,10 +806,20 @@ void set_smem_limits(const FftPlan &p)
   cudaFuncSetAttribute(k_fft_strided<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss);
   if (std::is_same<C, float2>::value) {
     const int wx = (int)wtile_smem(p.F[0]), ws = (int)std::max(wtile_smem(p.F[1]), wtile_smem(p.F[2]));
-    cudaFuncSetAttribute(k_rfft_xw<float, float2, BoxSrc<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
-    cudaFuncSetAttribute(k_rfft_xw<float, float2, MappedSrc<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
-    cudaFuncSetAttribute(k_irfft_xw<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
-    cudaFuncSetAttribute(k_fft_stridedw<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = decltype(L)::value;
+      cudaFuncSetAttribute(k_rfft_xw<float, float2, BoxSrc<float>, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           wx);
+      cudaFuncSetAttribute(k_rfft_xw<float, float2, MappedSrc<float>, NC>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
+      cudaFuncSetAttribute(k_irfft_xw<float2, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, wx);
+    });
+    for (int d = 1; d <= 2; d++)
+      with_length(p.F[d], [&](auto L) {
+        constexpr int NC = decltype(L)::value;
+        cudaFuncSetAttribute(k_fft_stridedw<float2, NC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);
+        cudaFuncSetAttribute(k_fft_stridedw<float2, NC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ws);
+      });
   }
 }
 
@@ -763,8 +869,16 @@ void strided_pass_batch(const PassBatch<C> &pb, int nb, const FftPlan &p, int d,
       cudaEventCreate(&e1);
       cudaEventRecord(e0, s);
     }
-    k_fft_stridedw<float2><<<dim3((unsigned)(xb * nouter), (unsigned)nb), 32 * kWLines, wtile_smem(n), s>>>(
-        pb, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+    const dim3 grid((unsigned)(xb * nouter), (unsigned)nb);
+    with_length(n, [&](auto L) {
+      constexpr int NC = decltype(L)::value;
+      if (inverse)
+        k_fft_stridedw<float2, NC, true><<<grid, 32 * kWLines, wtile_smem(n), s>>>(pb, X, n, es, outer,
+                                                                                   stages(p.ax[d]), tw);
+      else
+        k_fft_stridedw<float2, NC, false><<<grid, 32 * kWLines, wtile_smem(n), s>>>(pb, X, n, es, outer,
+                                                                                    stages(p.ax[d]), tw);
+    });
     if (timed) {
       cudaEventRecord(e1, s);
       double units = 0.0;   // half spectra moved
@@ -807,8 +921,11 @@ void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, c
     SrcBatch<Src, C> sb{};
     sb.src[0] = src;
     sb.spec[0] = spec;
-    k_rfft_xw<T, C, Src><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
-        sb, g, stages(p.ax[0]), tw[0]);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = decltype(L)::value;
+      k_rfft_xw<T, C, Src, NC><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
+          sb, g, stages(p.ax[0]), tw[0]);
+    });
   } else {
     SrcBatch<Src, C> sb{};
     sb.src[0] = src;
@@ -841,8 +958,11 @@ void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double 
     ob.spec[0] = spec;
     ob.out[0] = out;
     ob.out32[0] = out32;
-    k_irfft_xw<C><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
-        ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = decltype(L)::value;
+      k_irfft_xw<C, NC><<<(unsigned)((npairs + kWLines - 1) / kWLines), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
+          ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    });
   } else {
     OutBatch<C> ob{};
     ob.spec[0] = spec;
@@ -868,9 +988,12 @@ void rfft_forward_mapped_batch_impl(const MapSrc *m, int nb, C *const *spec, con
     pb.out[b] = spec[b];
   }
   if constexpr (std::is_same<C, float2>::value)
-    k_rfft_xw<T, C, MappedSrc<T>>
-        <<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
-            sb, g, stages(p.ax[0]), tw[0]);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = decltype(L)::value;
+      k_rfft_xw<T, C, MappedSrc<T>, NC>
+          <<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines, wtile_smem(p.F[0]), s>>>(
+              sb, g, stages(p.ax[0]), tw[0]);
+    });
   else
     k_rfft_x<T, C, MappedSrc<T>><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
                                    tile_smem<C>(p.F[0]), s>>>(sb, g, stages(p.ax[0]), tw[0]);
@@ -907,8 +1030,11 @@ void rfft_inverse_batch_impl(const C *a, const C *const *k, int nb, C *const *wo
   const XGeom g = xgeom(p);
   const long npairs = (g.nlines + 1) / 2;
   if constexpr (std::is_same<C, float2>::value)
-    k_irfft_xw<C><<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines,
-                    wtile_smem(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = decltype(L)::value;
+      k_irfft_xw<C, NC><<<dim3((unsigned)((npairs + kWLines - 1) / kWLines), (unsigned)nb), 32 * kWLines,
+                          wtile_smem(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    });
   else
     k_irfft_x<C><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
                    tile_smem<C>(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
