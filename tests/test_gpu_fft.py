@@ -196,9 +196,10 @@ def test_fp32_storage_schur_product_equals_the_fp64_storage_one():
 
 @pytest.mark.parametrize("n", [96, 128])
 def test_fp32_fft_codelet_lengths(n):
-    """The compile-time codelets of the FP32 passes (y/z lengths 96 and 128, x lengths 150 and 180 at 96^3 and
-    128^3): with every FP32 sum an FFT the Schur product's nonlocal part and J v equal the FP64 products to 1e-5 of
-    their max norms, and the FP32 fill the FP64 fill to 1e-4."""
+    """The compile-time codelets of the FP32 and FP64 passes (y/z lengths 96 and 128, x lengths 150 and 180 at 96^3
+    and 128^3): with every FP32 sum an FFT the Schur product's nonlocal part and J v equal the FP64 products to 1e-5
+    of their max norms, the FP32 fill the FP64 fill to 1e-4, and the FP64 FFT fill (every stencil by FFT) the direct
+    FP64 fill to 5e-12, as at 64^3."""
     from tramonto_gb300 import native, setup
     from goldens import rel_err
     p, _ = setup.config2(n=n)
@@ -222,4 +223,9 @@ def test_fp32_fft_codelet_lengths(n):
     s.set_fill_arithmetic(native.FILL_FP64)
     R64 = s.fill(x, mode=1)
     assert np.abs(R32 - R64).max() <= 1e-4 * max(1.0, np.abs(R64).max())
+    s.set_fill_arithmetic(native.FILL_FFT)
+    s.set_fft_threshold(0)
+    Rfft = s.fill(x, mode=1)
+    print(n, "FP64 FFT fill: max |R_fft - R_fp64|", np.abs(Rfft - R64).max())
+    assert np.abs(Rfft - R64).max() <= 5e-12
     s.close()

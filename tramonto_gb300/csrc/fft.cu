@@ -190,6 +190,84 @@ __device__ C *fft_tile(C *buf0, C *buf1, int n, int ls, int nlines, const Stages
   return in;
 }
 
+// ---- compile-time codelets for the common lengths -------------------------------------------------------------
+// The passes are bound by instruction issue; for the lengths the 3-D workloads use, the stages' radices, strides,
+// twiddle steps and the direction are template constants (no runtime switch, division or direction selects).  The
+// radices of N in stage order (fours first, then 2, 3, 5; any order gives the DFT in natural order):
+__host__ __device__ constexpr int ct_radix(int n, int s)
+{
+  for (int k = 0; n > 1; k++) {
+    const int r = n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : 0;
+    if (r == 0) return 0;
+    if (k == s) return r;
+    n /= r;
+  }
+  return 0;
+}
+__host__ __device__ constexpr int ct_ns(int n, int s)   // product of the radices before stage s
+{
+  int p = 1;
+  for (int k = 0; k < s; k++) p *= ct_radix(n, k);
+  return p;
+}
+__host__ __device__ constexpr bool ct_factors(int n)    // n a product of 2, 3, 5
+{
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  while (n % 5 == 0) n /= 5;
+  return n == 1;
+}
+
+template <int R, int N, int NS, bool INV, class C>
+__device__ __forceinline__ void fft_stage_ct(const C *in, C *out, int ls, int nlines, const C *tw)
+{
+  constexpr int nb = N / R, step = N / (NS * R);
+  for (int t = threadIdx.x; t < nlines * nb; t += blockDim.x) {
+    const int line = t / nb, j = t - line * nb;
+    const C *src = in + line * ls;
+    C *dst = out + line * ls;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = src[j + r * nb];
+    const int q = j / NS, k = j - q * NS;
+    if (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        C w = tw[r * k * step];
+        if (INV) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    dft_small<R, C>(v, INV ? 1 : 0);
+    const int idx = q * NS * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) dst[idx + r * NS] = v[r];
+  }
+}
+
+template <int N, int S, bool INV, class C>
+struct TileFftCt {
+  static __device__ __forceinline__ C *run(C *in, C *out, int ls, int nlines, const C *tw)
+  {
+    constexpr int R = ct_radix(N, S);
+    if constexpr (R == 0) {
+      return in;
+    } else {
+      fft_stage_ct<R, N, ct_ns(N, S), INV, C>(in, out, ls, nlines, tw);
+      __syncthreads();
+      return TileFftCt<N, S + 1, INV, C>::run(out, in, ls, nlines, tw);
+    }
+  }
+};
+
+// fft_tile for the lengths with codelets (N = 0: the run-time stages)
+template <int N, bool INV, class C>
+__device__ __forceinline__ C *tile_fft_n(C *b0, C *b1, int n, int ls, int nlines, const Stages &st, const C *tw)
+{
+  if constexpr (N == 0) return fft_tile<C>(b0, b1, n, ls, nlines, st, tw, INV ? 1 : 0);
+  else return TileFftCt<N, 0, INV, C>::run(b0, b1, ls, nlines, tw);
+}
+
 // Geometry of the real box as the x passes see it: where a line's values come from (forward) or go to (inverse)
 struct XGeom {
   int F0, F1, Fh;            // transform lengths along x and y, half-spectrum length along x
@@ -269,7 +347,7 @@ struct OutBatch {
 };
 
 // x pass of the forward transform: two real lines per complex line, split into two half-spectrum lines
-template <class T, class C, class Src>
+template <class T, class C, class Src, int NC = 0>
 __global__ void __launch_bounds__(kFftThreads) k_rfft_x(SrcBatch<Src, C> sb, XGeom g, Stages st,
                                                       const C *__restrict__ tw_g)
 {
@@ -277,7 +355,7 @@ __global__ void __launch_bounds__(kFftThreads) k_rfft_x(SrcBatch<Src, C> sb, XGe
   C *__restrict__ spec = sb.spec[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
-  const int n = g.F0, ls = n + 1;
+  const int n = NC ? NC : g.F0, ls = n + 1;
   C *b0 = sm, *b1 = sm + kFftLines * ls, *tw = b1 + kFftLines * ls;
   for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
   const long pair0 = (long)blockIdx.x * kFftLines;
@@ -296,7 +374,7 @@ __global__ void __launch_bounds__(kFftThreads) k_rfft_x(SrcBatch<Src, C> sb, XGe
     b0[l * ls + x] = C{v[0], v[1]};
   }
   __syncthreads();
-  const C *res = fft_tile<C>(b0, b1, n, ls, np, st, tw, 0);
+  const C *res = tile_fft_n<NC, false, C>(b0, b1, n, ls, np, st, tw);
   using R = T;
   for (int q = threadIdx.x; q < np * g.Fh; q += blockDim.x) {
     const int l = q / g.Fh, k = q - l * g.Fh;
@@ -309,7 +387,7 @@ __global__ void __launch_bounds__(kFftThreads) k_rfft_x(SrcBatch<Src, C> sb, XGe
 
 // x pass of the inverse transform: two half-spectrum lines as one complex line, written out as the real outputs
 // of the interior nodes (out[node] = scale * value, or += when accumulate)
-template <class C>
+template <class C, int NC = 0>
 __global__ void __launch_bounds__(kFftThreads) k_irfft_x(OutBatch<C> ob, XGeom g, Stages st,
                                                        const C *__restrict__ tw_g, double scale, int accumulate)
 {
@@ -317,7 +395,7 @@ __global__ void __launch_bounds__(kFftThreads) k_irfft_x(OutBatch<C> ob, XGeom g
   double *__restrict__ out = ob.out[blockIdx.y];
   extern __shared__ __align__(16) unsigned char smraw[];
   C *sm = reinterpret_cast<C *>(smraw);
-  const int n = g.F0, ls = n + 1;
+  const int n = NC ? NC : g.F0, ls = n + 1;
   C *b0 = sm, *b1 = sm + kFftLines * ls, *tw = b1 + kFftLines * ls;
   for (int q = threadIdx.x; q < n; q += blockDim.x) tw[q] = tw_g[q];
   const long pair0 = (long)blockIdx.x * kFftLines;
@@ -334,7 +412,7 @@ __global__ void __launch_bounds__(kFftThreads) k_irfft_x(OutBatch<C> ob, XGeom g
     b0[l * ls + k] = up ? C{A.x - B.y, A.y + B.x} : C{A.x + B.y, B.x - A.y};
   }
   __syncthreads();
-  const C *res = fft_tile<C>(b0, b1, n, ls, np, st, tw, 1);
+  const C *res = tile_fft_n<NC, true, C>(b0, b1, n, ls, np, st, tw);
   const int nx0 = g.nx[0];
   for (int q = threadIdx.x; q < np * 2 * nx0; q += blockDim.x) {
     const int lh = q / nx0, x = q - lh * nx0;
@@ -352,11 +430,11 @@ __global__ void __launch_bounds__(kFftThreads) k_irfft_x(OutBatch<C> ob, XGeom g
 
 // y and z passes: lines of element stride es; a CTA takes kFftLines consecutive x at one (outer) index; reads `in`
 // (or the products of `terms`) and writes `out` (in place when out == in)
-template <class C>
-__global__ void __launch_bounds__(kFftThreads) k_fft_strided(PassBatch<C> pb, int X, int n, long es,
-                                                           long outer_stride, Stages st, const C *__restrict__ tw_g,
-                                                           int inv)
+template <class C, int NC, bool INV>
+__global__ void __launch_bounds__(kFftThreads) k_fft_strided(PassBatch<C> pb, int X, int n_rt, long es,
+                                                           long outer_stride, Stages st, const C *__restrict__ tw_g)
 {
+  const int n = NC ? NC : n_rt;
   const C *in = pb.in[blockIdx.y];
   C *out = pb.out[blockIdx.y];
   const Terms<C> &terms = pb.terms[blockIdx.y];
@@ -394,7 +472,7 @@ __global__ void __launch_bounds__(kFftThreads) k_fft_strided(PassBatch<C> pb, in
     }
   }
   __syncthreads();
-  const C *res = fft_tile<C>(b0, b1, n, ls, nl, st, tw, inv);
+  const C *res = tile_fft_n<NC, INV, C>(b0, b1, n, ls, nl, st, tw);
   for (int q = threadIdx.x; q < kFftLines * n; q += blockDim.x) {
     const int e = q / kFftLines, l = q - e * kFftLines;
     if (l < nl) out[base + e * es + l] = res[l * ls + e];
@@ -454,32 +532,7 @@ __device__ __forceinline__ C *warp_fft(C *b0, C *b1, int n, const Stages &st, co
 }
 
 // ---- compile-time codelets of the warp passes for the common lengths ------------------------------------------
-// The passes are bound by instruction issue; for the lengths the 3-D workloads use, the stages' radices, strides,
-// twiddle steps and the direction are template constants (no runtime switch, division or direction selects).  The
-// radices of N in stage order (fours first, then 2, 3, 5; any order gives the DFT in natural order):
-__host__ __device__ constexpr int ct_radix(int n, int s)
-{
-  for (int k = 0; n > 1; k++) {
-    const int r = n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : 0;
-    if (r == 0) return 0;
-    if (k == s) return r;
-    n /= r;
-  }
-  return 0;
-}
-__host__ __device__ constexpr int ct_ns(int n, int s)   // product of the radices before stage s
-{
-  int p = 1;
-  for (int k = 0; k < s; k++) p *= ct_radix(n, k);
-  return p;
-}
-__host__ __device__ constexpr bool ct_factors(int n)    // n a product of 2, 3, 5
-{
-  while (n % 2 == 0) n /= 2;
-  while (n % 3 == 0) n /= 3;
-  while (n % 5 == 0) n /= 5;
-  return n == 1;
-}
+// (the radices' helpers ct_radix, ct_ns are defined with the tile codelets above)
 
 template <int R, int N, int NS, bool INV, class C>
 __device__ __forceinline__ void warp_stage_ct(const C *src, C *dst, const C *tw, int lane)
@@ -795,15 +848,30 @@ size_t tile_smem(int n)
   return sizeof(C) * (2 * (size_t)kFftLines * (n + 1) + n);
 }
 
+// the block-tile codelet length for C (the FP64 passes; the FP32 ones run one warp per line)
+template <class C>
+constexpr int tile_codelet(int n)
+{
+  return std::is_same<C, double2>::value ? n : 0;
+}
+
 template <class T, class C>
 void set_smem_limits(const FftPlan &p)
 {
   const int sx = (int)tile_smem<C>(p.F[0]);
-  cudaFuncSetAttribute(k_rfft_x<T, C, BoxSrc<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
-  cudaFuncSetAttribute(k_rfft_x<T, C, MappedSrc<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
-  cudaFuncSetAttribute(k_irfft_x<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+  with_length(p.F[0], [&](auto L) {
+    constexpr int NC = tile_codelet<C>(decltype(L)::value);
+    cudaFuncSetAttribute(k_rfft_x<T, C, BoxSrc<T>, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+    cudaFuncSetAttribute(k_rfft_x<T, C, MappedSrc<T>, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+    cudaFuncSetAttribute(k_irfft_x<C, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sx);
+  });
   const int ss = (int)std::max(tile_smem<C>(p.F[1]), tile_smem<C>(p.F[2]));
-  cudaFuncSetAttribute(k_fft_strided<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss);
+  for (int d = 1; d <= 2; d++)
+    with_length(p.F[d], [&](auto L) {
+      constexpr int NC = tile_codelet<C>(decltype(L)::value);
+      cudaFuncSetAttribute(k_fft_strided<C, NC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss);
+      cudaFuncSetAttribute(k_fft_strided<C, NC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, ss);
+    });
   if (std::is_same<C, float2>::value) {
     const int wx = (int)wtile_smem(p.F[0]), ws = (int)std::max(wtile_smem(p.F[1]), wtile_smem(p.F[2]));
     with_length(p.F[0], [&](auto L) {
@@ -890,8 +958,16 @@ void strided_pass_batch(const PassBatch<C> &pb, int nb, const FftPlan &p, int d,
     }
   } else {
     const int xblocks = (X + kFftLines - 1) / kFftLines;
-    k_fft_strided<C><<<dim3((unsigned)(xblocks * nouter), (unsigned)nb), kFftThreads, tile_smem<C>(n), s>>>(
-        pb, X, n, es, outer, stages(p.ax[d]), tw, inverse ? 1 : 0);
+    const dim3 grid((unsigned)(xblocks * nouter), (unsigned)nb);
+    with_length(n, [&](auto L) {
+      constexpr int NC = tile_codelet<C>(decltype(L)::value);
+      if (inverse)
+        k_fft_strided<C, NC, true><<<grid, kFftThreads, tile_smem<C>(n), s>>>(pb, X, n, es, outer, stages(p.ax[d]),
+                                                                             tw);
+      else
+        k_fft_strided<C, NC, false><<<grid, kFftThreads, tile_smem<C>(n), s>>>(pb, X, n, es, outer, stages(p.ax[d]),
+                                                                              tw);
+    });
   }
 }
 
@@ -930,8 +1006,11 @@ void rfft_forward_impl(const Src &src, bool padded, C *spec, const FftPlan &p, c
     SrcBatch<Src, C> sb{};
     sb.src[0] = src;
     sb.spec[0] = spec;
-    k_rfft_x<T, C, Src><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
-        sb, g, stages(p.ax[0]), tw[0]);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = tile_codelet<C>(decltype(L)::value);
+      k_rfft_x<T, C, Src, NC><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]),
+                                s>>>(sb, g, stages(p.ax[0]), tw[0]);
+    });
   }
   const Terms<C> none{};
   for (int d = 1; d <= 2; d++)
@@ -967,8 +1046,11 @@ void rfft_inverse_impl(const Terms<C> &terms, C *spec, const FftPlan &p, double 
     OutBatch<C> ob{};
     ob.spec[0] = spec;
     ob.out[0] = out;
-    k_irfft_x<C><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
-        ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = tile_codelet<C>(decltype(L)::value);
+      k_irfft_x<C, NC><<<(unsigned)((npairs + kFftLines - 1) / kFftLines), kFftThreads, tile_smem<C>(p.F[0]), s>>>(
+          ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    });
   }
 }
 
@@ -995,8 +1077,11 @@ void rfft_forward_mapped_batch_impl(const MapSrc *m, int nb, C *const *spec, con
               sb, g, stages(p.ax[0]), tw[0]);
     });
   else
-    k_rfft_x<T, C, MappedSrc<T>><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
-                                   tile_smem<C>(p.F[0]), s>>>(sb, g, stages(p.ax[0]), tw[0]);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = tile_codelet<C>(decltype(L)::value);
+      k_rfft_x<T, C, MappedSrc<T>, NC><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb),
+                                         kFftThreads, tile_smem<C>(p.F[0]), s>>>(sb, g, stages(p.ax[0]), tw[0]);
+    });
   for (int d = 1; d <= 2; d++)
     if (p.F[d] > 1) strided_pass_batch<C>(pb, nb, p, d, false, tw[d], s);
 }
@@ -1036,8 +1121,11 @@ void rfft_inverse_batch_impl(const C *a, const C *const *k, int nb, C *const *wo
                           wtile_smem(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
     });
   else
-    k_irfft_x<C><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
-                   tile_smem<C>(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    with_length(p.F[0], [&](auto L) {
+      constexpr int NC = tile_codelet<C>(decltype(L)::value);
+      k_irfft_x<C, NC><<<dim3((unsigned)((npairs + kFftLines - 1) / kFftLines), (unsigned)nb), kFftThreads,
+                         tile_smem<C>(p.F[0]), s>>>(ob, g, stages(p.ax[0]), tw[0], scale, accumulate ? 1 : 0);
+    });
 }
 
 }  // namespace
