@@ -289,6 +289,15 @@ struct BoxSrc {   // a padded channel, or a real box [F2][F1][F0] (off 0)
   {
     return p[(long)(z + g.off[2]) * sz + (long)(y + g.off[1]) * sy + x + g.off[0]];
   }
+  // a line's part of the address, then the element (the warp passes read a line at a time)
+  struct Line {
+    long base;
+  };
+  __device__ __forceinline__ Line line(const XGeom &g, int y, int z) const
+  {
+    return Line{(long)(z + g.off[2]) * sz + (long)(y + g.off[1]) * sy + g.off[0]};
+  }
+  __device__ __forceinline__ T at(const XGeom &, const Line &L, int x) const { return p[L.base + x]; }
 };
 template <class T>
 struct MappedSrc {   // the unpadded channel through the boundary maps (the padded box's values, computed)
@@ -312,6 +321,47 @@ struct MappedSrc {   // the unpadded channel through the boundary maps (the padd
     if (m.zc >= 0 && m.zero[(long)m.zc * m.N + node]) return (T)0;
     const T v = m.src32 ? (T)m.src32[node] : to_arith<T>(m.src[node]);
     return (__popc(refl & m.signmask) & 1) ? -v : v;
+  }
+  // the same with the y and z part of a line resolved once: the node offset and reflections of the line, or the
+  // sentinel of its first out-of-range dimension after x (x still decides first)
+  struct Line {
+    long base;
+    int refl, sent;   // sent 0: the line is inside
+  };
+  __device__ __forceinline__ Line line(const XGeom &g, int y, int z) const
+  {
+    Line L{0, 0, 0};
+    const int q[3] = {0, y + g.off[1], z + g.off[2]};
+    long idx[3] = {0, 0, 0};
+    for (int d = 1; d < m.ndim; d++) {
+      const int v = m.map[d][q[d]];
+      if (v < 0) {
+        L.sent = v;
+        return L;
+      }
+      if (v & kReflBit) L.refl |= 1 << d;
+      idx[d] = v & ~kReflBit;
+    }
+    L.base = (long)m.nx[0] * (idx[1] + (long)m.nx[1] * idx[2]);
+    return L;
+  }
+  __device__ __forceinline__ T sentinel(int v) const
+  {
+    if (v == kSentBulk) return (T)m.bulk_lo;
+    if (v == kSentBulkHi) return (T)m.bulk_hi;
+    if (v == kSentWall) return (T)0;
+    return (T)__longlong_as_double(0x7ff8000000000000ULL);
+  }
+  __device__ __forceinline__ T at(const XGeom &g, const Line &L, int x) const
+  {
+    const int v = m.map[0][x + g.off[0]];
+    if (v < 0) return sentinel(v);
+    if (L.sent) return sentinel(L.sent);
+    const int refl = L.refl | ((v & kReflBit) ? 1 : 0);
+    const long node = L.base + (v & ~kReflBit);
+    if (m.zc >= 0 && m.zero[(long)m.zc * m.N + node]) return (T)0;
+    const T val = m.src32 ? (T)m.src32[node] : to_arith<T>(m.src[node]);
+    return (__popc(refl & m.signmask) & 1) ? -val : val;
   }
 };
 
@@ -606,6 +656,9 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
   const int y0 = (int)(L % g.F1), z0 = (int)(L / g.F1);
   const int y1 = (int)((L + 1) % g.F1), z1 = (int)((L + 1) / g.F1);
   const bool r0 = y0 < g.ext[1] && z0 < g.ext[2], r1 = two && y1 < g.ext[1] && z1 < g.ext[2];
+  // (lines beyond the source's extent are zeros and read no map)
+  const typename Src::Line l0 = r0 ? src.line(g, y0, z0) : typename Src::Line{};
+  const typename Src::Line l1 = r1 ? src.line(g, y1, z1) : typename Src::Line{};
   for (int x0 = lane; x0 < n; x0 += 32 * kLoadBatch) {
     T a[kLoadBatch], b[kLoadBatch];
 #pragma unroll
@@ -614,8 +667,8 @@ __global__ void __launch_bounds__(32 * kWLines) k_rfft_xw(SrcBatch<Src, C> sb, X
       a[u] = 0;
       b[u] = 0;
       if (x < g.ext[0]) {
-        if (r0) a[u] = src(g, x, y0, z0);
-        if (r1) b[u] = src(g, x, y1, z1);
+        if (r0) a[u] = src.at(g, l0, x);
+        if (r1) b[u] = src.at(g, l1, x);
       }
     }
 #pragma unroll
