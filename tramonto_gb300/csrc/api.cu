@@ -210,6 +210,8 @@ struct Ctx : tgpu_ctx {
   // there while such a product runs
   bool store32 = false;
   float *d_conv32 = nullptr, *d_chan32 = nullptr, *d_tr32 = nullptr, *d_ymf32 = nullptr, *d_hcoef32 = nullptr;
+  double *d_inv32 = nullptr;           // 1/rho of the state's Euler-Lagrange rows, and their kinds (k_row_info32)
+  signed char *d_kind32 = nullptr;
   int hcoef32_form = -1;
 };
 
@@ -1092,7 +1094,11 @@ const double *hess_coef(Ctx *c)
   tgpu::launch_hess_coef(c->d_x, c->d_hcoef, c->stream, c->d_hcoef32);   // with the FP32 table once it exists
   c->stats.kernel_launches++;
   c->hcoef_form = form;
-  if (c->d_hcoef32) c->hcoef32_form = form;
+  if (c->d_hcoef32) {
+    tgpu::launch_row_info32(c->d_x, c->d_vext, c->d_zero, c->d_inv32, c->d_kind32, c->stream);
+    c->stats.kernel_launches++;
+    c->hcoef32_form = form;
+  }
   return c->d_hcoef;
 }
 
@@ -1136,13 +1142,16 @@ void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
     c->d_tr32 = dalloc<float>((size_t)g.ncomp * N);
     c->d_ymf32 = dalloc<float>((size_t)g.ncomp * N);
     c->d_hcoef32 = dalloc<float>((size_t)(tgpu::kHessCoef + g.nrb) * N);
+    c->d_inv32 = dalloc<double>((size_t)g.ncomp * N);
+    c->d_kind32 = dalloc<signed char>((size_t)g.ncomp * N);
   }
   if (c->hcoef32_form != g.jac_exact) {
     if (c->hcoef_form != g.jac_exact) {
       hess_coef(c);   // both tables in one pass (the FP64 one serves the Schur right-hand side)
     } else {
       tgpu::launch_hess_coef32(c->d_x, c->d_hcoef32, c->stream);
-      c->stats.kernel_launches++;
+      tgpu::launch_row_info32(c->d_x, c->d_vext, c->d_zero, c->d_inv32, c->d_kind32, c->stream);
+      c->stats.kernel_launches += 2;
       c->hcoef32_form = g.jac_exact;
     }
   }
@@ -1158,7 +1167,7 @@ void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
   }
   c->store32 = false;
   c->pad_src32 = nullptr;
-  tgpu::launch_schur_combine32(c->d_x, c->d_vext, c->d_zero, d_v2, c->d_tr32, c->d_ymf32, d_y2, c->stream);
+  tgpu::launch_schur_combine32(c->d_inv32, c->d_kind32, d_v2, c->d_tr32, c->d_ymf32, d_y2, c->stream);
   c->stats.kernel_launches += 2;
   c->stats.schur_applies++;
 }
@@ -2595,6 +2604,7 @@ int tgpu_destroy(tgpu_handle h)
     dfree(c->cr.d_node); dfree(c->cr.d_rptr); dfree(c->cr.d_rcol); dfree(c->cr.d_ra);
     dfree(c->cr.d_pptr); dfree(c->cr.d_pcol); dfree(c->cr.d_pw); dfree(c->cr.d_kind); dfree(c->d_rowkind);
     dfree(c->d_conv32); dfree(c->d_chan32); dfree(c->d_tr32); dfree(c->d_ymf32); dfree(c->d_hcoef32);
+    dfree(c->d_inv32); dfree(c->d_kind32);
     for (int d = 0; d < 3; d++) dfree(c->d_map[d]);
     tgpu::tc_free_slab(c->tcslab);
     dfree(c->d_vext); dfree(c->d_zero); dfree(c->d_bnodes); dfree(c->d_fmask); dfree(c->d_hw_targets);
@@ -2702,6 +2712,7 @@ int tgpu_set_vext(tgpu_handle h, const double *vext)
     for (size_t i = 0; i < n; i++)
       if (std::isnan(vext[i])) throw Error(TGPU_ERR_NONFINITE, "NaN in the external field");
     c->h_vext.assign(vext, vext + n);
+    c->hcoef32_form = -1;   // the FP32 products' row kinds follow V_ext (vext_max rows)
     if (c->finalized) ck(cudaMemcpyAsync(c->d_vext, vext, n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "h2d");
     ck(cudaStreamSynchronize(c->stream), "sync");
     return TGPU_OK;

@@ -1079,29 +1079,52 @@ void launch_schur_combine(const double *x, const double *vext, const signed char
   k_schur_combine<<<1184, kThreads, 0, s>>>(x, vext, zero, v2, tr, ymf, y2);
 }
 
-// k_schur_combine with the transposed sums and -u_MF in FP32 storage
-__global__ void k_schur_combine32(const double *__restrict__ x, const double *__restrict__ vext,
-                                  const signed char *__restrict__ zero, const double *__restrict__ v2,
-                                  const float *__restrict__ tr, const float *__restrict__ ymf, double *__restrict__ y2)
+// The Euler-Lagrange rows of a state for the FP32 products: kind 0 a full row, 1 a row ln rho - ln c (pinned,
+// BULK_ZONE, PB_ZONE), 2 a zero-density row; inv = 1/rho (0 on zero-density rows), in FP64: the local part v2 / rho
+// dominates the product near walls, where rho is small
+__global__ void k_row_info32(const double *__restrict__ x, const double *__restrict__ vext,
+                             const signed char *__restrict__ zero, double *__restrict__ inv,
+                             signed char *__restrict__ kind)
 {
   const long N = c_g.N;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     for (int ic = 0; ic < c_g.ncomp; ic++) {
       const long k = (long)ic * N + i;
-      if (zero_row(vext, zero, ic, i)) {
-        y2[k] = log_row(vext, zero, ic, i) ? v2[k] / x[(long)(c_g.first_rho + ic) * N + i] : v2[k];
-      } else {
-        float a21y = tr[k];
-        if (c_g.attraction) a21y += ymf[k];
-        y2[k] = v2[k] / x[(long)(c_g.first_rho + ic) * N + i] - (double)a21y;
-      }
+      const bool zr = zero_row(vext, zero, ic, i), lr = zr && log_row(vext, zero, ic, i);
+      kind[k] = !zr ? 0 : lr ? 1 : 2;
+      inv[k] = (!zr || lr) ? 1.0 / x[(long)(c_g.first_rho + ic) * N + i] : 0.0;
     }
 }
 
-void launch_schur_combine32(const double *x, const double *vext, const signed char *zero, const double *v2,
-                            const float *tr, const float *ymf, double *y2, cudaStream_t s)
+void launch_row_info32(const double *x, const double *vext, const signed char *zero, double *inv, signed char *kind,
+                       cudaStream_t s)
 {
-  k_schur_combine32<<<1184, kThreads, 0, s>>>(x, vext, zero, v2, tr, ymf, y2);
+  k_row_info32<<<1184, kThreads, 0, s>>>(x, vext, zero, inv, kind);
+}
+
+// k_schur_combine with the transposed sums and -u_MF in FP32 storage and the rows of k_row_info32 (no FP64 division
+// or comparison per product)
+__global__ void k_schur_combine32(const double *__restrict__ inv, const signed char *__restrict__ kind,
+                                  const double *__restrict__ v2, const float *__restrict__ tr,
+                                  const float *__restrict__ ymf, double *__restrict__ y2)
+{
+  const long n = (long)c_g.ncomp * c_g.N;
+  const bool att = c_g.attraction != 0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const int kd = kind[k];
+    if (kd == 2) {
+      y2[k] = v2[k];
+    } else {
+      const double t = v2[k] * inv[k];
+      y2[k] = kd == 0 ? t - (double)(att ? tr[k] + ymf[k] : tr[k]) : t;
+    }
+  }
+}
+
+void launch_schur_combine32(const double *inv, const signed char *kind, const double *v2, const float *tr,
+                            const float *ymf, double *y2, cudaStream_t s)
+{
+  k_schur_combine32<<<1184, kThreads, 0, s>>>(inv, kind, v2, tr, ymf, y2);
 }
 
 __global__ void k_jv_combine(const double *__restrict__ x, const double *__restrict__ vext,

@@ -524,8 +524,10 @@ void launch_hess_coef(const double *x, double *coef, cudaStream_t s, float *coef
 // [kHessCoef + nrb][N]; the local step and the combination on FP32 sums, channels and transposed sums
 void launch_hess_coef32(const double *x, float *coef, cudaStream_t s);
 void launch_schur_local32(int ndim, const float *conv, const float *coef, float *chan, float *ymf, cudaStream_t s);
-void launch_schur_combine32(const double *x, const double *vext, const signed char *zero, const double *v2,
-                            const float *tr, const float *ymf, double *y2, cudaStream_t s);
+void launch_row_info32(const double *x, const double *vext, const signed char *zero, double *inv, signed char *kind,
+                       cudaStream_t s);
+void launch_schur_combine32(const double *inv, const signed char *kind, const double *v2, const float *tr,
+                            const float *ymf, double *y2, cudaStream_t s);
 void launch_schur_local(const double *x, const double *conv, double *chan, double *ymf, const double *coef,
                         cudaStream_t s, bool f32 = false);
 // f32: the per-node Hessian in FP32 arithmetic (FP32 products)
