@@ -229,3 +229,27 @@ def test_fp32_fft_codelet_lengths(n):
     print(n, "FP64 FFT fill: max |R_fft - R_fp64|", np.abs(Rfft - R64).max())
     assert np.abs(Rfft - R64).max() <= 5e-12
     s.close()
+
+
+def test_pass_timer_counts_the_fp32_pass_launches():
+    """tgpu_pass_timer_begin/_end: over one FP32 Schur product with every sum an FFT it sees the y/z pass launches
+    (two per transform batch), their summed duration, and per transform at least the half spectrum written and read
+    once (8 bytes per complex point each way)."""
+    from tramonto_gb300 import native, setup
+    p, _ = setup.config2(n=40)
+    s = native.Solver(p)
+    x = setup.initial_state(s, p)
+    s.fill(x)
+    s.set_precision(native.FP32)
+    s.set_fft32_policy(1)
+    v2 = np.random.default_rng(2).standard_normal((p.ncomp, p.nnodes))
+    s.schur(v2)
+    s.pass_timer_begin()
+    s.schur(v2)
+    launches, ms, nbytes, transforms = s.pass_timer_end()
+    _, nh, _ = s.time_fft_pass(native.FP32, 1, reps=1)
+    print("launches", launches, "ms", ms, "bytes", nbytes, "transforms", transforms)
+    assert launches > 0 and launches % 2 == 0 and ms > 0.0
+    assert transforms >= launches and nbytes >= transforms * 2 * 8 * nh
+    assert s.pass_timer_end()[0] == 0          # the timer is off and empty after end
+    s.close()
