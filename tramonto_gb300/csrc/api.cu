@@ -1132,7 +1132,8 @@ bool schur_store32_ok(Ctx *c)
   return true;
 }
 
-void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
+// the FP32 storage's buffers, and the state's FP32 Hessian table and row table (made from the FP64 evaluation)
+void ensure_store32(Ctx *c)
 {
   const tgpu::DevGeom &g = c->dg;
   const size_t N = (size_t)g.N;
@@ -1146,15 +1147,17 @@ void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
     c->d_kind32 = dalloc<signed char>((size_t)g.ncomp * N);
   }
   if (c->hcoef32_form != g.jac_exact) {
-    if (c->hcoef_form != g.jac_exact) {
-      hess_coef(c);   // both tables in one pass (the FP64 one serves the Schur right-hand side)
-    } else {
-      tgpu::launch_hess_coef32(c->d_x, c->d_hcoef32, c->stream);
-      tgpu::launch_row_info32(c->d_x, c->d_vext, c->d_zero, c->d_inv32, c->d_kind32, c->stream);
-      c->stats.kernel_launches += 2;
-      c->hcoef32_form = g.jac_exact;
-    }
+    tgpu::launch_hess_coef32(c->d_x, c->d_hcoef32, c->stream);
+    tgpu::launch_row_info32(c->d_x, c->d_vext, c->d_zero, c->d_inv32, c->d_kind32, c->stream);
+    c->stats.kernel_launches += 2;
+    c->hcoef32_form = g.jac_exact;
   }
+}
+
+void schur_device_store32(Ctx *c, const double *d_v2, double *d_y2)
+{
+  const tgpu::DevGeom &g = c->dg;
+  ensure_store32(c);
   c->store32 = true;
   try {
     forward_pass(c, d_v2, c->pads.rho_jac, true);
@@ -1230,8 +1233,25 @@ void schur_rhs_device(Ctx *c, const double *d_b, double *d_b2s)
     tgpu::launch_prolong(c->d_cscr, g.first_rb, g.nunk - g.ncomp, g.nunk, g.N, c->cr, nullptr, c->stream);
     b = c->d_cscr;
   }
-  tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
   TcScope tcs(c);
+  if (prod_f32(c) && schur_store32_ok(c)) {   // the FP32 products' right-hand side in FP32 storage
+    ensure_store32(c);
+    tgpu::launch_rhs_local32(g.ndim, b, c->d_hcoef32, c->d_chan32, c->d_ymf32, c->stream);
+    c->store32 = true;
+    try {
+      transpose_pass(c, c->pads.tr_jac, true);
+    } catch (...) {
+      c->store32 = false;
+      c->pad_src32 = nullptr;
+      throw;
+    }
+    c->store32 = false;
+    c->pad_src32 = nullptr;
+    tgpu::launch_rhs_combine32(c->d_kind32, b, c->d_tr32, c->d_ymf32, d_b2s, c->stream);
+    c->stats.kernel_launches += 2;
+    return;
+  }
+  tgpu::launch_rhs_local(c->d_x, b, c->d_chan, c->d_ymf, hess_coef(c), c->stream);
   transpose_pass(c, c->pads.tr_jac, prod_f32(c));
   tgpu::launch_rhs_combine(c->d_vext, c->d_zero, b, c->d_tr, c->d_ymf, d_b2s, c->stream);
   if (c->coarse()) tgpu::launch_zero_nodes(d_b2s, g.ncomp, g.N, c->cr, c->stream);

@@ -1198,6 +1198,88 @@ void launch_rhs_local(const double *x, const double *b, double *chan, double *ym
   k_rhs_local<<<1184, kThreads, 0, s>>>(x, b, chan, ymf, coef);
 }
 
+// k_rhs_local in FP32 storage (the FP32 products' right-hand side b2 - A21 A11^-1 b1: FP32 arithmetic on the FP32
+// table of the state, FP32 channels for the FP32 transposed sums; ymf = -b_MF)
+template <int ND>
+__global__ void k_rhs_local32(const double *__restrict__ b, const float *__restrict__ coef, float *__restrict__ chan,
+                              float *__restrict__ ymf)
+{
+  constexpr int NRB = 4 + 2 * ND;
+  const long N = c_g.N;
+  int src_k[NRB];
+  float dep_c[NRB];
+  bool dep[NRB];
+#pragma unroll
+  for (int k = 0; k < NRB; k++) {
+    double cd = 0.0;
+    dep[k] = dep_rb(k, &src_k[k], &cd);
+    dep_c[k] = (float)cd;
+  }
+  const int ncomp = c_g.ncomp;
+  const double *brb = b + (long)c_g.first_rb * N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    float ysv[NRB], y[NRB], z[NRB], n[NRB];
+#pragma unroll
+    for (int k = 0; k < NRB; k++) {
+      const float bk = (float)brb[(long)k * N + i];
+      ysv[k] = dep[k] ? -bk - dep_c[k] * (float)brb[(long)src_k[k] * N + i] : -bk;
+    }
+    y[0] = ysv[3]; y[1] = ysv[2]; y[2] = ysv[1]; y[3] = ysv[0];
+#pragma unroll
+    for (int d = 0; d < ND; d++) { y[4 + d] = ysv[4 + ND + d]; y[4 + ND + d] = ysv[4 + d]; }
+#pragma unroll
+    for (int k = 0; k < NRB; k++) n[k] = coef[(long)(kHessCoef + k) * N + i];
+    HessCoefT<float> hc;
+    hc.a = coef[i];
+    hc.a2 = coef[N + i];
+    hc.h13 = coef[2 * N + i];
+    hc.h22 = coef[3 * N + i];
+    hc.h23 = coef[4 * N + i];
+    hc.h33 = coef[5 * N + i];
+    hc.ff = coef[6 * N + i];
+    hc.gvf1 = coef[7 * N + i];
+    hc.g2vr_f = coef[8 * N + i];
+    hc.g2vc_f = coef[9 * N + i];
+    hc.gvv = coef[10 * N + i];
+    hc.gvv_out = coef[11 * N + i];
+    fmt_hess_apply_coef(hc, n, y, z, ND, false);
+    for (int ic = 0; ic < ncomp; ic++) {
+      const float fc = (float)c_g.fac[ic], i4pr = (float)c_g.inv_4pir[ic], i4pr2 = (float)c_g.inv_4pirsq[ic];
+      const long base = (long)ic * (ND + 2);
+      chan[base * N + i] = fc * (z[0] * i4pr2 + z[1] * i4pr + z[2]);
+#pragma unroll
+      for (int d = 0; d < ND; d++) chan[(base + 1 + d) * N + i] = fc * (z[4 + d] * i4pr + z[4 + ND + d]);
+      chan[(base + ND + 1) * N + i] = fc * z[3];
+    }
+    if (c_g.attraction)
+      for (int ic = 0; ic < ncomp; ic++) ymf[(long)ic * N + i] = -(float)b[(long)(c_g.first_mf + ic) * N + i];
+  }
+}
+
+void launch_rhs_local32(int ndim, const double *b, const float *coef, float *chan, float *ymf, cudaStream_t s)
+{
+  if (ndim == 3) k_rhs_local32<3><<<1184, kThreads, 0, s>>>(b, coef, chan, ymf);
+  else if (ndim == 2) k_rhs_local32<2><<<1184, kThreads, 0, s>>>(b, coef, chan, ymf);
+  else k_rhs_local32<1><<<1184, kThreads, 0, s>>>(b, coef, chan, ymf);
+}
+
+// b2s = b2 - A21 y1 on full Euler-Lagrange rows (the rows' kinds from k_row_info32), b2 elsewhere
+__global__ void k_rhs_combine32(const signed char *__restrict__ kind, const double *__restrict__ b,
+                                const float *__restrict__ tr, const float *__restrict__ ymf, double *__restrict__ b2s)
+{
+  const long n = (long)c_g.ncomp * c_g.N;
+  const bool att = c_g.attraction != 0;
+  const double *b2 = b + (long)c_g.first_rho * c_g.N;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+    b2s[k] = kind[k] == 0 ? b2[k] - (double)(att ? tr[k] + ymf[k] : tr[k]) : b2[k];
+}
+
+void launch_rhs_combine32(const signed char *kind, const double *b, const float *tr, const float *ymf, double *b2s,
+                          cudaStream_t s)
+{
+  k_rhs_combine32<<<1184, kThreads, 0, s>>>(kind, b, tr, ymf, b2s);
+}
+
 __global__ void k_rhs_combine(const double *__restrict__ vext, const signed char *__restrict__ zero,
                               const double *__restrict__ b, const double *__restrict__ tr,
                               const double *__restrict__ ymf, double *__restrict__ b2s)

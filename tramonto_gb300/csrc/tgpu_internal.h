@@ -524,6 +524,9 @@ void launch_hess_coef(const double *x, double *coef, cudaStream_t s, float *coef
 // [kHessCoef + nrb][N]; the local step and the combination on FP32 sums, channels and transposed sums
 void launch_hess_coef32(const double *x, float *coef, cudaStream_t s);
 void launch_schur_local32(int ndim, const float *conv, const float *coef, float *chan, float *ymf, cudaStream_t s);
+void launch_rhs_local32(int ndim, const double *b, const float *coef, float *chan, float *ymf, cudaStream_t s);
+void launch_rhs_combine32(const signed char *kind, const double *b, const float *tr, const float *ymf, double *b2s,
+                          cudaStream_t s);
 void launch_row_info32(const double *x, const double *vext, const signed char *zero, double *inv, signed char *kind,
                        cudaStream_t s);
 void launch_schur_combine32(const double *inv, const signed char *kind, const double *v2, const float *tr,
