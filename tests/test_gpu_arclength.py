@@ -144,3 +144,24 @@ def test_turning_point_continuation_in_the_wall_strength(branch):
         d1 = np.diff(mus) * np.sign(eps[1] - eps[0])
         assert np.all(d1 < 0)
         assert np.max(np.abs(np.diff(d1))) <= 0.1 * np.min(np.abs(d1))
+
+
+def test_phase_transition_between_the_spinodals(branch):
+    """The reference's phase-transition algorithm (isotherm.phase_transition) started from a point of the dilute
+    branch and one of the condensed branch near the middle of the hysteresis loop converges to two states at one
+    beta mu (||R||_2 <= 1e-9 each) with equal grand free energy (|g| <= 1e-9 of |Omega|), the condensed one holding
+    more particles, at a beta mu strictly between the evaporation and condensation turning points."""
+    from tramonto_gb300 import isotherm
+    recs, _ = branch
+    tp = _turning_points(recs)
+    mu_cond, mu_evap = recs[tp[0]]["betamu"], recs[tp[1]]["betamu"]
+    mu0 = 0.5 * (mu_cond + mu_evap)
+    lo = min(recs[1:tp[0]], key=lambda r: abs(r["betamu"] - mu0))
+    hi = min(recs[tp[1] + 1:], key=lambda r: abs(r["betamu"] - mu0))
+    rec = isotherm.phase_transition(_spec(), lo["x"], hi["x"], mu0, tol=1e-9)
+    print("coexistence: beta mu", rec["betamu"], "N", rec["N1"], rec["N2"], "iters", rec["iters"], "g", rec["g"],
+          "spinodals", mu_evap, mu_cond, "starts", lo["betamu"], hi["betamu"])
+    assert rec["converged"] and rec["resid"] <= 1e-9
+    assert mu_evap < rec["betamu"] < mu_cond
+    assert rec["N2"] > rec["N1"] + 0.5
+    assert abs(rec["g"]) <= 1e-8
