@@ -441,63 +441,68 @@ def phase_transition(spec, x1, x2, mu0, tol=1e-9, max_iter=30, perturb=1e-6, log
     s = native.Solver(p)
     try:
         set_mode(s, False)
-        r0 = p.first_rho
-        live = _live_rows(p)[0]
-        R_mu = np.zeros(s.shape)
-        R_mu[r0][live] = -1.0
-        x1, x2, mu = np.array(x1, np.float64), np.array(x2, np.float64), float(mu0)
-
-        def lin(rhs):
-            return s.solve(rhs, tol=1e-12, max_iter=2000)[0]
-
-        def g(y1, y2, m):
-            return grand_free_energy(s, p, y1, m) - grand_free_energy(s, p, y2, m)
-
-        def dirder(g0, v1, v2):
-            """(g(x1 + h v1, x2 + h v2) - g) / h; the backward difference, then smaller steps, where a step leaves
-            the functional's domain."""
-            h = perturb * np.sqrt(np.sum(x1 * x1) / (np.sum(v1 * v1) + perturb)
-                                  + np.sum(x2 * x2) / (np.sum(v2 * v2) + perturb))
-            for hh in (h, -h, h / 16, -h / 16):
-                try:
-                    return (g(x1 + hh * v1, x2 + hh * v2, mu) - g0) / hh
-                except native.TgpuError as err:
-                    if err.status != native.TGPU_ERR_DOMAIN:
-                        raise
-            raise native.TgpuError(native.TGPU_ERR_DOMAIN, "no finite-difference step inside the domain")
-
-        def frac(x, dx):
-            rho, drho = x[r0], dx[r0]
-            neg = live & (drho < -0.9 * rho)
-            return min(1.0, float(np.min(-0.9 * rho[neg] / drho[neg]))) if neg.any() else 1.0
-
-        rn, gv, dmu = float("inf"), float("inf"), float("inf")
-        for it in range(max_iter + 1):
-            s.set_chemical_potential([mu])
-            R1 = s.fill(x1, mode=0)
-            a1, b1 = lin(R1), lin(R_mu)
-            R2 = s.fill(x2, mode=0)
-            a2, b2 = lin(R2), lin(R_mu)
-            rn = max(float(np.linalg.norm(R1)), float(np.linalg.norm(R2)))
-            gv = g(x1, x2, mu)
-            if log is not None:
-                log(it, mu, rn, gv)
-            if it > 0 and rn <= tol and abs(dmu) <= 1e-10 * (1.0 + abs(mu)):
-                return dict(betamu=mu, x1=x1, x2=x2, N1=float(adsorption(p, x1)[0]), N2=float(adsorption(p, x2)[0]),
-                            resid=rn, g=gv, iters=it, converged=True)
-            if it == max_iter:
-                break
-            hm = perturb * (abs(mu) + perturb)
-            g_mu = (g(x1, x2, mu + hm) - gv) / hm
-            Da, Db = dirder(gv, a1, a2), dirder(gv, b1, b2)
-            den = Db - g_mu
-            if den == 0.0 or not np.isfinite(den):
-                break
-            dmu = (gv - Da) / den
-            dx1, dx2 = -a1 - dmu * b1, -a2 - dmu * b2
-            f = min(frac(x1, dx1), frac(x2, dx2))
-            x1, x2, mu = x1 + f * dx1, x2 + f * dx2, mu + f * dmu
-        return dict(betamu=mu, x1=x1, x2=x2, N1=float(adsorption(p, x1)[0]), N2=float(adsorption(p, x2)[0]),
-                    resid=rn, g=gv, iters=max_iter, converged=False)
+        return _pt_solver(s, p, x1, x2, mu0, tol, max_iter, perturb, log)
     finally:
         s.close()
+
+
+def _pt_solver(s, p, x1, x2, mu0, tol=1e-9, max_iter=30, perturb=1e-6, log=None):
+    """phase_transition's iterations on a live solver (any object with the Solver methods it calls)."""
+    r0 = p.first_rho
+    live = _live_rows(p)[0]
+    R_mu = np.zeros(s.shape)
+    R_mu[r0][live] = -1.0
+    x1, x2, mu = np.array(x1, np.float64), np.array(x2, np.float64), float(mu0)
+
+    def lin(rhs):
+        return s.solve(rhs, tol=1e-12, max_iter=2000)[0]
+
+    def g(y1, y2, m):
+        return grand_free_energy(s, p, y1, m) - grand_free_energy(s, p, y2, m)
+
+    def dirder(g0, v1, v2):
+        """(g(x1 + h v1, x2 + h v2) - g) / h; the backward difference, then smaller steps, where a step leaves
+        the functional's domain."""
+        h = perturb * np.sqrt(np.sum(x1 * x1) / (np.sum(v1 * v1) + perturb)
+                              + np.sum(x2 * x2) / (np.sum(v2 * v2) + perturb))
+        for hh in (h, -h, h / 16, -h / 16):
+            try:
+                return (g(x1 + hh * v1, x2 + hh * v2, mu) - g0) / hh
+            except native.TgpuError as err:
+                if err.status != native.TGPU_ERR_DOMAIN:
+                    raise
+        raise native.TgpuError(native.TGPU_ERR_DOMAIN, "no finite-difference step inside the domain")
+
+    def frac(x, dx):
+        rho, drho = x[r0], dx[r0]
+        neg = live & (drho < -0.9 * rho)
+        return min(1.0, float(np.min(-0.9 * rho[neg] / drho[neg]))) if neg.any() else 1.0
+
+    rn, gv, dmu = float("inf"), float("inf"), float("inf")
+    for it in range(max_iter + 1):
+        s.set_chemical_potential([mu])
+        R1 = s.fill(x1, mode=0)
+        a1, b1 = lin(R1), lin(R_mu)
+        R2 = s.fill(x2, mode=0)
+        a2, b2 = lin(R2), lin(R_mu)
+        rn = max(float(np.linalg.norm(R1)), float(np.linalg.norm(R2)))
+        gv = g(x1, x2, mu)
+        if log is not None:
+            log(it, mu, rn, gv)
+        if it > 0 and rn <= tol and abs(dmu) <= 1e-10 * (1.0 + abs(mu)):
+            return dict(betamu=mu, x1=x1, x2=x2, N1=float(adsorption(p, x1)[0]), N2=float(adsorption(p, x2)[0]),
+                        resid=rn, g=gv, iters=it, converged=True)
+        if it == max_iter:
+            break
+        hm = perturb * (abs(mu) + perturb)
+        g_mu = (g(x1, x2, mu + hm) - gv) / hm
+        Da, Db = dirder(gv, a1, a2), dirder(gv, b1, b2)
+        den = Db - g_mu
+        if den == 0.0 or not np.isfinite(den):
+            break
+        dmu = (gv - Da) / den
+        dx1, dx2 = -a1 - dmu * b1, -a2 - dmu * b2
+        f = min(frac(x1, dx1), frac(x2, dx2))
+        x1, x2, mu = x1 + f * dx1, x2 + f * dx2, mu + f * dmu
+    return dict(betamu=mu, x1=x1, x2=x2, N1=float(adsorption(p, x1)[0]), N2=float(adsorption(p, x2)[0]),
+                resid=rn, g=gv, iters=max_iter, converged=False)
