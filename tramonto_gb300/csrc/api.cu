@@ -2501,7 +2501,8 @@ void build_device_tables(Ctx *c)
   c->d_gt = dalloc<double>(c->n2);
   c->d_gx = dalloc<double>(c->n2);
   c->d_gb = dalloc<double>(c->n2);
-  c->d_partial = dalloc<double>((size_t)1024 * 1024);
+  c->d_partial = dalloc<double>((size_t)tgpu::kPartialWords);
+  ck(cudaMemsetAsync(c->d_partial + tgpu::kPartialWords - 1, 0, sizeof(double), c->stream), "memset");
   c->d_red = dalloc<double>(4096);
   ck(cudaMallocHost(&c->h_red, 4096 * sizeof(double)), "cudaMallocHost");
   tgpu::upload_geom(dg, c->stream);

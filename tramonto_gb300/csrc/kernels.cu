@@ -1798,9 +1798,33 @@ __device__ __forceinline__ double block_min(double v, double *sh)
   return v;
 }
 
-// partial[j*nb + b] = sum over block b's chunk of V[j] . w
+// The last block of a reduction to finish adds up every block's partials, in block order as k_reduce_rows does
+// (the same result, without its launch): the blocks count themselves in an unsigned counter, which that last
+// block resets.  Partials written by other blocks are read through L2.
+__device__ __forceinline__ bool last_block_done(unsigned *counter)
+{
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return last;
+}
+
+__device__ void reduce_rows_last(const double *partial, int nb, int nrow, double *out, double *sh, unsigned *counter)
+{
+  for (int j = 0; j < nrow; j++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += __ldcg(partial + (long)j * nb + b);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[j] = s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// partial[j*nb + b] = sum over block b's chunk of V[j] . w; out[j] = sum over b (the last block)
 __global__ void k_multidot(const double *__restrict__ V, long ldv, int nvec, const double *__restrict__ w, long n,
-                           double *__restrict__ partial)
+                           double *__restrict__ partial, double *__restrict__ out, unsigned *__restrict__ counter)
 {
   __shared__ double sh[32];
   const long chunk = (n + gridDim.x - 1) / gridDim.x;
@@ -1811,6 +1835,7 @@ __global__ void k_multidot(const double *__restrict__ V, long ldv, int nvec, con
     s = block_sum(s, sh);
     if (threadIdx.x == 0) partial[(long)j * gridDim.x + blockIdx.x] = s;
   }
+  if (last_block_done(counter)) reduce_rows_last(partial, gridDim.x, nvec, out, sh, counter);
 }
 
 __global__ void k_reduce_rows(const double *__restrict__ partial, int nb, int nrow, double *__restrict__ out)
@@ -1824,11 +1849,12 @@ __global__ void k_reduce_rows(const double *__restrict__ partial, int nb, int nr
   }
 }
 
+// partial: the base of a kPartialWords reduction buffer (its last word is the completion counter)
 void launch_multidot(const double *V, long ldv, int nvec, const double *w, long n, double *partial, int nblocks,
                      double *result, cudaStream_t s)
 {
-  k_multidot<<<nblocks, kThreads, 0, s>>>(V, ldv, nvec, w, n, partial);
-  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, nvec, result);
+  unsigned *counter = reinterpret_cast<unsigned *>(partial + kPartialWords - 1);
+  k_multidot<<<nblocks, kThreads, 0, s>>>(V, ldv, nvec, w, n, partial, result, counter);
 }
 
 __global__ void k_multiaxpy(double *__restrict__ w, const double *__restrict__ V, long ldv, int nvec,
@@ -1963,7 +1989,8 @@ void launch_newton_update(double *x, const double *dx, double frac, double rel, 
   k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
 }
 
-__global__ void k_norm2(const double *__restrict__ x, long n, double *__restrict__ partial)
+__global__ void k_norm2(const double *__restrict__ x, long n, double *__restrict__ partial, double *__restrict__ out,
+                        unsigned *__restrict__ counter)
 {
   __shared__ double sh[32];
   double s = 0.0;
@@ -1971,12 +1998,14 @@ __global__ void k_norm2(const double *__restrict__ x, long n, double *__restrict
     s = fma(x[i], x[i], s);
   s = block_sum(s, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (last_block_done(counter)) reduce_rows_last(partial, gridDim.x, 1, out, sh, counter);
 }
 
+// partial: the base of a kPartialWords reduction buffer (its last word is the completion counter)
 void launch_norm2(const double *x, long n, double *partial, int nblocks, double *result, cudaStream_t s)
 {
-  k_norm2<<<nblocks, kThreads, 0, s>>>(x, n, partial);
-  k_reduce_rows<<<1, kThreads, 0, s>>>(partial, nblocks, 1, result);
+  unsigned *counter = reinterpret_cast<unsigned *>(partial + kPartialWords - 1);
+  k_norm2<<<nblocks, kThreads, 0, s>>>(x, n, partial, result, counter);
 }
 
 // out = a - ref; result[0] = max |a - ref|, result[1] = max |a|

@@ -33,6 +33,9 @@ __host__ __device__ __forceinline__ double to_f64(float x) { return (double)x; }
 __host__ __device__ __forceinline__ double to_f64(double x) { return x; }
 
 constexpr int kMaxC = TGPU_MAXC;
+// words of a handle's reduction buffer; the last one counts the blocks of a norm or multi-dot product that have
+// finished (zero between launches)
+constexpr long kPartialWords = 1024L * 1024L;
 constexpr int kMaxRb = 10;            // 4 + 2*3 weighted densities
 constexpr int kSentBulk = -1, kSentWall = -2, kSentBulkHi = -3, kSentBad = -9;   // kSentBulk: the low side's bulk
 constexpr int kReflBit = 1 << 30;     // flag bit in a per-dimension map entry
