@@ -39,3 +39,53 @@ def test_converged_reference_state_satisfies_the_averaged_rows():
     R = orc.Oracle(p).resid(z["x_newton"])
     rows = np.asarray(p.zone_flag) < 0
     assert np.abs(R[:, rows]).max() <= 1e-10
+
+
+def test_one_dimensional_boundary_fixture_structure():
+    """fmt1_wca_3d_1dbc (L1D_bc = 1, X_1D_bc = 1 sigma, Grad_dim x): the nodes within 1 sigma of either x end are
+    flagged -999 except the line y = z = 0, every other node keeps zone 0; the oracle's rows there are
+    x(node) - x(line node) for every unknown (load_coarse_node_1dim)."""
+    import orc
+    z, p = load("fmt1_wca_3d_1dbc")
+    assert p.l1d_bc == 1 and p.dim_1dbc == 0 and coarsened(p)
+    flag = np.asarray(p.zone_flag)
+    nx, ny, nz = p.nx
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    ix, iy, iz = (a.transpose(2, 1, 0).reshape(-1) for a in (ix, iy, iz))   # node = x + nx (y + ny z)
+    xpos = ix * p.esize[0]
+    near = (xpos <= 1.0 + 1e-8) | (xpos >= (nx - 1) * p.esize[0] - (1.0 + 1e-8))
+    line = (iy == 0) & (iz == 0)
+    assert np.array_equal(flag == -999, near & ~line)
+    assert np.all(flag[~(near & ~line)] == 0)
+    x = np.asarray(z[f"x{len(z['states']) - 1}"])
+    R = orc.Oracle(p).resid(x)
+    nodes = np.nonzero(flag == -999)[0]
+    want = x[:, nodes] - x[:, ix[nodes]]          # the line node of (x, y, z) is x itself
+    assert np.array_equal(R[:, nodes], want)
+
+
+@pytest.mark.parametrize("kind", ["bulk", "pb"])
+def test_bulk_and_pb_zone_rows_in_the_oracle(kind):
+    """The oracle's Euler-Lagrange rows at BULK_ZONE (-888) / PB_ZONE (-777) nodes: ln rho - ln rho_b
+    (fill_bulk_density) / ln rho - ln rho_b + V_ext (the PB branches, no nonlocal terms); rows of other nodes and
+    the other unknowns' rows as with zone 0 there."""
+    import copy
+    import orc
+    z, p = load("lj1d_zones")
+    q = copy.copy(p)
+    f = np.asarray(p.zone_flag)
+    q.zone_flag = np.where(f != 0, -888 if kind == "bulk" else -777, 0).astype(np.int32)
+    q.mesh_coarsening = 2 if kind == "bulk" else 3
+    x = np.asarray(z["x1"])
+    R = orc.Oracle(q).resid(x)
+    rho = x[q.first_rho]
+    flagged = (q.zone_flag < 0) & (np.asarray(q.zero_density)[0] == 0) & (np.asarray(q.vext)[0] < q.vext_max)
+    want = np.log(rho[flagged]) - np.log(q.rho_b[0])
+    if kind == "pb":
+        want = want + np.asarray(q.vext)[0][flagged]
+    assert np.allclose(R[q.first_rho][flagged], want, rtol=0, atol=1e-13)
+    # unflagged nodes: the same rows as the problem without the flags (zone 0 there)
+    zq = copy.copy(p)
+    zq.zone_flag = np.zeros_like(f)
+    R0 = orc.Oracle(zq).resid(x)
+    assert np.array_equal(R[:, q.zone_flag == 0], R0[:, q.zone_flag == 0])
