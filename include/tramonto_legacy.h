@@ -21,15 +21,31 @@
 #ifndef TRAMONTO_LEGACY_H
 #define TRAMONTO_LEGACY_H
 
+/* The communicator argument of the create calls: the caller's MPI_Comm wherever mpi.h is on the include path (the
+ * reference's own declaration, so that its headers and this one agree in one translation unit), otherwise an
+ * opaque word.  It is not read (one process, one GPU), and either type is passed in the third integer argument
+ * register of the x86-64 and AArch64 C calling conventions; this library is built with TGPU_LEGACY_NO_MPI. */
+#if !defined(TGPU_LEGACY_NO_MPI) && defined(__has_include)
+#if __has_include(<mpi.h>)
+#include <mpi.h>
+#define TGPU_LEGACY_MPI_COMM 1
+#endif
+#endif
+#ifdef TGPU_LEGACY_MPI_COMM
+typedef MPI_Comm tgpu_legacy_comm;
+#else
+typedef void *tgpu_legacy_comm;
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
 
 /* dft_basic_lin_prob_mgr_create (src/dft_basic_lin_prob_mgr_wrapper.h:44) */
-void *dft_basic_lin_prob_mgr_create(int numUnks, void *parameter_list, void *comm);
-/* dft_hardsphere_lin_prob_mgr_create / _create_debug (src/dft_hardsphere_lin_prob_mgr_wrapper.h:45,50) */
-void *dft_hardsphere_lin_prob_mgr_create(int numUnks, void *parameter_list, void *comm);
-void *dft_hardsphere_lin_prob_mgr_create_debug(int numUnks, void *parameter_list, void *comm);
+void *dft_basic_lin_prob_mgr_create(int numUnks, void *parameter_list, tgpu_legacy_comm comm);
+/* dft_hardsphere_lin_prob_mgr_create / _create_debug (src/dft_hardsphere_lin_prob_mgr_wrapper.h:43,48) */
+void *dft_hardsphere_lin_prob_mgr_create(int numUnks, void *parameter_list, tgpu_legacy_comm comm);
+void *dft_hardsphere_lin_prob_mgr_create_debug(int numUnks, void *parameter_list, tgpu_legacy_comm comm);
 /* dft_hardsphere_lin_prob_mgr_destruct (:52), dft_linprobmgr_destruct (basic :46) */
 void dft_hardsphere_lin_prob_mgr_destruct(void *mgr);
 void dft_linprobmgr_destruct(void *mgr);

@@ -21,6 +21,7 @@
 #include <unordered_map>
 #include <vector>
 
+#define TGPU_LEGACY_NO_MPI 1   // the communicator is not read: an opaque word here
 #include "../../include/tramonto_legacy.h"
 
 namespace {
@@ -769,9 +770,9 @@ extern "C" {
 
 const char *tgpu_legacy_last_error(void) { return g_err.c_str(); }
 
-void *dft_basic_lin_prob_mgr_create(int numUnks, void *, void *) { return create(numUnks, false); }
-void *dft_hardsphere_lin_prob_mgr_create(int numUnks, void *, void *) { return create(numUnks, true); }
-void *dft_hardsphere_lin_prob_mgr_create_debug(int numUnks, void *, void *) { return create(numUnks, true); }
+void *dft_basic_lin_prob_mgr_create(int numUnks, void *, tgpu_legacy_comm) { return create(numUnks, false); }
+void *dft_hardsphere_lin_prob_mgr_create(int numUnks, void *, tgpu_legacy_comm) { return create(numUnks, true); }
+void *dft_hardsphere_lin_prob_mgr_create_debug(int numUnks, void *, tgpu_legacy_comm) { return create(numUnks, true); }
 void dft_hardsphere_lin_prob_mgr_destruct(void *mgr) { destroy(mgr); }
 void dft_linprobmgr_destruct(void *mgr) { destroy(mgr); }
 
