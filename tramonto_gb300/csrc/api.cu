@@ -1356,7 +1356,7 @@ int gmres(Ctx *c, const double *d_rhs, double *d_x2, double tol, int maxit, int 
       tgpu::launch_multidot(V, n, k + 1, c->d_gt, n, c->d_partial, nb, d_h2, c->stream);
       tgpu::launch_multiaxpy(c->d_gt, V, n, k + 1, d_h2, n, c->stream);
       tgpu::launch_norm2(c->d_gt, n, c->d_partial, nb, d_nrm, c->stream);
-      c->stats.kernel_launches += 9;
+      c->stats.kernel_launches += 6;
       red_to_host(c, 2 * (kdim + 1) + 1);
       const double hn = std::sqrt(c->h_red[2 * (kdim + 1)]);
       if (!std::isfinite(hn)) throw Error(TGPU_ERR_NONFINITE, "non-finite Krylov vector in the Schur solve");
@@ -1451,7 +1451,7 @@ int newton_device(Ctx *c, double *d_x, double rel_tol, double abs_tol, double up
     const double upd = std::sqrt(c->h_red[0]);
     if (!std::isfinite(upd)) throw Error(TGPU_ERR_NONFINITE, "non-finite Newton update");
     converged = upd <= 1.0;
-    c->stats.kernel_launches += 6;
+    c->stats.kernel_launches += 5;
   }
   *iters = it;
   if (final_resid) {
